@@ -1,0 +1,98 @@
+"""ctypes binding of the engine's C ABI (include/gpvmc_gb300.h).
+
+The shared library is built in-tree by ``python -m gpvmc_gb300.build``.  There
+is no fallback: if the library is missing or a CUDA device is absent, the
+calls fail with an explicit error.
+"""
+import ctypes
+import os
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_lib", "libgpvmc_gb300.so")
+
+GV_OK = 0
+STATUS_NAMES = {0: "ok", 1: "invalid", 2: "singular", 3: "nan", 4: "zero amplitude", 5: "drift",
+                6: "timeout", 7: "out of memory", 8: "cuda error", 9: "not ready"}
+
+GV_CH_GROUNDSTATE, GV_CH_TRANS = 0, 1
+GV_PREC_FP64, GV_PREC_MIXED = 0, 1
+GV_MEAS_PROJHEIS, GV_MEAS_STAGMAGN, GV_MEAS_STATSPIN = 1, 2, 4
+
+
+class GvError(RuntimeError):
+    def __init__(self, status, where):
+        self.status = status
+        super().__init__("%s failed: %s (%d)" % (where, STATUS_NAMES.get(status, "?"), status))
+
+
+class JobConfig(ctypes.Structure):
+    _fields_ = [("L", ctypes.c_int32), ("channel", ctypes.c_int32), ("q", ctypes.c_int32 * 2),
+                ("phi", ctypes.c_double), ("neel", ctypes.c_double), ("neel_exp", ctypes.c_double),
+                ("phase_shift", ctypes.c_double * 2), ("phi_range", ctypes.c_double * 2),
+                ("neel_range", ctypes.c_double * 2), ("n_walkers", ctypes.c_int32),
+                ("precision", ctypes.c_int32), ("seed", ctypes.c_uint64), ("walker_base", ctypes.c_uint32),
+                ("reinv_every", ctypes.c_int32), ("meas_mask", ctypes.c_int32), ("flags", ctypes.c_int32)]
+
+
+class Trace(ctypes.Structure):
+    _fields_ = [("v1", ctypes.c_int32), ("v2", ctypes.c_int32), ("kind", ctypes.c_int32),
+                ("accepted", ctypes.c_int32), ("khop", ctypes.c_int32), ("pad", ctypes.c_int32),
+                ("ratio", ctypes.c_double), ("u4", ctypes.c_double)]
+
+
+# name -> (argtypes); every function returns gv_status (int32) unless noted
+_P = ctypes.c_void_p
+_SIGS = {
+    "gv_job_create": [ctypes.POINTER(JobConfig), ctypes.POINTER(ctypes.c_void_p)],
+    "gv_job_destroy": [_P],
+    "gv_job_dims": [_P] + [ctypes.POINTER(ctypes.c_int32)] * 4,
+    "gv_job_footprint": [ctypes.POINTER(JobConfig), ctypes.POINTER(ctypes.c_uint64)],
+    "gv_job_init_walkers": [_P, ctypes.c_void_p],
+    "gv_job_set_meas_mask": [_P, ctypes.c_int32],
+    "gv_job_walk": [_P, ctypes.c_uint64, ctypes.c_uint64],
+    "gv_job_walk_traced": [_P, ctypes.c_uint64, ctypes.c_uint64, ctypes.c_int32, ctypes.c_void_p],
+    "gv_job_synchronize": [_P],
+    "gv_job_reinvert": [_P],
+    "gv_job_drift": [_P, ctypes.c_void_p],
+    "gv_job_virt_update": [_P, ctypes.c_int32, ctypes.c_int32, ctypes.c_void_p, ctypes.c_void_p],
+    "gv_job_read_config": [_P, ctypes.c_void_p],
+    "gv_job_read_particles": [_P, ctypes.c_int32, ctypes.c_int32, ctypes.c_void_p],
+    "gv_job_read_amplitude": [_P, ctypes.c_void_p, ctypes.c_void_p],
+    "gv_job_read_inverse": [_P, ctypes.c_int32, ctypes.c_int32, ctypes.c_void_p],
+    "gv_job_read_counts": [_P, ctypes.c_void_p],
+    "gv_job_read_state_index": [_P, ctypes.c_void_p],
+    "gv_job_read_projheis": [_P, ctypes.c_void_p, ctypes.c_void_p],
+    "gv_job_read_stagmagn": [_P, ctypes.c_void_p, ctypes.c_void_p],
+    "gv_job_read_statspin": [_P, ctypes.c_void_p, ctypes.c_void_p],
+    "gv_job_last_walk_ms": [_P, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_int64)],
+}
+# exported names that take no status-returning signature above
+EXTRA_SYMBOLS = ["gv_version", "gv_status_string"]
+
+_lib = None
+
+
+def lib():
+    """Load libgpvmc_gb300.so (once).  Raises if it was not built."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        raise RuntimeError("gpvmc_gb300 native library missing (%s); build it with "
+                           "`python -m gpvmc_gb300.build`" % LIB_PATH)
+    L = ctypes.CDLL(LIB_PATH)
+    for name, args in _SIGS.items():
+        f = getattr(L, name)
+        f.argtypes = args
+        f.restype = ctypes.c_int32
+    L.gv_version.restype = ctypes.c_char_p
+    L.gv_version.argtypes = []
+    L.gv_status_string.restype = ctypes.c_char_p
+    L.gv_status_string.argtypes = [ctypes.c_int32]
+    _lib = L
+    return L
+
+
+def check(status, where):
+    if status != GV_OK:
+        raise GvError(status, where)

@@ -1,0 +1,168 @@
+// Device-side building blocks shared by the engine kernels: complex
+// arithmetic over float/double, Philox4x32-10, uniform mapping, block
+// reductions and the job descriptor passed to every kernel.
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "../../include/gpvmc_gb300.h"
+
+namespace gv {
+
+template <typename T>
+struct alignas(2 * sizeof(T)) cx {
+    T x, y;
+};
+
+template <typename T>
+__host__ __device__ __forceinline__ cx<T> mk(T a, T b) { return cx<T>{a, b}; }
+template <typename T>
+__host__ __device__ __forceinline__ cx<T> operator+(cx<T> a, cx<T> b) { return {a.x + b.x, a.y + b.y}; }
+template <typename T>
+__host__ __device__ __forceinline__ cx<T> operator-(cx<T> a, cx<T> b) { return {a.x - b.x, a.y - b.y}; }
+template <typename T>
+__host__ __device__ __forceinline__ cx<T> operator*(cx<T> a, cx<T> b)
+{
+    return {a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x};
+}
+template <typename T>
+__host__ __device__ __forceinline__ cx<T> operator*(cx<T> a, T s) { return {a.x * s, a.y * s}; }
+template <typename T>
+__host__ __device__ __forceinline__ T norm2(cx<T> a) { return a.x * a.x + a.y * a.y; }
+template <typename T>
+__host__ __device__ __forceinline__ cx<T> cinv(cx<T> a)
+{
+    T d = a.x * a.x + a.y * a.y;
+    return {a.x / d, -a.y / d};
+}
+// a += b * c (complex multiply-accumulate)
+template <typename T>
+__device__ __forceinline__ void cmac(cx<T>& a, cx<T> b, cx<T> c)
+{
+    a.x = fma(b.x, c.x, a.x);
+    a.x = fma(-b.y, c.y, a.x);
+    a.y = fma(b.x, c.y, a.y);
+    a.y = fma(b.y, c.x, a.y);
+}
+// Product rounded like the host's non-contracted (ac - bd, ad + bc).
+__device__ __forceinline__ cx<double> cmul_rn(cx<double> a, cx<double> b)
+{
+    return {__dsub_rn(__dmul_rn(a.x, b.x), __dmul_rn(a.y, b.y)),
+            __dadd_rn(__dmul_rn(a.x, b.y), __dmul_rn(a.y, b.x))};
+}
+__device__ __forceinline__ cx<float> cmul_rn(cx<float> a, cx<float> b)
+{
+    return {__fsub_rn(__fmul_rn(a.x, b.x), __fmul_rn(a.y, b.y)),
+            __fadd_rn(__fmul_rn(a.x, b.y), __fmul_rn(a.y, b.x))};
+}
+
+template <typename T>
+__device__ __forceinline__ cx<double> to_d(cx<T> a) { return {double(a.x), double(a.y)}; }
+
+// Philox4x32-10 (Salmon et al., SC'11).
+__host__ __device__ __forceinline__ void philox4x32_10(uint32_t c0, uint32_t c1, uint32_t c2, uint32_t c3,
+                                                       uint32_t k0, uint32_t k1, uint32_t out[4])
+{
+#pragma unroll
+    for (int r = 0; r < 10; ++r) {
+        if (r) { k0 += 0x9E3779B9u; k1 += 0xBB67AE85u; }
+#ifdef __CUDA_ARCH__
+        uint32_t hi0 = __umulhi(0xD2511F53u, c0), lo0 = 0xD2511F53u * c0;
+        uint32_t hi1 = __umulhi(0xCD9E8D57u, c2), lo1 = 0xCD9E8D57u * c2;
+#else
+        uint64_t p0 = uint64_t(0xD2511F53u) * c0, p1 = uint64_t(0xCD9E8D57u) * c2;
+        uint32_t hi0 = uint32_t(p0 >> 32), lo0 = uint32_t(p0), hi1 = uint32_t(p1 >> 32), lo1 = uint32_t(p1);
+#endif
+        uint32_t n0 = hi1 ^ c1 ^ k0, n2 = hi0 ^ c3 ^ k1;
+        c1 = lo1; c3 = lo0; c0 = n0; c2 = n2;
+    }
+    out[0] = c0; out[1] = c1; out[2] = c2; out[3] = c3;
+}
+
+// 52 random bits -> (m + 1/2) * 2^-52, exactly representable, in (0, 1).
+__host__ __device__ __forceinline__ double u01(uint32_t a, uint32_t b)
+{
+    uint64_t m = ((uint64_t(a) << 20) ^ uint64_t(b >> 12)) & ((uint64_t(1) << 52) - 1);
+    return (double(m) + 0.5) * (1.0 / 4503599627370496.0);
+}
+
+// Stream layout: counter {call_lo, call_hi, walker, stream}, key {seed_lo,
+// seed_hi}; uniform k comes from call k/2 (words 0,1 for even k, 2,3 for odd).
+__host__ __device__ __forceinline__ void philox_call(uint64_t seed, uint32_t walker, uint32_t stream,
+                                                     uint64_t call, uint32_t out[4])
+{
+    philox4x32_10(uint32_t(call), uint32_t(call >> 32), walker, stream, uint32_t(seed),
+                  uint32_t(seed >> 32), out);
+}
+
+__host__ __device__ __forceinline__ double uniform_at(uint64_t seed, uint32_t walker, uint32_t stream,
+                                                      uint64_t k)
+{
+    uint32_t x[4];
+    philox_call(seed, walker, stream, k >> 1, x);
+    return (k & 1) ? u01(x[2], x[3]) : u01(x[0], x[1]);
+}
+
+// Everything a kernel needs about a job (device pointers, sizes).
+struct DevJob {
+    int L, Ns, Nk, Nexc, W;
+    int N[2], Nmax;
+    int precision, channel;
+    uint64_t seed;
+    uint32_t walker_base;
+    int reinv_every;
+    const int32_t* nbr;        // Ns*4
+    const int32_t* edges;      // 2*Ns*2 (i, j) in creation order
+    const cx<double>* phase64; // Ns*Nk
+    const cx<float>* phase32;
+    const cx<double>* coef64;  // W*2fl*2sub*Ns
+    const cx<float>* coef32;
+    void* Ai[2];               // W * N[fl]^2, row-major [particle][row]
+    int16_t* fock;             // W*2*Ns: particle index at site or -1
+    int16_t* part;             // W*2*Nmax: site of particle
+    cx<double>* amp_m;         // W amplitude mantissa (|m| in [1,2) or 0)
+    int32_t* amp_e;            // W amplitude base-2 exponent
+    uint64_t* rng_next;        // W Metropolis uniform index
+    unsigned long long* counts;// W*5
+    int32_t* since_reinv;      // W
+    int32_t* status;           // W
+    cx<double>* pj;            // W*2
+    int32_t* pj_n;
+    cx<double>* sm;            // W
+    int32_t* sm_n;
+    double* ss;                // 5*Ns*Ns complex (interleaved) job-wide
+    int32_t* ss_n;
+    cx<double>* scratch64;     // per-CTA FP64 N*N scratch for re-inversion (W*Nmax*Nmax)
+    gv_trace* trace;
+    int trace_walker;
+};
+
+// Amplitude kept as (complex mantissa, base-2 exponent); renormalised
+// exactly by powers of two.
+__device__ __forceinline__ void amp_normalise(cx<double>& m, int& e)
+{
+    double a = fmax(fabs(m.x), fabs(m.y));
+    if (a == 0.0 || !isfinite(a)) return;
+    int k;
+    frexp(a, &k);
+    m.x = ldexp(m.x, -k);
+    m.y = ldexp(m.y, -k);
+    e += k;
+}
+
+template <int NT>
+__device__ __forceinline__ double block_sum_d(double v, double* red)
+{
+#pragma unroll
+    for (int o = 16; o; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    __syncthreads();
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = v;
+    __syncthreads();
+    double s = 0;
+#pragma unroll
+    for (int w = 0; w < NT / 32; ++w) s += red[w];
+    return s;
+}
+
+}  // namespace gv

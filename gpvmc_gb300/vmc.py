@@ -1,0 +1,352 @@
+"""Host-side mirror of the reference's sampling-path API over the C ABI.
+
+The reference builds one Markov chain per process from SquareLattice,
+LatticeState, a StagFlux* WaveFunction, SlaterDeterminant, LatticeStepper and
+MetroMC, then attaches Quantity objects (vmc.cpp:140-285).  Here a ``Job``
+holds ``walkers`` such chains on the GPU; the classes below keep the
+reference's names and call semantics on top of it:
+
+    wav = StagFluxGroundState(L=8, phi=0.25 * pi, neel=0.1)
+    job = Job(wav, walkers=1, seed=1234)
+    amp = SlaterDeterminant(job)             # amp.Init(), amp.Amp(), amp.VirtUpdate(...)
+    step = LatticeStepper(job)
+    mc = MetroMC(step)
+    heis = ProjHeis(step); mc.AddQuantity(heis)
+    mc.Walk(therm * L * L, 0); mc.Walk(meas * n, meas)
+    heis.save()                               # m_vals / m_meas per walker
+
+Errors are raised as ``GvError`` (the reference aborts, or throws under
+-DEXCEPT).
+"""
+import ctypes
+import math
+
+import numpy as np
+
+from . import _lib
+from ._lib import GvError, check
+
+CHANNELS = {"groundstate": _lib.GV_CH_GROUNDSTATE, "trans": _lib.GV_CH_TRANS}
+PRECISIONS = {"fp64": _lib.GV_PREC_FP64, "mixed": _lib.GV_PREC_MIXED}
+
+
+def _p(a):
+    return a.ctypes.data_as(ctypes.c_void_p)
+
+
+class SquareLattice:
+    """Periodic L x L lattice (SquareLattice.cpp:9-28) with the reference's
+    vertex numbering v = y*L + x and edge/neighbour order."""
+
+    def __init__(self, Lx, Ly=None):
+        if Ly is not None and Ly != Lx:
+            raise ValueError("only square lattices are on this path")
+        self.L = Lx
+        self.Nv = Lx * Lx
+        edges, nbr = [], [[] for _ in range(self.Nv)]
+        for x in range(Lx):
+            for y in range(Lx):
+                a = y * Lx + x
+                for b in (((y + 1) % Lx) * Lx + x, y * Lx + (x + 1) % Lx):
+                    edges.append((a, b))
+                    nbr[a].append(b)
+                    nbr[b].append(a)
+        self.edges = np.array(edges, dtype=np.int32)
+        self.neighbours = np.array(nbr, dtype=np.int32)
+
+    def GetNv(self):
+        return self.Nv
+
+    def GetLx(self):
+        return self.L
+
+    def GetLy(self):
+        return self.L
+
+
+class StagFluxWaveFunction:
+    """Parameters of a staggered-flux (+Neel) trial state (StagFluxWaveFunction.cpp:8-43).
+    ``phi`` is in radians, the value the reference's constructor receives."""
+
+    channel = "groundstate"
+
+    def __init__(self, L, phi, neel, neel_exp=0.0, phase_shift=(1.0, 1.0), q=(0, 0)):
+        self.L, self.phi, self.neel, self.neel_exp = L, phi, neel, neel_exp
+        self.phase_shift = tuple(phase_shift)
+        self.q = tuple(q)
+
+
+class StagFluxGroundState(StagFluxWaveFunction):
+    channel = "groundstate"
+
+
+class StagFluxTransExciton(StagFluxWaveFunction):
+    channel = "trans"
+
+
+class Job:
+    """A batch of independent chains of one wavefunction on the GPU (gv_job)."""
+
+    def __init__(self, wav, walkers=1, seed=1234, precision="fp64", reinv_every=0, walker_base=0,
+                 phi_range=None, neel_range=None):
+        L = _lib.lib()
+        cfg = _lib.JobConfig()
+        cfg.L = wav.L
+        cfg.channel = CHANNELS[wav.channel]
+        cfg.q[0], cfg.q[1] = wav.q
+        cfg.phi, cfg.neel, cfg.neel_exp = wav.phi, wav.neel, wav.neel_exp
+        cfg.phase_shift[0], cfg.phase_shift[1] = wav.phase_shift
+        if phi_range:
+            cfg.phi_range[0], cfg.phi_range[1] = phi_range
+        if neel_range:
+            cfg.neel_range[0], cfg.neel_range[1] = neel_range
+        cfg.n_walkers = walkers
+        cfg.precision = PRECISIONS[precision]
+        cfg.seed = seed
+        cfg.walker_base = walker_base
+        cfg.reinv_every = reinv_every
+        cfg.meas_mask = 0
+        self.cfg = cfg
+        self.wav = wav
+        self.walkers = walkers
+        self.precision = precision
+        h = ctypes.c_void_p()
+        check(L.gv_job_create(ctypes.byref(cfg), ctypes.byref(h)), "gv_job_create")
+        self._h = h
+        dims = [ctypes.c_int32() for _ in range(4)]
+        check(L.gv_job_dims(h, *[ctypes.byref(d) for d in dims]), "gv_job_dims")
+        self.Ns, Nup, Ndn, self.Nexc = (d.value for d in dims)
+        self.N = (Nup, Ndn)
+        self.lattice = SquareLattice(wav.L)
+
+    @staticmethod
+    def footprint(wav, walkers, precision="fp64"):
+        cfg = _lib.JobConfig()
+        cfg.L, cfg.channel = wav.L, CHANNELS[wav.channel]
+        cfg.n_walkers, cfg.precision = walkers, PRECISIONS[precision]
+        out = ctypes.c_uint64()
+        check(_lib.lib().gv_job_footprint(ctypes.byref(cfg), ctypes.byref(out)), "gv_job_footprint")
+        return out.value
+
+    def close(self):
+        if getattr(self, "_h", None):
+            _lib.lib().gv_job_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    # -- calls -----------------------------------------------------------
+    def set_measurements(self, mask):
+        check(_lib.lib().gv_job_set_meas_mask(self._h, mask), "gv_job_set_meas_mask")
+
+    def init_walkers(self, up=None):
+        if up is None:
+            check(_lib.lib().gv_job_init_walkers(self._h, None), "gv_job_init_walkers")
+        else:
+            up = np.ascontiguousarray(up, dtype=np.int8).reshape(self.walkers, self.Ns)
+            check(_lib.lib().gv_job_init_walkers(self._h, _p(up)), "gv_job_init_walkers")
+
+    def walk(self, length, meas=0, sync=True):
+        check(_lib.lib().gv_job_walk(self._h, length, meas), "gv_job_walk")
+        if sync:
+            self.synchronize()
+
+    def walk_traced(self, length, meas=0, walker=0):
+        buf = (_lib.Trace * max(length, 1))()
+        check(_lib.lib().gv_job_walk_traced(self._h, length, meas, walker, buf), "gv_job_walk_traced")
+        arr = np.frombuffer(bytes(buf), dtype=np.dtype([("v1", "<i4"), ("v2", "<i4"), ("kind", "<i4"),
+                                                         ("accepted", "<i4"), ("khop", "<i4"), ("pad", "<i4"),
+                                                         ("ratio", "<f8"), ("u4", "<f8")]))
+        return arr[:length].copy()
+
+    def synchronize(self):
+        check(_lib.lib().gv_job_synchronize(self._h), "gv_job_synchronize")
+
+    def reinvert(self):
+        check(_lib.lib().gv_job_reinvert(self._h), "gv_job_reinvert")
+
+    def drift(self):
+        out = np.zeros(2 * self.walkers)
+        check(_lib.lib().gv_job_drift(self._h, _p(out)), "gv_job_drift")
+        return out.reshape(self.walkers, 2)
+
+    def virt_update(self, walker, hops):
+        hops = np.ascontiguousarray(hops, dtype=np.int32).reshape(-1, 4)
+        out = np.zeros(2 * len(hops) * self.Nexc)
+        check(_lib.lib().gv_job_virt_update(self._h, walker, len(hops), _p(hops), _p(out)), "gv_job_virt_update")
+        return (out[0::2] + 1j * out[1::2]).reshape(self.Nexc, len(hops))
+
+    def last_walk_ms(self):
+        ms, n = ctypes.c_double(), ctypes.c_int64()
+        check(_lib.lib().gv_job_last_walk_ms(self._h, ctypes.byref(ms), ctypes.byref(n)), "gv_job_last_walk_ms")
+        return ms.value, n.value
+
+    # -- readers ---------------------------------------------------------
+    def config(self):
+        out = np.zeros(self.walkers * self.Ns, dtype=np.int8)
+        check(_lib.lib().gv_job_read_config(self._h, _p(out)), "gv_job_read_config")
+        return out.reshape(self.walkers, self.Ns)
+
+    def particles(self, walker, fl):
+        out = np.zeros(self.N[fl], dtype=np.int32)
+        check(_lib.lib().gv_job_read_particles(self._h, walker, fl, _p(out)), "gv_job_read_particles")
+        return out
+
+    def amplitude(self):
+        m = np.zeros(2 * self.walkers)
+        e = np.zeros(self.walkers, dtype=np.int32)
+        check(_lib.lib().gv_job_read_amplitude(self._h, _p(m), _p(e)), "gv_job_read_amplitude")
+        return m[0::2] + 1j * m[1::2], e
+
+    def inverse(self, walker, fl):
+        n = self.N[fl]
+        out = np.zeros(2 * n * n)
+        check(_lib.lib().gv_job_read_inverse(self._h, walker, fl, _p(out)), "gv_job_read_inverse")
+        return (out[0::2] + 1j * out[1::2]).reshape(n, n).T.copy()   # [p, f]
+
+    def counts(self):
+        out = np.zeros(5 * self.walkers, dtype=np.uint64)
+        check(_lib.lib().gv_job_read_counts(self._h, _p(out)), "gv_job_read_counts")
+        return out.reshape(self.walkers, 5)
+
+    def projheis(self):
+        vals = np.zeros(4 * self.walkers)
+        n = np.zeros(self.walkers, dtype=np.int32)
+        check(_lib.lib().gv_job_read_projheis(self._h, _p(vals), _p(n)), "gv_job_read_projheis")
+        return (vals[0::2] + 1j * vals[1::2]).reshape(self.walkers, 2), n
+
+    def stagmagn(self):
+        vals = np.zeros(2 * self.walkers)
+        n = np.zeros(self.walkers, dtype=np.int32)
+        check(_lib.lib().gv_job_read_stagmagn(self._h, _p(vals), _p(n)), "gv_job_read_stagmagn")
+        return vals[0::2] + 1j * vals[1::2], n
+
+    def statspin(self):
+        vals = np.zeros(10 * self.Ns * self.Ns)
+        n = np.zeros(1, dtype=np.int32)
+        check(_lib.lib().gv_job_read_statspin(self._h, _p(vals), _p(n)), "gv_job_read_statspin")
+        return (vals[0::2] + 1j * vals[1::2]).reshape(5, self.Ns, self.Ns), int(n[0])
+
+
+# ---------------------------------------------------------------------------
+# Reference-named classes
+
+class SlaterDeterminant:
+    """SlaterDeterminant (SlaterDeterminant.h:44-71) over all walkers of a job."""
+
+    def __init__(self, job):
+        self.job = job
+
+    def Init(self):
+        self.job.reinvert()
+
+    def Amp(self, walker=0):
+        m, e = self.job.amplitude()
+        return m[walker] * 10.0 ** float(e[walker])
+
+    def VirtUpdate(self, rhop, walker=0):
+        """rhop: list of (up_hop, dn_hop) with hop = (from_site, to_site) or None.
+        Returns qs / Amp() for every set (ground state: one channel state)."""
+        rows = []
+        for up, dn in rhop:
+            rows.append([*(up if up else (-1, -1)), *(dn if dn else (-1, -1))])
+        return self.job.virt_update(walker, np.array(rows, dtype=np.int32))
+
+
+class LatticeStepper:
+    """LatticeStepper (LatticeStepper.h:16-37): nearest-neighbour exchanges."""
+
+    def __init__(self, job):
+        self.job = job
+
+    def GetAmp(self):
+        return SlaterDeterminant(self.job)
+
+
+class Quantity:
+    mask = 0
+
+    def __init__(self, stepper):
+        self.job = stepper.job
+
+    def GetNmeas(self):
+        return self._read()[1]
+
+
+class ProjHeis(Quantity):
+    """ProjHeis (ProjHeis.cpp:40-158), Bx = 0: for the ground state m_vals is
+    [sum of E/site samples, count] per walker."""
+
+    mask = _lib.GV_MEAS_PROJHEIS
+
+    def _read(self):
+        return self.job.projheis()
+
+    def save(self):
+        v, n = self._read()
+        return v / np.maximum(n, 1)[:, None]
+
+
+class StagMagnZ(Quantity):
+    mask = _lib.GV_MEAS_STAGMAGN
+
+    def _read(self):
+        return self.job.stagmagn()
+
+    def save(self):
+        v, n = self._read()
+        return v / np.maximum(n, 1)
+
+
+class StatSpinStruct(Quantity):
+    """StatSpinStruct (StatSpinStruct.cpp:16-135): 5 x Ns x Ns sums over all walkers."""
+
+    mask = _lib.GV_MEAS_STATSPIN
+
+    def _read(self):
+        return self.job.statspin()
+
+    def GetNmeas(self):
+        return self._read()[1]
+
+    def save(self):
+        v, n = self._read()
+        return v / max(n, 1)
+
+
+class MetroMC:
+    """MetroMC (MetroMC.h:11-45): Walk(len, meas), Rejection()."""
+
+    def __init__(self, stepper):
+        self.job = stepper.job
+        self.quantities = []
+
+    def AddQuantity(self, q):
+        self.quantities.append(q)
+        mask = 0
+        for x in self.quantities:
+            mask |= x.mask
+        self.job.set_measurements(mask)
+
+    def GetQuantities(self):
+        return self.quantities
+
+    def Walk(self, length, meas):
+        self.job.walk(length, meas)
+
+    def Rejection(self):
+        c = self.job.counts().astype(np.float64)
+        return np.where(c[:, 0] > 0, c[:, 3] / np.maximum(c[:, 0], 1), 0.0)
+
+
+def pi_phi(phi_over_pi):
+    """The CLI's phi is in units of pi (vmc.cpp:120)."""
+    return phi_over_pi * math.pi
+
+
+__all__ = ["SquareLattice", "StagFluxGroundState", "StagFluxTransExciton", "Job", "SlaterDeterminant",
+           "LatticeStepper", "MetroMC", "ProjHeis", "StagMagnZ", "StatSpinStruct", "GvError", "pi_phi"]

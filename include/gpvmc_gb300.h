@@ -1,0 +1,172 @@
+/*
+ * gpvmc_gb300.h -- C ABI of the GB300 engine for the gpvmc Metropolis
+ * sampling path (Gutzwiller-projected staggered-flux Slater determinants,
+ * nearest-neighbour spin-exchange moves, ProjHeis / StagMagnZ /
+ * StatSpinStruct measurements).
+ *
+ * Plain pointers and sizes only.  Every function returns a gv_status (0 =
+ * GV_OK); nothing aborts.  A job owns its device memory and its CUDA stream;
+ * the caller owns the job handle.  Calls on one job are not thread-safe;
+ * distinct jobs may be driven from distinct host threads.
+ *
+ * The reference interfaces these entry points replace (reference files,
+ * EPFL-LQM/gpvmc):
+ *   gv_job_create          StagFlux{GroundState,TransExciton}::ctor + SquareLattice ctor +
+ *                          LatticeState ctor + SlaterDeterminant ctor
+ *                          (vmc.cpp:140-160; SlaterDeterminant.cpp:21-55)
+ *   gv_job_init_walkers    LatticeState::FockInit / RanInit + SlaterDeterminant::Init +
+ *                          excited-state arg-max + MetroMC ctor weight()
+ *                          (vmc.cpp:161-263; LatticeState.cpp:37-113;
+ *                          SlaterDeterminant.cpp:60-92; MetroMC.cpp:17-25)
+ *   gv_job_walk            MetroMC::Walk(len, meas) with the attached quantities
+ *                          (MetroMC.cpp:45-88 -> MetroMC::Step 90-103 ->
+ *                          LatticeStepper::trystep/step LatticeStepper.cpp:36-147 ->
+ *                          SlaterDeterminant::VirtUpdate/Update SlaterDeterminant.cpp:96-326)
+ *   gv_job_reinvert        SlaterDeterminant::Init (SlaterDeterminant.cpp:60-92)
+ *   gv_job_virt_update     SlaterDeterminant::VirtUpdate (SlaterDeterminant.cpp:96-268)
+ *   gv_job_read_*          LatticeState::Getfs, SlaterDeterminant::Amp,
+ *                          MetroMC::Rejection, Quantity m_vals / GetNmeas
+ *                          (State.cpp:55-63; SlaterDeterminant.cpp:94;
+ *                          MetroMC.cpp:105-111; Quantity.h:12-28)
+ */
+#ifndef GPVMC_GB300_H
+#define GPVMC_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef int32_t gv_status;
+#define GV_OK 0
+#define GV_ERR_INVALID 1      /* bad argument / unsupported configuration */
+#define GV_ERR_SINGULAR 2     /* no non-singular start, or singular update (linalg.cpp:23, 562-570) */
+#define GV_ERR_NAN 3          /* NaN/Inf met (BigComplex.h:24-31, StagFluxWaveFunction.cpp:65-77) */
+#define GV_ERR_ZERO_AMP 4     /* stepped to a zero overlap (LatticeStepper.cpp:121-124) */
+#define GV_ERR_DRIFT 5        /* inverse drift above threshold after re-inversion */
+#define GV_ERR_TIMEOUT 6      /* a bounded device wait gave up */
+#define GV_ERR_OOM 7          /* device allocation failed */
+#define GV_ERR_CUDA 8         /* other CUDA runtime error */
+#define GV_ERR_NOT_READY 9    /* walkers not initialised */
+
+#define GV_CH_GROUNDSTATE 0   /* StagFluxGroundState */
+#define GV_CH_TRANS 1         /* StagFluxTransExciton */
+
+#define GV_PREC_FP64 0        /* plain form: FP64 inverses, FP64 Sherman-Morrison */
+#define GV_PREC_MIXED 1       /* FP32 inverses/updates, FP64 periodic re-inversion */
+
+#define GV_MEAS_PROJHEIS 1    /* ProjHeis (ProjHeis.cpp:40-158), Bx = 0 */
+#define GV_MEAS_STAGMAGN 2    /* StagMagnZ (StagMagnZ.cpp:12-43) */
+#define GV_MEAS_STATSPIN 4    /* StatSpinStruct (StatSpinStruct.cpp:16-135) */
+
+typedef struct gv_job gv_job;
+
+/* One VMC job: one wavefunction channel on an L x L lattice and n_walkers
+ * independent Markov chains (the reference runs one chain per MPI rank,
+ * vmc.cpp:119-127). */
+typedef struct {
+    int32_t L;                /* lattice side (vmc.cpp:69) */
+    int32_t channel;          /* GV_CH_* (vmc.cpp:93, 147-154) */
+    int32_t q[2];             /* exciton momentum qx, qy (vmc.cpp:73-74) */
+    double phi;               /* staggered flux in radians: the CLI value times pi (vmc.cpp:120) */
+    double neel;              /* Neel field (vmc.cpp:81) */
+    double neel_exp;          /* Neel field exponent (vmc.cpp:82) */
+    double phase_shift[2];    /* boundary phases in units of pi (vmc.cpp:83-84) */
+    double phi_range[2];      /* if phi_range[1] > phi_range[0]: per-walker phi ~ U[lo, hi) (radians) */
+    double neel_range[2];     /* if neel_range[1] > neel_range[0]: per-walker neel ~ U[lo, hi) */
+    int32_t n_walkers;        /* independent chains in this job */
+    int32_t precision;        /* GV_PREC_* */
+    uint64_t seed;            /* Philox key (vmc.cpp:79, 119) */
+    uint32_t walker_base;     /* Philox walker id of walker 0 */
+    int32_t reinv_every;      /* re-invert after this many accepted exchanges, 0 = never */
+    int32_t meas_mask;        /* GV_MEAS_* quantities measured by gv_job_walk when meas > 0 */
+    int32_t flags;            /* reserved, 0 */
+} gv_job_config;
+
+/* Per-step record of one walker (parity traces). */
+typedef struct {
+    int32_t v1, v2;           /* proposal vertices (LatticeStepper.cpp:45-47) */
+    int32_t kind;             /* 0 = same flavour (no-op), 1 = spin exchange */
+    int32_t accepted;         /* MetroMC::YesNo outcome */
+    int32_t khop;             /* arg-max channel state after the proposal, -1 for no-op */
+    int32_t pad;
+    double ratio;             /* Metropolis ratio fed to YesNo */
+    double u4;                /* the uniform YesNo compared against */
+} gv_trace;
+
+/* Create / destroy. */
+gv_status gv_job_create(const gv_job_config* cfg, gv_job** out);
+gv_status gv_job_destroy(gv_job* job);
+gv_status gv_job_dims(const gv_job* job, int32_t* Ns, int32_t* Nup, int32_t* Ndn, int32_t* Nexc);
+/* Device bytes this job holds (admission by HBM footprint). */
+gv_status gv_job_footprint(const gv_job_config* cfg, uint64_t* bytes);
+
+/* Select the quantities measured by later gv_job_walk calls (MetroMC::AddQuantity,
+ * MetroMC.h:31). */
+gv_status gv_job_set_meas_mask(gv_job* job, int32_t meas_mask);
+
+/* Start configurations.  up: n_walkers x Ns bytes, 1 where flavour 0 sits
+ * (LatticeState::FockInit), or NULL for the reference's random start with up
+ * to 10 retries (vmc.cpp:221-241), drawn from Philox stream 1. */
+gv_status gv_job_init_walkers(gv_job* job, const int8_t* up);
+
+/* MetroMC::Walk(len, meas) on every walker: len Metropolis steps, the
+ * requested quantities measured after steps s with s % meas == 0 (meas = 0:
+ * no measurement).  Quantities are reset at the start of a measuring walk
+ * (MetroMC.cpp:49-51).  Enqueued on the job's stream; returns immediately. */
+gv_status gv_job_walk(gv_job* job, uint64_t len, uint64_t meas);
+/* As gv_job_walk, also recording walker `walker`'s per-step trace into the
+ * host array trace[len] (synchronous). */
+gv_status gv_job_walk_traced(gv_job* job, uint64_t len, uint64_t meas, int32_t walker, gv_trace* trace);
+/* Wait for the job's stream; returns the first walker error status if any. */
+gv_status gv_job_synchronize(gv_job* job);
+
+/* SlaterDeterminant::Init on every walker: FP64 LU re-inversion of both
+ * Slater matrices from the current configuration (also resets the drift). */
+gv_status gv_job_reinvert(gv_job* job);
+/* max |(A * A^-1 - I)_ij| per walker and flavour, FP64, out[walker*2 + fl]. */
+gv_status gv_job_drift(gv_job* job, double* out);
+
+/* SlaterDeterminant::VirtUpdate for `nset` real-space hop sets of walker
+ * `walker`: hops[4*i..4*i+3] = (up_from, up_to, dn_from, dn_to) site
+ * indices, -1 for no hop in that flavour.  For each set i and channel state k,
+ * out[2*(k*nset+i)..+1] = det ratio product over flavours including the
+ * channel-state hop sign, relative to the current amplitude (qs / Amp()). */
+gv_status gv_job_virt_update(gv_job* job, int32_t walker, int32_t nset, const int32_t* hops, double* out);
+
+/* Readers (synchronise the job's stream first). */
+gv_status gv_job_read_config(gv_job* job, int8_t* up /* n_walkers x Ns */);
+gv_status gv_job_read_particles(gv_job* job, int32_t walker, int32_t fl, int32_t* part /* N[fl] */);
+/* Amplitude Amp() of each walker as a base-10 mantissa/exponent pair:
+ * mant[2*w], mant[2*w+1] (re, im) with |mant| in [1,10), exp10[w]. */
+gv_status gv_job_read_amplitude(gv_job* job, double* mant, int32_t* exp10);
+/* Inverse Slater matrix of walker/flavour in the reference's column-major
+ * layout (m_mati[p + f*N]) as interleaved complex doubles. */
+gv_status gv_job_read_inverse(gv_job* job, int32_t walker, int32_t fl, double* out);
+/* counts[w*5 + i]: steps, accepted exchanges, accepted no-ops, rejections,
+ * re-inversions. */
+gv_status gv_job_read_counts(gv_job* job, uint64_t* counts);
+gv_status gv_job_read_state_index(gv_job* job, int32_t* state /* n_walkers */);
+/* Quantity sums since the last measuring walk began, per walker:
+ * ProjHeis m_vals (2*Nexc*Nexc complex per walker; for the ground state
+ * [E*L^2-normalised sum, count]), StagMagnZ (1 complex per walker), and the
+ * job-wide StatSpinStruct sums (5*Ns*Ns complex: szz, s+-, s-+, s++, s--),
+ * with the number of measurements each walker made. */
+gv_status gv_job_read_projheis(gv_job* job, double* vals, int32_t* nmeas);
+gv_status gv_job_read_stagmagn(gv_job* job, double* vals, int32_t* nmeas);
+gv_status gv_job_read_statspin(gv_job* job, double* vals, int32_t* nmeas);
+
+/* Device-time of the last gv_job_walk in milliseconds (CUDA events on the
+ * job's stream) and the number of kernels it launched. */
+gv_status gv_job_last_walk_ms(gv_job* job, double* ms, int64_t* launches);
+
+/* Library version string. */
+const char* gv_version(void);
+/* Message for a status code. */
+const char* gv_status_string(gv_status s);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

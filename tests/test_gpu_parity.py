@@ -1,0 +1,165 @@
+"""GPU engine vs the oracle on the same seeded inputs (through the C ABI).
+
+Bar: bit-exact configurations, proposals and accept decisions (except
+near-ties |u4 - ratio| < 1e-9, flagged), Metropolis ratios and amplitudes to
+1e-10 relative, quantity sums to 1e-10 relative, in the plain FP64 form.
+"""
+import math
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+PHI = 0.25 * math.pi
+RTOL = 1e-10
+
+
+def _pair(engine, oracle, L, neel, seed=1234, walkers=1, reinv=0, precision="fp64", walker=0):
+    job = engine.Job(engine.StagFluxGroundState(L, PHI, neel), walkers=walkers, seed=seed,
+                     precision=precision, reinv_every=reinv)
+    orc = oracle.OracleChain(L, PHI, neel, seed=seed, walker=walker)
+    return job, orc
+
+
+def _compare_traces(tg, to):
+    assert (tg["v1"] == to["v1"]).all()
+    assert (tg["v2"] == to["v2"]).all()
+    assert (tg["kind"] == to["kind"]).all()
+    tie = np.abs(to["u"][:, 3] - to["ratio"]) < 1e-9
+    assert ((tg["accepted"] == to["accepted"]) | tie).all()
+    real = to["kind"] == 1
+    # ratios that vanish by symmetry are rounding noise in both codes: the
+    # absolute floor 1e-13 is far below any ratio a uniform can accept
+    err = np.abs(tg["ratio"][real] - to["ratio"][real])
+    bad = err > RTOL * np.abs(to["ratio"][real]) + 1e-13
+    assert not bad.any(), (to["ratio"][real][bad][:5], tg["ratio"][real][bad][:5])
+    assert (tg["u4"] == to["u"][:, 3]).all()
+    return int(tie.sum())
+
+
+@pytest.mark.parametrize("L,neel", [(4, 0.1), (8, 0.1), (12, 0.05)])
+def test_start_and_inverse(engine, oracle, L, neel):
+    job, orc = _pair(engine, oracle, L, neel)
+    job.init_walkers()
+    assert orc.random_start() == 0
+    assert (job.config()[0] == orc.config()).all()
+    m, e = job.amplitude()
+    om, oe = orc.amp()
+    a, b = m[0] * 10.0 ** (e[0] - oe), om
+    assert abs(a - b) < RTOL * abs(b)
+    for fl in (0, 1):
+        gi, oi = job.inverse(0, fl), orc.inverse(fl)
+        assert np.abs(gi - oi).max() < RTOL * np.abs(oi).max()
+
+
+@pytest.mark.parametrize("L,neel,steps", [(4, 0.1, 3000), (8, 0.1, 6000), (12, 0.05, 4000)])
+def test_trace_parity(engine, oracle, L, neel, steps):
+    job, orc = _pair(engine, oracle, L, neel, seed=77)
+    job.init_walkers()
+    orc.random_start()
+    tg = job.walk_traced(steps, 0)
+    to = orc.walk(steps, trace=True)
+    _compare_traces(tg, to)
+    assert (job.config()[0] == orc.config()).all()
+    m, e = job.amplitude()
+    om, oe = orc.amp()
+    assert abs(m[0] * 10.0 ** (e[0] - oe) - om) < 1e-9 * abs(om)
+    for fl in (0, 1):
+        gi, oi = job.inverse(0, fl), orc.inverse(fl)
+        assert np.abs(gi - oi).max() < 1e-9 * np.abs(oi).max()
+    c = job.counts()[0]
+    assert c[0] == steps and c[1] == int((to["accepted"] & (to["kind"] == 1)).sum())
+
+
+def test_measurements_parity(engine, oracle):
+    L, neel = 8, 0.1
+    job, orc = _pair(engine, oracle, L, neel, seed=5)
+    job.set_measurements(7)
+    job.init_walkers()
+    orc.random_start()
+    job.walk(200 * L * L, 0)
+    orc.walk(200 * L * L)
+    tg = job.walk_traced(L * L * 30, L * L)
+    to = orc.walk(L * L * 30, meas=L * L, mask=7, trace=True)
+    _compare_traces(tg, to)
+    pj, n = job.projheis()
+    opj, on = orc.projheis()
+    assert n[0] == on == 30
+    assert abs(pj[0, 0] - opj[0, 0]) < RTOL * abs(opj[0, 0])
+    assert pj[0, 1].real == opj[1, 0].real
+    sm, sn = job.stagmagn()
+    osm, osn = orc.stagmagn()
+    assert sn[0] == osn and abs(sm[0] - osm) < 1e-12 * max(1.0, abs(osm))
+    ss, ssn = job.statspin()
+    oss, ossn = orc.statspin()
+    assert ssn == ossn == 30
+    assert np.abs(ss - oss).max() < RTOL * np.abs(oss).max()
+
+
+def test_reinversion_cadence(engine, oracle):
+    """Config-1 form: FP64 re-inversion after every L^2 accepted exchanges."""
+    L, neel = 8, 0.1
+    job, orc = _pair(engine, oracle, L, neel, seed=11, reinv=L * L)
+    job.init_walkers()
+    orc.random_start()
+    tg = job.walk_traced(8000, 0)
+    to = orc.walk(8000, reinv_every=L * L, trace=True)
+    _compare_traces(tg, to)
+    assert job.counts()[0][4] == orc.counts()[3] > 0
+
+
+def test_batched_walkers_match_single_chains(engine, oracle):
+    L, neel, W, steps = 8, 0.1, 16, 1500
+    job = engine.Job(engine.StagFluxGroundState(L, PHI, neel), walkers=W, seed=99)
+    job.init_walkers()
+    job.walk(steps, 0)
+    cfg = job.config()
+    for w in (0, 5, 15):
+        orc = oracle.OracleChain(L, PHI, neel, seed=99, walker=w)
+        orc.random_start()
+        orc.walk(steps)
+        assert (cfg[w] == orc.config()).all()
+
+
+def test_virt_update_bond_ratios(engine, oracle):
+    L, neel = 8, 0.1
+    job, orc = _pair(engine, oracle, L, neel, seed=3)
+    job.init_walkers()
+    orc.random_start()
+    up = job.config()[0].astype(bool)
+    lat = engine.SquareLattice(L)
+    hops = []
+    for a, b in lat.edges:
+        if up[a] != up[b]:
+            u, d = (a, b) if up[a] else (b, a)
+            hops.append((u, d, d, u))
+    hops.append((5 if up[5] else 6, 9, -1, -1) if False else (-1, -1, -1, -1))
+    hops = np.array(hops, dtype=np.int32)
+    g = job.virt_update(0, hops)[0]
+    qm, qe = orc.virt_update(hops)
+    am, ae = orc.amp()
+    ref = (qm[0] / am) * 10.0 ** (qe[0] - ae)
+    assert np.abs(g - ref).max() < RTOL * np.abs(ref).max()
+
+
+def test_mixed_precision_tracks_fp64(engine, oracle):
+    L, neel, steps = 8, 0.1, 3000
+    j64 = engine.Job(engine.StagFluxGroundState(L, PHI, neel), walkers=4, seed=21, precision="fp64")
+    j32 = engine.Job(engine.StagFluxGroundState(L, PHI, neel), walkers=4, seed=21, precision="mixed")
+    for j in (j64, j32):
+        j.init_walkers()
+    t64 = j64.walk_traced(steps, 0, walker=1)
+    t32 = j32.walk_traced(steps, 0, walker=1)
+    # until the chains part at a near-tie, the FP32 ratios follow the FP64 ones
+    diff = np.nonzero((t64["accepted"] != t32["accepted"]) | (t64["v1"] != t32["v1"]))[0]
+    upto = diff[0] if len(diff) else steps
+    real = t64["kind"][:upto] == 1
+    a, b = t32["ratio"][:upto][real], t64["ratio"][:upto][real]
+    # FP32 ratio error: 1e-4 relative, with an absolute floor for ratios that
+    # vanish by cancellation (never accepted)
+    assert upto > 200 and (np.abs(a - b) <= 1e-4 * b + 1e-6).all()
+    if upto < steps:   # the chains may only part where u4 sits within FP32 error of the ratio
+        assert abs(t64["u4"][upto] - t64["ratio"][upto]) < 1e-4 * max(1.0, t64["ratio"][upto])
+    d = j32.drift()
+    assert d.max() < 1e-3
