@@ -65,9 +65,14 @@ _SIGS = {
     "gv_job_read_stagmagn": [_P, ctypes.c_void_p, ctypes.c_void_p],
     "gv_job_read_statspin": [_P, ctypes.c_void_p, ctypes.c_void_p],
     "gv_job_last_walk_ms": [_P, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_int64)],
+    "gv_phi_table": [ctypes.c_int32, ctypes.c_double, ctypes.c_double, ctypes.c_double, ctypes.c_void_p,
+                     ctypes.c_int32, ctypes.c_void_p],
+    "gv_lattice_neighbours": [ctypes.c_int32, ctypes.c_void_p],
+    "gv_channel_orbitals": [ctypes.c_int32, ctypes.c_void_p, ctypes.c_int32, ctypes.c_void_p, ctypes.c_int32,
+                            ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p],
 }
 # exported names that take no status-returning signature above
-EXTRA_SYMBOLS = ["gv_version", "gv_status_string"]
+EXTRA_SYMBOLS = ["gv_version", "gv_status_string", "gv_philox4x32_10", "gv_uniform_at"]
 
 _lib = None
 
@@ -89,6 +94,10 @@ def lib():
     L.gv_version.argtypes = []
     L.gv_status_string.restype = ctypes.c_char_p
     L.gv_status_string.argtypes = [ctypes.c_int32]
+    L.gv_philox4x32_10.restype = None
+    L.gv_philox4x32_10.argtypes = [ctypes.POINTER(ctypes.c_uint32)] * 3
+    L.gv_uniform_at.restype = ctypes.c_double
+    L.gv_uniform_at.argtypes = [ctypes.c_uint64, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint64]
     _lib = L
     return L
 

@@ -807,6 +807,59 @@ extern "C" {
 
 const char* gv_version(void) { return "gpvmc_gb300 0.1 (sm_103a)"; }
 
+gv_status gv_phi_table(int32_t L, double phi, double neel, double neel_exp, const double* bc, int32_t fl, double* out)
+{
+    if (L < 2 || L > 64 || (L % 2) || !bc || fl < 0 || fl > 1 || !out) return GV_ERR_INVALID;
+    Orbitals o = make_orbitals(L, bc[0], bc[1]);
+    if (!o.ok) return GV_ERR_INVALID;
+    std::vector<zd> ph, coef(size_t(2) * o.Ns);
+    phase_table(o, ph);
+    if (!stagflux_coefs(o, phi, neel, neel_exp, fl, coef.data())) return GV_ERR_NAN;
+    for (int orb = 0; orb < o.Ns; ++orb)
+        for (int s = 0; s < o.Ns; ++s) {
+            const int sub = ((s % L) + (s / L)) & 1;
+            zd v = phi_elem(ph[size_t(s) * o.Nk + orb / 2], coef[size_t(sub) * o.Ns + orb]);
+            out[2 * (size_t(orb) * o.Ns + s)] = v.real();
+            out[2 * (size_t(orb) * o.Ns + s) + 1] = v.imag();
+        }
+    return GV_OK;
+}
+
+gv_status gv_lattice_neighbours(int32_t L, int32_t* nbr)
+{
+    if (L < 2 || L > 64 || !nbr) return GV_ERR_INVALID;
+    Lattice lat = make_square_lattice(L);
+    std::memcpy(nbr, lat.nbr.data(), sizeof(int32_t) * lat.nbr.size());
+    return GV_OK;
+}
+
+gv_status gv_channel_orbitals(int32_t L, const double* bc, int32_t channel, const int32_t* q, int32_t fl,
+                              int32_t* orb, int32_t* N, int32_t* Nexc)
+{
+    if (L < 2 || L > 64 || (L % 2) || !bc || !q || fl < 0 || fl > 1) return GV_ERR_INVALID;
+    if (channel != GV_CH_GROUNDSTATE && channel != GV_CH_TRANS) return GV_ERR_INVALID;
+    Orbitals o = make_orbitals(L, bc[0], bc[1]);
+    if (!o.ok) return GV_ERR_INVALID;
+    Channel ch = make_channel(o, channel, q[0], q[1]);
+    if (!ch.ok) return GV_ERR_INVALID;
+    if (N) *N = ch.N[fl];
+    if (Nexc) *Nexc = ch.Nexc;
+    if (orb)
+        for (int x = 0; x < o.Ns; ++x)
+            if (ch.fock0[fl][x] < ch.N[fl]) orb[ch.fock0[fl][x]] = x;
+    return GV_OK;
+}
+
+void gv_philox4x32_10(const uint32_t* c, const uint32_t* k, uint32_t* out)
+{
+    philox4x32_10(c[0], c[1], c[2], c[3], k[0], k[1], out);
+}
+
+double gv_uniform_at(uint64_t seed, uint32_t walker, uint32_t stream, uint64_t k)
+{
+    return uniform_at(seed, walker, stream, k);
+}
+
 const char* gv_status_string(gv_status s)
 {
     switch (s) {

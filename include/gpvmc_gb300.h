@@ -161,6 +161,26 @@ gv_status gv_job_read_statspin(gv_job* job, double* vals, int32_t* nmeas);
  * job's stream) and the number of kernels it launched. */
 gv_status gv_job_last_walk_ms(gv_job* job, double* ms, int64_t* launches);
 
+/* Host-side tables (no device needed).
+ * gv_phi_table: WaveFunction::MatEl cache m_cache[fl][o*Ns + s] of the
+ *   staggered-flux orbitals (StagFluxWaveFunction.cpp:51-79; WaveFunction.cpp:27-37),
+ *   interleaved complex doubles, Ns*Ns entries.
+ * gv_lattice_neighbours: nbr[v*4 + e], e-th neighbour of v in LatticeStepper's
+ *   draw order (SquareLattice.cpp:9-28; LatticeStepper.cpp:45-47).
+ * gv_channel_orbitals: occupied orbitals of flavour fl in the channel's first
+ *   state, by particle (row) index (StagFluxGroundState.cpp:3-15).
+ * gv_philox4x32_10 / gv_uniform_at: the Philox4x32-10 stream every walker
+ *   draws (counter {call_lo, call_hi, walker, stream}, key {seed_lo, seed_hi},
+ *   uniform k from call k/2) -- stream 0 Metropolis, 1 start configuration,
+ *   2 per-walker (phi, neel). */
+gv_status gv_phi_table(int32_t L, double phi, double neel, double neel_exp, const double* phase_shift,
+                       int32_t fl, double* out);
+gv_status gv_lattice_neighbours(int32_t L, int32_t* nbr);
+gv_status gv_channel_orbitals(int32_t L, const double* phase_shift, int32_t channel, const int32_t* q,
+                              int32_t fl, int32_t* orb, int32_t* N, int32_t* Nexc);
+void gv_philox4x32_10(const uint32_t* ctr, const uint32_t* key, uint32_t* out);
+double gv_uniform_at(uint64_t seed, uint32_t walker, uint32_t stream, uint64_t k);
+
 /* Library version string. */
 const char* gv_version(void);
 /* Message for a status code. */

@@ -1,0 +1,88 @@
+"""The C-ABI library loads and exports every symbol include/*.h declares;
+host-side entry points work without a GPU.  CPU only."""
+import ctypes
+import glob
+import math
+import os
+import re
+
+import numpy as np
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+@pytest.fixture(scope="module")
+def lib():
+    import gpvmc_gb300
+    from gpvmc_gb300 import build as b
+    if not os.path.exists(b.LIB):
+        b.build()
+    return gpvmc_gb300.lib()
+
+
+def declared_symbols():
+    names = set()
+    for h in glob.glob(os.path.join(ROOT, "include", "*.h")):
+        text = open(h).read()
+        text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+        names |= set(re.findall(r"\b(gv_[a-z0-9_]+)\s*\(", text))
+    return sorted(names)
+
+
+def test_every_declared_symbol_is_exported(lib):
+    names = declared_symbols()
+    assert len(names) >= 25
+    for n in names:
+        assert hasattr(lib, n), n
+
+
+def test_version_and_status(lib):
+    assert b"sm_103a" in lib.gv_version()
+    for s in range(10):
+        assert lib.gv_status_string(s)
+
+
+def test_invalid_arguments_are_rejected(lib):
+    from gpvmc_gb300 import _lib
+    cfg = _lib.JobConfig()
+    cfg.L, cfg.n_walkers, cfg.precision = 7, 1, 0
+    h = ctypes.c_void_p()
+    assert lib.gv_job_create(ctypes.byref(cfg), ctypes.byref(h)) == _lib.GV_OK + 1
+    assert lib.gv_job_create(None, ctypes.byref(h)) == 1
+    out = ctypes.c_uint64()
+    cfg.L = 16
+    cfg.n_walkers = 2048
+    assert lib.gv_job_footprint(ctypes.byref(cfg), ctypes.byref(out)) == 0
+    assert out.value > 2048 * 2 * 128 * 128 * 16
+
+
+@pytest.mark.parametrize("name,L", [("phi_L4.npz", 4), ("phi_L6.npz", 6), ("phi_L8.npz", 8)])
+def test_host_phi_table_matches_reference(lib, name, L):
+    g = np.load(os.path.join(ROOT, "tests", "golden", name))
+    bc = (ctypes.c_double * 2)(*g["bc"])
+    for fl in (0, 1):
+        out = np.zeros(2 * L ** 4)
+        st = lib.gv_phi_table(L, float(g["phi"]), float(g["neel"]), float(g["neel_exp"]), bc, fl,
+                              out.ctypes.data_as(ctypes.c_void_p))
+        assert st == 0
+        t = (out[0::2] + 1j * out[1::2]).reshape(L * L, L * L)[: g["phi%d" % fl].shape[0]]
+        np.testing.assert_array_equal(t, g["phi%d" % fl])
+    nbr = np.zeros(4 * L * L, dtype=np.int32)
+    assert lib.gv_lattice_neighbours(L, nbr.ctypes.data_as(ctypes.c_void_p)) == 0
+    np.testing.assert_array_equal(nbr.reshape(-1, 4), g["nbr"])
+    orb = np.zeros(L * L // 2, dtype=np.int32)
+    q = (ctypes.c_int32 * 2)(0, 0)
+    N, Nexc = ctypes.c_int32(), ctypes.c_int32()
+    assert lib.gv_channel_orbitals(L, bc, 0, q, 0, orb.ctypes.data_as(ctypes.c_void_p), ctypes.byref(N),
+                                   ctypes.byref(Nexc)) == 0
+    np.testing.assert_array_equal(orb, g["orb0"])
+
+
+def test_python_api_lattice():
+    import gpvmc_gb300 as g
+    lat = g.SquareLattice(8)
+    gold = np.load(os.path.join(ROOT, "tests", "golden", "phi_L8.npz"))
+    np.testing.assert_array_equal(lat.neighbours, gold["nbr"])
+    assert len(lat.edges) == 2 * 64
+    assert g.pi_phi(0.25) == 0.25 * math.pi

@@ -163,3 +163,23 @@ def test_mixed_precision_tracks_fp64(engine, oracle):
         assert abs(t64["u4"][upto] - t64["ratio"][upto]) < 1e-4 * max(1.0, t64["ratio"][upto])
     d = j32.drift()
     assert d.max() < 1e-3
+
+
+def test_singular_start_retry_gives_clean_state(engine, oracle):
+    """vmc.cpp:230-241 retries singular random starts; the reference's retry
+    keeps stale occupancies (State::InitFock never clears m_fock), the engine
+    restarts from a clean state and keeps drawing the same Philox stream."""
+    L = 4
+    seed = next(s for s in range(6, 200)
+                if int(_start_config(oracle, L, s).sum()) != L * L // 2)
+    job = engine.Job(engine.StagFluxGroundState(L, PHI, 0.1), walkers=1, seed=seed, walker_base=2)
+    job.init_walkers()
+    assert int(job.config()[0].sum()) == L * L // 2
+    job.walk(500, 0)
+    assert int(job.config()[0].sum()) == L * L // 2
+
+
+def _start_config(oracle, L, seed):
+    o = oracle.OracleChain(L, PHI, 0.1, seed=seed, walker=2)
+    o.random_start()
+    return o.config()
