@@ -1,0 +1,318 @@
+#!/usr/bin/env python
+"""Benchmark of the GB300 engine on the gpvmc sampling hot path.
+
+Workload (one GPU): L = 16 square lattice (256 sites, 128 x 128 complex
+Slater matrices per spin), staggered-flux ground state, 2048 independent
+walkers with per-walker phi ~ U[0.1, 0.4) pi and neel ~ U[0, 0.15) (Philox
+stream 2), ProjHeis measured once per sweep (every L^2 = 256 Metropolis
+steps), FP64 re-inversion after every 128 accepted exchanges.  Inputs are
+synthetic (seeded Philox start configurations); nothing is read from disk.
+
+One bench "step" = one sweep of every walker = 2048 * 256 Metropolis steps
+(MetroMC::Step).  value = Metropolis steps/s of the mixed-precision engine
+(FP32 inverses and Sherman-Morrison updates, FP64 re-inversion), with the
+plain FP64 engine measured on the same workload beside it.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+
+For N > 1 (torchrun) every rank runs an independent replica of the workload
+with its own walker ids (walkers are independent chains: no data-path
+collective); value = all ranks' steps / max rank time.
+"""
+import argparse
+import json
+import math
+import multiprocessing as mp
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "Metropolis steps/s, L=16×2048 walkers, mixed vs FP64 on GB300 @ΔE≤1e-5; p99 lat"
+L, WALKERS, SWEEP = 16, 2048, 256
+PHI_RANGE = (0.1 * math.pi, 0.4 * math.pi)
+NEEL_RANGE = (0.0, 0.15)
+REINV = 128
+SEED = 20261203
+
+
+def workload_config(precision):
+    return {"workload": "staggered-flux ground state L=16 (128x128 complex per spin), 2048 walkers, "
+                        "phi~U[0.1,0.4)pi, neel~U[0,0.15), ProjHeis every sweep, FP64 re-inversion every "
+                        "128 accepted exchanges",
+            "L": L, "walkers": WALKERS, "sweep_steps": SWEEP, "precision": precision,
+            "reinv_every_accepted": REINV, "step": "one sweep of every walker (2048*256 Metropolis steps)",
+            "l2": "inputs larger than L2: walker inverses %d MiB" % (WALKERS * 2 * 128 * 128 * (8 if precision == "mixed" else 16) >> 20)}
+
+
+# ---------------------------------------------------------------------------
+# CPU side: the oracle port (the reference's algorithm restated in C) timed on
+# the host cores.  Runs in spawned processes before any GPU work.
+
+def _cpu_chain(args):
+    walker, sweeps, measure = args
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    import oracle_lib as ol
+    from gpvmc_gb300 import _lib
+    u_phi = _lib.lib().gv_uniform_at(SEED, walker, 2, 0)
+    u_neel = _lib.lib().gv_uniform_at(SEED, walker, 2, 1)
+    phi = PHI_RANGE[0] + (PHI_RANGE[1] - PHI_RANGE[0]) * u_phi
+    neel = NEEL_RANGE[0] + (NEEL_RANGE[1] - NEEL_RANGE[0]) * u_neel
+    o = ol.OracleChain(L, phi, neel, seed=SEED, walker=walker)
+    if o.random_start():
+        return 0, 0.0
+    t0 = time.perf_counter()
+    o.walk(SWEEP * sweeps, meas=SWEEP if measure else 0, mask=ol.MEAS_PROJHEIS if measure else 0,
+           reinv_every=REINV)
+    return SWEEP * sweeps, time.perf_counter() - t0
+
+
+def cpu_baseline(cores, sweeps):
+    subprocess.run(["make", "-s", "-C", os.path.join(ROOT, "oracle"), "all"], check=True)
+    ctx = mp.get_context("spawn")
+    with ctx.Pool(cores) as pool:
+        t0 = time.perf_counter()
+        res = pool.map(_cpu_chain, [(w, sweeps, True) for w in range(cores)])
+        wall = time.perf_counter() - t0
+    rates = [r[0] / r[1] for r in res if r[1] > 0]
+    # chains run concurrently, one per core: aggregate = sum of per-chain rates
+    return {"value": sum(rates), "unit": "steps/s", "cores": cores, "kind": "port",
+            "per_core": statistics.mean(rates), "wall_s": wall,
+            "sample": "%d independent L=16 chains (one per core, walkers 0..%d of the workload), %d sweeps "
+                      "each with ProjHeis per sweep and re-inversion every 128 accepted moves" % (cores, cores - 1, sweeps)}
+
+
+# ---------------------------------------------------------------------------
+# GPU side
+
+class Clocks:
+    """nvidia-smi samples during the timed region."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.Q,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except OSError:
+            self.proc = None
+        return self
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.out, _ = self.proc.communicate(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+                self.out, _ = self.proc.communicate()
+
+    def summary(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in (self.out or "").strip().splitlines():
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx.append(float(f[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, f[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "samples": len(sm), "reasons": sorted(reasons)}
+
+
+def measured_peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            p = json.load(f)
+        return float(p["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def make_job(g, precision, rank):
+    wav = g.StagFluxGroundState(L, 0.25 * math.pi, 0.0)
+    job = g.Job(wav, walkers=WALKERS, seed=SEED, precision=precision, reinv_every=REINV,
+                walker_base=rank * WALKERS, phi_range=PHI_RANGE, neel_range=NEEL_RANGE)
+    job.set_measurements(1)
+    return job
+
+
+def run_gpu(g, precision, steps, warmup, rank, clocks_index=None):
+    job = make_job(g, precision, rank)
+    job.init_walkers()
+    for _ in range(warmup):
+        job.walk(SWEEP, SWEEP, sync=False)
+    job.synchronize()
+    c0 = job.counts().sum(axis=0)
+    lat = []
+    clk = Clocks(clocks_index) if clocks_index is not None else None
+    if clk:
+        clk.__enter__()
+    job.timer_start()
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        t = time.perf_counter()
+        job.walk(SWEEP, SWEEP, sync=False)
+        lat.append(t)
+    ms, launches = job.timer_stop()
+    wall = time.perf_counter() - t0
+    if clk:
+        clk.__exit__()
+    job.synchronize()
+    c1 = job.counts().sum(axis=0)
+    pj, n = job.projheis()
+    e_site = float((pj[:, 0].real / n).mean())
+    d = (c1 - c0).astype(float)
+    res = {"ms": ms, "wall_s": wall, "launches": launches, "steps": float(d[0]),
+           "p_acc": d[1] / d[0], "p_ap": (d[1] + d[3]) / d[0], "reinv": float(d[4]), "e_site": e_site,
+           "clocks": clk.summary() if clk else None}
+    job.close()
+    return res
+
+
+def run_e2e(g, precision, steps, rank):
+    """Through the public API with host buffers: job creation (host tables ->
+    device), host random start configurations -> device, FP64 LU start, then
+    each step one sweep and a device->host read of the per-walker results."""
+    import numpy as np
+    t0 = time.perf_counter()
+    job = make_job(g, precision, rank)
+    job.init_walkers()
+    results = []
+    for _ in range(steps):
+        job.walk(SWEEP, SWEEP, sync=False)
+        pj, n = job.projheis()
+        results.append(pj[:, 0].real / np.maximum(n, 1))
+    wall = time.perf_counter() - t0
+    job.close()
+    ns = L * L
+    h2d = (ns * (ns // 2) * (16 + 8) + WALKERS * 4 * ns * (16 + 8) + WALKERS * (2 * ns + 2 * ns // 2) * 2 + 4 * ns * 4
+           + 4 * ns * 4)
+    d2h = WALKERS * (2 * 16 + 4)
+    return {"value": WALKERS * SWEEP * steps / wall, "unit": "steps/s", "h2d_bytes_per_step": int(h2d / steps),
+            "d2h_bytes_per_step": d2h, "wall_s": wall,
+            "includes": "job creation + start upload + FP64 LU start amortised over the steps"}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
+    ap.add_argument("--cpu-sweeps", type=int, default=300)
+    ap.add_argument("--no-fp64-arm", action="store_true")
+    args = ap.parse_args()
+
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+
+    if args.impl == "reference":
+        # The reference's CPU path (its algorithm restated in oracle/vmc_oracle.c;
+        # the reference build itself needs its sources, absent on the GPU host).
+        if rank != 0:
+            return
+        cores = os.cpu_count() or 1
+        v = cpu_baseline(cores, args.cpu_sweeps)
+        out = {"metric": METRIC, "impl": "reference", "value": v["value"], "unit": "steps/s", "n_gpus": args.gpus,
+               "steps": args.steps, "warmup": args.warmup, "higher_is_better": True, "scaling": "weak",
+               "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+               "config": workload_config("fp64"),
+               "cpu_baseline": {"value": v["value"], "unit": "steps/s", "cores": v["cores"], "kind": v["kind"],
+                                "sample": v["sample"]},
+               "e2e": {"value": v["value"], "unit": "steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+        print(json.dumps(out))
+        return
+
+    cpu = None
+    if rank == 0 and world == 1:
+        cpu = cpu_baseline(os.cpu_count() or 1, args.cpu_sweeps)
+
+    dist = None
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+    import gpvmc_gb300 as g
+
+    if dist:
+        dist.barrier()
+    res = run_gpu(g, args.precision, args.steps, args.warmup, rank, clocks_index=local)
+    ms = res["ms"]
+    if dist:
+        import torch
+        t = torch.tensor([ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+        dist.barrier()
+    total_steps = res["steps"] * world
+    value = total_steps / (ms * 1e-3)
+
+    fp64 = None
+    if rank == 0 and not args.no_fp64_arm and args.precision == "mixed":
+        r64 = run_gpu(g, "fp64", max(2, args.steps // 4), 1, rank)
+        fp64 = {"value": r64["steps"] / (r64["ms"] * 1e-3), "ms_per_step": r64["ms"] / max(2, args.steps // 4),
+                "e_site_mean": r64["e_site"], "p_acc": r64["p_acc"]}
+
+    e2e = run_e2e(g, args.precision, args.steps, rank)
+    if dist:
+        import torch
+        t = torch.tensor([e2e["wall_s"]], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e["value"] = WALKERS * SWEEP * args.steps * world / float(t.item())
+
+    if rank != 0:
+        return
+    # Roofline of the walk kernel (HBM bound): algorithmic bytes per Metropolis
+    # step = p_ap * (2 spins * 2 * N * s) [inverse row + orbital column] +
+    #        p_acc * (2 spins * 3 * N^2 * s) [A^-1 u read, A^-1 read + write]
+    N, s = L * L // 2, (8 if args.precision == "mixed" else 16)
+    bytes_step = res["p_ap"] * (2 * 2 * N * s) + res["p_acc"] * (2 * 3 * N * N * s)
+    per_launch_steps = res["steps"] / max(1, res["launches"])
+    ms_launch = res["ms"] / max(1, res["launches"])
+    achieved = bytes_step * per_launch_steps / (ms_launch * 1e-3) / 1e9
+    peak, peak_kind = measured_peaks()
+    out = {"metric": METRIC, "value": value, "unit": "steps/s", "n_gpus": world, "steps": args.steps,
+           "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
+           "vs_baseline": None, "dtype": "f32" if args.precision == "mixed" else "f64", "data": "synthetic",
+           "config": workload_config(args.precision),
+           "e2e": {k: e2e[k] for k in ("value", "unit", "h2d_bytes_per_step", "d2h_bytes_per_step", "includes")},
+           "gpu_launches": int(res["launches"]),
+           "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                        "frac": achieved / peak, "traffic": None, "peak_kind": peak_kind,
+                        "kernel": "k_walk_gs", "bytes_per_step": bytes_step},
+           "acceptance": {"p_acc": res["p_acc"], "p_ap": res["p_ap"], "reinversions": res["reinv"]},
+           "e_site_mean": res["e_site"],
+           "clocks": res["clocks"]}
+    if fp64:
+        out["fp64_engine"] = fp64
+        out["mixed_over_fp64"] = value / world / fp64["value"]
+    if cpu:
+        out["cpu_baseline"] = {k: cpu[k] for k in ("value", "unit", "cores", "kind", "sample")}
+        out["cpu_baseline"]["per_core"] = cpu["per_core"]
+    print(json.dumps(out))
+
+
+if __name__ == "__main__":
+    main()

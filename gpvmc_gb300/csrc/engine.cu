@@ -681,6 +681,9 @@ struct gv_job {
     int nt = 128;
     double last_ms = 0.0;
     int64_t last_launches = 0;
+    int64_t total_launches = 0;
+    int64_t timer_launch0 = 0;
+    cudaEvent_t tev0 = nullptr, tev1 = nullptr;
     std::vector<double> wphi, wneel;
     std::vector<uint64_t> start_draws;   // Philox stream-1 uniform index per walker
 };
@@ -729,6 +732,7 @@ gv_status launch_walk(gv_job* j, uint64_t nsteps, uint64_t s0, uint64_t meas, in
     k_walk_gs<T, NT><<<j->W, NT, sm, j->stream>>>(j->d, nsteps, s0, meas, mask);
     GV_CK(cudaGetLastError());
     ++j->last_launches;
+    ++j->total_launches;
     return GV_OK;
 }
 
@@ -749,6 +753,7 @@ gv_status statspin_dispatch(gv_job* j)
     else k_statspin<float, 128><<<j->W, 128, sm, j->stream>>>(j->d);
     GV_CK(cudaGetLastError());
     ++j->last_launches;
+    ++j->total_launches;
     return GV_OK;
 }
 
@@ -759,6 +764,7 @@ gv_status launch_invert(gv_job* j)
     GV_CK(cudaFuncSetAttribute(k_invert<T, NT>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(sm)));
     k_invert<T, NT><<<j->W, NT, sm, j->stream>>>(j->d, 0, j->W);
     GV_CK(cudaGetLastError());
+    ++j->total_launches;
     return GV_OK;
 }
 
@@ -1011,6 +1017,8 @@ gv_status gv_job_destroy(gv_job* j)
     if (j->stream) cudaStreamSynchronize(j->stream);
     for (void* p : j->allocs) cudaFree(p);
     if (j->ev0) cudaEventDestroy(j->ev0);
+    if (j->tev0) cudaEventDestroy(j->tev0);
+    if (j->tev1) cudaEventDestroy(j->tev1);
     if (j->ev1) cudaEventDestroy(j->ev1);
     if (j->stream) cudaStreamDestroy(j->stream);
     delete j;
@@ -1145,6 +1153,30 @@ gv_status gv_job_synchronize(gv_job* j)
     GV_CK(cudaMemcpy(status.data(), j->d.status, sizeof(int32_t) * j->W, cudaMemcpyDeviceToHost));
     for (int32_t s : status)
         if (s) return s;
+    return GV_OK;
+}
+
+gv_status gv_job_timer_start(gv_job* j)
+{
+    if (!j) return GV_ERR_INVALID;
+    if (!j->tev0) {
+        GV_CK(cudaEventCreate(&j->tev0));
+        GV_CK(cudaEventCreate(&j->tev1));
+    }
+    j->timer_launch0 = j->total_launches;
+    GV_CK(cudaEventRecord(j->tev0, j->stream));
+    return GV_OK;
+}
+
+gv_status gv_job_timer_stop(gv_job* j, double* ms, int64_t* launches)
+{
+    if (!j || !j->tev0) return GV_ERR_INVALID;
+    GV_CK(cudaEventRecord(j->tev1, j->stream));
+    GV_CK(cudaEventSynchronize(j->tev1));
+    float f = 0;
+    GV_CK(cudaEventElapsedTime(&f, j->tev0, j->tev1));
+    if (ms) *ms = f;
+    if (launches) *launches = j->total_launches - j->timer_launch0;
     return GV_OK;
 }
 

@@ -180,6 +180,14 @@ class Job:
         check(_lib.lib().gv_job_virt_update(self._h, walker, len(hops), _p(hops), _p(out)), "gv_job_virt_update")
         return (out[0::2] + 1j * out[1::2]).reshape(self.Nexc, len(hops))
 
+    def timer_start(self):
+        check(_lib.lib().gv_job_timer_start(self._h), "gv_job_timer_start")
+
+    def timer_stop(self):
+        ms, n = ctypes.c_double(), ctypes.c_int64()
+        check(_lib.lib().gv_job_timer_stop(self._h, ctypes.byref(ms), ctypes.byref(n)), "gv_job_timer_stop")
+        return ms.value, n.value
+
     def last_walk_ms(self):
         ms, n = ctypes.c_double(), ctypes.c_int64()
         check(_lib.lib().gv_job_last_walk_ms(self._h, ctypes.byref(ms), ctypes.byref(n)), "gv_job_last_walk_ms")

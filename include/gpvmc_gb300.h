@@ -157,6 +157,12 @@ gv_status gv_job_read_projheis(gv_job* job, double* vals, int32_t* nmeas);
 gv_status gv_job_read_stagmagn(gv_job* job, double* vals, int32_t* nmeas);
 gv_status gv_job_read_statspin(gv_job* job, double* vals, int32_t* nmeas);
 
+/* CUDA-event timer on the job's stream: start records an event, stop
+ * records another, waits for it and returns the elapsed milliseconds; the
+ * launch count covers every kernel this job enqueued in between. */
+gv_status gv_job_timer_start(gv_job* job);
+gv_status gv_job_timer_stop(gv_job* job, double* ms, int64_t* launches);
+
 /* Device-time of the last gv_job_walk in milliseconds (CUDA events on the
  * job's stream) and the number of kernels it launched. */
 gv_status gv_job_last_walk_ms(gv_job* job, double* ms, int64_t* launches);

@@ -4,6 +4,7 @@ import ctypes
 import glob
 import math
 import os
+import platform
 import re
 
 import numpy as np
@@ -67,7 +68,10 @@ def test_host_phi_table_matches_reference(lib, name, L):
                               out.ctypes.data_as(ctypes.c_void_p))
         assert st == 0
         t = (out[0::2] + 1j * out[1::2]).reshape(L * L, L * L)[: g["phi%d" % fl].shape[0]]
-        np.testing.assert_array_equal(t, g["phi%d" % fl])
+        if platform.machine() in ("x86_64", "AMD64"):   # the fixtures' architecture: bit-exact
+            np.testing.assert_array_equal(t, g["phi%d" % fl])
+        else:                                            # other libm: last-bit differences
+            np.testing.assert_allclose(t, g["phi%d" % fl], rtol=0, atol=1e-14)
     nbr = np.zeros(4 * L * L, dtype=np.int32)
     assert lib.gv_lattice_neighbours(L, nbr.ctypes.data_as(ctypes.c_void_p)) == 0
     np.testing.assert_array_equal(nbr.reshape(-1, 4), g["nbr"])
