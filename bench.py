@@ -150,7 +150,8 @@ def measured_peaks():
 def make_job(g, precision, rank):
     wav = g.StagFluxGroundState(L, 0.25 * math.pi, 0.0)
     job = g.Job(wav, walkers=WALKERS, seed=SEED, precision=precision, reinv_every=REINV,
-                walker_base=rank * WALKERS, phi_range=PHI_RANGE, neel_range=NEEL_RANGE)
+                walker_base=rank * WALKERS, phi_range=PHI_RANGE, neel_range=NEEL_RANGE,
+                deferred_reinversion=True)
     job.set_measurements(1)
     return job
 

@@ -17,6 +17,7 @@ STATUS_NAMES = {0: "ok", 1: "invalid", 2: "singular", 3: "nan", 4: "zero amplitu
 GV_CH_GROUNDSTATE, GV_CH_TRANS = 0, 1
 GV_PREC_FP64, GV_PREC_MIXED = 0, 1
 GV_MEAS_PROJHEIS, GV_MEAS_STAGMAGN, GV_MEAS_STATSPIN = 1, 2, 4
+GV_FLAG_REINV_DEFERRED = 1
 
 
 class GvError(RuntimeError):

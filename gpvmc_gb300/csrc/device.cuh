@@ -113,7 +113,7 @@ struct DevJob {
     uint32_t walker_base;
     int reinv_every;
     const int32_t* nbr;        // Ns*4
-    const int32_t* edges;      // 2*Ns*2 (i, j) in creation order
+    const int4* edges;         // 2*Ns edges (i, j, slot of j in nbr[i], slot of i in nbr[j]), creation order
     const cx<double>* phase64; // Ns*Nk
     const cx<float>* phase32;
     const cx<double>* coef64;  // W*2fl*2sub*Ns

@@ -20,648 +20,10 @@
 #include <vector>
 
 #include "device.cuh"
+#include "kernels.cuh"
 #include "model.hpp"
 
 using namespace gv;
-
-namespace {
-
-// ------------------------------------------------------------------------
-// Small device helpers
-
-template <typename T> struct Tab;
-template <> struct Tab<double> {
-    static __device__ __forceinline__ const cx<double>* phase(const DevJob& J) { return J.phase64; }
-    static __device__ __forceinline__ const cx<double>* coef(const DevJob& J) { return J.coef64; }
-};
-template <> struct Tab<float> {
-    static __device__ __forceinline__ const cx<float>* phase(const DevJob& J) { return J.phase32; }
-    static __device__ __forceinline__ const cx<float>* coef(const DevJob& J) { return J.coef32; }
-};
-
-template <typename T>
-__device__ __forceinline__ cx<T>* ai_ptr(const DevJob& J, int fl, int w)
-{
-    return static_cast<cx<T>*>(J.Ai[fl]) + size_t(w) * J.N[fl] * J.N[fl];
-}
-
-__device__ __forceinline__ int sublattice(int s, int L) { return ((s % L) + (s / L)) & 1; }
-
-template <typename T>
-__device__ __forceinline__ cx<T> warp_sum(cx<T> v)
-{
-#pragma unroll
-    for (int o = 16; o; o >>= 1) {
-        v.x += __shfl_xor_sync(0xffffffffu, v.x, o);
-        v.y += __shfl_xor_sync(0xffffffffu, v.y, o);
-    }
-    return v;
-}
-
-// ------------------------------------------------------------------------
-// FP64 Gauss-Jordan inversion with partial (row) pivoting on max |re|+|im|,
-// in place on M (N x N row-major, global scratch).  Pivots equal those of
-// LAPACK zgetrf, so det = prod(pivots) * (-1)^swaps as in linalg::DetInv
-// (linalg.cpp:9-44).  Returns false if a pivot column is exactly zero.
-template <int NT>
-__device__ bool gj_invert(cx<double>* M, int N, cx<double>* rowk, cx<double>* fcol, int* perm,
-                          double* redv, int* redi, cx<double>& det_m, int& det_e)
-{
-    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    constexpr int NW = NT / 32;
-    cx<double> dm = {1.0, 0.0};
-    int de = 0;
-    for (int k = 0; k < N; ++k) {
-        double best = -1.0;
-        int bi = N;
-        for (int i = k + tid; i < N; i += NT) {
-            cx<double> v = M[size_t(i) * N + k];
-            double a = fabs(v.x) + fabs(v.y);
-            if (a > best) { best = a; bi = i; }
-        }
-#pragma unroll
-        for (int o = 16; o; o >>= 1) {
-            double ob = __shfl_xor_sync(0xffffffffu, best, o);
-            int oi = __shfl_xor_sync(0xffffffffu, bi, o);
-            if (ob > best || (ob == best && oi < bi)) { best = ob; bi = oi; }
-        }
-        if (lane == 0) { redv[warp] = best; redi[warp] = bi; }
-        __syncthreads();
-        best = redv[0];
-        bi = redi[0];
-        for (int q = 1; q < NW; ++q)
-            if (redv[q] > best || (redv[q] == best && redi[q] < bi)) { best = redv[q]; bi = redi[q]; }
-        if (!(best > 0.0)) return false;
-        const int p = bi;
-        if (p != k)
-            for (int j = tid; j < N; j += NT) {
-                cx<double> a = M[size_t(k) * N + j];
-                M[size_t(k) * N + j] = M[size_t(p) * N + j];
-                M[size_t(p) * N + j] = a;
-            }
-        __syncthreads();
-        const cx<double> piv = M[size_t(k) * N + k];
-        if (tid == 0) {
-            perm[k] = p;
-            dm = dm * piv;
-            if (p != k) { dm.x = -dm.x; dm.y = -dm.y; }
-            amp_normalise(dm, de);
-        }
-        const cx<double> inv = cinv(piv);
-        for (int j = tid; j < N; j += NT) {
-            cx<double> v = (j == k) ? cx<double>{1.0, 0.0} : M[size_t(k) * N + j];
-            v = v * inv;
-            rowk[j] = v;
-        }
-        for (int i = tid; i < N; i += NT) fcol[i] = (i == k) ? cx<double>{0.0, 0.0} : M[size_t(i) * N + k];
-        __syncthreads();
-        for (int j = tid; j < N; j += NT) M[size_t(k) * N + j] = rowk[j];
-        for (int i = warp; i < N; i += NW) {
-            if (i == k) continue;
-            const cx<double> f = fcol[i];
-            for (int j = lane; j < N; j += 32) {
-                cx<double> v = (j == k) ? cx<double>{0.0, 0.0} : M[size_t(i) * N + j];
-                cmac(v, cx<double>{-f.x, -f.y}, rowk[j]);
-                M[size_t(i) * N + j] = v;
-            }
-        }
-        __syncthreads();
-    }
-    for (int k = N - 1; k >= 0; --k) {
-        const int p = perm[k];
-        if (p != k)
-            for (int i = tid; i < N; i += NT) {
-                cx<double> a = M[size_t(i) * N + k];
-                M[size_t(i) * N + k] = M[size_t(i) * N + p];
-                M[size_t(i) * N + p] = a;
-            }
-        __syncthreads();
-    }
-    if (tid == 0) { det_m = dm; det_e = de; }
-    return true;
-}
-
-// Shared-memory scratch used by gj_invert.
-struct GJSmem {
-    cx<double>* rowk;
-    cx<double>* fcol;
-    int* perm;
-    double* redv;
-    int* redi;
-    cx<double>* detm;
-    int* dete;
-    int* flag;
-};
-
-// SlaterDeterminant::Init for walker w (SlaterDeterminant.cpp:60-92): build
-// A(f, r) = phi_{2f}(site of particle r) in FP64 (ground-state rows), invert,
-// store Ai in T, amplitude = det_0 * det_1.  Returns a gv_status.
-template <typename T, int NT>
-__device__ int reinvert_walker(const DevJob& J, int w, cx<double>* M, const GJSmem& S,
-                               const int16_t* part_s /* smem or null */)
-{
-    const int tid = threadIdx.x;
-    cx<double> am = {1.0, 0.0};
-    int ae = 0;
-    int status = GV_OK;
-    for (int fl = 0; fl < 2; ++fl) {
-        const int N = J.N[fl];
-        const int16_t* part = part_s ? part_s + fl * J.Nmax : J.part + (size_t(w) * 2 + fl) * J.Nmax;
-        const cx<double>* coef = J.coef64 + (size_t(w) * 2 + fl) * 2 * J.Ns;
-        for (int idx = tid; idx < N * N; idx += NT) {
-            const int f = idx / N, r = idx % N;
-            const int s = part[r];
-            const int sub = sublattice(s, J.L);
-            M[idx] = cmul_rn(J.phase64[size_t(s) * J.Nk + f], coef[size_t(sub) * J.Ns + 2 * f]);
-        }
-        __syncthreads();
-        cx<double> dm;
-        int de;
-        bool ok = gj_invert<NT>(M, N, S.rowk, S.fcol, S.perm, S.redv, S.redi, dm, de);
-        if (tid == 0) { S.detm[0] = dm; S.dete[0] = de; S.flag[0] = ok; }
-        __syncthreads();
-        ok = S.flag[0];
-        dm = S.detm[0];
-        de = S.dete[0];
-        __syncthreads();
-        // reference: singular if |det|^2 < 1e-9, amplitude zero if exponent10 < -8
-        double l10 = ok ? (log10(sqrt(norm2(dm))) + de * 0.30102999566398119521) : -1e300;
-        if (!ok || 2.0 * l10 < -9.0 || floor(l10) < -8.0) status = GV_ERR_SINGULAR;
-        cx<T>* out = ai_ptr<T>(J, fl, w);
-        for (int idx = tid; idx < N * N; idx += NT) {
-            cx<double> v = M[idx];
-            out[idx] = cx<T>{T(v.x), T(v.y)};
-        }
-        am = am * dm;
-        ae += de;
-        amp_normalise(am, ae);
-        __syncthreads();
-    }
-    if (tid == 0) {
-        if (status == GV_OK) { J.amp_m[w] = am; J.amp_e[w] = ae; }
-        else { J.amp_m[w] = cx<double>{0.0, 0.0}; J.amp_e[w] = 0; }
-    }
-    return status;
-}
-
-template <int NT>
-__device__ GJSmem carve_gj(char*& p, int Nmax)
-{
-    GJSmem S;
-    S.rowk = reinterpret_cast<cx<double>*>(p); p += sizeof(cx<double>) * Nmax;
-    S.fcol = reinterpret_cast<cx<double>*>(p); p += sizeof(cx<double>) * Nmax;
-    S.detm = reinterpret_cast<cx<double>*>(p); p += sizeof(cx<double>) * 2;
-    S.redv = reinterpret_cast<double*>(p); p += sizeof(double) * (NT / 32);
-    S.perm = reinterpret_cast<int*>(p); p += sizeof(int) * Nmax;
-    S.redi = reinterpret_cast<int*>(p); p += sizeof(int) * (NT / 32);
-    S.dete = reinterpret_cast<int*>(p); p += sizeof(int) * 2;
-    S.flag = reinterpret_cast<int*>(p); p += sizeof(int) * 2;
-    p = reinterpret_cast<char*>((reinterpret_cast<uintptr_t>(p) + 15) & ~uintptr_t(15));
-    return S;
-}
-
-__host__ __device__ inline size_t gj_smem_bytes(int Nmax, int NT)
-{
-    return sizeof(cx<double>) * (2 * Nmax + 2) + sizeof(double) * (NT / 32) + sizeof(int) * (Nmax + NT / 32 + 4) + 16;
-}
-
-template <typename T, int NT>
-__global__ void __launch_bounds__(NT) k_invert(DevJob J, int w0, int nw)
-{
-    extern __shared__ __align__(16) char smem[];
-    const int w = w0 + blockIdx.x;
-    if (blockIdx.x >= nw || w >= J.W) return;
-    char* p = smem;
-    GJSmem S = carve_gj<NT>(p, J.Nmax);
-    cx<double>* M = J.scratch64 + size_t(blockIdx.x) * J.Nmax * J.Nmax;
-    int st = reinvert_walker<T, NT>(J, w, M, S, nullptr);
-    if (threadIdx.x == 0) J.status[w] = st;
-}
-
-// ------------------------------------------------------------------------
-// Metropolis walk, ground-state channel.  One CTA per walker; the walker's
-// occupancy, coefficients and work vectors live in shared memory, its
-// inverses in HBM.  Each step follows MetroMC::Step (MetroMC.cpp:90-103):
-// 4 uniforms (vertex, neighbour, internal state, accept), a no-op for equal
-// flavours, otherwise the two determinant ratios
-//   r_fl = sum_f Ai_fl[c][f] phi_{2f}(d)       (linalg.cpp:297-303 / 146)
-// and, on acceptance, the Sherman-Morrison update of both inverses
-//   Ai <- Ai - (Ai u - e_c)(e_c^T Ai)/r        (linalg.cpp:402-573, rc=1 rr=0).
-template <typename T, int NT>
-struct WalkSmem {
-    int16_t* fock;   // 2*Ns
-    int16_t* part;   // 2*Nmax
-    int32_t* nbr;    // 4*Ns
-    cx<T>* coef;     // 2 fl * 2 sub * Nmax   (row f -> orbital 2f)
-    cx<T>* uu;       // 2*Nmax
-    cx<T>* row;      // 2*Nmax
-    cx<T>* wv;       // 2*Nmax
-    double* red;     // 2 buffers * (NT/32) * 4
-    double* redm;    // NT/32 * 4 (measurements)
-};
-
-template <typename T, int NT>
-__host__ __device__ inline size_t walk_smem_bytes(int Ns, int Nmax)
-{
-    size_t b = 0;
-    b += sizeof(int16_t) * (2 * Ns + 2 * Nmax);
-    b = (b + 15) & ~size_t(15);
-    b += sizeof(int32_t) * 4 * Ns;
-    b = (b + 15) & ~size_t(15);
-    b += sizeof(cx<T>) * (4 * Nmax + 6 * Nmax);
-    b += sizeof(double) * (2 * (NT / 32) * 4 + (NT / 32) * 4);
-    b = (b + 15) & ~size_t(15);
-    b += gj_smem_bytes(Nmax, NT) + 16;
-    return b;
-}
-
-template <typename T>
-__device__ __forceinline__ cx<T> phi_at(const cx<T>* phase, const cx<T>* coef_fl, int Nk, int Nmax, int L, int s, int f)
-{
-    // GS row f <-> orbital 2f: phase index f, coefficient of orbital 2f
-    const int sub = sublattice(s, L);
-    return cmul_rn(phase[size_t(s) * Nk + f], coef_fl[sub * Nmax + f]);
-}
-
-// Ratio of moving particle c of flavour fl to site d: one warp.
-template <typename T>
-__device__ __forceinline__ cx<T> warp_ratio(const DevJob& J, const cx<T>* Ai, const cx<T>* phase,
-                                            const cx<T>* coef_fl, int N, int c, int d)
-{
-    const int lane = threadIdx.x & 31;
-    cx<T> acc = {T(0), T(0)};
-    const cx<T>* row = Ai + size_t(c) * N;
-    for (int f = lane; f < N; f += 32) cmac(acc, row[f], phi_at<T>(phase, coef_fl, J.Nk, J.Nmax, J.L, d, f));
-    return warp_sum(acc);
-}
-
-template <typename T, int NT>
-__global__ void __launch_bounds__(NT) k_walk_gs(DevJob J, uint64_t nsteps, uint64_t s0, uint64_t meas, int mask)
-{
-    extern __shared__ __align__(16) char smem[];
-    constexpr int NW = NT / 32;
-    const int w = blockIdx.x;
-    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    if (w >= J.W) return;
-    if (J.status[w] != GV_OK) return;
-    const int Ns = J.Ns, Nmax = J.Nmax, L = J.L;
-    const int N0 = J.N[0], N1 = J.N[1];
-
-    char* p = smem;
-    WalkSmem<T, NT> S;
-    S.fock = reinterpret_cast<int16_t*>(p); p += sizeof(int16_t) * 2 * Ns;
-    S.part = reinterpret_cast<int16_t*>(p); p += sizeof(int16_t) * 2 * Nmax;
-    p = reinterpret_cast<char*>((reinterpret_cast<uintptr_t>(p) + 15) & ~uintptr_t(15));
-    S.nbr = reinterpret_cast<int32_t*>(p); p += sizeof(int32_t) * 4 * Ns;
-    p = reinterpret_cast<char*>((reinterpret_cast<uintptr_t>(p) + 15) & ~uintptr_t(15));
-    S.coef = reinterpret_cast<cx<T>*>(p); p += sizeof(cx<T>) * 4 * Nmax;
-    S.uu = reinterpret_cast<cx<T>*>(p); p += sizeof(cx<T>) * 2 * Nmax;
-    S.row = reinterpret_cast<cx<T>*>(p); p += sizeof(cx<T>) * 2 * Nmax;
-    S.wv = reinterpret_cast<cx<T>*>(p); p += sizeof(cx<T>) * 2 * Nmax;
-    S.red = reinterpret_cast<double*>(p); p += sizeof(double) * 2 * NW * 4;
-    S.redm = reinterpret_cast<double*>(p); p += sizeof(double) * NW * 4;
-    p = reinterpret_cast<char*>((reinterpret_cast<uintptr_t>(p) + 15) & ~uintptr_t(15));
-    GJSmem G = carve_gj<NT>(p, Nmax);
-
-    for (int i = tid; i < 2 * Ns; i += NT) S.fock[i] = J.fock[size_t(w) * 2 * Ns + i];
-    for (int i = tid; i < 2 * Nmax; i += NT) S.part[i] = J.part[size_t(w) * 2 * Nmax + i];
-    for (int i = tid; i < 4 * Ns; i += NT) S.nbr[i] = J.nbr[i];
-    {
-        const cx<T>* cg = Tab<T>::coef(J) + size_t(w) * 4 * Ns;   // [fl][sub][orbital]
-        for (int i = tid; i < 4 * Nmax; i += NT) {
-            const int fl = i / (2 * Nmax), sub = (i / Nmax) & 1, f = i % Nmax;
-            S.coef[i] = cg[(size_t(fl) * 2 + sub) * Ns + 2 * f];
-        }
-    }
-    __syncthreads();
-
-    const cx<T>* phase = Tab<T>::phase(J);
-    cx<T>* A0 = ai_ptr<T>(J, 0, w);
-    cx<T>* A1 = ai_ptr<T>(J, 1, w);
-    const uint32_t wid = J.walker_base + uint32_t(w);
-    uint64_t k = J.rng_next[w];
-    unsigned long long c_acc = 0, c_noop = 0, c_rej = 0, c_reinv = 0;
-    int since = J.since_reinv[w];
-    cx<double> am = J.amp_m[w];
-    int ae = J.amp_e[w];
-    int status = GV_OK;
-    int rbuf = 0;
-    const double inv_ns = 1.0 / double(Ns);
-
-    for (uint64_t s = 0; s < nsteps; ++s, k += 4) {
-        uint32_t x[4], y[4];
-        philox_call(J.seed, wid, 0, k >> 1, x);
-        philox_call(J.seed, wid, 0, (k >> 1) + 1, y);
-        const double u1 = u01(x[0], x[1]), u2 = u01(x[2], x[3]), u4 = u01(y[2], y[3]);
-        const int v1 = int(double(Ns) * u1);
-        const int v2 = S.nbr[v1 * 4 + int(4.0 * u2)];
-        const int f1 = S.fock[v1] >= 0 ? 0 : 1;
-        const int f2 = S.fock[v2] >= 0 ? 0 : 1;
-        int kind = 0, accepted;
-        double ratio = 1.0;
-        if (f1 == f2) {
-            accepted = 1;   // ratio m_weight/m_state_weight = 1 (MetroMC.cpp:41 with u4 < 1)
-            ++c_noop;
-        } else {
-            kind = 1;
-            const int upf = (f1 == 0) ? v1 : v2, upt = (f1 == 0) ? v2 : v1;
-            const int dnf = upt, dnt = upf;
-            const int cu = S.fock[upf], cd = S.fock[Ns + dnf];
-            cx<T> au = {T(0), T(0)}, ad = {T(0), T(0)};
-            for (int f = tid; f < N0; f += NT) {
-                const cx<T> u = phi_at<T>(phase, S.coef, J.Nk, Nmax, L, upt, f);
-                const cx<T> a = A0[size_t(cu) * N0 + f];
-                S.uu[f] = u;
-                S.row[f] = a;
-                cmac(au, a, u);
-            }
-            for (int f = tid; f < N1; f += NT) {
-                const cx<T> u = phi_at<T>(phase, S.coef + 2 * Nmax, J.Nk, Nmax, L, dnt, f);
-                const cx<T> a = A1[size_t(cd) * N1 + f];
-                S.uu[Nmax + f] = u;
-                S.row[Nmax + f] = a;
-                cmac(ad, a, u);
-            }
-            au = warp_sum(au);
-            ad = warp_sum(ad);
-            double* rb = S.red + rbuf * NW * 4;
-            rbuf ^= 1;
-            if (lane == 0) { rb[warp * 4 + 0] = au.x; rb[warp * 4 + 1] = au.y; rb[warp * 4 + 2] = ad.x; rb[warp * 4 + 3] = ad.y; }
-            __syncthreads();
-            cx<T> ru = {T(0), T(0)}, rd = {T(0), T(0)};
-            for (int q = 0; q < NW; ++q) {
-                ru.x += T(rb[q * 4 + 0]); ru.y += T(rb[q * 4 + 1]);
-                rd.x += T(rb[q * 4 + 2]); rd.y += T(rb[q * 4 + 3]);
-            }
-            const cx<double> q = to_d(ru) * to_d(rd);
-            ratio = norm2(q);
-            if (!isfinite(ratio)) { status = GV_ERR_NAN; break; }
-            accepted = ratio > 1.0 ? (u4 < 1.0) : (u4 < ratio);
-            if (!accepted) {
-                ++c_rej;
-            } else {
-                if (norm2(to_d(ru)) < 1e-9 || norm2(to_d(rd)) < 1e-9) { status = GV_ERR_SINGULAR; break; }
-                // w = Ai u - e_c (warp per row)
-                for (int pr = warp; pr < N0; pr += NW) {
-                    cx<T> a = {T(0), T(0)};
-                    const cx<T>* r = A0 + size_t(pr) * N0;
-                    for (int f = lane; f < N0; f += 32) cmac(a, r[f], S.uu[f]);
-                    a = warp_sum(a);
-                    if (lane == 0) { if (pr == cu) a.x -= T(1); S.wv[pr] = a; }
-                }
-                for (int pr = warp; pr < N1; pr += NW) {
-                    cx<T> a = {T(0), T(0)};
-                    const cx<T>* r = A1 + size_t(pr) * N1;
-                    for (int f = lane; f < N1; f += 32) cmac(a, r[f], S.uu[Nmax + f]);
-                    a = warp_sum(a);
-                    if (lane == 0) { if (pr == cd) a.x -= T(1); S.wv[Nmax + pr] = a; }
-                }
-                __syncthreads();
-                const cx<T> iu = cinv(ru), id = cinv(rd);
-                for (int f = tid; f < N0; f += NT) {
-                    const cx<T> rr = S.row[f] * iu;
-                    const cx<T> nr = {-rr.x, -rr.y};
-                    for (int pr = 0; pr < N0; ++pr) {
-                        cx<T> a = A0[size_t(pr) * N0 + f];
-                        cmac(a, S.wv[pr], nr);
-                        A0[size_t(pr) * N0 + f] = a;
-                    }
-                }
-                for (int f = tid; f < N1; f += NT) {
-                    const cx<T> rr = S.row[Nmax + f] * id;
-                    const cx<T> nr = {-rr.x, -rr.y};
-                    for (int pr = 0; pr < N1; ++pr) {
-                        cx<T> a = A1[size_t(pr) * N1 + f];
-                        cmac(a, S.wv[Nmax + pr], nr);
-                        A1[size_t(pr) * N1 + f] = a;
-                    }
-                }
-                __syncthreads();
-                if (tid == 0) {
-                    S.fock[upt] = int16_t(cu); S.fock[upf] = -1; S.part[cu] = int16_t(upt);
-                    S.fock[Ns + dnt] = int16_t(cd); S.fock[Ns + dnf] = -1; S.part[Nmax + cd] = int16_t(dnt);
-                }
-                am = am * q;
-                amp_normalise(am, ae);
-                ++c_acc;
-                ++since;
-                __syncthreads();
-                if (J.reinv_every > 0 && since >= J.reinv_every) {
-                    cx<double>* M = J.scratch64 + size_t(w) * Nmax * Nmax;
-                    int st = reinvert_walker<T, NT>(J, w, M, G, S.part);
-                    if (st != GV_OK) { status = st; break; }
-                    am = J.amp_m[w];   // written by thread 0; visible after the block barrier in reinvert
-                    __syncthreads();
-                    am = J.amp_m[w];
-                    ae = J.amp_e[w];
-                    since = 0;
-                    ++c_reinv;
-                }
-            }
-        }
-        if (J.trace && w == J.trace_walker && tid == 0) {
-            gv_trace t;
-            t.v1 = v1; t.v2 = v2; t.kind = kind; t.accepted = accepted; t.khop = kind ? 0 : -1; t.pad = 0;
-            t.ratio = ratio; t.u4 = u4;
-            J.trace[s] = t;
-        }
-        const uint64_t gs = s0 + s;
-        if (meas && (meas == 1 || gs % meas == 0) && mask) {
-            // ProjHeis (ProjHeis.cpp:40-158): E/site sample
-            if (mask & GV_MEAS_PROJHEIS) {
-                cx<double> e = {0.0, 0.0};
-                for (int ed = warp; ed < 2 * Ns; ed += NW) {
-                    const int vi = J.edges[2 * ed], vj = J.edges[2 * ed + 1];
-                    const bool ui = S.fock[vi] >= 0, uj = S.fock[vj] >= 0;
-                    if (ui == uj) { if (lane == 0) e.x += 0.25; continue; }
-                    const int upf = ui ? vi : vj, upt = ui ? vj : vi;
-                    const cx<T> ru = warp_ratio<T>(J, A0, phase, S.coef, N0, S.fock[upf], upt);
-                    const cx<T> rd = warp_ratio<T>(J, A1, phase, S.coef + 2 * Nmax, N1, S.fock[Ns + upt], upf);
-                    if (lane == 0) {
-                        const cx<double> r = to_d(ru) * to_d(rd);
-                        e.x += -0.25 - 0.5 * r.x;
-                        e.y += -0.5 * r.y;
-                    }
-                }
-                if (lane == 0) { S.redm[warp * 4] = e.x; S.redm[warp * 4 + 1] = e.y; }
-                __syncthreads();
-                if (tid == 0) {
-                    cx<double> t = {0.0, 0.0};
-                    for (int q = 0; q < NW; ++q) { t.x += S.redm[q * 4]; t.y += S.redm[q * 4 + 1]; }
-                    cx<double>& acc = J.pj[size_t(w) * 2];
-                    acc.x += t.x * inv_ns;
-                    acc.y += t.y * inv_ns;
-                    J.pj[size_t(w) * 2 + 1].x += 1.0;
-                    J.pj_n[w] += 1;
-                }
-                __syncthreads();
-            }
-            // StagMagnZ (StagMagnZ.cpp:12-43)
-            if (mask & GV_MEAS_STAGMAGN) {
-                int m = 0;
-                for (int v = tid; v < Ns; v += NT) {
-                    const int sg = (((v % L) + (v / L)) & 1) ? -1 : 1;
-                    m += sg * (S.fock[v] >= 0 ? 1 : -1);
-                }
-#pragma unroll
-                for (int o = 16; o; o >>= 1) m += __shfl_xor_sync(0xffffffffu, m, o);
-                if (lane == 0) S.redm[warp * 4 + 2] = double(m);
-                __syncthreads();
-                if (tid == 0) {
-                    double t = 0;
-                    for (int q = 0; q < NW; ++q) t += S.redm[q * 4 + 2];
-                    J.sm[w].x += t * inv_ns;
-                    J.sm_n[w] += 1;
-                }
-                __syncthreads();
-            }
-        }
-    }
-    __syncthreads();
-    for (int i = tid; i < 2 * Ns; i += NT) J.fock[size_t(w) * 2 * Ns + i] = S.fock[i];
-    for (int i = tid; i < 2 * Nmax; i += NT) J.part[size_t(w) * 2 * Nmax + i] = S.part[i];
-    if (tid == 0) {
-        J.rng_next[w] = k;
-        unsigned long long* c = J.counts + size_t(w) * 5;
-        c[0] += c_acc + c_noop + c_rej;
-        c[1] += c_acc;
-        c[2] += c_noop;
-        c[3] += c_rej;
-        c[4] += c_reinv;
-        J.since_reinv[w] = since;
-        J.amp_m[w] = am;
-        J.amp_e[w] = ae;
-        J.status[w] = status;
-    }
-}
-
-// ------------------------------------------------------------------------
-// StatSpinStruct (StatSpinStruct.cpp:16-135), ground state: for every pair
-// i <= j of the walker's configuration, szz +-1/4 and, for antiparallel
-// pairs, s-+ / s+- -= r_up(p_i -> j) r_dn(q_j -> i) (the swap ratio; the
-// conj(amp) swamp / w factor of the reference is that ratio).
-template <typename T, int NT>
-__global__ void __launch_bounds__(NT) k_statspin(DevJob J)
-{
-    const int w = blockIdx.x;
-    if (w >= J.W || J.status[w] != GV_OK) return;
-    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    constexpr int NW = NT / 32;
-    const int Ns = J.Ns, Nmax = J.Nmax;
-    const int16_t* fock = J.fock + size_t(w) * 2 * Ns;
-    const cx<T>* phase = Tab<T>::phase(J);
-    const cx<T>* cg = Tab<T>::coef(J) + size_t(w) * 4 * Ns;
-    extern __shared__ __align__(16) char smem[];
-    cx<T>* coef = reinterpret_cast<cx<T>*>(smem);   // 2 fl * 2 sub * Nmax
-    for (int i = tid; i < 4 * Nmax; i += NT) {
-        const int fl = i / (2 * Nmax), sub = (i / Nmax) & 1, f = i % Nmax;
-        coef[i] = cg[(size_t(fl) * 2 + sub) * Ns + 2 * f];
-    }
-    __syncthreads();
-    const cx<T>* A0 = ai_ptr<T>(J, 0, w);
-    const cx<T>* A1 = ai_ptr<T>(J, 1, w);
-    double* szz = J.ss;
-    double* spm = J.ss + 2 * size_t(Ns) * Ns;
-    double* smp = J.ss + 4 * size_t(Ns) * Ns;
-    for (int idx = warp; idx < Ns * Ns; idx += NW) {
-        const int vi = idx / Ns, vj = idx % Ns;
-        if (vj < vi) continue;
-        const bool ui = fock[vi] >= 0, uj = fock[vj] >= 0;
-        const size_t ij = size_t(vi) * Ns + vj, ji = size_t(vj) * Ns + vi;
-        if (ui == uj) {
-            if (lane == 0) {
-                if (vi == vj) {
-                    atomicAdd(&szz[2 * ij], 0.25);
-                    atomicAdd(ui ? &spm[2 * ij] : &smp[2 * ij], 1.0);
-                } else {
-                    atomicAdd(&szz[2 * ij], 0.25);
-                    atomicAdd(&szz[2 * ji], 0.25);
-                }
-            }
-            continue;
-        }
-        const int upf = ui ? vi : vj, upt = ui ? vj : vi;
-        const cx<T> ru = warp_ratio<T>(J, A0, phase, coef, J.N[0], fock[upf], upt);
-        const cx<T> rd = warp_ratio<T>(J, A1, phase, coef + 2 * Nmax, J.N[1], fock[Ns + upt], upf);
-        if (lane == 0) {
-            const cx<double> r = to_d(ru) * to_d(rd);
-            atomicAdd(&szz[2 * ij], -0.25);
-            atomicAdd(&szz[2 * ji], -0.25);
-            double* a = ui ? smp : spm;   // vi up: s-+[ij], s+-[ji]; vi down: s+-[ij], s-+[ji]
-            double* b = ui ? spm : smp;
-            atomicAdd(&a[2 * ij], -r.x); atomicAdd(&a[2 * ij + 1], -r.y);
-            atomicAdd(&b[2 * ji], -r.x); atomicAdd(&b[2 * ji + 1], -r.y);
-        }
-    }
-    if (tid == 0) atomicAdd(J.ss_n, 1);
-    (void)lane;
-}
-
-// ------------------------------------------------------------------------
-// VirtUpdate-style ratios for explicit hop sets of one walker (ground state).
-template <typename T>
-__global__ void k_virt_update(DevJob J, int w, int nset, const int32_t* hops, double* out)
-{
-    const int lane = threadIdx.x & 31;
-    const int set = blockIdx.x * (blockDim.x / 32) + (threadIdx.x >> 5);
-    if (set >= nset) return;
-    const int Ns = J.Ns, Nmax = J.Nmax;
-    const int16_t* fock = J.fock + size_t(w) * 2 * Ns;
-    const cx<T>* cg = Tab<T>::coef(J) + size_t(w) * 4 * Ns;
-    const cx<T>* phase = Tab<T>::phase(J);
-    cx<double> r = {1.0, 0.0};
-    for (int fl = 0; fl < 2; ++fl) {
-        const int from = hops[4 * set + 2 * fl], to = hops[4 * set + 2 * fl + 1];
-        if (from < 0) continue;
-        const int c = fock[fl * Ns + from];
-        if (c < 0) { r = cx<double>{nan(""), nan("")}; break; }   // no particle of this flavour there
-        const int N = J.N[fl];
-        const cx<T>* row = ai_ptr<T>(J, fl, w) + size_t(c) * N;
-        cx<T> acc = {T(0), T(0)};
-        const int sub = sublattice(to, J.L);
-        for (int f = lane; f < N; f += 32)
-            cmac(acc, row[f], cmul_rn(phase[size_t(to) * J.Nk + f], cg[(size_t(fl) * 2 + sub) * Ns + 2 * f]));
-        acc = warp_sum(acc);
-        r = r * to_d(acc);
-        (void)Nmax;
-    }
-    if (lane == 0) { out[2 * set] = r.x; out[2 * set + 1] = r.y; }
-}
-
-// max |(A Ai)_{f f'} - delta| per walker/flavour in FP64.
-template <typename T, int NT>
-__global__ void __launch_bounds__(NT) k_drift(DevJob J, double* out)
-{
-    const int w = blockIdx.x, fl = blockIdx.y;
-    const int N = J.N[fl], Ns = J.Ns;
-    const int16_t* part = J.part + (size_t(w) * 2 + fl) * J.Nmax;
-    const cx<double>* coef = J.coef64 + (size_t(w) * 2 + fl) * 2 * Ns;
-    const cx<T>* Ai = ai_ptr<T>(J, fl, w);
-    double mx = 0.0;
-    for (int idx = threadIdx.x; idx < N * N; idx += NT) {
-        const int f = idx / N, g = idx % N;
-        cx<double> s = {0.0, 0.0};
-        for (int pr = 0; pr < N; ++pr) {
-            const int site = part[pr];
-            const cx<double> a = cmul_rn(J.phase64[size_t(site) * J.Nk + f], coef[size_t(sublattice(site, J.L)) * Ns + 2 * f]);
-            cmac(s, a, to_d(Ai[size_t(pr) * N + g]));
-        }
-        if (f == g) s.x -= 1.0;
-        mx = fmax(mx, fmax(fabs(s.x), fabs(s.y)));
-    }
-    __shared__ double red[NT / 32];
-#pragma unroll
-    for (int o = 16; o; o >>= 1) mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, o));
-    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = mx;
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        double m = 0;
-        for (int q = 0; q < NT / 32; ++q) m = fmax(m, red[q]);
-        out[w * 2 + fl] = m;
-    }
-}
-
-}  // namespace
 
 // ==========================================================================
 // Host side
@@ -727,9 +89,10 @@ size_t scratch_walkers(const gv_job* j) { return size_t(j->W); }
 template <typename T, int NT>
 gv_status launch_walk(gv_job* j, uint64_t nsteps, uint64_t s0, uint64_t meas, int mask)
 {
-    size_t sm = walk_smem_bytes<T, NT>(j->Ns, j->Nmax);
-    GV_CK(cudaFuncSetAttribute(k_walk_gs<T, NT>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(sm)));
-    k_walk_gs<T, NT><<<j->W, NT, sm, j->stream>>>(j->d, nsteps, s0, meas, mask);
+    const bool inkernel = !(j->cfg.flags & GV_FLAG_REINV_DEFERRED);
+    const WalkLayout lay = walk_layout<T, NT>(j->Ns, j->Nmax, (mask & GV_MEAS_PROJHEIS) != 0, inkernel);
+    GV_CK(cudaFuncSetAttribute(k_walk_gs<T, NT>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(lay.total)));
+    k_walk_gs<T, NT><<<j->W, NT, lay.total, j->stream>>>(j->d, nsteps, s0, meas, mask, inkernel ? 1 : 0);
     GV_CK(cudaGetLastError());
     ++j->last_launches;
     ++j->total_launches;
@@ -758,19 +121,20 @@ gv_status statspin_dispatch(gv_job* j)
 }
 
 template <typename T, int NT>
-gv_status launch_invert(gv_job* j)
+gv_status launch_invert(gv_job* j, int only_due)
 {
     size_t sm = gj_smem_bytes(j->Nmax, NT) + 64;
     GV_CK(cudaFuncSetAttribute(k_invert<T, NT>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(sm)));
-    k_invert<T, NT><<<j->W, NT, sm, j->stream>>>(j->d, 0, j->W);
+    k_invert<T, NT><<<j->W, NT, sm, j->stream>>>(j->d, only_due);
     GV_CK(cudaGetLastError());
     ++j->total_launches;
     return GV_OK;
 }
 
-gv_status invert_all(gv_job* j)
+gv_status invert_all(gv_job* j, int only_due = 0)
 {
-    return j->cfg.precision == GV_PREC_FP64 ? launch_invert<double, 256>(j) : launch_invert<float, 256>(j);
+    return j->cfg.precision == GV_PREC_FP64 ? launch_invert<double, 256>(j, only_due)
+                                            : launch_invert<float, 256>(j, only_due);
 }
 
 // LatticeState::RanInit (LatticeState.cpp:37-82) for the two-flavour
@@ -955,8 +319,14 @@ gv_status gv_job_create(const gv_job_config* cfg, gv_job** out)
         cf64[i] = {coef[i].real(), coef[i].imag()};
         cf32[i] = {float(coef[i].real()), float(coef[i].imag())};
     }
-    std::vector<int32_t> edges(size_t(2) * j->Ns * 2);
-    for (int e = 0; e < 2 * j->Ns; ++e) { edges[2 * e] = j->lat.edge_i[e]; edges[2 * e + 1] = j->lat.edge_j[e]; }
+    std::vector<int32_t> edges(size_t(2) * j->Ns * 4);
+    for (int e = 0; e < 2 * j->Ns; ++e) {
+        const int a = j->lat.edge_i[e], b = j->lat.edge_j[e];
+        int ka = 0, kb = 0;
+        while (ka < 3 && j->lat.nbr[a * 4 + ka] != b) ++ka;
+        while (kb < 3 && j->lat.nbr[b * 4 + kb] != a) ++kb;
+        edges[4 * e] = a; edges[4 * e + 1] = b; edges[4 * e + 2] = ka; edges[4 * e + 3] = kb;
+    }
 
     auto fail = [&](gv_status s) { gv_job_destroy(j); return s; };
     if (cudaStreamCreateWithFlags(&j->stream, cudaStreamNonBlocking) != cudaSuccess) { delete j; return GV_ERR_CUDA; }
@@ -997,7 +367,7 @@ gv_status gv_job_create(const gv_job_config* cfg, gv_job** out)
         (st = dalloc(j, &d.ss_n, sizeof(int32_t))) ||
         (st = dalloc(j, &d.scratch64, scratch_walkers(j) * j->Nmax * j->Nmax * sizeof(cx<double>))))
         return fail(st);
-    d.nbr = nbr; d.edges = edg; d.phase64 = p64; d.phase32 = p32; d.coef64 = c64; d.coef32 = c32;
+    d.nbr = nbr; d.edges = reinterpret_cast<const int4*>(edg); d.phase64 = p64; d.phase32 = p32; d.coef64 = c64; d.coef32 = c32;
     d.Ai[0] = a0; d.Ai[1] = a1;
     if (cudaMemcpyAsync(nbr, j->lat.nbr.data(), sizeof(int32_t) * 4 * j->Ns, cudaMemcpyHostToDevice, j->stream) ||
         cudaMemcpyAsync(edg, edges.data(), edges.size() * sizeof(int32_t), cudaMemcpyHostToDevice, j->stream) ||
@@ -1120,6 +490,7 @@ static gv_status walk_impl(gv_job* j, uint64_t len, uint64_t meas, gv_trace* dtr
         }
         j->d.trace = dtrace;
     }
+    if (!st && (j->cfg.flags & GV_FLAG_REINV_DEFERRED) && j->cfg.reinv_every > 0) st = invert_all(j, 1);
     GV_CK(cudaEventRecord(j->ev1, j->stream));
     j->d.trace = nullptr;
     j->d.trace_walker = -1;
@@ -1291,24 +662,15 @@ gv_status gv_job_read_inverse(gv_job* j, int32_t walker, int32_t fl, double* out
     GV_CK(cudaStreamSynchronize(j->stream));
     const int N = j->N[fl];
     const size_t n = size_t(N) * N;
+    // AiT[f][p] = (A^-1)(p, f) is the reference's column-major m_mati[p + f*N].
     if (j->cfg.precision == GV_PREC_FP64) {
-        std::vector<cx<double>> a(n);
-        GV_CK(cudaMemcpy(a.data(), static_cast<cx<double>*>(j->d.Ai[fl]) + size_t(walker) * n, n * sizeof(cx<double>),
+        GV_CK(cudaMemcpy(out, static_cast<cx<double>*>(j->d.Ai[fl]) + size_t(walker) * n, n * sizeof(cx<double>),
                          cudaMemcpyDeviceToHost));
-        for (int p = 0; p < N; ++p)
-            for (int f = 0; f < N; ++f) {
-                out[2 * (size_t(p) + size_t(f) * N)] = a[size_t(p) * N + f].x;
-                out[2 * (size_t(p) + size_t(f) * N) + 1] = a[size_t(p) * N + f].y;
-            }
     } else {
         std::vector<cx<float>> a(n);
         GV_CK(cudaMemcpy(a.data(), static_cast<cx<float>*>(j->d.Ai[fl]) + size_t(walker) * n, n * sizeof(cx<float>),
                          cudaMemcpyDeviceToHost));
-        for (int p = 0; p < N; ++p)
-            for (int f = 0; f < N; ++f) {
-                out[2 * (size_t(p) + size_t(f) * N)] = a[size_t(p) * N + f].x;
-                out[2 * (size_t(p) + size_t(f) * N) + 1] = a[size_t(p) * N + f].y;
-            }
+        for (size_t i = 0; i < n; ++i) { out[2 * i] = a[i].x; out[2 * i + 1] = a[i].y; }
     }
     return GV_OK;
 }

@@ -1,0 +1,687 @@
+// Engine kernels (ground-state channel).  Included by engine.cu.
+//
+// Inverse layout: AiT[f][p] = (A^-1)(p, f) -- row f (orbital row of A) is
+// contiguous over particles p.  This is the reference's column-major m_mati
+// (m_mati[p + f*N]).  With it the two O(N^2) passes of an accepted move are
+// thread-per-particle loops over rows f: every load is coalesced across the
+// warp, accumulations stay in registers, and particle p's column is owned
+// by one thread in both passes, so the matrix-vector product and the rank-1
+// update need no barrier between them.
+#pragma once
+
+#include "device.cuh"
+
+namespace gv {
+namespace {
+
+template <typename T> struct Tab;
+template <> struct Tab<double> {
+    static __device__ __forceinline__ const cx<double>* phase(const DevJob& J) { return J.phase64; }
+    static __device__ __forceinline__ const cx<double>* coef(const DevJob& J) { return J.coef64; }
+};
+template <> struct Tab<float> {
+    static __device__ __forceinline__ const cx<float>* phase(const DevJob& J) { return J.phase32; }
+    static __device__ __forceinline__ const cx<float>* coef(const DevJob& J) { return J.coef32; }
+};
+
+template <typename T>
+__device__ __forceinline__ cx<T>* ai_ptr(const DevJob& J, int fl, int w)
+{
+    return static_cast<cx<T>*>(J.Ai[fl]) + size_t(w) * J.N[fl] * J.N[fl];
+}
+
+__device__ __forceinline__ int sublattice(int s, int L) { return ((s % L) + (s / L)) & 1; }
+
+template <typename T>
+__device__ __forceinline__ cx<T> warp_sum(cx<T> v)
+{
+#pragma unroll
+    for (int o = 16; o; o >>= 1) {
+        v.x += __shfl_xor_sync(0xffffffffu, v.x, o);
+        v.y += __shfl_xor_sync(0xffffffffu, v.y, o);
+    }
+    return v;
+}
+
+// phi_{2f}(s) for ground-state row f: phase[s][f] * coef[sub(s)][2f]
+// (coef_fl here is the per-row copy [sub][f]).
+template <typename T>
+__device__ __forceinline__ cx<T> phi_row(const cx<T>* phase, const cx<T>* coef_fl, int Nk, int Nmax, int L, int s,
+                                         int f)
+{
+    return cmul_rn(phase[size_t(s) * Nk + f], coef_fl[sublattice(s, L) * Nmax + f]);
+}
+
+// ------------------------------------------------------------------------
+// FP64 Gauss-Jordan inversion with partial (row) pivoting on max |re|+|im|,
+// in place on M (N x N row-major).  det = prod(pivots) * (-1)^swaps.
+struct GJSmem {
+    cx<double>* rowk;
+    cx<double>* fcol;
+    int* perm;
+    double* redv;
+    int* redi;
+    cx<double>* detm;
+    int* dete;
+    int* flag;
+};
+
+template <int NT>
+__device__ __forceinline__ GJSmem carve_gj(char*& p, int Nmax)
+{
+    GJSmem S;
+    S.rowk = reinterpret_cast<cx<double>*>(p); p += sizeof(cx<double>) * Nmax;
+    S.fcol = reinterpret_cast<cx<double>*>(p); p += sizeof(cx<double>) * Nmax;
+    S.detm = reinterpret_cast<cx<double>*>(p); p += sizeof(cx<double>) * 2;
+    S.redv = reinterpret_cast<double*>(p); p += sizeof(double) * (NT / 32);
+    S.perm = reinterpret_cast<int*>(p); p += sizeof(int) * Nmax;
+    S.redi = reinterpret_cast<int*>(p); p += sizeof(int) * (NT / 32);
+    S.dete = reinterpret_cast<int*>(p); p += sizeof(int) * 2;
+    S.flag = reinterpret_cast<int*>(p); p += sizeof(int) * 2;
+    p = reinterpret_cast<char*>((reinterpret_cast<uintptr_t>(p) + 15) & ~uintptr_t(15));
+    return S;
+}
+
+__host__ __device__ inline size_t gj_smem_bytes(int Nmax, int NT)
+{
+    return sizeof(cx<double>) * (2 * Nmax + 2) + sizeof(double) * (NT / 32) + sizeof(int) * (Nmax + NT / 32 + 4) + 16;
+}
+
+template <int NT>
+__device__ bool gj_invert(cx<double>* M, int N, const GJSmem& S, cx<double>& det_m, int& det_e)
+{
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    constexpr int NW = NT / 32;
+    cx<double> dm = {1.0, 0.0};
+    int de = 0;
+    for (int k = 0; k < N; ++k) {
+        double best = -1.0;
+        int bi = N;
+        for (int i = k + tid; i < N; i += NT) {
+            const cx<double> v = M[size_t(i) * N + k];
+            const double a = fabs(v.x) + fabs(v.y);
+            if (a > best) { best = a; bi = i; }
+        }
+#pragma unroll
+        for (int o = 16; o; o >>= 1) {
+            const double ob = __shfl_xor_sync(0xffffffffu, best, o);
+            const int oi = __shfl_xor_sync(0xffffffffu, bi, o);
+            if (ob > best || (ob == best && oi < bi)) { best = ob; bi = oi; }
+        }
+        if (lane == 0) { S.redv[warp] = best; S.redi[warp] = bi; }
+        __syncthreads();
+        best = S.redv[0];
+        bi = S.redi[0];
+        for (int q = 1; q < NW; ++q)
+            if (S.redv[q] > best || (S.redv[q] == best && S.redi[q] < bi)) { best = S.redv[q]; bi = S.redi[q]; }
+        if (!(best > 0.0)) return false;
+        const int p = bi;
+        if (p != k)
+            for (int j = tid; j < N; j += NT) {
+                const cx<double> a = M[size_t(k) * N + j];
+                M[size_t(k) * N + j] = M[size_t(p) * N + j];
+                M[size_t(p) * N + j] = a;
+            }
+        __syncthreads();
+        const cx<double> piv = M[size_t(k) * N + k];
+        if (tid == 0) {
+            S.perm[k] = p;
+            dm = dm * piv;
+            if (p != k) { dm.x = -dm.x; dm.y = -dm.y; }
+            amp_normalise(dm, de);
+        }
+        const cx<double> inv = cinv(piv);
+        for (int j = tid; j < N; j += NT) {
+            cx<double> v = (j == k) ? cx<double>{1.0, 0.0} : M[size_t(k) * N + j];
+            S.rowk[j] = v * inv;
+        }
+        for (int i = tid; i < N; i += NT) S.fcol[i] = (i == k) ? cx<double>{0.0, 0.0} : M[size_t(i) * N + k];
+        __syncthreads();
+        for (int j = tid; j < N; j += NT) M[size_t(k) * N + j] = S.rowk[j];
+        for (int i = warp; i < N; i += NW) {
+            if (i == k) continue;
+            const cx<double> f = S.fcol[i];
+            const cx<double> nf = {-f.x, -f.y};
+            for (int j = lane; j < N; j += 32) {
+                cx<double> v = (j == k) ? cx<double>{0.0, 0.0} : M[size_t(i) * N + j];
+                cmac(v, nf, S.rowk[j]);
+                M[size_t(i) * N + j] = v;
+            }
+        }
+        __syncthreads();
+    }
+    for (int k = N - 1; k >= 0; --k) {
+        const int p = S.perm[k];
+        if (p != k)
+            for (int i = tid; i < N; i += NT) {
+                const cx<double> a = M[size_t(i) * N + k];
+                M[size_t(i) * N + k] = M[size_t(i) * N + p];
+                M[size_t(i) * N + p] = a;
+            }
+        __syncthreads();
+    }
+    if (tid == 0) { det_m = dm; det_e = de; }
+    return true;
+}
+
+// SlaterDeterminant::Init for walker w (SlaterDeterminant.cpp:60-92).
+// Inverts M = A^T, M[r][f] = phi_{2f}(site of particle r): M^-1 = (A^-1)^T,
+// i.e. M^-1[f][p] = (A^-1)(p, f), already in the AiT layout.  Amplitude =
+// det_0 * det_1; singular as linalg::DetInv (|det|^2 < 1e-9) or zero overlap
+// (base-10 exponent < -8, SlaterDeterminant.cpp:78-81).
+template <typename T, int NT>
+__device__ __noinline__ int reinvert_walker(const DevJob& J, int w, cx<double>* M, const GJSmem& S,
+                                            const int16_t* part_s)
+{
+    const int tid = threadIdx.x;
+    cx<double> am = {1.0, 0.0};
+    int ae = 0;
+    int status = GV_OK;
+    for (int fl = 0; fl < 2; ++fl) {
+        const int N = J.N[fl];
+        const int16_t* part = part_s ? part_s + fl * J.Nmax : J.part + (size_t(w) * 2 + fl) * J.Nmax;
+        const cx<double>* coef = J.coef64 + (size_t(w) * 2 + fl) * 2 * J.Ns;
+        for (int idx = tid; idx < N * N; idx += NT) {
+            const int r = idx / N, f = idx % N;
+            const int s = part[r];
+            M[idx] = cmul_rn(J.phase64[size_t(s) * J.Nk + f], coef[size_t(sublattice(s, J.L)) * J.Ns + 2 * f]);
+        }
+        __syncthreads();
+        cx<double> dm;
+        int de;
+        bool ok = gj_invert<NT>(M, N, S, dm, de);
+        if (tid == 0) { S.detm[0] = dm; S.dete[0] = de; S.flag[0] = ok; }
+        __syncthreads();
+        ok = S.flag[0];
+        dm = S.detm[0];
+        de = S.dete[0];
+        __syncthreads();
+        const double l10 = ok ? (log10(sqrt(norm2(dm))) + de * 0.30102999566398119521) : -1e300;
+        if (!ok || 2.0 * l10 < -9.0 || floor(l10) < -8.0) status = GV_ERR_SINGULAR;
+        cx<T>* out = ai_ptr<T>(J, fl, w);
+        for (int idx = tid; idx < N * N; idx += NT) {
+            const cx<double> v = M[idx];
+            out[idx] = cx<T>{T(v.x), T(v.y)};
+        }
+        am = am * dm;
+        ae += de;
+        amp_normalise(am, ae);
+        __syncthreads();
+    }
+    if (tid == 0) {
+        if (status == GV_OK) { J.amp_m[w] = am; J.amp_e[w] = ae; }
+        else { J.amp_m[w] = cx<double>{0.0, 0.0}; J.amp_e[w] = 0; }
+    }
+    __syncthreads();
+    return status;
+}
+
+// Initial inversion / re-inversion of every walker (only_due: only walkers
+// whose accepted-move count reached reinv_every, the deferred cadence).
+template <typename T, int NT>
+__global__ void __launch_bounds__(NT) k_invert(DevJob J, int only_due)
+{
+    extern __shared__ __align__(16) char smem[];
+    const int w = blockIdx.x;
+    if (w >= J.W) return;
+    if (only_due) {
+        if (J.status[w] != GV_OK || J.reinv_every <= 0 || J.since_reinv[w] < J.reinv_every) return;
+    }
+    char* p = smem;
+    GJSmem S = carve_gj<NT>(p, J.Nmax);
+    cx<double>* M = J.scratch64 + size_t(w) * J.Nmax * J.Nmax;
+    const int st = reinvert_walker<T, NT>(J, w, M, S, nullptr);
+    if (threadIdx.x == 0) {
+        J.status[w] = st;
+        if (only_due) { J.since_reinv[w] = 0; J.counts[size_t(w) * 5 + 4] += 1; }
+    }
+}
+
+// ------------------------------------------------------------------------
+// Metropolis walk, ground-state channel: one CTA per walker.  Each step is
+// MetroMC::Step (MetroMC.cpp:90-103): uniforms u1..u4 (vertex, neighbour,
+// internal state, accept test); equal flavours are a no-op that is always
+// accepted; otherwise the determinant ratios
+//     r_fl = sum_f (A^-1)(c, f) phi_{2f}(d)          (linalg.cpp:297-303 / 146)
+// and on acceptance the Sherman-Morrison update of both inverses
+//     A^-1 <- A^-1 - (A^-1 u - e_c)(e_c^T A^-1) / r  (linalg.cpp:402-573, rc=1).
+struct WalkLayout {
+    size_t fock, part, nbr, coef, uu, row, rr, red, rdn, gj, total;
+};
+
+template <typename T, int NT>
+__host__ __device__ inline WalkLayout walk_layout(int Ns, int Nmax, bool projheis, bool gj)
+{
+    WalkLayout l;
+    size_t b = 0;
+    auto al = [&](size_t x) { b = (b + 15) & ~size_t(15); size_t r = b; b += x; return r; };
+    l.fock = al(sizeof(int16_t) * 2 * Ns);
+    l.part = al(sizeof(int16_t) * 2 * Nmax);
+    l.nbr = al(sizeof(int16_t) * 4 * Ns);
+    l.coef = al(sizeof(cx<T>) * 4 * Nmax);
+    l.uu = al(sizeof(cx<T>) * 2 * Nmax);
+    l.row = al(sizeof(cx<T>) * 2 * Nmax);
+    l.rr = al(sizeof(cx<T>) * 2 * Nmax);
+    l.red = al(sizeof(double) * (2 * (NT / 32) * 4 + (NT / 32) * 4));
+    l.rdn = al(projheis ? sizeof(cx<T>) * 4 * Ns : 16);
+    l.gj = al(gj ? gj_smem_bytes(Nmax, NT) : 16);
+    l.total = al(16);
+    return l;
+}
+
+// Column p of AiT (rows f = 0..N-1): acc = sum_f AiT[f][p] * v[f], 8 loads in flight.
+template <typename T>
+__device__ __forceinline__ cx<T> col_dot(const cx<T>* __restrict__ A, int N, int p, const cx<T>* v)
+{
+    cx<T> acc = {T(0), T(0)};
+    int f = 0;
+    for (; f + 8 <= N; f += 8) {
+        cx<T> a[8];
+#pragma unroll
+        for (int k = 0; k < 8; ++k) a[k] = A[size_t(f + k) * N + p];
+#pragma unroll
+        for (int k = 0; k < 8; ++k) cmac(acc, a[k], v[f + k]);
+    }
+    for (; f < N; ++f) cmac(acc, A[size_t(f) * N + p], v[f]);
+    return acc;
+}
+
+// Column p of AiT: AiT[f][p] -= w * rr[f], 8 loads in flight.
+template <typename T>
+__device__ __forceinline__ void col_update(cx<T>* A, int N, int p, cx<T> w, const cx<T>* rr)
+{
+    const cx<T> nw = {-w.x, -w.y};
+    int f = 0;
+    for (; f + 8 <= N; f += 8) {
+        cx<T> a[8];
+#pragma unroll
+        for (int k = 0; k < 8; ++k) a[k] = A[size_t(f + k) * N + p];
+#pragma unroll
+        for (int k = 0; k < 8; ++k) {
+            cmac(a[k], nw, rr[f + k]);
+            A[size_t(f + k) * N + p] = a[k];
+        }
+    }
+    for (; f < N; ++f) {
+        cx<T> a = A[size_t(f) * N + p];
+        cmac(a, nw, rr[f]);
+        A[size_t(f) * N + p] = a;
+    }
+}
+
+template <typename T, int NT>
+__global__ void __launch_bounds__(NT) k_walk_gs(DevJob J, uint64_t nsteps, uint64_t s0, uint64_t meas, int mask,
+                                                int inkernel_reinv)
+{
+    extern __shared__ __align__(16) char smem[];
+    constexpr int NW = NT / 32;
+    const int w = blockIdx.x;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    if (w >= J.W || J.status[w] != GV_OK) return;
+    const int Ns = J.Ns, Nmax = J.Nmax, L = J.L, Nk = J.Nk;
+    const int N0 = J.N[0], N1 = J.N[1];
+    const WalkLayout lay = walk_layout<T, NT>(Ns, Nmax, (mask & GV_MEAS_PROJHEIS) != 0, inkernel_reinv != 0);
+    int16_t* s_fock = reinterpret_cast<int16_t*>(smem + lay.fock);
+    int16_t* s_part = reinterpret_cast<int16_t*>(smem + lay.part);
+    int16_t* s_nbr = reinterpret_cast<int16_t*>(smem + lay.nbr);
+    cx<T>* s_coef = reinterpret_cast<cx<T>*>(smem + lay.coef);
+    cx<T>* s_uu = reinterpret_cast<cx<T>*>(smem + lay.uu);
+    cx<T>* s_row = reinterpret_cast<cx<T>*>(smem + lay.row);
+    cx<T>* s_rr = reinterpret_cast<cx<T>*>(smem + lay.rr);
+    double* s_red = reinterpret_cast<double*>(smem + lay.red);
+    double* s_redm = s_red + 2 * NW * 4;
+    cx<T>* s_rq = reinterpret_cast<cx<T>*>(smem + lay.rdn);
+
+    for (int i = tid; i < 2 * Ns; i += NT) s_fock[i] = J.fock[size_t(w) * 2 * Ns + i];
+    for (int i = tid; i < 2 * Nmax; i += NT) s_part[i] = J.part[size_t(w) * 2 * Nmax + i];
+    for (int i = tid; i < 4 * Ns; i += NT) s_nbr[i] = int16_t(J.nbr[i]);
+    {
+        const cx<T>* cg = Tab<T>::coef(J) + size_t(w) * 4 * Ns;   // [fl][sub][orbital]
+        for (int i = tid; i < 4 * Nmax; i += NT) {
+            const int fl = i / (2 * Nmax), sub = (i / Nmax) & 1, f = i % Nmax;
+            s_coef[i] = cg[(size_t(fl) * 2 + sub) * Ns + 2 * f];
+        }
+    }
+    __syncthreads();
+
+    const cx<T>* phase = Tab<T>::phase(J);
+    cx<T>* A0 = ai_ptr<T>(J, 0, w);
+    cx<T>* A1 = ai_ptr<T>(J, 1, w);
+    const uint32_t wid = J.walker_base + uint32_t(w);
+    uint64_t k = J.rng_next[w];
+    unsigned long long c_acc = 0, c_noop = 0, c_rej = 0, c_reinv = 0;
+    int since = J.since_reinv[w];
+    cx<double> am = J.amp_m[w];
+    int ae = J.amp_e[w];
+    int status = GV_OK;
+    int rbuf = 0;
+    const double inv_ns = 1.0 / double(Ns);
+
+    for (uint64_t s = 0; s < nsteps; ++s, k += 4) {
+        uint32_t x[4], y[4];
+        philox_call(J.seed, wid, 0, k >> 1, x);
+        philox_call(J.seed, wid, 0, (k >> 1) + 1, y);
+        const double u1 = u01(x[0], x[1]), u2 = u01(x[2], x[3]), u4 = u01(y[2], y[3]);
+        const int v1 = int(double(Ns) * u1);
+        const int v2 = s_nbr[v1 * 4 + int(4.0 * u2)];
+        const int f1 = s_fock[v1] >= 0 ? 0 : 1;
+        const int f2 = s_fock[v2] >= 0 ? 0 : 1;
+        int kind = 0, accepted;
+        double ratio = 1.0;
+        if (f1 == f2) {
+            accepted = 1;   // m_weight / m_state_weight = 1, u4 < 1 (MetroMC.cpp:41)
+            ++c_noop;
+        } else {
+            kind = 1;
+            const int upf = (f1 == 0) ? v1 : v2, upt = (f1 == 0) ? v2 : v1;
+            const int dnf = upt, dnt = upf;
+            const int cu = s_fock[upf], cd = s_fock[Ns + dnf];
+            cx<T> au = {T(0), T(0)}, ad = {T(0), T(0)};
+            for (int f = tid; f < N0; f += NT) {
+                const cx<T> a = A0[size_t(f) * N0 + cu];
+                const cx<T> u = phi_row<T>(phase, s_coef, Nk, Nmax, L, upt, f);
+                s_row[f] = a;
+                s_uu[f] = u;
+                cmac(au, a, u);
+            }
+            for (int f = tid; f < N1; f += NT) {
+                const cx<T> a = A1[size_t(f) * N1 + cd];
+                const cx<T> u = phi_row<T>(phase, s_coef + 2 * Nmax, Nk, Nmax, L, dnt, f);
+                s_row[Nmax + f] = a;
+                s_uu[Nmax + f] = u;
+                cmac(ad, a, u);
+            }
+            au = warp_sum(au);
+            ad = warp_sum(ad);
+            double* rb = s_red + rbuf * NW * 4;
+            rbuf ^= 1;
+            if (lane == 0) { rb[warp * 4 + 0] = au.x; rb[warp * 4 + 1] = au.y; rb[warp * 4 + 2] = ad.x; rb[warp * 4 + 3] = ad.y; }
+            __syncthreads();
+            cx<T> ru = {T(0), T(0)}, rd = {T(0), T(0)};
+            for (int q = 0; q < NW; ++q) {
+                ru.x += T(rb[q * 4 + 0]); ru.y += T(rb[q * 4 + 1]);
+                rd.x += T(rb[q * 4 + 2]); rd.y += T(rb[q * 4 + 3]);
+            }
+            const cx<double> q = to_d(ru) * to_d(rd);
+            ratio = norm2(q);
+            if (!isfinite(ratio)) { status = GV_ERR_NAN; break; }
+            accepted = ratio > 1.0 ? (u4 < 1.0) : (u4 < ratio);
+            if (!accepted) {
+                ++c_rej;
+            } else {
+                if (norm2(to_d(ru)) < 1e-9 || norm2(to_d(rd)) < 1e-9) { status = GV_ERR_SINGULAR; break; }
+                const cx<T> iu = cinv(ru), id = cinv(rd);
+                for (int f = tid; f < N0; f += NT) s_rr[f] = s_row[f] * iu;
+                for (int f = tid; f < N1; f += NT) s_rr[Nmax + f] = s_row[Nmax + f] * id;
+                __syncthreads();
+                // Per particle column p (one owner thread): w_p = (A^-1 u)_p - [p == c],
+                // then column update with the old row c of A^-1 divided by r.
+                for (int p = tid; p < N0; p += NT) {
+                    cx<T> wp = col_dot<T>(A0, N0, p, s_uu);
+                    if (p == cu) wp.x -= T(1);
+                    col_update<T>(A0, N0, p, wp, s_rr);
+                }
+                for (int p = tid; p < N1; p += NT) {
+                    cx<T> wp = col_dot<T>(A1, N1, p, s_uu + Nmax);
+                    if (p == cd) wp.x -= T(1);
+                    col_update<T>(A1, N1, p, wp, s_rr + Nmax);
+                }
+                __syncthreads();
+                if (tid == 0) {
+                    s_fock[upt] = int16_t(cu); s_fock[upf] = -1; s_part[cu] = int16_t(upt);
+                    s_fock[Ns + dnt] = int16_t(cd); s_fock[Ns + dnf] = -1; s_part[Nmax + cd] = int16_t(dnt);
+                }
+                am = am * q;
+                amp_normalise(am, ae);
+                ++c_acc;
+                ++since;
+                __syncthreads();
+                if (inkernel_reinv && J.reinv_every > 0 && since >= J.reinv_every) {
+                    char* gp = smem + lay.gj;
+                    GJSmem G = carve_gj<NT>(gp, Nmax);
+                    cx<double>* M = J.scratch64 + size_t(w) * Nmax * Nmax;
+                    const int st = reinvert_walker<T, NT>(J, w, M, G, s_part);
+                    if (st != GV_OK) { status = st; break; }
+                    am = J.amp_m[w];
+                    ae = J.amp_e[w];
+                    since = 0;
+                    ++c_reinv;
+                }
+            }
+        }
+        if (J.trace && w == J.trace_walker && tid == 0) {
+            gv_trace t;
+            t.v1 = v1; t.v2 = v2; t.kind = kind; t.accepted = accepted; t.khop = kind ? 0 : -1; t.pad = 0;
+            t.ratio = ratio; t.u4 = u4;
+            J.trace[s] = t;
+        }
+        const uint64_t gs = s0 + s;
+        if (meas && (meas == 1 || gs % meas == 0) && mask) {
+            if (mask & GV_MEAS_PROJHEIS) {
+                // ProjHeis (ProjHeis.cpp:40-158): pass 1, every particle computes the ratio of
+                // moving it to each antiparallel neighbour into rq[site][slot] (a site holds
+                // one particle); pass 2 walks the edges in creation order and pairs the two
+                // flavours' ratios of each antiparallel bond.
+                for (int idx = tid; idx < N0 + N1; idx += NT) {
+                    const int fl = idx < N0 ? 0 : 1;
+                    const int p = fl ? idx - N0 : idx;
+                    const int N = fl ? N1 : N0;
+                    const cx<T>* A = fl ? A1 : A0;
+                    const cx<T>* cf = s_coef + fl * 2 * Nmax;
+                    const int site = s_part[fl * Nmax + p];
+                    int js[4];
+                    bool anti[4];
+#pragma unroll
+                    for (int kk = 0; kk < 4; ++kk) {
+                        js[kk] = s_nbr[site * 4 + kk];
+                        anti[kk] = (s_fock[js[kk]] >= 0) != (fl == 0);
+                    }
+                    cx<T> acc[4] = {{T(0), T(0)}, {T(0), T(0)}, {T(0), T(0)}, {T(0), T(0)}};
+                    for (int f = 0; f < N; ++f) {
+                        const cx<T> a = A[size_t(f) * N + p];
+#pragma unroll
+                        for (int kk = 0; kk < 4; ++kk)
+                            if (anti[kk]) cmac(acc[kk], a, phi_row<T>(phase, cf, Nk, Nmax, L, js[kk], f));
+                    }
+#pragma unroll
+                    for (int kk = 0; kk < 4; ++kk) s_rq[site * 4 + kk] = acc[kk];
+                }
+                __syncthreads();
+                cx<double> e = {0.0, 0.0};
+                for (int ed = tid; ed < 2 * Ns; ed += NT) {
+                    const int4 E = J.edges[ed];   // (i, j, slot of j at i, slot of i at j)
+                    const bool ui = s_fock[E.x] >= 0, uj = s_fock[E.y] >= 0;
+                    if (ui == uj) { e.x += 0.25; continue; }
+                    const cx<double> r = to_d(s_rq[E.x * 4 + E.z]) * to_d(s_rq[E.y * 4 + E.w]);
+                    e.x += -0.25 - 0.5 * r.x;
+                    e.y += -0.5 * r.y;
+                }
+#pragma unroll
+                for (int o = 16; o; o >>= 1) {
+                    e.x += __shfl_xor_sync(0xffffffffu, e.x, o);
+                    e.y += __shfl_xor_sync(0xffffffffu, e.y, o);
+                }
+                if (lane == 0) { s_redm[warp * 4] = e.x; s_redm[warp * 4 + 1] = e.y; }
+                __syncthreads();
+                if (tid == 0) {
+                    double ex = 0, ey = 0;
+                    for (int q = 0; q < NW; ++q) { ex += s_redm[q * 4]; ey += s_redm[q * 4 + 1]; }
+                    J.pj[size_t(w) * 2].x += ex * inv_ns;
+                    J.pj[size_t(w) * 2].y += ey * inv_ns;
+                    J.pj[size_t(w) * 2 + 1].x += 1.0;
+                    J.pj_n[w] += 1;
+                }
+                __syncthreads();
+            }
+            if (mask & GV_MEAS_STAGMAGN) {   // StagMagnZ (StagMagnZ.cpp:12-43)
+                int m = 0;
+                for (int v = tid; v < Ns; v += NT) {
+                    const int sg = (((v % L) + (v / L)) & 1) ? -1 : 1;
+                    m += sg * (s_fock[v] >= 0 ? 1 : -1);
+                }
+#pragma unroll
+                for (int o = 16; o; o >>= 1) m += __shfl_xor_sync(0xffffffffu, m, o);
+                if (lane == 0) s_redm[warp * 4 + 2] = double(m);
+                __syncthreads();
+                if (tid == 0) {
+                    double t = 0;
+                    for (int q = 0; q < NW; ++q) t += s_redm[q * 4 + 2];
+                    J.sm[w].x += t * inv_ns;
+                    J.sm_n[w] += 1;
+                }
+                __syncthreads();
+            }
+        }
+    }
+    __syncthreads();
+    for (int i = tid; i < 2 * Ns; i += NT) J.fock[size_t(w) * 2 * Ns + i] = s_fock[i];
+    for (int i = tid; i < 2 * Nmax; i += NT) J.part[size_t(w) * 2 * Nmax + i] = s_part[i];
+    if (tid == 0) {
+        J.rng_next[w] = k;
+        unsigned long long* c = J.counts + size_t(w) * 5;
+        c[0] += c_acc + c_noop + c_rej;
+        c[1] += c_acc;
+        c[2] += c_noop;
+        c[3] += c_rej;
+        c[4] += c_reinv;
+        J.since_reinv[w] = since;
+        J.amp_m[w] = am;
+        J.amp_e[w] = ae;
+        J.status[w] = status;
+    }
+}
+
+// Ratio of moving particle c of flavour fl to site d (one warp, lanes over rows).
+template <typename T>
+__device__ __forceinline__ cx<T> warp_ratio(const DevJob& J, const cx<T>* A, const cx<T>* phase,
+                                            const cx<T>* coef_fl, int N, int c, int d)
+{
+    const int lane = threadIdx.x & 31;
+    cx<T> acc = {T(0), T(0)};
+    for (int f = lane; f < N; f += 32) cmac(acc, A[size_t(f) * N + c], phi_row<T>(phase, coef_fl, J.Nk, J.Nmax, J.L, d, f));
+    return warp_sum(acc);
+}
+
+// StatSpinStruct (StatSpinStruct.cpp:16-135), two flavours: for every pair
+// i <= j, szz +-1/4 and, for antiparallel pairs, s-+ / s+- -= the swap ratio
+// r_up(p_i -> j) r_dn(q_j -> i) (the reference's conj(amp) swamp / w).
+template <typename T, int NT>
+__global__ void __launch_bounds__(NT) k_statspin(DevJob J)
+{
+    const int w = blockIdx.x;
+    if (w >= J.W || J.status[w] != GV_OK) return;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    constexpr int NW = NT / 32;
+    const int Ns = J.Ns, Nmax = J.Nmax;
+    const int16_t* fock = J.fock + size_t(w) * 2 * Ns;
+    const cx<T>* phase = Tab<T>::phase(J);
+    const cx<T>* cg = Tab<T>::coef(J) + size_t(w) * 4 * Ns;
+    extern __shared__ __align__(16) char smem[];
+    cx<T>* coef = reinterpret_cast<cx<T>*>(smem);
+    for (int i = tid; i < 4 * Nmax; i += NT) {
+        const int fl = i / (2 * Nmax), sub = (i / Nmax) & 1, f = i % Nmax;
+        coef[i] = cg[(size_t(fl) * 2 + sub) * Ns + 2 * f];
+    }
+    __syncthreads();
+    const cx<T>* A0 = ai_ptr<T>(J, 0, w);
+    const cx<T>* A1 = ai_ptr<T>(J, 1, w);
+    double* szz = J.ss;
+    double* spm = J.ss + 2 * size_t(Ns) * Ns;
+    double* smp = J.ss + 4 * size_t(Ns) * Ns;
+    for (int idx = warp; idx < Ns * Ns; idx += NW) {
+        const int vi = idx / Ns, vj = idx % Ns;
+        if (vj < vi) continue;
+        const bool ui = fock[vi] >= 0, uj = fock[vj] >= 0;
+        const size_t ij = size_t(vi) * Ns + vj, ji = size_t(vj) * Ns + vi;
+        if (ui == uj) {
+            if (lane == 0) {
+                if (vi == vj) {
+                    atomicAdd(&szz[2 * ij], 0.25);
+                    atomicAdd(ui ? &spm[2 * ij] : &smp[2 * ij], 1.0);
+                } else {
+                    atomicAdd(&szz[2 * ij], 0.25);
+                    atomicAdd(&szz[2 * ji], 0.25);
+                }
+            }
+            continue;
+        }
+        const int upf = ui ? vi : vj, upt = ui ? vj : vi;
+        const cx<T> ru = warp_ratio<T>(J, A0, phase, coef, J.N[0], fock[upf], upt);
+        const cx<T> rd = warp_ratio<T>(J, A1, phase, coef + 2 * Nmax, J.N[1], fock[Ns + upt], upf);
+        if (lane == 0) {
+            const cx<double> r = to_d(ru) * to_d(rd);
+            atomicAdd(&szz[2 * ij], -0.25);
+            atomicAdd(&szz[2 * ji], -0.25);
+            double* a = ui ? smp : spm;   // vi up: s-+[ij], s+-[ji]; vi down: s+-[ij], s-+[ji]
+            double* b = ui ? spm : smp;
+            atomicAdd(&a[2 * ij], -r.x); atomicAdd(&a[2 * ij + 1], -r.y);
+            atomicAdd(&b[2 * ji], -r.x); atomicAdd(&b[2 * ji + 1], -r.y);
+        }
+    }
+    if (tid == 0) atomicAdd(J.ss_n, w == 0 ? 1 : 0);
+}
+
+// VirtUpdate-style ratios for explicit hop sets of one walker.
+template <typename T>
+__global__ void k_virt_update(DevJob J, int w, int nset, const int32_t* hops, double* out)
+{
+    const int lane = threadIdx.x & 31;
+    const int set = blockIdx.x * (blockDim.x / 32) + (threadIdx.x >> 5);
+    if (set >= nset) return;
+    const int Ns = J.Ns;
+    const int16_t* fock = J.fock + size_t(w) * 2 * Ns;
+    const cx<T>* cg = Tab<T>::coef(J) + size_t(w) * 4 * Ns;
+    const cx<T>* phase = Tab<T>::phase(J);
+    cx<double> r = {1.0, 0.0};
+    for (int fl = 0; fl < 2; ++fl) {
+        const int from = hops[4 * set + 2 * fl], to = hops[4 * set + 2 * fl + 1];
+        if (from < 0) continue;
+        const int c = fock[fl * Ns + from];
+        if (c < 0) { r = cx<double>{nan(""), nan("")}; break; }   // no particle of this flavour there
+        const int N = J.N[fl];
+        const cx<T>* A = ai_ptr<T>(J, fl, w);
+        cx<T> acc = {T(0), T(0)};
+        const int sub = sublattice(to, J.L);
+        for (int f = lane; f < N; f += 32)
+            cmac(acc, A[size_t(f) * N + c], cmul_rn(phase[size_t(to) * J.Nk + f], cg[(size_t(fl) * 2 + sub) * Ns + 2 * f]));
+        acc = warp_sum(acc);
+        r = r * to_d(acc);
+    }
+    if (lane == 0) { out[2 * set] = r.x; out[2 * set + 1] = r.y; }
+}
+
+// max |(A A^-1 - I)_{f g}| per walker/flavour in FP64.
+template <typename T, int NT>
+__global__ void __launch_bounds__(NT) k_drift(DevJob J, double* out)
+{
+    const int w = blockIdx.x, fl = blockIdx.y;
+    const int N = J.N[fl], Ns = J.Ns;
+    const int16_t* part = J.part + (size_t(w) * 2 + fl) * J.Nmax;
+    const cx<double>* coef = J.coef64 + (size_t(w) * 2 + fl) * 2 * Ns;
+    const cx<T>* A = ai_ptr<T>(J, fl, w);
+    double mx = 0.0;
+    for (int idx = threadIdx.x; idx < N * N; idx += NT) {
+        const int f = idx / N, g = idx % N;
+        cx<double> s = {0.0, 0.0};
+        for (int pr = 0; pr < N; ++pr) {
+            const int site = part[pr];
+            const cx<double> a = cmul_rn(J.phase64[size_t(site) * J.Nk + f], coef[size_t(sublattice(site, J.L)) * Ns + 2 * f]);
+            cmac(s, a, to_d(A[size_t(g) * N + pr]));
+        }
+        if (f == g) s.x -= 1.0;
+        mx = fmax(mx, fmax(fabs(s.x), fabs(s.y)));
+    }
+    __shared__ double red[NT / 32];
+#pragma unroll
+    for (int o = 16; o; o >>= 1) mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = mx;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double m = 0;
+        for (int q = 0; q < NT / 32; ++q) m = fmax(m, red[q]);
+        out[w * 2 + fl] = m;
+    }
+}
+
+}  // namespace
+}  // namespace gv

@@ -88,7 +88,7 @@ class Job:
     """A batch of independent chains of one wavefunction on the GPU (gv_job)."""
 
     def __init__(self, wav, walkers=1, seed=1234, precision="fp64", reinv_every=0, walker_base=0,
-                 phi_range=None, neel_range=None):
+                 phi_range=None, neel_range=None, deferred_reinversion=False):
         L = _lib.lib()
         cfg = _lib.JobConfig()
         cfg.L = wav.L
@@ -106,6 +106,7 @@ class Job:
         cfg.walker_base = walker_base
         cfg.reinv_every = reinv_every
         cfg.meas_mask = 0
+        cfg.flags = _lib.GV_FLAG_REINV_DEFERRED if deferred_reinversion else 0
         self.cfg = cfg
         self.wav = wav
         self.walkers = walkers

@@ -56,6 +56,10 @@ typedef int32_t gv_status;
 #define GV_PREC_FP64 0        /* plain form: FP64 inverses, FP64 Sherman-Morrison */
 #define GV_PREC_MIXED 1       /* FP32 inverses/updates, FP64 periodic re-inversion */
 
+#define GV_FLAG_REINV_DEFERRED 1  /* re-invert walkers that reached reinv_every accepted
+                                     exchanges at the end of each gv_job_walk call (one
+                                     batched launch) rather than right after the move */
+
 #define GV_MEAS_PROJHEIS 1    /* ProjHeis (ProjHeis.cpp:40-158), Bx = 0 */
 #define GV_MEAS_STAGMAGN 2    /* StagMagnZ (StagMagnZ.cpp:12-43) */
 #define GV_MEAS_STATSPIN 4    /* StatSpinStruct (StatSpinStruct.cpp:16-135) */
@@ -81,7 +85,7 @@ typedef struct {
     uint32_t walker_base;     /* Philox walker id of walker 0 */
     int32_t reinv_every;      /* re-invert after this many accepted exchanges, 0 = never */
     int32_t meas_mask;        /* GV_MEAS_* quantities measured by gv_job_walk when meas > 0 */
-    int32_t flags;            /* reserved, 0 */
+    int32_t flags;            /* GV_FLAG_* */
 } gv_job_config;
 
 /* Per-step record of one walker (parity traces). */

@@ -184,3 +184,16 @@ def _start_config(oracle, L, seed):
     o = oracle.OracleChain(L, PHI, 0.1, seed=seed, walker=2)
     o.random_start()
     return o.config()
+
+
+def test_deferred_reinversion_resets_drift(engine):
+    """GV_FLAG_REINV_DEFERRED: walkers past reinv_every accepted exchanges are
+    re-inverted in one batched launch at the end of the walk call."""
+    L = 8
+    job = engine.Job(engine.StagFluxGroundState(L, PHI, 0.1), walkers=8, seed=4, precision="mixed",
+                     reinv_every=16, deferred_reinversion=True)
+    job.init_walkers()
+    job.walk(L * L * 4, 0)
+    c = job.counts()
+    assert (c[:, 4] >= 1).all() and (c[:, 1] >= 16).all()
+    assert job.drift().max() < 1e-4
