@@ -175,6 +175,8 @@ def run_gpu(g, precision, steps, warmup, rank, clocks_index=None):
         lat.append(t)
     ms, launches = job.timer_stop()
     wall = time.perf_counter() - t0
+    walk_ms, walk_n = job.kernel_ms(0)
+    inv_ms, inv_n = job.kernel_ms(1)
     if clk:
         clk.__exit__()
     job.synchronize()
@@ -182,7 +184,8 @@ def run_gpu(g, precision, steps, warmup, rank, clocks_index=None):
     pj, n = job.projheis()
     e_site = float((pj[:, 0].real / n).mean())
     d = (c1 - c0).astype(float)
-    res = {"ms": ms, "wall_s": wall, "launches": launches, "steps": float(d[0]),
+    res = {"ms": ms, "wall_s": wall, "launches": launches, "steps": float(d[0]), "walk_ms": walk_ms,
+           "walk_launches": walk_n, "inv_ms": inv_ms, "inv_launches": inv_n,
            "p_acc": d[1] / d[0], "p_ap": (d[1] + d[3]) / d[0], "reinv": float(d[4]), "e_site": e_site,
            "clocks": clk.summary() if clk else None}
     job.close()
@@ -214,6 +217,7 @@ def run_e2e(g, precision, steps, rank):
 
 
 def main():
+    global WALKERS
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=20)
@@ -222,6 +226,9 @@ def main():
     ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
     ap.add_argument("--cpu-sweeps", type=int, default=300)
     ap.add_argument("--no-fp64-arm", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline (profiling runs)")
+    ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end leg (profiling runs)")
+    ap.add_argument("--walkers", type=int, default=WALKERS, help="walkers (profiling a smaller case)")
     args = ap.parse_args()
 
     rank = int(os.environ.get("RANK", "0"))
@@ -245,8 +252,9 @@ def main():
         print(json.dumps(out))
         return
 
+    WALKERS = args.walkers
     cpu = None
-    if rank == 0 and world == 1:
+    if rank == 0 and world == 1 and not args.no_cpu:
         cpu = cpu_baseline(os.cpu_count() or 1, args.cpu_sweeps)
 
     dist = None
@@ -276,8 +284,8 @@ def main():
         fp64 = {"value": r64["steps"] / (r64["ms"] * 1e-3), "ms_per_step": r64["ms"] / max(2, args.steps // 4),
                 "e_site_mean": r64["e_site"], "p_acc": r64["p_acc"]}
 
-    e2e = run_e2e(g, args.precision, args.steps, rank)
-    if dist:
+    e2e = run_e2e(g, args.precision, args.steps, rank) if not args.no_e2e else None
+    if dist and e2e:
         import torch
         t = torch.tensor([e2e["wall_s"]], device="cuda")
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
@@ -290,19 +298,23 @@ def main():
     #        p_acc * (2 spins * 3 * N^2 * s) [A^-1 u read, A^-1 read + write]
     N, s = L * L // 2, (8 if args.precision == "mixed" else 16)
     bytes_step = res["p_ap"] * (2 * 2 * N * s) + res["p_acc"] * (2 * 3 * N * N * s)
-    per_launch_steps = res["steps"] / max(1, res["launches"])
-    ms_launch = res["ms"] / max(1, res["launches"])
+    per_launch_steps = res["steps"] / max(1, res["walk_launches"])
+    ms_launch = res["walk_ms"] / max(1, res["walk_launches"])
     achieved = bytes_step * per_launch_steps / (ms_launch * 1e-3) / 1e9
     peak, peak_kind = measured_peaks()
     out = {"metric": METRIC, "value": value, "unit": "steps/s", "n_gpus": world, "steps": args.steps,
            "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
            "vs_baseline": None, "dtype": "f32" if args.precision == "mixed" else "f64", "data": "synthetic",
            "config": workload_config(args.precision),
-           "e2e": {k: e2e[k] for k in ("value", "unit", "h2d_bytes_per_step", "d2h_bytes_per_step", "includes")},
+           "e2e": ({k: e2e[k] for k in ("value", "unit", "h2d_bytes_per_step", "d2h_bytes_per_step", "includes")}
+                   if e2e else None),
            "gpu_launches": int(res["launches"]),
            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                         "frac": achieved / peak, "traffic": None, "peak_kind": peak_kind,
-                        "kernel": "k_walk_gs", "bytes_per_step": bytes_step},
+                        "kernel": "k_walk_gs", "bytes_per_step": bytes_step,
+                        "kernel_ms_per_launch": ms_launch},
+           "kernel_share": {"walk_ms": res["walk_ms"], "reinversion_ms": res["inv_ms"],
+                            "reinversion_launches": res["inv_launches"], "total_ms": res["ms"]},
            "acceptance": {"p_acc": res["p_acc"], "p_ap": res["p_ap"], "reinversions": res["reinv"]},
            "e_site_mean": res["e_site"],
            "clocks": res["clocks"]}

@@ -68,6 +68,7 @@ _SIGS = {
     "gv_job_last_walk_ms": [_P, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_int64)],
     "gv_job_timer_start": [_P],
     "gv_job_timer_stop": [_P, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_int64)],
+    "gv_job_kernel_ms": [_P, ctypes.c_int32, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_int64)],
     "gv_phi_table": [ctypes.c_int32, ctypes.c_double, ctypes.c_double, ctypes.c_double, ctypes.c_void_p,
                      ctypes.c_int32, ctypes.c_void_p],
     "gv_lattice_neighbours": [ctypes.c_int32, ctypes.c_void_p],

@@ -46,6 +46,12 @@ struct gv_job {
     int64_t total_launches = 0;
     int64_t timer_launch0 = 0;
     cudaEvent_t tev0 = nullptr, tev1 = nullptr;
+    // per-launch event pairs while the timer runs: kind 0 walk, 1 re-inversion, 2 measurement
+    bool timing = false;
+    std::vector<cudaEvent_t> ev_pool;
+    std::vector<std::pair<int, int>> ev_used;   // (kind, index of first event of the pair)
+    double kind_ms[3] = {0, 0, 0};
+    int64_t kind_n[3] = {0, 0, 0};
     std::vector<double> wphi, wneel;
     std::vector<uint64_t> start_draws;   // Philox stream-1 uniform index per walker
 };
@@ -86,14 +92,39 @@ int pick_threads(int Nmax) { return Nmax > 128 ? 256 : 128; }
 
 size_t scratch_walkers(const gv_job* j) { return size_t(j->W); }
 
+cudaError_t mark_begin(gv_job* j, int kind, int* slot)
+{
+    *slot = -1;
+    if (!j->timing) return cudaSuccess;
+    const size_t need = 2 * (j->ev_used.size() + 1);
+    while (j->ev_pool.size() < need) {
+        cudaEvent_t e;
+        cudaError_t r = cudaEventCreate(&e);
+        if (r) return r;
+        j->ev_pool.push_back(e);
+    }
+    *slot = int(2 * j->ev_used.size());
+    j->ev_used.push_back({kind, *slot});
+    return cudaEventRecord(j->ev_pool[*slot], j->stream);
+}
+
+cudaError_t mark_end(gv_job* j, int slot)
+{
+    if (slot < 0) return cudaSuccess;
+    return cudaEventRecord(j->ev_pool[slot + 1], j->stream);
+}
+
 template <typename T, int NT>
 gv_status launch_walk(gv_job* j, uint64_t nsteps, uint64_t s0, uint64_t meas, int mask)
 {
     const bool inkernel = !(j->cfg.flags & GV_FLAG_REINV_DEFERRED);
     const WalkLayout lay = walk_layout<T, NT>(j->Ns, j->Nmax, (mask & GV_MEAS_PROJHEIS) != 0, inkernel);
     GV_CK(cudaFuncSetAttribute(k_walk_gs<T, NT>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(lay.total)));
+    int slot;
+    GV_CK(mark_begin(j, 0, &slot));
     k_walk_gs<T, NT><<<j->W, NT, lay.total, j->stream>>>(j->d, nsteps, s0, meas, mask, inkernel ? 1 : 0);
     GV_CK(cudaGetLastError());
+    GV_CK(mark_end(j, slot));
     ++j->last_launches;
     ++j->total_launches;
     return GV_OK;
@@ -112,9 +143,12 @@ gv_status statspin_dispatch(gv_job* j)
 {
     const bool fp64 = j->cfg.precision == GV_PREC_FP64;
     size_t sm = (fp64 ? sizeof(cx<double>) : sizeof(cx<float>)) * 4 * j->Nmax;
+    int slot;
+    GV_CK(mark_begin(j, 2, &slot));
     if (fp64) k_statspin<double, 128><<<j->W, 128, sm, j->stream>>>(j->d);
     else k_statspin<float, 128><<<j->W, 128, sm, j->stream>>>(j->d);
     GV_CK(cudaGetLastError());
+    GV_CK(mark_end(j, slot));
     ++j->last_launches;
     ++j->total_launches;
     return GV_OK;
@@ -125,8 +159,11 @@ gv_status launch_invert(gv_job* j, int only_due)
 {
     size_t sm = gj_smem_bytes(j->Nmax, NT) + 64;
     GV_CK(cudaFuncSetAttribute(k_invert<T, NT>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(sm)));
+    int slot;
+    GV_CK(mark_begin(j, 1, &slot));
     k_invert<T, NT><<<j->W, NT, sm, j->stream>>>(j->d, only_due);
     GV_CK(cudaGetLastError());
+    GV_CK(mark_end(j, slot));
     ++j->total_launches;
     return GV_OK;
 }
@@ -387,6 +424,7 @@ gv_status gv_job_destroy(gv_job* j)
     if (j->stream) cudaStreamSynchronize(j->stream);
     for (void* p : j->allocs) cudaFree(p);
     if (j->ev0) cudaEventDestroy(j->ev0);
+    for (cudaEvent_t e : j->ev_pool) cudaEventDestroy(e);
     if (j->tev0) cudaEventDestroy(j->tev0);
     if (j->tev1) cudaEventDestroy(j->tev1);
     if (j->ev1) cudaEventDestroy(j->ev1);
@@ -535,6 +573,8 @@ gv_status gv_job_timer_start(gv_job* j)
         GV_CK(cudaEventCreate(&j->tev1));
     }
     j->timer_launch0 = j->total_launches;
+    j->timing = true;
+    j->ev_used.clear();
     GV_CK(cudaEventRecord(j->tev0, j->stream));
     return GV_OK;
 }
@@ -548,6 +588,23 @@ gv_status gv_job_timer_stop(gv_job* j, double* ms, int64_t* launches)
     GV_CK(cudaEventElapsedTime(&f, j->tev0, j->tev1));
     if (ms) *ms = f;
     if (launches) *launches = j->total_launches - j->timer_launch0;
+    j->timing = false;
+    for (double& k : j->kind_ms) k = 0.0;
+    for (int64_t& k : j->kind_n) k = 0;
+    for (auto& u : j->ev_used) {
+        float t = 0;
+        GV_CK(cudaEventElapsedTime(&t, j->ev_pool[u.second], j->ev_pool[u.second + 1]));
+        j->kind_ms[u.first] += t;
+        j->kind_n[u.first] += 1;
+    }
+    return GV_OK;
+}
+
+gv_status gv_job_kernel_ms(gv_job* j, int32_t kind, double* ms, int64_t* launches)
+{
+    if (!j || kind < 0 || kind > 2) return GV_ERR_INVALID;
+    if (ms) *ms = j->kind_ms[kind];
+    if (launches) *launches = j->kind_n[kind];
     return GV_OK;
 }
 

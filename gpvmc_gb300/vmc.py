@@ -189,6 +189,12 @@ class Job:
         check(_lib.lib().gv_job_timer_stop(self._h, ctypes.byref(ms), ctypes.byref(n)), "gv_job_timer_stop")
         return ms.value, n.value
 
+    def kernel_ms(self, kind):
+        """(ms, launches) of walk (0), re-inversion (1) or measurement (2) kernels in the last timer window."""
+        ms, n = ctypes.c_double(), ctypes.c_int64()
+        check(_lib.lib().gv_job_kernel_ms(self._h, kind, ctypes.byref(ms), ctypes.byref(n)), "gv_job_kernel_ms")
+        return ms.value, n.value
+
     def last_walk_ms(self):
         ms, n = ctypes.c_double(), ctypes.c_int64()
         check(_lib.lib().gv_job_last_walk_ms(self._h, ctypes.byref(ms), ctypes.byref(n)), "gv_job_last_walk_ms")

@@ -166,6 +166,10 @@ gv_status gv_job_read_statspin(gv_job* job, double* vals, int32_t* nmeas);
  * launch count covers every kernel this job enqueued in between. */
 gv_status gv_job_timer_start(gv_job* job);
 gv_status gv_job_timer_stop(gv_job* job, double* ms, int64_t* launches);
+/* Device time (CUDA events around each launch) spent between the last
+ * timer start/stop in kernels of one kind: 0 Metropolis walk, 1 FP64
+ * (re-)inversion, 2 measurement kernels; with their launch count. */
+gv_status gv_job_kernel_ms(gv_job* job, int32_t kind, double* ms, int64_t* launches);
 
 /* Device-time of the last gv_job_walk in milliseconds (CUDA events on the
  * job's stream) and the number of kernels it launched. */
