@@ -37,15 +37,19 @@ L, WALKERS, SWEEP = 16, 2048, 256
 PHI_RANGE = (0.1 * math.pi, 0.4 * math.pi)
 NEEL_RANGE = (0.0, 0.15)
 REINV = 128
+DRIFT_THRESHOLD = 1e-5
 SEED = 20261203
 
 
-def workload_config(precision):
+def workload_config(precision, policy="drift"):
+    pol = ("FP64 drift check every 128 accepted exchanges, FP64 re-inversion when ||A A^-1 - I||_max > %g"
+           % DRIFT_THRESHOLD) if policy == "drift" else (
+        "FP64 re-inversion every 128 accepted exchanges" if policy == "always" else "no re-inversion")
     return {"workload": "staggered-flux ground state L=16 (128x128 complex per spin), 2048 walkers, "
-                        "phi~U[0.1,0.4)pi, neel~U[0,0.15), ProjHeis every sweep, FP64 re-inversion every "
-                        "128 accepted exchanges",
+                        "phi~U[0.1,0.4)pi, neel~U[0,0.15), ProjHeis every sweep, " + pol,
             "L": L, "walkers": WALKERS, "sweep_steps": SWEEP, "precision": precision,
-            "reinv_every_accepted": REINV, "step": "one sweep of every walker (2048*256 Metropolis steps)",
+            "reinv_every_accepted": REINV, "reinversion_policy": policy,
+            "step": "one sweep of every walker (2048*256 Metropolis steps)",
             "l2": "inputs larger than L2: walker inverses %d MiB" % (WALKERS * 2 * 128 * 128 * (8 if precision == "mixed" else 16) >> 20)}
 
 
@@ -147,17 +151,38 @@ def measured_peaks():
         return 6800.0, "fallback"
 
 
-def make_job(g, precision, rank):
+def make_job(g, precision, rank, policy="drift"):
     wav = g.StagFluxGroundState(L, 0.25 * math.pi, 0.0)
-    job = g.Job(wav, walkers=WALKERS, seed=SEED, precision=precision, reinv_every=REINV,
+    job = g.Job(wav, walkers=WALKERS, seed=SEED, precision=precision, reinv_every=REINV if policy != "none" else 0,
                 walker_base=rank * WALKERS, phi_range=PHI_RANGE, neel_range=NEEL_RANGE,
-                deferred_reinversion=True)
+                deferred_reinversion=True, drift_threshold=DRIFT_THRESHOLD if policy == "drift" else None)
     job.set_measurements(1)
     return job
 
 
-def run_gpu(g, precision, steps, warmup, rank, clocks_index=None):
-    job = make_job(g, precision, rank)
+def delta_e(g, job, rank):
+    """|E/site| difference between the engine's estimator on its own
+    (drifted) inverses and the FP64 engine on fresh FP64 inverses of the
+    same configurations, per walker."""
+    import numpy as np
+    job.reset_quantities()
+    job.measure()
+    pj, n = job.projheis()
+    e_mixed = pj[:, 0].real / np.maximum(n, 1)
+    ref = make_job(g, "fp64", rank, policy="none")
+    ref.init_walkers(job.config())
+    ref.measure()
+    pr, nr = ref.projheis()
+    e_ref = pr[:, 0].real / np.maximum(nr, 1)
+    ref.close()
+    d = np.abs(e_mixed - e_ref)
+    return {"max": float(d.max()), "mean": float(d.mean()), "walkers": int(len(d)),
+            "bar": 1e-5, "within_bar": bool(d.max() <= 1e-5),
+            "note": "same configurations, ProjHeis E/site from the engine's inverses vs fresh FP64 inverses"}
+
+
+def run_gpu(g, precision, steps, warmup, rank, clocks_index=None, policy="drift", check_delta=False):
+    job = make_job(g, precision, rank, policy)
     job.init_walkers()
     for _ in range(warmup):
         job.walk(SWEEP, SWEEP, sync=False)
@@ -177,6 +202,8 @@ def run_gpu(g, precision, steps, warmup, rank, clocks_index=None):
     wall = time.perf_counter() - t0
     walk_ms, walk_n = job.kernel_ms(0)
     inv_ms, inv_n = job.kernel_ms(1)
+    import numpy as np
+    sweep_each = np.array(job.kernel_times(0))
     if clk:
         clk.__exit__()
     job.synchronize()
@@ -184,10 +211,16 @@ def run_gpu(g, precision, steps, warmup, rank, clocks_index=None):
     pj, n = job.projheis()
     e_site = float((pj[:, 0].real / n).mean())
     d = (c1 - c0).astype(float)
+    drift_seen, nchecks = job.drift_checks()
     res = {"ms": ms, "wall_s": wall, "launches": launches, "steps": float(d[0]), "walk_ms": walk_ms,
            "walk_launches": walk_n, "inv_ms": inv_ms, "inv_launches": inv_n,
+           "sweep_p50_ms": float(np.percentile(sweep_each, 50)) if len(sweep_each) else None,
+           "sweep_p99_ms": float(np.percentile(sweep_each, 99)) if len(sweep_each) else None,
+           "checks_without_reinversion": int(nchecks.sum()), "max_drift_at_check": float(drift_seen.max()),
            "p_acc": d[1] / d[0], "p_ap": (d[1] + d[3]) / d[0], "reinv": float(d[4]), "e_site": e_site,
            "clocks": clk.summary() if clk else None}
+    if check_delta:
+        res["delta_e_site"] = delta_e(g, job, rank)
     job.close()
     return res
 
@@ -245,7 +278,7 @@ def main():
         out = {"metric": METRIC, "impl": "reference", "value": v["value"], "unit": "steps/s", "n_gpus": args.gpus,
                "steps": args.steps, "warmup": args.warmup, "higher_is_better": True, "scaling": "weak",
                "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-               "config": workload_config("fp64"),
+               "config": workload_config("fp64", "always"),
                "cpu_baseline": {"value": v["value"], "unit": "steps/s", "cores": v["cores"], "kind": v["kind"],
                                 "sample": v["sample"]},
                "e2e": {"value": v["value"], "unit": "steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
@@ -267,7 +300,8 @@ def main():
 
     if dist:
         dist.barrier()
-    res = run_gpu(g, args.precision, args.steps, args.warmup, rank, clocks_index=local)
+    res = run_gpu(g, args.precision, args.steps, args.warmup, rank, clocks_index=local,
+                  check_delta=(rank == 0 and args.precision == "mixed"))
     ms = res["ms"]
     if dist:
         import torch
@@ -278,11 +312,17 @@ def main():
     total_steps = res["steps"] * world
     value = total_steps / (ms * 1e-3)
 
-    fp64 = None
+    fp64 = always = None
     if rank == 0 and not args.no_fp64_arm and args.precision == "mixed":
-        r64 = run_gpu(g, "fp64", max(2, args.steps // 4), 1, rank)
-        fp64 = {"value": r64["steps"] / (r64["ms"] * 1e-3), "ms_per_step": r64["ms"] / max(2, args.steps // 4),
-                "e_site_mean": r64["e_site"], "p_acc": r64["p_acc"]}
+        k = max(2, args.steps // 4)
+        r64 = run_gpu(g, "fp64", k, args.warmup, rank, policy="none")
+        fp64 = {"value": r64["steps"] / (r64["ms"] * 1e-3), "ms_per_step": r64["ms"] / k,
+                "p_acc": r64["p_acc"], "reinversion_policy": "none (the reference never re-inverts)",
+                "steps": k}
+        ra = run_gpu(g, "mixed", k, args.warmup, rank, policy="always")
+        always = {"value": ra["steps"] / (ra["ms"] * 1e-3), "ms_per_step": ra["ms"] / k,
+                  "walk_ms": ra["walk_ms"], "reinversion_ms": ra["inv_ms"], "reinversions": ra["reinv"],
+                  "reinversion_policy": "FP64 re-inversion every 128 accepted exchanges", "steps": k}
 
     e2e = run_e2e(g, args.precision, args.steps, rank) if not args.no_e2e else None
     if dist and e2e:
@@ -305,7 +345,7 @@ def main():
     out = {"metric": METRIC, "value": value, "unit": "steps/s", "n_gpus": world, "steps": args.steps,
            "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
            "vs_baseline": None, "dtype": "f32" if args.precision == "mixed" else "f64", "data": "synthetic",
-           "config": workload_config(args.precision),
+           "config": workload_config(args.precision, "drift"),
            "e2e": ({k: e2e[k] for k in ("value", "unit", "h2d_bytes_per_step", "d2h_bytes_per_step", "includes")}
                    if e2e else None),
            "gpu_launches": int(res["launches"]),
@@ -315,12 +355,19 @@ def main():
                         "kernel_ms_per_launch": ms_launch},
            "kernel_share": {"walk_ms": res["walk_ms"], "reinversion_ms": res["inv_ms"],
                             "reinversion_launches": res["inv_launches"], "total_ms": res["ms"]},
-           "acceptance": {"p_acc": res["p_acc"], "p_ap": res["p_ap"], "reinversions": res["reinv"]},
+           "acceptance": {"p_acc": res["p_acc"], "p_ap": res["p_ap"], "reinversions": res["reinv"],
+                          "checks_without_reinversion": res["checks_without_reinversion"],
+                          "max_drift_at_check": res["max_drift_at_check"]},
+           "latency": {"sweep_p50_ms": res["sweep_p50_ms"], "sweep_p99_ms": res["sweep_p99_ms"],
+                       "what": "device time of one sweep of all walkers (walk kernel launch)"},
+           "delta_e_site": res.get("delta_e_site"),
            "e_site_mean": res["e_site"],
            "clocks": res["clocks"]}
     if fp64:
         out["fp64_engine"] = fp64
         out["mixed_over_fp64"] = value / world / fp64["value"]
+    if always:
+        out["mixed_reinvert_every_128"] = always
     if cpu:
         out["cpu_baseline"] = {k: cpu[k] for k in ("value", "unit", "cores", "kind", "sample")}
         out["cpu_baseline"]["per_core"] = cpu["per_core"]

@@ -18,6 +18,7 @@ GV_CH_GROUNDSTATE, GV_CH_TRANS = 0, 1
 GV_PREC_FP64, GV_PREC_MIXED = 0, 1
 GV_MEAS_PROJHEIS, GV_MEAS_STAGMAGN, GV_MEAS_STATSPIN = 1, 2, 4
 GV_FLAG_REINV_DEFERRED = 1
+GV_FLAG_REINV_ON_DRIFT = 2
 
 
 class GvError(RuntimeError):
@@ -32,7 +33,8 @@ class JobConfig(ctypes.Structure):
                 ("phase_shift", ctypes.c_double * 2), ("phi_range", ctypes.c_double * 2),
                 ("neel_range", ctypes.c_double * 2), ("n_walkers", ctypes.c_int32),
                 ("precision", ctypes.c_int32), ("seed", ctypes.c_uint64), ("walker_base", ctypes.c_uint32),
-                ("reinv_every", ctypes.c_int32), ("meas_mask", ctypes.c_int32), ("flags", ctypes.c_int32)]
+                ("reinv_every", ctypes.c_int32), ("meas_mask", ctypes.c_int32), ("flags", ctypes.c_int32),
+                ("drift_threshold", ctypes.c_double)]
 
 
 class Trace(ctypes.Structure):
@@ -50,6 +52,9 @@ _SIGS = {
     "gv_job_footprint": [ctypes.POINTER(JobConfig), ctypes.POINTER(ctypes.c_uint64)],
     "gv_job_init_walkers": [_P, ctypes.c_void_p],
     "gv_job_set_meas_mask": [_P, ctypes.c_int32],
+    "gv_job_measure": [_P],
+    "gv_job_reset_quantities": [_P],
+    "gv_job_read_drift_checks": [_P, ctypes.c_void_p, ctypes.c_void_p],
     "gv_job_walk": [_P, ctypes.c_uint64, ctypes.c_uint64],
     "gv_job_walk_traced": [_P, ctypes.c_uint64, ctypes.c_uint64, ctypes.c_int32, ctypes.c_void_p],
     "gv_job_synchronize": [_P],
@@ -69,6 +74,7 @@ _SIGS = {
     "gv_job_timer_start": [_P],
     "gv_job_timer_stop": [_P, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_int64)],
     "gv_job_kernel_ms": [_P, ctypes.c_int32, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_int64)],
+    "gv_job_kernel_times": [_P, ctypes.c_int32, ctypes.c_void_p, ctypes.c_int64, ctypes.POINTER(ctypes.c_int64)],
     "gv_phi_table": [ctypes.c_int32, ctypes.c_double, ctypes.c_double, ctypes.c_double, ctypes.c_void_p,
                      ctypes.c_int32, ctypes.c_void_p],
     "gv_lattice_neighbours": [ctypes.c_int32, ctypes.c_void_p],

@@ -125,7 +125,9 @@ struct DevJob {
     int32_t* amp_e;            // W amplitude base-2 exponent
     uint64_t* rng_next;        // W Metropolis uniform index
     unsigned long long* counts;// W*5
-    int32_t* since_reinv;      // W
+    int32_t* since_reinv;      // W accepted exchanges since the last re-inversion / drift check
+    unsigned long long* checks;// W drift checks that did not need a re-inversion
+    double* drift_seen;        // W largest sampled drift seen at a check
     int32_t* status;           // W
     cx<double>* pj;            // W*2
     int32_t* pj_n;

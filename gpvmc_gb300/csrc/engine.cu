@@ -52,6 +52,7 @@ struct gv_job {
     std::vector<std::pair<int, int>> ev_used;   // (kind, index of first event of the pair)
     double kind_ms[3] = {0, 0, 0};
     int64_t kind_n[3] = {0, 0, 0};
+    std::vector<double> kind_each[3];
     std::vector<double> wphi, wneel;
     std::vector<uint64_t> start_draws;   // Philox stream-1 uniform index per walker
 };
@@ -85,6 +86,9 @@ bool valid_config(const gv_job_config* c)
     if (c->n_walkers < 1 || c->n_walkers > (1 << 20)) return false;
     if (c->precision != GV_PREC_FP64 && c->precision != GV_PREC_MIXED) return false;
     if (c->reinv_every < 0) return false;
+    if (c->flags & ~(GV_FLAG_REINV_DEFERRED | GV_FLAG_REINV_ON_DRIFT)) return false;
+    if ((c->flags & GV_FLAG_REINV_ON_DRIFT) && (!(c->flags & GV_FLAG_REINV_DEFERRED) || !(c->drift_threshold > 0.0)))
+        return false;
     return true;
 }
 
@@ -115,14 +119,18 @@ cudaError_t mark_end(gv_job* j, int slot)
 }
 
 template <typename T, int NT>
-gv_status launch_walk(gv_job* j, uint64_t nsteps, uint64_t s0, uint64_t meas, int mask)
+gv_status launch_walk(gv_job* j, uint64_t nsteps, uint64_t s0, uint64_t meas, int mask, int measure_first)
 {
     const bool inkernel = !(j->cfg.flags & GV_FLAG_REINV_DEFERRED);
     const WalkLayout lay = walk_layout<T, NT>(j->Ns, j->Nmax, (mask & GV_MEAS_PROJHEIS) != 0, inkernel);
     GV_CK(cudaFuncSetAttribute(k_walk_gs<T, NT>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(lay.total)));
+    // shared-memory carveout for 8 resident walkers per SM, the rest stays L1
+    const int carve = int(std::min<size_t>(100, (8 * (lay.total + 1024) * 100 + 233471) / 233472));
+    GV_CK(cudaFuncSetAttribute(k_walk_gs<T, NT>, cudaFuncAttributePreferredSharedMemoryCarveout, carve));
     int slot;
     GV_CK(mark_begin(j, 0, &slot));
-    k_walk_gs<T, NT><<<j->W, NT, lay.total, j->stream>>>(j->d, nsteps, s0, meas, mask, inkernel ? 1 : 0);
+    k_walk_gs<T, NT><<<j->W, NT, lay.total, j->stream>>>(j->d, nsteps, s0, meas, mask, inkernel ? 1 : 0,
+                                                          measure_first);
     GV_CK(cudaGetLastError());
     GV_CK(mark_end(j, slot));
     ++j->last_launches;
@@ -130,13 +138,36 @@ gv_status launch_walk(gv_job* j, uint64_t nsteps, uint64_t s0, uint64_t meas, in
     return GV_OK;
 }
 
-gv_status walk_dispatch(gv_job* j, uint64_t nsteps, uint64_t s0, uint64_t meas, int mask)
+gv_status walk_dispatch(gv_job* j, uint64_t nsteps, uint64_t s0, uint64_t meas, int mask, int measure_first = 0)
 {
     const bool fp64 = j->cfg.precision == GV_PREC_FP64;
-    if (j->nt == 128) return fp64 ? launch_walk<double, 128>(j, nsteps, s0, meas, mask)
-                                  : launch_walk<float, 128>(j, nsteps, s0, meas, mask);
-    return fp64 ? launch_walk<double, 256>(j, nsteps, s0, meas, mask)
-                : launch_walk<float, 256>(j, nsteps, s0, meas, mask);
+    if (j->nt == 128) return fp64 ? launch_walk<double, 128>(j, nsteps, s0, meas, mask, measure_first)
+                                  : launch_walk<float, 128>(j, nsteps, s0, meas, mask, measure_first);
+    return fp64 ? launch_walk<double, 256>(j, nsteps, s0, meas, mask, measure_first)
+                : launch_walk<float, 256>(j, nsteps, s0, meas, mask, measure_first);
+}
+
+template <typename T, int NT>
+gv_status launch_check(gv_job* j, double threshold)
+{
+    const size_t sm = check_smem_bytes(j->Nmax, NT) + 64;
+    GV_CK(cudaFuncSetAttribute(k_check_reinvert<T, NT>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(sm)));
+    int slot;
+    GV_CK(mark_begin(j, 1, &slot));
+    k_check_reinvert<T, NT><<<j->W, NT, sm, j->stream>>>(j->d, threshold);
+    GV_CK(cudaGetLastError());
+    GV_CK(mark_end(j, slot));
+    ++j->last_launches;
+    ++j->total_launches;
+    return GV_OK;
+}
+
+// Deferred cadence: walkers past reinv_every accepted exchanges are checked
+// (GV_FLAG_REINV_ON_DRIFT) or re-inverted outright.
+gv_status deferred_reinversion(gv_job* j)
+{
+    const double thr = (j->cfg.flags & GV_FLAG_REINV_ON_DRIFT) ? j->cfg.drift_threshold : -1.0;
+    return j->cfg.precision == GV_PREC_FP64 ? launch_check<double, 256>(j, thr) : launch_check<float, 256>(j, thr);
 }
 
 gv_status statspin_dispatch(gv_job* j)
@@ -395,6 +426,8 @@ gv_status gv_job_create(const gv_job_config* cfg, gv_job** out)
         (st = dalloc(j, &d.rng_next, size_t(j->W) * sizeof(uint64_t))) ||
         (st = dalloc(j, &d.counts, size_t(j->W) * 5 * sizeof(unsigned long long))) ||
         (st = dalloc(j, &d.since_reinv, size_t(j->W) * sizeof(int32_t))) ||
+        (st = dalloc(j, &d.checks, size_t(j->W) * sizeof(unsigned long long))) ||
+        (st = dalloc(j, &d.drift_seen, size_t(j->W) * sizeof(double))) ||
         (st = dalloc(j, &d.status, size_t(j->W) * sizeof(int32_t))) ||
         (st = dalloc(j, &d.pj, size_t(j->W) * 2 * sizeof(cx<double>))) ||
         (st = dalloc(j, &d.pj_n, size_t(j->W) * sizeof(int32_t))) ||
@@ -450,6 +483,43 @@ gv_status gv_job_set_meas_mask(gv_job* j, int32_t mask)
     return GV_OK;
 }
 
+static gv_status reset_quantities(gv_job* j)
+{
+    GV_CK(cudaMemsetAsync(j->d.pj, 0, sizeof(cx<double>) * 2 * j->W, j->stream));
+    GV_CK(cudaMemsetAsync(j->d.pj_n, 0, sizeof(int32_t) * j->W, j->stream));
+    GV_CK(cudaMemsetAsync(j->d.sm, 0, sizeof(cx<double>) * j->W, j->stream));
+    GV_CK(cudaMemsetAsync(j->d.sm_n, 0, sizeof(int32_t) * j->W, j->stream));
+    GV_CK(cudaMemsetAsync(j->d.ss, 0, sizeof(double) * 10 * j->Ns * j->Ns, j->stream));
+    GV_CK(cudaMemsetAsync(j->d.ss_n, 0, sizeof(int32_t), j->stream));
+    return GV_OK;
+}
+
+gv_status gv_job_reset_quantities(gv_job* j)
+{
+    if (!j) return GV_ERR_INVALID;
+    return reset_quantities(j);
+}
+
+gv_status gv_job_measure(gv_job* j)
+{
+    if (!j) return GV_ERR_INVALID;
+    if (!j->ready) return GV_ERR_NOT_READY;
+    const int mask = j->cfg.meas_mask;
+    gv_status st = GV_OK;
+    if (mask & (GV_MEAS_PROJHEIS | GV_MEAS_STAGMAGN)) st = walk_dispatch(j, 0, 0, 1, mask & ~GV_MEAS_STATSPIN, 1);
+    if (!st && (mask & GV_MEAS_STATSPIN)) st = statspin_dispatch(j);
+    return st ? st : gv_job_synchronize(j);
+}
+
+gv_status gv_job_read_drift_checks(gv_job* j, double* drift, uint64_t* checks)
+{
+    if (!j) return GV_ERR_INVALID;
+    GV_CK(cudaStreamSynchronize(j->stream));
+    if (drift) GV_CK(cudaMemcpy(drift, j->d.drift_seen, sizeof(double) * j->W, cudaMemcpyDeviceToHost));
+    if (checks) GV_CK(cudaMemcpy(checks, j->d.checks, sizeof(uint64_t) * j->W, cudaMemcpyDeviceToHost));
+    return GV_OK;
+}
+
 gv_status gv_job_init_walkers(gv_job* j, const int8_t* up)
 {
     if (!j) return GV_ERR_INVALID;
@@ -472,6 +542,8 @@ gv_status gv_job_init_walkers(gv_job* j, const int8_t* up)
     GV_CK(cudaMemsetAsync(j->d.rng_next, 0, sizeof(uint64_t) * W, j->stream));
     GV_CK(cudaMemsetAsync(j->d.counts, 0, sizeof(unsigned long long) * 5 * W, j->stream));
     GV_CK(cudaMemsetAsync(j->d.since_reinv, 0, sizeof(int32_t) * W, j->stream));
+    GV_CK(cudaMemsetAsync(j->d.checks, 0, sizeof(unsigned long long) * W, j->stream));
+    GV_CK(cudaMemsetAsync(j->d.drift_seen, 0, sizeof(double) * W, j->stream));
     // vmc.cpp:221-241: up to 10 random starts until the amplitude is non-zero.
     for (int attempt = 0; attempt < 10; ++attempt) {
         gv_status st = upload_configs(j, cfg);
@@ -502,12 +574,8 @@ static gv_status walk_impl(gv_job* j, uint64_t len, uint64_t meas, gv_trace* dtr
     j->d.trace_walker = trace_walker;
     j->last_launches = 0;
     if (meas) {
-        GV_CK(cudaMemsetAsync(j->d.pj, 0, sizeof(cx<double>) * 2 * j->W, j->stream));
-        GV_CK(cudaMemsetAsync(j->d.pj_n, 0, sizeof(int32_t) * j->W, j->stream));
-        GV_CK(cudaMemsetAsync(j->d.sm, 0, sizeof(cx<double>) * j->W, j->stream));
-        GV_CK(cudaMemsetAsync(j->d.sm_n, 0, sizeof(int32_t) * j->W, j->stream));
-        GV_CK(cudaMemsetAsync(j->d.ss, 0, sizeof(double) * 10 * j->Ns * j->Ns, j->stream));
-        GV_CK(cudaMemsetAsync(j->d.ss_n, 0, sizeof(int32_t), j->stream));
+        gv_status rs = reset_quantities(j);
+        if (rs) return rs;
     }
     GV_CK(cudaEventRecord(j->ev0, j->stream));
     gv_status st = GV_OK;
@@ -528,7 +596,7 @@ static gv_status walk_impl(gv_job* j, uint64_t len, uint64_t meas, gv_trace* dtr
         }
         j->d.trace = dtrace;
     }
-    if (!st && (j->cfg.flags & GV_FLAG_REINV_DEFERRED) && j->cfg.reinv_every > 0) st = invert_all(j, 1);
+    if (!st && (j->cfg.flags & GV_FLAG_REINV_DEFERRED) && j->cfg.reinv_every > 0) st = deferred_reinversion(j);
     GV_CK(cudaEventRecord(j->ev1, j->stream));
     j->d.trace = nullptr;
     j->d.trace_walker = -1;
@@ -589,13 +657,13 @@ gv_status gv_job_timer_stop(gv_job* j, double* ms, int64_t* launches)
     if (ms) *ms = f;
     if (launches) *launches = j->total_launches - j->timer_launch0;
     j->timing = false;
-    for (double& k : j->kind_ms) k = 0.0;
-    for (int64_t& k : j->kind_n) k = 0;
+    for (int q = 0; q < 3; ++q) { j->kind_ms[q] = 0.0; j->kind_n[q] = 0; j->kind_each[q].clear(); }
     for (auto& u : j->ev_used) {
         float t = 0;
         GV_CK(cudaEventElapsedTime(&t, j->ev_pool[u.second], j->ev_pool[u.second + 1]));
         j->kind_ms[u.first] += t;
         j->kind_n[u.first] += 1;
+        j->kind_each[u.first].push_back(t);
     }
     return GV_OK;
 }
@@ -605,6 +673,16 @@ gv_status gv_job_kernel_ms(gv_job* j, int32_t kind, double* ms, int64_t* launche
     if (!j || kind < 0 || kind > 2) return GV_ERR_INVALID;
     if (ms) *ms = j->kind_ms[kind];
     if (launches) *launches = j->kind_n[kind];
+    return GV_OK;
+}
+
+gv_status gv_job_kernel_times(gv_job* j, int32_t kind, double* out, int64_t capacity, int64_t* n)
+{
+    if (!j || kind < 0 || kind > 2 || (capacity > 0 && !out)) return GV_ERR_INVALID;
+    const auto& v = j->kind_each[kind];
+    const int64_t m = std::min<int64_t>(capacity, int64_t(v.size()));
+    for (int64_t i = 0; i < m; ++i) out[i] = v[i];
+    if (n) *n = int64_t(v.size());
     return GV_OK;
 }
 

@@ -309,9 +309,121 @@ __device__ __forceinline__ void col_update(cx<T>* A, int N, int p, cx<T> w, cons
     }
 }
 
+// Pointers a walk CTA keeps for its walker (shared-memory copies and its
+// inverses), passed to the measurement code.
+template <typename T>
+struct WalkCtx {
+    const DevJob* J;
+    int w, Ns, Nmax, L, Nk, N0, N1;
+    int16_t* s_fock;
+    int16_t* s_part;
+    int16_t* s_nbr;
+    cx<T>* s_coef;
+    cx<T>* s_rq;
+    double* s_redm;
+    const cx<T>* phase;
+    cx<T>* A0;
+    cx<T>* A1;
+};
+
+// ProjHeis and StagMagnZ of the walker's current configuration, added to
+// its accumulators (Quantity::measure, Quantity.cpp:24-27).
+template <typename T, int NT>
+__device__ void measure_now(const WalkCtx<T>& C, int mask)
+{
+    constexpr int NW = NT / 32;
+    const DevJob& J = *C.J;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int w = C.w, Ns = C.Ns, Nmax = C.Nmax, L = C.L, Nk = C.Nk, N0 = C.N0, N1 = C.N1;
+    int16_t* s_fock = C.s_fock;
+    int16_t* s_part = C.s_part;
+    int16_t* s_nbr = C.s_nbr;
+    cx<T>* s_coef = C.s_coef;
+    cx<T>* s_rq = C.s_rq;
+    double* s_redm = C.s_redm;
+    const cx<T>* phase = C.phase;
+    const cx<T>* A0 = C.A0;
+    const cx<T>* A1 = C.A1;
+    const double inv_ns = 1.0 / double(Ns);
+    if (mask & GV_MEAS_PROJHEIS) {
+        // ProjHeis (ProjHeis.cpp:40-158): pass 1, every particle computes the ratio of
+        // moving it to each antiparallel neighbour into rq[site][slot] (a site holds
+        // one particle); pass 2 walks the edges in creation order and pairs the two
+        // flavours' ratios of each antiparallel bond.
+        for (int idx = tid; idx < N0 + N1; idx += NT) {
+            const int fl = idx < N0 ? 0 : 1;
+            const int p = fl ? idx - N0 : idx;
+            const int N = fl ? N1 : N0;
+            const cx<T>* A = fl ? A1 : A0;
+            const cx<T>* cf = s_coef + fl * 2 * Nmax;
+            const int site = s_part[fl * Nmax + p];
+            int js[4];
+            bool anti[4];
+#pragma unroll
+            for (int kk = 0; kk < 4; ++kk) {
+                js[kk] = s_nbr[site * 4 + kk];
+                anti[kk] = (s_fock[js[kk]] >= 0) != (fl == 0);
+            }
+            cx<T> acc[4] = {{T(0), T(0)}, {T(0), T(0)}, {T(0), T(0)}, {T(0), T(0)}};
+            for (int f = 0; f < N; ++f) {
+                const cx<T> a = A[size_t(f) * N + p];
+#pragma unroll
+                for (int kk = 0; kk < 4; ++kk)
+                    if (anti[kk]) cmac(acc[kk], a, phi_row<T>(phase, cf, Nk, Nmax, L, js[kk], f));
+            }
+#pragma unroll
+            for (int kk = 0; kk < 4; ++kk) s_rq[site * 4 + kk] = acc[kk];
+        }
+        __syncthreads();
+        cx<double> e = {0.0, 0.0};
+        for (int ed = tid; ed < 2 * Ns; ed += NT) {
+            const int4 E = J.edges[ed];   // (i, j, slot of j at i, slot of i at j)
+            const bool ui = s_fock[E.x] >= 0, uj = s_fock[E.y] >= 0;
+            if (ui == uj) { e.x += 0.25; continue; }
+            const cx<double> r = to_d(s_rq[E.x * 4 + E.z]) * to_d(s_rq[E.y * 4 + E.w]);
+            e.x += -0.25 - 0.5 * r.x;
+            e.y += -0.5 * r.y;
+        }
+#pragma unroll
+        for (int o = 16; o; o >>= 1) {
+            e.x += __shfl_xor_sync(0xffffffffu, e.x, o);
+            e.y += __shfl_xor_sync(0xffffffffu, e.y, o);
+        }
+        if (lane == 0) { s_redm[warp * 4] = e.x; s_redm[warp * 4 + 1] = e.y; }
+        __syncthreads();
+        if (tid == 0) {
+            double ex = 0, ey = 0;
+            for (int q = 0; q < NW; ++q) { ex += s_redm[q * 4]; ey += s_redm[q * 4 + 1]; }
+            J.pj[size_t(w) * 2].x += ex * inv_ns;
+            J.pj[size_t(w) * 2].y += ey * inv_ns;
+            J.pj[size_t(w) * 2 + 1].x += 1.0;
+            J.pj_n[w] += 1;
+        }
+        __syncthreads();
+    }
+    if (mask & GV_MEAS_STAGMAGN) {   // StagMagnZ (StagMagnZ.cpp:12-43)
+        int m = 0;
+        for (int v = tid; v < Ns; v += NT) {
+            const int sg = (((v % L) + (v / L)) & 1) ? -1 : 1;
+            m += sg * (s_fock[v] >= 0 ? 1 : -1);
+        }
+#pragma unroll
+        for (int o = 16; o; o >>= 1) m += __shfl_xor_sync(0xffffffffu, m, o);
+        if (lane == 0) s_redm[warp * 4 + 2] = double(m);
+        __syncthreads();
+        if (tid == 0) {
+            double t = 0;
+            for (int q = 0; q < NW; ++q) t += s_redm[q * 4 + 2];
+            J.sm[w].x += t * inv_ns;
+            J.sm_n[w] += 1;
+        }
+        __syncthreads();
+    }
+}
+
 template <typename T, int NT>
 __global__ void __launch_bounds__(NT) k_walk_gs(DevJob J, uint64_t nsteps, uint64_t s0, uint64_t meas, int mask,
-                                                int inkernel_reinv)
+                                                int inkernel_reinv, int measure_first)
 {
     extern __shared__ __align__(16) char smem[];
     constexpr int NW = NT / 32;
@@ -329,7 +441,6 @@ __global__ void __launch_bounds__(NT) k_walk_gs(DevJob J, uint64_t nsteps, uint6
     cx<T>* s_row = reinterpret_cast<cx<T>*>(smem + lay.row);
     cx<T>* s_rr = reinterpret_cast<cx<T>*>(smem + lay.rr);
     double* s_red = reinterpret_cast<double*>(smem + lay.red);
-    double* s_redm = s_red + 2 * NW * 4;
     cx<T>* s_rq = reinterpret_cast<cx<T>*>(smem + lay.rdn);
 
     for (int i = tid; i < 2 * Ns; i += NT) s_fock[i] = J.fock[size_t(w) * 2 * Ns + i];
@@ -355,7 +466,9 @@ __global__ void __launch_bounds__(NT) k_walk_gs(DevJob J, uint64_t nsteps, uint6
     int ae = J.amp_e[w];
     int status = GV_OK;
     int rbuf = 0;
-    const double inv_ns = 1.0 / double(Ns);
+    const WalkCtx<T> C = {&J, w, Ns, Nmax, L, Nk, N0, N1, s_fock, s_part, s_nbr, s_coef, s_rq, s_red + 2 * NW * 4,
+                          phase, A0, A1};
+    if (measure_first && mask) measure_now<T, NT>(C, mask);
 
     for (uint64_t s = 0; s < nsteps; ++s, k += 4) {
         uint32_t x[4], y[4];
@@ -456,82 +569,8 @@ __global__ void __launch_bounds__(NT) k_walk_gs(DevJob J, uint64_t nsteps, uint6
             J.trace[s] = t;
         }
         const uint64_t gs = s0 + s;
-        if (meas && (meas == 1 || gs % meas == 0) && mask) {
-            if (mask & GV_MEAS_PROJHEIS) {
-                // ProjHeis (ProjHeis.cpp:40-158): pass 1, every particle computes the ratio of
-                // moving it to each antiparallel neighbour into rq[site][slot] (a site holds
-                // one particle); pass 2 walks the edges in creation order and pairs the two
-                // flavours' ratios of each antiparallel bond.
-                for (int idx = tid; idx < N0 + N1; idx += NT) {
-                    const int fl = idx < N0 ? 0 : 1;
-                    const int p = fl ? idx - N0 : idx;
-                    const int N = fl ? N1 : N0;
-                    const cx<T>* A = fl ? A1 : A0;
-                    const cx<T>* cf = s_coef + fl * 2 * Nmax;
-                    const int site = s_part[fl * Nmax + p];
-                    int js[4];
-                    bool anti[4];
-#pragma unroll
-                    for (int kk = 0; kk < 4; ++kk) {
-                        js[kk] = s_nbr[site * 4 + kk];
-                        anti[kk] = (s_fock[js[kk]] >= 0) != (fl == 0);
-                    }
-                    cx<T> acc[4] = {{T(0), T(0)}, {T(0), T(0)}, {T(0), T(0)}, {T(0), T(0)}};
-                    for (int f = 0; f < N; ++f) {
-                        const cx<T> a = A[size_t(f) * N + p];
-#pragma unroll
-                        for (int kk = 0; kk < 4; ++kk)
-                            if (anti[kk]) cmac(acc[kk], a, phi_row<T>(phase, cf, Nk, Nmax, L, js[kk], f));
-                    }
-#pragma unroll
-                    for (int kk = 0; kk < 4; ++kk) s_rq[site * 4 + kk] = acc[kk];
-                }
-                __syncthreads();
-                cx<double> e = {0.0, 0.0};
-                for (int ed = tid; ed < 2 * Ns; ed += NT) {
-                    const int4 E = J.edges[ed];   // (i, j, slot of j at i, slot of i at j)
-                    const bool ui = s_fock[E.x] >= 0, uj = s_fock[E.y] >= 0;
-                    if (ui == uj) { e.x += 0.25; continue; }
-                    const cx<double> r = to_d(s_rq[E.x * 4 + E.z]) * to_d(s_rq[E.y * 4 + E.w]);
-                    e.x += -0.25 - 0.5 * r.x;
-                    e.y += -0.5 * r.y;
-                }
-#pragma unroll
-                for (int o = 16; o; o >>= 1) {
-                    e.x += __shfl_xor_sync(0xffffffffu, e.x, o);
-                    e.y += __shfl_xor_sync(0xffffffffu, e.y, o);
-                }
-                if (lane == 0) { s_redm[warp * 4] = e.x; s_redm[warp * 4 + 1] = e.y; }
-                __syncthreads();
-                if (tid == 0) {
-                    double ex = 0, ey = 0;
-                    for (int q = 0; q < NW; ++q) { ex += s_redm[q * 4]; ey += s_redm[q * 4 + 1]; }
-                    J.pj[size_t(w) * 2].x += ex * inv_ns;
-                    J.pj[size_t(w) * 2].y += ey * inv_ns;
-                    J.pj[size_t(w) * 2 + 1].x += 1.0;
-                    J.pj_n[w] += 1;
-                }
-                __syncthreads();
-            }
-            if (mask & GV_MEAS_STAGMAGN) {   // StagMagnZ (StagMagnZ.cpp:12-43)
-                int m = 0;
-                for (int v = tid; v < Ns; v += NT) {
-                    const int sg = (((v % L) + (v / L)) & 1) ? -1 : 1;
-                    m += sg * (s_fock[v] >= 0 ? 1 : -1);
-                }
-#pragma unroll
-                for (int o = 16; o; o >>= 1) m += __shfl_xor_sync(0xffffffffu, m, o);
-                if (lane == 0) s_redm[warp * 4 + 2] = double(m);
-                __syncthreads();
-                if (tid == 0) {
-                    double t = 0;
-                    for (int q = 0; q < NW; ++q) t += s_redm[q * 4 + 2];
-                    J.sm[w].x += t * inv_ns;
-                    J.sm_n[w] += 1;
-                }
-                __syncthreads();
-            }
-        }
+        if (meas && (meas == 1 || gs % meas == 0) && mask)
+            measure_now<T, NT>(C, mask);
     }
     __syncthreads();
     for (int i = tid; i < 2 * Ns; i += NT) J.fock[size_t(w) * 2 * Ns + i] = s_fock[i];
@@ -619,6 +658,90 @@ __global__ void __launch_bounds__(NT) k_statspin(DevJob J)
         }
     }
     if (tid == 0) atomicAdd(J.ss_n, w == 0 ? 1 : 0);
+}
+
+// Drift-checked re-inversion (deferred policy).  For every walker whose
+// accepted-exchange count since the last check reached reinv_every, estimate
+// ||A A^-1 - I||_max in FP64 on 8 rows f of the residual (rows rotate from
+// check to check): (A A^-1)(f, g) = sum_p phi_{2f}(x_p) (A^-1)(p, g), with A
+// rebuilt in FP64 from the orbital tables.  Walkers above the threshold (or
+// all of them when threshold < 0) get the FP64 Gauss-Jordan re-inversion.
+template <typename T, int NT>
+__global__ void __launch_bounds__(NT) k_check_reinvert(DevJob J, double threshold)
+{
+    extern __shared__ __align__(16) char smem[];
+    constexpr int NR = 8;
+    constexpr int NW = NT / 32;
+    const int w = blockIdx.x;
+    if (w >= J.W || J.status[w] != GV_OK || J.reinv_every <= 0 || J.since_reinv[w] < J.reinv_every) return;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int Nmax = J.Nmax, Ns = J.Ns;
+    cx<double>* arow = reinterpret_cast<cx<double>*>(smem);             // NR * Nmax
+    double* red = reinterpret_cast<double*>(arow + NR * Nmax);          // NW
+    char* gp = reinterpret_cast<char*>(red + NW + 2);
+    gp = reinterpret_cast<char*>((reinterpret_cast<uintptr_t>(gp) + 15) & ~uintptr_t(15));
+    double drift = 0.0;
+    if (threshold >= 0.0) {
+        const unsigned long long nchk = J.counts[size_t(w) * 5 + 4] + J.checks[w];
+        for (int fl = 0; fl < 2; ++fl) {
+            const int N = J.N[fl];
+            const int16_t* part = J.part + (size_t(w) * 2 + fl) * Nmax;
+            const cx<double>* coef = J.coef64 + (size_t(w) * 2 + fl) * 2 * Ns;
+            const cx<T>* A = ai_ptr<T>(J, fl, w);
+            int rows[NR];
+#pragma unroll
+            for (int i = 0; i < NR; ++i) rows[i] = int((nchk * NR + size_t(i) * (N / NR) + i) % N);
+            for (int idx = tid; idx < NR * N; idx += NT) {
+                const int i = idx / N, p = idx % N;
+                const int site = part[p];
+                arow[i * Nmax + p] = cmul_rn(J.phase64[size_t(site) * J.Nk + rows[i]],
+                                             coef[size_t(sublattice(site, J.L)) * Ns + 2 * rows[i]]);
+            }
+            __syncthreads();
+            for (int g = warp; g < N; g += NW) {
+                cx<double> acc[NR];
+#pragma unroll
+                for (int i = 0; i < NR; ++i) acc[i] = {0.0, 0.0};
+                for (int p = lane; p < N; p += 32) {
+                    const cx<double> x = to_d(A[size_t(g) * N + p]);
+#pragma unroll
+                    for (int i = 0; i < NR; ++i) cmac(acc[i], arow[i * Nmax + p], x);
+                }
+#pragma unroll
+                for (int i = 0; i < NR; ++i) {
+                    cx<double> v = warp_sum(acc[i]);
+                    if (rows[i] == g) v.x -= 1.0;
+                    drift = fmax(drift, fmax(fabs(v.x), fabs(v.y)));
+                }
+            }
+            __syncthreads();
+        }
+#pragma unroll
+        for (int o = 16; o; o >>= 1) drift = fmax(drift, __shfl_xor_sync(0xffffffffu, drift, o));
+        if (lane == 0) red[warp] = drift;
+        __syncthreads();
+        drift = 0.0;
+        for (int q = 0; q < NW; ++q) drift = fmax(drift, red[q]);
+        __syncthreads();
+    }
+    const bool redo = threshold < 0.0 || drift > threshold;
+    if (redo) {
+        GJSmem S = carve_gj<NT>(gp, Nmax);
+        cx<double>* M = J.scratch64 + size_t(w) * Nmax * Nmax;
+        const int st = reinvert_walker<T, NT>(J, w, M, S, nullptr);
+        if (tid == 0) { J.status[w] = st; J.counts[size_t(w) * 5 + 4] += 1; }
+    } else if (tid == 0) {
+        J.checks[w] += 1;
+    }
+    if (tid == 0) {
+        J.since_reinv[w] = 0;
+        J.drift_seen[w] = fmax(J.drift_seen[w], drift);
+    }
+}
+
+__host__ __device__ inline size_t check_smem_bytes(int Nmax, int NT)
+{
+    return sizeof(cx<double>) * 8 * Nmax + sizeof(double) * (NT / 32 + 2) + 16 + gj_smem_bytes(Nmax, NT) + 16;
 }
 
 // VirtUpdate-style ratios for explicit hop sets of one walker.

@@ -88,7 +88,7 @@ class Job:
     """A batch of independent chains of one wavefunction on the GPU (gv_job)."""
 
     def __init__(self, wav, walkers=1, seed=1234, precision="fp64", reinv_every=0, walker_base=0,
-                 phi_range=None, neel_range=None, deferred_reinversion=False):
+                 phi_range=None, neel_range=None, deferred_reinversion=False, drift_threshold=None):
         L = _lib.lib()
         cfg = _lib.JobConfig()
         cfg.L = wav.L
@@ -106,7 +106,10 @@ class Job:
         cfg.walker_base = walker_base
         cfg.reinv_every = reinv_every
         cfg.meas_mask = 0
-        cfg.flags = _lib.GV_FLAG_REINV_DEFERRED if deferred_reinversion else 0
+        cfg.flags = _lib.GV_FLAG_REINV_DEFERRED if (deferred_reinversion or drift_threshold) else 0
+        if drift_threshold:
+            cfg.flags |= _lib.GV_FLAG_REINV_ON_DRIFT
+            cfg.drift_threshold = drift_threshold
         self.cfg = cfg
         self.wav = wav
         self.walkers = walkers
@@ -164,6 +167,19 @@ class Job:
                                                          ("ratio", "<f8"), ("u4", "<f8")]))
         return arr[:length].copy()
 
+    def measure(self):
+        """Quantity::measure on the current configurations (no step)."""
+        check(_lib.lib().gv_job_measure(self._h), "gv_job_measure")
+
+    def reset_quantities(self):
+        check(_lib.lib().gv_job_reset_quantities(self._h), "gv_job_reset_quantities")
+
+    def drift_checks(self):
+        d = np.zeros(self.walkers)
+        n = np.zeros(self.walkers, dtype=np.uint64)
+        check(_lib.lib().gv_job_read_drift_checks(self._h, _p(d), _p(n)), "gv_job_read_drift_checks")
+        return d, n
+
     def synchronize(self):
         check(_lib.lib().gv_job_synchronize(self._h), "gv_job_synchronize")
 
@@ -194,6 +210,13 @@ class Job:
         ms, n = ctypes.c_double(), ctypes.c_int64()
         check(_lib.lib().gv_job_kernel_ms(self._h, kind, ctypes.byref(ms), ctypes.byref(n)), "gv_job_kernel_ms")
         return ms.value, n.value
+
+    def kernel_times(self, kind):
+        n = ctypes.c_int64()
+        check(_lib.lib().gv_job_kernel_times(self._h, kind, None, 0, ctypes.byref(n)), "gv_job_kernel_times")
+        out = np.zeros(n.value)
+        check(_lib.lib().gv_job_kernel_times(self._h, kind, _p(out), n.value, ctypes.byref(n)), "gv_job_kernel_times")
+        return out
 
     def last_walk_ms(self):
         ms, n = ctypes.c_double(), ctypes.c_int64()

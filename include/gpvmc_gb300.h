@@ -59,6 +59,9 @@ typedef int32_t gv_status;
 #define GV_FLAG_REINV_DEFERRED 1  /* re-invert walkers that reached reinv_every accepted
                                      exchanges at the end of each gv_job_walk call (one
                                      batched launch) rather than right after the move */
+#define GV_FLAG_REINV_ON_DRIFT 2  /* with GV_FLAG_REINV_DEFERRED: at that point check the
+                                     FP64 sampled drift ||A A^-1 - I||_max and re-invert
+                                     only when it exceeds drift_threshold */
 
 #define GV_MEAS_PROJHEIS 1    /* ProjHeis (ProjHeis.cpp:40-158), Bx = 0 */
 #define GV_MEAS_STAGMAGN 2    /* StagMagnZ (StagMagnZ.cpp:12-43) */
@@ -86,6 +89,7 @@ typedef struct {
     int32_t reinv_every;      /* re-invert after this many accepted exchanges, 0 = never */
     int32_t meas_mask;        /* GV_MEAS_* quantities measured by gv_job_walk when meas > 0 */
     int32_t flags;            /* GV_FLAG_* */
+    double drift_threshold;   /* GV_FLAG_REINV_ON_DRIFT threshold (e.g. 1e-5) */
 } gv_job_config;
 
 /* Per-step record of one walker (parity traces). */
@@ -109,6 +113,15 @@ gv_status gv_job_footprint(const gv_job_config* cfg, uint64_t* bytes);
 /* Select the quantities measured by later gv_job_walk calls (MetroMC::AddQuantity,
  * MetroMC.h:31). */
 gv_status gv_job_set_meas_mask(gv_job* job, int32_t meas_mask);
+
+/* Quantity::measure on every walker's current configuration, without a
+ * step, added to the sums (Quantity.cpp:24-27); gv_job_reset_quantities is
+ * Quantity::init (Quantity.cpp:19-22). */
+gv_status gv_job_measure(gv_job* job);
+gv_status gv_job_reset_quantities(gv_job* job);
+/* Largest sampled FP64 drift seen at a drift check, per walker, and the
+ * number of checks that needed no re-inversion. */
+gv_status gv_job_read_drift_checks(gv_job* job, double* drift_seen, uint64_t* checks_without_reinversion);
 
 /* Start configurations.  up: n_walkers x Ns bytes, 1 where flavour 0 sits
  * (LatticeState::FockInit), or NULL for the reference's random start with up
@@ -170,6 +183,8 @@ gv_status gv_job_timer_stop(gv_job* job, double* ms, int64_t* launches);
  * timer start/stop in kernels of one kind: 0 Metropolis walk, 1 FP64
  * (re-)inversion, 2 measurement kernels; with their launch count. */
 gv_status gv_job_kernel_ms(gv_job* job, int32_t kind, double* ms, int64_t* launches);
+/* The individual launch durations behind gv_job_kernel_ms (up to capacity). */
+gv_status gv_job_kernel_times(gv_job* job, int32_t kind, double* out, int64_t capacity, int64_t* n);
 
 /* Device-time of the last gv_job_walk in milliseconds (CUDA events on the
  * job's stream) and the number of kernels it launched. */

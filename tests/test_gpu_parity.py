@@ -197,3 +197,40 @@ def test_deferred_reinversion_resets_drift(engine):
     c = job.counts()
     assert (c[:, 4] >= 1).all() and (c[:, 1] >= 16).all()
     assert job.drift().max() < 1e-4
+
+
+def test_measure_without_step_matches_oracle(engine, oracle):
+    """gv_job_measure (Quantity::measure on the current configuration) equals
+    the oracle's ProjHeis/StagMagnZ/StatSpinStruct measure on the same state."""
+    L = 8
+    job, orc = _pair(engine, oracle, L, 0.1, seed=31)
+    job.set_measurements(7)
+    job.init_walkers()
+    orc.random_start()
+    job.walk(500, 0)
+    orc.walk(500)
+    assert (job.config()[0] == orc.config()).all()
+    job.reset_quantities()
+    job.measure()
+    orc.reset_quantities()
+    orc.measure(7)
+    pj, n = job.projheis()
+    opj, on = orc.projheis()
+    assert n[0] == on == 1 and abs(pj[0, 0] - opj[0, 0]) < RTOL * abs(opj[0, 0])
+    assert abs(job.stagmagn()[0][0] - orc.stagmagn()[0]) < 1e-12
+    ss, _ = job.statspin()
+    oss, _ = orc.statspin()
+    assert np.abs(ss - oss).max() < RTOL * np.abs(oss).max()
+
+
+def test_drift_checked_reinversion(engine):
+    L = 8
+    job = engine.Job(engine.StagFluxGroundState(L, PHI, 0.1), walkers=16, seed=8, precision="mixed",
+                     reinv_every=16, drift_threshold=1e-6)
+    job.init_walkers()
+    for _ in range(6):
+        job.walk(L * L, 0)
+    drift, checks = job.drift_checks()
+    c = job.counts()
+    assert (c[:, 4] + checks).min() >= 1          # every walker was checked at least once
+    assert job.drift().max() < 1e-3
