@@ -422,7 +422,7 @@ __device__ void measure_now(const WalkCtx<T>& C, int mask)
 }
 
 template <typename T, int NT>
-__global__ void __launch_bounds__(NT) k_walk_gs(DevJob J, uint64_t nsteps, uint64_t s0, uint64_t meas, int mask,
+__global__ void __launch_bounds__(NT, 768 / NT) k_walk_gs(DevJob J, uint64_t nsteps, uint64_t s0, uint64_t meas, int mask,
                                                 int inkernel_reinv, int measure_first)
 {
     extern __shared__ __align__(16) char smem[];
