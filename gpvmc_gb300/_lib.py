@@ -12,7 +12,7 @@ LIB_PATH = os.path.join(HERE, "_lib", "libgpvmc_gb300.so")
 
 GV_OK = 0
 STATUS_NAMES = {0: "ok", 1: "invalid", 2: "singular", 3: "nan", 4: "zero amplitude", 5: "drift",
-                6: "timeout", 7: "out of memory", 8: "cuda error", 9: "not ready"}
+                6: "timeout", 7: "out of memory", 8: "cuda error", 9: "not ready", 10: "too large"}
 
 GV_CH_GROUNDSTATE, GV_CH_TRANS = 0, 1
 GV_PREC_FP64, GV_PREC_MIXED = 0, 1
@@ -55,6 +55,7 @@ _SIGS = {
     "gv_job_measure": [_P],
     "gv_job_reset_quantities": [_P],
     "gv_job_read_drift_checks": [_P, ctypes.c_void_p, ctypes.c_void_p],
+    "gv_slater_invert_noalloc": [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int32, ctypes.c_void_p, ctypes.c_void_p],
     "gv_job_walk": [_P, ctypes.c_uint64, ctypes.c_uint64],
     "gv_job_walk_traced": [_P, ctypes.c_uint64, ctypes.c_uint64, ctypes.c_int32, ctypes.c_void_p],
     "gv_job_synchronize": [_P],

@@ -311,6 +311,7 @@ const char* gv_status_string(gv_status s)
         case GV_ERR_OOM: return "device allocation failed";
         case GV_ERR_CUDA: return "CUDA runtime error";
         case GV_ERR_NOT_READY: return "walkers not initialised";
+        case GV_ERR_TOO_LARGE: return "size exceeds the entry point's fixed limit (gv_slater_invert_noalloc: N <= 128)";
         default: return "unknown status";
     }
 }

@@ -49,6 +49,7 @@ typedef int32_t gv_status;
 #define GV_ERR_OOM 7          /* device allocation failed */
 #define GV_ERR_CUDA 8         /* other CUDA runtime error */
 #define GV_ERR_NOT_READY 9    /* walkers not initialised */
+#define GV_ERR_TOO_LARGE 10   /* size beyond a fixed-size entry point's limit */
 
 #define GV_CH_GROUNDSTATE 0   /* StagFluxGroundState */
 #define GV_CH_TRANS 1         /* StagFluxTransExciton */
@@ -209,6 +210,27 @@ gv_status gv_channel_orbitals(int32_t L, const double* phase_shift, int32_t chan
                               int32_t fl, int32_t* orb, int32_t* N, int32_t* Nexc);
 void gv_philox4x32_10(const uint32_t* ctr, const uint32_t* key, uint32_t* out);
 double gv_uniform_at(uint64_t seed, uint32_t walker, uint32_t stream, uint64_t k);
+
+/* Allocation-free inversion of one Slater matrix, for callers that cannot let
+ * a library allocate device memory (applications that pre-allocate all of
+ * their HBM at start-up and forbid later allocations, or latency-critical
+ * loops where cudaMalloc's implicit synchronisation is not acceptable).  It
+ * has no counterpart in the reference; it performs what linalg::DetInv does
+ * for one matrix, in FP64 on the GPU.
+ *   d_A    device, N x N complex (interleaved re, im) in the reference's
+ *          column-major m_mat layout, A[r*N + f] = A(f, r); not modified
+ *   d_Ai   device output, the inverse in the m_mati layout (N x N complex)
+ *   d_info device output, 4 doubles: det mantissa (re, im), det base-2
+ *          exponent, status (GV_OK or GV_ERR_SINGULAR)
+ *   stream cudaStream_t to enqueue on (NULL: the default stream)
+ * The only working memory is a static device array sized for
+ * N <= GV_NOALLOC_MAX_N (256 KiB, held by every GPU that loads the library
+ * until exit); larger N returns GV_ERR_TOO_LARGE.  The call allocates and
+ * frees nothing.  Its first call on a device looks up that array's device
+ * address (make that first call before any stream capture).  All calls share
+ * the array: calls that overlap on the GPU race and must be serialised. */
+#define GV_NOALLOC_MAX_N 128
+gv_status gv_slater_invert_noalloc(const double* d_A, double* d_Ai, int32_t N, double* d_info, void* stream);
 
 /* Library version string. */
 const char* gv_version(void);
