@@ -38,6 +38,7 @@ PHI_RANGE = (0.1 * math.pi, 0.4 * math.pi)
 NEEL_RANGE = (0.0, 0.15)
 REINV = 128
 DRIFT_THRESHOLD = 1e-5
+THERM_SWEEPS = 16   # untimed thermalisation before the warm-up steps, every GPU arm alike
 SEED = 20261203
 
 
@@ -48,7 +49,7 @@ def workload_config(precision, policy="drift"):
     return {"workload": "staggered-flux ground state L=16 (128x128 complex per spin), 2048 walkers, "
                         "phi~U[0.1,0.4)pi, neel~U[0,0.15), ProjHeis every sweep, " + pol,
             "L": L, "walkers": WALKERS, "sweep_steps": SWEEP, "precision": precision,
-            "reinv_every_accepted": REINV, "reinversion_policy": policy,
+            "reinv_every_accepted": REINV, "reinversion_policy": policy, "thermalisation_sweeps": THERM_SWEEPS,
             "step": "one sweep of every walker (2048*256 Metropolis steps)",
             "l2": "inputs larger than L2: walker inverses %d MiB" % (WALKERS * 2 * 128 * 128 * (8 if precision == "mixed" else 16) >> 20)}
 
@@ -152,9 +153,10 @@ def measured_peaks():
 
 
 def make_job(g, precision, rank, policy="drift"):
+    from gpvmc_gb300.replicas import walker_base
     wav = g.StagFluxGroundState(L, 0.25 * math.pi, 0.0)
     job = g.Job(wav, walkers=WALKERS, seed=SEED, precision=precision, reinv_every=REINV if policy != "none" else 0,
-                walker_base=rank * WALKERS, phi_range=PHI_RANGE, neel_range=NEEL_RANGE,
+                walker_base=walker_base(rank, WALKERS), phi_range=PHI_RANGE, neel_range=NEEL_RANGE,
                 deferred_reinversion=True, drift_threshold=DRIFT_THRESHOLD if policy == "drift" else None)
     job.set_measurements(1)
     return job
@@ -184,6 +186,8 @@ def delta_e(g, job, rank):
 def run_gpu(g, precision, steps, warmup, rank, clocks_index=None, policy="drift", check_delta=False):
     job = make_job(g, precision, rank, policy)
     job.init_walkers()
+    for _ in range(THERM_SWEEPS):
+        job.walk(SWEEP, 0, sync=False)
     for _ in range(warmup):
         job.walk(SWEEP, SWEEP, sync=False)
     job.synchronize()
