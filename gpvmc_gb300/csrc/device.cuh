@@ -87,6 +87,32 @@ __host__ __device__ __forceinline__ double u01(uint32_t a, uint32_t b)
     return (double(m) + 0.5) * (1.0 / 4503599627370496.0);
 }
 
+// 52 random bits of a uniform (the integer m in (m + 1/2) * 2^-52).
+__host__ __device__ __forceinline__ uint64_t u52(uint32_t a, uint32_t b)
+{
+    return ((uint64_t(a) << 20) ^ uint64_t(b >> 12)) & ((uint64_t(1) << 52) - 1);
+}
+
+// floor(double(n) * u) for u = (m + 1/2) 2^-52 and 1 <= n < 2^10, computed in
+// integers with the IEEE double product's round-to-nearest-even, so that it
+// equals the reference's size_t(n * RanGen::uniform()) bit for bit
+// (LatticeStepper.cpp:45) without touching the FP64 pipe.
+__host__ __device__ __forceinline__ int scaled_floor(uint32_t n, uint64_t m)
+{
+    const uint64_t X = uint64_t(n) * (2 * m + 1);   // exact product n (2m+1), < 2^63
+#ifdef __CUDA_ARCH__
+    const int b = 64 - __clzll((long long)X);
+#else
+    const int b = 64 - __builtin_clzll(X);
+#endif
+    if (b <= 53) return int(X >> 53);               // exactly representable
+    const int s = b - 53;
+    uint64_t q = X >> s;
+    const uint64_t r = X & ((uint64_t(1) << s) - 1), half = uint64_t(1) << (s - 1);
+    if (r > half || (r == half && (q & 1))) ++q;    // round half to even
+    return int((q << s) >> 53);
+}
+
 // Stream layout: counter {call_lo, call_hi, walker, stream}, key {seed_lo,
 // seed_hi}; uniform k comes from call k/2 (words 0,1 for even k, 2,3 for odd).
 __host__ __device__ __forceinline__ void philox_call(uint64_t seed, uint32_t walker, uint32_t stream,

@@ -245,6 +245,22 @@ __global__ void __launch_bounds__(NT) k_invert(DevJob J, int only_due)
 //     r_fl = sum_f (A^-1)(c, f) phi_{2f}(d)          (linalg.cpp:297-303 / 146)
 // and on acceptance the Sherman-Morrison update of both inverses
 //     A^-1 <- A^-1 - (A^-1 u - e_c)(e_c^T A^-1) / r  (linalg.cpp:402-573, rc=1).
+// The Metropolis ratio |r_0 r_1|^2 and the accept uniform: the plain form in
+// FP64 exactly as MetroMC::YesNo compares; the mixed form in FP32 (a 24-bit
+// uniform), which keeps the per-step scalar work off the FP64 pipe.
+template <typename T> struct Accept;
+template <> struct Accept<double> {
+    static __device__ __forceinline__ double ratio(cx<double> a, cx<double> b) { return norm2(a * b); }
+    static __device__ __forceinline__ double uniform(uint64_t m) { return (double(m) + 0.5) * (1.0 / 4503599627370496.0); }
+};
+template <> struct Accept<float> {
+    static __device__ __forceinline__ float ratio(cx<float> a, cx<float> b) { return norm2(a) * norm2(b); }
+    static __device__ __forceinline__ float uniform(uint64_t m)
+    {
+        return (float(uint32_t(m >> 28)) + 0.5f) * (1.0f / 16777216.0f);
+    }
+};
+
 struct WalkLayout {
     size_t fock, part, nbr, coef, uu, row, rr, red, rdn, gj, total;
 };
@@ -474,13 +490,16 @@ __global__ void __launch_bounds__(NT, 768 / NT) k_walk_gs(DevJob J, uint64_t nst
         uint32_t x[4], y[4];
         philox_call(J.seed, wid, 0, k >> 1, x);
         philox_call(J.seed, wid, 0, (k >> 1) + 1, y);
-        const double u1 = u01(x[0], x[1]), u2 = u01(x[2], x[3]), u4 = u01(y[2], y[3]);
-        const int v1 = int(double(Ns) * u1);
-        const int v2 = s_nbr[v1 * 4 + int(4.0 * u2)];
+        // u1 -> vertex, u2 -> neighbour slot, u3 unused, u4 -> accept test; the
+        // vertex and slot are computed in integers, bit-identical to
+        // size_t(n * uniform()) (LatticeStepper.cpp:45-47).
+        const uint64_t m4 = u52(y[2], y[3]);
+        const int v1 = scaled_floor(uint32_t(Ns), u52(x[0], x[1]));
+        const int v2 = s_nbr[v1 * 4 + int(u52(x[2], x[3]) >> 50)];
         const int f1 = s_fock[v1] >= 0 ? 0 : 1;
         const int f2 = s_fock[v2] >= 0 ? 0 : 1;
         int kind = 0, accepted;
-        double ratio = 1.0;
+        T ratio = T(1);
         if (f1 == f2) {
             accepted = 1;   // m_weight / m_state_weight = 1, u4 < 1 (MetroMC.cpp:41)
             ++c_noop;
@@ -506,23 +525,23 @@ __global__ void __launch_bounds__(NT, 768 / NT) k_walk_gs(DevJob J, uint64_t nst
             }
             au = warp_sum(au);
             ad = warp_sum(ad);
-            double* rb = s_red + rbuf * NW * 4;
+            T* rb = reinterpret_cast<T*>(s_red) + rbuf * NW * 4;
             rbuf ^= 1;
             if (lane == 0) { rb[warp * 4 + 0] = au.x; rb[warp * 4 + 1] = au.y; rb[warp * 4 + 2] = ad.x; rb[warp * 4 + 3] = ad.y; }
             __syncthreads();
             cx<T> ru = {T(0), T(0)}, rd = {T(0), T(0)};
             for (int q = 0; q < NW; ++q) {
-                ru.x += T(rb[q * 4 + 0]); ru.y += T(rb[q * 4 + 1]);
-                rd.x += T(rb[q * 4 + 2]); rd.y += T(rb[q * 4 + 3]);
+                ru.x += rb[q * 4 + 0]; ru.y += rb[q * 4 + 1];
+                rd.x += rb[q * 4 + 2]; rd.y += rb[q * 4 + 3];
             }
-            const cx<double> q = to_d(ru) * to_d(rd);
-            ratio = norm2(q);
+            ratio = Accept<T>::ratio(ru, rd);
             if (!isfinite(ratio)) { status = GV_ERR_NAN; break; }
-            accepted = ratio > 1.0 ? (u4 < 1.0) : (u4 < ratio);
+            // MetroMC::YesNo (MetroMC.cpp:41): ratio > 1 draws u4 < 1, always true here
+            accepted = ratio > T(1) ? 1 : (Accept<T>::uniform(m4) < ratio);
             if (!accepted) {
                 ++c_rej;
             } else {
-                if (norm2(to_d(ru)) < 1e-9 || norm2(to_d(rd)) < 1e-9) { status = GV_ERR_SINGULAR; break; }
+                if (norm2(ru) < T(1e-9) || norm2(rd) < T(1e-9)) { status = GV_ERR_SINGULAR; break; }
                 const cx<T> iu = cinv(ru), id = cinv(rd);
                 for (int f = tid; f < N0; f += NT) s_rr[f] = s_row[f] * iu;
                 for (int f = tid; f < N1; f += NT) s_rr[Nmax + f] = s_row[Nmax + f] * id;
@@ -544,8 +563,10 @@ __global__ void __launch_bounds__(NT, 768 / NT) k_walk_gs(DevJob J, uint64_t nst
                     s_fock[upt] = int16_t(cu); s_fock[upf] = -1; s_part[cu] = int16_t(upt);
                     s_fock[Ns + dnt] = int16_t(cd); s_fock[Ns + dnf] = -1; s_part[Nmax + cd] = int16_t(dnt);
                 }
-                am = am * q;
-                amp_normalise(am, ae);
+                if (tid == 0) {   // the amplitude lives in thread 0 (FP64, once per accept)
+                    am = am * (to_d(ru) * to_d(rd));
+                    amp_normalise(am, ae);
+                }
                 ++c_acc;
                 ++since;
                 __syncthreads();
@@ -565,7 +586,7 @@ __global__ void __launch_bounds__(NT, 768 / NT) k_walk_gs(DevJob J, uint64_t nst
         if (J.trace && w == J.trace_walker && tid == 0) {
             gv_trace t;
             t.v1 = v1; t.v2 = v2; t.kind = kind; t.accepted = accepted; t.khop = kind ? 0 : -1; t.pad = 0;
-            t.ratio = ratio; t.u4 = u4;
+            t.ratio = double(ratio); t.u4 = u01(y[2], y[3]);
             J.trace[s] = t;
         }
         const uint64_t gs = s0 + s;
