@@ -19,6 +19,7 @@ GV_PREC_FP64, GV_PREC_MIXED = 0, 1
 GV_MEAS_PROJHEIS, GV_MEAS_STAGMAGN, GV_MEAS_STATSPIN = 1, 2, 4
 GV_FLAG_REINV_DEFERRED = 1
 GV_FLAG_REINV_ON_DRIFT = 2
+GV_FLAG_DELAYED_UPDATES = 4
 
 
 class GvError(RuntimeError):

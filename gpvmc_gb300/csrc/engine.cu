@@ -86,7 +86,7 @@ bool valid_config(const gv_job_config* c)
     if (c->n_walkers < 1 || c->n_walkers > (1 << 20)) return false;
     if (c->precision != GV_PREC_FP64 && c->precision != GV_PREC_MIXED) return false;
     if (c->reinv_every < 0) return false;
-    if (c->flags & ~(GV_FLAG_REINV_DEFERRED | GV_FLAG_REINV_ON_DRIFT)) return false;
+    if (c->flags & ~(GV_FLAG_REINV_DEFERRED | GV_FLAG_REINV_ON_DRIFT | GV_FLAG_DELAYED_UPDATES)) return false;
     if ((c->flags & GV_FLAG_REINV_ON_DRIFT) && (!(c->flags & GV_FLAG_REINV_DEFERRED) || !(c->drift_threshold > 0.0)))
         return false;
     return true;
@@ -118,19 +118,19 @@ cudaError_t mark_end(gv_job* j, int slot)
     return cudaEventRecord(j->ev_pool[slot + 1], j->stream);
 }
 
-template <typename T, int NT>
+template <typename T, int NT, int KD>
 gv_status launch_walk(gv_job* j, uint64_t nsteps, uint64_t s0, uint64_t meas, int mask, int measure_first)
 {
     const bool inkernel = !(j->cfg.flags & GV_FLAG_REINV_DEFERRED);
-    const WalkLayout lay = walk_layout<T, NT>(j->Ns, j->Nmax, (mask & GV_MEAS_PROJHEIS) != 0, inkernel);
-    GV_CK(cudaFuncSetAttribute(k_walk_gs<T, NT>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(lay.total)));
-    // shared-memory carveout for 8 resident walkers per SM, the rest stays L1
+    const WalkLayout lay = walk_layout<T, NT, KD>(j->Ns, j->Nmax, (mask & GV_MEAS_PROJHEIS) != 0, inkernel);
+    GV_CK(cudaFuncSetAttribute(k_walk_gs<T, NT, KD>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(lay.total)));
+    // shared-memory carveout for up to 8 resident walkers per SM, the rest stays L1
     const int carve = int(std::min<size_t>(100, (8 * (lay.total + 1024) * 100 + 233471) / 233472));
-    GV_CK(cudaFuncSetAttribute(k_walk_gs<T, NT>, cudaFuncAttributePreferredSharedMemoryCarveout, carve));
+    GV_CK(cudaFuncSetAttribute(k_walk_gs<T, NT, KD>, cudaFuncAttributePreferredSharedMemoryCarveout, carve));
     int slot;
     GV_CK(mark_begin(j, 0, &slot));
-    k_walk_gs<T, NT><<<j->W, NT, lay.total, j->stream>>>(j->d, nsteps, s0, meas, mask, inkernel ? 1 : 0,
-                                                          measure_first);
+    k_walk_gs<T, NT, KD><<<j->W, NT, lay.total, j->stream>>>(j->d, nsteps, s0, meas, mask, inkernel ? 1 : 0,
+                                                              measure_first);
     GV_CK(cudaGetLastError());
     GV_CK(mark_end(j, slot));
     ++j->last_launches;
@@ -138,13 +138,22 @@ gv_status launch_walk(gv_job* j, uint64_t nsteps, uint64_t s0, uint64_t meas, in
     return GV_OK;
 }
 
+// Delayed updates (depth 8) when requested and every particle column has its
+// own thread; otherwise immediate rank-1 updates.
 gv_status walk_dispatch(gv_job* j, uint64_t nsteps, uint64_t s0, uint64_t meas, int mask, int measure_first = 0)
 {
     const bool fp64 = j->cfg.precision == GV_PREC_FP64;
-    if (j->nt == 128) return fp64 ? launch_walk<double, 128>(j, nsteps, s0, meas, mask, measure_first)
-                                  : launch_walk<float, 128>(j, nsteps, s0, meas, mask, measure_first);
-    return fp64 ? launch_walk<double, 256>(j, nsteps, s0, meas, mask, measure_first)
-                : launch_walk<float, 256>(j, nsteps, s0, meas, mask, measure_first);
+    const bool delayed = (j->cfg.flags & GV_FLAG_DELAYED_UPDATES) && j->Nmax <= j->nt;
+    if (j->nt == 128) {
+        if (delayed) return fp64 ? launch_walk<double, 128, 8>(j, nsteps, s0, meas, mask, measure_first)
+                                 : launch_walk<float, 128, 8>(j, nsteps, s0, meas, mask, measure_first);
+        return fp64 ? launch_walk<double, 128, 0>(j, nsteps, s0, meas, mask, measure_first)
+                    : launch_walk<float, 128, 0>(j, nsteps, s0, meas, mask, measure_first);
+    }
+    if (delayed) return fp64 ? launch_walk<double, 256, 8>(j, nsteps, s0, meas, mask, measure_first)
+                             : launch_walk<float, 256, 8>(j, nsteps, s0, meas, mask, measure_first);
+    return fp64 ? launch_walk<double, 256, 0>(j, nsteps, s0, meas, mask, measure_first)
+                : launch_walk<float, 256, 0>(j, nsteps, s0, meas, mask, measure_first);
 }
 
 template <typename T, int NT>

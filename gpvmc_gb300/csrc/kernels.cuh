@@ -262,10 +262,10 @@ template <> struct Accept<float> {
 };
 
 struct WalkLayout {
-    size_t fock, part, nbr, coef, uu, row, rr, red, rdn, gj, total;
+    size_t fock, part, nbr, coef, uu, row, rr, red, rdn, gj, pend, redk, total;
 };
 
-template <typename T, int NT>
+template <typename T, int NT, int KD>
 __host__ __device__ inline WalkLayout walk_layout(int Ns, int Nmax, bool projheis, bool gj)
 {
     WalkLayout l;
@@ -281,6 +281,9 @@ __host__ __device__ inline WalkLayout walk_layout(int Ns, int Nmax, bool projhei
     l.red = al(sizeof(double) * (2 * (NT / 32) * 4 + (NT / 32) * 4));
     l.rdn = al(projheis ? sizeof(cx<T>) * 4 * Ns : 16);
     l.gj = al(gj ? gj_smem_bytes(Nmax, NT) : 16);
+    // delayed updates: per flavour KD row vectors rr_j[f], KD column vectors w_j[p]
+    l.pend = al(KD ? sizeof(cx<T>) * 2 * 2 * KD * Nmax : 16);
+    l.redk = al(KD ? sizeof(T) * 4 * KD * (NT / 32) + sizeof(cx<T>) * 2 * KD : 16);
     l.total = al(16);
     return l;
 }
@@ -437,7 +440,135 @@ __device__ void measure_now(const WalkCtx<T>& C, int mask)
     }
 }
 
-template <typename T, int NT>
+// Pending rank-1 updates (delayed Sherman-Morrison, McDaniel et al., J. Chem.
+// Phys. 147, 174107 (2017)): the stored AiT0 lags the current inverse by the
+// pending pairs, AiT_cur[f][p] = AiT0[f][p] - sum_j rr_j[f] w_j[p].
+template <typename T, int KD>
+struct Pending {
+    cx<T>* rr;   // [fl][KD][Nmax]
+    cx<T>* w;    // [fl][KD][Nmax]
+    int n;
+};
+
+// Write the pending pairs into AiT0 (one read + write pass per column).
+template <typename T, int NT, int KD>
+__device__ __forceinline__ void flush_pending(Pending<T, KD>& P, cx<T>* A0, cx<T>* A1, int N0, int N1, int Nmax)
+{
+    if (KD == 0 || P.n == 0) return;
+    for (int fl = 0; fl < 2; ++fl) {
+        const int N = fl ? N1 : N0;
+        cx<T>* A = fl ? A1 : A0;
+        const cx<T>* rr = P.rr + size_t(fl) * KD * Nmax;
+        const cx<T>* wv = P.w + size_t(fl) * KD * Nmax;
+        for (int p = threadIdx.x; p < N; p += NT) {
+            cx<T> w[KD > 0 ? KD : 1];
+#pragma unroll
+            for (int j = 0; j < KD; ++j) w[j] = j < P.n ? cx<T>{-wv[j * Nmax + p].x, -wv[j * Nmax + p].y} : cx<T>{T(0), T(0)};
+            for (int f = 0; f < N; ++f) {
+                cx<T> a = A[size_t(f) * N + p];
+#pragma unroll
+                for (int j = 0; j < KD; ++j)
+                    if (j < P.n) cmac(a, w[j], rr[j * Nmax + f]);
+                A[size_t(f) * N + p] = a;
+            }
+        }
+    }
+    P.n = 0;
+    __syncthreads();
+}
+
+
+// Accepted exchange with delayed updates.  With r the ratio, row_c the
+// current row c of A^-1 and u the new orbital column:
+//   rr_new = row_c / r,  w_new = A_cur^-1 u - e_c,
+//   A_cur^-1 u = AiT0^T u - sum_j w_j (rr_j . u).
+// The column pass reads AiT0 once to form AiT0^T u; when the list is full the
+// same pass also writes the KD pending pairs into AiT0 (and the new pair
+// starts the next list), so the matrix is written once per KD accepts.
+template <typename T, int NT, int KD>
+__device__ __noinline__ void accept_delayed(Pending<T, KD>& P, cx<T>* A0, cx<T>* A1, int N0, int N1, int Nmax,
+                                            int cu, int cd, cx<T> iu, cx<T> id, const cx<T>* s_row,
+                                            const cx<T>* s_uu, T* red)
+{
+    constexpr int NW = NT / 32;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int np = P.n;
+    // s_j = rr_j . u for both flavours (block reduction of 2*np complex numbers)
+#pragma unroll
+    for (int fl = 0; fl < 2; ++fl) {
+        const int N = fl ? N1 : N0;
+#pragma unroll
+        for (int j = 0; j < KD; ++j) {
+            cx<T> a = {T(0), T(0)};
+            if (j < np)
+                for (int f = tid; f < N; f += NT) cmac(a, P.rr[(fl * KD + j) * Nmax + f], s_uu[fl * Nmax + f]);
+            a = warp_sum(a);
+            if (lane == 0) { red[((fl * KD + j) * NW + warp) * 2] = a.x; red[((fl * KD + j) * NW + warp) * 2 + 1] = a.y; }
+        }
+    }
+    __syncthreads();
+    cx<T>* sj = reinterpret_cast<cx<T>*>(red + 4 * KD * NW);   // [fl][KD], after the partials
+    if (tid < 2 * KD) {
+        cx<T> a = {T(0), T(0)};
+        for (int q = 0; q < NW; ++q) { a.x += red[(tid * NW + q) * 2]; a.y += red[(tid * NW + q) * 2 + 1]; }
+        sj[tid] = a;
+    }
+    __syncthreads();
+    const bool full = np == KD;
+    const int slot = full ? 0 : np;
+    // rows rr_new go to the list after the column pass (the pass may still read old rows)
+    cx<T> wnew[2];
+    int pidx[2];
+#pragma unroll
+    for (int fl = 0; fl < 2; ++fl) {
+        const int N = fl ? N1 : N0;
+        cx<T>* A = fl ? A1 : A0;
+        const int c = fl ? cd : cu;
+        const cx<T>* rr = P.rr + size_t(fl) * KD * Nmax;
+        const cx<T>* wv = P.w + size_t(fl) * KD * Nmax;
+        const cx<T>* u = s_uu + fl * Nmax;
+        pidx[fl] = -1;
+        for (int p = tid; p < N; p += NT) {
+            cx<T> wold[KD];
+#pragma unroll
+            for (int j = 0; j < KD; ++j) wold[j] = j < np ? wv[j * Nmax + p] : cx<T>{T(0), T(0)};
+            cx<T> acc;
+            if (!full) {
+                acc = col_dot<T>(A, N, p, u);
+            } else {
+                acc = {T(0), T(0)};
+                cx<T> nw[KD];
+#pragma unroll
+                for (int j = 0; j < KD; ++j) nw[j] = {-wold[j].x, -wold[j].y};
+                for (int f = 0; f < N; ++f) {
+                    cx<T> a = A[size_t(f) * N + p];
+                    cmac(acc, a, u[f]);
+#pragma unroll
+                    for (int j = 0; j < KD; ++j) cmac(a, nw[j], rr[j * Nmax + f]);
+                    A[size_t(f) * N + p] = a;
+                }
+            }
+#pragma unroll
+            for (int j = 0; j < KD; ++j)
+                if (j < np) cmac(acc, cx<T>{-wold[j].x, -wold[j].y}, sj[fl * KD + j]);
+            if (p == c) acc.x -= T(1);
+            wnew[fl] = acc;
+            pidx[fl] = p;
+        }
+    }
+    __syncthreads();   // every read of the old pairs is done
+#pragma unroll
+    for (int fl = 0; fl < 2; ++fl) {
+        const int N = fl ? N1 : N0;
+        const cx<T> inv = fl ? id : iu;
+        for (int f = tid; f < N; f += NT) P.rr[(fl * KD + slot) * Nmax + f] = s_row[fl * Nmax + f] * inv;
+        if (pidx[fl] >= 0) P.w[(fl * KD + slot) * Nmax + pidx[fl]] = wnew[fl];
+    }
+    P.n = slot + 1;
+    __syncthreads();
+}
+
+template <typename T, int NT, int KD>
 __global__ void __launch_bounds__(NT, 768 / NT) k_walk_gs(DevJob J, uint64_t nsteps, uint64_t s0, uint64_t meas, int mask,
                                                 int inkernel_reinv, int measure_first)
 {
@@ -448,7 +579,9 @@ __global__ void __launch_bounds__(NT, 768 / NT) k_walk_gs(DevJob J, uint64_t nst
     if (w >= J.W || J.status[w] != GV_OK) return;
     const int Ns = J.Ns, Nmax = J.Nmax, L = J.L, Nk = J.Nk;
     const int N0 = J.N[0], N1 = J.N[1];
-    const WalkLayout lay = walk_layout<T, NT>(Ns, Nmax, (mask & GV_MEAS_PROJHEIS) != 0, inkernel_reinv != 0);
+    const WalkLayout lay = walk_layout<T, NT, KD>(Ns, Nmax, (mask & GV_MEAS_PROJHEIS) != 0, inkernel_reinv != 0);
+    Pending<T, KD> P = {reinterpret_cast<cx<T>*>(smem + lay.pend),
+                        reinterpret_cast<cx<T>*>(smem + lay.pend) + 2 * KD * Nmax, 0};
     int16_t* s_fock = reinterpret_cast<int16_t*>(smem + lay.fock);
     int16_t* s_part = reinterpret_cast<int16_t*>(smem + lay.part);
     int16_t* s_nbr = reinterpret_cast<int16_t*>(smem + lay.nbr);
@@ -510,14 +643,22 @@ __global__ void __launch_bounds__(NT, 768 / NT) k_walk_gs(DevJob J, uint64_t nst
             const int cu = s_fock[upf], cd = s_fock[Ns + dnf];
             cx<T> au = {T(0), T(0)}, ad = {T(0), T(0)};
             for (int f = tid; f < N0; f += NT) {
-                const cx<T> a = A0[size_t(f) * N0 + cu];
+                cx<T> a = A0[size_t(f) * N0 + cu];
+                for (int j = 0; j < P.n; ++j) {   // current row c: stored row minus pending pairs
+                    const cx<T> wj = P.w[j * Nmax + cu];
+                    cmac(a, cx<T>{-wj.x, -wj.y}, P.rr[j * Nmax + f]);
+                }
                 const cx<T> u = phi_row<T>(phase, s_coef, Nk, Nmax, L, upt, f);
                 s_row[f] = a;
                 s_uu[f] = u;
                 cmac(au, a, u);
             }
             for (int f = tid; f < N1; f += NT) {
-                const cx<T> a = A1[size_t(f) * N1 + cd];
+                cx<T> a = A1[size_t(f) * N1 + cd];
+                for (int j = 0; j < P.n; ++j) {
+                    const cx<T> wj = P.w[(KD + j) * Nmax + cd];
+                    cmac(a, cx<T>{-wj.x, -wj.y}, P.rr[(KD + j) * Nmax + f]);
+                }
                 const cx<T> u = phi_row<T>(phase, s_coef + 2 * Nmax, Nk, Nmax, L, dnt, f);
                 s_row[Nmax + f] = a;
                 s_uu[Nmax + f] = u;
@@ -543,22 +684,27 @@ __global__ void __launch_bounds__(NT, 768 / NT) k_walk_gs(DevJob J, uint64_t nst
             } else {
                 if (norm2(ru) < T(1e-9) || norm2(rd) < T(1e-9)) { status = GV_ERR_SINGULAR; break; }
                 const cx<T> iu = cinv(ru), id = cinv(rd);
-                for (int f = tid; f < N0; f += NT) s_rr[f] = s_row[f] * iu;
-                for (int f = tid; f < N1; f += NT) s_rr[Nmax + f] = s_row[Nmax + f] * id;
-                __syncthreads();
-                // Per particle column p (one owner thread): w_p = (A^-1 u)_p - [p == c],
-                // then column update with the old row c of A^-1 divided by r.
-                for (int p = tid; p < N0; p += NT) {
-                    cx<T> wp = col_dot<T>(A0, N0, p, s_uu);
-                    if (p == cu) wp.x -= T(1);
-                    col_update<T>(A0, N0, p, wp, s_rr);
+                if constexpr (KD == 0) {
+                    for (int f = tid; f < N0; f += NT) s_rr[f] = s_row[f] * iu;
+                    for (int f = tid; f < N1; f += NT) s_rr[Nmax + f] = s_row[Nmax + f] * id;
+                    __syncthreads();
+                    // Per particle column p (one owner thread): w_p = (A^-1 u)_p - [p == c],
+                    // then column update with the old row c of A^-1 divided by r.
+                    for (int p = tid; p < N0; p += NT) {
+                        cx<T> wp = col_dot<T>(A0, N0, p, s_uu);
+                        if (p == cu) wp.x -= T(1);
+                        col_update<T>(A0, N0, p, wp, s_rr);
+                    }
+                    for (int p = tid; p < N1; p += NT) {
+                        cx<T> wp = col_dot<T>(A1, N1, p, s_uu + Nmax);
+                        if (p == cd) wp.x -= T(1);
+                        col_update<T>(A1, N1, p, wp, s_rr + Nmax);
+                    }
+                    __syncthreads();
+                } else {
+                    accept_delayed<T, NT, KD>(P, A0, A1, N0, N1, Nmax, cu, cd, iu, id, s_row, s_uu,
+                                              reinterpret_cast<T*>(smem + lay.redk));
                 }
-                for (int p = tid; p < N1; p += NT) {
-                    cx<T> wp = col_dot<T>(A1, N1, p, s_uu + Nmax);
-                    if (p == cd) wp.x -= T(1);
-                    col_update<T>(A1, N1, p, wp, s_rr + Nmax);
-                }
-                __syncthreads();
                 if (tid == 0) {
                     s_fock[upt] = int16_t(cu); s_fock[upf] = -1; s_part[cu] = int16_t(upt);
                     s_fock[Ns + dnt] = int16_t(cd); s_fock[Ns + dnf] = -1; s_part[Nmax + cd] = int16_t(dnt);
@@ -571,6 +717,7 @@ __global__ void __launch_bounds__(NT, 768 / NT) k_walk_gs(DevJob J, uint64_t nst
                 ++since;
                 __syncthreads();
                 if (inkernel_reinv && J.reinv_every > 0 && since >= J.reinv_every) {
+                    flush_pending<T, NT, KD>(P, A0, A1, N0, N1, Nmax);
                     char* gp = smem + lay.gj;
                     GJSmem G = carve_gj<NT>(gp, Nmax);
                     cx<double>* M = J.scratch64 + size_t(w) * Nmax * Nmax;
@@ -590,9 +737,12 @@ __global__ void __launch_bounds__(NT, 768 / NT) k_walk_gs(DevJob J, uint64_t nst
             J.trace[s] = t;
         }
         const uint64_t gs = s0 + s;
-        if (meas && (meas == 1 || gs % meas == 0) && mask)
+        if (meas && (meas == 1 || gs % meas == 0) && mask) {
+            flush_pending<T, NT, KD>(P, A0, A1, N0, N1, Nmax);
             measure_now<T, NT>(C, mask);
+        }
     }
+    flush_pending<T, NT, KD>(P, A0, A1, N0, N1, Nmax);
     __syncthreads();
     for (int i = tid; i < 2 * Ns; i += NT) J.fock[size_t(w) * 2 * Ns + i] = s_fock[i];
     for (int i = tid; i < 2 * Nmax; i += NT) J.part[size_t(w) * 2 * Nmax + i] = s_part[i];

@@ -88,7 +88,8 @@ class Job:
     """A batch of independent chains of one wavefunction on the GPU (gv_job)."""
 
     def __init__(self, wav, walkers=1, seed=1234, precision="fp64", reinv_every=0, walker_base=0,
-                 phi_range=None, neel_range=None, deferred_reinversion=False, drift_threshold=None):
+                 phi_range=None, neel_range=None, deferred_reinversion=False, drift_threshold=None,
+                 delayed_updates=False):
         L = _lib.lib()
         cfg = _lib.JobConfig()
         cfg.L = wav.L
@@ -110,6 +111,8 @@ class Job:
         if drift_threshold:
             cfg.flags |= _lib.GV_FLAG_REINV_ON_DRIFT
             cfg.drift_threshold = drift_threshold
+        if delayed_updates:
+            cfg.flags |= _lib.GV_FLAG_DELAYED_UPDATES
         self.cfg = cfg
         self.wav = wav
         self.walkers = walkers

@@ -63,6 +63,9 @@ typedef int32_t gv_status;
 #define GV_FLAG_REINV_ON_DRIFT 2  /* with GV_FLAG_REINV_DEFERRED: at that point check the
                                      FP64 sampled drift ||A A^-1 - I||_max and re-invert
                                      only when it exceeds drift_threshold */
+#define GV_FLAG_DELAYED_UPDATES 4 /* delayed rank-8 Sherman-Morrison updates: the inverse is
+                                     written back once per 8 accepted exchanges (the same
+                                     Markov chain; the inverse differs only by rounding) */
 
 #define GV_MEAS_PROJHEIS 1    /* ProjHeis (ProjHeis.cpp:40-158), Bx = 0 */
 #define GV_MEAS_STAGMAGN 2    /* StagMagnZ (StagMagnZ.cpp:12-43) */

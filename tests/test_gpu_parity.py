@@ -234,3 +234,35 @@ def test_drift_checked_reinversion(engine):
     c = job.counts()
     assert (c[:, 4] + checks).min() >= 1          # every walker was checked at least once
     assert job.drift().max() < 1e-3
+
+
+@pytest.mark.parametrize("L,steps", [(8, 6000), (16, 3000)])
+def test_delayed_updates_fp64_parity(engine, oracle, L, steps):
+    """Delayed rank-8 updates (GV_FLAG_DELAYED_UPDATES) walk the same chain as
+    the immediate Sherman-Morrison: in FP64 the oracle's decisions and ratios
+    to 1e-10 hold across many write-backs of the pending pairs."""
+    job = engine.Job(engine.StagFluxGroundState(L, PHI, 0.1), walkers=2, seed=123, delayed_updates=True)
+    orc = oracle.OracleChain(L, PHI, 0.1, seed=123, walker=1)
+    job.init_walkers()
+    orc.random_start()
+    tg = job.walk_traced(steps, 0, walker=1)
+    to = orc.walk(steps, trace=True)
+    _compare_traces(tg, to)
+    assert job.counts()[1][1] > 16
+    for fl in (0, 1):
+        gi, oi = job.inverse(1, fl), orc.inverse(fl)
+        assert np.abs(gi - oi).max() < 1e-9 * np.abs(oi).max()
+
+
+def test_delayed_updates_mixed_with_measurements(engine):
+    L = 16
+    a = engine.Job(engine.StagFluxGroundState(L, PHI, 0.05), walkers=32, seed=5, precision="mixed",
+                   delayed_updates=True)
+    a.set_measurements(3)
+    a.init_walkers()
+    a.walk(L * L * 6, L * L)
+    assert a.drift().max() < 1e-3
+    pj, n = a.projheis()
+    assert (n == 6).all() and np.isfinite(pj).all()
+    e = pj[:, 0].real / n
+    assert (-1.0 < e).all() and (e < 0.0).all()
