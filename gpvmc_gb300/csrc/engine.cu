@@ -138,20 +138,25 @@ gv_status launch_walk(gv_job* j, uint64_t nsteps, uint64_t s0, uint64_t meas, in
     return GV_OK;
 }
 
-// Delayed updates (depth 8) when requested and every particle column has its
+#ifndef GV_DELAY_DEPTH
+#define GV_DELAY_DEPTH 4
+#endif
+constexpr int kDelay = GV_DELAY_DEPTH;
+
+// Delayed updates (depth kDelay) when requested and every particle column has its
 // own thread; otherwise immediate rank-1 updates.
 gv_status walk_dispatch(gv_job* j, uint64_t nsteps, uint64_t s0, uint64_t meas, int mask, int measure_first = 0)
 {
     const bool fp64 = j->cfg.precision == GV_PREC_FP64;
     const bool delayed = (j->cfg.flags & GV_FLAG_DELAYED_UPDATES) && j->Nmax <= j->nt;
     if (j->nt == 128) {
-        if (delayed) return fp64 ? launch_walk<double, 128, 8>(j, nsteps, s0, meas, mask, measure_first)
-                                 : launch_walk<float, 128, 8>(j, nsteps, s0, meas, mask, measure_first);
+        if (delayed) return fp64 ? launch_walk<double, 128, kDelay>(j, nsteps, s0, meas, mask, measure_first)
+                                 : launch_walk<float, 128, kDelay>(j, nsteps, s0, meas, mask, measure_first);
         return fp64 ? launch_walk<double, 128, 0>(j, nsteps, s0, meas, mask, measure_first)
                     : launch_walk<float, 128, 0>(j, nsteps, s0, meas, mask, measure_first);
     }
-    if (delayed) return fp64 ? launch_walk<double, 256, 8>(j, nsteps, s0, meas, mask, measure_first)
-                             : launch_walk<float, 256, 8>(j, nsteps, s0, meas, mask, measure_first);
+    if (delayed) return fp64 ? launch_walk<double, 256, kDelay>(j, nsteps, s0, meas, mask, measure_first)
+                             : launch_walk<float, 256, kDelay>(j, nsteps, s0, meas, mask, measure_first);
     return fp64 ? launch_walk<double, 256, 0>(j, nsteps, s0, meas, mask, measure_first)
                 : launch_walk<float, 256, 0>(j, nsteps, s0, meas, mask, measure_first);
 }

@@ -464,11 +464,22 @@ __device__ __forceinline__ void flush_pending(Pending<T, KD>& P, cx<T>* A0, cx<T
             cx<T> w[KD > 0 ? KD : 1];
 #pragma unroll
             for (int j = 0; j < KD; ++j) w[j] = j < P.n ? cx<T>{-wv[j * Nmax + p].x, -wv[j * Nmax + p].y} : cx<T>{T(0), T(0)};
-            for (int f = 0; f < N; ++f) {
+            int f = 0;
+            for (; f + 8 <= N; f += 8) {
+                cx<T> a[8];
+#pragma unroll
+                for (int q = 0; q < 8; ++q) a[q] = A[size_t(f + q) * N + p];
+#pragma unroll
+                for (int q = 0; q < 8; ++q) {
+#pragma unroll
+                    for (int j = 0; j < KD; ++j) cmac(a[q], w[j], rr[j * Nmax + f + q]);
+                    A[size_t(f + q) * N + p] = a[q];
+                }
+            }
+            for (; f < N; ++f) {
                 cx<T> a = A[size_t(f) * N + p];
 #pragma unroll
-                for (int j = 0; j < KD; ++j)
-                    if (j < P.n) cmac(a, w[j], rr[j * Nmax + f]);
+                for (int j = 0; j < KD; ++j) cmac(a, w[j], rr[j * Nmax + f]);
                 A[size_t(f) * N + p] = a;
             }
         }
@@ -540,7 +551,20 @@ __device__ __noinline__ void accept_delayed(Pending<T, KD>& P, cx<T>* A0, cx<T>*
                 cx<T> nw[KD];
 #pragma unroll
                 for (int j = 0; j < KD; ++j) nw[j] = {-wold[j].x, -wold[j].y};
-                for (int f = 0; f < N; ++f) {
+                int f = 0;
+                for (; f + 8 <= N; f += 8) {   // 8 loads in flight, then update and store
+                    cx<T> a[8];
+#pragma unroll
+                    for (int q = 0; q < 8; ++q) a[q] = A[size_t(f + q) * N + p];
+#pragma unroll
+                    for (int q = 0; q < 8; ++q) {
+                        cmac(acc, a[q], u[f + q]);
+#pragma unroll
+                        for (int j = 0; j < KD; ++j) cmac(a[q], nw[j], rr[j * Nmax + f + q]);
+                        A[size_t(f + q) * N + p] = a[q];
+                    }
+                }
+                for (; f < N; ++f) {
                     cx<T> a = A[size_t(f) * N + p];
                     cmac(acc, a, u[f]);
 #pragma unroll
