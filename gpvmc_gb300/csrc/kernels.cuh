@@ -472,14 +472,16 @@ __device__ __forceinline__ void flush_pending(Pending<T, KD>& P, cx<T>* A0, cx<T
 #pragma unroll
                 for (int q = 0; q < 8; ++q) {
 #pragma unroll
-                    for (int j = 0; j < KD; ++j) cmac(a[q], w[j], rr[j * Nmax + f + q]);
+                    for (int j = 0; j < KD; ++j)
+                        if (j < P.n) cmac(a[q], w[j], rr[j * Nmax + f + q]);   // rows past n are not written yet
                     A[size_t(f + q) * N + p] = a[q];
                 }
             }
             for (; f < N; ++f) {
                 cx<T> a = A[size_t(f) * N + p];
 #pragma unroll
-                for (int j = 0; j < KD; ++j) cmac(a, w[j], rr[j * Nmax + f]);
+                for (int j = 0; j < KD; ++j)
+                    if (j < P.n) cmac(a, w[j], rr[j * Nmax + f]);
                 A[size_t(f) * N + p] = a;
             }
         }
