@@ -50,7 +50,7 @@ def workload_config(precision, policy="drift"):
                         "phi~U[0.1,0.4)pi, neel~U[0,0.15), ProjHeis every sweep, " + pol,
             "L": L, "walkers": WALKERS, "sweep_steps": SWEEP, "precision": precision,
             "reinv_every_accepted": REINV, "reinversion_policy": policy, "thermalisation_sweeps": THERM_SWEEPS,
-            "updates": "delayed rank-8 Sherman-Morrison" if precision == "mixed" else "rank-1 Sherman-Morrison",
+            "updates": "rank-1 Sherman-Morrison per accepted exchange",
             "step": "one sweep of every walker (2048*256 Metropolis steps)",
             "l2": "inputs larger than L2: walker inverses %d MiB" % (WALKERS * 2 * 128 * 128 * (8 if precision == "mixed" else 16) >> 20)}
 
@@ -159,7 +159,7 @@ def make_job(g, precision, rank, policy="drift"):
     job = g.Job(wav, walkers=WALKERS, seed=SEED, precision=precision, reinv_every=REINV if policy != "none" else 0,
                 walker_base=walker_base(rank, WALKERS), phi_range=PHI_RANGE, neel_range=NEEL_RANGE,
                 deferred_reinversion=True, drift_threshold=DRIFT_THRESHOLD if policy == "drift" else None,
-                delayed_updates=(precision == "mixed"))
+                delayed_updates=False)
     job.set_measurements(1)
     return job
 
