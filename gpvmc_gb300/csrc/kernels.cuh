@@ -594,64 +594,6 @@ __device__ __noinline__ void accept_delayed(Pending<T, KD>& P, cx<T>* A0, cx<T>*
     __syncthreads();
 }
 
-// Two adjacent particle columns (p, p+1) of AiT per thread, loaded as one
-// 2-complex vector: the accept's two passes with 8 rows in flight.
-template <typename T>
-struct alignas(4 * sizeof(T)) cx2 {
-    cx<T> a, b;
-};
-
-template <typename T>
-__device__ __forceinline__ void col2_dot(const cx<T>* __restrict__ A, int N, int p, const cx<T>* v, cx<T>& r0, cx<T>& r1)
-{
-    const cx2<T>* A2 = reinterpret_cast<const cx2<T>*>(A);
-    const int n2 = N / 2, p2 = p / 2;
-    r0 = {T(0), T(0)};
-    r1 = {T(0), T(0)};
-    int f = 0;
-    for (; f + 8 <= N; f += 8) {
-        cx2<T> a[8];
-#pragma unroll
-        for (int k = 0; k < 8; ++k) a[k] = A2[size_t(f + k) * n2 + p2];
-#pragma unroll
-        for (int k = 0; k < 8; ++k) {
-            cmac(r0, a[k].a, v[f + k]);
-            cmac(r1, a[k].b, v[f + k]);
-        }
-    }
-    for (; f < N; ++f) {
-        const cx2<T> a = A2[size_t(f) * n2 + p2];
-        cmac(r0, a.a, v[f]);
-        cmac(r1, a.b, v[f]);
-    }
-}
-
-template <typename T>
-__device__ __forceinline__ void col2_update(cx<T>* A, int N, int p, cx<T> w0, cx<T> w1, const cx<T>* rr)
-{
-    cx2<T>* A2 = reinterpret_cast<cx2<T>*>(A);
-    const int n2 = N / 2, p2 = p / 2;
-    const cx<T> n0 = {-w0.x, -w0.y}, n1 = {-w1.x, -w1.y};
-    int f = 0;
-    for (; f + 8 <= N; f += 8) {
-        cx2<T> a[8];
-#pragma unroll
-        for (int k = 0; k < 8; ++k) a[k] = A2[size_t(f + k) * n2 + p2];
-#pragma unroll
-        for (int k = 0; k < 8; ++k) {
-            cmac(a[k].a, n0, rr[f + k]);
-            cmac(a[k].b, n1, rr[f + k]);
-            A2[size_t(f + k) * n2 + p2] = a[k];
-        }
-    }
-    for (; f < N; ++f) {
-        cx2<T> a = A2[size_t(f) * n2 + p2];
-        cmac(a.a, n0, rr[f]);
-        cmac(a.b, n1, rr[f]);
-        A2[size_t(f) * n2 + p2] = a;
-    }
-}
-
 template <typename T, int NT, int KD>
 __global__ void __launch_bounds__(NT, 768 / NT) k_walk_gs(DevJob J, uint64_t nsteps, uint64_t s0, uint64_t meas, int mask,
                                                 int inkernel_reinv, int measure_first)
@@ -774,29 +716,15 @@ __global__ void __launch_bounds__(NT, 768 / NT) k_walk_gs(DevJob J, uint64_t nst
                     __syncthreads();
                     // Per particle column p (one owner thread): w_p = (A^-1 u)_p - [p == c],
                     // then column update with the old row c of A^-1 divided by r.
-                    if (N0 == N1 && (N0 & 1) == 0 && N0 <= NT) {
-                        // both flavours at once, two adjacent columns per thread
-                        const int fl = tid / (NT / 2), p = 2 * (tid % (NT / 2));
-                        if (p < N0) {
-                            cx<T>* A = fl ? A1 : A0;
-                            const int c = fl ? cd : cu;
-                            cx<T> w0, w1;
-                            col2_dot<T>(A, N0, p, s_uu + fl * Nmax, w0, w1);
-                            if (p == c) w0.x -= T(1);
-                            if (p + 1 == c) w1.x -= T(1);
-                            col2_update<T>(A, N0, p, w0, w1, s_rr + fl * Nmax);
-                        }
-                    } else {
-                        for (int p = tid; p < N0; p += NT) {
-                            cx<T> wp = col_dot<T>(A0, N0, p, s_uu);
-                            if (p == cu) wp.x -= T(1);
-                            col_update<T>(A0, N0, p, wp, s_rr);
-                        }
-                        for (int p = tid; p < N1; p += NT) {
-                            cx<T> wp = col_dot<T>(A1, N1, p, s_uu + Nmax);
-                            if (p == cd) wp.x -= T(1);
-                            col_update<T>(A1, N1, p, wp, s_rr + Nmax);
-                        }
+                    for (int p = tid; p < N0; p += NT) {
+                        cx<T> wp = col_dot<T>(A0, N0, p, s_uu);
+                        if (p == cu) wp.x -= T(1);
+                        col_update<T>(A0, N0, p, wp, s_rr);
+                    }
+                    for (int p = tid; p < N1; p += NT) {
+                        cx<T> wp = col_dot<T>(A1, N1, p, s_uu + Nmax);
+                        if (p == cd) wp.x -= T(1);
+                        col_update<T>(A1, N1, p, wp, s_rr + Nmax);
                     }
                     __syncthreads();
                 } else {
