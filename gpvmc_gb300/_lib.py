@@ -11,6 +11,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "_lib", "libgpvmc_gb300.so")
 
 GV_OK = 0
+GV_ERR_OOM, GV_ERR_CUDA = 7, 8
 STATUS_NAMES = {0: "ok", 1: "invalid", 2: "singular", 3: "nan", 4: "zero amplitude", 5: "drift",
                 6: "timeout", 7: "out of memory", 8: "cuda error", 9: "not ready", 10: "too large"}
 
@@ -23,9 +24,10 @@ GV_FLAG_DELAYED_UPDATES = 4
 
 
 class GvError(RuntimeError):
-    def __init__(self, status, where):
+    def __init__(self, status, where, detail=""):
         self.status = status
-        super().__init__("%s failed: %s (%d)" % (where, STATUS_NAMES.get(status, "?"), status))
+        msg = "%s failed: %s (%d)" % (where, STATUS_NAMES.get(status, "?"), status)
+        super().__init__(msg + (": " + detail if detail else ""))
 
 
 class JobConfig(ctypes.Structure):
@@ -69,6 +71,9 @@ _SIGS = {
     "gv_job_read_inverse": [_P, ctypes.c_int32, ctypes.c_int32, ctypes.c_void_p],
     "gv_job_read_counts": [_P, ctypes.c_void_p],
     "gv_job_read_state_index": [_P, ctypes.c_void_p],
+    "gv_job_read_weight": [_P, ctypes.c_void_p],
+    "gv_job_read_status": [_P, ctypes.c_void_p],
+    "gv_job_read_orbitals": [_P, ctypes.c_int32, ctypes.c_int32, ctypes.c_void_p],
     "gv_job_read_projheis": [_P, ctypes.c_void_p, ctypes.c_void_p],
     "gv_job_read_stagmagn": [_P, ctypes.c_void_p, ctypes.c_void_p],
     "gv_job_read_statspin": [_P, ctypes.c_void_p, ctypes.c_void_p],
@@ -80,6 +85,8 @@ _SIGS = {
     "gv_phi_table": [ctypes.c_int32, ctypes.c_double, ctypes.c_double, ctypes.c_double, ctypes.c_void_p,
                      ctypes.c_int32, ctypes.c_void_p],
     "gv_lattice_neighbours": [ctypes.c_int32, ctypes.c_void_p],
+    "gv_channel_states": [ctypes.c_int32, ctypes.c_void_p, ctypes.c_int32, ctypes.c_void_p, ctypes.c_void_p,
+                          ctypes.c_void_p],
     "gv_channel_orbitals": [ctypes.c_int32, ctypes.c_void_p, ctypes.c_int32, ctypes.c_void_p, ctypes.c_int32,
                             ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p],
 }
@@ -106,6 +113,8 @@ def lib():
     L.gv_version.argtypes = []
     L.gv_status_string.restype = ctypes.c_char_p
     L.gv_status_string.argtypes = [ctypes.c_int32]
+    L.gv_last_cuda_error.restype = ctypes.c_char_p
+    L.gv_last_cuda_error.argtypes = []
     L.gv_philox4x32_10.restype = None
     L.gv_philox4x32_10.argtypes = [ctypes.POINTER(ctypes.c_uint32)] * 3
     L.gv_uniform_at.restype = ctypes.c_double
@@ -116,4 +125,7 @@ def lib():
 
 def check(status, where):
     if status != GV_OK:
-        raise GvError(status, where)
+        detail = ""
+        if status in (GV_ERR_CUDA, GV_ERR_OOM) and _lib is not None:
+            detail = _lib.gv_last_cuda_error().decode()
+        raise GvError(status, where, detail)

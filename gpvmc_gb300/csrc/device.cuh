@@ -164,6 +164,21 @@ struct DevJob {
     cx<double>* scratch64;     // per-CTA FP64 N*N scratch for re-inversion (W*Nmax*Nmax)
     gv_trace* trace;
     int trace_walker;
+    // Transverse-exciton channel only (null for the ground state).  The
+    // wavefunction's Fock state per walker: Slater row (slot) f holds orbital
+    // worb[f]; wslot[o] is the slot of orbital o or -1.  Channel state k
+    // differs from the current one `cur` by one flavour-0 hop
+    // exc_up[cur] -> exc_up[k] and one flavour-1 hop exc_dn[k] -> exc_dn[cur].
+    int16_t* worb;             // W*2*Nmax
+    int16_t* wslot;            // W*2*Ns
+    const int16_t* exc_up;     // Nexc: flavour-0 upper-band orbital of state k
+    const int16_t* exc_dn;     // Nexc: flavour-1 lower-band hole of state k
+    int32_t* cur;              // W: current channel state (WaveFunction::m_c_exc)
+    int32_t* wsign;            // W: sign of the wavefunction's Fock state (State::m_sign)
+    double* sigma;             // W: state weight / |det_0 det_1|^2 = sum_k |ratio_k|^2
+    void* gup;                 // W*N0*Nexc, GupT[f][k] = sum_p phi_{exc_up[k]}(x_p) (A0^-1)(p, f)
+    void* gdn;                 // W*Nmax,    g[f] = sum_p phi_{exc_dn[cur]}(x_p) (A1^-1)(p, f)
+    cx<double>* pjx;           // W*2*Nexc*Nexc ProjHeis H and O sums
 };
 
 // Amplitude kept as (complex mantissa, base-2 exponent); renormalised

@@ -21,6 +21,7 @@
 
 #include "device.cuh"
 #include "kernels.cuh"
+#include "kernels_trans.cuh"
 #include "model.hpp"
 
 using namespace gv;
@@ -55,16 +56,26 @@ struct gv_job {
     std::vector<double> kind_each[3];
     std::vector<double> wphi, wneel;
     std::vector<uint64_t> start_draws;   // Philox stream-1 uniform index per walker
+    bool trans = false;                  // transverse-exciton channel
+    std::vector<int16_t> exu, exd;       // channel tables (Channel::exc_up / exc_dn)
 };
 
 namespace {
 
+thread_local const char* g_last_cuda_error = "";
+
+// Status for a failed CUDA call, remembering its message for gv_last_cuda_error.
+gv_status cuda_status(cudaError_t e)
+{
+    if (e == cudaSuccess) return GV_OK;
+    g_last_cuda_error = cudaGetErrorString(e);
+    return e == cudaErrorMemoryAllocation ? GV_ERR_OOM : GV_ERR_CUDA;
+}
+
 #define GV_CK(x)                                                   \
     do {                                                           \
         cudaError_t e_ = (x);                                      \
-        if (e_ != cudaSuccess) {                                   \
-            return e_ == cudaErrorMemoryAllocation ? GV_ERR_OOM : GV_ERR_CUDA; \
-        }                                                          \
+        if (e_ != cudaSuccess) return cuda_status(e_);             \
     } while (0)
 
 template <typename P>
@@ -82,7 +93,9 @@ bool valid_config(const gv_job_config* c)
 {
     if (!c) return false;
     if (c->L < 4 || c->L > 64 || (c->L % 2)) return false;
-    if (c->channel != GV_CH_GROUNDSTATE) return false;
+    if (c->channel == GV_CH_TRANS && c->L > 32) return false;
+    if (c->channel != GV_CH_GROUNDSTATE && c->channel != GV_CH_TRANS) return false;
+    if (c->channel == GV_CH_TRANS && (c->flags & GV_FLAG_DELAYED_UPDATES)) return false;
     if (c->n_walkers < 1 || c->n_walkers > (1 << 20)) return false;
     if (c->precision != GV_PREC_FP64 && c->precision != GV_PREC_MIXED) return false;
     if (c->reinv_every < 0) return false;
@@ -93,6 +106,77 @@ bool valid_config(const gv_job_config* c)
 }
 
 int pick_threads(int Nmax) { return Nmax > 128 ? 256 : 128; }
+
+// Exciton channel tables, checked against the channel's hop table
+// (WaveFunction::m_exc, WaveFunction.cpp:39-67): from state a, state b != a
+// must be the flavour-0 hop exc_up[a] -> exc_up[b] and the flavour-1 hop
+// exc_dn[b] -> exc_dn[a], the structure the exciton kernels rely on.
+bool trans_tables(const Channel& ch, std::vector<int16_t>& up, std::vector<int16_t>& dn)
+{
+    const int n = ch.Nexc;
+    if (n < 2 || int(ch.exc_up.size()) != n || int(ch.exc_dn.size()) != n) return false;
+    up.assign(n, 0);
+    dn.assign(n, 0);
+    for (int k = 0; k < n; ++k) { up[k] = int16_t(ch.exc_up[k]); dn[k] = int16_t(ch.exc_dn[k]); }
+    for (int a = 0; a < n; ++a)
+        for (int b = 0; b < n; ++b) {
+            const size_t i = (size_t(a) * n + b) * 2;
+            if (a == b) {
+                if (ch.hop_from[i] >= 0 || ch.hop_from[i + 1] >= 0) return false;
+                continue;
+            }
+            if (ch.hop_from[i] != up[a] || ch.hop_to[i] != up[b] || ch.hop_from[i + 1] != dn[b] ||
+                ch.hop_to[i + 1] != dn[a])
+                return false;
+        }
+    return true;
+}
+
+// The wavefunction's Fock state on the host (State, State.cpp): slot of every
+// orbital (-1 empty), orbital of every slot, sign, channel state.
+struct WavHost {
+    std::vector<int16_t> slot[2], orb[2];
+    int sign = 1, cur = 0;
+};
+
+WavHost wav_state0(const gv_job* j)
+{
+    WavHost s;
+    for (int fl = 0; fl < 2; ++fl) {
+        s.slot[fl].assign(j->Ns, -1);
+        s.orb[fl].assign(j->Nmax, 0);
+        for (int x = 0; x < j->Ns; ++x)
+            if (j->ch.fock0[fl][x] < j->ch.N[fl]) {
+                s.slot[fl][x] = int16_t(j->ch.fock0[fl][x]);
+                s.orb[fl][j->ch.fock0[fl][x]] = int16_t(x);
+            }
+    }
+    return s;
+}
+
+// WaveFunction::Hop to state k (WaveFunction.cpp:69-73): State::Hop with the
+// sign of State::HopSign (State.cpp:73-115), parities taken before the hop.
+void wav_hop(const gv_job* j, WavHost& s, int k)
+{
+    const Channel& ch = j->ch;
+    const size_t i = (size_t(s.cur) * ch.Nexc + k) * 2;
+    int odd = 0;
+    for (int fl = 0; fl < 2; ++fl) {
+        const int from = ch.hop_from[i + fl], to = ch.hop_to[i + fl];
+        if (from < 0) continue;
+        for (int x = std::min(from, to) + 1; x < std::max(from, to); ++x) odd ^= s.slot[fl][x] >= 0 ? 1 : 0;
+    }
+    s.sign *= odd ? -1 : 1;
+    for (int fl = 0; fl < 2; ++fl) {
+        const int from = ch.hop_from[i + fl], to = ch.hop_to[i + fl];
+        if (from < 0) continue;
+        const int16_t p = s.slot[fl][from];
+        s.slot[fl][from] = -1;
+        s.slot[fl][to] = p;
+        s.orb[fl][p] = int16_t(to);
+    }
+    s.cur = k;
+}
 
 size_t scratch_walkers(const gv_job* j) { return size_t(j->W); }
 
@@ -187,7 +271,7 @@ gv_status deferred_reinversion(gv_job* j)
 gv_status statspin_dispatch(gv_job* j)
 {
     const bool fp64 = j->cfg.precision == GV_PREC_FP64;
-    size_t sm = (fp64 ? sizeof(cx<double>) : sizeof(cx<float>)) * 4 * j->Nmax;
+    size_t sm = (fp64 ? sizeof(cx<double>) : sizeof(cx<float>)) * 4 * j->Nmax + sizeof(int16_t) * 2 * j->Nmax + 16;
     int slot;
     GV_CK(mark_begin(j, 2, &slot));
     if (fp64) k_statspin<double, 128><<<j->W, 128, sm, j->stream>>>(j->d);
@@ -217,6 +301,153 @@ gv_status invert_all(gv_job* j, int only_due = 0)
 {
     return j->cfg.precision == GV_PREC_FP64 ? launch_invert<double, 256>(j, only_due)
                                             : launch_invert<float, 256>(j, only_due);
+}
+
+template <typename T>
+gv_status launch_walk_trans(gv_job* j, uint64_t nsteps)
+{
+    constexpr int NT = 256;
+    const bool inkernel = !(j->cfg.flags & GV_FLAG_REINV_DEFERRED);
+    const TransLayout lay = trans_layout<T, NT>(j->Ns, j->Nmax, j->ch.Nexc, inkernel);
+    GV_CK(cudaFuncSetAttribute(k_walk_trans<T, NT>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(lay.total)));
+    int slot;
+    GV_CK(mark_begin(j, 0, &slot));
+    k_walk_trans<T, NT><<<j->W, NT, lay.total, j->stream>>>(j->d, nsteps, inkernel ? 1 : 0);
+    GV_CK(cudaGetLastError());
+    GV_CK(mark_end(j, slot));
+    ++j->last_launches;
+    ++j->total_launches;
+    return GV_OK;
+}
+
+gv_status walk_trans_dispatch(gv_job* j, uint64_t nsteps)
+{
+    return j->cfg.precision == GV_PREC_FP64 ? launch_walk_trans<double>(j, nsteps) : launch_walk_trans<float>(j, nsteps);
+}
+
+template <typename T>
+gv_status launch_measure_trans(gv_job* j, int mask)
+{
+    constexpr int NT = 256;
+    const MeasLayout lay = meas_layout<T, NT>(j->Ns, j->Nmax, j->ch.Nexc);
+    GV_CK(cudaFuncSetAttribute(k_measure_trans<T, NT>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(lay.total)));
+    int slot;
+    GV_CK(mark_begin(j, 2, &slot));
+    k_measure_trans<T, NT><<<j->W, NT, lay.total, j->stream>>>(j->d, mask);
+    GV_CK(cudaGetLastError());
+    GV_CK(mark_end(j, slot));
+    ++j->last_launches;
+    ++j->total_launches;
+    return GV_OK;
+}
+
+gv_status measure_trans_dispatch(gv_job* j, int mask)
+{
+    return j->cfg.precision == GV_PREC_FP64 ? launch_measure_trans<double>(j, mask) : launch_measure_trans<float>(j, mask);
+}
+
+// sigma (and, with out, every state's |rho0_k|^2) of every walker.
+gv_status trans_overlaps(gv_job* j, double* out)
+{
+    if (j->cfg.precision == GV_PREC_FP64) k_trans_overlaps<double, 128><<<j->W, 128, 0, j->stream>>>(j->d, out);
+    else k_trans_overlaps<float, 128><<<j->W, 128, 0, j->stream>>>(j->d, out);
+    GV_CK(cudaGetLastError());
+    ++j->total_launches;
+    return GV_OK;
+}
+
+gv_status upload_wav(gv_job* j, const std::vector<WavHost>& ws)
+{
+    const int W = j->W, Ns = j->Ns, Nmax = j->Nmax;
+    std::vector<int16_t> slot(size_t(W) * 2 * Ns), orb(size_t(W) * 2 * Nmax);
+    std::vector<int32_t> cur(W), sign(W);
+    for (int w = 0; w < W; ++w) {
+        for (int fl = 0; fl < 2; ++fl) {
+            std::copy(ws[w].slot[fl].begin(), ws[w].slot[fl].end(), slot.begin() + (size_t(w) * 2 + fl) * Ns);
+            std::copy(ws[w].orb[fl].begin(), ws[w].orb[fl].end(), orb.begin() + (size_t(w) * 2 + fl) * Nmax);
+        }
+        cur[w] = ws[w].cur;
+        sign[w] = ws[w].sign;
+    }
+    GV_CK(cudaMemcpyAsync(j->d.wslot, slot.data(), slot.size() * sizeof(int16_t), cudaMemcpyHostToDevice, j->stream));
+    GV_CK(cudaMemcpyAsync(j->d.worb, orb.data(), orb.size() * sizeof(int16_t), cudaMemcpyHostToDevice, j->stream));
+    GV_CK(cudaMemcpyAsync(j->d.cur, cur.data(), W * sizeof(int32_t), cudaMemcpyHostToDevice, j->stream));
+    GV_CK(cudaMemcpyAsync(j->d.wsign, sign.data(), W * sizeof(int32_t), cudaMemcpyHostToDevice, j->stream));
+    GV_CK(cudaStreamSynchronize(j->stream));
+    return GV_OK;
+}
+
+gv_status virt_update_trans(gv_job* j, int walker, int nset, const int32_t* hops, double* out)
+{
+    for (int i = 0; i < 4 * nset; ++i)
+        if (hops[i] < -1 || hops[i] >= j->Ns) return GV_ERR_INVALID;
+    const size_t nout = size_t(nset) * j->ch.Nexc * 2;
+    int32_t* dh = nullptr;
+    double* dout = nullptr;
+    GV_CK(cudaMalloc(&dh, sizeof(int32_t) * 4 * nset));
+    if (cudaMalloc(&dout, sizeof(double) * nout)) { cudaFree(dh); return GV_ERR_OOM; }
+    cudaError_t e = cudaMemcpyAsync(dh, hops, sizeof(int32_t) * 4 * nset, cudaMemcpyHostToDevice, j->stream);
+    const size_t sm = (j->cfg.precision == GV_PREC_FP64 ? sizeof(cx<double>) : sizeof(cx<float>)) * 2 * j->Nmax +
+                      sizeof(double) * 6 * 4 + 16;
+    if (!e) {
+        if (j->cfg.precision == GV_PREC_FP64) k_virt_trans<double, 128><<<nset, 128, sm, j->stream>>>(j->d, walker, nset, dh, dout);
+        else k_virt_trans<float, 128><<<nset, 128, sm, j->stream>>>(j->d, walker, nset, dh, dout);
+        e = cudaGetLastError();
+    }
+    if (!e) e = cudaMemcpyAsync(out, dout, sizeof(double) * nout, cudaMemcpyDeviceToHost, j->stream);
+    if (!e) e = cudaStreamSynchronize(j->stream);
+    cudaFree(dh);
+    cudaFree(dout);
+    return cuda_status(e);
+}
+
+constexpr double kMixedMaxInverse = 1e6;
+
+// Largest |(A^-1)_ij| over both flavours of every walker (stored precision).
+gv_status inverse_max_abs(gv_job* j, double* out)
+{
+    double* d = nullptr;
+    GV_CK(cudaMalloc(&d, sizeof(double) * j->W));
+    if (j->cfg.precision == GV_PREC_FP64) k_inverse_max_abs<double, 256><<<j->W, 256, 0, j->stream>>>(j->d, d);
+    else k_inverse_max_abs<float, 256><<<j->W, 256, 0, j->stream>>>(j->d, d);
+    cudaError_t e = cudaGetLastError();
+    if (!e) e = cudaMemcpyAsync(out, d, sizeof(double) * j->W, cudaMemcpyDeviceToHost, j->stream);
+    if (!e) e = cudaStreamSynchronize(j->stream);
+    cudaFree(d);
+    ++j->total_launches;
+    return cuda_status(e);
+}
+
+// vmc.cpp:243-263 for the exciton channel: with every walker inverted in
+// channel state 0, pick the state of largest |Amp| (first maximum; the
+// overlaps come from the determinant lemma instead of one LU per state),
+// replay the reference's hop path 0 -> 1 -> ... -> Nexc-1 -> kmax for the
+// Fock-state slots and sign, invert in that state and set the weight.
+gv_status trans_start(gv_job* j)
+{
+    const int W = j->W, Nexc = j->ch.Nexc;
+    double* dov = nullptr;
+    GV_CK(cudaMalloc(&dov, sizeof(double) * size_t(W) * Nexc));
+    std::vector<double> ov(size_t(W) * Nexc);
+    gv_status st = trans_overlaps(j, dov);
+    if (!st && (cudaMemcpyAsync(ov.data(), dov, ov.size() * sizeof(double), cudaMemcpyDeviceToHost, j->stream) ||
+                cudaStreamSynchronize(j->stream)))
+        st = GV_ERR_CUDA;
+    cudaFree(dov);
+    if (st) return st;
+    WavHost base = wav_state0(j);
+    for (int k = 0; k < Nexc; ++k) wav_hop(j, base, k);
+    std::vector<WavHost> ws(W, base);
+    for (int w = 0; w < W; ++w) {
+        int kmax = 0;
+        double best = ov[size_t(w) * Nexc];
+        for (int k = 1; k < Nexc; ++k)
+            if (ov[size_t(w) * Nexc + k] > best) { best = ov[size_t(w) * Nexc + k]; kmax = k; }
+        wav_hop(j, ws[w], kmax);
+    }
+    if ((st = upload_wav(j, ws))) return st;
+    if ((st = invert_all(j))) return st;
+    return trans_overlaps(j, nullptr);
 }
 
 // LatticeState::RanInit (LatticeState.cpp:37-82) for the two-flavour
@@ -302,6 +533,19 @@ gv_status gv_channel_orbitals(int32_t L, const double* bc, int32_t channel, cons
     return GV_OK;
 }
 
+gv_status gv_channel_states(int32_t L, const double* bc, int32_t channel, const int32_t* q, int32_t* exc_up,
+                            int32_t* exc_dn)
+{
+    if (L < 4 || L > 32 || (L % 2) || !bc || !q || !exc_up || !exc_dn || channel != GV_CH_TRANS) return GV_ERR_INVALID;
+    Orbitals o = make_orbitals(L, bc[0], bc[1]);
+    if (!o.ok) return GV_ERR_INVALID;
+    Channel ch = make_channel(o, channel, q[0], q[1]);
+    std::vector<int16_t> up, dn;
+    if (!ch.ok || !trans_tables(ch, up, dn)) return GV_ERR_INVALID;
+    for (int k = 0; k < ch.Nexc; ++k) { exc_up[k] = up[k]; exc_dn[k] = dn[k]; }
+    return GV_OK;
+}
+
 void gv_philox4x32_10(const uint32_t* c, const uint32_t* k, uint32_t* out)
 {
     philox4x32_10(c[0], c[1], c[2], c[3], k[0], k[1], out);
@@ -311,6 +555,8 @@ double gv_uniform_at(uint64_t seed, uint32_t walker, uint32_t stream, uint64_t k
 {
     return uniform_at(seed, walker, stream, k);
 }
+
+const char* gv_last_cuda_error(void) { return g_last_cuda_error; }
 
 const char* gv_status_string(gv_status s)
 {
@@ -334,7 +580,9 @@ gv_status gv_job_footprint(const gv_job_config* c, uint64_t* bytes)
 {
     if (!valid_config(c) || !bytes) return GV_ERR_INVALID;
     const uint64_t Ns = uint64_t(c->L) * c->L, Nk = Ns / 2, W = c->n_walkers;
-    const uint64_t N0 = Ns / 2, N1 = Ns / 2, Nmax = std::max(N0, N1);
+    const bool tr = c->channel == GV_CH_TRANS;
+    const uint64_t N0 = tr ? Ns / 2 + 1 : Ns / 2, N1 = tr ? Ns / 2 - 1 : Ns / 2, Nmax = std::max(N0, N1);
+    const uint64_t Nexc = tr ? Ns / 2 : 1;
     const uint64_t es = c->precision == GV_PREC_FP64 ? 16 : 8;
     uint64_t b = 0;
     b += Ns * Nk * (16 + 8);                 // phase tables
@@ -344,6 +592,11 @@ gv_status gv_job_footprint(const gv_job_config* c, uint64_t* bytes)
     b += W * 256;                            // per-walker scalars
     b += W * Nmax * Nmax * 16;               // FP64 re-inversion scratch
     b += 5 * Ns * Ns * 16;                   // StatSpinStruct sums
+    if (tr) {
+        b += W * (N0 * Nexc + Nmax) * es;    // overlap rows GupT and g
+        b += W * (2 * Ns + 2 * Nmax) * 2;    // wavefunction Fock state
+        b += W * 2 * Nexc * Nexc * 16;       // ProjHeis H and O sums
+    }
     *bytes = b;
     return GV_OK;
 }
@@ -359,8 +612,10 @@ gv_status gv_job_create(const gv_job_config* cfg, gv_job** out)
     j->lat = make_square_lattice(L);
     j->orb = make_orbitals(L, cfg->phase_shift[0], cfg->phase_shift[1]);
     if (!j->orb.ok) { delete j; return GV_ERR_INVALID; }
-    j->ch = make_channel(j->orb, 0, cfg->q[0], cfg->q[1]);
+    j->ch = make_channel(j->orb, cfg->channel, cfg->q[0], cfg->q[1]);
     if (!j->ch.ok) { delete j; return GV_ERR_INVALID; }
+    j->trans = cfg->channel == GV_CH_TRANS;
+    if (j->trans && !trans_tables(j->ch, j->exu, j->exd)) { delete j; return GV_ERR_INVALID; }
     j->Ns = L * L;
     j->Nk = j->orb.Nk;
     j->N[0] = j->ch.N[0];
@@ -416,7 +671,7 @@ gv_status gv_job_create(const gv_job_config* cfg, gv_job** out)
     if (cudaEventCreate(&j->ev0) != cudaSuccess || cudaEventCreate(&j->ev1) != cudaSuccess) return fail(GV_ERR_CUDA);
 
     DevJob& d = j->d;
-    d.L = L; d.Ns = j->Ns; d.Nk = j->Nk; d.Nexc = 1; d.W = j->W;
+    d.L = L; d.Ns = j->Ns; d.Nk = j->Nk; d.Nexc = j->ch.Nexc; d.W = j->W;
     d.N[0] = j->N[0]; d.N[1] = j->N[1]; d.Nmax = j->Nmax;
     d.precision = cfg->precision; d.channel = cfg->channel;
     d.seed = cfg->seed; d.walker_base = cfg->walker_base; d.reinv_every = cfg->reinv_every;
@@ -454,6 +709,27 @@ gv_status gv_job_create(const gv_job_config* cfg, gv_job** out)
         return fail(st);
     d.nbr = nbr; d.edges = reinterpret_cast<const int4*>(edg); d.phase64 = p64; d.phase32 = p32; d.coef64 = c64; d.coef32 = c32;
     d.Ai[0] = a0; d.Ai[1] = a1;
+    d.worb = nullptr; d.wslot = nullptr; d.exc_up = nullptr; d.exc_dn = nullptr; d.cur = nullptr; d.wsign = nullptr;
+    d.sigma = nullptr; d.gup = nullptr; d.gdn = nullptr; d.pjx = nullptr;
+    if (j->trans) {
+        const int Nexc = j->ch.Nexc;
+        int16_t *eu = nullptr, *ed = nullptr;
+        if ((st = dalloc(j, &d.worb, size_t(j->W) * 2 * j->Nmax * sizeof(int16_t))) ||
+            (st = dalloc(j, &d.wslot, size_t(j->W) * 2 * j->Ns * sizeof(int16_t))) ||
+            (st = dalloc(j, &eu, size_t(Nexc) * sizeof(int16_t))) ||
+            (st = dalloc(j, &ed, size_t(Nexc) * sizeof(int16_t))) ||
+            (st = dalloc(j, &d.cur, size_t(j->W) * sizeof(int32_t))) ||
+            (st = dalloc(j, &d.wsign, size_t(j->W) * sizeof(int32_t))) ||
+            (st = dalloc(j, &d.sigma, size_t(j->W) * sizeof(double))) ||
+            (st = dalloc(j, &d.gup, size_t(j->W) * j->N[0] * Nexc * es)) ||
+            (st = dalloc(j, &d.gdn, size_t(j->W) * j->Nmax * es)) ||
+            (st = dalloc(j, &d.pjx, size_t(j->W) * 2 * Nexc * Nexc * sizeof(cx<double>))))
+            return fail(st);
+        d.exc_up = eu; d.exc_dn = ed;
+        if (cudaMemcpyAsync(eu, j->exu.data(), Nexc * sizeof(int16_t), cudaMemcpyHostToDevice, j->stream) ||
+            cudaMemcpyAsync(ed, j->exd.data(), Nexc * sizeof(int16_t), cudaMemcpyHostToDevice, j->stream))
+            return fail(GV_ERR_CUDA);
+    }
     if (cudaMemcpyAsync(nbr, j->lat.nbr.data(), sizeof(int32_t) * 4 * j->Ns, cudaMemcpyHostToDevice, j->stream) ||
         cudaMemcpyAsync(edg, edges.data(), edges.size() * sizeof(int32_t), cudaMemcpyHostToDevice, j->stream) ||
         cudaMemcpyAsync(p64, ph64.data(), ph64.size() * sizeof(cx<double>), cudaMemcpyHostToDevice, j->stream) ||
@@ -487,7 +763,7 @@ gv_status gv_job_dims(const gv_job* j, int32_t* Ns, int32_t* Nup, int32_t* Ndn, 
     if (Ns) *Ns = j->Ns;
     if (Nup) *Nup = j->N[0];
     if (Ndn) *Ndn = j->N[1];
-    if (Nexc) *Nexc = 1;
+    if (Nexc) *Nexc = j->ch.Nexc;
     return GV_OK;
 }
 
@@ -506,6 +782,8 @@ static gv_status reset_quantities(gv_job* j)
     GV_CK(cudaMemsetAsync(j->d.sm_n, 0, sizeof(int32_t) * j->W, j->stream));
     GV_CK(cudaMemsetAsync(j->d.ss, 0, sizeof(double) * 10 * j->Ns * j->Ns, j->stream));
     GV_CK(cudaMemsetAsync(j->d.ss_n, 0, sizeof(int32_t), j->stream));
+    if (j->trans)
+        GV_CK(cudaMemsetAsync(j->d.pjx, 0, sizeof(cx<double>) * 2 * size_t(j->W) * j->ch.Nexc * j->ch.Nexc, j->stream));
     return GV_OK;
 }
 
@@ -521,7 +799,9 @@ gv_status gv_job_measure(gv_job* j)
     if (!j->ready) return GV_ERR_NOT_READY;
     const int mask = j->cfg.meas_mask;
     gv_status st = GV_OK;
-    if (mask & (GV_MEAS_PROJHEIS | GV_MEAS_STAGMAGN)) st = walk_dispatch(j, 0, 0, 1, mask & ~GV_MEAS_STATSPIN, 1);
+    if (mask & (GV_MEAS_PROJHEIS | GV_MEAS_STAGMAGN))
+        st = j->trans ? measure_trans_dispatch(j, mask & ~GV_MEAS_STATSPIN)
+                      : walk_dispatch(j, 0, 0, 1, mask & ~GV_MEAS_STATSPIN, 1);
     if (!st && (mask & GV_MEAS_STATSPIN)) st = statspin_dispatch(j);
     return st ? st : gv_job_synchronize(j);
 }
@@ -560,7 +840,17 @@ gv_status gv_job_init_walkers(gv_job* j, const int8_t* up)
     GV_CK(cudaMemsetAsync(j->d.checks, 0, sizeof(unsigned long long) * W, j->stream));
     GV_CK(cudaMemsetAsync(j->d.drift_seen, 0, sizeof(double) * W, j->stream));
     // vmc.cpp:221-241: up to 10 random starts until the amplitude is non-zero.
+    // The mixed-precision exciton job also redraws a start whose inverse in the
+    // picked channel state has an entry above kMixedMaxInverse: such a
+    // configuration's amplitude is many orders below its neighbours', and its
+    // FP32 ratios would overflow or cancel to noise on the first step.
+    const bool screen = j->trans && j->cfg.precision == GV_PREC_MIXED && !up;
+    std::vector<double> amax(W);
     for (int attempt = 0; attempt < 10; ++attempt) {
+        if (j->trans) {   // every walker starts in channel state 0
+            gv_status st = upload_wav(j, std::vector<WavHost>(W, wav_state0(j)));
+            if (st) return st;
+        }
         gv_status st = upload_configs(j, cfg);
         if (st) return st;
         st = invert_all(j);
@@ -570,6 +860,16 @@ gv_status gv_job_init_walkers(gv_job* j, const int8_t* up)
         bool again = false;
         for (int w = 0; w < W; ++w)
             if (status[w] == GV_ERR_SINGULAR && !up) { ran_init(j, w, &cfg[size_t(w) * Ns]); again = true; }
+        if (!again && j->trans) {
+            for (int w = 0; w < W; ++w)
+                if (status[w] != GV_OK) { j->ready = true; return status[w]; }
+            if ((st = trans_start(j))) return st;
+            if (screen) {
+                if ((st = inverse_max_abs(j, amax.data()))) return st;
+                for (int w = 0; w < W; ++w)
+                    if (!(amax[w] <= kMixedMaxInverse)) { ran_init(j, w, &cfg[size_t(w) * Ns]); again = true; }
+            }
+        }
         if (!again) break;
         if (attempt == 9) return GV_ERR_SINGULAR;
         GV_CK(cudaMemsetAsync(j->d.status, 0, sizeof(int32_t) * W, j->stream));
@@ -577,7 +877,7 @@ gv_status gv_job_init_walkers(gv_job* j, const int8_t* up)
     for (int w = 0; w < W; ++w)
         if (status[w] != GV_OK) { j->ready = true; return status[w]; }
     j->ready = true;
-    return GV_OK;
+    return j->trans ? gv_job_synchronize(j) : GV_OK;
 }
 
 static gv_status walk_impl(gv_job* j, uint64_t len, uint64_t meas, gv_trace* dtrace, int trace_walker)
@@ -594,19 +894,29 @@ static gv_status walk_impl(gv_job* j, uint64_t len, uint64_t meas, gv_trace* dtr
     }
     GV_CK(cudaEventRecord(j->ev0, j->stream));
     gv_status st = GV_OK;
-    if (!(mask & GV_MEAS_STATSPIN)) {
-        st = walk_dispatch(j, len, 0, meas, mask);
+    const int inner = mask & ~GV_MEAS_STATSPIN;
+    if (!(mask & GV_MEAS_STATSPIN) && !(j->trans && mask)) {
+        st = j->trans ? walk_trans_dispatch(j, len) : walk_dispatch(j, len, 0, meas, mask);
     } else {
-        // Split at the measurement points: steps [a, b) then measure after b-1.
+        // Split at the measurement points: steps [a, m] then measure after step m.
         uint64_t a = 0;
         while (a < len && !st) {
             uint64_t m = (a == 0) ? 0 : ((a + meas - 1) / meas) * meas;   // next s with s % meas == 0, s >= a
             if (j->d.trace) j->d.trace = dtrace + a;
-            if (m >= len) { st = walk_dispatch(j, len - a, a, 0, 0); a = len; break; }
-            // run steps a..m (inclusive) with in-kernel ProjHeis/StagMagnZ at m
+            if (m >= len) {
+                st = j->trans ? walk_trans_dispatch(j, len - a) : walk_dispatch(j, len - a, a, 0, 0);
+                a = len;
+                break;
+            }
             const uint64_t nsteps = m - a + 1;
-            st = walk_dispatch(j, nsteps, a, meas, mask & ~GV_MEAS_STATSPIN);
-            if (!st) st = statspin_dispatch(j);
+            if (j->trans) {
+                st = walk_trans_dispatch(j, nsteps);
+                if (!st && inner) st = measure_trans_dispatch(j, inner);
+            } else {
+                // ground state: ProjHeis / StagMagnZ inside the walk kernel at step m
+                st = walk_dispatch(j, nsteps, a, meas, inner);
+            }
+            if (!st && (mask & GV_MEAS_STATSPIN)) st = statspin_dispatch(j);
             a = m + 1;
         }
         j->d.trace = dtrace;
@@ -641,6 +951,7 @@ gv_status gv_job_synchronize(gv_job* j)
     GV_CK(cudaStreamSynchronize(j->stream));
     float ms = 0;
     if (cudaEventElapsedTime(&ms, j->ev0, j->ev1) == cudaSuccess) j->last_ms = ms;
+    else cudaGetLastError();   // no walk recorded yet: clear the (non-sticky) error
     std::vector<int32_t> status(j->W);
     GV_CK(cudaMemcpy(status.data(), j->d.status, sizeof(int32_t) * j->W, cudaMemcpyDeviceToHost));
     for (int32_t s : status)
@@ -731,13 +1042,14 @@ gv_status gv_job_drift(gv_job* j, double* out)
     if (!e) e = cudaMemcpyAsync(out, d, sizeof(double) * 2 * j->W, cudaMemcpyDeviceToHost, j->stream);
     if (!e) e = cudaStreamSynchronize(j->stream);
     cudaFree(d);
-    return e ? GV_ERR_CUDA : GV_OK;
+    return cuda_status(e);
 }
 
 gv_status gv_job_virt_update(gv_job* j, int32_t walker, int32_t nset, const int32_t* hops, double* out)
 {
     if (!j || !hops || !out || walker < 0 || walker >= j->W || nset < 0) return GV_ERR_INVALID;
     if (!j->ready) return GV_ERR_NOT_READY;
+    if (j->trans) return virt_update_trans(j, walker, nset, hops, out);
     if (nset == 0) return GV_OK;
     for (int i = 0; i < 4 * nset; ++i)
         if (hops[i] < -1 || hops[i] >= j->Ns) return GV_ERR_INVALID;
@@ -758,7 +1070,7 @@ gv_status gv_job_virt_update(gv_job* j, int32_t walker, int32_t nset, const int3
     if (!e) e = cudaStreamSynchronize(j->stream);
     cudaFree(dh);
     cudaFree(dout);
-    return e ? GV_ERR_CUDA : GV_OK;
+    return cuda_status(e);
 }
 
 gv_status gv_job_read_config(gv_job* j, int8_t* up)
@@ -788,9 +1100,11 @@ gv_status gv_job_read_amplitude(gv_job* j, double* mant, int32_t* exp10)
     if (!j || !mant || !exp10) return GV_ERR_INVALID;
     GV_CK(cudaStreamSynchronize(j->stream));
     std::vector<cx<double>> m(j->W);
-    std::vector<int32_t> e(j->W);
+    std::vector<int32_t> e(j->W), sg(j->W, 1);
     GV_CK(cudaMemcpy(m.data(), j->d.amp_m, sizeof(cx<double>) * j->W, cudaMemcpyDeviceToHost));
     GV_CK(cudaMemcpy(e.data(), j->d.amp_e, sizeof(int32_t) * j->W, cudaMemcpyDeviceToHost));
+    if (j->trans) GV_CK(cudaMemcpy(sg.data(), j->d.wsign, sizeof(int32_t) * j->W, cudaMemcpyDeviceToHost));
+    for (int w = 0; w < j->W; ++w) m[w] = m[w] * double(sg[w]);   // SlaterDeterminant::Amp (SlaterDeterminant.cpp:94)
     for (int w = 0; w < j->W; ++w) {
         const double a = std::hypot(m[w].x, m[w].y);
         if (a == 0.0) { mant[2 * w] = mant[2 * w + 1] = 0.0; exp10[w] = 0; continue; }
@@ -836,7 +1150,12 @@ gv_status gv_job_read_counts(gv_job* j, uint64_t* counts)
 gv_status gv_job_read_state_index(gv_job* j, int32_t* state)
 {
     if (!j || !state) return GV_ERR_INVALID;
-    for (int w = 0; w < j->W; ++w) state[w] = 0;
+    if (!j->trans) {
+        for (int w = 0; w < j->W; ++w) state[w] = 0;
+        return GV_OK;
+    }
+    GV_CK(cudaStreamSynchronize(j->stream));
+    GV_CK(cudaMemcpy(state, j->d.cur, sizeof(int32_t) * j->W, cudaMemcpyDeviceToHost));
     return GV_OK;
 }
 
@@ -844,8 +1163,47 @@ gv_status gv_job_read_projheis(gv_job* j, double* vals, int32_t* nmeas)
 {
     if (!j || !vals) return GV_ERR_INVALID;
     GV_CK(cudaStreamSynchronize(j->stream));
-    GV_CK(cudaMemcpy(vals, j->d.pj, sizeof(cx<double>) * 2 * j->W, cudaMemcpyDeviceToHost));
+    if (j->trans)
+        GV_CK(cudaMemcpy(vals, j->d.pjx, sizeof(cx<double>) * 2 * size_t(j->W) * j->ch.Nexc * j->ch.Nexc,
+                         cudaMemcpyDeviceToHost));
+    else
+        GV_CK(cudaMemcpy(vals, j->d.pj, sizeof(cx<double>) * 2 * j->W, cudaMemcpyDeviceToHost));
     if (nmeas) GV_CK(cudaMemcpy(nmeas, j->d.pj_n, sizeof(int32_t) * j->W, cudaMemcpyDeviceToHost));
+    return GV_OK;
+}
+
+gv_status gv_job_read_orbitals(gv_job* j, int32_t walker, int32_t fl, int32_t* orb)
+{
+    if (!j || !orb || walker < 0 || walker >= j->W || fl < 0 || fl > 1) return GV_ERR_INVALID;
+    if (!j->trans) {
+        for (int f = 0; f < j->N[fl]; ++f) orb[f] = 2 * f;
+        return GV_OK;
+    }
+    GV_CK(cudaStreamSynchronize(j->stream));
+    std::vector<int16_t> o(j->Nmax);
+    GV_CK(cudaMemcpy(o.data(), j->d.worb + (size_t(walker) * 2 + fl) * j->Nmax, sizeof(int16_t) * j->Nmax,
+                     cudaMemcpyDeviceToHost));
+    for (int f = 0; f < j->N[fl]; ++f) orb[f] = o[f];
+    return GV_OK;
+}
+
+gv_status gv_job_read_status(gv_job* j, int32_t* status)
+{
+    if (!j || !status) return GV_ERR_INVALID;
+    GV_CK(cudaStreamSynchronize(j->stream));
+    GV_CK(cudaMemcpy(status, j->d.status, sizeof(int32_t) * j->W, cudaMemcpyDeviceToHost));
+    return GV_OK;
+}
+
+gv_status gv_job_read_weight(gv_job* j, double* sigma)
+{
+    if (!j || !sigma) return GV_ERR_INVALID;
+    if (!j->trans) {
+        for (int w = 0; w < j->W; ++w) sigma[w] = 1.0;
+        return GV_OK;
+    }
+    GV_CK(cudaStreamSynchronize(j->stream));
+    GV_CK(cudaMemcpy(sigma, j->d.sigma, sizeof(double) * j->W, cudaMemcpyDeviceToHost));
     return GV_OK;
 }
 

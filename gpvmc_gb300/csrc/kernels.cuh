@@ -32,6 +32,23 @@ __device__ __forceinline__ cx<T>* ai_ptr(const DevJob& J, int fl, int w)
 
 __device__ __forceinline__ int sublattice(int s, int L) { return ((s % L) + (s / L)) & 1; }
 
+// Orbital held by Slater row f of flavour fl: the ground state fills the
+// lower band in order (orbital 2f); the exciton channel keeps a per-walker
+// table, read from `worb` ([fl][Nmax], a shared-memory copy) when given.
+__device__ __forceinline__ int row_orbital(const DevJob& J, const int16_t* worb, int w, int fl, int f)
+{
+    if (worb) return worb[fl * J.Nmax + f];
+    if (J.worb) return J.worb[(size_t(w) * 2 + fl) * J.Nmax + f];
+    return 2 * f;
+}
+
+// phi_o(s) = phase[s][o/2] * coef[sub(s)][o] (coef_fl: [sub][Ns] for one flavour).
+template <typename T>
+__device__ __forceinline__ cx<T> phi_orb(const cx<T>* phase, const cx<T>* coef_fl, int Nk, int Ns, int L, int s, int o)
+{
+    return cmul_rn(phase[size_t(s) * Nk + (o >> 1)], coef_fl[size_t(sublattice(s, L)) * Ns + o]);
+}
+
 template <typename T>
 __device__ __forceinline__ cx<T> warp_sum(cx<T> v)
 {
@@ -171,7 +188,7 @@ __device__ bool gj_invert(cx<double>* M, int N, const GJSmem& S, cx<double>& det
 // (base-10 exponent < -8, SlaterDeterminant.cpp:78-81).
 template <typename T, int NT>
 __device__ __noinline__ int reinvert_walker(const DevJob& J, int w, cx<double>* M, const GJSmem& S,
-                                            const int16_t* part_s)
+                                            const int16_t* part_s, const int16_t* worb_s = nullptr)
 {
     const int tid = threadIdx.x;
     cx<double> am = {1.0, 0.0};
@@ -183,8 +200,8 @@ __device__ __noinline__ int reinvert_walker(const DevJob& J, int w, cx<double>* 
         const cx<double>* coef = J.coef64 + (size_t(w) * 2 + fl) * 2 * J.Ns;
         for (int idx = tid; idx < N * N; idx += NT) {
             const int r = idx / N, f = idx % N;
-            const int s = part[r];
-            M[idx] = cmul_rn(J.phase64[size_t(s) * J.Nk + f], coef[size_t(sublattice(s, J.L)) * J.Ns + 2 * f]);
+            const int s = part[r], o = row_orbital(J, worb_s, w, fl, f);
+            M[idx] = cmul_rn(J.phase64[size_t(s) * J.Nk + (o >> 1)], coef[size_t(sublattice(s, J.L)) * J.Ns + o]);
         }
         __syncthreads();
         cx<double> dm;
@@ -216,6 +233,52 @@ __device__ __noinline__ int reinvert_walker(const DevJob& J, int w, cx<double>* 
     return status;
 }
 
+// Exciton channel: rebuild the overlap rows of a freshly inverted walker,
+//   GupT[f][k] = sum_p phi_{exc_up[k]}(x_p) (A0^-1)(p, f)   (every candidate upper orbital)
+//   g[f]       = sum_p phi_{exc_dn[cur]}(x_p) (A1^-1)(p, f) (the hole orbital of `cur`)
+// from the stored inverses, in the walk precision.  These are the
+// R A^-1 products of linalg::DetUpdate / InvUpdate (linalg.cpp:107-573) for
+// every row a channel-state hop can bring in: with them a proposal costs one
+// Nexc x N0 product instead of the reference's full A^-1 C and R (A^-1 C)
+// per step.  The FP64 re-inversion scratch holds Phi[p][k] meanwhile.
+template <typename T, int NT>
+__device__ __noinline__ void trans_rebuild(const DevJob& J, int w, const int16_t* part_s, int cur)
+{
+    constexpr int NW = NT / 32;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int N0 = J.N[0], N1 = J.N[1], Nexc = J.Nexc, Ns = J.Ns, Nk = J.Nk, L = J.L;
+    const int16_t* part0 = part_s ? part_s : J.part + size_t(w) * 2 * J.Nmax;
+    const int16_t* part1 = part0 + J.Nmax;
+    const cx<T>* phase = Tab<T>::phase(J);
+    const cx<T>* cf0 = Tab<T>::coef(J) + size_t(w) * 4 * Ns;
+    const cx<T>* cf1 = cf0 + 2 * Ns;
+    cx<T>* Phi = reinterpret_cast<cx<T>*>(J.scratch64 + size_t(w) * J.Nmax * J.Nmax);
+    for (int idx = tid; idx < N0 * Nexc; idx += NT) {
+        const int p = idx / Nexc, k = idx % Nexc;
+        Phi[idx] = phi_orb<T>(phase, cf0, Nk, Ns, L, part0[p], J.exc_up[k]);
+    }
+    __syncthreads();
+    const cx<T>* A0 = ai_ptr<T>(J, 0, w);
+    cx<T>* G = static_cast<cx<T>*>(J.gup) + size_t(w) * N0 * Nexc;
+    for (int idx = tid; idx < N0 * Nexc; idx += NT) {
+        const int f = idx / Nexc, k = idx % Nexc;
+        cx<T> acc = {T(0), T(0)};
+        for (int p = 0; p < N0; ++p) cmac(acc, Phi[size_t(p) * Nexc + k], A0[size_t(f) * N0 + p]);
+        G[idx] = acc;
+    }
+    const int hole = J.exc_dn[cur];
+    const cx<T>* A1 = ai_ptr<T>(J, 1, w);
+    cx<T>* g = static_cast<cx<T>*>(J.gdn) + size_t(w) * J.Nmax;
+    for (int f = warp; f < N1; f += NW) {
+        cx<T> acc = {T(0), T(0)};
+        for (int p = lane; p < N1; p += 32)
+            cmac(acc, phi_orb<T>(phase, cf1, Nk, Ns, L, part1[p], hole), A1[size_t(f) * N1 + p]);
+        acc = warp_sum(acc);
+        if (lane == 0) g[f] = acc;
+    }
+    __syncthreads();
+}
+
 // Initial inversion / re-inversion of every walker (only_due: only walkers
 // whose accepted-move count reached reinv_every, the deferred cadence).
 template <typename T, int NT>
@@ -231,6 +294,7 @@ __global__ void __launch_bounds__(NT) k_invert(DevJob J, int only_due)
     GJSmem S = carve_gj<NT>(p, J.Nmax);
     cx<double>* M = J.scratch64 + size_t(w) * J.Nmax * J.Nmax;
     const int st = reinvert_walker<T, NT>(J, w, M, S, nullptr);
+    if (J.channel == GV_CH_TRANS && st == GV_OK) trans_rebuild<T, NT>(J, w, nullptr, J.cur[w]);
     if (threadIdx.x == 0) {
         J.status[w] = st;
         if (only_due) { J.since_reinv[w] = 0; J.counts[size_t(w) * 5 + 4] += 1; }
@@ -787,20 +851,26 @@ __global__ void __launch_bounds__(NT, 768 / NT) k_walk_gs(DevJob J, uint64_t nst
     }
 }
 
-// Ratio of moving particle c of flavour fl to site d (one warp, lanes over rows).
+// Ratio of moving particle c of flavour fl to site d (one warp, lanes over
+// rows); row f's orbital has phase column pcol_fl[f] and coefficients
+// coef_fl[sub][f].
 template <typename T>
 __device__ __forceinline__ cx<T> warp_ratio(const DevJob& J, const cx<T>* A, const cx<T>* phase,
-                                            const cx<T>* coef_fl, int N, int c, int d)
+                                            const cx<T>* coef_fl, const int16_t* pcol_fl, int N, int c, int d)
 {
     const int lane = threadIdx.x & 31;
+    const int sub = sublattice(d, J.L);
     cx<T> acc = {T(0), T(0)};
-    for (int f = lane; f < N; f += 32) cmac(acc, A[size_t(f) * N + c], phi_row<T>(phase, coef_fl, J.Nk, J.Nmax, J.L, d, f));
+    for (int f = lane; f < N; f += 32)
+        cmac(acc, A[size_t(f) * N + c], cmul_rn(phase[size_t(d) * J.Nk + pcol_fl[f]], coef_fl[sub * J.Nmax + f]));
     return warp_sum(acc);
 }
 
 // StatSpinStruct (StatSpinStruct.cpp:16-135), two flavours: for every pair
 // i <= j, szz +-1/4 and, for antiparallel pairs, s-+ / s+- -= the swap ratio
-// r_up(p_i -> j) r_dn(q_j -> i) (the reference's conj(amp) swamp / w).
+// r_up(p_i -> j) r_dn(q_j -> i) (the reference's conj(amp) swamp / w).  In the
+// exciton channel the swap keeps the channel state and w is the weight over
+// all states, so the ratio is divided by sigma = w / |Amp|^2.
 template <typename T, int NT>
 __global__ void __launch_bounds__(NT) k_statspin(DevJob J)
 {
@@ -814,11 +884,16 @@ __global__ void __launch_bounds__(NT) k_statspin(DevJob J)
     const cx<T>* cg = Tab<T>::coef(J) + size_t(w) * 4 * Ns;
     extern __shared__ __align__(16) char smem[];
     cx<T>* coef = reinterpret_cast<cx<T>*>(smem);
+    int16_t* pcol = reinterpret_cast<int16_t*>(coef + 4 * Nmax);
     for (int i = tid; i < 4 * Nmax; i += NT) {
         const int fl = i / (2 * Nmax), sub = (i / Nmax) & 1, f = i % Nmax;
-        coef[i] = cg[(size_t(fl) * 2 + sub) * Ns + 2 * f];
+        const int o = f < J.N[fl] ? row_orbital(J, nullptr, w, fl, f) : 0;
+        coef[i] = cg[(size_t(fl) * 2 + sub) * Ns + o];
+        if (!sub) pcol[fl * Nmax + f] = int16_t(o >> 1);
     }
     __syncthreads();
+    const bool scaled = J.channel == GV_CH_TRANS;
+    const double inv_sigma = scaled ? 1.0 / J.sigma[w] : 1.0;
     const cx<T>* A0 = ai_ptr<T>(J, 0, w);
     const cx<T>* A1 = ai_ptr<T>(J, 1, w);
     double* szz = J.ss;
@@ -842,10 +917,11 @@ __global__ void __launch_bounds__(NT) k_statspin(DevJob J)
             continue;
         }
         const int upf = ui ? vi : vj, upt = ui ? vj : vi;
-        const cx<T> ru = warp_ratio<T>(J, A0, phase, coef, J.N[0], fock[upf], upt);
-        const cx<T> rd = warp_ratio<T>(J, A1, phase, coef + 2 * Nmax, J.N[1], fock[Ns + upt], upf);
+        const cx<T> ru = warp_ratio<T>(J, A0, phase, coef, pcol, J.N[0], fock[upf], upt);
+        const cx<T> rd = warp_ratio<T>(J, A1, phase, coef + 2 * Nmax, pcol + Nmax, J.N[1], fock[Ns + upt], upf);
         if (lane == 0) {
-            const cx<double> r = to_d(ru) * to_d(rd);
+            cx<double> r = to_d(ru) * to_d(rd);
+            if (scaled) r = r * inv_sigma;
             atomicAdd(&szz[2 * ij], -0.25);
             atomicAdd(&szz[2 * ji], -0.25);
             double* a = ui ? smp : spm;   // vi up: s-+[ij], s+-[ji]; vi down: s+-[ij], s-+[ji]
@@ -891,8 +967,9 @@ __global__ void __launch_bounds__(NT) k_check_reinvert(DevJob J, double threshol
             for (int idx = tid; idx < NR * N; idx += NT) {
                 const int i = idx / N, p = idx % N;
                 const int site = part[p];
-                arow[i * Nmax + p] = cmul_rn(J.phase64[size_t(site) * J.Nk + rows[i]],
-                                             coef[size_t(sublattice(site, J.L)) * Ns + 2 * rows[i]]);
+                const int o = row_orbital(J, nullptr, w, fl, rows[i]);
+                arow[i * Nmax + p] = cmul_rn(J.phase64[size_t(site) * J.Nk + (o >> 1)],
+                                             coef[size_t(sublattice(site, J.L)) * Ns + o]);
             }
             __syncthreads();
             for (int g = warp; g < N; g += NW) {
@@ -926,6 +1003,7 @@ __global__ void __launch_bounds__(NT) k_check_reinvert(DevJob J, double threshol
         GJSmem S = carve_gj<NT>(gp, Nmax);
         cx<double>* M = J.scratch64 + size_t(w) * Nmax * Nmax;
         const int st = reinvert_walker<T, NT>(J, w, M, S, nullptr);
+        if (J.channel == GV_CH_TRANS && st == GV_OK) trans_rebuild<T, NT>(J, w, nullptr, J.cur[w]);
         if (tid == 0) { J.status[w] = st; J.counts[size_t(w) * 5 + 4] += 1; }
     } else if (tid == 0) {
         J.checks[w] += 1;
@@ -985,7 +1063,8 @@ __global__ void __launch_bounds__(NT) k_drift(DevJob J, double* out)
         cx<double> s = {0.0, 0.0};
         for (int pr = 0; pr < N; ++pr) {
             const int site = part[pr];
-            const cx<double> a = cmul_rn(J.phase64[size_t(site) * J.Nk + f], coef[size_t(sublattice(site, J.L)) * Ns + 2 * f]);
+            const int o = row_orbital(J, nullptr, w, fl, f);
+            const cx<double> a = cmul_rn(J.phase64[size_t(site) * J.Nk + (o >> 1)], coef[size_t(sublattice(site, J.L)) * Ns + o]);
             cmac(s, a, to_d(A[size_t(g) * N + pr]));
         }
         if (f == g) s.x -= 1.0;

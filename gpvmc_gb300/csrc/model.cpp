@@ -180,6 +180,8 @@ Channel make_channel(const Orbitals& o, int kind, int qx, int qy)
             su[2 * fe + 1] = 1;
             occ[0].push_back(su);
             occ[1].push_back(sd);
+            ch.exc_up.push_back(2 * fe + 1);
+            ch.exc_dn.push_back(hole);
         }
     } else {
         return ch;

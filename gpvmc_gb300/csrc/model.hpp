@@ -63,6 +63,8 @@ struct Channel {
     int Nexc = 0;
     std::vector<int32_t> fock0[2];        // state 0 Fock vectors: orbital -> particle or N
     std::vector<int32_t> hop_from, hop_to; // (a*Nexc + b)*2 + fl
+    // transverse exciton: flavour-0 upper-band orbital and flavour-1 hole of state k
+    std::vector<int32_t> exc_up, exc_dn;
     bool ok = false;
 };
 Channel make_channel(const Orbitals& o, int kind, int qx, int qy);

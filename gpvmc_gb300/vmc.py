@@ -254,9 +254,39 @@ class Job:
         check(_lib.lib().gv_job_read_counts(self._h, _p(out)), "gv_job_read_counts")
         return out.reshape(self.walkers, 5)
 
+    def orbitals(self, walker, fl):
+        """Orbital of every Slater row of the walker's wavefunction Fock state."""
+        out = np.zeros(self.N[fl], dtype=np.int32)
+        check(_lib.lib().gv_job_read_orbitals(self._h, walker, fl, _p(out)), "gv_job_read_orbitals")
+        return out
+
+    def status(self):
+        """Per-walker status codes (0 = running)."""
+        out = np.zeros(self.walkers, dtype=np.int32)
+        check(_lib.lib().gv_job_read_status(self._h, _p(out)), "gv_job_read_status")
+        return out
+
+    def state_index(self):
+        """WaveFunction::m_c_exc of every walker (0 for the ground state)."""
+        out = np.zeros(self.walkers, dtype=np.int32)
+        check(_lib.lib().gv_job_read_state_index(self._h, _p(out)), "gv_job_read_state_index")
+        return out
+
+    def weight(self):
+        """LatticeStepper weight over |Amp|^2 per walker: sum_k |q_k / Amp|^2 (1 for the ground state)."""
+        out = np.zeros(self.walkers)
+        check(_lib.lib().gv_job_read_weight(self._h, _p(out)), "gv_job_read_weight")
+        return out
+
     def projheis(self):
-        vals = np.zeros(4 * self.walkers)
+        """Ground state: [E/site sum, count] per walker, shape (walkers, 2).  Exciton
+        channel: m_vals = [H; O] per walker, shape (walkers, 2*Nexc, Nexc)."""
         n = np.zeros(self.walkers, dtype=np.int32)
+        if self.Nexc > 1:
+            vals = np.zeros(4 * self.walkers * self.Nexc * self.Nexc)
+            check(_lib.lib().gv_job_read_projheis(self._h, _p(vals), _p(n)), "gv_job_read_projheis")
+            return (vals[0::2] + 1j * vals[1::2]).reshape(self.walkers, 2 * self.Nexc, self.Nexc), n
+        vals = np.zeros(4 * self.walkers)
         check(_lib.lib().gv_job_read_projheis(self._h, _p(vals), _p(n)), "gv_job_read_projheis")
         return (vals[0::2] + 1j * vals[1::2]).reshape(self.walkers, 2), n
 
@@ -329,7 +359,7 @@ class ProjHeis(Quantity):
 
     def save(self):
         v, n = self._read()
-        return v / np.maximum(n, 1)[:, None]
+        return v / np.maximum(n, 1).reshape((-1,) + (1,) * (v.ndim - 1))
 
 
 class StagMagnZ(Quantity):

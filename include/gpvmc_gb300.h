@@ -168,7 +168,18 @@ gv_status gv_job_read_inverse(gv_job* job, int32_t walker, int32_t fl, double* o
 /* counts[w*5 + i]: steps, accepted exchanges, accepted no-ops, rejections,
  * re-inversions. */
 gv_status gv_job_read_counts(gv_job* job, uint64_t* counts);
+/* The wavefunction's Fock state of one walker and flavour (State::m_part):
+ * orb[f] = orbital held by Slater row f (N[fl] entries; ground state: 2f). */
+gv_status gv_job_read_orbitals(gv_job* job, int32_t walker, int32_t fl, int32_t* orb);
+/* Status of every walker (GV_OK, or the error that stopped it; a stopped
+ * walker takes no further steps until gv_job_init_walkers). */
+gv_status gv_job_read_status(gv_job* job, int32_t* status /* n_walkers */);
+/* WaveFunction::m_c_exc: current channel state of every walker (0 for the
+ * ground state). */
 gv_status gv_job_read_state_index(gv_job* job, int32_t* state /* n_walkers */);
+/* LatticeStepper's weight (LatticeStepper.cpp:149-169) over |Amp()|^2 per
+ * walker: sum over channel states k of |q_k / Amp()|^2 (1 for the ground state). */
+gv_status gv_job_read_weight(gv_job* job, double* sigma /* n_walkers */);
 /* Quantity sums since the last measuring walk began, per walker:
  * ProjHeis m_vals (2*Nexc*Nexc complex per walker; for the ground state
  * [E*L^2-normalised sum, count]), StagMagnZ (1 complex per walker), and the
@@ -211,6 +222,11 @@ gv_status gv_phi_table(int32_t L, double phi, double neel, double neel_exp, cons
 gv_status gv_lattice_neighbours(int32_t L, int32_t* nbr);
 gv_status gv_channel_orbitals(int32_t L, const double* phase_shift, int32_t channel, const int32_t* q,
                               int32_t fl, int32_t* orb, int32_t* N, int32_t* Nexc);
+/* gv_channel_states: the channel's state table, exciton channel only
+ * (StagFluxTransExciton.cpp:7-44): state k adds orbital exc_up[k] to flavour
+ * 0 and removes orbital exc_dn[k] from flavour 1 (Nexc entries each). */
+gv_status gv_channel_states(int32_t L, const double* phase_shift, int32_t channel, const int32_t* q,
+                            int32_t* exc_up, int32_t* exc_dn);
 void gv_philox4x32_10(const uint32_t* ctr, const uint32_t* key, uint32_t* out);
 double gv_uniform_at(uint64_t seed, uint32_t walker, uint32_t stream, uint64_t k);
 
@@ -239,6 +255,9 @@ gv_status gv_slater_invert_noalloc(const double* d_A, double* d_Ai, int32_t N, d
 const char* gv_version(void);
 /* Message for a status code. */
 const char* gv_status_string(gv_status s);
+/* The CUDA runtime's message for the last CUDA error this thread's calls into
+ * the library met (behind a GV_ERR_CUDA / GV_ERR_OOM status), "" if none. */
+const char* gv_last_cuda_error(void);
 
 #ifdef __cplusplus
 }
