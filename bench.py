@@ -255,6 +255,116 @@ def run_e2e(g, precision, steps, rank):
             "includes": "job creation + start upload + FP64 LU start amortised over the steps"}
 
 
+# ---------------------------------------------------------------------------
+# Exciton channel: transverse exciton L=16, q = (n, n) for n = 0..7, 512 walkers
+# per momentum (N0 = 129, N1 = 127, Nexc = 128), ProjHeis H / O every sweep.
+
+EXC_QS = [(n, n) for n in range(8)]
+EXC_WALKERS = 512
+
+
+def _cpu_exciton_chain(args):
+    walker, sweeps = args
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    import oracle_lib as ol
+    q = EXC_QS[walker % len(EXC_QS)]
+    o = ol.OracleChain(L, 0.25 * math.pi, 0.1, channel=ol.TRANS, q=q, seed=SEED, walker=walker)
+    if o.random_start():
+        return 0, 0.0
+    t0 = time.perf_counter()
+    o.walk(SWEEP * sweeps, meas=SWEEP, mask=ol.MEAS_PROJHEIS)
+    return SWEEP * sweeps, time.perf_counter() - t0
+
+
+def cpu_exciton_baseline(cores, sweeps):
+    subprocess.run(["make", "-s", "-C", os.path.join(ROOT, "oracle"), "all"], check=True)
+    with mp.get_context("spawn").Pool(cores) as pool:
+        res = pool.map(_cpu_exciton_chain, [(w, sweeps) for w in range(cores)])
+    rates = [r[0] / r[1] for r in res if r[1] > 0]
+    return {"value": sum(rates), "unit": "steps/s", "cores": cores, "kind": "port", "per_core": statistics.mean(rates),
+            "sample": "%d independent exciton chains L=16 (q=(n,n) round robin), %d sweeps each with ProjHeis "
+                      "H/O per sweep" % (cores, sweeps)}
+
+
+def exciton_jobs(g, precision, walkers=EXC_WALKERS, qs=EXC_QS):
+    jobs = []
+    for i, q in enumerate(qs):
+        wav = g.StagFluxTransExciton(L, 0.25 * math.pi, 0.1, q=q)
+        kw = dict(reinv_every=REINV)
+        if precision == "mixed":
+            kw["drift_threshold"] = DRIFT_THRESHOLD
+        j = g.Job(wav, walkers=walkers, seed=SEED, precision=precision, walker_base=i * walkers, **kw)
+        j.set_measurements(1)
+        j.init_walkers()
+        jobs.append(j)
+    return jobs
+
+
+def run_exciton(g, sweeps, fp64_sweeps):
+    """All eight momenta at once (one stream per job), wall time between
+    synchronisations; the walk-kernel roofline from the q=(4,4) job alone."""
+    import numpy as np
+    out = {"workload": "transverse exciton L=16 (129x129 / 127x127 complex per spin, Nexc=128), "
+                       "q=(n,n) n=0..7, 512 walkers per q, ProjHeis H/O (128x128 each) every sweep",
+           "unit": "steps/s"}
+    for prec, n in (("mixed", sweeps), ("fp64", fp64_sweeps)):
+        jobs = exciton_jobs(g, prec)
+        for j in jobs:
+            j.walk(SWEEP, 0, sync=False)
+        for j in jobs:
+            j.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(n):
+            for j in jobs:
+                j.walk(SWEEP, SWEEP, sync=False)
+        for j in jobs:
+            j.synchronize()
+        wall = time.perf_counter() - t0
+        steps = len(jobs) * EXC_WALKERS * SWEEP * n
+        out[prec] = {"value": steps / wall, "sweeps": n, "wall_s": wall}
+        if prec == "mixed":
+            # single job, kernel-timed, for the walk kernel's roofline
+            j = jobs[4]
+            c0 = j.counts().sum(axis=0)
+            j.timer_start()
+            for _ in range(n):
+                j.walk(SWEEP, 0, sync=False)
+            ms, _ = j.timer_stop()
+            wk, wn = j.kernel_ms(0)
+            mk, mn = j.kernel_ms(2)
+            d = (j.counts().sum(axis=0) - c0).astype(float)
+            p_acc, p_ap = d[1] / d[0], (d[1] + d[3]) / d[0]
+            N0, N1, Nexc, sz = L * L // 2 + 1, L * L // 2 - 1, L * L // 2, 8
+            bytes_step = p_ap * (Nexc * N0 + N0 + N1 + Nexc) * sz + p_acc * 2 * (N0 * N0 + N1 * N1 + N0 * Nexc) * sz
+            achieved = bytes_step * d[0] / (wk * 1e-3) / 1e9
+            peak, kind = measured_peaks()
+            out["roofline"] = {"kernel": "k_walk_trans", "bound": "hbm", "achieved": achieved, "peak": peak,
+                               "unit": "GB/s", "frac": achieved / peak, "peak_kind": kind, "bytes_per_step": bytes_step,
+                               "walk_ms_per_sweep": wk / max(1, wn), "kernel_steps_per_s": d[0] / (wk * 1e-3),
+                               "p_acc": p_acc, "p_ap": p_ap, "q": [4, 4], "walkers": EXC_WALKERS}
+            # H / O accuracy of the mixed form against FP64 on the same configurations
+            cfg = j.config()
+            j.reset_quantities()
+            j.measure()
+            pm, _ = j.projheis()
+            ref = g.Job(g.StagFluxTransExciton(L, 0.25 * math.pi, 0.1, q=(4, 4)), walkers=EXC_WALKERS, seed=SEED,
+                        precision="fp64")
+            ref.set_measurements(1)
+            ref.init_walkers(cfg)
+            ref.reset_quantities()
+            ref.measure()
+            pr, _ = ref.projheis()
+            err = np.abs(pm - pr).max(axis=(1, 2)) / np.abs(pr).max(axis=(1, 2))
+            out["ho_error_vs_fp64"] = {"median": float(np.median(err)), "max": float(err.max()),
+                                       "what": "max |H,O mixed - H,O FP64| / max |H,O FP64| per walker, one measurement"}
+            out["measure_ms_per_sweep"] = mk / max(1, mn) if mn else None
+            ref.close()
+        for j in jobs:
+            j.close()
+    out["mixed_over_fp64"] = out["mixed"]["value"] / out["fp64"]["value"]
+    return out
+
+
 def main():
     global WALKERS
     ap = argparse.ArgumentParser()
@@ -268,6 +378,7 @@ def main():
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline (profiling runs)")
     ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end leg (profiling runs)")
     ap.add_argument("--walkers", type=int, default=WALKERS, help="walkers (profiling a smaller case)")
+    ap.add_argument("--no-exciton", action="store_true", help="skip the exciton-channel section")
     args = ap.parse_args()
 
     rank = int(os.environ.get("RANK", "0"))
@@ -292,9 +403,11 @@ def main():
         return
 
     WALKERS = args.walkers
-    cpu = None
+    cpu = cpu_exc = None
     if rank == 0 and world == 1 and not args.no_cpu:
         cpu = cpu_baseline(os.cpu_count() or 1, args.cpu_sweeps)
+        if not args.no_exciton:
+            cpu_exc = cpu_exciton_baseline(os.cpu_count() or 1, 4)
 
     dist = None
     if world > 1:
@@ -330,6 +443,7 @@ def main():
                   "walk_ms": ra["walk_ms"], "reinversion_ms": ra["inv_ms"], "reinversions": ra["reinv"],
                   "reinversion_policy": "FP64 re-inversion every 128 accepted exchanges", "steps": k}
 
+    exc = run_exciton(g, 4, 1) if (rank == 0 and not args.no_exciton) else None
     e2e = run_e2e(g, args.precision, args.steps, rank) if not args.no_e2e else None
     if dist and e2e:
         import torch
@@ -377,6 +491,10 @@ def main():
     if cpu:
         out["cpu_baseline"] = {k: cpu[k] for k in ("value", "unit", "cores", "kind", "sample")}
         out["cpu_baseline"]["per_core"] = cpu["per_core"]
+    if exc:
+        if cpu_exc:
+            exc["cpu_baseline"] = {k: cpu_exc[k] for k in ("value", "unit", "cores", "kind", "sample", "per_core")}
+        out["exciton"] = exc
     print(json.dumps(out))
 
 
