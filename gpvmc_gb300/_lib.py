@@ -21,6 +21,7 @@ GV_MEAS_PROJHEIS, GV_MEAS_STAGMAGN, GV_MEAS_STATSPIN = 1, 2, 4
 GV_FLAG_REINV_DEFERRED = 1
 GV_FLAG_REINV_ON_DRIFT = 2
 GV_FLAG_DELAYED_UPDATES = 4
+GV_FLAG_STREAM_INVERSES = 8
 
 
 class GvError(RuntimeError):

@@ -36,6 +36,8 @@ __host__ __device__ __forceinline__ cx<T> cinv(cx<T> a)
     T d = a.x * a.x + a.y * a.y;
     return {a.x / d, -a.y / d};
 }
+template <typename T>
+__host__ __device__ __forceinline__ cx<T> cneg(cx<T> a) { return {-a.x, -a.y}; }
 // a += b * c (complex multiply-accumulate)
 template <typename T>
 __device__ __forceinline__ void cmac(cx<T>& a, cx<T> b, cx<T> c)

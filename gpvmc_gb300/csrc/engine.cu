@@ -22,6 +22,7 @@
 #include "device.cuh"
 #include "kernels.cuh"
 #include "kernels_trans.cuh"
+#include "kernels_res.cuh"
 #include "model.hpp"
 
 using namespace gv;
@@ -99,7 +100,8 @@ bool valid_config(const gv_job_config* c)
     if (c->n_walkers < 1 || c->n_walkers > (1 << 20)) return false;
     if (c->precision != GV_PREC_FP64 && c->precision != GV_PREC_MIXED) return false;
     if (c->reinv_every < 0) return false;
-    if (c->flags & ~(GV_FLAG_REINV_DEFERRED | GV_FLAG_REINV_ON_DRIFT | GV_FLAG_DELAYED_UPDATES)) return false;
+    if (c->flags & ~(GV_FLAG_REINV_DEFERRED | GV_FLAG_REINV_ON_DRIFT | GV_FLAG_DELAYED_UPDATES | GV_FLAG_STREAM_INVERSES))
+        return false;
     if ((c->flags & GV_FLAG_REINV_ON_DRIFT) && (!(c->flags & GV_FLAG_REINV_DEFERRED) || !(c->drift_threshold > 0.0)))
         return false;
     return true;
@@ -227,10 +229,35 @@ gv_status launch_walk(gv_job* j, uint64_t nsteps, uint64_t s0, uint64_t meas, in
 #endif
 constexpr int kDelay = GV_DELAY_DEPTH;
 
+// On-chip walk (both FP32 inverses in TMEM / shared memory for the whole call):
+// mixed ground state, N <= 128, deferred re-inversion, no delayed updates.
+bool resident_ok(const gv_job* j, uint64_t nsteps)
+{
+    const int f = j->cfg.flags;
+    return nsteps > 0 && !j->trans && j->cfg.precision == GV_PREC_MIXED && j->N[0] == j->N[1] && j->Nmax <= 128 &&
+           (f & GV_FLAG_REINV_DEFERRED) && !(f & GV_FLAG_DELAYED_UPDATES) && !(f & GV_FLAG_STREAM_INVERSES);
+}
+
+gv_status launch_walk_res(gv_job* j, uint64_t nsteps, uint64_t s0, uint64_t meas, int mask)
+{
+    const ResLayout lay = res_layout(j->Ns, j->N[0], (mask & GV_MEAS_PROJHEIS) != 0);
+    GV_CK(cudaFuncSetAttribute(k_walk_gs_res, cudaFuncAttributeMaxDynamicSharedMemorySize, int(lay.total)));
+    GV_CK(cudaFuncSetAttribute(k_walk_gs_res, cudaFuncAttributePreferredSharedMemoryCarveout, 100));
+    int slot;
+    GV_CK(mark_begin(j, 0, &slot));
+    k_walk_gs_res<<<j->W, kResThreads, lay.total, j->stream>>>(j->d, nsteps, s0, meas, mask);
+    GV_CK(cudaGetLastError());
+    GV_CK(mark_end(j, slot));
+    ++j->last_launches;
+    ++j->total_launches;
+    return GV_OK;
+}
+
 // Delayed updates (depth kDelay) when requested and every particle column has its
 // own thread; otherwise immediate rank-1 updates.
 gv_status walk_dispatch(gv_job* j, uint64_t nsteps, uint64_t s0, uint64_t meas, int mask, int measure_first = 0)
 {
+    if (!measure_first && resident_ok(j, nsteps)) return launch_walk_res(j, nsteps, s0, meas, mask);
     const bool fp64 = j->cfg.precision == GV_PREC_FP64;
     const bool delayed = (j->cfg.flags & GV_FLAG_DELAYED_UPDATES) && j->Nmax <= j->nt;
     if (j->nt == 128) {

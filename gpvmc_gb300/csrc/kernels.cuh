@@ -409,30 +409,92 @@ struct WalkCtx {
     cx<T>* A1;
 };
 
+// ProjHeis pass 2 (ProjHeis.cpp:40-158): with every particle's ratio to each
+// antiparallel neighbour in rq[site][slot] (a site holds one particle), walk
+// the edges in creation order, pair the two flavours' ratios of each
+// antiparallel bond and add E/site to the walker's accumulator
+// (Quantity::measure, Quantity.cpp:24-27).
+template <typename T, int NT>
+__device__ void projheis_from_rq(const WalkCtx<T>& C)
+{
+    constexpr int NW = NT / 32;
+    const DevJob& J = *C.J;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int16_t* s_fock = C.s_fock;
+    const cx<T>* s_rq = C.s_rq;
+    double* s_redm = C.s_redm;
+    cx<double> e = {0.0, 0.0};
+    for (int ed = tid; ed < 2 * C.Ns; ed += NT) {
+        const int4 E = J.edges[ed];   // (i, j, slot of j at i, slot of i at j)
+        const bool ui = s_fock[E.x] >= 0, uj = s_fock[E.y] >= 0;
+        if (ui == uj) { e.x += 0.25; continue; }
+        const cx<double> r = to_d(s_rq[E.x * 4 + E.z]) * to_d(s_rq[E.y * 4 + E.w]);
+        e.x += -0.25 - 0.5 * r.x;
+        e.y += -0.5 * r.y;
+    }
+#pragma unroll
+    for (int o = 16; o; o >>= 1) {
+        e.x += __shfl_xor_sync(0xffffffffu, e.x, o);
+        e.y += __shfl_xor_sync(0xffffffffu, e.y, o);
+    }
+    if (lane == 0) { s_redm[warp * 4] = e.x; s_redm[warp * 4 + 1] = e.y; }
+    __syncthreads();
+    if (tid == 0) {
+        const double inv_ns = 1.0 / double(C.Ns);
+        double ex = 0, ey = 0;
+        for (int q = 0; q < NW; ++q) { ex += s_redm[q * 4]; ey += s_redm[q * 4 + 1]; }
+        J.pj[size_t(C.w) * 2].x += ex * inv_ns;
+        J.pj[size_t(C.w) * 2].y += ey * inv_ns;
+        J.pj[size_t(C.w) * 2 + 1].x += 1.0;
+        J.pj_n[C.w] += 1;
+    }
+    __syncthreads();
+}
+
+// StagMagnZ (StagMagnZ.cpp:12-43) of the walker's current configuration.
+template <typename T, int NT>
+__device__ void stagmagn_now(const WalkCtx<T>& C)
+{
+    constexpr int NW = NT / 32;
+    const DevJob& J = *C.J;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int L = C.L;
+    int m = 0;
+    for (int v = tid; v < C.Ns; v += NT) {
+        const int sg = (((v % L) + (v / L)) & 1) ? -1 : 1;
+        m += sg * (C.s_fock[v] >= 0 ? 1 : -1);
+    }
+#pragma unroll
+    for (int o = 16; o; o >>= 1) m += __shfl_xor_sync(0xffffffffu, m, o);
+    if (lane == 0) C.s_redm[warp * 4 + 2] = double(m);
+    __syncthreads();
+    if (tid == 0) {
+        double t = 0;
+        for (int q = 0; q < NW; ++q) t += C.s_redm[q * 4 + 2];
+        const double inv_ns = 1.0 / double(C.Ns);
+        J.sm[C.w].x += t * inv_ns;
+        J.sm_n[C.w] += 1;
+    }
+    __syncthreads();
+}
+
 // ProjHeis and StagMagnZ of the walker's current configuration, added to
 // its accumulators (Quantity::measure, Quantity.cpp:24-27).
 template <typename T, int NT>
 __device__ void measure_now(const WalkCtx<T>& C, int mask)
 {
-    constexpr int NW = NT / 32;
-    const DevJob& J = *C.J;
-    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    const int w = C.w, Ns = C.Ns, Nmax = C.Nmax, L = C.L, Nk = C.Nk, N0 = C.N0, N1 = C.N1;
-    int16_t* s_fock = C.s_fock;
-    int16_t* s_part = C.s_part;
-    int16_t* s_nbr = C.s_nbr;
-    cx<T>* s_coef = C.s_coef;
+    const int tid = threadIdx.x;
+    const int Nmax = C.Nmax, L = C.L, Nk = C.Nk, N0 = C.N0, N1 = C.N1;
+    const int16_t* s_fock = C.s_fock;
+    const int16_t* s_part = C.s_part;
+    const int16_t* s_nbr = C.s_nbr;
+    const cx<T>* s_coef = C.s_coef;
     cx<T>* s_rq = C.s_rq;
-    double* s_redm = C.s_redm;
     const cx<T>* phase = C.phase;
     const cx<T>* A0 = C.A0;
     const cx<T>* A1 = C.A1;
-    const double inv_ns = 1.0 / double(Ns);
     if (mask & GV_MEAS_PROJHEIS) {
-        // ProjHeis (ProjHeis.cpp:40-158): pass 1, every particle computes the ratio of
-        // moving it to each antiparallel neighbour into rq[site][slot] (a site holds
-        // one particle); pass 2 walks the edges in creation order and pairs the two
-        // flavours' ratios of each antiparallel bond.
+        // pass 1: every particle's ratio of moving to each antiparallel neighbour
         for (int idx = tid; idx < N0 + N1; idx += NT) {
             const int fl = idx < N0 ? 0 : 1;
             const int p = fl ? idx - N0 : idx;
@@ -458,50 +520,9 @@ __device__ void measure_now(const WalkCtx<T>& C, int mask)
             for (int kk = 0; kk < 4; ++kk) s_rq[site * 4 + kk] = acc[kk];
         }
         __syncthreads();
-        cx<double> e = {0.0, 0.0};
-        for (int ed = tid; ed < 2 * Ns; ed += NT) {
-            const int4 E = J.edges[ed];   // (i, j, slot of j at i, slot of i at j)
-            const bool ui = s_fock[E.x] >= 0, uj = s_fock[E.y] >= 0;
-            if (ui == uj) { e.x += 0.25; continue; }
-            const cx<double> r = to_d(s_rq[E.x * 4 + E.z]) * to_d(s_rq[E.y * 4 + E.w]);
-            e.x += -0.25 - 0.5 * r.x;
-            e.y += -0.5 * r.y;
-        }
-#pragma unroll
-        for (int o = 16; o; o >>= 1) {
-            e.x += __shfl_xor_sync(0xffffffffu, e.x, o);
-            e.y += __shfl_xor_sync(0xffffffffu, e.y, o);
-        }
-        if (lane == 0) { s_redm[warp * 4] = e.x; s_redm[warp * 4 + 1] = e.y; }
-        __syncthreads();
-        if (tid == 0) {
-            double ex = 0, ey = 0;
-            for (int q = 0; q < NW; ++q) { ex += s_redm[q * 4]; ey += s_redm[q * 4 + 1]; }
-            J.pj[size_t(w) * 2].x += ex * inv_ns;
-            J.pj[size_t(w) * 2].y += ey * inv_ns;
-            J.pj[size_t(w) * 2 + 1].x += 1.0;
-            J.pj_n[w] += 1;
-        }
-        __syncthreads();
+        projheis_from_rq<T, NT>(C);
     }
-    if (mask & GV_MEAS_STAGMAGN) {   // StagMagnZ (StagMagnZ.cpp:12-43)
-        int m = 0;
-        for (int v = tid; v < Ns; v += NT) {
-            const int sg = (((v % L) + (v / L)) & 1) ? -1 : 1;
-            m += sg * (s_fock[v] >= 0 ? 1 : -1);
-        }
-#pragma unroll
-        for (int o = 16; o; o >>= 1) m += __shfl_xor_sync(0xffffffffu, m, o);
-        if (lane == 0) s_redm[warp * 4 + 2] = double(m);
-        __syncthreads();
-        if (tid == 0) {
-            double t = 0;
-            for (int q = 0; q < NW; ++q) t += s_redm[q * 4 + 2];
-            J.sm[w].x += t * inv_ns;
-            J.sm_n[w] += 1;
-        }
-        __syncthreads();
-    }
+    if (mask & GV_MEAS_STAGMAGN) stagmagn_now<T, NT>(C);
 }
 
 // Pending rank-1 updates (delayed Sherman-Morrison, McDaniel et al., J. Chem.

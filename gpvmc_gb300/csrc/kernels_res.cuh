@@ -1,0 +1,371 @@
+// Ground-state Metropolis walk with both inverses resident in tensor memory
+// (mixed precision, N <= 128).  Included by engine.cu after kernels.cuh.
+//
+// The streaming kernel (k_walk_gs) keeps the inverses in HBM and runs several
+// walkers per SM to hide the latency of every proposal's row gather and every
+// accepted move's read-modify-write; it settles at ~75% of the HBM copy
+// bandwidth.  Here one CTA per SM owns one walker for a whole walk call and
+// keeps both FP32 inverses in the SM's tensor memory (TMEM: 128 lanes x 512
+// 32-bit columns = 256 KB): flavour g occupies columns [256 g, 256 g + 256),
+// lane f holds row f of AiT (AiT[f][p] = (A^-1)(p, f)) with the real and
+// imaginary part of particle p in columns 2p and 2p + 1.  HBM is touched once
+// per walk call (load at entry, store at exit).  Warpgroup g (threads
+// 128 g .. 128 g + 127; TMEM lane f = thread f of the warpgroup) serves flavour
+// g; both flavours run concurrently:
+//   proposal: thread f loads its lane's element of column c (one 2-column
+//             load), forms (A^-1)(c, f) u_f and the warpgroup sums the
+//             ratio r = sum_f (A^-1)(c, f) u_f  (linalg.cpp:297-303);
+//   accept:   w = A^-1 u for every particle: each warp multiplies its 32 rows
+//             by u_f and transposes-and-sums them across its lanes with
+//             shuffles, the four warps' partial sums meet in shared memory;
+//             then every lane updates its row,
+//             AiT[f][p] -= (w_p - [p == c]) (A^-1)(c, f) / r  (linalg.cpp:402-573, rc = 1).
+// Uniforms are drawn 32 steps at a time by one warp into shared memory (the
+// Metropolis stream does not depend on the walk).  Same uniforms, decisions
+// and formulas as k_walk_gs.
+#pragma once
+
+#include "kernels.cuh"
+
+namespace gv {
+namespace {
+
+// ---- tensor memory (tcgen05): allocation and 32-lane access ----
+__device__ __forceinline__ void tmem_alloc(uint32_t* dst_smem, uint32_t ncols)
+{
+    const uint32_t a = static_cast<uint32_t>(__cvta_generic_to_shared(dst_smem));
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(a), "r"(ncols) : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+}
+__device__ __forceinline__ void tmem_dealloc(uint32_t taddr, uint32_t ncols)
+{
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(taddr), "r"(ncols) : "memory");
+}
+__device__ __forceinline__ void tmem_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void tmem_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void tmem_wait_st() { asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory"); }
+// Thread i of a warp accesses lane (lane base of taddr) + i, columns [col, col + n);
+// the wait takes the registers as operands so that no use is hoisted above it.
+__device__ __forceinline__ void tmem_ld2(uint32_t taddr, uint32_t (&r)[2])
+{
+    asm volatile("tcgen05.ld.sync.aligned.32x32b.x2.b32 {%0,%1}, [%2];" : "=r"(r[0]), "=r"(r[1]) : "r"(taddr));
+}
+__device__ __forceinline__ void tmem_wait_ld(uint32_t (&r)[2])
+{
+    asm volatile("tcgen05.wait::ld.sync.aligned;" : "+r"(r[0]), "+r"(r[1])::"memory");
+}
+__device__ __forceinline__ void tmem_ld64(uint32_t taddr, uint32_t (&r)[64])
+{
+    asm volatile("tcgen05.ld.sync.aligned.32x32b.x64.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31,%32,%33,%34,%35,%36,%37,%38,%39,%40,%41,%42,%43,%44,%45,%46,%47,%48,%49,%50,%51,%52,%53,%54,%55,%56,%57,%58,%59,%60,%61,%62,%63}, [%64];" : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]), "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]), "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31]), "=r"(r[32]), "=r"(r[33]), "=r"(r[34]), "=r"(r[35]), "=r"(r[36]), "=r"(r[37]), "=r"(r[38]), "=r"(r[39]), "=r"(r[40]), "=r"(r[41]), "=r"(r[42]), "=r"(r[43]), "=r"(r[44]), "=r"(r[45]), "=r"(r[46]), "=r"(r[47]), "=r"(r[48]), "=r"(r[49]), "=r"(r[50]), "=r"(r[51]), "=r"(r[52]), "=r"(r[53]), "=r"(r[54]), "=r"(r[55]), "=r"(r[56]), "=r"(r[57]), "=r"(r[58]), "=r"(r[59]), "=r"(r[60]), "=r"(r[61]), "=r"(r[62]), "=r"(r[63]) : "r"(taddr));
+}
+__device__ __forceinline__ void tmem_wait_ld(uint32_t (&r)[64])
+{
+    asm volatile("tcgen05.wait::ld.sync.aligned;" : "+r"(r[0]), "+r"(r[1]), "+r"(r[2]), "+r"(r[3]), "+r"(r[4]), "+r"(r[5]), "+r"(r[6]), "+r"(r[7]), "+r"(r[8]), "+r"(r[9]), "+r"(r[10]), "+r"(r[11]), "+r"(r[12]), "+r"(r[13]), "+r"(r[14]), "+r"(r[15]), "+r"(r[16]), "+r"(r[17]), "+r"(r[18]), "+r"(r[19]), "+r"(r[20]), "+r"(r[21]), "+r"(r[22]), "+r"(r[23]), "+r"(r[24]), "+r"(r[25]), "+r"(r[26]), "+r"(r[27]), "+r"(r[28]), "+r"(r[29]), "+r"(r[30]), "+r"(r[31]), "+r"(r[32]), "+r"(r[33]), "+r"(r[34]), "+r"(r[35]), "+r"(r[36]), "+r"(r[37]), "+r"(r[38]), "+r"(r[39]), "+r"(r[40]), "+r"(r[41]), "+r"(r[42]), "+r"(r[43]), "+r"(r[44]), "+r"(r[45]), "+r"(r[46]), "+r"(r[47]), "+r"(r[48]), "+r"(r[49]), "+r"(r[50]), "+r"(r[51]), "+r"(r[52]), "+r"(r[53]), "+r"(r[54]), "+r"(r[55]), "+r"(r[56]), "+r"(r[57]), "+r"(r[58]), "+r"(r[59]), "+r"(r[60]), "+r"(r[61]), "+r"(r[62]), "+r"(r[63])::"memory");
+}
+__device__ __forceinline__ void tmem_st64(uint32_t taddr, const uint32_t (&r)[64])
+{
+    asm volatile("tcgen05.st.sync.aligned.32x32b.x64.b32 [%0], {%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31,%32,%33,%34,%35,%36,%37,%38,%39,%40,%41,%42,%43,%44,%45,%46,%47,%48,%49,%50,%51,%52,%53,%54,%55,%56,%57,%58,%59,%60,%61,%62,%63,%64};" ::"r"(taddr), "r"(r[0]), "r"(r[1]), "r"(r[2]), "r"(r[3]), "r"(r[4]), "r"(r[5]), "r"(r[6]), "r"(r[7]), "r"(r[8]), "r"(r[9]), "r"(r[10]), "r"(r[11]), "r"(r[12]), "r"(r[13]), "r"(r[14]), "r"(r[15]), "r"(r[16]), "r"(r[17]), "r"(r[18]), "r"(r[19]), "r"(r[20]), "r"(r[21]), "r"(r[22]), "r"(r[23]), "r"(r[24]), "r"(r[25]), "r"(r[26]), "r"(r[27]), "r"(r[28]), "r"(r[29]), "r"(r[30]), "r"(r[31]), "r"(r[32]), "r"(r[33]), "r"(r[34]), "r"(r[35]), "r"(r[36]), "r"(r[37]), "r"(r[38]), "r"(r[39]), "r"(r[40]), "r"(r[41]), "r"(r[42]), "r"(r[43]), "r"(r[44]), "r"(r[45]), "r"(r[46]), "r"(r[47]), "r"(r[48]), "r"(r[49]), "r"(r[50]), "r"(r[51]), "r"(r[52]), "r"(r[53]), "r"(r[54]), "r"(r[55]), "r"(r[56]), "r"(r[57]), "r"(r[58]), "r"(r[59]), "r"(r[60]), "r"(r[61]), "r"(r[62]), "r"(r[63]) : "memory");
+}
+// barrier over one warpgroup (ids 1, 2; id 0 is __syncthreads)
+__device__ __forceinline__ void wg_sync(int g) { asm volatile("bar.sync %0, 128;" ::"r"(1 + g) : "memory"); }
+
+constexpr int kResThreads = 256;
+constexpr int kResTmemCols = 512;                 // both flavours, 128 complex FP32 per lane each
+constexpr size_t kResMinSmem = 116 * 1024;        // over half an SM's shared memory: one CTA per SM
+constexpr int kResRngBatch = 32;
+
+struct ResLayout {
+    size_t fock, part, nbr, sub, coef, red, wpart, w, rv, ru4, ru4d, rq, redm, tbase, total, used;
+};
+
+__host__ __device__ inline ResLayout res_layout(int Ns, int N, bool projheis)
+{
+    ResLayout l;
+    size_t b = 0;
+    auto al = [&](size_t x) { b = (b + 15) & ~size_t(15); size_t r = b; b += x; return r; };
+    const size_t c = sizeof(cx<float>);
+    l.fock = al(sizeof(int16_t) * 2 * Ns);
+    l.part = al(sizeof(int16_t) * 2 * N);
+    l.nbr = al(sizeof(int16_t) * 4 * Ns);
+    l.sub = al(sizeof(int8_t) * Ns);
+    l.coef = al(c * 4 * N);
+    l.red = al(sizeof(float) * 2 * 16);
+    l.wpart = al(c * 2 * 4 * 128);
+    l.w = al(c * 2 * 128);
+    l.rv = al(sizeof(int16_t) * 2 * kResRngBatch);
+    l.ru4 = al(sizeof(float) * kResRngBatch);
+    l.ru4d = al(sizeof(double) * kResRngBatch);
+    l.rq = al(projheis ? c * 4 * Ns : 16);
+    l.redm = al(sizeof(double) * 4 * (kResThreads / 32));
+    l.tbase = al(sizeof(uint32_t));
+    l.used = al(16);
+    l.total = l.used < kResMinSmem ? kResMinSmem : l.used;
+    return l;
+}
+
+// v[0..31] per lane -> lane l returns sum over the warp's lanes of v[l]
+// (recursive halving: at each round a lane keeps the half of its values
+// selected by one bit of its lane id and adds its partner's copy of that half).
+__device__ __forceinline__ cx<float> warp_transpose_sum(cx<float> (&v)[32])
+{
+    const int lane = threadIdx.x & 31;
+#pragma unroll
+    for (int k = 16; k >= 1; k >>= 1) {
+        const bool upper = (lane & k) != 0;
+#pragma unroll
+        for (int i = 0; i < k; ++i) {
+            const cx<float> send = upper ? v[i] : v[i + k];
+            const cx<float> keep = upper ? v[i + k] : v[i];
+            cx<float> recv;
+            recv.x = __shfl_xor_sync(0xffffffffu, send.x, k);
+            recv.y = __shfl_xor_sync(0xffffffffu, send.y, k);
+            v[i] = keep + recv;
+        }
+    }
+    return v[0];
+}
+
+__global__ void __launch_bounds__(kResThreads, 1) k_walk_gs_res(DevJob J, uint64_t nsteps, uint64_t s0, uint64_t meas,
+                                                                int mask)
+{
+    extern __shared__ __align__(16) char smem[];
+    using T = float;
+    const int w = blockIdx.x;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    if (w >= J.W || J.status[w] != GV_OK) return;   // before any TMEM allocation
+    const int Ns = J.Ns, N = J.N[0], L = J.L, Nk = J.Nk;
+    const int NCH = (N + 31) / 32;                  // 32-particle column chunks
+    const ResLayout lay = res_layout(Ns, N, (mask & GV_MEAS_PROJHEIS) != 0);
+    int16_t* s_fock = reinterpret_cast<int16_t*>(smem + lay.fock);
+    int16_t* s_part = reinterpret_cast<int16_t*>(smem + lay.part);
+    int16_t* s_nbr = reinterpret_cast<int16_t*>(smem + lay.nbr);
+    int8_t* s_sub = reinterpret_cast<int8_t*>(smem + lay.sub);
+    cx<T>* s_coef = reinterpret_cast<cx<T>*>(smem + lay.coef);
+    T* s_red = reinterpret_cast<T*>(smem + lay.red);
+    cx<T>* s_wpart = reinterpret_cast<cx<T>*>(smem + lay.wpart);   // [g][warp][p]
+    cx<T>* s_w = reinterpret_cast<cx<T>*>(smem + lay.w);           // [g][p]
+    int16_t* s_rv = reinterpret_cast<int16_t*>(smem + lay.rv);     // [step][v1, v2]
+    float* s_ru4 = reinterpret_cast<float*>(smem + lay.ru4);
+    double* s_ru4d = reinterpret_cast<double*>(smem + lay.ru4d);
+    cx<T>* s_rq = reinterpret_cast<cx<T>*>(smem + lay.rq);
+    double* s_redm = reinterpret_cast<double*>(smem + lay.redm);
+    uint32_t* s_tbase = reinterpret_cast<uint32_t*>(smem + lay.tbase);
+
+    if (warp == 0) tmem_alloc(s_tbase, kResTmemCols);
+    for (int i = tid; i < 2 * Ns; i += kResThreads) s_fock[i] = J.fock[size_t(w) * 2 * Ns + i];
+    for (int i = tid; i < 2 * N; i += kResThreads) {
+        const int fl = i / N, p = i % N;
+        s_part[i] = J.part[(size_t(w) * 2 + fl) * J.Nmax + p];
+    }
+    for (int i = tid; i < 4 * Ns; i += kResThreads) s_nbr[i] = int16_t(J.nbr[i]);
+    for (int i = tid; i < Ns; i += kResThreads) s_sub[i] = int8_t(sublattice(i, L));
+    {
+        const cx<T>* cg = J.coef32 + size_t(w) * 4 * Ns;   // [fl][sub][orbital]
+        for (int i = tid; i < 4 * N; i += kResThreads) {
+            const int fl = i / (2 * N), sub = (i / N) & 1, f = i % N;
+            s_coef[i] = cg[(size_t(fl) * 2 + sub) * Ns + 2 * f];
+        }
+    }
+    tmem_fence_before();
+    __syncthreads();
+    tmem_fence_after();
+    const uint32_t tbase = *s_tbase;
+    const int g = tid >> 7;                       // warpgroup = flavour
+    const int f = tid & 127;                      // TMEM lane = Slater row of this thread
+    const uint32_t trow = tbase + ((uint32_t(warp & 3) * 32) << 16) + uint32_t(256 * g);
+    cx<T>* Ag = ai_ptr<T>(J, g, w);
+    // inverse of flavour g -> TMEM: lane f = row f of AiT (contiguous in HBM), zero padding
+    for (int c = 0; c < NCH; ++c) {
+        uint32_t r[64];
+#pragma unroll
+        for (int j = 0; j < 32; ++j) {
+            const int p = 32 * c + j;
+            cx<T> a = {0.f, 0.f};
+            if (f < N && p < N) a = Ag[size_t(f) * N + p];
+            r[2 * j] = __float_as_uint(a.x);
+            r[2 * j + 1] = __float_as_uint(a.y);
+        }
+        tmem_st64(trow + 64 * c, r);
+    }
+    tmem_wait_st();
+    tmem_fence_before();
+    __syncthreads();
+    tmem_fence_after();
+
+    const cx<T>* phase = J.phase32;
+    const cx<T>* cf = s_coef + g * 2 * N;         // this flavour's [sub][f]
+    const uint32_t wid = J.walker_base + uint32_t(w);
+    uint64_t k = J.rng_next[w];
+    unsigned long long c_acc = 0, c_noop = 0, c_rej = 0;
+    int since = J.since_reinv[w];
+    cx<double> am = J.amp_m[w];
+    int ae = J.amp_e[w];
+    int status = GV_OK;
+    int rbuf = 0;
+    const WalkCtx<T> C = {&J, w, Ns, N, L, Nk, N, N, s_fock, s_part, s_nbr, s_coef, s_rq, s_redm,
+                          phase, ai_ptr<T>(J, 0, w), ai_ptr<T>(J, 1, w)};
+
+    for (uint64_t s = 0; s < nsteps; ++s, k += 4) {
+        const int bi = int(s % kResRngBatch);
+        if (bi == 0) {   // the next batch of proposals and accept uniforms (one lane per step)
+            __syncthreads();   // every thread is done with the previous batch
+            if (warp == 0 && s + lane < nsteps) {
+                const uint64_t kl = k + 4 * uint64_t(lane);
+                uint32_t x[4], y[4];
+                philox_call(J.seed, wid, 0, kl >> 1, x);
+                philox_call(J.seed, wid, 0, (kl >> 1) + 1, y);
+                const int v1 = scaled_floor(uint32_t(Ns), u52(x[0], x[1]));
+                s_rv[2 * lane] = int16_t(v1);
+                s_rv[2 * lane + 1] = s_nbr[v1 * 4 + int(u52(x[2], x[3]) >> 50)];
+                s_ru4[lane] = Accept<T>::uniform(u52(y[2], y[3]));
+                s_ru4d[lane] = u01(y[2], y[3]);
+            }
+            __syncthreads();
+        }
+        const int v1 = s_rv[2 * bi], v2 = s_rv[2 * bi + 1];
+        const int f1 = s_fock[v1] >= 0 ? 0 : 1;
+        const int f2 = s_fock[v2] >= 0 ? 0 : 1;
+        int kind = 0, accepted;
+        T ratio = T(1);
+        if (f1 == f2) {
+            accepted = 1;   // m_weight / m_state_weight = 1 (MetroMC.cpp:41)
+            ++c_noop;
+        } else {
+            kind = 1;
+            const int upf = (f1 == 0) ? v1 : v2, upt = (f1 == 0) ? v2 : v1;
+            const int dnf = upt, dnt = upf;
+            const int cu = s_fock[upf], cd = s_fock[Ns + dnf];
+            const int cg = g ? cd : cu, tg = g ? dnt : upt;   // this flavour's particle and destination
+            T* rb = s_red + rbuf * 16;
+            rbuf ^= 1;
+            // proposal: (A^-1)(c, f) from this lane's column c, u_f = phi_{2f}(t)
+            cx<T> u = {0.f, 0.f}, a;
+            {
+                uint32_t r[2];
+                tmem_ld2(trow + 2 * cg, r);
+                if (f < N) u = cmul_rn(phase[size_t(tg) * Nk + f], cf[s_sub[tg] * N + f]);
+                tmem_wait_ld(r);
+                a = cx<T>{__uint_as_float(r[0]), __uint_as_float(r[1])};
+            }
+            cx<T> part = warp_sum(a * u);
+            if (lane == 0) { rb[warp * 2] = part.x; rb[warp * 2 + 1] = part.y; }
+            __syncthreads();
+            const cx<T> ru = {rb[0] + rb[2] + rb[4] + rb[6], rb[1] + rb[3] + rb[5] + rb[7]};
+            const cx<T> rd = {rb[8] + rb[10] + rb[12] + rb[14], rb[9] + rb[11] + rb[13] + rb[15]};
+            ratio = Accept<T>::ratio(ru, rd);
+            if (!isfinite(ratio)) { status = GV_ERR_NAN; break; }
+            accepted = ratio > T(1) ? 1 : (s_ru4[bi] < ratio);
+            if (!accepted) {
+                ++c_rej;
+            } else {
+                if (norm2(ru) < T(1e-9) || norm2(rd) < T(1e-9)) { status = GV_ERR_SINGULAR; break; }
+                const cx<T> ir = cinv(g ? rd : ru);
+                // w = A^-1 u: this warp's 32 rows times u_f, summed over lanes per particle
+                cx<T>* wpart = s_wpart + (g * 4 + (warp & 3)) * 128;
+                for (int c = 0; c < NCH; ++c) {
+                    uint32_t r[64];
+                    tmem_ld64(trow + 64 * c, r);
+                    tmem_wait_ld(r);
+                    cx<T> v[32];
+#pragma unroll
+                    for (int j = 0; j < 32; ++j) v[j] = cx<T>{__uint_as_float(r[2 * j]), __uint_as_float(r[2 * j + 1])} * u;
+                    wpart[32 * c + lane] = warp_transpose_sum(v);
+                }
+                wg_sync(g);
+                if (f < 32 * NCH) {
+                    const cx<T>* wp0 = s_wpart + g * 4 * 128;
+                    s_w[g * 128 + f] = wp0[f] + wp0[128 + f] + wp0[256 + f] + wp0[384 + f];
+                }
+                wg_sync(g);
+                // row update: AiT[f][p] -= (w_p - [p == c]) * (A^-1)(c, f) / r
+                const cx<T> coef = cneg(a * ir);
+                const cx<T>* wv = s_w + g * 128;
+                for (int c = 0; c < NCH; ++c) {
+                    uint32_t r[64];
+                    tmem_ld64(trow + 64 * c, r);
+                    tmem_wait_ld(r);
+#pragma unroll
+                    for (int j = 0; j < 32; ++j) {
+                        const int p = 32 * c + j;
+                        cx<T> wq = wv[p];
+                        if (p == cg) wq.x -= 1.f;
+                        cx<T> e = {__uint_as_float(r[2 * j]), __uint_as_float(r[2 * j + 1])};
+                        cmac(e, wq, coef);
+                        r[2 * j] = __float_as_uint(e.x);
+                        r[2 * j + 1] = __float_as_uint(e.y);
+                    }
+                    tmem_st64(trow + 64 * c, r);
+                }
+                tmem_wait_st();
+                if (tid == 0) {
+                    s_fock[upt] = int16_t(cu); s_fock[upf] = -1; s_part[cu] = int16_t(upt);
+                    s_fock[Ns + dnt] = int16_t(cd); s_fock[Ns + dnf] = -1; s_part[N + cd] = int16_t(dnt);
+                    am = am * (to_d(ru) * to_d(rd));
+                    amp_normalise(am, ae);
+                }
+                ++c_acc;
+                ++since;
+                __syncthreads();
+            }
+        }
+        if (J.trace && w == J.trace_walker && tid == 0) {
+            gv_trace t;
+            t.v1 = v1; t.v2 = v2; t.kind = kind; t.accepted = accepted; t.khop = kind ? 0 : -1; t.pad = 0;
+            t.ratio = double(ratio); t.u4 = s_ru4d[bi];
+            J.trace[s] = t;
+        }
+        const uint64_t gs = s0 + s;
+        if (meas && (meas == 1 || gs % meas == 0) && mask) {
+            // write both inverses back and measure from HBM/L2 as the streaming kernel
+            for (int c = 0; c < NCH; ++c) {
+                uint32_t r[64];
+                tmem_ld64(trow + 64 * c, r);
+                tmem_wait_ld(r);
+#pragma unroll
+                for (int j = 0; j < 32; ++j) {
+                    const int p = 32 * c + j;
+                    if (f < N && p < N) Ag[size_t(f) * N + p] = cx<T>{__uint_as_float(r[2 * j]), __uint_as_float(r[2 * j + 1])};
+                }
+            }
+            __syncthreads();
+            measure_now<T, kResThreads>(C, mask);
+            __syncthreads();
+        }
+    }
+    __syncthreads();
+    // write back: both inverses from TMEM, occupancy, counters
+    for (int c = 0; c < NCH; ++c) {
+        uint32_t r[64];
+        tmem_ld64(trow + 64 * c, r);
+        tmem_wait_ld(r);
+#pragma unroll
+        for (int j = 0; j < 32; ++j) {
+            const int p = 32 * c + j;
+            if (f < N && p < N) Ag[size_t(f) * N + p] = cx<T>{__uint_as_float(r[2 * j]), __uint_as_float(r[2 * j + 1])};
+        }
+    }
+    for (int i = tid; i < 2 * Ns; i += kResThreads) J.fock[size_t(w) * 2 * Ns + i] = s_fock[i];
+    for (int i = tid; i < 2 * N; i += kResThreads) {
+        const int fl = i / N, p = i % N;
+        J.part[(size_t(w) * 2 + fl) * J.Nmax + p] = s_part[i];
+    }
+    if (tid == 0) {
+        J.rng_next[w] = k;
+        unsigned long long* cn = J.counts + size_t(w) * 5;
+        cn[0] += c_acc + c_noop + c_rej;
+        cn[1] += c_acc;
+        cn[2] += c_noop;
+        cn[3] += c_rej;
+        J.since_reinv[w] = since;
+        J.amp_m[w] = am;
+        J.amp_e[w] = ae;
+        J.status[w] = status;
+    }
+    tmem_fence_before();
+    __syncthreads();
+    tmem_fence_after();
+    if (warp == 0) tmem_dealloc(tbase, kResTmemCols);
+}
+
+}  // namespace
+}  // namespace gv

@@ -32,10 +32,6 @@
 namespace gv {
 namespace {
 
-template <typename T>
-__device__ __forceinline__ cx<T> cneg(cx<T> a) { return {-a.x, -a.y}; }
-template <typename T>
-__device__ __forceinline__ cx<T> cdiv(cx<T> a, cx<T> b) { return a * cinv(b); }
 
 // Number of occupied orbitals strictly between a and b in one flavour's
 // wavefunction Fock state (slot table wslot_fl), by one warp.

@@ -89,7 +89,7 @@ class Job:
 
     def __init__(self, wav, walkers=1, seed=1234, precision="fp64", reinv_every=0, walker_base=0,
                  phi_range=None, neel_range=None, deferred_reinversion=False, drift_threshold=None,
-                 delayed_updates=False):
+                 delayed_updates=False, stream_inverses=False):
         L = _lib.lib()
         cfg = _lib.JobConfig()
         cfg.L = wav.L
@@ -113,6 +113,8 @@ class Job:
             cfg.drift_threshold = drift_threshold
         if delayed_updates:
             cfg.flags |= _lib.GV_FLAG_DELAYED_UPDATES
+        if stream_inverses:
+            cfg.flags |= _lib.GV_FLAG_STREAM_INVERSES
         self.cfg = cfg
         self.wav = wav
         self.walkers = walkers

@@ -63,9 +63,13 @@ typedef int32_t gv_status;
 #define GV_FLAG_REINV_ON_DRIFT 2  /* with GV_FLAG_REINV_DEFERRED: at that point check the
                                      FP64 sampled drift ||A A^-1 - I||_max and re-invert
                                      only when it exceeds drift_threshold */
-#define GV_FLAG_DELAYED_UPDATES 4 /* delayed rank-8 Sherman-Morrison updates: the inverse is
-                                     written back once per 8 accepted exchanges (the same
+#define GV_FLAG_DELAYED_UPDATES 4 /* delayed Sherman-Morrison updates: the inverse is
+                                     written back once per 4 accepted exchanges (the same
                                      Markov chain; the inverse differs only by rounding) */
+#define GV_FLAG_STREAM_INVERSES 8 /* mixed ground state: keep the inverses in HBM during the
+                                     walk (the streaming kernel) instead of on chip; the
+                                     on-chip kernel runs by default when N <= 128 and the
+                                     re-inversion is deferred */
 
 #define GV_MEAS_PROJHEIS 1    /* ProjHeis (ProjHeis.cpp:40-158), Bx = 0 */
 #define GV_MEAS_STAGMAGN 2    /* StagMagnZ (StagMagnZ.cpp:12-43) */
