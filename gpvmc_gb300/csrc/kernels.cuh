@@ -479,8 +479,10 @@ __device__ void stagmagn_now(const WalkCtx<T>& C)
 }
 
 // ProjHeis and StagMagnZ of the walker's current configuration, added to
-// its accumulators (Quantity::measure, Quantity.cpp:24-27).
-template <typename T, int NT>
+// its accumulators (Quantity::measure, Quantity.cpp:24-27).  RND rows of the
+// inverse per round in pass 1 (more loads in flight for callers with spare
+// registers).
+template <typename T, int NT, int RND = 1>
 __device__ void measure_now(const WalkCtx<T>& C, int mask)
 {
     const int tid = threadIdx.x;
@@ -509,12 +511,36 @@ __device__ void measure_now(const WalkCtx<T>& C, int mask)
                 js[kk] = s_nbr[site * 4 + kk];
                 anti[kk] = (s_fock[js[kk]] >= 0) != (fl == 0);
             }
+            // phi_{2f}(j) = phase[j][f] coef[sub(j)][f]: per neighbour one phase row and
+            // one coefficient row; RND rows f per round keep the loads in flight
+            const cx<T>* ph[4];
+            const cx<T>* cr[4];
+#pragma unroll
+            for (int kk = 0; kk < 4; ++kk) {
+                ph[kk] = phase + size_t(js[kk]) * Nk;
+                cr[kk] = cf + sublattice(js[kk], L) * Nmax;
+            }
             cx<T> acc[4] = {{T(0), T(0)}, {T(0), T(0)}, {T(0), T(0)}, {T(0), T(0)}};
-            for (int f = 0; f < N; ++f) {
+            int f = 0;
+            for (; f + RND <= N; f += RND) {
+                cx<T> a[RND], q[4][RND];
+#pragma unroll
+                for (int i = 0; i < RND; ++i) a[i] = A[size_t(f + i) * N + p];
+#pragma unroll
+                for (int kk = 0; kk < 4; ++kk)
+#pragma unroll
+                    for (int i = 0; i < RND; ++i) q[kk][i] = anti[kk] ? ph[kk][f + i] : cx<T>{T(0), T(0)};
+#pragma unroll
+                for (int kk = 0; kk < 4; ++kk)
+#pragma unroll
+                    for (int i = 0; i < RND; ++i)
+                        if (anti[kk]) cmac(acc[kk], a[i], cmul_rn(q[kk][i], cr[kk][f + i]));
+            }
+            for (; f < N; ++f) {
                 const cx<T> a = A[size_t(f) * N + p];
 #pragma unroll
                 for (int kk = 0; kk < 4; ++kk)
-                    if (anti[kk]) cmac(acc[kk], a, phi_row<T>(phase, cf, Nk, Nmax, L, js[kk], f));
+                    if (anti[kk]) cmac(acc[kk], a, cmul_rn(ph[kk][f], cr[kk][f]));
             }
 #pragma unroll
             for (int kk = 0; kk < 4; ++kk) s_rq[site * 4 + kk] = acc[kk];
@@ -954,11 +980,45 @@ __global__ void __launch_bounds__(NT) k_statspin(DevJob J)
     if (tid == 0) atomicAdd(J.ss_n, w == 0 ? 1 : 0);
 }
 
+// s + c += a x with a = ah + al (double-float) and x exact: exact product
+// (Dekker, via FMA) and compensated sum (Knuth's two-sum), every operation
+// explicitly rounded so that nothing is contracted or reassociated.
+__device__ __forceinline__ void ff_madd(float& s, float& c, float ah, float al, float x)
+{
+    const float p = __fmul_rn(ah, x);
+    const float e = __fmaf_rn(ah, x, -p);
+    const float t = __fadd_rn(s, p);
+    const float bb = __fsub_rn(t, s);
+    const float err = __fadd_rn(__fsub_rn(s, __fsub_rn(t, bb)), __fsub_rn(p, bb));
+    s = t;
+    c = __fadd_rn(c, __fadd_rn(err, __fadd_rn(e, __fmul_rn(al, x))));
+}
+
+// s + c += s2 + c2 (two double-float numbers)
+__device__ __forceinline__ void ff_add(float& s, float& c, float s2, float c2)
+{
+    const float t = __fadd_rn(s, s2);
+    const float bb = __fsub_rn(t, s);
+    const float err = __fadd_rn(__fsub_rn(s, __fsub_rn(t, bb)), __fsub_rn(s2, bb));
+    s = t;
+    c = __fadd_rn(c, __fadd_rn(err, c2));
+}
+
+__device__ __forceinline__ void ff_cmac(cx<float>& s, cx<float>& c, cx<float> ah, cx<float> al, cx<float> x)
+{
+    ff_madd(s.x, c.x, ah.x, al.x, x.x);
+    ff_madd(s.x, c.x, -ah.y, -al.y, x.y);
+    ff_madd(s.y, c.y, ah.x, al.x, x.y);
+    ff_madd(s.y, c.y, ah.y, al.y, x.x);
+}
+
 // Drift-checked re-inversion (deferred policy).  For every walker whose
 // accepted-exchange count since the last check reached reinv_every, estimate
-// ||A A^-1 - I||_max in FP64 on 8 rows f of the residual (rows rotate from
-// check to check): (A A^-1)(f, g) = sum_p phi_{2f}(x_p) (A^-1)(p, g), with A
-// rebuilt in FP64 from the orbital tables.  Walkers above the threshold (or
+// ||A A^-1 - I||_max to FP64 accuracy on 8 rows f of the residual (rows rotate
+// from check to check): (A A^-1)(f, g) = sum_p phi_{2f}(x_p) (A^-1)(p, g),
+// with A rebuilt in FP64 from the orbital tables; for an FP32-stored inverse
+// the sums run in double-float arithmetic on the FP32 pipe (GB300's FP64 rate
+// is 1/64 of its FP32 rate).  Walkers above the threshold (or
 // all of them when threshold < 0) get the FP64 Gauss-Jordan re-inversion.
 template <typename T, int NT>
 __global__ void __launch_bounds__(NT) k_check_reinvert(DevJob J, double threshold)
@@ -989,24 +1049,66 @@ __global__ void __launch_bounds__(NT) k_check_reinvert(DevJob J, double threshol
                 const int i = idx / N, p = idx % N;
                 const int site = part[p];
                 const int o = row_orbital(J, nullptr, w, fl, rows[i]);
-                arow[i * Nmax + p] = cmul_rn(J.phase64[size_t(site) * J.Nk + (o >> 1)],
+                const cx<double> v = cmul_rn(J.phase64[size_t(site) * J.Nk + (o >> 1)],
                                              coef[size_t(sublattice(site, J.L)) * Ns + o]);
+                if constexpr (sizeof(T) == 4) {   // hi + lo floats, same bytes as one FP64 complex
+                    cx<float>* ahi = reinterpret_cast<cx<float>*>(arow);
+                    const cx<float> h = {float(v.x), float(v.y)};
+                    ahi[i * Nmax + p] = h;
+                    ahi[(NR + i) * Nmax + p] = cx<float>{float(v.x - double(h.x)), float(v.y - double(h.y))};
+                } else {
+                    arow[i * Nmax + p] = v;
+                }
             }
             __syncthreads();
-            for (int g = warp; g < N; g += NW) {
-                cx<double> acc[NR];
+            if constexpr (sizeof(T) == 4) {
+                // FP32-stored inverse: the residual in double-float arithmetic on the
+                // FP32 pipe (A's FP64 entries split into hi + lo floats, exact
+                // products, compensated sums), FP64 only for the final lane sums
+                const cx<float>* ahi = reinterpret_cast<const cx<float>*>(arow);
+                const cx<float>* alo = ahi + NR * Nmax;
+                for (int g = warp; g < N; g += NW) {
+                    cx<float> sm[NR], cm[NR];
 #pragma unroll
-                for (int i = 0; i < NR; ++i) acc[i] = {0.0, 0.0};
-                for (int p = lane; p < N; p += 32) {
-                    const cx<double> x = to_d(A[size_t(g) * N + p]);
+                    for (int i = 0; i < NR; ++i) { sm[i] = {0.f, 0.f}; cm[i] = {0.f, 0.f}; }
+                    for (int p = lane; p < N; p += 32) {
+                        const cx<float> x = reinterpret_cast<const cx<float>*>(A)[size_t(g) * N + p];
 #pragma unroll
-                    for (int i = 0; i < NR; ++i) cmac(acc[i], arow[i * Nmax + p], x);
+                        for (int i = 0; i < NR; ++i) ff_cmac(sm[i], cm[i], ahi[i * Nmax + p], alo[i * Nmax + p], x);
+                    }
+#pragma unroll
+                    for (int i = 0; i < NR; ++i) {
+                        // lane sums in double-float too; FP64 only for the final value
+#pragma unroll
+                        for (int o = 16; o; o >>= 1) {
+                            ff_add(sm[i].x, cm[i].x, __shfl_xor_sync(0xffffffffu, sm[i].x, o),
+                                   __shfl_xor_sync(0xffffffffu, cm[i].x, o));
+                            ff_add(sm[i].y, cm[i].y, __shfl_xor_sync(0xffffffffu, sm[i].y, o),
+                                   __shfl_xor_sync(0xffffffffu, cm[i].y, o));
+                        }
+                        if (lane == 0) {
+                            cx<double> v = {double(sm[i].x) + double(cm[i].x), double(sm[i].y) + double(cm[i].y)};
+                            if (rows[i] == g) v.x -= 1.0;
+                            drift = fmax(drift, fmax(fabs(v.x), fabs(v.y)));
+                        }
+                    }
                 }
+            } else {
+                for (int g = warp; g < N; g += NW) {
+                    cx<double> acc[NR];
 #pragma unroll
-                for (int i = 0; i < NR; ++i) {
-                    cx<double> v = warp_sum(acc[i]);
-                    if (rows[i] == g) v.x -= 1.0;
-                    drift = fmax(drift, fmax(fabs(v.x), fabs(v.y)));
+                    for (int i = 0; i < NR; ++i) acc[i] = {0.0, 0.0};
+                    for (int p = lane; p < N; p += 32) {
+                        const cx<double> x = to_d(A[size_t(g) * N + p]);
+#pragma unroll
+                        for (int i = 0; i < NR; ++i) cmac(acc[i], arow[i * Nmax + p], x);
+                    }
+#pragma unroll
+                    for (int i = 0; i < NR; ++i) {
+                        cx<double> v = warp_sum(acc[i]);
+                        if (rows[i] == g) v.x -= 1.0;
+                        drift = fmax(drift, fmax(fabs(v.x), fabs(v.y)));
+                    }
                 }
             }
             __syncthreads();

@@ -75,7 +75,7 @@ constexpr size_t kResMinSmem = 116 * 1024;        // over half an SM's shared me
 constexpr int kResRngBatch = 32;
 
 struct ResLayout {
-    size_t fock, part, nbr, sub, coef, red, wpart, w, rv, ru4, ru4d, rq, redm, tbase, total, used;
+    size_t fock, part, nbr, sub, coef, red, wpart, w, tile, rv, ru4, ru4d, racc, rq, rqp, nb, redm, tbase, total, used;
 };
 
 __host__ __device__ inline ResLayout res_layout(int Ns, int N, bool projheis)
@@ -92,10 +92,14 @@ __host__ __device__ inline ResLayout res_layout(int Ns, int N, bool projheis)
     l.red = al(sizeof(float) * 2 * 16);
     l.wpart = al(c * 2 * 4 * 128);
     l.w = al(c * 2 * 128);
+    l.tile = al(c * (kResThreads / 32) * 32 * 33);   // per warp 32 x 32 products, row stride 33
     l.rv = al(sizeof(int16_t) * 2 * kResRngBatch);
     l.ru4 = al(sizeof(float) * kResRngBatch);
     l.ru4d = al(sizeof(double) * kResRngBatch);
+    l.racc = al(sizeof(cx<float>) * 2 * kResRngBatch);   // accepted ratio pairs of the batch
     l.rq = al(projheis ? c * 4 * Ns : 16);
+    l.rqp = al(projheis ? c * 2 * 4 * 4 * 128 : 16);   // [g][warp][slot][p] partial bond ratios
+    l.nb = al(projheis ? sizeof(int16_t) * 2 * 4 * 128 : 16);   // [g][slot][p] antiparallel neighbour or -1
     l.redm = al(sizeof(double) * 4 * (kResThreads / 32));
     l.tbase = al(sizeof(uint32_t));
     l.used = al(16);
@@ -103,26 +107,22 @@ __host__ __device__ inline ResLayout res_layout(int Ns, int N, bool projheis)
     return l;
 }
 
-// v[0..31] per lane -> lane l returns sum over the warp's lanes of v[l]
-// (recursive halving: at each round a lane keeps the half of its values
-// selected by one bit of its lane id and adds its partner's copy of that half).
-__device__ __forceinline__ cx<float> warp_transpose_sum(cx<float> (&v)[32])
+// v[0..31] per lane -> lane l returns the sum over the warp's lanes of v[l],
+// through this warp's 32 x 33 shared-memory tile (conflict-free both ways).
+__device__ __forceinline__ cx<float> warp_transpose_sum(const cx<float> (&v)[32], cx<float>* tile)
 {
     const int lane = threadIdx.x & 31;
 #pragma unroll
-    for (int k = 16; k >= 1; k >>= 1) {
-        const bool upper = (lane & k) != 0;
+    for (int j = 0; j < 32; ++j) tile[lane * 33 + j] = v[j];
+    __syncwarp();
+    cx<float> a = {0.f, 0.f}, b = {0.f, 0.f};
 #pragma unroll
-        for (int i = 0; i < k; ++i) {
-            const cx<float> send = upper ? v[i] : v[i + k];
-            const cx<float> keep = upper ? v[i + k] : v[i];
-            cx<float> recv;
-            recv.x = __shfl_xor_sync(0xffffffffu, send.x, k);
-            recv.y = __shfl_xor_sync(0xffffffffu, send.y, k);
-            v[i] = keep + recv;
-        }
+    for (int i = 0; i < 32; i += 2) {
+        a = a + tile[i * 33 + lane];
+        b = b + tile[(i + 1) * 33 + lane];
     }
-    return v[0];
+    __syncwarp();
+    return a + b;
 }
 
 __global__ void __launch_bounds__(kResThreads, 1) k_walk_gs_res(DevJob J, uint64_t nsteps, uint64_t s0, uint64_t meas,
@@ -144,10 +144,14 @@ __global__ void __launch_bounds__(kResThreads, 1) k_walk_gs_res(DevJob J, uint64
     T* s_red = reinterpret_cast<T*>(smem + lay.red);
     cx<T>* s_wpart = reinterpret_cast<cx<T>*>(smem + lay.wpart);   // [g][warp][p]
     cx<T>* s_w = reinterpret_cast<cx<T>*>(smem + lay.w);           // [g][p]
+    cx<T>* s_tile = reinterpret_cast<cx<T>*>(smem + lay.tile) + warp * 32 * 33;
     int16_t* s_rv = reinterpret_cast<int16_t*>(smem + lay.rv);     // [step][v1, v2]
     float* s_ru4 = reinterpret_cast<float*>(smem + lay.ru4);
     double* s_ru4d = reinterpret_cast<double*>(smem + lay.ru4d);
+    cx<T>* s_racc = reinterpret_cast<cx<T>*>(smem + lay.racc);
     cx<T>* s_rq = reinterpret_cast<cx<T>*>(smem + lay.rq);
+    cx<T>* s_rqp = reinterpret_cast<cx<T>*>(smem + lay.rqp);
+    int16_t* s_nb = reinterpret_cast<int16_t*>(smem + lay.nb);
     double* s_redm = reinterpret_cast<double*>(smem + lay.redm);
     uint32_t* s_tbase = reinterpret_cast<uint32_t*>(smem + lay.tbase);
 
@@ -202,13 +206,25 @@ __global__ void __launch_bounds__(kResThreads, 1) k_walk_gs_res(DevJob J, uint64
     int ae = J.amp_e[w];
     int status = GV_OK;
     int rbuf = 0;
+    int nacc = 0;   // accepted ratio pairs waiting to be multiplied into the amplitude
     const WalkCtx<T> C = {&J, w, Ns, N, L, Nk, N, N, s_fock, s_part, s_nbr, s_coef, s_rq, s_redm,
                           phase, ai_ptr<T>(J, 0, w), ai_ptr<T>(J, 1, w)};
+    // phase[v][f] for both sites of the next proposal, loaded one step ahead
+    cx<T> ph_a = {0.f, 0.f}, ph_b = {0.f, 0.f};
+    bool have_ph = false;
 
     for (uint64_t s = 0; s < nsteps; ++s, k += 4) {
         const int bi = int(s % kResRngBatch);
         if (bi == 0) {   // the next batch of proposals and accept uniforms (one lane per step)
             __syncthreads();   // every thread is done with the previous batch
+            // the amplitude (FP64, off the per-step path): the previous batch's accepted ratios
+            if (tid == 32) {
+                for (int i = 0; i < nacc; ++i) {
+                    am = am * (to_d(s_racc[2 * i]) * to_d(s_racc[2 * i + 1]));
+                    amp_normalise(am, ae);
+                }
+            }
+            nacc = 0;
             if (warp == 0 && s + lane < nsteps) {
                 const uint64_t kl = k + 4 * uint64_t(lane);
                 uint32_t x[4], y[4];
@@ -223,6 +239,14 @@ __global__ void __launch_bounds__(kResThreads, 1) k_walk_gs_res(DevJob J, uint64
             __syncthreads();
         }
         const int v1 = s_rv[2 * bi], v2 = s_rv[2 * bi + 1];
+        const cx<T> ph1 = ph_a, ph2 = ph_b;
+        const bool ph_ok = have_ph;
+        have_ph = false;
+        if (bi + 1 < kResRngBatch && s + 1 < nsteps && f < N) {
+            ph_a = phase[size_t(s_rv[2 * bi + 2]) * Nk + f];
+            ph_b = phase[size_t(s_rv[2 * bi + 3]) * Nk + f];
+            have_ph = true;
+        }
         const int f1 = s_fock[v1] >= 0 ? 0 : 1;
         const int f2 = s_fock[v2] >= 0 ? 0 : 1;
         int kind = 0, accepted;
@@ -243,7 +267,10 @@ __global__ void __launch_bounds__(kResThreads, 1) k_walk_gs_res(DevJob J, uint64
             {
                 uint32_t r[2];
                 tmem_ld2(trow + 2 * cg, r);
-                if (f < N) u = cmul_rn(phase[size_t(tg) * Nk + f], cf[s_sub[tg] * N + f]);
+                if (f < N) {
+                    const cx<T> ph = ph_ok ? (tg == v1 ? ph1 : ph2) : phase[size_t(tg) * Nk + f];
+                    u = cmul_rn(ph, cf[s_sub[tg] * N + f]);
+                }
                 tmem_wait_ld(r);
                 a = cx<T>{__uint_as_float(r[0]), __uint_as_float(r[1])};
             }
@@ -269,12 +296,14 @@ __global__ void __launch_bounds__(kResThreads, 1) k_walk_gs_res(DevJob J, uint64
                     cx<T> v[32];
 #pragma unroll
                     for (int j = 0; j < 32; ++j) v[j] = cx<T>{__uint_as_float(r[2 * j]), __uint_as_float(r[2 * j + 1])} * u;
-                    wpart[32 * c + lane] = warp_transpose_sum(v);
+                    wpart[32 * c + lane] = warp_transpose_sum(v, s_tile);
                 }
                 wg_sync(g);
-                if (f < 32 * NCH) {
+                if (f < 32 * NCH) {   // w_p - [p == c]
                     const cx<T>* wp0 = s_wpart + g * 4 * 128;
-                    s_w[g * 128 + f] = wp0[f] + wp0[128 + f] + wp0[256 + f] + wp0[384 + f];
+                    cx<T> wq = wp0[f] + wp0[128 + f] + wp0[256 + f] + wp0[384 + f];
+                    if (f == cg) wq.x -= 1.f;
+                    s_w[g * 128 + f] = wq;
                 }
                 wg_sync(g);
                 // row update: AiT[f][p] -= (w_p - [p == c]) * (A^-1)(c, f) / r
@@ -287,10 +316,8 @@ __global__ void __launch_bounds__(kResThreads, 1) k_walk_gs_res(DevJob J, uint64
 #pragma unroll
                     for (int j = 0; j < 32; ++j) {
                         const int p = 32 * c + j;
-                        cx<T> wq = wv[p];
-                        if (p == cg) wq.x -= 1.f;
                         cx<T> e = {__uint_as_float(r[2 * j]), __uint_as_float(r[2 * j + 1])};
-                        cmac(e, wq, coef);
+                        cmac(e, wv[p], coef);
                         r[2 * j] = __float_as_uint(e.x);
                         r[2 * j + 1] = __float_as_uint(e.y);
                     }
@@ -300,9 +327,10 @@ __global__ void __launch_bounds__(kResThreads, 1) k_walk_gs_res(DevJob J, uint64
                 if (tid == 0) {
                     s_fock[upt] = int16_t(cu); s_fock[upf] = -1; s_part[cu] = int16_t(upt);
                     s_fock[Ns + dnt] = int16_t(cd); s_fock[Ns + dnf] = -1; s_part[N + cd] = int16_t(dnt);
-                    am = am * (to_d(ru) * to_d(rd));
-                    amp_normalise(am, ae);
+                    s_racc[2 * nacc] = ru;
+                    s_racc[2 * nacc + 1] = rd;
                 }
+                ++nacc;
                 ++c_acc;
                 ++since;
                 __syncthreads();
@@ -316,23 +344,68 @@ __global__ void __launch_bounds__(kResThreads, 1) k_walk_gs_res(DevJob J, uint64
         }
         const uint64_t gs = s0 + s;
         if (meas && (meas == 1 || gs % meas == 0) && mask) {
-            // write both inverses back and measure from HBM/L2 as the streaming kernel
-            for (int c = 0; c < NCH; ++c) {
-                uint32_t r[64];
-                tmem_ld64(trow + 64 * c, r);
-                tmem_wait_ld(r);
+            if (mask & GV_MEAS_PROJHEIS) {
+                // ProjHeis pass 1 from TMEM: the ratio of moving particle p of flavour g to
+                // neighbour slot kk is sum_f (A^-1)(p, f) phi_{2f}(j); lane f forms its
+                // terms for 32 particles at a time (phase[j][f] is coalesced over the lanes)
+                // and the warp transposes-and-sums them; the four warps meet in shared memory.
+                cx<T>* part_g = s_rqp + (g * 4 + (warp & 3)) * 4 * 128;
+                int16_t* nb_g = s_nb + g * 4 * 128;
+                {
+                    const bool ok = f < N;
+                    const int site = ok ? s_part[g * N + f] : 0;
 #pragma unroll
-                for (int j = 0; j < 32; ++j) {
-                    const int p = 32 * c + j;
-                    if (f < N && p < N) Ag[size_t(f) * N + p] = cx<T>{__uint_as_float(r[2 * j]), __uint_as_float(r[2 * j + 1])};
+                    for (int kk = 0; kk < 4; ++kk) {
+                        const int js = s_nbr[site * 4 + kk];
+                        nb_g[kk * 128 + f] = (ok && ((s_fock[js] >= 0) != (g == 0))) ? int16_t(js) : int16_t(-1);
+                    }
                 }
+                wg_sync(g);
+                for (int c = 0; c < NCH; ++c) {
+                    uint32_t r[64];
+                    tmem_ld64(trow + 64 * c, r);
+                    tmem_wait_ld(r);
+                    for (int kk = 0; kk < 4; ++kk) {
+                        cx<T> v[32];
+                        int jsv[32];
+#pragma unroll
+                        for (int j = 0; j < 32; ++j) {   // every load of the chunk in flight at once
+                            jsv[j] = nb_g[kk * 128 + 32 * c + j];
+                            v[j] = (jsv[j] >= 0 && f < N) ? phase[size_t(jsv[j]) * Nk + f] : cx<T>{0.f, 0.f};
+                        }
+#pragma unroll
+                        for (int j = 0; j < 32; ++j) {
+                            if (jsv[j] >= 0 && f < N) {
+                                const cx<T> a = {__uint_as_float(r[2 * j]), __uint_as_float(r[2 * j + 1])};
+                                v[j] = a * cmul_rn(v[j], cf[s_sub[jsv[j]] * N + f]);
+                            }
+                        }
+                        part_g[kk * 128 + 32 * c + lane] = warp_transpose_sum(v, s_tile);
+                    }
+                }
+                wg_sync(g);
+                if (f < N) {
+                    const cx<T>* q = s_rqp + g * 4 * 4 * 128;
+                    const int site = s_part[g * N + f];
+#pragma unroll
+                    for (int kk = 0; kk < 4; ++kk) {
+                        const int i = kk * 128 + f;
+                        s_rq[site * 4 + kk] = q[i] + q[512 + i] + q[1024 + i] + q[1536 + i];
+                    }
+                }
+                __syncthreads();
+                projheis_from_rq<T, kResThreads>(C);
             }
-            __syncthreads();
-            measure_now<T, kResThreads>(C, mask);
-            __syncthreads();
+            if (mask & GV_MEAS_STAGMAGN) stagmagn_now<T, kResThreads>(C);
         }
     }
     __syncthreads();
+    if (tid == 32) {
+        for (int i = 0; i < nacc; ++i) {
+            am = am * (to_d(s_racc[2 * i]) * to_d(s_racc[2 * i + 1]));
+            amp_normalise(am, ae);
+        }
+    }
     // write back: both inverses from TMEM, occupancy, counters
     for (int c = 0; c < NCH; ++c) {
         uint32_t r[64];
@@ -357,9 +430,11 @@ __global__ void __launch_bounds__(kResThreads, 1) k_walk_gs_res(DevJob J, uint64
         cn[2] += c_noop;
         cn[3] += c_rej;
         J.since_reinv[w] = since;
+        J.status[w] = status;
+    }
+    if (tid == 32) {
         J.amp_m[w] = am;
         J.amp_e[w] = ae;
-        J.status[w] = status;
     }
     tmem_fence_before();
     __syncthreads();

@@ -128,3 +128,18 @@ def test_resident_deferred_reinversion_and_drift_policy(engine):
     d, n = job.drift_checks()
     assert n.sum() + job.counts()[:, 4].sum() > 0     # checks happened
     assert job.drift().max() < 1e-4
+
+
+def test_double_float_drift_check_matches_fp64(engine):
+    """The drift check of an FP32-stored inverse runs in double-float
+    arithmetic; its sampled drift never exceeds the full FP64 residual and
+    tracks it (threshold high enough that nothing is re-inverted)."""
+    L, W = 12, 64
+    job = _job(engine, L, W, 17, reinv_every=32, drift_threshold=1.0)
+    job.init_walkers()
+    job.walk(L * L * 8, 0)
+    seen, n = job.drift_checks()
+    full = job.drift().max(axis=1)
+    assert (n > 0).all()
+    assert (seen <= full * (1 + 1e-6) + 1e-12).all()
+    assert np.median(seen / full) > 0.05
