@@ -462,6 +462,7 @@ def main():
     ms_launch = res["walk_ms"] / max(1, res["walk_launches"])
     achieved = bytes_step * per_launch_steps / (ms_launch * 1e-3) / 1e9
     peak, peak_kind = measured_peaks()
+    resident = args.precision == "mixed" and L * L // 2 <= 128
     out = {"metric": METRIC, "value": value, "unit": "steps/s", "n_gpus": world, "steps": args.steps,
            "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
            "vs_baseline": None, "dtype": "f32" if args.precision == "mixed" else "f64", "data": "synthetic",
@@ -470,8 +471,14 @@ def main():
                    if e2e else None),
            "gpu_launches": int(res["launches"]),
            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                        "frac": achieved / peak, "traffic": None, "peak_kind": peak_kind,
-                        "kernel": "k_walk_gs", "bytes_per_step": bytes_step,
+                        "frac": achieved / peak, "peak_kind": peak_kind,
+                        # DRAM bytes per walk launch from one ncu capture of the same kernel at
+                        # 304 walkers (profiles/), scaled by walkers: each walker's inverses are
+                        # loaded and stored once per launch
+                        "traffic": (108.2e6 * WALKERS / 304) if resident else None,
+                        "kernel": "k_walk_gs_res" if resident else "k_walk_gs", "bytes_per_step": bytes_step,
+                        "bytes_per_step_meaning": "HBM bytes the streaming formulation of a Metropolis step moves "
+                                                  "(inverse rows and columns, accepted-move read-modify-write)",
                         "kernel_ms_per_launch": ms_launch},
            "kernel_share": {"walk_ms": res["walk_ms"], "reinversion_ms": res["inv_ms"],
                             "reinversion_launches": res["inv_launches"], "total_ms": res["ms"]},
