@@ -11,7 +11,8 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "_lib", "libgpvmc_gb300.so")
 
 GV_OK = 0
-GV_ERR_OOM, GV_ERR_CUDA = 7, 8
+GV_ERR_TIMEOUT, GV_ERR_OOM, GV_ERR_CUDA = 6, 7, 8
+GV_REQ_PENDING, GV_REQ_RUNNING, GV_REQ_DONE = 0, 1, 2
 STATUS_NAMES = {0: "ok", 1: "invalid", 2: "singular", 3: "nan", 4: "zero amplitude", 5: "drift",
                 6: "timeout", 7: "out of memory", 8: "cuda error", 9: "not ready", 10: "too large"}
 
@@ -39,6 +40,22 @@ class JobConfig(ctypes.Structure):
                 ("precision", ctypes.c_int32), ("seed", ctypes.c_uint64), ("walker_base", ctypes.c_uint32),
                 ("reinv_every", ctypes.c_int32), ("meas_mask", ctypes.c_int32), ("flags", ctypes.c_int32),
                 ("drift_threshold", ctypes.c_double)]
+
+class ServerConfig(ctypes.Structure):
+    _fields_ = [("hbm_budget", ctypes.c_uint64), ("max_jobs", ctypes.c_int32), ("chunk_sweeps", ctypes.c_int32)]
+
+
+class Request(ctypes.Structure):
+    _fields_ = [("job", JobConfig), ("therm_sweeps", ctypes.c_uint64), ("sweeps", ctypes.c_uint64),
+                ("meas", ctypes.c_uint64), ("validate", ctypes.c_int32), ("pad", ctypes.c_int32)]
+
+
+class Result(ctypes.Structure):
+    _fields_ = [("state", ctypes.c_int32), ("status", ctypes.c_int32), ("steps", ctypes.c_uint64),
+                ("accepted", ctypes.c_uint64), ("footprint", ctypes.c_uint64), ("e_site", ctypes.c_double),
+                ("stagmagn", ctypes.c_double), ("validation_error", ctypes.c_double), ("t_submit", ctypes.c_double),
+                ("t_admit", ctypes.c_double), ("t_done", ctypes.c_double)]
+
 
 
 class Trace(ctypes.Structure):
@@ -74,6 +91,14 @@ _SIGS = {
     "gv_job_read_state_index": [_P, ctypes.c_void_p],
     "gv_job_read_weight": [_P, ctypes.c_void_p],
     "gv_job_read_status": [_P, ctypes.c_void_p],
+    "gv_job_walk_continue": [_P, ctypes.c_uint64, ctypes.c_uint64],
+    "gv_job_stream": [_P, ctypes.c_void_p],
+    "gv_server_create": [ctypes.c_void_p, ctypes.c_void_p],
+    "gv_server_submit": [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p],
+    "gv_server_poll": [ctypes.c_void_p, ctypes.c_uint64, ctypes.c_void_p],
+    "gv_server_wait": [ctypes.c_void_p, ctypes.c_uint64, ctypes.c_double, ctypes.c_void_p],
+    "gv_server_drain": [ctypes.c_void_p, ctypes.c_double],
+    "gv_server_destroy": [ctypes.c_void_p],
     "gv_job_read_orbitals": [_P, ctypes.c_int32, ctypes.c_int32, ctypes.c_void_p],
     "gv_job_read_projheis": [_P, ctypes.c_void_p, ctypes.c_void_p],
     "gv_job_read_stagmagn": [_P, ctypes.c_void_p, ctypes.c_void_p],

@@ -17,7 +17,7 @@ CSRC = os.path.join(HERE, "csrc")
 OUT_DIR = os.path.join(HERE, "_lib")
 LIB = os.path.join(OUT_DIR, "libgpvmc_gb300.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-SOURCES = ["engine.cu", "model.cpp", "noalloc.cu"]
+SOURCES = ["engine.cu", "model.cpp", "noalloc.cu", "server.cpp"]
 
 
 def nvcc():
@@ -28,7 +28,7 @@ def nvcc():
 
 
 def _flags():
-    return ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-ffp-contract=off",
+    return ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-ffp-contract=off,-pthread",
                    "-I" + os.path.join(ROOT, "include"), "-I" + CSRC]
 
 
@@ -52,7 +52,7 @@ def build(verbose=False, extra=()):
         for log in logs:
             sys.stderr.write(log)
     tmp = LIB + ".tmp"
-    cmd = [nvcc(), "-shared", "-o", tmp] + objs + ARCH + ["-lcudart"]
+    cmd = [nvcc(), "-shared", "-o", tmp] + objs + ARCH + ["-lcudart", "-Xcompiler", "-pthread"]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode:
         raise RuntimeError("link failed:\n%s\n%s" % (" ".join(cmd), r.stderr))

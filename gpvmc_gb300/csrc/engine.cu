@@ -907,7 +907,8 @@ gv_status gv_job_init_walkers(gv_job* j, const int8_t* up)
     return j->trans ? gv_job_synchronize(j) : GV_OK;
 }
 
-static gv_status walk_impl(gv_job* j, uint64_t len, uint64_t meas, gv_trace* dtrace, int trace_walker)
+static gv_status walk_impl(gv_job* j, uint64_t len, uint64_t meas, gv_trace* dtrace, int trace_walker,
+                           bool reset = true)
 {
     if (!j) return GV_ERR_INVALID;
     if (!j->ready) return GV_ERR_NOT_READY;
@@ -915,7 +916,7 @@ static gv_status walk_impl(gv_job* j, uint64_t len, uint64_t meas, gv_trace* dtr
     j->d.trace = dtrace;
     j->d.trace_walker = trace_walker;
     j->last_launches = 0;
-    if (meas) {
+    if (meas && reset) {
         gv_status rs = reset_quantities(j);
         if (rs) return rs;
     }
@@ -956,6 +957,18 @@ static gv_status walk_impl(gv_job* j, uint64_t len, uint64_t meas, gv_trace* dtr
 }
 
 gv_status gv_job_walk(gv_job* j, uint64_t len, uint64_t meas) { return walk_impl(j, len, meas, nullptr, -1); }
+
+gv_status gv_job_walk_continue(gv_job* j, uint64_t len, uint64_t meas)
+{
+    return walk_impl(j, len, meas, nullptr, -1, false);
+}
+
+gv_status gv_job_stream(gv_job* j, void** stream)
+{
+    if (!j || !stream) return GV_ERR_INVALID;
+    *stream = j->stream;
+    return GV_OK;
+}
 
 gv_status gv_job_walk_traced(gv_job* j, uint64_t len, uint64_t meas, int32_t walker, gv_trace* trace)
 {

@@ -141,6 +141,13 @@ gv_status gv_job_init_walkers(gv_job* job, const int8_t* up);
  * no measurement).  Quantities are reset at the start of a measuring walk
  * (MetroMC.cpp:49-51).  Enqueued on the job's stream; returns immediately. */
 gv_status gv_job_walk(gv_job* job, uint64_t len, uint64_t meas);
+/* As gv_job_walk, but the quantity sums keep accumulating from the previous
+ * call instead of restarting (a long MetroMC::Walk cut into pieces: with len
+ * a multiple of meas the measurement points are the same). */
+gv_status gv_job_walk_continue(gv_job* job, uint64_t len, uint64_t meas);
+/* The job's CUDA stream (cudaStream_t), for callers that order their own work
+ * after the job's kernels. */
+gv_status gv_job_stream(gv_job* job, void** stream);
 /* As gv_job_walk, also recording walker `walker`'s per-step trace into the
  * host array trace[len] (synchronous). */
 gv_status gv_job_walk_traced(gv_job* job, uint64_t len, uint64_t meas, int32_t walker, gv_trace* trace);
@@ -262,6 +269,64 @@ const char* gv_status_string(gv_status s);
 /* The CUDA runtime's message for the last CUDA error this thread's calls into
  * the library met (behind a GV_ERR_CUDA / GV_ERR_OOM status), "" if none. */
 const char* gv_last_cuda_error(void);
+
+/* ---- Serving: a request loop with continuous batching -------------------
+ * Requests (a job configuration plus thermalisation and measured sweeps) are
+ * queued as they arrive; a host thread admits them in arrival order while the
+ * device bytes of the admitted jobs (gv_job_footprint) stay within the budget
+ * and a slot is free, keeps every admitted job's walkers resident on the
+ * device, advances all admitted jobs concurrently (each on its own stream,
+ * two walk calls of chunk_sweeps sweeps in flight per job, so their kernels
+ * overlap on the GPU), and retires each job when its sweeps are done.  A job
+ * depends only on its own request: its results are the same alone and in the
+ * mix. */
+typedef struct gv_server gv_server;
+
+typedef struct {
+    uint64_t hbm_budget;      /* device bytes the admitted jobs may hold; 0: 80% of the free memory */
+    int32_t max_jobs;         /* jobs on the device at once */
+    int32_t chunk_sweeps;     /* sweeps per walk call of a job (re-inversion checks run at call ends) */
+} gv_server_config;
+
+typedef struct {
+    gv_job_config job;        /* wavefunction, walkers, precision, seed, re-inversion policy, meas_mask */
+    uint64_t therm_sweeps;    /* sweeps (L*L steps) before measuring */
+    uint64_t sweeps;          /* measured sweeps */
+    uint64_t meas;            /* steps between measurements; divides L*L */
+    int32_t validate;         /* 1: at the end compare one ProjHeis measurement with fresh FP64 inverses */
+    int32_t pad;
+} gv_request;
+
+#define GV_REQ_PENDING 0
+#define GV_REQ_RUNNING 1
+#define GV_REQ_DONE 2
+
+typedef struct {
+    int32_t state;            /* GV_REQ_* */
+    gv_status status;         /* the job's status once done */
+    uint64_t steps;           /* Metropolis steps over all walkers, thermalisation included */
+    uint64_t accepted;        /* accepted exchanges */
+    uint64_t footprint;       /* device bytes the job was admitted with */
+    double e_site;            /* ground state: mean over walkers of the ProjHeis E/site average;
+                                 exciton: mean over walkers of Re tr H / (Ns Re tr O) */
+    double stagmagn;          /* mean over walkers of the StagMagnZ average */
+    double validation_error;  /* validate = 1: ground state max |dE/site| over walkers; exciton
+                                 max |H,O - H,O(FP64)| / max |H,O(FP64)|; -1 otherwise */
+    double t_submit, t_admit, t_done;   /* seconds since the server started */
+} gv_result;
+
+gv_status gv_server_create(const gv_server_config* cfg, gv_server** out);
+/* Queue a request; returns its ticket.  GV_ERR_INVALID for a configuration
+ * the engine rejects (checked at submission). */
+gv_status gv_server_submit(gv_server* srv, const gv_request* req, uint64_t* ticket);
+/* State and, once done, results of a request (non-blocking). */
+gv_status gv_server_poll(gv_server* srv, uint64_t ticket, gv_result* out);
+/* Wait until the request is done or timeout_s elapsed (GV_ERR_TIMEOUT). */
+gv_status gv_server_wait(gv_server* srv, uint64_t ticket, double timeout_s, gv_result* out);
+/* Wait until every submitted request is done (GV_ERR_TIMEOUT after timeout_s). */
+gv_status gv_server_drain(gv_server* srv, double timeout_s);
+/* Finish the admitted and queued requests, then stop the loop and free it. */
+gv_status gv_server_destroy(gv_server* srv);
 
 #ifdef __cplusplus
 }
