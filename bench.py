@@ -365,6 +365,77 @@ def run_exciton(g, sweeps, fp64_sweeps):
     return out
 
 
+# ---------------------------------------------------------------------------
+# Serving stream: Poisson arrivals (20 jobs/s) of heterogeneous requests --
+# L in {8,12,16,20,24}, phi ~ U[0,0.5) pi, neel ~ U[0,0.2), ground state 80% /
+# transverse exciton 20% (q on the diagonal), 64-1024 walkers (log-uniform) --
+# served by the engine's request loop with footprint admission.
+
+SERVE_JOBS = 48
+SERVE_RATE = 20.0          # jobs per second
+SERVE_SWEEP_SCALE = 200    # sweeps per job: log-uniform [1e3, 1e4] / 200 = [5, 50]
+
+
+def serving_requests(g, n=SERVE_JOBS):
+    import numpy as np
+    rng = np.random.default_rng(SEED)
+    reqs, t = [], 0.0
+    for i in range(n):
+        t += rng.exponential(1.0 / SERVE_RATE)
+        L = int(rng.choice([8, 12, 16, 20, 24]))
+        phi, neel = math.pi * rng.uniform(0.0, 0.5), rng.uniform(0.0, 0.2)
+        if rng.uniform() < 0.2:
+            qn = int(rng.integers(0, L // 2))
+            wav = g.StagFluxTransExciton(L, phi, neel, q=(qn, qn))
+        else:
+            wav = g.StagFluxGroundState(L, phi, neel)
+        walkers = int(round(math.exp(rng.uniform(math.log(64), math.log(1024)))))
+        sweeps = max(1, int(round(math.exp(rng.uniform(math.log(1e3), math.log(1e4))) / SERVE_SWEEP_SCALE)))
+        reqs.append((t, dict(wav=wav, walkers=walkers, sweeps=sweeps, therm_sweeps=max(1, sweeps // 5),
+                             seed=SEED + i, walker_base=0, precision="mixed", validate=(i % 6 == 0))))
+    return reqs
+
+
+def run_serving(g):
+    import numpy as np
+    reqs = serving_requests(g)
+    srv = g.Server(max_jobs=32, chunk_sweeps=4)
+    tickets = []
+    t0 = time.perf_counter()
+    for t_arr, r in reqs:
+        dt = t_arr - (time.perf_counter() - t0)
+        if dt > 0:
+            time.sleep(dt)
+        tickets.append(srv.submit(**r))
+    srv.drain(1800)
+    res = [srv.poll(t) for t in tickets]
+    srv.close()
+    ok = [r for r in res if r["status"] == 0]
+    lat = np.array([r["t_done"] - r["t_submit"] for r in ok])
+    queue = np.array([r["t_admit"] - r["t_submit"] for r in ok])
+    span = max(r["t_done"] for r in ok) - min(r["t_submit"] for r in res)
+    steps = sum(r["steps"] for r in ok)
+    gs_err = [r["validation_error"] for (t, q), r in zip(reqs, res)
+              if r["status"] == 0 and r["validation_error"] >= 0 and q["wav"].channel == "groundstate"]
+    tr_err = [r["validation_error"] for (t, q), r in zip(reqs, res)
+              if r["status"] == 0 and r["validation_error"] >= 0 and q["wav"].channel == "trans"]
+    return {"workload": "%d requests, Poisson arrivals at %g/s, L~U{8,12,16,20,24}, phi~U[0,0.5)pi, "
+                        "neel~U[0,0.2), ground state 80%% / transverse exciton 20%% (q on the diagonal), "
+                        "64-1024 walkers log-uniform, sweeps log-uniform [1e3,1e4] scaled by 1/%d, mixed "
+                        "precision, drift-checked FP64 re-inversion every 128 accepted moves; ProjHeis and "
+                        "StagMagnZ every sweep" % (SERVE_JOBS, SERVE_RATE, SERVE_SWEEP_SCALE),
+            "jobs": len(res), "failed": len(res) - len(ok),
+            "latency_p50_s": float(np.percentile(lat, 50)), "latency_p99_s": float(np.percentile(lat, 99)),
+            "queue_p50_s": float(np.percentile(queue, 50)), "queue_p99_s": float(np.percentile(queue, 99)),
+            "steps_per_s": steps / span, "wall_s": span, "steps": int(steps),
+            "e_site_error_vs_fp64_max": max(gs_err) if gs_err else None,
+            "exciton_ho_error_vs_fp64_max": max(tr_err) if tr_err else None,
+            "validated_jobs": len(gs_err) + len(tr_err),
+            "what": "latency = done - submitted (host clock, includes queueing, walker start and FP64 start "
+                    "inversions); error: the job's final configurations measured with its own inverses and "
+                    "with fresh FP64 inverses"}
+
+
 def main():
     global WALKERS
     ap = argparse.ArgumentParser()
@@ -379,6 +450,7 @@ def main():
     ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end leg (profiling runs)")
     ap.add_argument("--walkers", type=int, default=WALKERS, help="walkers (profiling a smaller case)")
     ap.add_argument("--no-exciton", action="store_true", help="skip the exciton-channel section")
+    ap.add_argument("--no-serving", action="store_true", help="skip the serving-stream section")
     args = ap.parse_args()
 
     rank = int(os.environ.get("RANK", "0"))
@@ -444,6 +516,7 @@ def main():
                   "reinversion_policy": "FP64 re-inversion every 128 accepted exchanges", "steps": k}
 
     exc = run_exciton(g, 4, 1) if (rank == 0 and not args.no_exciton) else None
+    serving = run_serving(g) if (rank == 0 and world == 1 and not args.no_serving) else None
     e2e = run_e2e(g, args.precision, args.steps, rank) if not args.no_e2e else None
     if dist and e2e:
         import torch
@@ -502,6 +575,8 @@ def main():
         if cpu_exc:
             exc["cpu_baseline"] = {k: cpu_exc[k] for k in ("value", "unit", "cores", "kind", "sample", "per_core")}
         out["exciton"] = exc
+    if serving:
+        out["serving"] = serving
     print(json.dumps(out))
 
 

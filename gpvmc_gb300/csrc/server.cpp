@@ -3,18 +3,21 @@
 // concurrently (continuous batching).  Host-side C++ over the engine's C ABI;
 // declared in include/gpvmc_gb300.h.
 //
-// One worker thread owns every job.  Each pass over its state it
+// A worker thread schedules every job.  Each pass over its state it
 //   1. admits queued requests in arrival order while a slot is free and the
 //      admitted jobs' gv_job_footprint bytes stay within the budget (a request
 //      larger than the whole budget runs when the device is otherwise empty),
-//      creating the job and its walkers (vmc.cpp:140-263 for one request);
+//      and creates the job and its walkers (vmc.cpp:140-263 for one request)
+//      on a helper thread, since the FP64 start inversions take a while;
 //   2. keeps two walk calls of chunk_sweeps sweeps in flight on every admitted
 //      job's stream (thermalisation first, then the measured sweeps, whose
 //      quantity sums accumulate across calls), so that work of all admitted
 //      jobs overlaps on the device;
-//   3. retires jobs whose calls have completed: reads their results
-//      (optionally re-measures the final configurations with fresh FP64
-//      inverses), frees the job and its bytes, and wakes waiting callers.
+//   3. retires jobs whose calls have completed: a helper thread reads their
+//      results (optionally re-measures the final configurations with fresh
+//      FP64 inverses), frees the job and its bytes, and wakes waiting callers.
+// A job is touched by one thread at a time (its helper, then the worker, then
+// its helper); jobs run on their own streams.
 // A job's chain depends only on its own request (seed, walkers, chunking), so
 // its results do not depend on what else is running.
 #include <cuda_runtime.h>
@@ -24,6 +27,7 @@
 #include <cmath>
 #include <condition_variable>
 #include <deque>
+#include <future>
 #include <map>
 #include <memory>
 #include <mutex>
@@ -48,6 +52,8 @@ struct Req {
     int inflight = 0;        // issued calls not yet seen complete
     uint64_t therm_calls = 0;
     uint64_t chunk_len = 0;  // steps per call
+    std::future<gv_status> start_f;   // job creation and walker start on a helper thread
+    std::future<void> finish_f;       // result collection on a helper thread
 };
 
 }  // namespace
@@ -60,7 +66,9 @@ struct gv_server {
     std::condition_variable cv_work, cv_done;
     std::deque<Req*> pending;
     std::map<uint64_t, std::unique_ptr<Req>> reqs;
-    std::vector<Req*> running;   // worker thread only
+    std::vector<Req*> starting;  // worker thread only: jobs being created
+    std::vector<Req*> running;   // worker thread only: jobs whose walks are being issued
+    std::vector<Req*> finishing; // worker thread only: jobs whose results are being collected
     uint64_t next_ticket = 1;
     uint64_t used = 0;
     int n_running = 0;
@@ -70,7 +78,7 @@ struct gv_server {
 
     double now() const { return std::chrono::duration<double>(Clock::now() - t0).count(); }
     void run();
-    void start(Req* q);
+    gv_status start(Req* q);
     void finish(Req* q, gv_status st);
     bool advance(Req* q);
 };
@@ -157,6 +165,7 @@ gv_status validate(gv_job* j, const gv_job_config& c, int W, int Ns, int Nexc, d
 
 void gv_server::finish(Req* q, gv_status st)
 {
+    cudaSetDevice(device);
     const gv_job_config& c = q->r.job;
     gv_result res = q->res;
     res.validation_error = -1.0;
@@ -185,8 +194,11 @@ void gv_server::finish(Req* q, gv_status st)
     cv_done.notify_all();
 }
 
-void gv_server::start(Req* q)
+// Job creation and walker start (FP64 start inversions, the exciton's state
+// pick): on a helper thread, so that the worker keeps issuing other jobs' walks.
+gv_status gv_server::start(Req* q)
 {
+    cudaSetDevice(device);
     const gv_job_config& c = q->r.job;
     gv_status st = gv_job_create(&c, &q->job);
     if (!st) st = gv_job_set_meas_mask(q->job, c.meas_mask);
@@ -194,13 +206,12 @@ void gv_server::start(Req* q)
     if (!st && (cudaEventCreateWithFlags(&q->ev[0], cudaEventDisableTiming) != cudaSuccess ||
                 cudaEventCreateWithFlags(&q->ev[1], cudaEventDisableTiming) != cudaSuccess))
         st = GV_ERR_CUDA;
-    if (st) { finish(q, st); return; }
     const uint64_t sweep = uint64_t(c.L) * c.L;
     const uint64_t cs = uint64_t(std::max(1, cfg.chunk_sweeps));
     q->chunk_len = cs * sweep;
     q->therm_calls = (q->r.therm_sweeps + cs - 1) / cs;
     q->total = q->therm_calls + (q->r.sweeps + cs - 1) / cs;
-    running.push_back(q);
+    return st;
 }
 
 // Issue calls up to two in flight, retire completed ones; true if anything moved.
@@ -241,7 +252,7 @@ void gv_server::run()
         std::vector<Req*> admit;
         {
             std::lock_guard<std::mutex> lk(m);
-            if (stop && pending.empty() && n_running == 0) break;
+            if (stop && pending.empty() && n_running == 0 && starting.empty() && finishing.empty()) break;
             while (!pending.empty() && n_running < cfg.max_jobs) {
                 Req* q = pending.front();
                 if (used + q->footprint > budget && n_running > 0) break;
@@ -254,13 +265,40 @@ void gv_server::run()
             }
         }
         bool moved = !admit.empty();
-        for (Req* q : admit) start(q);
+        for (Req* q : admit) {
+            q->start_f = std::async(std::launch::async, [this, q] { return start(q); });
+            starting.push_back(q);
+        }
+        for (size_t i = 0; i < starting.size();) {
+            Req* q = starting[i];
+            if (q->start_f.wait_for(std::chrono::seconds(0)) != std::future_status::ready) { ++i; continue; }
+            const gv_status st = q->start_f.get();
+            starting.erase(starting.begin() + i);
+            if (st) {
+                q->finish_f = std::async(std::launch::async, [this, q, st] { finish(q, st); });
+                finishing.push_back(q);
+            } else {
+                running.push_back(q);
+            }
+            moved = true;
+        }
         for (size_t i = 0; i < running.size();) {
             Req* q = running[i];
             moved |= advance(q);
             if (q->issued == q->total && q->inflight == 0) {
                 running.erase(running.begin() + i);
-                finish(q, q->res.status);
+                const gv_status st = q->res.status;
+                q->finish_f = std::async(std::launch::async, [this, q, st] { finish(q, st); });
+                finishing.push_back(q);
+                moved = true;
+            } else {
+                ++i;
+            }
+        }
+        for (size_t i = 0; i < finishing.size();) {
+            if (finishing[i]->finish_f.wait_for(std::chrono::seconds(0)) == std::future_status::ready) {
+                finishing[i]->finish_f.get();
+                finishing.erase(finishing.begin() + i);
                 moved = true;
             } else {
                 ++i;
