@@ -376,6 +376,81 @@ SERVE_RATE = 20.0          # jobs per second
 SERVE_SWEEP_SCALE = 200    # sweeps per job: log-uniform [1e3, 1e4] / 200 = [5, 50]
 
 
+PAIR_MEAS = 4
+
+
+def run_pairs(g, walkers):
+    """StatSpinStruct on the headline workload's configurations: every
+    antiparallel pair ratio of every walker, as split-TF32 tensor-core
+    G = Phi A^-1 products (k_statspin_tc) and, beside it, as FP32 dot products
+    on the CUDA cores; both against fresh FP64 inverses of the same
+    configurations."""
+    import numpy as np
+    job = make_job(g, "mixed", 0)
+    job.init_walkers()
+    for _ in range(4):
+        job.walk(SWEEP, 0, sync=False)
+    job.synchronize()
+    cfg = job.config()
+    job.set_measurements(4)
+
+    def timed(j, n):
+        j.reset_quantities()
+        j.measure()   # warm-up
+        j.reset_quantities()
+        j.timer_start()
+        for _ in range(n):
+            j.measure()
+        j.timer_stop()
+        ms, launches = j.kernel_ms(2)
+        return ms / max(1, launches), j.statspin()[0]
+
+    ms_tc, ss_tc = timed(job, PAIR_MEAS)
+    job.close()
+    from gpvmc_gb300.replicas import walker_base
+    wav = g.StagFluxGroundState(L, 0.25 * math.pi, 0.0)
+    common = dict(walkers=walkers, seed=SEED, reinv_every=REINV, walker_base=walker_base(0, walkers),
+                  phi_range=PHI_RANGE, neel_range=NEEL_RANGE, deferred_reinversion=True)
+    js = g.Job(wav, precision="mixed", scalar_pairs=True, **common)
+    js.init_walkers(cfg)
+    js.set_measurements(4)
+    ms_sc, ss_sc = timed(js, 1)
+    js.close()
+    j64 = g.Job(wav, precision="fp64", **common)
+    j64.init_walkers(cfg)
+    j64.set_measurements(4)
+    j64.reset_quantities()
+    j64.measure()
+    ss64 = j64.statspin()[0]
+    j64.close()
+    # ss_tc holds PAIR_MEAS measurements of the same configurations, ss_sc one
+    scale = np.abs(ss64[1:3]).max()
+    err_tc = float(np.abs(ss_tc[1:3] / PAIR_MEAS - ss64[1:3]).max() / scale)
+    err_sc = float(np.abs(ss_sc[1:3] - ss64[1:3]).max() / scale)
+    N = L * L // 2
+    useful = 2 * 8.0 * N ** 3 * walkers              # two complex N^3 products per walker
+    executed = 2 * 3 * 4 * 2.0 * 128 * N * N * walkers   # 3 split terms x 4 real products, M padded to 128
+    peak_tf32 = None
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            peak_tf32 = float(json.load(f)["bf16_tflops"]) / 2
+    except Exception:
+        peak_tf32 = 1900.0 / 2
+    tens = executed / (ms_tc * 1e-3) / 1e12
+    return {"workload": "StatSpinStruct of %d walkers at L=16 (all 128x128 antiparallel pair ratios per walker), "
+                        "configurations of the headline workload after 4 sweeps" % walkers,
+            "kernel": "k_statspin_tc (tcgen05.mma kind::tf32, split precision, FP32 accumulation in TMEM)",
+            "ms_per_measurement": ms_tc, "scalar_ms_per_measurement": ms_sc,
+            "speedup_over_cuda_cores": ms_sc / ms_tc,
+            "useful_tflops": useful / (ms_tc * 1e-3) / 1e12,
+            "tensor_tflops_executed": tens,
+            "tensor_peak_tflops": peak_tf32,
+            "tensor_frac": tens / peak_tf32,
+            "tensor_peak_kind": "TF32 dense = half the measured bf16 dense burst (the nominal ratio)",
+            "pair_error_vs_fp64": err_tc, "scalar_pair_error_vs_fp64": err_sc,
+            "error_what": "max |s+-, s-+ (engine) - same from fresh FP64 inverses| / max |s+-, s-+|"}
+
+
 def serving_requests(g, n=SERVE_JOBS):
     import numpy as np
     rng = np.random.default_rng(SEED)
@@ -451,6 +526,7 @@ def main():
     ap.add_argument("--walkers", type=int, default=WALKERS, help="walkers (profiling a smaller case)")
     ap.add_argument("--no-exciton", action="store_true", help="skip the exciton-channel section")
     ap.add_argument("--no-serving", action="store_true", help="skip the serving-stream section")
+    ap.add_argument("--no-pairs", action="store_true", help="skip the StatSpinStruct tensor-core section")
     args = ap.parse_args()
 
     rank = int(os.environ.get("RANK", "0"))
@@ -517,6 +593,7 @@ def main():
 
     exc = run_exciton(g, 4, 1) if (rank == 0 and not args.no_exciton) else None
     serving = run_serving(g) if (rank == 0 and world == 1 and not args.no_serving) else None
+    pairs = run_pairs(g, WALKERS) if (rank == 0 and not args.no_pairs) else None
     e2e = run_e2e(g, args.precision, args.steps, rank) if not args.no_e2e else None
     if dist and e2e:
         import torch
@@ -577,6 +654,8 @@ def main():
         out["exciton"] = exc
     if serving:
         out["serving"] = serving
+    if pairs:
+        out["statspin_tensor_cores"] = pairs
     print(json.dumps(out))
 
 

@@ -23,6 +23,8 @@ GV_FLAG_REINV_DEFERRED = 1
 GV_FLAG_REINV_ON_DRIFT = 2
 GV_FLAG_DELAYED_UPDATES = 4
 GV_FLAG_STREAM_INVERSES = 8
+GV_FLAG_SCALAR_PAIRS = 16
+GV_CKPT_INVERSES = 1
 
 
 class GvError(RuntimeError):
@@ -93,6 +95,9 @@ _SIGS = {
     "gv_job_read_status": [_P, ctypes.c_void_p],
     "gv_job_walk_continue": [_P, ctypes.c_uint64, ctypes.c_uint64],
     "gv_job_stream": [_P, ctypes.c_void_p],
+    "gv_job_checkpoint_size": [_P, ctypes.c_int32, ctypes.POINTER(ctypes.c_uint64)],
+    "gv_job_checkpoint": [_P, ctypes.c_int32, ctypes.c_void_p, ctypes.c_uint64, ctypes.POINTER(ctypes.c_uint64)],
+    "gv_job_restore": [_P, ctypes.c_void_p, ctypes.c_uint64],
     "gv_server_create": [ctypes.c_void_p, ctypes.c_void_p],
     "gv_server_submit": [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p],
     "gv_server_poll": [ctypes.c_void_p, ctypes.c_uint64, ctypes.c_void_p],

@@ -161,7 +161,8 @@ struct DevJob {
     int32_t* pj_n;
     cx<double>* sm;            // W
     int32_t* sm_n;
-    double* ss;                // 5*Ns*Ns complex (interleaved) job-wide
+    double* ss;                // job-wide StatSpinStruct sums, compact: T (Ns*Ns complex) then
+                               // Aud (Ns*Ns real) in a 10*Ns*Ns-double buffer
     int32_t* ss_n;
     cx<double>* scratch64;     // per-CTA FP64 N*N scratch for re-inversion (W*Nmax*Nmax)
     gv_trace* trace;

@@ -23,6 +23,7 @@
 #include "kernels.cuh"
 #include "kernels_trans.cuh"
 #include "kernels_res.cuh"
+#include "kernels_tc.cuh"
 #include "model.hpp"
 
 using namespace gv;
@@ -57,6 +58,7 @@ struct gv_job {
     std::vector<double> kind_each[3];
     std::vector<double> wphi, wneel;
     std::vector<uint64_t> start_draws;   // Philox stream-1 uniform index per walker
+    int n_sm = 1;                        // SMs of the job's device (persistent grids)
     bool trans = false;                  // transverse-exciton channel
     std::vector<int16_t> exu, exd;       // channel tables (Channel::exc_up / exc_dn)
 };
@@ -100,7 +102,8 @@ bool valid_config(const gv_job_config* c)
     if (c->n_walkers < 1 || c->n_walkers > (1 << 20)) return false;
     if (c->precision != GV_PREC_FP64 && c->precision != GV_PREC_MIXED) return false;
     if (c->reinv_every < 0) return false;
-    if (c->flags & ~(GV_FLAG_REINV_DEFERRED | GV_FLAG_REINV_ON_DRIFT | GV_FLAG_DELAYED_UPDATES | GV_FLAG_STREAM_INVERSES))
+    if (c->flags & ~(GV_FLAG_REINV_DEFERRED | GV_FLAG_REINV_ON_DRIFT | GV_FLAG_DELAYED_UPDATES | GV_FLAG_STREAM_INVERSES |
+                     GV_FLAG_SCALAR_PAIRS))
         return false;
     if ((c->flags & GV_FLAG_REINV_ON_DRIFT) && (!(c->flags & GV_FLAG_REINV_DEFERRED) || !(c->drift_threshold > 0.0)))
         return false;
@@ -295,8 +298,27 @@ gv_status deferred_reinversion(gv_job* j)
     return j->cfg.precision == GV_PREC_FP64 ? launch_check<double, 256>(j, thr) : launch_check<float, 256>(j, thr);
 }
 
+// Tensor-core StatSpinStruct: mixed ground state with N_0 = N_1 <= 128.
+bool statspin_tc_ok(const gv_job* j)
+{
+    return !j->trans && j->cfg.precision == GV_PREC_MIXED && j->N[0] == j->N[1] && j->N[0] <= kTcM &&
+           !(j->cfg.flags & GV_FLAG_SCALAR_PAIRS);
+}
+
 gv_status statspin_dispatch(gv_job* j)
 {
+    if (statspin_tc_ok(j)) {
+        const TcLayout lay = tc_layout(j->N[0]);
+        GV_CK(cudaFuncSetAttribute(k_statspin_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, int(lay.total)));
+        int slot;
+        GV_CK(mark_begin(j, 2, &slot));
+        k_statspin_tc<<<std::min(j->W, j->n_sm), kTcThreads, lay.total, j->stream>>>(j->d);
+        GV_CK(cudaGetLastError());
+        GV_CK(mark_end(j, slot));
+        ++j->last_launches;
+        ++j->total_launches;
+        return GV_OK;
+    }
     const bool fp64 = j->cfg.precision == GV_PREC_FP64;
     size_t sm = (fp64 ? sizeof(cx<double>) : sizeof(cx<float>)) * 4 * j->Nmax + sizeof(int16_t) * 2 * j->Nmax + 16;
     int slot;
@@ -511,6 +533,115 @@ gv_status upload_configs(gv_job* j, const std::vector<int8_t>& up)
     return GV_OK;
 }
 
+// ---- Checkpoint blob: header, then the device arrays below in this order,
+// each copied whole.
+constexpr char kCkptMagic[8] = {'G', 'V', 'C', 'K', 'P', 'T', '0', '1'};
+
+struct CkptHeader {
+    char magic[8];
+    uint32_t header_bytes;
+    int32_t flags;
+    int32_t L, channel, q[2], precision, n_walkers, N[2], Nexc;
+    uint32_t walker_base;
+    uint64_t seed;
+    double phi, neel, neel_exp, phase_shift[2], phi_range[2], neel_range[2];
+    uint64_t payload_bytes;
+    uint64_t checksum;   // FNV-1a 64 over the payload
+};
+
+struct CkptSection {
+    void* dev;
+    size_t bytes;
+};
+
+std::vector<CkptSection> ckpt_sections(gv_job* j, bool inverses)
+{
+    const size_t W = size_t(j->W), Ns = size_t(j->Ns), Nmax = size_t(j->Nmax);
+    const DevJob& d = j->d;
+    std::vector<CkptSection> s = {
+        {d.fock, W * 2 * Ns * sizeof(int16_t)},
+        {d.part, W * 2 * Nmax * sizeof(int16_t)},
+        {d.amp_m, W * sizeof(cx<double>)},
+        {d.amp_e, W * sizeof(int32_t)},
+        {d.rng_next, W * sizeof(uint64_t)},
+        {d.counts, W * 5 * sizeof(unsigned long long)},
+        {d.since_reinv, W * sizeof(int32_t)},
+        {d.checks, W * sizeof(unsigned long long)},
+        {d.drift_seen, W * sizeof(double)},
+        {d.status, W * sizeof(int32_t)},
+        {d.pj, W * 2 * sizeof(cx<double>)},
+        {d.pj_n, W * sizeof(int32_t)},
+        {d.sm, W * sizeof(cx<double>)},
+        {d.sm_n, W * sizeof(int32_t)},
+        {d.ss, size_t(10) * Ns * Ns * sizeof(double)},
+        {d.ss_n, sizeof(int32_t)},
+    };
+    const size_t Nexc = size_t(j->ch.Nexc);
+    if (j->trans) {
+        s.push_back({d.worb, W * 2 * Nmax * sizeof(int16_t)});
+        s.push_back({d.wslot, W * 2 * Ns * sizeof(int16_t)});
+        s.push_back({d.cur, W * sizeof(int32_t)});
+        s.push_back({d.wsign, W * sizeof(int32_t)});
+        s.push_back({d.sigma, W * sizeof(double)});
+        s.push_back({d.pjx, W * 2 * Nexc * Nexc * sizeof(cx<double>)});
+    }
+    if (inverses) {
+        const size_t es = j->cfg.precision == GV_PREC_FP64 ? sizeof(cx<double>) : sizeof(cx<float>);
+        s.push_back({d.Ai[0], W * size_t(j->N[0]) * j->N[0] * es});
+        s.push_back({d.Ai[1], W * size_t(j->N[1]) * j->N[1] * es});
+        if (j->trans) {
+            s.push_back({d.gup, W * size_t(j->N[0]) * Nexc * es});
+            s.push_back({d.gdn, W * Nmax * es});
+        }
+    }
+    return s;
+}
+
+uint64_t fnv1a64(const unsigned char* p, size_t n)
+{
+    uint64_t h = 0xcbf29ce484222325ull;
+    for (size_t i = 0; i < n; ++i) { h ^= p[i]; h *= 0x100000001b3ull; }
+    return h;
+}
+
+CkptHeader ckpt_header(const gv_job* j, int flags)
+{
+    CkptHeader h;
+    std::memset(&h, 0, sizeof(h));
+    std::memcpy(h.magic, kCkptMagic, sizeof(h.magic));
+    h.header_bytes = sizeof(CkptHeader);
+    h.flags = flags;
+    const gv_job_config& c = j->cfg;
+    h.L = c.L; h.channel = c.channel; h.q[0] = c.q[0]; h.q[1] = c.q[1];
+    h.precision = c.precision; h.n_walkers = c.n_walkers;
+    h.N[0] = j->N[0]; h.N[1] = j->N[1]; h.Nexc = j->ch.Nexc;
+    h.walker_base = c.walker_base; h.seed = c.seed;
+    h.phi = c.phi; h.neel = c.neel; h.neel_exp = c.neel_exp;
+    for (int i = 0; i < 2; ++i) {
+        h.phase_shift[i] = c.phase_shift[i];
+        h.phi_range[i] = c.phi_range[i];
+        h.neel_range[i] = c.neel_range[i];
+    }
+    return h;
+}
+
+// The fields of two headers that must agree for a restore (the blob's
+// precision only matters when it carries inverses).
+bool ckpt_compatible(const CkptHeader& a, const CkptHeader& b)
+{
+    if (a.L != b.L || a.channel != b.channel || a.q[0] != b.q[0] || a.q[1] != b.q[1] ||
+        a.n_walkers != b.n_walkers || a.N[0] != b.N[0] || a.N[1] != b.N[1] || a.Nexc != b.Nexc ||
+        a.walker_base != b.walker_base || a.seed != b.seed)
+        return false;
+    if (a.phi != b.phi || a.neel != b.neel || a.neel_exp != b.neel_exp) return false;
+    for (int i = 0; i < 2; ++i)
+        if (a.phase_shift[i] != b.phase_shift[i] || a.phi_range[i] != b.phi_range[i] ||
+            a.neel_range[i] != b.neel_range[i])
+            return false;
+    if ((a.flags & GV_CKPT_INVERSES) && a.precision != b.precision) return false;
+    return true;
+}
+
 }  // namespace
 
 extern "C" {
@@ -694,6 +825,14 @@ gv_status gv_job_create(const gv_job_config* cfg, gv_job** out)
     }
 
     auto fail = [&](gv_status s) { gv_job_destroy(j); return s; };
+    {
+        int dev = 0;
+        if (cudaGetDevice(&dev) != cudaSuccess ||
+            cudaDeviceGetAttribute(&j->n_sm, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) {
+            delete j;
+            return GV_ERR_CUDA;
+        }
+    }
     if (cudaStreamCreateWithFlags(&j->stream, cudaStreamNonBlocking) != cudaSuccess) { delete j; return GV_ERR_CUDA; }
     if (cudaEventCreate(&j->ev0) != cudaSuccess || cudaEventCreate(&j->ev1) != cudaSuccess) return fail(GV_ERR_CUDA);
 
@@ -867,11 +1006,11 @@ gv_status gv_job_init_walkers(gv_job* j, const int8_t* up)
     GV_CK(cudaMemsetAsync(j->d.checks, 0, sizeof(unsigned long long) * W, j->stream));
     GV_CK(cudaMemsetAsync(j->d.drift_seen, 0, sizeof(double) * W, j->stream));
     // vmc.cpp:221-241: up to 10 random starts until the amplitude is non-zero.
-    // The mixed-precision exciton job also redraws a start whose inverse in the
-    // picked channel state has an entry above kMixedMaxInverse: such a
+    // A mixed-precision job also redraws a random start whose inverse (in the
+    // picked channel state) has an entry above kMixedMaxInverse: such a
     // configuration's amplitude is many orders below its neighbours', and its
     // FP32 ratios would overflow or cancel to noise on the first step.
-    const bool screen = j->trans && j->cfg.precision == GV_PREC_MIXED && !up;
+    const bool screen = j->cfg.precision == GV_PREC_MIXED && !up;
     std::vector<double> amax(W);
     for (int attempt = 0; attempt < 10; ++attempt) {
         if (j->trans) {   // every walker starts in channel state 0
@@ -891,11 +1030,14 @@ gv_status gv_job_init_walkers(gv_job* j, const int8_t* up)
             for (int w = 0; w < W; ++w)
                 if (status[w] != GV_OK) { j->ready = true; return status[w]; }
             if ((st = trans_start(j))) return st;
-            if (screen) {
-                if ((st = inverse_max_abs(j, amax.data()))) return st;
-                for (int w = 0; w < W; ++w)
-                    if (!(amax[w] <= kMixedMaxInverse)) { ran_init(j, w, &cfg[size_t(w) * Ns]); again = true; }
-            }
+        }
+        if (!again && screen) {
+            if ((st = inverse_max_abs(j, amax.data()))) return st;
+            for (int w = 0; w < W; ++w)
+                if (status[w] == GV_OK && !(amax[w] <= kMixedMaxInverse)) {
+                    ran_init(j, w, &cfg[size_t(w) * Ns]);
+                    again = true;
+                }
         }
         if (!again) break;
         if (attempt == 9) return GV_ERR_SINGULAR;
@@ -1256,13 +1398,102 @@ gv_status gv_job_read_stagmagn(gv_job* j, double* vals, int32_t* nmeas)
     return GV_OK;
 }
 
+// StatSpinStruct m_vals from the compact device sums: with M the number of
+// (walker, measurement) pairs, u_i / d_i the times site i held flavour 0 / 1,
+//   szz[i][j] = (M - 2 (Aud[i][j] + Aud[j][i])) / 4  (i != j),  szz[i][i] = M / 4
+//   s+-[i][j] = -T[j][i] + [i == j] u_i,   s-+[i][j] = -T[i][j] + [i == j] d_i
+// (every site is held by exactly one flavour: u_i N_1 = sum_j Aud[i][j],
+// d_i N_0 = sum_j Aud[j][i], u_i + d_i = M).
 gv_status gv_job_read_statspin(gv_job* j, double* vals, int32_t* nmeas)
 {
     if (!j || !vals) return GV_ERR_INVALID;
     GV_CK(cudaStreamSynchronize(j->stream));
-    GV_CK(cudaMemcpy(vals, j->d.ss, sizeof(double) * 10 * j->Ns * j->Ns, cudaMemcpyDeviceToHost));
+    const size_t Ns = size_t(j->Ns), n2 = Ns * Ns;
+    std::vector<double> raw(3 * n2);
+    GV_CK(cudaMemcpy(raw.data(), j->d.ss, sizeof(double) * 3 * n2, cudaMemcpyDeviceToHost));
     if (nmeas) GV_CK(cudaMemcpy(nmeas, j->d.ss_n, sizeof(int32_t), cudaMemcpyDeviceToHost));
+    const double* T = raw.data();
+    const double* Aud = raw.data() + 2 * n2;
+    std::vector<double> u(Ns, 0.0), dn(Ns, 0.0);
+    for (size_t i = 0; i < Ns; ++i)
+        for (size_t k = 0; k < Ns; ++k) { u[i] += Aud[i * Ns + k]; dn[i] += Aud[k * Ns + i]; }
+    for (size_t i = 0; i < Ns; ++i) { u[i] /= double(j->N[1]); dn[i] /= double(j->N[0]); }
+    const double M = Ns ? u[0] + dn[0] : 0.0;
+    std::fill(vals, vals + 10 * n2, 0.0);
+    double* szz = vals;
+    double* spm = vals + 2 * n2;
+    double* smp = vals + 4 * n2;
+    for (size_t i = 0; i < Ns; ++i)
+        for (size_t k = 0; k < Ns; ++k) {
+            const size_t ik = i * Ns + k, ki = k * Ns + i;
+            szz[2 * ik] = i == k ? 0.25 * M : 0.25 * (M - 2.0 * (Aud[ik] + Aud[ki]));
+            spm[2 * ik] = -T[2 * ki] + (i == k ? u[i] : 0.0);
+            spm[2 * ik + 1] = -T[2 * ki + 1];
+            smp[2 * ik] = -T[2 * ik] + (i == k ? dn[i] : 0.0);
+            smp[2 * ik + 1] = -T[2 * ik + 1];
+        }
     return GV_OK;
+}
+
+gv_status gv_job_checkpoint_size(gv_job* j, int32_t flags, uint64_t* bytes)
+{
+    if (!j || !bytes || (flags & ~GV_CKPT_INVERSES)) return GV_ERR_INVALID;
+    uint64_t n = sizeof(CkptHeader);
+    for (const CkptSection& s : ckpt_sections(j, flags & GV_CKPT_INVERSES)) n += s.bytes;
+    *bytes = n;
+    return GV_OK;
+}
+
+gv_status gv_job_checkpoint(gv_job* j, int32_t flags, void* buf, uint64_t capacity, uint64_t* written)
+{
+    uint64_t need = 0;
+    if (!buf || gv_job_checkpoint_size(j, flags, &need) || capacity < need) return GV_ERR_INVALID;
+    if (!j->ready) return GV_ERR_NOT_READY;
+    unsigned char* out = static_cast<unsigned char*>(buf);
+    unsigned char* p = out + sizeof(CkptHeader);
+    for (const CkptSection& s : ckpt_sections(j, flags & GV_CKPT_INVERSES)) {
+        GV_CK(cudaMemcpyAsync(p, s.dev, s.bytes, cudaMemcpyDeviceToHost, j->stream));
+        p += s.bytes;
+    }
+    GV_CK(cudaStreamSynchronize(j->stream));
+    CkptHeader h = ckpt_header(j, flags);
+    h.payload_bytes = uint64_t(p - out) - sizeof(CkptHeader);
+    h.checksum = fnv1a64(out + sizeof(CkptHeader), h.payload_bytes);
+    std::memcpy(out, &h, sizeof(h));
+    if (written) *written = need;
+    return GV_OK;
+}
+
+gv_status gv_job_restore(gv_job* j, const void* buf, uint64_t size)
+{
+    if (!j || !buf || size < sizeof(CkptHeader)) return GV_ERR_INVALID;
+    CkptHeader h;
+    std::memcpy(&h, buf, sizeof(h));
+    if (std::memcmp(h.magic, kCkptMagic, sizeof(h.magic)) || h.header_bytes != sizeof(CkptHeader) ||
+        (h.flags & ~GV_CKPT_INVERSES) || !ckpt_compatible(h, ckpt_header(j, 0)))
+        return GV_ERR_INVALID;
+    const bool inverses = (h.flags & GV_CKPT_INVERSES) != 0;
+    const std::vector<CkptSection> secs = ckpt_sections(j, inverses);
+    uint64_t payload = 0;
+    for (const CkptSection& s : secs) payload += s.bytes;
+    const unsigned char* in = static_cast<const unsigned char*>(buf) + sizeof(CkptHeader);
+    if (h.payload_bytes != payload || size != sizeof(CkptHeader) + payload || fnv1a64(in, payload) != h.checksum)
+        return GV_ERR_INVALID;
+    GV_CK(cudaStreamSynchronize(j->stream));
+    for (const CkptSection& s : secs) {
+        GV_CK(cudaMemcpyAsync(s.dev, in, s.bytes, cudaMemcpyHostToDevice, j->stream));
+        in += s.bytes;
+    }
+    // The pageable source must outlive the copies: wait before returning.
+    GV_CK(cudaStreamSynchronize(j->stream));
+    j->ready = true;
+    if (inverses) return GV_OK;
+    // SlaterDeterminant::Init from the restored configurations (and, for the
+    // exciton channel, the overlap rows of the restored channel state).
+    gv_status st = invert_all(j);
+    if (st) return st;
+    GV_CK(cudaMemsetAsync(j->d.since_reinv, 0, sizeof(int32_t) * j->W, j->stream));
+    return gv_job_synchronize(j);
 }
 
 }  // extern "C"

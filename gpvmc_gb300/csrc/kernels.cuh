@@ -913,11 +913,15 @@ __device__ __forceinline__ cx<T> warp_ratio(const DevJob& J, const cx<T>* A, con
     return warp_sum(acc);
 }
 
-// StatSpinStruct (StatSpinStruct.cpp:16-135), two flavours: for every pair
-// i <= j, szz +-1/4 and, for antiparallel pairs, s-+ / s+- -= the swap ratio
-// r_up(p_i -> j) r_dn(q_j -> i) (the reference's conj(amp) swamp / w).  In the
-// exciton channel the swap keeps the channel state and w is the weight over
-// all states, so the ratio is divided by sigma = w / |Amp|^2.
+// StatSpinStruct (StatSpinStruct.cpp:16-135), two flavours, accumulated in
+// compact form: for every antiparallel pair (flavour-0 particle c at site i,
+// flavour-1 particle q at site j), one warp per pair,
+//     T[i][j]   += r_up(c -> j) r_dn(q -> i)   (the reference's conj(amp) swamp / w)
+//     Aud[i][j] += 1
+// (T complex, Aud real, both Ns x Ns, job-wide).  szz, s+- and s-+ follow
+// from them and the occupation counts they imply (gv_job_read_statspin).  In
+// the exciton channel the swap keeps the channel state and w is the weight
+// over all states, so the ratio is divided by sigma = w / |Amp|^2.
 template <typename T, int NT>
 __global__ void __launch_bounds__(NT) k_statspin(DevJob J)
 {
@@ -925,8 +929,8 @@ __global__ void __launch_bounds__(NT) k_statspin(DevJob J)
     if (w >= J.W || J.status[w] != GV_OK) return;
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     constexpr int NW = NT / 32;
-    const int Ns = J.Ns, Nmax = J.Nmax;
-    const int16_t* fock = J.fock + size_t(w) * 2 * Ns;
+    const int Ns = J.Ns, Nmax = J.Nmax, N0 = J.N[0], N1 = J.N[1];
+    const int16_t* part = J.part + size_t(w) * 2 * Nmax;
     const cx<T>* phase = Tab<T>::phase(J);
     const cx<T>* cg = Tab<T>::coef(J) + size_t(w) * 4 * Ns;
     extern __shared__ __align__(16) char smem[];
@@ -943,38 +947,20 @@ __global__ void __launch_bounds__(NT) k_statspin(DevJob J)
     const double inv_sigma = scaled ? 1.0 / J.sigma[w] : 1.0;
     const cx<T>* A0 = ai_ptr<T>(J, 0, w);
     const cx<T>* A1 = ai_ptr<T>(J, 1, w);
-    double* szz = J.ss;
-    double* spm = J.ss + 2 * size_t(Ns) * Ns;
-    double* smp = J.ss + 4 * size_t(Ns) * Ns;
-    for (int idx = warp; idx < Ns * Ns; idx += NW) {
-        const int vi = idx / Ns, vj = idx % Ns;
-        if (vj < vi) continue;
-        const bool ui = fock[vi] >= 0, uj = fock[vj] >= 0;
-        const size_t ij = size_t(vi) * Ns + vj, ji = size_t(vj) * Ns + vi;
-        if (ui == uj) {
-            if (lane == 0) {
-                if (vi == vj) {
-                    atomicAdd(&szz[2 * ij], 0.25);
-                    atomicAdd(ui ? &spm[2 * ij] : &smp[2 * ij], 1.0);
-                } else {
-                    atomicAdd(&szz[2 * ij], 0.25);
-                    atomicAdd(&szz[2 * ji], 0.25);
-                }
-            }
-            continue;
-        }
-        const int upf = ui ? vi : vj, upt = ui ? vj : vi;
-        const cx<T> ru = warp_ratio<T>(J, A0, phase, coef, pcol, J.N[0], fock[upf], upt);
-        const cx<T> rd = warp_ratio<T>(J, A1, phase, coef + 2 * Nmax, pcol + Nmax, J.N[1], fock[Ns + upt], upf);
+    double* Tsum = J.ss;
+    double* Aud = J.ss + 2 * size_t(Ns) * Ns;
+    for (int idx = warp; idx < N0 * N1; idx += NW) {
+        const int c = idx / N1, q = idx % N1;
+        const int si = part[c], sj = part[Nmax + q];
+        const cx<T> ru = warp_ratio<T>(J, A0, phase, coef, pcol, N0, c, sj);
+        const cx<T> rd = warp_ratio<T>(J, A1, phase, coef + 2 * Nmax, pcol + Nmax, N1, q, si);
         if (lane == 0) {
             cx<double> r = to_d(ru) * to_d(rd);
             if (scaled) r = r * inv_sigma;
-            atomicAdd(&szz[2 * ij], -0.25);
-            atomicAdd(&szz[2 * ji], -0.25);
-            double* a = ui ? smp : spm;   // vi up: s-+[ij], s+-[ji]; vi down: s+-[ij], s-+[ji]
-            double* b = ui ? spm : smp;
-            atomicAdd(&a[2 * ij], -r.x); atomicAdd(&a[2 * ij + 1], -r.y);
-            atomicAdd(&b[2 * ji], -r.x); atomicAdd(&b[2 * ji + 1], -r.y);
+            const size_t ij = size_t(si) * Ns + sj;
+            atomicAdd(&Tsum[2 * ij], r.x);
+            atomicAdd(&Tsum[2 * ij + 1], r.y);
+            atomicAdd(&Aud[ij], 1.0);
         }
     }
     if (tid == 0) atomicAdd(J.ss_n, w == 0 ? 1 : 0);

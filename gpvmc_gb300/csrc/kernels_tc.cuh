@@ -1,0 +1,363 @@
+// StatSpinStruct pair ratios on the tensor cores (mixed precision, ground
+// state, N_0 = N_1 = N <= 128).  Included by engine.cu after kernels_res.cuh.
+//
+// StatSpinStruct (StatSpinStruct.cpp:16-135) needs, for every antiparallel
+// pair (up particle c at site i, down particle q at site j), the swap ratio
+//     r(c, q) = G_up(c, q) * G_dn^T(c, q),
+//     G_up(c, q)   = sum_f (A_up^-1)(c, f) phi^up_f(j)   (up particle c -> site j)
+//     G_dn^T(c, q) = sum_f (A_dn^-1)(q, f) phi^dn_f(i)   (down particle q -> site i)
+// i.e. the G = Phi . A^-1 products of the reference's VirtUpdate for every
+// pair at once.  Both are complex N x N x N matrix products per walker,
+// computed here with tcgen05.mma kind::tf32 (M = 128 rows c, N = the down
+// particles q rounded up to 16, K = 8 per instruction), FP32 accumulators in
+// tensor memory (TMEM columns [0,128) Re G_up, [128,256) Im G_up,
+// [256,384) Re G_dn^T, [384,512) Im G_dn^T; lane = row c).
+//
+// Split precision (Ootomo & Yokota, IJHPCA 2022): every FP32 operand x is
+// split into x_hi = tf32(x) (round to nearest) and x_lo = tf32(x - x_hi);
+// each real product is x_hi y_hi + x_hi y_lo + x_lo y_hi, accumulated in
+// FP32, which recovers FP32 accuracy (relative error ~1e-6 per element).  A
+// complex product is four real ones: Re = Ar Br + Ai (-Bi), Im = Ar Bi + Ai Br,
+// with -Bi stored as its own operand, so every walker and K chunk issues
+// 4 x 3 x 4 = 48 MMAs per matrix.
+//
+// Operands are K-major in shared memory with the 128-byte swizzle: one row
+// (a particle) holds 32 TF32 values of K (the Slater rows f of one chunk) in
+// 128 bytes, 8-row groups 1024 bytes apart, 16-byte unit u of row r stored at
+// unit u ^ (r mod 8).  The CTA's threads build the operands directly from the
+// FP32 inverses (HBM) and the phase / coefficient tables (L2), so that the
+// split happens on the way in; one elected thread issues the MMAs and commits
+// them to an mbarrier that the CTA waits on (bounded).  The epilogue reads
+// the accumulators with tcgen05.ld and adds the pair ratios into the
+// job-wide sums.  One CTA per SM (its shared memory takes more than half of
+// the SM's), persistent over the walkers.
+#pragma once
+
+#include "kernels_res.cuh"
+
+namespace gv {
+namespace {
+
+constexpr int kTcThreads = 256;
+constexpr int kTcM = 128;                 // MMA rows (up particles, zero padded)
+constexpr int kTcWaitLimit = 1 << 22;     // mbarrier polls before a wait gives up
+
+__host__ __device__ inline int tc_ncols(int N) { return (N + 15) & ~15; }
+
+struct TcLayout {
+    size_t a[4], b[6], site, coef, bar, tbase, total;
+};
+
+// Operand tiles at 1024-byte multiples from a 1024-aligned base:
+// A: Re hi, Re lo, Im hi, Im lo (128 rows); B: the same and -Im hi, -Im lo
+// (tc_ncols(N) rows); each row 128 bytes.
+__host__ __device__ inline TcLayout tc_layout(int N)
+{
+    TcLayout l;
+    size_t o = 0;
+    const size_t at = size_t(kTcM) * 128, bt = size_t(tc_ncols(N)) * 128;
+    for (int i = 0; i < 4; ++i) { l.a[i] = o; o += at; }
+    for (int i = 0; i < 6; ++i) { l.b[i] = o; o += bt; }
+    l.site = o;
+    o += sizeof(int16_t) * 2 * kTcM;
+    l.coef = o;
+    o += sizeof(cx<float>) * 4 * kTcM;
+    l.bar = o;
+    o += 8;
+    l.tbase = o;
+    o += 8;
+    l.total = o + 1024;   // room to align the base
+    return l;
+}
+
+__device__ __forceinline__ uint32_t smem_addr(const void* p)
+{
+    return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+
+// Byte offset of 16-byte unit u (0..7) of row r in a K-major 128-byte-swizzled tile.
+__device__ __forceinline__ uint32_t sw128(int r, int u)
+{
+    return uint32_t((r >> 3) * 1024 + (r & 7) * 128 + (((u ^ r) & 7) << 4));
+}
+
+__device__ __forceinline__ float tf32_rna(float x)
+{
+    uint32_t r;
+    asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(r) : "f"(x));
+    return __uint_as_float(r);
+}
+
+// Four consecutive K values of one row (real and imaginary parts) -> the
+// hi / lo tiles (and the negated imaginary tiles when nt == 6).
+__device__ __forceinline__ void tc_store_split(char* base, const size_t* tiles, int nt, uint32_t off,
+                                               const float (&re)[4], const float (&im)[4])
+{
+    float4 rh, rl, ih, il;
+    float* prh = &rh.x; float* prl = &rl.x; float* pih = &ih.x; float* pil = &il.x;
+#pragma unroll
+    for (int t = 0; t < 4; ++t) {
+        prh[t] = tf32_rna(re[t]);
+        prl[t] = tf32_rna(__fsub_rn(re[t], prh[t]));
+        pih[t] = tf32_rna(im[t]);
+        pil[t] = tf32_rna(__fsub_rn(im[t], pih[t]));
+    }
+    *reinterpret_cast<float4*>(base + tiles[0] + off) = rh;
+    *reinterpret_cast<float4*>(base + tiles[1] + off) = rl;
+    *reinterpret_cast<float4*>(base + tiles[2] + off) = ih;
+    *reinterpret_cast<float4*>(base + tiles[3] + off) = il;
+    if (nt == 6) {
+        *reinterpret_cast<float4*>(base + tiles[4] + off) = make_float4(-ih.x, -ih.y, -ih.z, -ih.w);
+        *reinterpret_cast<float4*>(base + tiles[5] + off) = make_float4(-il.x, -il.y, -il.z, -il.w);
+    }
+}
+
+// Inverse operand, K chunk kc: row r holds AiT[f][r] = (A^-1)(r, f) for
+// f = 32 kc .. 32 kc + 31 (zero outside N x N).  Lanes run over rows, so
+// every warp reads whole 256-byte runs of an AiT row.
+__device__ __forceinline__ void tc_fill_inverse(char* base, const size_t* tiles, int nt, const cx<float>* Ai, int N,
+                                                int rows, int kc)
+{
+    for (int it = threadIdx.x; it < rows * 8; it += kTcThreads) {
+        const int r = it % rows, u = it / rows;
+        float re[4], im[4];
+#pragma unroll
+        for (int t = 0; t < 4; ++t) {
+            const int f = 32 * kc + 4 * u + t;
+            cx<float> a = {0.f, 0.f};
+            if (r < N && f < N) a = Ai[size_t(f) * N + r];
+            re[t] = a.x;
+            im[t] = a.y;
+        }
+        tc_store_split(base, tiles, nt, sw128(r, u), re, im);
+    }
+}
+
+// Orbital operand, K chunk kc: row r holds phi_{2f}(site[r]) =
+// phase[site][f] coef[sub(site)][f] (the walk's own FP32 product) for
+// f = 32 kc .. 32 kc + 31 (zero for r >= N or f >= N).
+__device__ __forceinline__ void tc_fill_phi(char* base, const size_t* tiles, int nt, const cx<float>* phase, int Nk,
+                                            const cx<float>* coef, const int16_t* site, int N, int L, int rows, int kc)
+{
+    for (int it = threadIdx.x; it < rows * 8; it += kTcThreads) {
+        const int r = it % rows, u = it / rows;
+        float re[4] = {0.f, 0.f, 0.f, 0.f}, im[4] = {0.f, 0.f, 0.f, 0.f};
+        if (r < N) {
+            const int s = site[r], sub = sublattice(s, L);
+#pragma unroll
+            for (int t = 0; t < 4; ++t) {
+                const int f = 32 * kc + 4 * u + t;
+                if (f < N) {
+                    const cx<float> v = cmul_rn(phase[size_t(s) * Nk + f], coef[sub * N + f]);
+                    re[t] = v.x;
+                    im[t] = v.y;
+                }
+            }
+        }
+        tc_store_split(base, tiles, nt, sw128(r, u), re, im);
+    }
+}
+
+// Shared-memory matrix descriptor: start address, leading byte offset 16
+// (unused by swizzled K-major operands), stride byte offset 1024 (8-row
+// groups), descriptor version 1, base offset 0, 128-byte swizzle.
+__device__ __forceinline__ uint64_t tc_desc(uint32_t saddr)
+{
+    return uint64_t((saddr & 0x3FFFFu) >> 4) | (uint64_t(1) << 16) | (uint64_t(1024 >> 4) << 32) |
+           (uint64_t(1) << 46) | (uint64_t(2) << 61);
+}
+
+// Instruction descriptor, kind::tf32: D FP32, A and B TF32, both K-major,
+// no negation, N = n, M = 128.
+__host__ __device__ inline uint32_t tc_idesc(int n)
+{
+    return (1u << 4) | (2u << 7) | (2u << 10) | (uint32_t(n >> 3) << 17) | (uint32_t(kTcM >> 4) << 24);
+}
+
+__device__ __forceinline__ void tc_mma(uint32_t d, uint64_t a, uint64_t b, uint32_t idesc, uint32_t acc)
+{
+    asm volatile(
+        "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
+        "tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n\t}" ::"r"(d),
+        "l"(a), "l"(b), "r"(idesc), "r"(acc));
+}
+
+__device__ __forceinline__ void tc_commit(uint32_t bar)
+{
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar) : "memory");
+}
+
+__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity)
+{
+    for (int i = 0; i < kTcWaitLimit; ++i) {
+        uint32_t done;
+        asm volatile(
+            "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+            "selp.b32 %0, 1, 0, p;\n\t}"
+            : "=r"(done)
+            : "r"(bar), "r"(parity)
+            : "memory");
+        if (done) return true;
+    }
+    return false;
+}
+
+__device__ __forceinline__ void tmem_ld16(uint32_t taddr, uint32_t* r)
+{
+    asm volatile("tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+                 : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+                   "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+                 : "r"(taddr));
+}
+
+// The 48 MMAs of one K chunk into the accumulator pair at column dcol:
+// Re += Ar Br + Ai (-Bi), Im += Ar Bi + Ai Br, each real product as three
+// split-precision terms, K = 8 per instruction (32 bytes along the row).
+__device__ __forceinline__ void tc_issue_chunk(uint32_t tbase, uint32_t dcol, uint32_t sbase, const TcLayout& lay,
+                                               uint32_t idesc, bool first)
+{
+    enum { RH = 0, RL = 1, IH = 2, IL = 3, NH = 4, NL = 5 };
+    const int re_terms[6][2] = {{RH, RH}, {RH, RL}, {RL, RH}, {IH, NH}, {IH, NL}, {IL, NH}};
+    const int im_terms[6][2] = {{RH, IH}, {RH, IL}, {RL, IH}, {IH, RH}, {IH, RL}, {IL, RH}};
+#pragma unroll
+    for (int kk = 0; kk < 4; ++kk) {
+#pragma unroll
+        for (int t = 0; t < 6; ++t) {
+            const uint32_t acc = (first && kk == 0 && t == 0) ? 0u : 1u;
+            tc_mma(tbase + dcol, tc_desc(sbase + uint32_t(lay.a[re_terms[t][0]]) + 32 * kk),
+                   tc_desc(sbase + uint32_t(lay.b[re_terms[t][1]]) + 32 * kk), idesc, acc);
+            tc_mma(tbase + dcol + 128, tc_desc(sbase + uint32_t(lay.a[im_terms[t][0]]) + 32 * kk),
+                   tc_desc(sbase + uint32_t(lay.b[im_terms[t][1]]) + 32 * kk), idesc, acc);
+        }
+    }
+}
+
+// The job-wide pair sums (StatSpinStruct m_vals in compact form):
+//   T[i][j]   += r  for up site i, down site j (complex),
+//   Aud[i][j] += 1  (antiparallel count),
+// from which szz, s+- and s-+ follow (gv_job_read_statspin).
+__global__ void __launch_bounds__(kTcThreads, 1) k_statspin_tc(DevJob J)
+{
+    extern __shared__ __align__(16) char smem_raw[];
+    const uint32_t raw = smem_addr(smem_raw);
+    char* base = smem_raw + ((1024u - (raw & 1023u)) & 1023u);
+    const uint32_t sbase = smem_addr(base);
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int N = J.N[0], Nt = tc_ncols(N), Ns = J.Ns, L = J.L, Nk = J.Nk;
+    const TcLayout lay = tc_layout(N);
+    int16_t* s_site = reinterpret_cast<int16_t*>(base + lay.site);      // [fl][p]
+    cx<float>* s_coef = reinterpret_cast<cx<float>*>(base + lay.coef);  // [fl][sub][f]
+    uint64_t* s_bar = reinterpret_cast<uint64_t*>(base + lay.bar);
+    uint32_t* s_tbase = reinterpret_cast<uint32_t*>(base + lay.tbase);
+    const uint32_t bar = smem_addr(s_bar);
+    double* T = J.ss;
+    double* Aud = J.ss + 2 * size_t(Ns) * Ns;
+
+    if (warp == 0) tmem_alloc(s_tbase, 512);
+    if (tid == 0) {
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(bar) : "memory");
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    tmem_fence_before();
+    __syncthreads();
+    tmem_fence_after();
+    const uint32_t tbase = *s_tbase;
+    const uint32_t idesc = tc_idesc(Nt);
+    const int KC = (N + 31) / 32;
+    uint32_t parity = 0;
+    bool failed = false;
+
+    for (int w = blockIdx.x; w < J.W; w += gridDim.x) {
+        if (J.status[w] != GV_OK) continue;
+        __syncthreads();   // the previous walker's epilogue is done with s_site and TMEM
+        for (int i = tid; i < 2 * N; i += kTcThreads) {
+            const int fl = i / N, p = i % N;
+            s_site[fl * kTcM + p] = J.part[(size_t(w) * 2 + fl) * J.Nmax + p];
+        }
+        {
+            const cx<float>* cg = J.coef32 + size_t(w) * 4 * Ns;   // [fl][sub][orbital]
+            for (int i = tid; i < 4 * N; i += kTcThreads) {
+                const int fl = i / (2 * N), sub = (i / N) & 1, f = i % N;
+                s_coef[i] = cg[(size_t(fl) * 2 + sub) * Ns + 2 * f];
+            }
+        }
+        __syncthreads();
+        for (int gm = 0; gm < 2 && !failed; ++gm) {
+            for (int kc = 0; kc < KC; ++kc) {
+                if (gm || kc) {   // the previous chunk's MMAs are done with the tiles
+                    const bool ok = mbar_wait(bar, parity);
+                    if (__syncthreads_or(!ok)) { failed = true; break; }
+                    parity ^= 1u;
+                }
+                if (gm == 0) {   // G_up: A = AiT_up^T (rows c), B = Phi_up at the down sites (rows q)
+                    tc_fill_inverse(base, lay.a, 4, ai_ptr<float>(J, 0, w), N, kTcM, kc);
+                    tc_fill_phi(base, lay.b, 6, J.phase32, Nk, s_coef, s_site + kTcM, N, L, Nt, kc);
+                } else {         // G_dn^T: A = Phi_dn at the up sites (rows c), B = AiT_dn^T (rows q)
+                    tc_fill_phi(base, lay.a, 4, J.phase32, Nk, s_coef + 2 * N, s_site, N, L, kTcM, kc);
+                    tc_fill_inverse(base, lay.b, 6, ai_ptr<float>(J, 1, w), N, Nt, kc);
+                }
+                asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+                tmem_fence_before();
+                __syncthreads();
+                if (tid == 0) {
+                    tmem_fence_after();
+                    tc_issue_chunk(tbase, uint32_t(256 * gm), sbase, lay, idesc, kc == 0);
+                    tc_commit(bar);
+                }
+            }
+        }
+        if (failed) {
+            if (tid == 0) J.status[w] = GV_ERR_TIMEOUT;
+            break;
+        }
+        {
+            const bool ok = mbar_wait(bar, parity);
+            if (__syncthreads_or(!ok)) {
+                failed = true;
+                if (tid == 0) J.status[w] = GV_ERR_TIMEOUT;
+                break;
+            }
+            parity ^= 1u;
+        }
+        tmem_fence_after();
+        // epilogue: warp -> TMEM lanes 32 (warp % 4) .. +31 (rows c), 16-column
+        // chunks of q split between the two warps of a lane group
+        const int lg = warp & 3, c = 32 * lg + lane;
+        const bool crow = c < N;
+        const int si = crow ? s_site[c] : 0;
+        for (int cc = warp >> 2; cc < Nt / 16; cc += 2) {
+            uint32_t r[64];
+            const uint32_t ta = tbase + (uint32_t(32 * lg) << 16) + uint32_t(16 * cc);
+            tmem_ld16(ta, r);
+            tmem_ld16(ta + 128, r + 16);
+            tmem_ld16(ta + 256, r + 32);
+            tmem_ld16(ta + 384, r + 48);
+            tmem_wait_ld(r);
+            if (crow) {
+#pragma unroll
+                for (int t = 0; t < 16; ++t) {
+                    const int q = 16 * cc + t;
+                    if (q < N) {
+                        const cx<double> gu = {double(__uint_as_float(r[t])), double(__uint_as_float(r[16 + t]))};
+                        const cx<double> gd = {double(__uint_as_float(r[32 + t])), double(__uint_as_float(r[48 + t]))};
+                        const cx<double> v = gu * gd;
+                        const size_t ij = size_t(si) * Ns + s_site[kTcM + q];
+                        atomicAdd(&T[2 * ij], v.x);
+                        atomicAdd(&T[2 * ij + 1], v.y);
+                        atomicAdd(&Aud[ij], 1.0);
+                    }
+                }
+            }
+        }
+        tmem_fence_before();
+        if (tid == 0) atomicAdd(J.ss_n, w == 0 ? 1 : 0);
+    }
+    if (failed) mbar_wait(bar, parity);   // the phase that timed out: MMAs in flight finish before TMEM is freed
+    tmem_fence_before();
+    __syncthreads();
+    tmem_fence_after();
+    if (warp == 0) tmem_dealloc(tbase, 512);
+}
+
+}  // namespace
+}  // namespace gv

@@ -89,7 +89,7 @@ class Job:
 
     def __init__(self, wav, walkers=1, seed=1234, precision="fp64", reinv_every=0, walker_base=0,
                  phi_range=None, neel_range=None, deferred_reinversion=False, drift_threshold=None,
-                 delayed_updates=False, stream_inverses=False):
+                 delayed_updates=False, stream_inverses=False, scalar_pairs=False):
         L = _lib.lib()
         cfg = _lib.JobConfig()
         cfg.L = wav.L
@@ -115,6 +115,8 @@ class Job:
             cfg.flags |= _lib.GV_FLAG_DELAYED_UPDATES
         if stream_inverses:
             cfg.flags |= _lib.GV_FLAG_STREAM_INVERSES
+        if scalar_pairs:
+            cfg.flags |= _lib.GV_FLAG_SCALAR_PAIRS
         self.cfg = cfg
         self.wav = wav
         self.walkers = walkers
@@ -163,6 +165,36 @@ class Job:
         check(_lib.lib().gv_job_walk(self._h, length, meas), "gv_job_walk")
         if sync:
             self.synchronize()
+
+    def walk_continue(self, length, meas=0, sync=True):
+        """As walk, with the quantity sums carried over from the previous call."""
+        check(_lib.lib().gv_job_walk_continue(self._h, length, meas), "gv_job_walk_continue")
+        if sync:
+            self.synchronize()
+
+    # -- checkpoint / resume -------------------------------------------------
+    def checkpoint(self, inverses=False):
+        """The job's chain state as bytes (gv_job_checkpoint); with inverses the
+        restored job continues bit for bit, without them it re-inverts in FP64."""
+        flags = _lib.GV_CKPT_INVERSES if inverses else 0
+        n = ctypes.c_uint64()
+        check(_lib.lib().gv_job_checkpoint_size(self._h, flags, ctypes.byref(n)), "gv_job_checkpoint_size")
+        buf = np.empty(n.value, dtype=np.uint8)
+        check(_lib.lib().gv_job_checkpoint(self._h, flags, _p(buf), n.value, None), "gv_job_checkpoint")
+        return buf.tobytes()
+
+    def restore(self, blob):
+        """Load a checkpoint taken from a job of the same configuration."""
+        buf = np.frombuffer(blob, dtype=np.uint8)
+        check(_lib.lib().gv_job_restore(self._h, _p(buf), buf.size), "gv_job_restore")
+
+    def save_checkpoint(self, path, inverses=False):
+        with open(path, "wb") as f:
+            f.write(self.checkpoint(inverses))
+
+    def load_checkpoint(self, path):
+        with open(path, "rb") as f:
+            self.restore(f.read())
 
     def walk_traced(self, length, meas=0, walker=0):
         buf = (_lib.Trace * max(length, 1))()

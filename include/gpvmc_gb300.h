@@ -28,6 +28,8 @@
  *                          MetroMC::Rejection, Quantity m_vals / GetNmeas
  *                          (State.cpp:55-63; SlaterDeterminant.cpp:94;
  *                          MetroMC.cpp:105-111; Quantity.h:12-28)
+ *   gv_job_checkpoint /    State::Save of the final Fock state and the --spinstate
+ *   gv_job_restore         resume (State.cpp:117-166; vmc.cpp:178-220, 329)
  */
 #ifndef GPVMC_GB300_H
 #define GPVMC_GB300_H
@@ -70,6 +72,10 @@ typedef int32_t gv_status;
                                      walk (the streaming kernel) instead of on chip; the
                                      on-chip kernel runs by default when N <= 128 and the
                                      re-inversion is deferred */
+#define GV_FLAG_SCALAR_PAIRS 16   /* mixed ground state: StatSpinStruct pair ratios from FP32
+                                     dot products on the CUDA cores instead of the
+                                     split-TF32 tensor-core G = Phi A^-1 products (the
+                                     tensor-core form runs by default when N_0 = N_1 <= 128) */
 
 #define GV_MEAS_PROJHEIS 1    /* ProjHeis (ProjHeis.cpp:40-158), Bx = 0 */
 #define GV_MEAS_STAGMAGN 2    /* StagMagnZ (StagMagnZ.cpp:12-43) */
@@ -133,7 +139,9 @@ gv_status gv_job_read_drift_checks(gv_job* job, double* drift_seen, uint64_t* ch
 
 /* Start configurations.  up: n_walkers x Ns bytes, 1 where flavour 0 sits
  * (LatticeState::FockInit), or NULL for the reference's random start with up
- * to 10 retries (vmc.cpp:221-241), drawn from Philox stream 1. */
+ * to 10 retries (vmc.cpp:221-241), drawn from Philox stream 1.  A
+ * mixed-precision job also redraws a random start whose inverse has an entry
+ * above 1e6 (its FP32 ratios would overflow on the first steps). */
 gv_status gv_job_init_walkers(gv_job* job, const int8_t* up);
 
 /* MetroMC::Walk(len, meas) on every walker: len Metropolis steps, the
@@ -199,6 +207,33 @@ gv_status gv_job_read_weight(gv_job* job, double* sigma /* n_walkers */);
 gv_status gv_job_read_projheis(gv_job* job, double* vals, int32_t* nmeas);
 gv_status gv_job_read_stagmagn(gv_job* job, double* vals, int32_t* nmeas);
 gv_status gv_job_read_statspin(gv_job* job, double* vals, int32_t* nmeas);
+
+/* Checkpoint / resume.  The reference saves the final lattice Fock state
+ * (State::Save, State.cpp:117-166) and resumes a chain from it with
+ * --spinstate (vmc.cpp:178-220, LatticeState::FockInit), re-inverting and
+ * drawing fresh random numbers.  A checkpoint here is a self-describing byte
+ * blob holding, per walker, the particle order on the lattice, the
+ * wavefunction's Fock state (exciton channel: slots, sign, channel state,
+ * weight), the amplitude, the Philox counter, the step / acceptance /
+ * re-inversion counters, the drift record, the status and the quantity sums,
+ * behind a header with the job configuration and an FNV-1a checksum.
+ *   GV_CKPT_INVERSES  also store the inverses (and exciton overlap rows) in
+ *                     the job's precision: the restored job then continues
+ *                     bit for bit as the checkpointed one would have.
+ *                     Without it the restore re-inverts in FP64
+ *                     (SlaterDeterminant::Init), which is what the
+ *                     checkpointed job would give after gv_job_reinvert.
+ * gv_job_checkpoint_size: bytes the blob needs.  gv_job_checkpoint waits for
+ * the job's stream and writes the blob (GV_ERR_INVALID if capacity is short).
+ * gv_job_restore loads a blob into a job created with the same lattice,
+ * channel, walkers, seed, walker_base and wavefunction parameters (and, with
+ * stored inverses, the same precision); any mismatch or a damaged blob is
+ * GV_ERR_INVALID and leaves the job as it was.  The quantity sums continue
+ * with gv_job_walk_continue. */
+#define GV_CKPT_INVERSES 1
+gv_status gv_job_checkpoint_size(gv_job* job, int32_t flags, uint64_t* bytes);
+gv_status gv_job_checkpoint(gv_job* job, int32_t flags, void* buf, uint64_t capacity, uint64_t* written);
+gv_status gv_job_restore(gv_job* job, const void* buf, uint64_t size);
 
 /* CUDA-event timer on the job's stream: start records an event, stop
  * records another, waits for it and returns the elapsed milliseconds; the

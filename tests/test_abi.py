@@ -56,6 +56,11 @@ def test_invalid_arguments_are_rejected(lib):
     cfg.n_walkers = 2048
     assert lib.gv_job_footprint(ctypes.byref(cfg), ctypes.byref(out)) == 0
     assert out.value > 2048 * 2 * 128 * 128 * 16
+    # checkpoint entry points reject a missing job or buffer before touching the device
+    assert lib.gv_job_checkpoint_size(None, 0, ctypes.byref(out)) == 1
+    assert lib.gv_job_checkpoint(None, 0, None, 0, None) == 1
+    buf = (ctypes.c_char * 64)()
+    assert lib.gv_job_restore(None, buf, 64) == 1
 
 
 @pytest.mark.parametrize("name,L", [("phi_L4.npz", 4), ("phi_L6.npz", 6), ("phi_L8.npz", 8)])

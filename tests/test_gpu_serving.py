@@ -73,5 +73,6 @@ def test_validation_and_invalid_request(engine):
         r, s = srv.wait(t), srv.wait(u)
         with pytest.raises(engine.GvError):
             srv.submit(gs(8, PHI, 0.1), walkers=8, sweeps=4, meas=7)      # meas must divide L*L
+    assert r["status"] == 0 and s["status"] == 0, (r, s)
     assert 0 <= r["validation_error"] < 1e-5
     assert 0 <= s["validation_error"] < 1e-3

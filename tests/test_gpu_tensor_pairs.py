@@ -1,0 +1,82 @@
+"""StatSpinStruct pair ratios from the split-TF32 tensor-core G = Phi A^-1
+products (k_statspin_tc) against the FP32 CUDA-core dot products
+(scalar_pairs=True) and the FP64 engine on the same configurations.
+
+Bars (stated against the largest entry of each sum):
+  * szz and the occupation diagonals are integer counts: identical;
+  * s+- / s-+ of the tensor-core form vs the FP32 dot products on the same
+    FP32 inverses: 1e-5 (the split recovers FP32 accuracy; plain TF32 would
+    sit near 1e-3);
+  * vs FP64 inverses of the same configurations: 5e-5 (adds the FP32
+    rounding of the inverses).
+"""
+import math
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+PHI = 0.25 * math.pi
+
+
+def _mixed(engine, L, W, seed, **kw):
+    return engine.Job(engine.StagFluxGroundState(L, PHI, 0.1), walkers=W, seed=seed, precision="mixed",
+                      reinv_every=64, deferred_reinversion=True, **kw)
+
+
+def _measure(job, oracle):
+    job.set_measurements(oracle.MEAS_STATSPIN)
+    job.reset_quantities()
+    job.measure()
+    return job.statspin()
+
+
+@pytest.mark.parametrize("L,W", [(4, 8), (8, 24), (12, 16), (16, 40)])
+def test_tensor_core_pairs_match_scalar_and_fp64(engine, oracle, L, W):
+    jt = _mixed(engine, L, W, 3)
+    jt.init_walkers()
+    jt.walk(L * L * 4, 0)
+    jt.reinvert()                       # FP32 copies of fresh FP64 inverses
+    cfg = jt.config()
+    js = _mixed(engine, L, W, 3, scalar_pairs=True)
+    js.init_walkers(cfg)
+    j64 = engine.Job(engine.StagFluxGroundState(L, PHI, 0.1), walkers=W, seed=3, precision="fp64")
+    j64.init_walkers(cfg)
+    st, nt = _measure(jt, oracle)
+    ss, ns = _measure(js, oracle)
+    s64, n64 = _measure(j64, oracle)
+    assert nt == ns == n64 == 1
+    st, ss, s64 = (a.reshape(5, L * L, L * L) for a in (st, ss, s64))
+    # szz (and every diagonal) are counts
+    assert np.array_equal(st[0], s64[0]) and np.array_equal(st[0], ss[0])
+    for a in (st, ss):
+        for k in (1, 2):
+            assert np.array_equal(np.diag(a[k]).real, np.diag(s64[k]).real)
+    scale = np.abs(s64[1:3]).max()
+    assert np.abs(st[1:3] - ss[1:3]).max() < 1e-5 * scale
+    assert np.abs(st[1:3] - s64[1:3]).max() < 5e-5 * scale
+    assert np.abs(ss[1:3] - s64[1:3]).max() < 5e-5 * scale
+    assert not st[3:].any()
+
+
+def test_tensor_core_pairs_inside_the_walk(engine, oracle):
+    """A measuring walk with StatSpinStruct: same chain on both paths (the
+    walk does not depend on how the pairs are summed), same counts, sums equal
+    to FP32 accuracy."""
+    L, W = 16, 24
+    jobs = [_mixed(engine, L, W, 9), _mixed(engine, L, W, 9, scalar_pairs=True)]
+    out = []
+    for j in jobs:
+        j.set_measurements(oracle.MEAS_STATSPIN | oracle.MEAS_PROJHEIS)
+        j.init_walkers()
+        j.walk(L * L * 2, 0)
+        j.walk(L * L * 3, L * L)
+        out.append((j.statspin(), j.projheis(), j.config()))
+    (st, nt), (pt, _), ct = out[0]
+    (ss, ns), (ps, _), cs = out[1]
+    assert nt == ns == 3
+    assert np.array_equal(ct, cs) and np.array_equal(pt, ps)
+    st, ss = st.reshape(5, L * L, L * L), ss.reshape(5, L * L, L * L)
+    assert np.array_equal(st[0], ss[0])
+    assert np.abs(st[1:3] - ss[1:3]).max() < 1e-5 * np.abs(ss[1:3]).max()
