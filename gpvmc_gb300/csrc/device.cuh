@@ -164,6 +164,7 @@ struct DevJob {
     double* ss;                // job-wide StatSpinStruct sums, compact: T (Ns*Ns complex) then
                                // Aud (Ns*Ns real) in a 10*Ns*Ns-double buffer
     int32_t* ss_n;
+    uint32_t* occ;             // 2*Ns*ceil(W/32) occupation bitsets (tensor-core StatSpinStruct)
     cx<double>* scratch64;     // per-CTA FP64 N*N scratch for re-inversion (W*Nmax*Nmax)
     gv_trace* trace;
     int trace_walker;

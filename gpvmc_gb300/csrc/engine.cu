@@ -312,8 +312,13 @@ gv_status statspin_dispatch(gv_job* j)
         GV_CK(cudaFuncSetAttribute(k_statspin_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, int(lay.total)));
         int slot;
         GV_CK(mark_begin(j, 2, &slot));
+        const int cells = j->Ns * ((j->W + 31) / 32);
+        k_occ_bits<<<(cells + 255) / 256, 256, 0, j->stream>>>(j->d, j->d.occ);
+        k_occ_pairs<<<j->Ns, 256, 0, j->stream>>>(j->d, j->d.occ);
         k_statspin_tc<<<std::min(j->W, j->n_sm), kTcThreads, lay.total, j->stream>>>(j->d);
         GV_CK(cudaGetLastError());
+        j->last_launches += 2;
+        j->total_launches += 2;
         GV_CK(mark_end(j, slot));
         ++j->last_launches;
         ++j->total_launches;
@@ -750,6 +755,7 @@ gv_status gv_job_footprint(const gv_job_config* c, uint64_t* bytes)
     b += W * 256;                            // per-walker scalars
     b += W * Nmax * Nmax * 16;               // FP64 re-inversion scratch
     b += 5 * Ns * Ns * 16;                   // StatSpinStruct sums
+    b += 2 * Ns * ((W + 31) / 32) * 4;       // occupation bitsets
     if (tr) {
         b += W * (N0 * Nexc + Nmax) * es;    // overlap rows GupT and g
         b += W * (2 * Ns + 2 * Nmax) * 2;    // wavefunction Fock state
@@ -871,6 +877,7 @@ gv_status gv_job_create(const gv_job_config* cfg, gv_job** out)
         (st = dalloc(j, &d.sm_n, size_t(j->W) * sizeof(int32_t))) ||
         (st = dalloc(j, &d.ss, size_t(5) * j->Ns * j->Ns * 2 * sizeof(double))) ||
         (st = dalloc(j, &d.ss_n, sizeof(int32_t))) ||
+        (st = dalloc(j, &d.occ, sizeof(uint32_t) * 2 * j->Ns * ((j->W + 31) / 32))) ||
         (st = dalloc(j, &d.scratch64, scratch_walkers(j) * j->Nmax * j->Nmax * sizeof(cx<double>))))
         return fail(st);
     d.nbr = nbr; d.edges = reinterpret_cast<const int4*>(edg); d.phase64 = p64; d.phase32 = p32; d.coef64 = c64; d.coef32 = c32;

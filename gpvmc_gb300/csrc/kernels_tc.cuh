@@ -59,9 +59,9 @@ __host__ __device__ inline TcLayout tc_layout(int N)
     for (int i = 0; i < 4; ++i) { l.a[i] = o; o += at; }
     for (int i = 0; i < 6; ++i) { l.b[i] = o; o += bt; }
     l.site = o;
-    o += sizeof(int16_t) * 2 * kTcM;
+    o += sizeof(int16_t) * 2 * 2 * kTcM;     // two walkers' buffers
     l.coef = o;
-    o += sizeof(cx<float>) * 4 * kTcM;
+    o += sizeof(cx<float>) * 2 * 4 * kTcM;
     l.bar = o;
     o += 8;
     l.tbase = o;
@@ -112,50 +112,93 @@ __device__ __forceinline__ void tc_store_split(char* base, const size_t* tiles, 
     }
 }
 
-// Inverse operand, K chunk kc: row r holds AiT[f][r] = (A^-1)(r, f) for
-// f = 32 kc .. 32 kc + 31 (zero outside N x N).  Lanes run over rows, so
-// every warp reads whole 256-byte runs of an AiT row.
-__device__ __forceinline__ void tc_fill_inverse(char* base, const size_t* tiles, int nt, const cx<float>* Ai, int N,
-                                                int rows, int kc)
+// Operand rows of one K chunk (f = 32 kc .. 32 kc + 31), fetched a chunk
+// ahead into registers so that the global loads fly while the previous
+// chunk's MMAs run.  Item i of a thread covers row r = it % rows and 16-byte
+// unit u = it / rows (K values 4u .. 4u + 3), it = threadIdx.x + 256 i; lanes
+// run over rows, so a warp reads whole runs of an AiT row.
+constexpr int kTcItems = 4;   // rows * 8 / kTcThreads for rows <= 128
+
+struct TcRegs {
+    cx<float> inv[kTcItems][4];   // inverse operand: AiT[f][r] = (A^-1)(r, f)
+    cx<float> ph[kTcItems][4];    // orbital operand: phase[site r][f]
+};
+
+__device__ __forceinline__ void tc_load_inverse(TcRegs& R, const cx<float>* Ai, int N, int rows, int kc)
 {
-    for (int it = threadIdx.x; it < rows * 8; it += kTcThreads) {
+#pragma unroll
+    for (int i = 0; i < kTcItems; ++i) {
+        const int it = threadIdx.x + kTcThreads * i, r = it % rows, u = it / rows;
+#pragma unroll
+        for (int t = 0; t < 4; ++t) {
+            const int f = 32 * kc + 4 * u + t;
+            R.inv[i][t] = (it < rows * 8 && r < N && f < N) ? Ai[size_t(f) * N + r] : cx<float>{0.f, 0.f};
+        }
+    }
+}
+
+__device__ __forceinline__ void tc_load_phase(TcRegs& R, const cx<float>* phase, int Nk, const int16_t* site, int N,
+                                              int rows, int kc)
+{
+#pragma unroll
+    for (int i = 0; i < kTcItems; ++i) {
+        const int it = threadIdx.x + kTcThreads * i, r = it % rows, u = it / rows;
+        const int s = (it < rows * 8 && r < N) ? site[r] : -1;
+#pragma unroll
+        for (int t = 0; t < 4; ++t) {
+            const int f = 32 * kc + 4 * u + t;
+            R.ph[i][t] = (s >= 0 && f < N) ? phase[size_t(s) * Nk + f] : cx<float>{0.f, 0.f};
+        }
+    }
+}
+
+// Inverse operand rows -> split tiles.
+__device__ __forceinline__ void tc_store_inverse(char* base, const size_t* tiles, int nt, const TcRegs& R, int rows)
+{
+#pragma unroll
+    for (int i = 0; i < kTcItems; ++i) {
+        const int it = threadIdx.x + kTcThreads * i;
+        if (it >= rows * 8) break;
         const int r = it % rows, u = it / rows;
+        float re[4], im[4];
+#pragma unroll
+        for (int t = 0; t < 4; ++t) { re[t] = R.inv[i][t].x; im[t] = R.inv[i][t].y; }
+        tc_store_split(base, tiles, nt, sw128(r, u), re, im);
+    }
+}
+
+// Orbital operand rows phi_{2f}(site r) = phase[site][f] coef[sub(site)][f]
+// (the walk's own FP32 product) -> split tiles.
+__device__ __forceinline__ void tc_store_phi(char* base, const size_t* tiles, int nt, const TcRegs& R,
+                                             const cx<float>* coef, const int16_t* site, int N, int L, int rows, int kc)
+{
+#pragma unroll
+    for (int i = 0; i < kTcItems; ++i) {
+        const int it = threadIdx.x + kTcThreads * i;
+        if (it >= rows * 8) break;
+        const int r = it % rows, u = it / rows;
+        const int sub = r < N ? sublattice(site[r], L) : 0;
         float re[4], im[4];
 #pragma unroll
         for (int t = 0; t < 4; ++t) {
             const int f = 32 * kc + 4 * u + t;
-            cx<float> a = {0.f, 0.f};
-            if (r < N && f < N) a = Ai[size_t(f) * N + r];
-            re[t] = a.x;
-            im[t] = a.y;
+            const cx<float> v = f < N ? cmul_rn(R.ph[i][t], coef[sub * N + f]) : cx<float>{0.f, 0.f};
+            re[t] = v.x;
+            im[t] = v.y;
         }
         tc_store_split(base, tiles, nt, sw128(r, u), re, im);
     }
 }
 
-// Orbital operand, K chunk kc: row r holds phi_{2f}(site[r]) =
-// phase[site][f] coef[sub(site)][f] (the walk's own FP32 product) for
-// f = 32 kc .. 32 kc + 31 (zero for r >= N or f >= N).
-__device__ __forceinline__ void tc_fill_phi(char* base, const size_t* tiles, int nt, const cx<float>* phase, int Nk,
-                                            const cx<float>* coef, const int16_t* site, int N, int L, int rows, int kc)
+// Exact FP32 -> FP64 widening in integer arithmetic (FP32 subnormals become
+// signed zeros), keeping the epilogue off GB300's narrow FP64 pipe: the pair
+// ratios are formed in FP32 and only the job-wide sums are FP64.
+__device__ __forceinline__ double f32_to_f64(float x)
 {
-    for (int it = threadIdx.x; it < rows * 8; it += kTcThreads) {
-        const int r = it % rows, u = it / rows;
-        float re[4] = {0.f, 0.f, 0.f, 0.f}, im[4] = {0.f, 0.f, 0.f, 0.f};
-        if (r < N) {
-            const int s = site[r], sub = sublattice(s, L);
-#pragma unroll
-            for (int t = 0; t < 4; ++t) {
-                const int f = 32 * kc + 4 * u + t;
-                if (f < N) {
-                    const cx<float> v = cmul_rn(phase[size_t(s) * Nk + f], coef[sub * N + f]);
-                    re[t] = v.x;
-                    im[t] = v.y;
-                }
-            }
-        }
-        tc_store_split(base, tiles, nt, sw128(r, u), re, im);
-    }
+    const uint32_t u = __float_as_uint(x), e = (u >> 23) & 0xFFu;
+    uint64_t d = uint64_t(u & 0x80000000u) << 32;
+    if (e) d |= (uint64_t(e == 0xFFu ? 0x7FFu : e + 896u) << 52) | (uint64_t(u & 0x7FFFFFu) << 29);
+    return __longlong_as_double(static_cast<long long>(d));
 }
 
 // Shared-memory matrix descriptor: start address, leading byte offset 16
@@ -234,8 +277,24 @@ __device__ __forceinline__ void tc_issue_chunk(uint32_t tbase, uint32_t dcol, ui
 
 // The job-wide pair sums (StatSpinStruct m_vals in compact form):
 //   T[i][j]   += r  for up site i, down site j (complex),
-//   Aud[i][j] += 1  (antiparallel count),
+//   Aud[i][j] += 1  (antiparallel count, from k_occ_pairs),
 // from which szz, s+- and s-+ follow (gv_job_read_statspin).
+//
+// Work of one CTA: its walkers w = blockIdx.x + k gridDim.x in turn, each as
+// 2 KC chunks (G_up then G_dn^T, KC = ceil(N / 32) K chunks each).  Per chunk:
+// wait for the previous chunk's MMAs (the tiles are free), split the
+// prefetched operand rows into the tiles, issue 48 MMAs and commit them, then
+// fetch the next chunk's rows (the next walker's first chunk after the last
+// one) while the MMAs run.  The epilogue of a walker follows its last chunk;
+// the per-walker tables (sites, coefficients) are double-buffered so that the
+// next walker's first rows can be fetched before it.
+__device__ __forceinline__ int tc_next_walker(const DevJob& J, int w)
+{
+    for (w += gridDim.x; w < J.W; w += gridDim.x)
+        if (J.status[w] == GV_OK) return w;
+    return -1;
+}
+
 __global__ void __launch_bounds__(kTcThreads, 1) k_statspin_tc(DevJob J)
 {
     extern __shared__ __align__(16) char smem_raw[];
@@ -245,13 +304,12 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_statspin_tc(DevJob J)
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const int N = J.N[0], Nt = tc_ncols(N), Ns = J.Ns, L = J.L, Nk = J.Nk;
     const TcLayout lay = tc_layout(N);
-    int16_t* s_site = reinterpret_cast<int16_t*>(base + lay.site);      // [fl][p]
-    cx<float>* s_coef = reinterpret_cast<cx<float>*>(base + lay.coef);  // [fl][sub][f]
+    int16_t* s_site = reinterpret_cast<int16_t*>(base + lay.site);      // [buf][fl][p]
+    cx<float>* s_coef = reinterpret_cast<cx<float>*>(base + lay.coef);  // [buf][fl][sub][f]
     uint64_t* s_bar = reinterpret_cast<uint64_t*>(base + lay.bar);
     uint32_t* s_tbase = reinterpret_cast<uint32_t*>(base + lay.tbase);
     const uint32_t bar = smem_addr(s_bar);
     double* T = J.ss;
-    double* Aud = J.ss + 2 * size_t(Ns) * Ns;
 
     if (warp == 0) tmem_alloc(s_tbase, 512);
     if (tid == 0) {
@@ -267,43 +325,71 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_statspin_tc(DevJob J)
     uint32_t parity = 0;
     bool failed = false;
 
-    for (int w = blockIdx.x; w < J.W; w += gridDim.x) {
-        if (J.status[w] != GV_OK) continue;
-        __syncthreads();   // the previous walker's epilogue is done with s_site and TMEM
+    // per-walker tables into buffer b
+    auto tables = [&](int w, int b) {
+        int16_t* st = s_site + b * 2 * kTcM;
+        cx<float>* sc = s_coef + b * 4 * kTcM;
         for (int i = tid; i < 2 * N; i += kTcThreads) {
             const int fl = i / N, p = i % N;
-            s_site[fl * kTcM + p] = J.part[(size_t(w) * 2 + fl) * J.Nmax + p];
+            st[fl * kTcM + p] = J.part[(size_t(w) * 2 + fl) * J.Nmax + p];
         }
-        {
-            const cx<float>* cg = J.coef32 + size_t(w) * 4 * Ns;   // [fl][sub][orbital]
-            for (int i = tid; i < 4 * N; i += kTcThreads) {
-                const int fl = i / (2 * N), sub = (i / N) & 1, f = i % N;
-                s_coef[i] = cg[(size_t(fl) * 2 + sub) * Ns + 2 * f];
-            }
+        const cx<float>* cg = J.coef32 + size_t(w) * 4 * Ns;   // [fl][sub][orbital]
+        for (int i = tid; i < 4 * N; i += kTcThreads) {
+            const int fl = i / (2 * N), sub = (i / N) & 1, f = i % N;
+            sc[i] = cg[(size_t(fl) * 2 + sub) * Ns + 2 * f];
         }
+    };
+    // chunk (gm, kc) of walker w: the inverse operand is A for G_up and B for
+    // G_dn^T; the orbital operand the other one
+    auto fetch = [&](TcRegs& R, int w, int b, int gm, int kc) {
+        const int16_t* st = s_site + b * 2 * kTcM;
+        tc_load_inverse(R, ai_ptr<float>(J, gm, w), N, gm == 0 ? kTcM : Nt, kc);
+        tc_load_phase(R, J.phase32, Nk, gm == 0 ? st + kTcM : st, N, gm == 0 ? Nt : kTcM, kc);
+    };
+
+    int w = blockIdx.x < J.W ? int(blockIdx.x) : -1;
+    if (w >= 0 && J.status[w] != GV_OK) w = tc_next_walker(J, w);
+    TcRegs R;
+    int b = 0;
+    if (w >= 0) {
+        tables(w, 0);
         __syncthreads();
-        for (int gm = 0; gm < 2 && !failed; ++gm) {
-            for (int kc = 0; kc < KC; ++kc) {
-                if (gm || kc) {   // the previous chunk's MMAs are done with the tiles
-                    const bool ok = mbar_wait(bar, parity);
-                    if (__syncthreads_or(!ok)) { failed = true; break; }
-                    parity ^= 1u;
-                }
-                if (gm == 0) {   // G_up: A = AiT_up^T (rows c), B = Phi_up at the down sites (rows q)
-                    tc_fill_inverse(base, lay.a, 4, ai_ptr<float>(J, 0, w), N, kTcM, kc);
-                    tc_fill_phi(base, lay.b, 6, J.phase32, Nk, s_coef, s_site + kTcM, N, L, Nt, kc);
-                } else {         // G_dn^T: A = Phi_dn at the up sites (rows c), B = AiT_dn^T (rows q)
-                    tc_fill_phi(base, lay.a, 4, J.phase32, Nk, s_coef + 2 * N, s_site, N, L, kTcM, kc);
-                    tc_fill_inverse(base, lay.b, 6, ai_ptr<float>(J, 1, w), N, Nt, kc);
-                }
-                asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-                tmem_fence_before();
+        fetch(R, w, 0, 0, 0);
+    }
+    bool first = true;   // no MMAs of this walker in flight yet
+    while (w >= 0 && !failed) {
+        const int wn = tc_next_walker(J, w);
+        const int16_t* st = s_site + b * 2 * kTcM;
+        const cx<float>* sc = s_coef + b * 4 * kTcM;
+        for (int step = 0; step < 2 * KC; ++step) {
+            const int gm = step / KC, kc = step % KC;
+            if (!first) {   // the previous chunk's MMAs are done with the tiles
+                const bool ok = mbar_wait(bar, parity);
+                if (__syncthreads_or(!ok)) { failed = true; break; }
+                parity ^= 1u;
+            }
+            first = false;
+            if (gm == 0) {   // G_up: A = AiT_up^T (rows c), B = Phi_up at the down sites (rows q)
+                tc_store_inverse(base, lay.a, 4, R, kTcM);
+                tc_store_phi(base, lay.b, 6, R, sc, st + kTcM, N, L, Nt, kc);
+            } else {         // G_dn^T: A = Phi_dn at the up sites (rows c), B = AiT_dn^T (rows q)
+                tc_store_phi(base, lay.a, 4, R, sc + 2 * N, st, N, L, kTcM, kc);
+                tc_store_inverse(base, lay.b, 6, R, Nt);
+            }
+            asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+            tmem_fence_before();
+            __syncthreads();
+            if (tid == 0) {
+                tmem_fence_after();
+                tc_issue_chunk(tbase, uint32_t(256 * gm), sbase, lay, idesc, kc == 0);
+                tc_commit(bar);
+            }
+            if (step + 1 < 2 * KC) {
+                fetch(R, w, b, (step + 1) / KC, (step + 1) % KC);
+            } else if (wn >= 0) {
+                tables(wn, b ^ 1);
                 __syncthreads();
-                if (tid == 0) {
-                    tmem_fence_after();
-                    tc_issue_chunk(tbase, uint32_t(256 * gm), sbase, lay, idesc, kc == 0);
-                    tc_commit(bar);
-                }
+                fetch(R, wn, b ^ 1, 0, 0);
             }
         }
         if (failed) {
@@ -324,7 +410,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_statspin_tc(DevJob J)
         // chunks of q split between the two warps of a lane group
         const int lg = warp & 3, c = 32 * lg + lane;
         const bool crow = c < N;
-        const int si = crow ? s_site[c] : 0;
+        const int si = crow ? st[c] : 0;
         for (int cc = warp >> 2; cc < Nt / 16; cc += 2) {
             uint32_t r[64];
             const uint32_t ta = tbase + (uint32_t(32 * lg) << 16) + uint32_t(16 * cc);
@@ -338,25 +424,62 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_statspin_tc(DevJob J)
                 for (int t = 0; t < 16; ++t) {
                     const int q = 16 * cc + t;
                     if (q < N) {
-                        const cx<double> gu = {double(__uint_as_float(r[t])), double(__uint_as_float(r[16 + t]))};
-                        const cx<double> gd = {double(__uint_as_float(r[32 + t])), double(__uint_as_float(r[48 + t]))};
-                        const cx<double> v = gu * gd;
-                        const size_t ij = size_t(si) * Ns + s_site[kTcM + q];
-                        atomicAdd(&T[2 * ij], v.x);
-                        atomicAdd(&T[2 * ij + 1], v.y);
-                        atomicAdd(&Aud[ij], 1.0);
+                        const cx<float> gu = {__uint_as_float(r[t]), __uint_as_float(r[16 + t])};
+                        const cx<float> gd = {__uint_as_float(r[32 + t]), __uint_as_float(r[48 + t])};
+                        const cx<float> v = cmul_rn(gu, gd);
+                        const size_t ij = size_t(si) * Ns + st[kTcM + q];
+                        atomicAdd(&T[2 * ij], f32_to_f64(v.x));
+                        atomicAdd(&T[2 * ij + 1], f32_to_f64(v.y));
                     }
                 }
             }
         }
         tmem_fence_before();
         if (tid == 0) atomicAdd(J.ss_n, w == 0 ? 1 : 0);
+        first = true;   // the next walker's first MMAs follow the __syncthreads of its first chunk
+        w = wn;
+        b ^= 1;
     }
     if (failed) mbar_wait(bar, parity);   // the phase that timed out: MMAs in flight finish before TMEM is freed
     tmem_fence_before();
     __syncthreads();
     tmem_fence_after();
     if (warp == 0) tmem_dealloc(tbase, 512);
+}
+
+// Occupation bitsets of the walkers still running: bit w % 32 of word
+// [fl][site][w / 32] is set when walker w holds flavour fl at the site.
+__global__ void k_occ_bits(DevJob J, uint32_t* bits)
+{
+    const int nw = (J.W + 31) / 32;
+    const int idx = blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= J.Ns * nw) return;
+    const int i = idx / nw, k = idx % nw;
+    uint32_t u = 0, d = 0;
+    for (int b = 0; b < 32; ++b) {
+        const int w = 32 * k + b;
+        if (w >= J.W || J.status[w] != GV_OK) continue;
+        if (J.fock[size_t(w) * 2 * J.Ns + i] >= 0) u |= 1u << b;
+        else d |= 1u << b;
+    }
+    bits[size_t(i) * nw + k] = u;
+    bits[size_t(J.Ns + i) * nw + k] = d;
+}
+
+// Aud[i][j] += number of running walkers with flavour 0 at site i and
+// flavour 1 at site j (one thread per entry, so no atomics): the
+// antiparallel counts of StatSpinStruct without one atomic per pair.
+__global__ void k_occ_pairs(DevJob J, const uint32_t* bits)
+{
+    const int nw = (J.W + 31) / 32, Ns = J.Ns, i = blockIdx.x;
+    double* Aud = J.ss + 2 * size_t(Ns) * Ns;
+    const uint32_t* U = bits + size_t(i) * nw;
+    for (int j = threadIdx.x; j < Ns; j += blockDim.x) {
+        const uint32_t* D = bits + size_t(Ns + j) * nw;
+        int c = 0;
+        for (int k = 0; k < nw; ++k) c += __popc(U[k] & D[k]);
+        if (c) Aud[size_t(i) * Ns + j] += double(c);
+    }
 }
 
 }  // namespace
