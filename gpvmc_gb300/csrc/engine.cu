@@ -15,6 +15,7 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <map>
 #include <mutex>
 #include <string>
 #include <vector>
@@ -185,6 +186,31 @@ void wav_hop(const gv_job* j, WavHost& s, int k)
 
 size_t scratch_walkers(const gv_job* j) { return size_t(j->W); }
 
+// Raise (never lower) a kernel's dynamic shared-memory limit on the current
+// device.  Jobs driven from different host threads launch the same kernel
+// instantiation with different sizes; a per-launch cudaFuncSetAttribute
+// could lower the limit between another thread's set and its launch.
+cudaError_t raise_smem_limit(const void* fn, size_t bytes)
+{
+    static std::mutex mu;
+    static std::map<std::pair<int, const void*>, size_t> limit;
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    std::lock_guard<std::mutex> lk(mu);
+    size_t& cur = limit[{dev, fn}];
+    if (bytes <= cur) return cudaSuccess;
+    e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, int(bytes));
+    if (e == cudaSuccess) cur = bytes;
+    return e;
+}
+
+template <typename K>
+cudaError_t raise_smem_limit(K* kernel, size_t bytes)
+{
+    return raise_smem_limit(reinterpret_cast<const void*>(kernel), bytes);
+}
+
 cudaError_t mark_begin(gv_job* j, int kind, int* slot)
 {
     *slot = -1;
@@ -212,7 +238,7 @@ gv_status launch_walk(gv_job* j, uint64_t nsteps, uint64_t s0, uint64_t meas, in
 {
     const bool inkernel = !(j->cfg.flags & GV_FLAG_REINV_DEFERRED);
     const WalkLayout lay = walk_layout<T, NT, KD>(j->Ns, j->Nmax, (mask & GV_MEAS_PROJHEIS) != 0, inkernel);
-    GV_CK(cudaFuncSetAttribute(k_walk_gs<T, NT, KD>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(lay.total)));
+    GV_CK(raise_smem_limit(k_walk_gs<T, NT, KD>, lay.total));
     // shared-memory carveout for up to 8 resident walkers per SM, the rest stays L1
     const int carve = int(std::min<size_t>(100, (8 * (lay.total + 1024) * 100 + 233471) / 233472));
     GV_CK(cudaFuncSetAttribute(k_walk_gs<T, NT, KD>, cudaFuncAttributePreferredSharedMemoryCarveout, carve));
@@ -244,7 +270,7 @@ bool resident_ok(const gv_job* j, uint64_t nsteps)
 gv_status launch_walk_res(gv_job* j, uint64_t nsteps, uint64_t s0, uint64_t meas, int mask)
 {
     const ResLayout lay = res_layout(j->Ns, j->N[0], (mask & GV_MEAS_PROJHEIS) != 0);
-    GV_CK(cudaFuncSetAttribute(k_walk_gs_res, cudaFuncAttributeMaxDynamicSharedMemorySize, int(lay.total)));
+    GV_CK(raise_smem_limit(k_walk_gs_res, lay.total));
     GV_CK(cudaFuncSetAttribute(k_walk_gs_res, cudaFuncAttributePreferredSharedMemoryCarveout, 100));
     int slot;
     GV_CK(mark_begin(j, 0, &slot));
@@ -279,7 +305,7 @@ template <typename T, int NT>
 gv_status launch_check(gv_job* j, double threshold)
 {
     const size_t sm = check_smem_bytes(j->Nmax, NT) + 64;
-    GV_CK(cudaFuncSetAttribute(k_check_reinvert<T, NT>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(sm)));
+    GV_CK(raise_smem_limit(k_check_reinvert<T, NT>, sm));
     int slot;
     GV_CK(mark_begin(j, 1, &slot));
     k_check_reinvert<T, NT><<<j->W, NT, sm, j->stream>>>(j->d, threshold);
@@ -309,7 +335,7 @@ gv_status statspin_dispatch(gv_job* j)
 {
     if (statspin_tc_ok(j)) {
         const TcLayout lay = tc_layout(j->N[0]);
-        GV_CK(cudaFuncSetAttribute(k_statspin_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, int(lay.total)));
+        GV_CK(raise_smem_limit(k_statspin_tc, lay.total));
         int slot;
         GV_CK(mark_begin(j, 2, &slot));
         const int cells = j->Ns * ((j->W + 31) / 32);
@@ -341,7 +367,7 @@ template <typename T, int NT>
 gv_status launch_invert(gv_job* j, int only_due)
 {
     size_t sm = gj_smem_bytes(j->Nmax, NT) + 64;
-    GV_CK(cudaFuncSetAttribute(k_invert<T, NT>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(sm)));
+    GV_CK(raise_smem_limit(k_invert<T, NT>, sm));
     int slot;
     GV_CK(mark_begin(j, 1, &slot));
     k_invert<T, NT><<<j->W, NT, sm, j->stream>>>(j->d, only_due);
@@ -363,7 +389,7 @@ gv_status launch_walk_trans(gv_job* j, uint64_t nsteps)
     constexpr int NT = 256;
     const bool inkernel = !(j->cfg.flags & GV_FLAG_REINV_DEFERRED);
     const TransLayout lay = trans_layout<T, NT>(j->Ns, j->Nmax, j->ch.Nexc, inkernel);
-    GV_CK(cudaFuncSetAttribute(k_walk_trans<T, NT>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(lay.total)));
+    GV_CK(raise_smem_limit(k_walk_trans<T, NT>, lay.total));
     int slot;
     GV_CK(mark_begin(j, 0, &slot));
     k_walk_trans<T, NT><<<j->W, NT, lay.total, j->stream>>>(j->d, nsteps, inkernel ? 1 : 0);
@@ -384,7 +410,7 @@ gv_status launch_measure_trans(gv_job* j, int mask)
 {
     constexpr int NT = 256;
     const MeasLayout lay = meas_layout<T, NT>(j->Ns, j->Nmax, j->ch.Nexc);
-    GV_CK(cudaFuncSetAttribute(k_measure_trans<T, NT>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(lay.total)));
+    GV_CK(raise_smem_limit(k_measure_trans<T, NT>, lay.total));
     int slot;
     GV_CK(mark_begin(j, 2, &slot));
     k_measure_trans<T, NT><<<j->W, NT, lay.total, j->stream>>>(j->d, mask);

@@ -87,6 +87,22 @@ class Job {
         check(gv_job_walk(job_, len, meas), "gv_job_walk");
         check(gv_job_synchronize(job_), "gv_job_synchronize");
     }
+    // State::Save (State.cpp:117-166) with the Philox counters, counters and
+    // quantity sums; with inverses the restored chain continues bit for bit.
+    std::vector<unsigned char> Checkpoint(bool inverses = false)
+    {
+        const int32_t fl = inverses ? GV_CKPT_INVERSES : 0;
+        uint64_t n = 0;
+        check(gv_job_checkpoint_size(job_, fl, &n), "gv_job_checkpoint_size");
+        std::vector<unsigned char> blob(n);
+        check(gv_job_checkpoint(job_, fl, blob.data(), n, nullptr), "gv_job_checkpoint");
+        return blob;
+    }
+    // The --spinstate resume (vmc.cpp:178-220) from a blob of a job with the same configuration.
+    void Restore(const std::vector<unsigned char>& blob)
+    {
+        check(gv_job_restore(job_, blob.data(), blob.size()), "gv_job_restore");
+    }
 
   private:
     gv_job* job_ = nullptr;

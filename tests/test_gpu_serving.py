@@ -76,3 +76,27 @@ def test_validation_and_invalid_request(engine):
     assert r["status"] == 0 and s["status"] == 0, (r, s)
     assert 0 <= r["validation_error"] < 1e-5
     assert 0 <= s["validation_error"] < 1e-3
+
+
+def test_jobs_driven_from_concurrent_threads(engine):
+    """Jobs of different sizes created, started and measured from several host
+    threads at once (as the server's helper threads do): kernels shared by the
+    jobs are launched with different shared-memory sizes from different
+    threads, and every launch must succeed."""
+    import concurrent.futures as cf
+
+    def work(args):
+        L, ch, seed = args
+        wav = (engine.StagFluxTransExciton(L, PHI, 0.1, q=(L // 2, L // 2)) if ch == "trans"
+               else engine.StagFluxGroundState(L, PHI, 0.1))
+        for _ in range(6):
+            j = engine.Job(wav, walkers=8, seed=seed, precision="fp64")
+            j.set_measurements(1)
+            j.init_walkers()
+            j.walk(L * L, L * L)
+            j.close()
+        return True
+
+    jobs = [(8, "gs", 1), (10, "gs", 2), (8, "trans", 3), (10, "trans", 4), (12, "gs", 5), (6, "trans", 6)]
+    with cf.ThreadPoolExecutor(len(jobs)) as ex:
+        assert all(ex.map(work, jobs))
