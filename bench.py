@@ -451,6 +451,46 @@ def run_pairs(g, walkers):
             "error_what": "max |s+-, s-+ (engine) - same from fresh FP64 inverses| / max |s+-, s-+|"}
 
 
+def run_graphs(g, calls=200):
+    """Walk calls of a small job (L=8, 64 walkers, one sweep per call with
+    ProjHeis, StagMagnZ and StatSpinStruct measured), enqueued kernel by
+    kernel and replayed as one CUDA graph per call (GV_FLAG_CUDA_GRAPHS);
+    host wall time of `calls` back-to-back calls."""
+    out = {}
+    for graphs in (False, True):
+        j = g.Job(g.StagFluxGroundState(8, 0.25 * math.pi, 0.1), walkers=64, seed=SEED, precision="mixed",
+                  reinv_every=REINV, deferred_reinversion=True, drift_threshold=DRIFT_THRESHOLD, cuda_graphs=graphs)
+        j.set_measurements(7)
+        j.init_walkers()
+        for _ in range(5):
+            j.walk_continue(64, 64, sync=False)
+        j.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(calls):
+            j.walk_continue(64, 64, sync=False)
+        j.synchronize()
+        dt = time.perf_counter() - t0
+        _, launches = j.last_walk_ms()
+        out["graphs" if graphs else "direct"] = {"calls_per_s": calls / dt, "us_per_call": dt / calls * 1e6,
+                                                 "kernels_per_call": launches,
+                                                 "graph_launches_per_call": 1 if graphs else 0}
+        j.close()
+    out["workload"] = ("L=8, 64 walkers, mixed, one sweep per walk call with ProjHeis, StagMagnZ and "
+                       "StatSpinStruct measured, %d calls back to back (host wall time)" % calls)
+    return out
+
+
+def run_autotune(g):
+    """The autotuner on the headline configuration: every walk-kernel variant
+    timed on a scratch job (608 walkers), the fastest chosen."""
+    job = make_job(g, "mixed", 0)
+    name, times = job.autotune(steps=SWEEP)
+    job.close()
+    return {"choice": name, "us_per_step_all_scratch_walkers": times,
+            "what": "gv_job_autotune on L=16 mixed ground state, drift-checked re-inversion; scratch job of "
+                    "min(walkers, 4 x SMs) walkers, one timed sweep after one warm-up sweep"}
+
+
 def serving_requests(g, n=SERVE_JOBS):
     import numpy as np
     rng = np.random.default_rng(SEED)
@@ -594,6 +634,8 @@ def main():
     exc = run_exciton(g, 4, 1) if (rank == 0 and not args.no_exciton) else None
     serving = run_serving(g) if (rank == 0 and world == 1 and not args.no_serving) else None
     pairs = run_pairs(g, WALKERS) if (rank == 0 and not args.no_pairs) else None
+    graphs = run_graphs(g) if (rank == 0 and not args.no_pairs) else None
+    tune = run_autotune(g) if (rank == 0 and not args.no_pairs) else None
     e2e = run_e2e(g, args.precision, args.steps, rank) if not args.no_e2e else None
     if dist and e2e:
         import torch
@@ -656,6 +698,10 @@ def main():
         out["serving"] = serving
     if pairs:
         out["statspin_tensor_cores"] = pairs
+    if graphs:
+        out["cuda_graphs"] = graphs
+    if tune:
+        out["autotune"] = tune
     print(json.dumps(out))
 
 

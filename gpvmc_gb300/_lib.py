@@ -24,6 +24,7 @@ GV_FLAG_REINV_ON_DRIFT = 2
 GV_FLAG_DELAYED_UPDATES = 4
 GV_FLAG_STREAM_INVERSES = 8
 GV_FLAG_SCALAR_PAIRS = 16
+GV_FLAG_CUDA_GRAPHS = 32
 GV_CKPT_INVERSES = 1
 
 
@@ -95,6 +96,8 @@ _SIGS = {
     "gv_job_read_status": [_P, ctypes.c_void_p],
     "gv_job_walk_continue": [_P, ctypes.c_uint64, ctypes.c_uint64],
     "gv_job_stream": [_P, ctypes.c_void_p],
+    "gv_job_graph_stats": [_P, ctypes.POINTER(ctypes.c_int32), ctypes.POINTER(ctypes.c_int64)],
+    "gv_job_autotune": [_P, ctypes.c_uint64, ctypes.POINTER(ctypes.c_int32), ctypes.c_void_p],
     "gv_job_checkpoint_size": [_P, ctypes.c_int32, ctypes.POINTER(ctypes.c_uint64)],
     "gv_job_checkpoint": [_P, ctypes.c_int32, ctypes.c_void_p, ctypes.c_uint64, ctypes.POINTER(ctypes.c_uint64)],
     "gv_job_restore": [_P, ctypes.c_void_p, ctypes.c_uint64],

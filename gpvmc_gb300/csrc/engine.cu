@@ -18,6 +18,7 @@
 #include <map>
 #include <mutex>
 #include <string>
+#include <tuple>
 #include <vector>
 
 #include "device.cuh"
@@ -61,6 +62,13 @@ struct gv_job {
     std::vector<uint64_t> start_draws;   // Philox stream-1 uniform index per walker
     int n_sm = 1;                        // SMs of the job's device (persistent grids)
     bool trans = false;                  // transverse-exciton channel
+    struct WalkGraph {
+        cudaGraphExec_t exec;
+        int64_t launches;
+    };
+    std::map<std::tuple<uint64_t, uint64_t, int, bool>, WalkGraph> graphs;   // GV_FLAG_CUDA_GRAPHS
+    bool graphs_off = false;
+    int64_t graph_replays = 0;
     std::vector<int16_t> exu, exd;       // channel tables (Channel::exc_up / exc_dn)
 };
 
@@ -104,7 +112,7 @@ bool valid_config(const gv_job_config* c)
     if (c->precision != GV_PREC_FP64 && c->precision != GV_PREC_MIXED) return false;
     if (c->reinv_every < 0) return false;
     if (c->flags & ~(GV_FLAG_REINV_DEFERRED | GV_FLAG_REINV_ON_DRIFT | GV_FLAG_DELAYED_UPDATES | GV_FLAG_STREAM_INVERSES |
-                     GV_FLAG_SCALAR_PAIRS))
+                     GV_FLAG_SCALAR_PAIRS | GV_FLAG_CUDA_GRAPHS))
         return false;
     if ((c->flags & GV_FLAG_REINV_ON_DRIFT) && (!(c->flags & GV_FLAG_REINV_DEFERRED) || !(c->drift_threshold > 0.0)))
         return false;
@@ -945,6 +953,7 @@ gv_status gv_job_destroy(gv_job* j)
 {
     if (!j) return GV_OK;
     if (j->stream) cudaStreamSynchronize(j->stream);
+    for (auto& kv : j->graphs) cudaGraphExecDestroy(kv.second.exec);
     for (void* p : j->allocs) cudaFree(p);
     if (j->ev0) cudaEventDestroy(j->ev0);
     for (cudaEvent_t e : j->ev_pool) cudaEventDestroy(e);
@@ -1082,20 +1091,13 @@ gv_status gv_job_init_walkers(gv_job* j, const int8_t* up)
     return j->trans ? gv_job_synchronize(j) : GV_OK;
 }
 
-static gv_status walk_impl(gv_job* j, uint64_t len, uint64_t meas, gv_trace* dtrace, int trace_walker,
-                           bool reset = true)
+// The kernels of one MetroMC::Walk(len, meas) call, enqueued on the job's stream.
+static gv_status enqueue_walk(gv_job* j, uint64_t len, uint64_t meas, int mask, gv_trace* dtrace, bool reset)
 {
-    if (!j) return GV_ERR_INVALID;
-    if (!j->ready) return GV_ERR_NOT_READY;
-    const int mask = meas ? j->cfg.meas_mask : 0;
-    j->d.trace = dtrace;
-    j->d.trace_walker = trace_walker;
-    j->last_launches = 0;
     if (meas && reset) {
         gv_status rs = reset_quantities(j);
         if (rs) return rs;
     }
-    GV_CK(cudaEventRecord(j->ev0, j->stream));
     gv_status st = GV_OK;
     const int inner = mask & ~GV_MEAS_STATSPIN;
     if (!(mask & GV_MEAS_STATSPIN) && !(j->trans && mask)) {
@@ -1125,6 +1127,65 @@ static gv_status walk_impl(gv_job* j, uint64_t len, uint64_t meas, gv_trace* dtr
         j->d.trace = dtrace;
     }
     if (!st && (j->cfg.flags & GV_FLAG_REINV_DEFERRED) && j->cfg.reinv_every > 0) st = deferred_reinversion(j);
+    return st;
+}
+
+// GV_FLAG_CUDA_GRAPHS: a walk call's kernels captured once per (len, meas,
+// mask, reset) into a CUDA graph and replayed (kernel arguments are fixed per
+// job: device pointers, step counts, the measurement mask).  A capture the
+// runtime refuses turns the job's graphs off and enqueues the kernels directly.
+static gv_status walk_graph(gv_job* j, uint64_t len, uint64_t meas, int mask, bool reset)
+{
+    const auto key = std::make_tuple(len, meas, mask, reset);
+    auto it = j->graphs.find(key);
+    if (it == j->graphs.end()) {
+        const int64_t l0 = j->total_launches, ll0 = j->last_launches;
+        GV_CK(cudaStreamBeginCapture(j->stream, cudaStreamCaptureModeThreadLocal));
+        gv_status st = enqueue_walk(j, len, meas, mask, nullptr, reset);
+        cudaGraph_t g = nullptr;
+        cudaError_t e = cudaStreamEndCapture(j->stream, &g);
+        const int64_t n = j->total_launches - l0;
+        j->total_launches = l0;
+        j->last_launches = ll0;
+        if (st || e != cudaSuccess) {
+            if (g) cudaGraphDestroy(g);
+            cudaGetLastError();
+            j->graphs_off = true;
+            return enqueue_walk(j, len, meas, mask, nullptr, reset);
+        }
+        cudaGraphExec_t x = nullptr;
+        e = cudaGraphInstantiate(&x, g, 0);
+        cudaGraphDestroy(g);
+        if (e != cudaSuccess) {
+            cudaGetLastError();
+            j->graphs_off = true;
+            return enqueue_walk(j, len, meas, mask, nullptr, reset);
+        }
+        if (j->graphs.size() >= 16) {
+            for (auto& kv : j->graphs) cudaGraphExecDestroy(kv.second.exec);
+            j->graphs.clear();
+        }
+        it = j->graphs.emplace(key, gv_job::WalkGraph{x, n}).first;
+    }
+    GV_CK(cudaGraphLaunch(it->second.exec, j->stream));
+    j->last_launches += it->second.launches;
+    j->total_launches += it->second.launches;
+    ++j->graph_replays;
+    return GV_OK;
+}
+
+static gv_status walk_impl(gv_job* j, uint64_t len, uint64_t meas, gv_trace* dtrace, int trace_walker,
+                           bool reset = true)
+{
+    if (!j) return GV_ERR_INVALID;
+    if (!j->ready) return GV_ERR_NOT_READY;
+    const int mask = meas ? j->cfg.meas_mask : 0;
+    j->d.trace = dtrace;
+    j->d.trace_walker = trace_walker;
+    j->last_launches = 0;
+    GV_CK(cudaEventRecord(j->ev0, j->stream));
+    const bool graph = (j->cfg.flags & GV_FLAG_CUDA_GRAPHS) && !j->graphs_off && !dtrace && !j->timing;
+    gv_status st = graph ? walk_graph(j, len, meas, mask, reset) : enqueue_walk(j, len, meas, mask, dtrace, reset);
     GV_CK(cudaEventRecord(j->ev1, j->stream));
     j->d.trace = nullptr;
     j->d.trace_walker = -1;
@@ -1465,6 +1526,119 @@ gv_status gv_job_read_statspin(gv_job* j, double* vals, int32_t* nmeas)
             smp[2 * ik] = -T[2 * ik] + (i == k ? dn[i] : 0.0);
             smp[2 * ik + 1] = -T[2 * ik + 1];
         }
+    return GV_OK;
+}
+
+// ---- Autotuner: the walk-kernel variants that compute the same chain for a
+// job's configuration, timed on a scratch job of the same configuration; the
+// fastest is applied to the job and remembered per configuration shape.
+namespace {
+
+struct TuneKey {
+    int dev, L, channel, precision, flags, wlog;
+    bool operator<(const TuneKey& o) const
+    {
+        return std::tie(dev, L, channel, precision, flags, wlog) <
+               std::tie(o.dev, o.L, o.channel, o.precision, o.flags, o.wlog);
+    }
+};
+std::mutex g_tune_mu;
+std::map<TuneKey, int> g_tune_cache;
+
+constexpr int kTuneVariants = 5;
+constexpr int kTunable = GV_FLAG_DELAYED_UPDATES | GV_FLAG_STREAM_INVERSES;
+
+// Variant v: 0 streaming, default CTA width, immediate updates; 1 the same
+// at 256 threads; 2 / 3 as 0 / 1 with delayed updates; 4 on-chip (TMEM).
+bool tune_applicable(const gv_job* j, int v)
+{
+    if (j->trans) return false;
+    const int dflt = pick_threads(j->Nmax);
+    const int nt = (v == 1 || v == 3) ? 256 : dflt;
+    if ((v == 1 || v == 3) && dflt == 256) return false;   // same as 0 / 2
+    if ((v == 2 || v == 3) && j->Nmax > nt) return false;
+    if (v == 4) {
+        const int f = j->cfg.flags;
+        return j->cfg.precision == GV_PREC_MIXED && j->N[0] == j->N[1] && j->Nmax <= 128 &&
+               (f & GV_FLAG_REINV_DEFERRED);
+    }
+    return true;
+}
+
+void tune_apply(gv_job* j, int v)
+{
+    int f = j->cfg.flags & ~kTunable;
+    if (v == 2 || v == 3) f |= GV_FLAG_DELAYED_UPDATES;
+    if (v != 4 && j->cfg.precision == GV_PREC_MIXED) f |= GV_FLAG_STREAM_INVERSES;
+    j->cfg.flags = f;
+    j->nt = (v == 1 || v == 3) ? 256 : pick_threads(j->Nmax);
+}
+
+}  // namespace
+
+gv_status gv_job_autotune(gv_job* j, uint64_t steps, int32_t* choice, double* us_per_step)
+{
+    if (!j) return GV_ERR_INVALID;
+    if (us_per_step)
+        for (int v = 0; v < kTuneVariants; ++v) us_per_step[v] = -1.0;
+    if (choice) *choice = -1;
+    if (j->trans) return GV_OK;   // one exciton walk kernel: nothing to choose
+    int dev = 0;
+    GV_CK(cudaGetDevice(&dev));
+    int wlog = 0;
+    while ((1 << wlog) < j->W) ++wlog;
+    const TuneKey key{dev, j->cfg.L, j->cfg.channel, j->cfg.precision, j->cfg.flags & ~(kTunable | GV_FLAG_CUDA_GRAPHS),
+                      wlog};
+    {
+        std::lock_guard<std::mutex> lk(g_tune_mu);
+        auto it = g_tune_cache.find(key);
+        if (it != g_tune_cache.end()) {
+            tune_apply(j, it->second);
+            if (choice) *choice = it->second;
+            return GV_OK;
+        }
+    }
+    if (!steps) steps = uint64_t(j->Ns);
+    gv_job_config c = j->cfg;
+    c.n_walkers = std::min(j->W, 4 * j->n_sm);
+    c.meas_mask = 0;
+    c.flags &= ~GV_FLAG_CUDA_GRAPHS;
+    int best = -1;
+    double best_us = 0.0;
+    for (int v = 0; v < kTuneVariants; ++v) {
+        if (!tune_applicable(j, v)) continue;
+        gv_job* s = nullptr;
+        gv_status st = gv_job_create(&c, &s);
+        if (st) return st;
+        tune_apply(s, v);
+        double ms = 0.0, tot = 0.0;
+        int64_t n = 0;
+        if (!(st = gv_job_init_walkers(s, nullptr)) && !(st = gv_job_walk(s, steps, 0)) &&
+            !(st = gv_job_synchronize(s)) && !(st = gv_job_timer_start(s)) && !(st = gv_job_walk(s, steps, 0)) &&
+            !(st = gv_job_timer_stop(s, &tot, &n)))
+            st = gv_job_kernel_ms(s, 0, &ms, &n);   // walk kernels only: the re-inversions are the same for all
+        if (!st) st = gv_job_synchronize(s);
+        gv_job_destroy(s);
+        if (st) return st;
+        const double us = ms * 1e3 / double(steps);   // per step of every scratch walker
+        if (us_per_step) us_per_step[v] = us;
+        if (best < 0 || us < best_us) { best = v; best_us = us; }
+    }
+    if (best < 0) return GV_OK;
+    tune_apply(j, best);
+    {
+        std::lock_guard<std::mutex> lk(g_tune_mu);
+        g_tune_cache[key] = best;
+    }
+    if (choice) *choice = best;
+    return GV_OK;
+}
+
+gv_status gv_job_graph_stats(gv_job* j, int32_t* cached, int64_t* replays)
+{
+    if (!j) return GV_ERR_INVALID;
+    if (cached) *cached = j->graphs_off ? -1 : int32_t(j->graphs.size());
+    if (replays) *replays = j->graph_replays;
     return GV_OK;
 }
 

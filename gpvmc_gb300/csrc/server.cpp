@@ -199,7 +199,8 @@ void gv_server::finish(Req* q, gv_status st)
 gv_status gv_server::start(Req* q)
 {
     cudaSetDevice(device);
-    const gv_job_config& c = q->r.job;
+    gv_job_config c = q->r.job;
+    c.flags |= GV_FLAG_CUDA_GRAPHS;   // the job's walk calls repeat: one graph launch each
     gv_status st = gv_job_create(&c, &q->job);
     if (!st) st = gv_job_set_meas_mask(q->job, c.meas_mask);
     if (!st) st = gv_job_init_walkers(q->job, nullptr);

@@ -89,7 +89,7 @@ class Job:
 
     def __init__(self, wav, walkers=1, seed=1234, precision="fp64", reinv_every=0, walker_base=0,
                  phi_range=None, neel_range=None, deferred_reinversion=False, drift_threshold=None,
-                 delayed_updates=False, stream_inverses=False, scalar_pairs=False):
+                 delayed_updates=False, stream_inverses=False, scalar_pairs=False, cuda_graphs=False):
         L = _lib.lib()
         cfg = _lib.JobConfig()
         cfg.L = wav.L
@@ -117,6 +117,8 @@ class Job:
             cfg.flags |= _lib.GV_FLAG_STREAM_INVERSES
         if scalar_pairs:
             cfg.flags |= _lib.GV_FLAG_SCALAR_PAIRS
+        if cuda_graphs:
+            cfg.flags |= _lib.GV_FLAG_CUDA_GRAPHS
         self.cfg = cfg
         self.wav = wav
         self.walkers = walkers
@@ -171,6 +173,23 @@ class Job:
         check(_lib.lib().gv_job_walk_continue(self._h, length, meas), "gv_job_walk_continue")
         if sync:
             self.synchronize()
+
+    TUNE_VARIANTS = ("streaming", "streaming-256", "streaming-delayed", "streaming-256-delayed", "on-chip")
+
+    def autotune(self, steps=0):
+        """gv_job_autotune: time the walk-kernel variants for this configuration
+        on a scratch job, apply the fastest; returns (name or None, {name: us/step})."""
+        c = ctypes.c_int32()
+        t = np.zeros(5)
+        check(_lib.lib().gv_job_autotune(self._h, steps, ctypes.byref(c), _p(t)), "gv_job_autotune")
+        times = {n: float(x) for n, x in zip(self.TUNE_VARIANTS, t) if x >= 0}
+        return (self.TUNE_VARIANTS[c.value] if c.value >= 0 else None), times
+
+    def graph_stats(self):
+        """(graphs cached, replays) with cuda_graphs=True; cached = -1 if capture was refused."""
+        c, r = ctypes.c_int32(), ctypes.c_int64()
+        check(_lib.lib().gv_job_graph_stats(self._h, ctypes.byref(c), ctypes.byref(r)), "gv_job_graph_stats")
+        return c.value, r.value
 
     # -- checkpoint / resume -------------------------------------------------
     def checkpoint(self, inverses=False):

@@ -72,6 +72,10 @@ typedef int32_t gv_status;
                                      walk (the streaming kernel) instead of on chip; the
                                      on-chip kernel runs by default when N <= 128 and the
                                      re-inversion is deferred */
+#define GV_FLAG_CUDA_GRAPHS 32    /* capture each distinct walk call (len, meas, measured
+                                     quantities) into a CUDA graph once and replay it: one
+                                     launch per call instead of one per kernel (not while a
+                                     job timer runs or a walk is traced) */
 #define GV_FLAG_SCALAR_PAIRS 16   /* mixed ground state: StatSpinStruct pair ratios from FP32
                                      dot products on the CUDA cores instead of the
                                      split-TF32 tensor-core G = Phi A^-1 products (the
@@ -153,6 +157,27 @@ gv_status gv_job_walk(gv_job* job, uint64_t len, uint64_t meas);
  * call instead of restarting (a long MetroMC::Walk cut into pieces: with len
  * a multiple of meas the measurement points are the same). */
 gv_status gv_job_walk_continue(gv_job* job, uint64_t len, uint64_t meas);
+/* Autotuner: times the walk-kernel variants that compute this job's chain --
+ *   0 HBM-streaming kernel, default CTA width (128 threads for N <= 128, else 256)
+ *   1 HBM-streaming kernel, 256 threads
+ *   2, 3 as 0, 1 with delayed updates (depth 4)
+ *   4 on-chip kernel (inverses in TMEM; mixed ground state, N <= 128, deferred re-inversion)
+ * on a scratch job of the same configuration (min(n_walkers, 4 x SMs)
+ * walkers, `steps` timed steps per walker after as many warm-up steps; 0:
+ * one sweep), applies the fastest to the job (its GV_FLAG_DELAYED_UPDATES /
+ * GV_FLAG_STREAM_INVERSES bits and CTA width) and remembers the choice for
+ * jobs of the same shape (device, L, channel, precision, other flags,
+ * walkers rounded up to a power of two) in this process.  *choice = the
+ * variant (-1: nothing to choose, e.g. the exciton channel); us_per_step[5]
+ * (optional) = walk-kernel device microseconds per step of all scratch
+ * walkers (re-inversions, the same under every variant, excluded), -1 for
+ * variants not applicable or not timed (a remembered choice times nothing).
+ * Call it before gv_job_init_walkers or between walks; the chain is the same
+ * under every variant up to FP32 rounding. */
+gv_status gv_job_autotune(gv_job* job, uint64_t steps, int32_t* choice, double* us_per_step);
+/* GV_FLAG_CUDA_GRAPHS: graphs cached for this job (-1: the runtime refused a
+ * capture and the job enqueues its kernels directly) and graph replays so far. */
+gv_status gv_job_graph_stats(gv_job* job, int32_t* cached, int64_t* replays);
 /* The job's CUDA stream (cudaStream_t), for callers that order their own work
  * after the job's kernels. */
 gv_status gv_job_stream(gv_job* job, void** stream);
