@@ -62,6 +62,15 @@ __device__ __forceinline__ void tmem_wait_ld(uint32_t (&r)[64])
 {
     asm volatile("tcgen05.wait::ld.sync.aligned;" : "+r"(r[0]), "+r"(r[1]), "+r"(r[2]), "+r"(r[3]), "+r"(r[4]), "+r"(r[5]), "+r"(r[6]), "+r"(r[7]), "+r"(r[8]), "+r"(r[9]), "+r"(r[10]), "+r"(r[11]), "+r"(r[12]), "+r"(r[13]), "+r"(r[14]), "+r"(r[15]), "+r"(r[16]), "+r"(r[17]), "+r"(r[18]), "+r"(r[19]), "+r"(r[20]), "+r"(r[21]), "+r"(r[22]), "+r"(r[23]), "+r"(r[24]), "+r"(r[25]), "+r"(r[26]), "+r"(r[27]), "+r"(r[28]), "+r"(r[29]), "+r"(r[30]), "+r"(r[31]), "+r"(r[32]), "+r"(r[33]), "+r"(r[34]), "+r"(r[35]), "+r"(r[36]), "+r"(r[37]), "+r"(r[38]), "+r"(r[39]), "+r"(r[40]), "+r"(r[41]), "+r"(r[42]), "+r"(r[43]), "+r"(r[44]), "+r"(r[45]), "+r"(r[46]), "+r"(r[47]), "+r"(r[48]), "+r"(r[49]), "+r"(r[50]), "+r"(r[51]), "+r"(r[52]), "+r"(r[53]), "+r"(r[54]), "+r"(r[55]), "+r"(r[56]), "+r"(r[57]), "+r"(r[58]), "+r"(r[59]), "+r"(r[60]), "+r"(r[61]), "+r"(r[62]), "+r"(r[63])::"memory");
 }
+__device__ __forceinline__ void tmem_wait_ld(uint32_t (&r)[4])
+{
+    asm volatile("tcgen05.wait::ld.sync.aligned;" : "+r"(r[0]), "+r"(r[1]), "+r"(r[2]), "+r"(r[3])::"memory");
+}
+__device__ __forceinline__ void tmem_wait_ld(uint32_t (&r)[8])
+{
+    asm volatile("tcgen05.wait::ld.sync.aligned;"
+                 : "+r"(r[0]), "+r"(r[1]), "+r"(r[2]), "+r"(r[3]), "+r"(r[4]), "+r"(r[5]), "+r"(r[6]), "+r"(r[7])::"memory");
+}
 __device__ __forceinline__ void tmem_st64(uint32_t taddr, const uint32_t (&r)[64])
 {
     asm volatile("tcgen05.st.sync.aligned.32x32b.x64.b32 [%0], {%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31,%32,%33,%34,%35,%36,%37,%38,%39,%40,%41,%42,%43,%44,%45,%46,%47,%48,%49,%50,%51,%52,%53,%54,%55,%56,%57,%58,%59,%60,%61,%62,%63,%64};" ::"r"(taddr), "r"(r[0]), "r"(r[1]), "r"(r[2]), "r"(r[3]), "r"(r[4]), "r"(r[5]), "r"(r[6]), "r"(r[7]), "r"(r[8]), "r"(r[9]), "r"(r[10]), "r"(r[11]), "r"(r[12]), "r"(r[13]), "r"(r[14]), "r"(r[15]), "r"(r[16]), "r"(r[17]), "r"(r[18]), "r"(r[19]), "r"(r[20]), "r"(r[21]), "r"(r[22]), "r"(r[23]), "r"(r[24]), "r"(r[25]), "r"(r[26]), "r"(r[27]), "r"(r[28]), "r"(r[29]), "r"(r[30]), "r"(r[31]), "r"(r[32]), "r"(r[33]), "r"(r[34]), "r"(r[35]), "r"(r[36]), "r"(r[37]), "r"(r[38]), "r"(r[39]), "r"(r[40]), "r"(r[41]), "r"(r[42]), "r"(r[43]), "r"(r[44]), "r"(r[45]), "r"(r[46]), "r"(r[47]), "r"(r[48]), "r"(r[49]), "r"(r[50]), "r"(r[51]), "r"(r[52]), "r"(r[53]), "r"(r[54]), "r"(r[55]), "r"(r[56]), "r"(r[57]), "r"(r[58]), "r"(r[59]), "r"(r[60]), "r"(r[61]), "r"(r[62]), "r"(r[63]) : "memory");
@@ -73,6 +82,7 @@ constexpr int kResThreads = 256;
 constexpr int kResTmemCols = 512;                 // both flavours, 128 complex FP32 per lane each
 constexpr size_t kResMinSmem = 116 * 1024;        // over half an SM's shared memory: one CTA per SM
 constexpr int kResRngBatch = 32;
+constexpr int kResSpec = 2;                       // proposals evaluated per barrier
 
 struct ResLayout {
     size_t fock, part, nbr, sub, coef, red, wpart, w, tile, rv, ru4, ru4d, racc, rq, rqp, nb, redm, tbase, total, used;
@@ -89,7 +99,7 @@ __host__ __device__ inline ResLayout res_layout(int Ns, int N, bool projheis)
     l.nbr = al(sizeof(int16_t) * 4 * Ns);
     l.sub = al(sizeof(int8_t) * Ns);
     l.coef = al(c * 4 * N);
-    l.red = al(sizeof(float) * 2 * 16);
+    l.red = al(sizeof(float) * 2 * 16 * kResSpec);
     l.wpart = al(c * 2 * 4 * 128);
     l.w = al(c * 2 * 128);
     l.tile = al(c * (kResThreads / 32) * 32 * 33);   // per warp 32 x 32 products, row stride 33
@@ -209,13 +219,19 @@ __global__ void __launch_bounds__(kResThreads, 1) k_walk_gs_res(DevJob J, uint64
     int nacc = 0;   // accepted ratio pairs waiting to be multiplied into the amplitude
     const WalkCtx<T> C = {&J, w, Ns, N, L, Nk, N, N, s_fock, s_part, s_nbr, s_coef, s_rq, s_redm,
                           phase, ai_ptr<T>(J, 0, w), ai_ptr<T>(J, 1, w)};
-    // phase[v][f] for both sites of the next proposal, loaded one step ahead
-    cx<T> ph_a = {0.f, 0.f}, ph_b = {0.f, 0.f};
-    bool have_ph = false;
-
-    for (uint64_t s = 0; s < nsteps; ++s, k += 4) {
-        const int bi = int(s % kResRngBatch);
-        if (bi == 0) {   // the next batch of proposals and accept uniforms (one lane per step)
+    // Proposals are evaluated kResSpec at a time: every thread forms its terms
+    // of the next kb proposals' ratios (same inverse, same occupancy), one
+    // barrier combines them, and the steps are then resolved in order until
+    // the first accepted move, whose update invalidates the rest (they are
+    // evaluated again, from the new inverse, in the next round).  A round
+    // never crosses a uniform batch or a measurement step.
+    const bool measuring = meas != 0 && mask != 0;
+    // steps from s to the next measuring step (0: s itself is measured)
+    uint64_t to_meas = measuring ? (meas == 1 ? 0 : (meas - (s0 % meas)) % meas) : ~uint64_t(0);
+    uint64_t s = 0;
+    while (s < nsteps) {
+        const int bi0 = int(s % kResRngBatch);
+        if (bi0 == 0) {   // the next batch of proposals and accept uniforms (one lane per step)
             __syncthreads();   // every thread is done with the previous batch
             // the amplitude (FP64, off the per-step path): the previous batch's accepted ratios
             if (tid == 32) {
@@ -226,7 +242,7 @@ __global__ void __launch_bounds__(kResThreads, 1) k_walk_gs_res(DevJob J, uint64
             }
             nacc = 0;
             if (warp == 0 && s + lane < nsteps) {
-                const uint64_t kl = k + 4 * uint64_t(lane);
+                const uint64_t kl = k + 4 * (s + uint64_t(lane));
                 uint32_t x[4], y[4];
                 philox_call(J.seed, wid, 0, kl >> 1, x);
                 philox_call(J.seed, wid, 0, (kl >> 1) + 1, y);
@@ -238,112 +254,148 @@ __global__ void __launch_bounds__(kResThreads, 1) k_walk_gs_res(DevJob J, uint64
             }
             __syncthreads();
         }
-        const int v1 = s_rv[2 * bi], v2 = s_rv[2 * bi + 1];
-        const cx<T> ph1 = ph_a, ph2 = ph_b;
-        const bool ph_ok = have_ph;
-        have_ph = false;
-        if (bi + 1 < kResRngBatch && s + 1 < nsteps && f < N) {
-            ph_a = phase[size_t(s_rv[2 * bi + 2]) * Nk + f];
-            ph_b = phase[size_t(s_rv[2 * bi + 3]) * Nk + f];
-            have_ph = true;
-        }
-        const int f1 = s_fock[v1] >= 0 ? 0 : 1;
-        const int f2 = s_fock[v2] >= 0 ? 0 : 1;
-        int kind = 0, accepted;
-        T ratio = T(1);
-        if (f1 == f2) {
-            accepted = 1;   // m_weight / m_state_weight = 1 (MetroMC.cpp:41)
-            ++c_noop;
-        } else {
-            kind = 1;
-            const int upf = (f1 == 0) ? v1 : v2, upt = (f1 == 0) ? v2 : v1;
-            const int dnf = upt, dnt = upf;
-            const int cu = s_fock[upf], cd = s_fock[Ns + dnf];
-            const int cg = g ? cd : cu, tg = g ? dnt : upt;   // this flavour's particle and destination
-            T* rb = s_red + rbuf * 16;
-            rbuf ^= 1;
-            // proposal: (A^-1)(c, f) from this lane's column c, u_f = phi_{2f}(t)
-            cx<T> u = {0.f, 0.f}, a;
-            {
-                uint32_t r[2];
-                tmem_ld2(trow + 2 * cg, r);
-                if (f < N) {
-                    const cx<T> ph = ph_ok ? (tg == v1 ? ph1 : ph2) : phase[size_t(tg) * Nk + f];
-                    u = cmul_rn(ph, cf[s_sub[tg] * N + f]);
+        uint64_t kb64 = nsteps - s;
+        if (kb64 > uint64_t(kResRngBatch - bi0)) kb64 = uint64_t(kResRngBatch - bi0);
+        if (kb64 > uint64_t(kResSpec)) kb64 = kResSpec;
+        if (measuring && kb64 > to_meas + 1) kb64 = to_meas + 1;   // to_meas < meas here
+        const int kb = int(kb64);
+        if (kb < 1) { status = GV_ERR_INVALID; break; }   // a round always resolves a step
+        // this thread's terms of the kb proposals: (A^-1)(c, f) from this lane's
+        // column c (one 2-column load each), u_f = phi_{2f}(t)
+        cx<T> pa[kResSpec], pu[kResSpec];
+        uint32_t rr[2 * kResSpec];
+        int psite[kResSpec], ppart[kResSpec];   // (upf | upt << 16), (cu | cd << 16) of proposal i
+        int anti = 0;   // bit i: proposal i exchanges antiparallel spins
+#pragma unroll
+        for (int i = 0; i < kResSpec; ++i) {
+            pu[i] = cx<T>{0.f, 0.f};
+            rr[2 * i] = rr[2 * i + 1] = 0u;
+            psite[i] = ppart[i] = 0;
+            if (i < kb) {
+                const int v1 = s_rv[2 * (bi0 + i)], v2 = s_rv[2 * (bi0 + i) + 1];
+                const bool up1 = s_fock[v1] >= 0, up2 = s_fock[v2] >= 0;
+                if (up1 != up2) {
+                    anti |= 1 << i;
+                    const int upf = up1 ? v1 : v2, upt = up1 ? v2 : v1;
+                    const int cu = s_fock[upf], cd = s_fock[Ns + upt];
+                    psite[i] = upf | (upt << 16);
+                    ppart[i] = cu | (cd << 16);
+                    const int cg = g ? cd : cu;     // this flavour's particle
+                    const int tg = g ? upf : upt;   // and its destination
+                    uint32_t r2[2];
+                    tmem_ld2(trow + 2 * cg, r2);
+                    rr[2 * i] = r2[0];
+                    rr[2 * i + 1] = r2[1];
+                    if (f < N) pu[i] = cmul_rn(phase[size_t(tg) * Nk + f], cf[s_sub[tg] * N + f]);
                 }
-                tmem_wait_ld(r);
-                a = cx<T>{__uint_as_float(r[0]), __uint_as_float(r[1])};
             }
-            cx<T> part = warp_sum(a * u);
-            if (lane == 0) { rb[warp * 2] = part.x; rb[warp * 2 + 1] = part.y; }
-            __syncthreads();
-            const cx<T> ru = {rb[0] + rb[2] + rb[4] + rb[6], rb[1] + rb[3] + rb[5] + rb[7]};
-            const cx<T> rd = {rb[8] + rb[10] + rb[12] + rb[14], rb[9] + rb[11] + rb[13] + rb[15]};
-            ratio = Accept<T>::ratio(ru, rd);
-            if (!isfinite(ratio)) { status = GV_ERR_NAN; break; }
-            accepted = ratio > T(1) ? 1 : (s_ru4[bi] < ratio);
-            if (!accepted) {
-                ++c_rej;
+        }
+        tmem_wait_ld(rr);
+        T* rb = s_red + rbuf * 16 * kResSpec;
+        rbuf ^= 1;
+#pragma unroll
+        for (int i = 0; i < kResSpec; ++i) {
+            pa[i] = cx<T>{__uint_as_float(rr[2 * i]), __uint_as_float(rr[2 * i + 1])};
+            if (anti & (1 << i)) {
+                const cx<T> part = warp_sum(pa[i] * pu[i]);
+                if (lane == 0) { rb[16 * i + warp * 2] = part.x; rb[16 * i + warp * 2 + 1] = part.y; }
+            }
+        }
+        __syncthreads();
+        int done = kb;
+#pragma unroll
+        for (int i = 0; i < kResSpec; ++i) {
+            if (i >= kb || done < kb) continue;
+            const int bi = bi0 + i;
+            const int v1 = s_rv[2 * bi], v2 = s_rv[2 * bi + 1];
+            int kind = 0, accepted;
+            T ratio = T(1);
+            if (!(anti & (1 << i))) {
+                accepted = 1;   // m_weight / m_state_weight = 1 (MetroMC.cpp:41)
+                ++c_noop;
             } else {
-                if (norm2(ru) < T(1e-9) || norm2(rd) < T(1e-9)) { status = GV_ERR_SINGULAR; break; }
-                const cx<T> ir = cinv(g ? rd : ru);
-                // w = A^-1 u: this warp's 32 rows times u_f, summed over lanes per particle
-                cx<T>* wpart = s_wpart + (g * 4 + (warp & 3)) * 128;
-                for (int c = 0; c < NCH; ++c) {
-                    uint32_t r[64];
-                    tmem_ld64(trow + 64 * c, r);
-                    tmem_wait_ld(r);
-                    cx<T> v[32];
+                kind = 1;
+                const T* q = rb + 16 * i;
+                const cx<T> ru = {q[0] + q[2] + q[4] + q[6], q[1] + q[3] + q[5] + q[7]};
+                const cx<T> rd = {q[8] + q[10] + q[12] + q[14], q[9] + q[11] + q[13] + q[15]};
+                ratio = Accept<T>::ratio(ru, rd);
+                if (!isfinite(ratio)) { status = GV_ERR_NAN; done = -1 - i; continue; }
+                accepted = ratio > T(1) ? 1 : (s_ru4[bi] < ratio);
+                if (!accepted) {
+                    ++c_rej;
+                } else {
+                    if (norm2(ru) < T(1e-9) || norm2(rd) < T(1e-9)) { status = GV_ERR_SINGULAR; done = -1 - i; continue; }
+                    // occupancy of this step as read before the round's barrier
+                    const int upf = psite[i] & 0xFFFF, upt = psite[i] >> 16;
+                    const int dnf = upt, dnt = upf;
+                    const int cu = ppart[i] & 0xFFFF, cd = ppart[i] >> 16;
+                    const int cg = g ? cd : cu;
+                    const cx<T> u = pu[i], a = pa[i];
+                    const cx<T> ir = cinv(g ? rd : ru);
+                    // w = A^-1 u: this warp's 32 rows times u_f, summed over lanes per particle
+                    cx<T>* wpart = s_wpart + (g * 4 + (warp & 3)) * 128;
+                    for (int c = 0; c < NCH; ++c) {
+                        uint32_t r[64];
+                        tmem_ld64(trow + 64 * c, r);
+                        tmem_wait_ld(r);
+                        cx<T> v[32];
 #pragma unroll
-                    for (int j = 0; j < 32; ++j) v[j] = cx<T>{__uint_as_float(r[2 * j]), __uint_as_float(r[2 * j + 1])} * u;
-                    wpart[32 * c + lane] = warp_transpose_sum(v, s_tile);
-                }
-                wg_sync(g);
-                if (f < 32 * NCH) {   // w_p - [p == c]
-                    const cx<T>* wp0 = s_wpart + g * 4 * 128;
-                    cx<T> wq = wp0[f] + wp0[128 + f] + wp0[256 + f] + wp0[384 + f];
-                    if (f == cg) wq.x -= 1.f;
-                    s_w[g * 128 + f] = wq;
-                }
-                wg_sync(g);
-                // row update: AiT[f][p] -= (w_p - [p == c]) * (A^-1)(c, f) / r
-                const cx<T> coef = cneg(a * ir);
-                const cx<T>* wv = s_w + g * 128;
-                for (int c = 0; c < NCH; ++c) {
-                    uint32_t r[64];
-                    tmem_ld64(trow + 64 * c, r);
-                    tmem_wait_ld(r);
-#pragma unroll
-                    for (int j = 0; j < 32; ++j) {
-                        const int p = 32 * c + j;
-                        cx<T> e = {__uint_as_float(r[2 * j]), __uint_as_float(r[2 * j + 1])};
-                        cmac(e, wv[p], coef);
-                        r[2 * j] = __float_as_uint(e.x);
-                        r[2 * j + 1] = __float_as_uint(e.y);
+                        for (int j = 0; j < 32; ++j) v[j] = cx<T>{__uint_as_float(r[2 * j]), __uint_as_float(r[2 * j + 1])} * u;
+                        wpart[32 * c + lane] = warp_transpose_sum(v, s_tile);
                     }
-                    tmem_st64(trow + 64 * c, r);
+                    wg_sync(g);
+                    if (f < 32 * NCH) {   // w_p - [p == c]
+                        const cx<T>* wp0 = s_wpart + g * 4 * 128;
+                        cx<T> wq = wp0[f] + wp0[128 + f] + wp0[256 + f] + wp0[384 + f];
+                        if (f == cg) wq.x -= 1.f;
+                        s_w[g * 128 + f] = wq;
+                    }
+                    wg_sync(g);
+                    // row update: AiT[f][p] -= (w_p - [p == c]) * (A^-1)(c, f) / r
+                    const cx<T> coef = cneg(a * ir);
+                    const cx<T>* wv = s_w + g * 128;
+                    for (int c = 0; c < NCH; ++c) {
+                        uint32_t r[64];
+                        tmem_ld64(trow + 64 * c, r);
+                        tmem_wait_ld(r);
+#pragma unroll
+                        for (int j = 0; j < 32; ++j) {
+                            const int p = 32 * c + j;
+                            cx<T> e = {__uint_as_float(r[2 * j]), __uint_as_float(r[2 * j + 1])};
+                            cmac(e, wv[p], coef);
+                            r[2 * j] = __float_as_uint(e.x);
+                            r[2 * j + 1] = __float_as_uint(e.y);
+                        }
+                        tmem_st64(trow + 64 * c, r);
+                    }
+                    tmem_wait_st();
+                    if (tid == 0) {
+                        s_fock[upt] = int16_t(cu); s_fock[upf] = -1; s_part[cu] = int16_t(upt);
+                        s_fock[Ns + dnt] = int16_t(cd); s_fock[Ns + dnf] = -1; s_part[N + cd] = int16_t(dnt);
+                        s_racc[2 * nacc] = ru;
+                        s_racc[2 * nacc + 1] = rd;
+                    }
+                    ++nacc;
+                    ++c_acc;
+                    ++since;
+                    __syncthreads();
+                    done = i + 1;   // the later proposals saw the old inverse and occupancy
                 }
-                tmem_wait_st();
-                if (tid == 0) {
-                    s_fock[upt] = int16_t(cu); s_fock[upf] = -1; s_part[cu] = int16_t(upt);
-                    s_fock[Ns + dnt] = int16_t(cd); s_fock[Ns + dnf] = -1; s_part[N + cd] = int16_t(dnt);
-                    s_racc[2 * nacc] = ru;
-                    s_racc[2 * nacc + 1] = rd;
-                }
-                ++nacc;
-                ++c_acc;
-                ++since;
-                __syncthreads();
+            }
+            if (J.trace && w == J.trace_walker && tid == 0) {
+                gv_trace t;
+                t.v1 = v1; t.v2 = v2; t.kind = kind; t.accepted = accepted; t.khop = kind ? 0 : -1; t.pad = 0;
+                t.ratio = double(ratio); t.u4 = s_ru4d[bi];
+                J.trace[s + i] = t;
             }
         }
-        if (J.trace && w == J.trace_walker && tid == 0) {
-            gv_trace t;
-            t.v1 = v1; t.v2 = v2; t.kind = kind; t.accepted = accepted; t.khop = kind ? 0 : -1; t.pad = 0;
-            t.ratio = double(ratio); t.u4 = s_ru4d[bi];
-            J.trace[s] = t;
+        if (done < 0) {   // stopped at step s - 1 - done: the walker takes no further steps
+            s += uint64_t(-1 - done);
+            break;
         }
-        const uint64_t gs = s0 + s;
-        if (meas && (meas == 1 || gs % meas == 0) && mask) {
+        s += uint64_t(done);
+        if (measuring && uint64_t(done) == to_meas + 1) {   // the round ended on a measuring step
+            to_meas = meas - 1;
             if (mask & GV_MEAS_PROJHEIS) {
                 // ProjHeis pass 1 from TMEM: the ratio of moving particle p of flavour g to
                 // neighbour slot kk is sum_f (A^-1)(p, f) phi_{2f}(j); lane f forms its
@@ -397,8 +449,11 @@ __global__ void __launch_bounds__(kResThreads, 1) k_walk_gs_res(DevJob J, uint64
                 projheis_from_rq<T, kResThreads>(C);
             }
             if (mask & GV_MEAS_STAGMAGN) stagmagn_now<T, kResThreads>(C);
+        } else if (measuring) {
+            to_meas -= uint64_t(done);
         }
     }
+    k += 4 * s;
     __syncthreads();
     if (tid == 32) {
         for (int i = 0; i < nacc; ++i) {
