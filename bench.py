@@ -357,8 +357,25 @@ def run_exciton(g, sweeps, fp64_sweeps):
             err = np.abs(pm - pr).max(axis=(1, 2)) / np.abs(pr).max(axis=(1, 2))
             out["ho_error_vs_fp64"] = {"median": float(np.median(err)), "max": float(err.max()),
                                        "what": "max |H,O mixed - H,O FP64| / max |H,O FP64| per walker, one measurement"}
-            out["measure_ms_per_sweep"] = mk / max(1, mn) if mn else None
             ref.close()
+
+            def measure_ms(job):
+                job.timer_start()
+                job.measure()
+                job.measure()
+                job.timer_stop()
+                m, _ = job.kernel_ms(2)
+                return m / 2
+
+            js = g.Job(g.StagFluxTransExciton(L, 0.25 * math.pi, 0.1, q=(4, 4)), walkers=EXC_WALKERS, seed=SEED,
+                       precision="mixed", scalar_pairs=True)
+            js.set_measurements(1)
+            js.init_walkers(cfg)
+            out["measure_ms"] = {"tensor_cores": measure_ms(j), "cuda_cores": measure_ms(js),
+                                 "what": "one ProjHeis H/O measurement of the q=(4,4) job's %d walkers (kernel time): "
+                                         "overlap rows Z = GupT^T Phi as split-TF32 tcgen05 products vs FP32 dot "
+                                         "products on the CUDA cores" % EXC_WALKERS}
+            js.close()
         for j in jobs:
             j.close()
     out["mixed_over_fp64"] = out["mixed"]["value"] / out["fp64"]["value"]

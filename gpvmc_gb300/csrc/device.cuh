@@ -183,6 +183,7 @@ struct DevJob {
     void* gup;                 // W*N0*Nexc, GupT[f][k] = sum_p phi_{exc_up[k]}(x_p) (A0^-1)(p, f)
     void* gdn;                 // W*Nmax,    g[f] = sum_p phi_{exc_dn[cur]}(x_p) (A1^-1)(p, f)
     cx<double>* pjx;           // W*2*Nexc*Nexc ProjHeis H and O sums
+    cx<float>* zbuf;           // W*N1*Nexc tensor-core Z[d][k] = sum_f GupT[f][k] phi_f(d) (mixed, or null)
 };
 
 // Amplitude kept as (complex mantissa, base-2 exponent); renormalised

@@ -332,6 +332,14 @@ gv_status deferred_reinversion(gv_job* j)
     return j->cfg.precision == GV_PREC_FP64 ? launch_check<double, 256>(j, thr) : launch_check<float, 256>(j, thr);
 }
 
+// Tensor-core exciton overlap rows Z = GupT^T Phi_0: mixed exciton channel with
+// Nexc <= 128, N1 <= 128, N0 <= 160.
+bool trans_z_tc_ok(const gv_job* j)
+{
+    return j->trans && j->cfg.precision == GV_PREC_MIXED && j->ch.Nexc <= kTcM && j->N[1] <= kTcM &&
+           j->N[0] <= kTcMaxK && !(j->cfg.flags & GV_FLAG_SCALAR_PAIRS);
+}
+
 // Tensor-core StatSpinStruct: mixed ground state with N_0 = N_1 <= 128.
 bool statspin_tc_ok(const gv_job* j)
 {
@@ -418,10 +426,23 @@ gv_status launch_measure_trans(gv_job* j, int mask)
 {
     constexpr int NT = 256;
     const MeasLayout lay = meas_layout<T, NT>(j->Ns, j->Nmax, j->ch.Nexc);
+    const cx<float>* zpre = nullptr;
+    if (j->d.zbuf && (mask & GV_MEAS_PROJHEIS)) {   // Z = GupT^T Phi_0 on the tensor cores first
+        const TcLayout zl = tc_layout_z(j->N[1]);
+        GV_CK(raise_smem_limit(k_trans_z_tc, zl.total));
+        int zs;
+        GV_CK(mark_begin(j, 2, &zs));
+        k_trans_z_tc<<<std::min(j->W, j->n_sm), kTcThreads, zl.total, j->stream>>>(j->d, j->d.zbuf);
+        GV_CK(cudaGetLastError());
+        GV_CK(mark_end(j, zs));
+        ++j->last_launches;
+        ++j->total_launches;
+        zpre = j->d.zbuf;
+    }
     GV_CK(raise_smem_limit(k_measure_trans<T, NT>, lay.total));
     int slot;
     GV_CK(mark_begin(j, 2, &slot));
-    k_measure_trans<T, NT><<<j->W, NT, lay.total, j->stream>>>(j->d, mask);
+    k_measure_trans<T, NT><<<j->W, NT, lay.total, j->stream>>>(j->d, mask, zpre);
     GV_CK(cudaGetLastError());
     GV_CK(mark_end(j, slot));
     ++j->last_launches;
@@ -794,6 +815,7 @@ gv_status gv_job_footprint(const gv_job_config* c, uint64_t* bytes)
         b += W * (N0 * Nexc + Nmax) * es;    // overlap rows GupT and g
         b += W * (2 * Ns + 2 * Nmax) * 2;    // wavefunction Fock state
         b += W * 2 * Nexc * Nexc * 16;       // ProjHeis H and O sums
+        if (c->precision == GV_PREC_MIXED) b += W * N1 * Nexc * 8;   // tensor-core overlap rows
     }
     *bytes = b;
     return GV_OK;
@@ -917,7 +939,7 @@ gv_status gv_job_create(const gv_job_config* cfg, gv_job** out)
     d.nbr = nbr; d.edges = reinterpret_cast<const int4*>(edg); d.phase64 = p64; d.phase32 = p32; d.coef64 = c64; d.coef32 = c32;
     d.Ai[0] = a0; d.Ai[1] = a1;
     d.worb = nullptr; d.wslot = nullptr; d.exc_up = nullptr; d.exc_dn = nullptr; d.cur = nullptr; d.wsign = nullptr;
-    d.sigma = nullptr; d.gup = nullptr; d.gdn = nullptr; d.pjx = nullptr;
+    d.sigma = nullptr; d.gup = nullptr; d.gdn = nullptr; d.pjx = nullptr; d.zbuf = nullptr;
     if (j->trans) {
         const int Nexc = j->ch.Nexc;
         int16_t *eu = nullptr, *ed = nullptr;
@@ -931,6 +953,8 @@ gv_status gv_job_create(const gv_job_config* cfg, gv_job** out)
             (st = dalloc(j, &d.gup, size_t(j->W) * j->N[0] * Nexc * es)) ||
             (st = dalloc(j, &d.gdn, size_t(j->W) * j->Nmax * es)) ||
             (st = dalloc(j, &d.pjx, size_t(j->W) * 2 * Nexc * Nexc * sizeof(cx<double>))))
+            return fail(st);
+        if (trans_z_tc_ok(j) && (st = dalloc(j, &d.zbuf, size_t(j->W) * j->N[1] * Nexc * sizeof(cx<float>))))
             return fail(st);
         d.exc_up = eu; d.exc_dn = ed;
         if (cudaMemcpyAsync(eu, j->exu.data(), Nexc * sizeof(int16_t), cudaMemcpyHostToDevice, j->stream) ||

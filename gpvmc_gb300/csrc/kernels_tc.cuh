@@ -124,7 +124,9 @@ struct TcRegs {
     cx<float> ph[kTcItems][4];    // orbital operand: phase[site r][f]
 };
 
-__device__ __forceinline__ void tc_load_inverse(TcRegs& R, const cx<float>* Ai, int N, int rows, int kc)
+// Rows r < nr of a matrix stored K-major in memory, M[f][r] at M + f ld + r,
+// K values f < nk (zero elsewhere).
+__device__ __forceinline__ void tc_load_rows(TcRegs& R, const cx<float>* M, int ld, int nr, int nk, int rows, int kc)
 {
 #pragma unroll
     for (int i = 0; i < kTcItems; ++i) {
@@ -132,7 +134,28 @@ __device__ __forceinline__ void tc_load_inverse(TcRegs& R, const cx<float>* Ai, 
 #pragma unroll
         for (int t = 0; t < 4; ++t) {
             const int f = 32 * kc + 4 * u + t;
-            R.inv[i][t] = (it < rows * 8 && r < N && f < N) ? Ai[size_t(f) * N + r] : cx<float>{0.f, 0.f};
+            R.inv[i][t] = (it < rows * 8 && r < nr && f < nk) ? M[size_t(f) * ld + r] : cx<float>{0.f, 0.f};
+        }
+    }
+}
+
+__device__ __forceinline__ void tc_load_inverse(TcRegs& R, const cx<float>* Ai, int N, int rows, int kc)
+{
+    tc_load_rows(R, Ai, N, N, N, rows, kc);
+}
+
+// Phase values phase[site r][pcol[f]] of rows r < nr, K values f < nk.
+__device__ __forceinline__ void tc_load_phase_cols(TcRegs& R, const cx<float>* phase, int Nk, const int16_t* site,
+                                                   const int16_t* pcol, int nr, int nk, int rows, int kc)
+{
+#pragma unroll
+    for (int i = 0; i < kTcItems; ++i) {
+        const int it = threadIdx.x + kTcThreads * i, r = it % rows, u = it / rows;
+        const int s = (it < rows * 8 && r < nr) ? site[r] : -1;
+#pragma unroll
+        for (int t = 0; t < 4; ++t) {
+            const int f = 32 * kc + 4 * u + t;
+            R.ph[i][t] = (s >= 0 && f < nk) ? phase[size_t(s) * Nk + pcol[f]] : cx<float>{0.f, 0.f};
         }
     }
 }
@@ -201,6 +224,30 @@ __device__ __forceinline__ double f32_to_f64(float x)
     return __longlong_as_double(static_cast<long long>(d));
 }
 
+// Orbital operand with an explicit row -> coefficient table: row r, K value f
+// holds phase[site r][pcol f] coef[sub(site r) * cld + f] (rows r < nr, f < nk).
+__device__ __forceinline__ void tc_store_phi_cols(char* base, const size_t* tiles, int nt, const TcRegs& R,
+                                                  const cx<float>* coef, int cld, const int16_t* site, int nr, int nk,
+                                                  int L, int rows, int kc)
+{
+#pragma unroll
+    for (int i = 0; i < kTcItems; ++i) {
+        const int it = threadIdx.x + kTcThreads * i;
+        if (it >= rows * 8) break;
+        const int r = it % rows, u = it / rows;
+        const int sub = r < nr ? sublattice(site[r], L) : 0;
+        float re[4], im[4];
+#pragma unroll
+        for (int t = 0; t < 4; ++t) {
+            const int f = 32 * kc + 4 * u + t;
+            const cx<float> v = f < nk ? cmul_rn(R.ph[i][t], coef[sub * cld + f]) : cx<float>{0.f, 0.f};
+            re[t] = v.x;
+            im[t] = v.y;
+        }
+        tc_store_split(base, tiles, nt, sw128(r, u), re, im);
+    }
+}
+
 // Shared-memory matrix descriptor: start address, leading byte offset 16
 // (unused by swizzled K-major operands), stride byte offset 1024 (8-row
 // groups), descriptor version 1, base offset 0, 128-byte swizzle.
@@ -243,6 +290,15 @@ __device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity)
         if (done) return true;
     }
     return false;
+}
+
+__device__ __forceinline__ void tmem_wait_ld(uint32_t (&r)[32])
+{
+    asm volatile("tcgen05.wait::ld.sync.aligned;"
+                 : "+r"(r[0]), "+r"(r[1]), "+r"(r[2]), "+r"(r[3]), "+r"(r[4]), "+r"(r[5]), "+r"(r[6]), "+r"(r[7]),
+                   "+r"(r[8]), "+r"(r[9]), "+r"(r[10]), "+r"(r[11]), "+r"(r[12]), "+r"(r[13]), "+r"(r[14]), "+r"(r[15]),
+                   "+r"(r[16]), "+r"(r[17]), "+r"(r[18]), "+r"(r[19]), "+r"(r[20]), "+r"(r[21]), "+r"(r[22]), "+r"(r[23]),
+                   "+r"(r[24]), "+r"(r[25]), "+r"(r[26]), "+r"(r[27]), "+r"(r[28]), "+r"(r[29]), "+r"(r[30]), "+r"(r[31])::"memory");
 }
 
 __device__ __forceinline__ void tmem_ld16(uint32_t taddr, uint32_t* r)
@@ -445,6 +501,166 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_statspin_tc(DevJob J)
     __syncthreads();
     tmem_fence_after();
     if (warp == 0) tmem_dealloc(tbase, 512);
+}
+
+// ---- Exciton overlap rows on the tensor cores (mixed exciton channel) ----
+// The exciton ProjHeis needs, for every channel state k and every flavour-1
+// site d, Z[k][d] = sum_f GupT[f][k] phi_{worb0[f]}(d) (the R A^-1 C block of
+// linalg::DetUpdate for all states and all bond targets at once,
+// linalg.cpp:274-290): per walker an Nexc x N0 x N1 complex product.  Same
+// split-TF32 scheme and pipeline as k_statspin_tc: A = GupT^T (rows k, K = f),
+// B = Phi_0 at the flavour-1 sites (rows d), one accumulator pair in TMEM
+// (256 columns).  Output Z[w][d][k] (FP32, k fastest) for k_measure_trans.
+constexpr int kTcMaxK = 160;   // N0 <= 160 (five K chunks)
+
+__host__ __device__ inline TcLayout tc_layout_z(int N1)
+{
+    TcLayout l;
+    size_t o = 0;
+    const size_t at = size_t(kTcM) * 128, bt = size_t(tc_ncols(N1)) * 128;
+    for (int i = 0; i < 4; ++i) { l.a[i] = o; o += at; }
+    for (int i = 0; i < 6; ++i) { l.b[i] = o; o += bt; }
+    l.site = o;   // [buf][ flavour-1 sites (128) | phase column of row f (kTcMaxK) ]
+    o += sizeof(int16_t) * 2 * (kTcM + kTcMaxK);
+    l.coef = o;   // [buf][sub][f]
+    o += sizeof(cx<float>) * 2 * 2 * kTcMaxK;
+    l.bar = o;
+    o += 8;
+    l.tbase = o;
+    o += 8;
+    l.total = o + 1024;
+    return l;
+}
+
+__global__ void __launch_bounds__(kTcThreads, 1) k_trans_z_tc(DevJob J, cx<float>* Z)
+{
+    extern __shared__ __align__(16) char smem_raw[];
+    const uint32_t raw = smem_addr(smem_raw);
+    char* base = smem_raw + ((1024u - (raw & 1023u)) & 1023u);
+    const uint32_t sbase = smem_addr(base);
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int N0 = J.N[0], N1 = J.N[1], Nexc = J.Nexc, Nt = tc_ncols(N1), Ns = J.Ns, L = J.L, Nk = J.Nk;
+    const TcLayout lay = tc_layout_z(N1);
+    int16_t* s_tab = reinterpret_cast<int16_t*>(base + lay.site);
+    cx<float>* s_cf = reinterpret_cast<cx<float>*>(base + lay.coef);
+    uint64_t* s_bar = reinterpret_cast<uint64_t*>(base + lay.bar);
+    uint32_t* s_tbase = reinterpret_cast<uint32_t*>(base + lay.tbase);
+    const uint32_t bar = smem_addr(s_bar);
+
+    if (warp == 0) tmem_alloc(s_tbase, 256);
+    if (tid == 0) {
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(bar) : "memory");
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    tmem_fence_before();
+    __syncthreads();
+    tmem_fence_after();
+    const uint32_t tbase = *s_tbase;
+    const uint32_t idesc = tc_idesc(Nt);
+    const int KC = (N0 + 31) / 32;
+    uint32_t parity = 0;
+    bool failed = false;
+
+    auto tables = [&](int w, int b) {
+        int16_t* site = s_tab + b * (kTcM + kTcMaxK);
+        int16_t* pcol = site + kTcM;
+        cx<float>* cf = s_cf + b * 2 * kTcMaxK;
+        for (int d = tid; d < N1; d += kTcThreads) site[d] = J.part[(size_t(w) * 2 + 1) * J.Nmax + d];
+        const cx<float>* cg = J.coef32 + size_t(w) * 4 * Ns;   // flavour 0: [sub][orbital]
+        for (int i = tid; i < 2 * N0; i += kTcThreads) {
+            const int sub = i / N0, f = i % N0;
+            const int o = J.worb[size_t(w) * 2 * J.Nmax + f];
+            cf[sub * kTcMaxK + f] = cg[size_t(sub) * Ns + o];
+            if (!sub) pcol[f] = int16_t(o >> 1);
+        }
+    };
+    auto fetch = [&](TcRegs& R, int w, int b, int kc) {
+        const int16_t* site = s_tab + b * (kTcM + kTcMaxK);
+        const cx<float>* G = static_cast<const cx<float>*>(J.gup) + size_t(w) * N0 * Nexc;
+        tc_load_rows(R, G, Nexc, Nexc, N0, kTcM, kc);
+        tc_load_phase_cols(R, J.phase32, Nk, site, site + kTcM, N1, N0, Nt, kc);
+    };
+
+    int w = blockIdx.x < J.W ? int(blockIdx.x) : -1;
+    if (w >= 0 && J.status[w] != GV_OK) w = tc_next_walker(J, w);
+    TcRegs R;
+    int b = 0;
+    if (w >= 0) {
+        tables(w, 0);
+        __syncthreads();
+        fetch(R, w, 0, 0);
+    }
+    bool first = true;
+    while (w >= 0 && !failed) {
+        const int wn = tc_next_walker(J, w);
+        const int16_t* site = s_tab + b * (kTcM + kTcMaxK);
+        const cx<float>* cf = s_cf + b * 2 * kTcMaxK;
+        for (int kc = 0; kc < KC; ++kc) {
+            if (!first) {
+                const bool ok = mbar_wait(bar, parity);
+                if (__syncthreads_or(!ok)) { failed = true; break; }
+                parity ^= 1u;
+            }
+            first = false;
+            tc_store_inverse(base, lay.a, 4, R, kTcM);
+            tc_store_phi_cols(base, lay.b, 6, R, cf, kTcMaxK, site, N1, N0, L, Nt, kc);
+            asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+            tmem_fence_before();
+            __syncthreads();
+            if (tid == 0) {
+                tmem_fence_after();
+                tc_issue_chunk(tbase, 0u, sbase, lay, idesc, kc == 0);
+                tc_commit(bar);
+            }
+            if (kc + 1 < KC) {
+                fetch(R, w, b, kc + 1);
+            } else if (wn >= 0) {
+                tables(wn, b ^ 1);
+                __syncthreads();
+                fetch(R, wn, b ^ 1, 0);
+            }
+        }
+        if (failed) {
+            if (tid == 0) J.status[w] = GV_ERR_TIMEOUT;
+            break;
+        }
+        {
+            const bool ok = mbar_wait(bar, parity);
+            if (__syncthreads_or(!ok)) {
+                failed = true;
+                if (tid == 0) J.status[w] = GV_ERR_TIMEOUT;
+                break;
+            }
+            parity ^= 1u;
+        }
+        tmem_fence_after();
+        // epilogue: lane k of TMEM -> Z[w][d][k], 16 columns d at a time
+        const int lg = warp & 3, k = 32 * lg + lane;
+        for (int cc = warp >> 2; cc < Nt / 16; cc += 2) {
+            uint32_t r[32];
+            const uint32_t ta = tbase + (uint32_t(32 * lg) << 16) + uint32_t(16 * cc);
+            tmem_ld16(ta, r);
+            tmem_ld16(ta + 128, r + 16);
+            tmem_wait_ld(r);
+            if (k < Nexc) {
+#pragma unroll
+                for (int t = 0; t < 16; ++t) {
+                    const int d = 16 * cc + t;
+                    if (d < N1)
+                        Z[(size_t(w) * N1 + d) * Nexc + k] = cx<float>{__uint_as_float(r[t]), __uint_as_float(r[16 + t])};
+                }
+            }
+        }
+        tmem_fence_before();
+        first = true;
+        w = wn;
+        b ^= 1;
+    }
+    if (failed) mbar_wait(bar, parity);
+    tmem_fence_before();
+    __syncthreads();
+    tmem_fence_after();
+    if (warp == 0) tmem_dealloc(tbase, 256);
 }
 
 // Occupation bitsets of the walkers still running: bit w % 32 of word

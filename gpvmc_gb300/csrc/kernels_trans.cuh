@@ -625,7 +625,7 @@ __host__ __device__ inline MeasLayout meas_layout(int Ns, int Nmax, int Nexc)
 }
 
 template <typename T, int NT>
-__global__ void __launch_bounds__(NT) k_measure_trans(DevJob J, int mask)
+__global__ void __launch_bounds__(NT) k_measure_trans(DevJob J, int mask, const cx<float>* zpre)
 {
     extern __shared__ __align__(16) char smem[];
     constexpr int NW = NT / 32;
@@ -729,12 +729,14 @@ __global__ void __launch_bounds__(NT) k_measure_trans(DevJob J, int mask)
         }
         __syncthreads();
         // Pass 3: tiles of flavour-1 sites d (targets of the flavour-0 moves).
+        // With zpre (the tensor-core product, Z[w][d][k]) the tile's Z values are read.
         for (int t0 = 0; t0 < N1; t0 += TT) {
             const int nt = min(TT, N1 - t0);
-            for (int idx = tid; idx < nt * N0; idx += NT) {
-                const int tt = idx / N0, f = idx % N0;
-                s_Ct[tt * Nmax + f] = phi_orb<T>(phase, cf0, Nk, Ns, L, s_part[Nmax + t0 + tt], s_worb[f]);
-            }
+            if (!zpre)
+                for (int idx = tid; idx < nt * N0; idx += NT) {
+                    const int tt = idx / N0, f = idx % N0;
+                    s_Ct[tt * Nmax + f] = phi_orb<T>(phase, cf0, Nk, Ns, L, s_part[Nmax + t0 + tt], s_worb[f]);
+                }
             for (int idx = tid; idx < nt * Nexc; idx += NT) {
                 const int tt = idx / Nexc, k = idx % Nexc;
                 const int rk = s_wslot[Ns + s_exd[k]];   // -1 for k = cur (its hole is empty)
@@ -760,11 +762,20 @@ __global__ void __launch_bounds__(NT) k_measure_trans(DevJob J, int mask)
                 cx<T> Z[TT];
 #pragma unroll
                 for (int tt = 0; tt < TT; ++tt) Z[tt] = {T(0), T(0)};
-                for (int f = 0; f < N0; ++f) {
-                    const cx<T> gk = G[size_t(f) * Nexc + k];
+                if (zpre) {
 #pragma unroll
                     for (int tt = 0; tt < TT; ++tt)
-                        if (tt < nt) cmac(Z[tt], gk, s_Ct[tt * Nmax + f]);
+                        if (tt < nt) {
+                            const cx<float> z = zpre[(size_t(w) * N1 + t0 + tt) * Nexc + k];
+                            Z[tt] = cx<T>{T(z.x), T(z.y)};
+                        }
+                } else {
+                    for (int f = 0; f < N0; ++f) {
+                        const cx<T> gk = G[size_t(f) * Nexc + k];
+#pragma unroll
+                        for (int tt = 0; tt < TT; ++tt)
+                            if (tt < nt) cmac(Z[tt], gk, s_Ct[tt * Nmax + f]);
+                    }
                 }
                 const int rk = s_wslot[Ns + s_exd[k]];
                 cx<double> acc = s_S[k];

@@ -76,10 +76,11 @@ typedef int32_t gv_status;
                                      quantities) into a CUDA graph once and replay it: one
                                      launch per call instead of one per kernel (not while a
                                      job timer runs or a walk is traced) */
-#define GV_FLAG_SCALAR_PAIRS 16   /* mixed ground state: StatSpinStruct pair ratios from FP32
-                                     dot products on the CUDA cores instead of the
-                                     split-TF32 tensor-core G = Phi A^-1 products (the
-                                     tensor-core form runs by default when N_0 = N_1 <= 128) */
+#define GV_FLAG_SCALAR_PAIRS 16   /* mixed precision: StatSpinStruct pair ratios (ground state)
+                                     and the exciton ProjHeis overlap rows Z = GupT^T Phi from
+                                     FP32 dot products on the CUDA cores instead of split-TF32
+                                     tensor-core products (the tensor-core forms run by default
+                                     when N_0 = N_1 <= 128, resp. Nexc, N_1 <= 128, N_0 <= 160) */
 
 #define GV_MEAS_PROJHEIS 1    /* ProjHeis (ProjHeis.cpp:40-158), Bx = 0 */
 #define GV_MEAS_STAGMAGN 2    /* StagMagnZ (StagMagnZ.cpp:12-43) */

@@ -80,3 +80,32 @@ def test_tensor_core_pairs_inside_the_walk(engine, oracle):
     st, ss = st.reshape(5, L * L, L * L), ss.reshape(5, L * L, L * L)
     assert np.array_equal(st[0], ss[0])
     assert np.abs(st[1:3] - ss[1:3]).max() < 1e-5 * np.abs(ss[1:3]).max()
+
+
+@pytest.mark.parametrize("L,q", [(8, (4, 4)), (12, (2, 2)), (16, (4, 4))])
+def test_exciton_overlap_rows_on_tensor_cores(engine, oracle, L, q):
+    """Exciton ProjHeis with Z = GupT^T Phi_0 from split-TF32 tensor-core
+    products (k_trans_z_tc) against the FP32 CUDA-core product on the same
+    FP32 state (2e-5 of the largest H / O entry) and against the FP64 engine
+    on the same configurations (H and O do not depend on the current state)."""
+    W = 12
+    wav = engine.StagFluxTransExciton(L, PHI, 0.1, q=q)
+    mk = lambda prec, **kw: engine.Job(wav, walkers=W, seed=21, precision=prec, reinv_every=64,
+                                       deferred_reinversion=True, **kw)
+    j0 = mk("mixed")
+    j0.init_walkers()
+    j0.walk(L * L * 2, 0)
+    cfg = j0.config()
+    out = []
+    for j in (mk("mixed"), mk("mixed", scalar_pairs=True), mk("fp64")):
+        j.init_walkers(cfg)
+        j.set_measurements(oracle.MEAS_PROJHEIS)
+        j.reset_quantities()
+        j.measure()
+        pj, n = j.projheis()
+        assert (n == 1).all()
+        out.append(pj)
+    pt, ps, p64 = out
+    scale = np.abs(p64).max(axis=(1, 2), keepdims=True)
+    assert (np.abs(pt - ps) / scale).max() < 2e-5
+    assert (np.abs(pt - p64) / scale).max() < 1e-3
