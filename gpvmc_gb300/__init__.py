@@ -6,7 +6,7 @@ gpvmc_gb300.vmc for the reference-named API.
 """
 from ._lib import GvError, lib  # noqa: F401
 from .vmc import (Job, LatticeStepper, MetroMC, ProjHeis, SlaterDeterminant, SquareLattice,  # noqa: F401
-                  StagFluxGroundState, StagFluxTransExciton, StagMagnZ, StatSpinStruct, pi_phi)
+                  StagFluxGroundState, StagFluxTransExciton, StagMagnTrack, StagMagnZ, StatSpinStruct, OverlapTrack, pi_phi)
 from .serving import Server  # noqa: F401
 
 __version__ = "0.1.0"

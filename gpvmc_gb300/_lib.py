@@ -19,6 +19,7 @@ STATUS_NAMES = {0: "ok", 1: "invalid", 2: "singular", 3: "nan", 4: "zero amplitu
 GV_CH_GROUNDSTATE, GV_CH_TRANS = 0, 1
 GV_PREC_FP64, GV_PREC_MIXED = 0, 1
 GV_MEAS_PROJHEIS, GV_MEAS_STAGMAGN, GV_MEAS_STATSPIN = 1, 2, 4
+GV_MEAS_STAGMAGN_TRACK, GV_MEAS_OVERLAP_TRACK = 8, 16
 GV_FLAG_REINV_DEFERRED = 1
 GV_FLAG_REINV_ON_DRIFT = 2
 GV_FLAG_DELAYED_UPDATES = 4
@@ -97,6 +98,8 @@ _SIGS = {
     "gv_job_walk_continue": [_P, ctypes.c_uint64, ctypes.c_uint64],
     "gv_job_stream": [_P, ctypes.c_void_p],
     "gv_job_graph_stats": [_P, ctypes.POINTER(ctypes.c_int32), ctypes.POINTER(ctypes.c_int64)],
+    "gv_job_set_track_capacity": [_P, ctypes.c_int32],
+    "gv_job_read_tracks": [_P, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p],
     "gv_job_autotune": [_P, ctypes.c_uint64, ctypes.POINTER(ctypes.c_int32), ctypes.c_void_p],
     "gv_job_checkpoint_size": [_P, ctypes.c_int32, ctypes.POINTER(ctypes.c_uint64)],
     "gv_job_checkpoint": [_P, ctypes.c_int32, ctypes.c_void_p, ctypes.c_uint64, ctypes.POINTER(ctypes.c_uint64)],

@@ -165,6 +165,10 @@ struct DevJob {
                                // Aud (Ns*Ns real) in a 10*Ns*Ns-double buffer
     int32_t* ss_n;
     uint32_t* occ;             // 2*Ns*ceil(W/32) occupation bitsets (tensor-core StatSpinStruct)
+    double* track_sm;          // W*track_cap StagMagnTrack values
+    double* track_lw;          // W*track_cap OverlapTrack log10 weights
+    int32_t* track_n;          // W entries recorded
+    int track_cap;
     cx<double>* scratch64;     // per-CTA FP64 N*N scratch for re-inversion (W*Nmax*Nmax)
     gv_trace* trace;
     int trace_walker;

@@ -332,6 +332,22 @@ gv_status deferred_reinversion(gv_job* j)
     return j->cfg.precision == GV_PREC_FP64 ? launch_check<double, 256>(j, thr) : launch_check<float, 256>(j, thr);
 }
 
+constexpr int kTrackMask = GV_MEAS_STAGMAGN_TRACK | GV_MEAS_OVERLAP_TRACK;
+constexpr int kInnerMask = GV_MEAS_PROJHEIS | GV_MEAS_STAGMAGN;   // measured inside the walk / measure kernels
+
+gv_status tracks_dispatch(gv_job* j, int mask)
+{
+    if (!j->d.track_cap) return GV_OK;
+    int slot;
+    GV_CK(mark_begin(j, 2, &slot));
+    k_tracks<<<(j->W + 7) / 8, 256, 0, j->stream>>>(j->d, mask);
+    GV_CK(cudaGetLastError());
+    GV_CK(mark_end(j, slot));
+    ++j->last_launches;
+    ++j->total_launches;
+    return GV_OK;
+}
+
 // Tensor-core exciton overlap rows Z = GupT^T Phi_0: mixed exciton channel with
 // Nexc <= 128, N1 <= 128, N0 <= 160.
 bool trans_z_tc_ok(const gv_job* j)
@@ -940,6 +956,7 @@ gv_status gv_job_create(const gv_job_config* cfg, gv_job** out)
     d.Ai[0] = a0; d.Ai[1] = a1;
     d.worb = nullptr; d.wslot = nullptr; d.exc_up = nullptr; d.exc_dn = nullptr; d.cur = nullptr; d.wsign = nullptr;
     d.sigma = nullptr; d.gup = nullptr; d.gdn = nullptr; d.pjx = nullptr; d.zbuf = nullptr;
+    d.track_sm = nullptr; d.track_lw = nullptr; d.track_n = nullptr; d.track_cap = 0;
     if (j->trans) {
         const int Nexc = j->ch.Nexc;
         int16_t *eu = nullptr, *ed = nullptr;
@@ -979,6 +996,9 @@ gv_status gv_job_destroy(gv_job* j)
     if (j->stream) cudaStreamSynchronize(j->stream);
     for (auto& kv : j->graphs) cudaGraphExecDestroy(kv.second.exec);
     for (void* p : j->allocs) cudaFree(p);
+    cudaFree(j->d.track_sm);
+    cudaFree(j->d.track_lw);
+    cudaFree(j->d.track_n);
     if (j->ev0) cudaEventDestroy(j->ev0);
     for (cudaEvent_t e : j->ev_pool) cudaEventDestroy(e);
     if (j->tev0) cudaEventDestroy(j->tev0);
@@ -1001,7 +1021,7 @@ gv_status gv_job_dims(const gv_job* j, int32_t* Ns, int32_t* Nup, int32_t* Ndn, 
 
 gv_status gv_job_set_meas_mask(gv_job* j, int32_t mask)
 {
-    if (!j || (mask & ~(GV_MEAS_PROJHEIS | GV_MEAS_STAGMAGN | GV_MEAS_STATSPIN))) return GV_ERR_INVALID;
+    if (!j || (mask & ~(GV_MEAS_PROJHEIS | GV_MEAS_STAGMAGN | GV_MEAS_STATSPIN | kTrackMask))) return GV_ERR_INVALID;
     j->cfg.meas_mask = mask;
     return GV_OK;
 }
@@ -1016,6 +1036,7 @@ static gv_status reset_quantities(gv_job* j)
     GV_CK(cudaMemsetAsync(j->d.ss_n, 0, sizeof(int32_t), j->stream));
     if (j->trans)
         GV_CK(cudaMemsetAsync(j->d.pjx, 0, sizeof(cx<double>) * 2 * size_t(j->W) * j->ch.Nexc * j->ch.Nexc, j->stream));
+    if (j->d.track_n) GV_CK(cudaMemsetAsync(j->d.track_n, 0, sizeof(int32_t) * j->W, j->stream));
     return GV_OK;
 }
 
@@ -1031,10 +1052,11 @@ gv_status gv_job_measure(gv_job* j)
     if (!j->ready) return GV_ERR_NOT_READY;
     const int mask = j->cfg.meas_mask;
     gv_status st = GV_OK;
-    if (mask & (GV_MEAS_PROJHEIS | GV_MEAS_STAGMAGN))
-        st = j->trans ? measure_trans_dispatch(j, mask & ~GV_MEAS_STATSPIN)
-                      : walk_dispatch(j, 0, 0, 1, mask & ~GV_MEAS_STATSPIN, 1);
+    const int inner = mask & kInnerMask;
+    if (inner)
+        st = j->trans ? measure_trans_dispatch(j, inner) : walk_dispatch(j, 0, 0, 1, inner, 1);
     if (!st && (mask & GV_MEAS_STATSPIN)) st = statspin_dispatch(j);
+    if (!st && (mask & kTrackMask)) st = tracks_dispatch(j, mask);
     return st ? st : gv_job_synchronize(j);
 }
 
@@ -1123,8 +1145,8 @@ static gv_status enqueue_walk(gv_job* j, uint64_t len, uint64_t meas, int mask, 
         if (rs) return rs;
     }
     gv_status st = GV_OK;
-    const int inner = mask & ~GV_MEAS_STATSPIN;
-    if (!(mask & GV_MEAS_STATSPIN) && !(j->trans && mask)) {
+    const int inner = mask & kInnerMask;
+    if (!(mask & (GV_MEAS_STATSPIN | kTrackMask)) && !(j->trans && mask)) {
         st = j->trans ? walk_trans_dispatch(j, len) : walk_dispatch(j, len, 0, meas, mask);
     } else {
         // Split at the measurement points: steps [a, m] then measure after step m.
@@ -1146,6 +1168,7 @@ static gv_status enqueue_walk(gv_job* j, uint64_t len, uint64_t meas, int mask, 
                 st = walk_dispatch(j, nsteps, a, meas, inner);
             }
             if (!st && (mask & GV_MEAS_STATSPIN)) st = statspin_dispatch(j);
+            if (!st && (mask & kTrackMask)) st = tracks_dispatch(j, mask);
             a = m + 1;
         }
         j->d.trace = dtrace;
@@ -1655,6 +1678,51 @@ gv_status gv_job_autotune(gv_job* j, uint64_t steps, int32_t* choice, double* us
         g_tune_cache[key] = best;
     }
     if (choice) *choice = best;
+    return GV_OK;
+}
+
+gv_status gv_job_set_track_capacity(gv_job* j, int32_t capacity)
+{
+    if (!j || capacity < 0) return GV_ERR_INVALID;
+    GV_CK(cudaStreamSynchronize(j->stream));
+    for (auto& kv : j->graphs) cudaGraphExecDestroy(kv.second.exec);   // they hold the old buffers
+    j->graphs.clear();
+    cudaFree(j->d.track_sm);
+    cudaFree(j->d.track_lw);
+    cudaFree(j->d.track_n);
+    j->d.track_sm = j->d.track_lw = nullptr;
+    j->d.track_n = nullptr;
+    j->d.track_cap = 0;
+    if (!capacity) return GV_OK;
+    const size_t n = size_t(j->W) * capacity;
+    if (cudaMalloc(&j->d.track_sm, n * sizeof(double)) || cudaMalloc(&j->d.track_lw, n * sizeof(double)) ||
+        cudaMalloc(&j->d.track_n, sizeof(int32_t) * j->W)) {
+        cudaGetLastError();
+        cudaFree(j->d.track_sm);
+        cudaFree(j->d.track_lw);
+        cudaFree(j->d.track_n);
+        j->d.track_sm = j->d.track_lw = nullptr;
+        j->d.track_n = nullptr;
+        return GV_ERR_OOM;
+    }
+    GV_CK(cudaMemset(j->d.track_n, 0, sizeof(int32_t) * j->W));
+    j->d.track_cap = capacity;
+    return GV_OK;
+}
+
+gv_status gv_job_read_tracks(gv_job* j, double* stagmagn, double* log10_weight, int32_t* n)
+{
+    if (!j) return GV_ERR_INVALID;
+    GV_CK(cudaStreamSynchronize(j->stream));
+    const size_t m = size_t(j->W) * j->d.track_cap;
+    if (!j->d.track_cap) {
+        if (n)
+            for (int w = 0; w < j->W; ++w) n[w] = 0;
+        return GV_OK;
+    }
+    if (stagmagn) GV_CK(cudaMemcpy(stagmagn, j->d.track_sm, m * sizeof(double), cudaMemcpyDeviceToHost));
+    if (log10_weight) GV_CK(cudaMemcpy(log10_weight, j->d.track_lw, m * sizeof(double), cudaMemcpyDeviceToHost));
+    if (n) GV_CK(cudaMemcpy(n, j->d.track_n, sizeof(int32_t) * j->W, cudaMemcpyDeviceToHost));
     return GV_OK;
 }
 

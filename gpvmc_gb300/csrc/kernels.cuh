@@ -898,6 +898,40 @@ __global__ void __launch_bounds__(NT, 768 / NT) k_walk_gs(DevJob J, uint64_t nst
     }
 }
 
+// StagMagnTrack / OverlapTrack (StagMagnTrack.cpp:21-50; OverlapTrack.cpp:26-29):
+// one warp per walker appends the staggered magnetisation and log10 of the
+// stepper weight (|Amp|^2, times sigma = sum_k |q_k|^2 / |Amp|^2 in the
+// exciton channel) to the walker's tracks.
+__global__ void k_tracks(DevJob J, int mask)
+{
+    const int w = int(blockIdx.x) * (blockDim.x / 32) + int(threadIdx.x / 32), lane = threadIdx.x & 31;
+    if (w >= J.W || J.status[w] != GV_OK) return;
+    const int n = J.track_n[w];
+    if (n >= J.track_cap) return;
+    const size_t at = size_t(w) * J.track_cap + n;
+    if (mask & GV_MEAS_STAGMAGN_TRACK) {
+        const int16_t* fock = J.fock + size_t(w) * 2 * J.Ns;
+        int m = 0;
+        for (int v = lane; v < J.Ns; v += 32) {
+            const int sg = (((v % J.L) + (v / J.L)) & 1) ? -1 : 1;
+            m += sg * (fock[v] >= 0 ? 1 : -1);
+        }
+#pragma unroll
+        for (int o = 16; o; o >>= 1) m += __shfl_xor_sync(0xffffffffu, m, o);
+        if (lane == 0) J.track_sm[at] = double(m) / double(J.Ns);
+    }
+    if (lane == 0) {
+        if (mask & GV_MEAS_OVERLAP_TRACK) {
+            const cx<double> a = J.amp_m[w];
+            const double mag = hypot(a.x, a.y);
+            double lw = mag > 0.0 ? 2.0 * (log10(mag) + double(J.amp_e[w]) * 0.30102999566398119521) : -INFINITY;
+            if (J.channel == GV_CH_TRANS) lw += log10(J.sigma[w]);
+            J.track_lw[at] = lw;
+        }
+        J.track_n[w] = n + 1;
+    }
+}
+
 // Ratio of moving particle c of flavour fl to site d (one warp, lanes over
 // rows); row f's orbital has phase column pcol_fl[f] and coefficients
 // coef_fl[sub][f].

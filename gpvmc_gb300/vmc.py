@@ -185,6 +185,22 @@ class Job:
         times = {n: float(x) for n, x in zip(self.TUNE_VARIANTS, t) if x >= 0}
         return (self.TUNE_VARIANTS[c.value] if c.value >= 0 else None), times
 
+    track_capacity = 0
+
+    def set_track_capacity(self, capacity):
+        """Room for `capacity` track entries per walker (StagMagnTrack / OverlapTrack)."""
+        check(_lib.lib().gv_job_set_track_capacity(self._h, capacity), "gv_job_set_track_capacity")
+        self.track_capacity = capacity
+
+    def tracks(self):
+        """(stagmagn[W, cap], log10_weight[W, cap], n[W]) recorded since the last measuring walk."""
+        cap = max(self.track_capacity, 1)
+        sm = np.zeros(self.walkers * cap)
+        lw = np.zeros(self.walkers * cap)
+        n = np.zeros(self.walkers, dtype=np.int32)
+        check(_lib.lib().gv_job_read_tracks(self._h, _p(sm), _p(lw), _p(n)), "gv_job_read_tracks")
+        return sm.reshape(self.walkers, cap), lw.reshape(self.walkers, cap), n
+
     def graph_stats(self):
         """(graphs cached, replays) with cuda_graphs=True; cached = -1 if capture was refused."""
         c, r = ctypes.c_int32(), ctypes.c_int64()
@@ -442,6 +458,45 @@ class StatSpinStruct(Quantity):
         return v / max(n, 1)
 
 
+class StagMagnTrack(Quantity):
+    """StagMagnTrack (StagMagnTrack.cpp:21-50): the staggered magnetisation of
+    every measurement since the walk began, per walker (a list of arrays)."""
+
+    mask = _lib.GV_MEAS_STAGMAGN_TRACK
+
+    def _read(self):
+        sm, _, n = self.job.tracks()
+        return sm, n
+
+    def save(self):
+        sm, n = self._read()
+        return [sm[w, :n[w]] for w in range(len(n))]
+
+
+class OverlapTrack(Quantity):
+    """OverlapTrack (OverlapTrack.cpp:26-29): the stepper weight of every
+    measurement divided by their mean, per walker (as OverlapTrack::save)."""
+
+    mask = _lib.GV_MEAS_OVERLAP_TRACK
+
+    def _read(self):
+        _, lw, n = self.job.tracks()
+        return lw, n
+
+    def save(self):
+        lw, n = self._read()
+        out = []
+        for w in range(len(n)):
+            x = lw[w, :n[w]]
+            if len(x) == 0:
+                out.append(x)
+                continue
+            m = x.max()
+            rel = 10.0 ** (x - m)
+            out.append(rel / rel.mean())
+        return out
+
+
 class MetroMC:
     """MetroMC (MetroMC.h:11-45): Walk(len, meas), Rejection()."""
 
@@ -460,6 +515,11 @@ class MetroMC:
         return self.quantities
 
     def Walk(self, length, meas):
+        if meas and any(q.mask & (_lib.GV_MEAS_STAGMAGN_TRACK | _lib.GV_MEAS_OVERLAP_TRACK)
+                        for q in self.quantities):
+            need = -(-length // meas)   # measurements of this walk
+            if self.job.track_capacity < need:
+                self.job.set_track_capacity(need)
         self.job.walk(length, meas)
 
     def Rejection(self):

@@ -85,6 +85,10 @@ typedef int32_t gv_status;
 #define GV_MEAS_PROJHEIS 1    /* ProjHeis (ProjHeis.cpp:40-158), Bx = 0 */
 #define GV_MEAS_STAGMAGN 2    /* StagMagnZ (StagMagnZ.cpp:12-43) */
 #define GV_MEAS_STATSPIN 4    /* StatSpinStruct (StatSpinStruct.cpp:16-135) */
+#define GV_MEAS_STAGMAGN_TRACK 8   /* StagMagnTrack (StagMagnTrack.cpp:21-50): every measurement's
+                                      staggered magnetisation, in order (gv_job_read_tracks) */
+#define GV_MEAS_OVERLAP_TRACK 16   /* OverlapTrack (OverlapTrack.cpp:26-29): every measurement's
+                                      stepper weight, as log10 (gv_job_read_tracks) */
 
 typedef struct gv_job gv_job;
 
@@ -233,6 +237,19 @@ gv_status gv_job_read_weight(gv_job* job, double* sigma /* n_walkers */);
 gv_status gv_job_read_projheis(gv_job* job, double* vals, int32_t* nmeas);
 gv_status gv_job_read_stagmagn(gv_job* job, double* vals, int32_t* nmeas);
 gv_status gv_job_read_statspin(gv_job* job, double* vals, int32_t* nmeas);
+
+/* Track quantities (GV_MEAS_STAGMAGN_TRACK, GV_MEAS_OVERLAP_TRACK): room for
+ * `capacity` measurements per walker (allocated here; 0 frees it); the tracks
+ * restart with every measuring gv_job_walk (Quantity::init) and stop growing
+ * when full.  gv_job_read_tracks copies, per walker, the staggered
+ * magnetisation values stagmagn[w * capacity + i] (real; the reference's
+ * complex value has zero imaginary part), log10 of the stepper weight
+ * log10_weight[w * capacity + i] (|Amp|^2; exciton: sum_k |q_k|^2) -- the
+ * reference's OverlapTrack::save divides the weights by their mean -- and the
+ * number of entries n[w]; any pointer may be NULL.  Tracks are not part of a
+ * checkpoint. */
+gv_status gv_job_set_track_capacity(gv_job* job, int32_t capacity);
+gv_status gv_job_read_tracks(gv_job* job, double* stagmagn, double* log10_weight, int32_t* n);
 
 /* Checkpoint / resume.  The reference saves the final lattice Fock state
  * (State::Save, State.cpp:117-166) and resumes a chain from it with
