@@ -1041,7 +1041,7 @@ __device__ __forceinline__ void ff_cmac(cx<float>& s, cx<float>& c, cx<float> ah
 // is 1/64 of its FP32 rate).  Walkers above the threshold (or
 // all of them when threshold < 0) get the FP64 Gauss-Jordan re-inversion.
 template <typename T, int NT>
-__global__ void __launch_bounds__(NT) k_check_reinvert(DevJob J, double threshold)
+__global__ void __launch_bounds__(NT, 2) k_check_reinvert(DevJob J, double threshold)
 {
     extern __shared__ __align__(16) char smem[];
     constexpr int NR = 8;
@@ -1050,70 +1050,65 @@ __global__ void __launch_bounds__(NT) k_check_reinvert(DevJob J, double threshol
     if (w >= J.W || J.status[w] != GV_OK || J.reinv_every <= 0 || J.since_reinv[w] < J.reinv_every) return;
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const int Nmax = J.Nmax, Ns = J.Ns;
-    cx<double>* arow = reinterpret_cast<cx<double>*>(smem);             // NR * Nmax
-    double* red = reinterpret_cast<double*>(arow + NR * Nmax);          // NW
+    cx<double>* arow = reinterpret_cast<cx<double>*>(smem);             // 2 * NR * Nmax
+    double* red = reinterpret_cast<double*>(arow + 2 * NR * Nmax);      // NW
     char* gp = reinterpret_cast<char*>(red + NW + 2);
     gp = reinterpret_cast<char*>((reinterpret_cast<uintptr_t>(gp) + 15) & ~uintptr_t(15));
     double drift = 0.0;
     if (threshold >= 0.0) {
         const unsigned long long nchk = J.counts[size_t(w) * 5 + 4] + J.checks[w];
+        auto sampled = [&](int i, int N) { return int((nchk * NR + size_t(i) * (N / NR) + i) % N); };
+        // the sampled rows of A of both flavours, FP64
         for (int fl = 0; fl < 2; ++fl) {
             const int N = J.N[fl];
             const int16_t* part = J.part + (size_t(w) * 2 + fl) * Nmax;
             const cx<double>* coef = J.coef64 + (size_t(w) * 2 + fl) * 2 * Ns;
-            const cx<T>* A = ai_ptr<T>(J, fl, w);
-            int rows[NR];
-#pragma unroll
-            for (int i = 0; i < NR; ++i) rows[i] = int((nchk * NR + size_t(i) * (N / NR) + i) % N);
             for (int idx = tid; idx < NR * N; idx += NT) {
                 const int i = idx / N, p = idx % N;
                 const int site = part[p];
-                const int o = row_orbital(J, nullptr, w, fl, rows[i]);
+                const int o = row_orbital(J, nullptr, w, fl, sampled(i, N));
                 const cx<double> v = cmul_rn(J.phase64[size_t(site) * J.Nk + (o >> 1)],
                                              coef[size_t(sublattice(site, J.L)) * Ns + o]);
                 if constexpr (sizeof(T) == 4) {   // hi + lo floats, same bytes as one FP64 complex
-                    cx<float>* ahi = reinterpret_cast<cx<float>*>(arow);
+                    cx<float>* ahi = reinterpret_cast<cx<float>*>(arow + fl * NR * Nmax);
                     const cx<float> h = {float(v.x), float(v.y)};
                     ahi[i * Nmax + p] = h;
                     ahi[(NR + i) * Nmax + p] = cx<float>{float(v.x - double(h.x)), float(v.y - double(h.y))};
                 } else {
-                    arow[i * Nmax + p] = v;
+                    arow[(fl * NR + i) * Nmax + p] = v;
                 }
             }
-            __syncthreads();
-            if constexpr (sizeof(T) == 4) {
-                // FP32-stored inverse: the residual in double-float arithmetic on the
-                // FP32 pipe (A's FP64 entries split into hi + lo floats, exact
-                // products, compensated sums), FP64 only for the final lane sums
-                const cx<float>* ahi = reinterpret_cast<const cx<float>*>(arow);
+        }
+        __syncthreads();
+        if constexpr (sizeof(T) == 4) {
+            // FP32-stored inverse: the residual (A A^-1)(i, g) = sum_p A(i, p) AiT[g][p]
+            // in double-float arithmetic on the FP32 pipe (A's FP64 entries split into
+            // hi + lo floats, exact products, compensated sums), one thread per row g
+            // of AiT of either flavour, so that no lane sums are needed
+            for (int idx = tid; idx < J.N[0] + J.N[1]; idx += NT) {
+                const int fl = idx < J.N[0] ? 0 : 1, g = fl ? idx - J.N[0] : idx, N = J.N[fl];
+                const cx<float>* ahi = reinterpret_cast<const cx<float>*>(arow + fl * NR * Nmax);
                 const cx<float>* alo = ahi + NR * Nmax;
-                for (int g = warp; g < N; g += NW) {
-                    cx<float> sm[NR], cm[NR];
+                const cx<float>* Ag = reinterpret_cast<const cx<float>*>(ai_ptr<T>(J, fl, w)) + size_t(g) * N;
+                cx<float> sm[NR], cm[NR];
 #pragma unroll
-                    for (int i = 0; i < NR; ++i) { sm[i] = {0.f, 0.f}; cm[i] = {0.f, 0.f}; }
-                    for (int p = lane; p < N; p += 32) {
-                        const cx<float> x = reinterpret_cast<const cx<float>*>(A)[size_t(g) * N + p];
+                for (int i = 0; i < NR; ++i) { sm[i] = {0.f, 0.f}; cm[i] = {0.f, 0.f}; }
+                for (int p = 0; p < N; ++p) {
+                    const cx<float> x = Ag[p];
 #pragma unroll
-                        for (int i = 0; i < NR; ++i) ff_cmac(sm[i], cm[i], ahi[i * Nmax + p], alo[i * Nmax + p], x);
-                    }
-#pragma unroll
-                    for (int i = 0; i < NR; ++i) {
-                        // lane sums in double-float too; FP64 only for the final value
-#pragma unroll
-                        for (int o = 16; o; o >>= 1) {
-                            ff_add(sm[i].x, cm[i].x, __shfl_xor_sync(0xffffffffu, sm[i].x, o),
-                                   __shfl_xor_sync(0xffffffffu, cm[i].x, o));
-                            ff_add(sm[i].y, cm[i].y, __shfl_xor_sync(0xffffffffu, sm[i].y, o),
-                                   __shfl_xor_sync(0xffffffffu, cm[i].y, o));
-                        }
-                        if (lane == 0) {
-                            cx<double> v = {double(sm[i].x) + double(cm[i].x), double(sm[i].y) + double(cm[i].y)};
-                            if (rows[i] == g) v.x -= 1.0;
-                            drift = fmax(drift, fmax(fabs(v.x), fabs(v.y)));
-                        }
-                    }
+                    for (int i = 0; i < NR; ++i) ff_cmac(sm[i], cm[i], ahi[i * Nmax + p], alo[i * Nmax + p], x);
                 }
-            } else {
+#pragma unroll
+                for (int i = 0; i < NR; ++i) {
+                    cx<double> v = {double(sm[i].x) + double(cm[i].x), double(sm[i].y) + double(cm[i].y)};
+                    if (sampled(i, N) == g) v.x -= 1.0;
+                    drift = fmax(drift, fmax(fabs(v.x), fabs(v.y)));
+                }
+            }
+        } else {
+            for (int fl = 0; fl < 2; ++fl) {
+                const int N = J.N[fl];
+                const cx<T>* A = ai_ptr<T>(J, fl, w);
                 for (int g = warp; g < N; g += NW) {
                     cx<double> acc[NR];
 #pragma unroll
@@ -1121,17 +1116,16 @@ __global__ void __launch_bounds__(NT) k_check_reinvert(DevJob J, double threshol
                     for (int p = lane; p < N; p += 32) {
                         const cx<double> x = to_d(A[size_t(g) * N + p]);
 #pragma unroll
-                        for (int i = 0; i < NR; ++i) cmac(acc[i], arow[i * Nmax + p], x);
+                        for (int i = 0; i < NR; ++i) cmac(acc[i], arow[(fl * NR + i) * Nmax + p], x);
                     }
 #pragma unroll
                     for (int i = 0; i < NR; ++i) {
                         cx<double> v = warp_sum(acc[i]);
-                        if (rows[i] == g) v.x -= 1.0;
+                        if (sampled(i, N) == g) v.x -= 1.0;
                         drift = fmax(drift, fmax(fabs(v.x), fabs(v.y)));
                     }
                 }
             }
-            __syncthreads();
         }
 #pragma unroll
         for (int o = 16; o; o >>= 1) drift = fmax(drift, __shfl_xor_sync(0xffffffffu, drift, o));
@@ -1159,7 +1153,7 @@ __global__ void __launch_bounds__(NT) k_check_reinvert(DevJob J, double threshol
 
 __host__ __device__ inline size_t check_smem_bytes(int Nmax, int NT)
 {
-    return sizeof(cx<double>) * 8 * Nmax + sizeof(double) * (NT / 32 + 2) + 16 + gj_smem_bytes(Nmax, NT) + 16;
+    return sizeof(cx<double>) * 2 * 8 * Nmax + sizeof(double) * (NT / 32 + 2) + 16 + gj_smem_bytes(Nmax, NT) + 16;
 }
 
 // VirtUpdate-style ratios for explicit hop sets of one walker.
