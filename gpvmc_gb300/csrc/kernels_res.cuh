@@ -135,6 +135,29 @@ __device__ __forceinline__ cx<float> warp_transpose_sum(const cx<float> (&v)[32]
     return a + b;
 }
 
+// v[0..31] per lane -> lane l returns the sum over the warp's lanes of v[l]:
+// a butterfly reduce-scatter in registers (at the step with offset o each
+// lane keeps the half of its o-wide block that its lane bit selects, sends
+// the other half to lane ^ o and adds what it receives): 31 complex shuffles
+// per lane, no shared memory.
+__device__ __forceinline__ cx<float> warp_reduce_scatter(cx<float> (&v)[32])
+{
+    const int lane = threadIdx.x & 31;
+#pragma unroll
+    for (int o = 16; o; o >>= 1) {
+        const bool hi = (lane & o) != 0;
+#pragma unroll
+        for (int t = 0; t < o; ++t) {
+            const cx<float> keep = hi ? v[o + t] : v[t];
+            cx<float> send = hi ? v[t] : v[o + t];
+            send.x = __shfl_xor_sync(0xffffffffu, send.x, o);
+            send.y = __shfl_xor_sync(0xffffffffu, send.y, o);
+            v[t] = keep + send;
+        }
+    }
+    return v[0];
+}
+
 __global__ void __launch_bounds__(kResThreads, 1) k_walk_gs_res(DevJob J, uint64_t nsteps, uint64_t s0, uint64_t meas,
                                                                 int mask)
 {
@@ -341,7 +364,7 @@ __global__ void __launch_bounds__(kResThreads, 1) k_walk_gs_res(DevJob J, uint64
                         cx<T> v[32];
 #pragma unroll
                         for (int j = 0; j < 32; ++j) v[j] = cx<T>{__uint_as_float(r[2 * j]), __uint_as_float(r[2 * j + 1])} * u;
-                        wpart[32 * c + lane] = warp_transpose_sum(v, s_tile);
+                        wpart[32 * c + lane] = warp_reduce_scatter(v);
                     }
                     wg_sync(g);
                     if (f < 32 * NCH) {   // w_p - [p == c]
