@@ -66,6 +66,11 @@ __device__ __forceinline__ void tmem_wait_ld(uint32_t (&r)[4])
 {
     asm volatile("tcgen05.wait::ld.sync.aligned;" : "+r"(r[0]), "+r"(r[1]), "+r"(r[2]), "+r"(r[3])::"memory");
 }
+__device__ __forceinline__ void tmem_wait_ld(uint32_t (&r)[6])
+{
+    asm volatile("tcgen05.wait::ld.sync.aligned;"
+                 : "+r"(r[0]), "+r"(r[1]), "+r"(r[2]), "+r"(r[3]), "+r"(r[4]), "+r"(r[5])::"memory");
+}
 __device__ __forceinline__ void tmem_wait_ld(uint32_t (&r)[8])
 {
     asm volatile("tcgen05.wait::ld.sync.aligned;"
