@@ -90,7 +90,7 @@ constexpr int kResRngBatch = 32;
 constexpr int kResSpec = 2;                       // proposals evaluated per barrier
 
 struct ResLayout {
-    size_t fock, part, nbr, sub, coef, red, wpart, w, tile, rv, ru4, ru4d, racc, rq, rqp, nb, redm, tbase, total, used;
+    size_t fock, part, nbr, sub, coef, red, wpart, w, rv, ru4, ru4d, racc, rq, rqp, nb, redm, tbase, total, used;
 };
 
 __host__ __device__ inline ResLayout res_layout(int Ns, int N, bool projheis)
@@ -107,7 +107,6 @@ __host__ __device__ inline ResLayout res_layout(int Ns, int N, bool projheis)
     l.red = al(sizeof(float) * 2 * 16 * kResSpec);
     l.wpart = al(c * 2 * 4 * 128);
     l.w = al(c * 2 * 128);
-    l.tile = al(c * (kResThreads / 32) * 32 * 33);   // per warp 32 x 32 products, row stride 33
     l.rv = al(sizeof(int16_t) * 2 * kResRngBatch);
     l.ru4 = al(sizeof(float) * kResRngBatch);
     l.ru4d = al(sizeof(double) * kResRngBatch);
@@ -120,24 +119,6 @@ __host__ __device__ inline ResLayout res_layout(int Ns, int N, bool projheis)
     l.used = al(16);
     l.total = l.used < kResMinSmem ? kResMinSmem : l.used;
     return l;
-}
-
-// v[0..31] per lane -> lane l returns the sum over the warp's lanes of v[l],
-// through this warp's 32 x 33 shared-memory tile (conflict-free both ways).
-__device__ __forceinline__ cx<float> warp_transpose_sum(const cx<float> (&v)[32], cx<float>* tile)
-{
-    const int lane = threadIdx.x & 31;
-#pragma unroll
-    for (int j = 0; j < 32; ++j) tile[lane * 33 + j] = v[j];
-    __syncwarp();
-    cx<float> a = {0.f, 0.f}, b = {0.f, 0.f};
-#pragma unroll
-    for (int i = 0; i < 32; i += 2) {
-        a = a + tile[i * 33 + lane];
-        b = b + tile[(i + 1) * 33 + lane];
-    }
-    __syncwarp();
-    return a + b;
 }
 
 // v[0..31] per lane -> lane l returns the sum over the warp's lanes of v[l]:
@@ -182,7 +163,6 @@ __global__ void __launch_bounds__(kResThreads, 1) k_walk_gs_res(DevJob J, uint64
     T* s_red = reinterpret_cast<T*>(smem + lay.red);
     cx<T>* s_wpart = reinterpret_cast<cx<T>*>(smem + lay.wpart);   // [g][warp][p]
     cx<T>* s_w = reinterpret_cast<cx<T>*>(smem + lay.w);           // [g][p]
-    cx<T>* s_tile = reinterpret_cast<cx<T>*>(smem + lay.tile) + warp * 32 * 33;
     int16_t* s_rv = reinterpret_cast<int16_t*>(smem + lay.rv);     // [step][v1, v2]
     float* s_ru4 = reinterpret_cast<float*>(smem + lay.ru4);
     double* s_ru4d = reinterpret_cast<double*>(smem + lay.ru4d);
@@ -428,7 +408,8 @@ __global__ void __launch_bounds__(kResThreads, 1) k_walk_gs_res(DevJob J, uint64
                 // ProjHeis pass 1 from TMEM: the ratio of moving particle p of flavour g to
                 // neighbour slot kk is sum_f (A^-1)(p, f) phi_{2f}(j); lane f forms its
                 // terms for 32 particles at a time (phase[j][f] is coalesced over the lanes)
-                // and the warp transposes-and-sums them; the four warps meet in shared memory.
+                // and the warp reduce-scatters them over its lanes; the four warps meet in
+                // shared memory.
                 cx<T>* part_g = s_rqp + (g * 4 + (warp & 3)) * 4 * 128;
                 int16_t* nb_g = s_nb + g * 4 * 128;
                 {
@@ -460,7 +441,7 @@ __global__ void __launch_bounds__(kResThreads, 1) k_walk_gs_res(DevJob J, uint64
                                 v[j] = a * cmul_rn(v[j], cf[s_sub[jsv[j]] * N + f]);
                             }
                         }
-                        part_g[kk * 128 + 32 * c + lane] = warp_transpose_sum(v, s_tile);
+                        part_g[kk * 128 + 32 * c + lane] = warp_reduce_scatter(v);
                     }
                 }
                 wg_sync(g);
