@@ -113,7 +113,7 @@ __host__ __device__ inline ResLayout res_layout(int Ns, int N, bool projheis)
     l.racc = al(sizeof(cx<float>) * 2 * kResRngBatch);   // accepted ratio pairs of the batch
     l.rq = al(projheis ? c * 4 * Ns : 16);
     l.rqp = al(projheis ? c * 2 * 4 * 4 * 128 : 16);   // [g][warp][slot][p] partial bond ratios
-    l.nb = al(projheis ? sizeof(int16_t) * 2 * 4 * 128 : 16);   // [g][slot][p] antiparallel neighbour or -1
+    l.nb = al(projheis ? sizeof(int32_t) * 2 * 4 * 128 : 16);   // [g][bond] particle, slot and site
     l.redm = al(sizeof(double) * 4 * (kResThreads / 32));
     l.tbase = al(sizeof(uint32_t));
     l.used = al(16);
@@ -169,7 +169,7 @@ __global__ void __launch_bounds__(kResThreads, 1) k_walk_gs_res(DevJob J, uint64
     cx<T>* s_racc = reinterpret_cast<cx<T>*>(smem + lay.racc);
     cx<T>* s_rq = reinterpret_cast<cx<T>*>(smem + lay.rq);
     cx<T>* s_rqp = reinterpret_cast<cx<T>*>(smem + lay.rqp);
-    int16_t* s_nb = reinterpret_cast<int16_t*>(smem + lay.nb);
+    int32_t* s_nb = reinterpret_cast<int32_t*>(smem + lay.nb);
     double* s_redm = reinterpret_cast<double*>(smem + lay.redm);
     uint32_t* s_tbase = reinterpret_cast<uint32_t*>(smem + lay.tbase);
 
@@ -405,53 +405,62 @@ __global__ void __launch_bounds__(kResThreads, 1) k_walk_gs_res(DevJob J, uint64
         if (measuring && uint64_t(done) == to_meas + 1) {   // the round ended on a measuring step
             to_meas = meas - 1;
             if (mask & GV_MEAS_PROJHEIS) {
-                // ProjHeis pass 1 from TMEM: the ratio of moving particle p of flavour g to
-                // neighbour slot kk is sum_f (A^-1)(p, f) phi_{2f}(j); lane f forms its
-                // terms for 32 particles at a time (phase[j][f] is coalesced over the lanes)
-                // and the warp reduce-scatters them over its lanes; the four warps meet in
-                // shared memory.
+                // ProjHeis pass 1 from TMEM: the ratio of moving particle p of flavour g
+                // to a neighbouring site j of the other flavour is
+                // sum_f (A^-1)(p, f) phi_{2f}(j).  The bonds are listed by site j (the
+                // four neighbours of each other-flavour particle q, entry 4 q + d), so
+                // that one phase row phase[j][f] (coalesced over the lanes f) serves
+                // the four bonds of j; lane f gathers (A^-1)(p, f) of each bond's
+                // particle from its TMEM row (2-column loads), and each warp
+                // reduce-scatters 32 bonds at a time over its lanes; the four warps'
+                // partial sums meet in shared memory.
+                int32_t* tab = s_nb + g * 4 * 128;   // p | kk << 8 | i << 10, or -1
                 cx<T>* part_g = s_rqp + (g * 4 + (warp & 3)) * 4 * 128;
-                int16_t* nb_g = s_nb + g * 4 * 128;
+                const int NE = 4 * N;
+                for (int e = f; e < NE; e += 128) {
+                    const int js = s_part[(1 - g) * N + (e >> 2)];
+                    const int i = s_nbr[js * 4 + (e & 3)];
+                    const int pi = g ? s_fock[Ns + i] : s_fock[i];   // flavour-g particle at i, or -1
+                    int kk = 0;
+                    while (kk < 3 && s_nbr[i * 4 + kk] != js) ++kk;
+                    tab[e] = pi >= 0 ? (pi | (kk << 8) | (i << 10)) : -1;
+                }
+                wg_sync(g);
+                for (int e0 = 0; e0 < NE; e0 += 32) {
+                    uint32_t rr[64];
+                    int ent[32];
+#pragma unroll
+                    for (int t = 0; t < 32; ++t) {
+                        ent[t] = e0 + t < NE ? tab[e0 + t] : -1;
+                        uint32_t r2[2] = {0u, 0u};
+                        if (ent[t] >= 0) tmem_ld2(trow + 2 * (ent[t] & 0xFF), r2);
+                        rr[2 * t] = r2[0];
+                        rr[2 * t + 1] = r2[1];
+                    }
+                    cx<T> phk[8];
+#pragma unroll
+                    for (int k = 0; k < 8; ++k) {   // the eight sites of this group of 32 bonds
+                        const int q = (e0 >> 2) + k;
+                        phk[k] = cx<T>{0.f, 0.f};
+                        if (q < N && f < N) {
+                            const int js = s_part[(1 - g) * N + q];
+                            phk[k] = cmul_rn(phase[size_t(js) * Nk + f], cf[s_sub[js] * N + f]);
+                        }
+                    }
+                    tmem_wait_ld(rr);
+                    cx<T> v[32];
+#pragma unroll
+                    for (int t = 0; t < 32; ++t)
+                        v[t] = ent[t] >= 0 ? cx<T>{__uint_as_float(rr[2 * t]), __uint_as_float(rr[2 * t + 1])} * phk[t >> 2]
+                                           : cx<T>{0.f, 0.f};
+                    part_g[e0 + lane] = warp_reduce_scatter(v);
+                }
+                wg_sync(g);
                 {
-                    const bool ok = f < N;
-                    const int site = ok ? s_part[g * N + f] : 0;
-#pragma unroll
-                    for (int kk = 0; kk < 4; ++kk) {
-                        const int js = s_nbr[site * 4 + kk];
-                        nb_g[kk * 128 + f] = (ok && ((s_fock[js] >= 0) != (g == 0))) ? int16_t(js) : int16_t(-1);
-                    }
-                }
-                wg_sync(g);
-                for (int c = 0; c < NCH; ++c) {
-                    uint32_t r[64];
-                    tmem_ld64(trow + 64 * c, r);
-                    tmem_wait_ld(r);
-                    for (int kk = 0; kk < 4; ++kk) {
-                        cx<T> v[32];
-                        int jsv[32];
-#pragma unroll
-                        for (int j = 0; j < 32; ++j) {   // every load of the chunk in flight at once
-                            jsv[j] = nb_g[kk * 128 + 32 * c + j];
-                            v[j] = (jsv[j] >= 0 && f < N) ? phase[size_t(jsv[j]) * Nk + f] : cx<T>{0.f, 0.f};
-                        }
-#pragma unroll
-                        for (int j = 0; j < 32; ++j) {
-                            if (jsv[j] >= 0 && f < N) {
-                                const cx<T> a = {__uint_as_float(r[2 * j]), __uint_as_float(r[2 * j + 1])};
-                                v[j] = a * cmul_rn(v[j], cf[s_sub[jsv[j]] * N + f]);
-                            }
-                        }
-                        part_g[kk * 128 + 32 * c + lane] = warp_reduce_scatter(v);
-                    }
-                }
-                wg_sync(g);
-                if (f < N) {
                     const cx<T>* q = s_rqp + g * 4 * 4 * 128;
-                    const int site = s_part[g * N + f];
-#pragma unroll
-                    for (int kk = 0; kk < 4; ++kk) {
-                        const int i = kk * 128 + f;
-                        s_rq[site * 4 + kk] = q[i] + q[512 + i] + q[1024 + i] + q[1536 + i];
+                    for (int e = f; e < NE; e += 128) {
+                        const int en = tab[e];
+                        if (en >= 0) s_rq[(en >> 10) * 4 + ((en >> 8) & 3)] = q[e] + q[512 + e] + q[1024 + e] + q[1536 + e];
                     }
                 }
                 __syncthreads();
