@@ -426,6 +426,16 @@ __global__ void __launch_bounds__(kResThreads, 1) k_walk_gs_res(DevJob J, uint64
                     tab[e] = pi >= 0 ? (pi | (kk << 8) | (i << 10)) : -1;
                 }
                 wg_sync(g);
+                // phase rows of the eight sites of a group of 32 bonds, fetched one group ahead
+                auto fetch_rows = [&](int e0, cx<T> (&ph)[8]) {
+#pragma unroll
+                    for (int k = 0; k < 8; ++k) {
+                        const int q = (e0 >> 2) + k;
+                        ph[k] = (q < N && f < N) ? phase[size_t(s_part[(1 - g) * N + q]) * Nk + f] : cx<T>{0.f, 0.f};
+                    }
+                };
+                cx<T> phn[8];
+                fetch_rows(0, phn);
                 for (int e0 = 0; e0 < NE; e0 += 32) {
                     uint32_t rr[64];
                     int ent[32];
@@ -439,13 +449,12 @@ __global__ void __launch_bounds__(kResThreads, 1) k_walk_gs_res(DevJob J, uint64
                     }
                     cx<T> phk[8];
 #pragma unroll
+                    for (int k = 0; k < 8; ++k) phk[k] = phn[k];
+                    if (e0 + 32 < NE) fetch_rows(e0 + 32, phn);
+#pragma unroll
                     for (int k = 0; k < 8; ++k) {   // the eight sites of this group of 32 bonds
                         const int q = (e0 >> 2) + k;
-                        phk[k] = cx<T>{0.f, 0.f};
-                        if (q < N && f < N) {
-                            const int js = s_part[(1 - g) * N + q];
-                            phk[k] = cmul_rn(phase[size_t(js) * Nk + f], cf[s_sub[js] * N + f]);
-                        }
+                        if (q < N && f < N) phk[k] = cmul_rn(phk[k], cf[s_sub[s_part[(1 - g) * N + q]] * N + f]);
                     }
                     tmem_wait_ld(rr);
                     cx<T> v[32];
