@@ -233,6 +233,10 @@ __global__ void __launch_bounds__(kResThreads, 1) k_walk_gs_res(DevJob J, uint64
     // the first accepted move, whose update invalidates the rest (they are
     // evaluated again, from the new inverse, in the next round).  A round
     // never crosses a uniform batch or a measurement step.
+    // phase rows of both sites of the next round's proposals, fetched during the
+    // current round (whichever site a proposal's particle moves to, its row is there)
+    cx<T> pf[kResSpec][2];
+    int pf_bi = -1;   // first proposal index of the prefetched rows, -1: none
     const bool measuring = meas != 0 && mask != 0;
     // steps from s to the next measuring step (0: s itself is measured)
     uint64_t to_meas = measuring ? (meas == 1 ? 0 : (meas - (s0 % meas)) % meas) : ~uint64_t(0);
@@ -294,8 +298,24 @@ __global__ void __launch_bounds__(kResThreads, 1) k_walk_gs_res(DevJob J, uint64
                     tmem_ld2(trow + 2 * cg, r2);
                     rr[2 * i] = r2[0];
                     rr[2 * i + 1] = r2[1];
-                    if (f < N) pu[i] = cmul_rn(phase[size_t(tg) * Nk + f], cf[s_sub[tg] * N + f]);
+                    if (f < N) {
+                        const cx<T> ph = pf_bi == bi0 ? (tg == v1 ? pf[i][0] : pf[i][1]) : phase[size_t(tg) * Nk + f];
+                        pu[i] = cmul_rn(ph, cf[s_sub[tg] * N + f]);
+                    }
                 }
+            }
+        }
+        {   // the next round's rows, assuming it starts right after this one
+            const int nb0 = bi0 + kb;
+            pf_bi = -1;
+            if (nb0 < kResRngBatch && s + uint64_t(kb) < nsteps) {
+#pragma unroll
+                for (int i = 0; i < kResSpec; ++i)
+                    if (nb0 + i < kResRngBatch && s + uint64_t(kb + i) < nsteps && f < N) {
+                        pf[i][0] = phase[size_t(s_rv[2 * (nb0 + i)]) * Nk + f];
+                        pf[i][1] = phase[size_t(s_rv[2 * (nb0 + i) + 1]) * Nk + f];
+                    }
+                pf_bi = nb0;
             }
         }
         tmem_wait_ld(rr);
