@@ -684,7 +684,7 @@ def main():
                         # DRAM bytes per walk launch from one ncu capture of the same kernel at
                         # 304 walkers (profiles/), scaled by walkers: each walker's inverses are
                         # loaded and stored once per launch
-                        "traffic": (108.2e6 * WALKERS / 304) if resident else None,
+                        "traffic": (108.8e6 * WALKERS / 304) if resident else None,
                         "kernel": "k_walk_gs_res" if resident else "k_walk_gs", "bytes_per_step": bytes_step,
                         "bytes_per_step_meaning": "HBM bytes the streaming formulation of a Metropolis step moves "
                                                   "(inverse rows and columns, accepted-move read-modify-write)",
