@@ -565,40 +565,44 @@ struct Pending {
 template <typename T, int NT, int KD>
 __device__ __forceinline__ void flush_pending(Pending<T, KD>& P, cx<T>* A0, cx<T>* A1, int N0, int N1, int Nmax)
 {
-    if (KD == 0 || P.n == 0) return;
-    for (int fl = 0; fl < 2; ++fl) {
-        const int N = fl ? N1 : N0;
-        cx<T>* A = fl ? A1 : A0;
-        const cx<T>* rr = P.rr + size_t(fl) * KD * Nmax;
-        const cx<T>* wv = P.w + size_t(fl) * KD * Nmax;
-        for (int p = threadIdx.x; p < N; p += NT) {
-            cx<T> w[KD > 0 ? KD : 1];
+    if constexpr (KD == 0) {
+        return;
+    } else {
+        if (P.n == 0) return;
+        for (int fl = 0; fl < 2; ++fl) {
+            const int N = fl ? N1 : N0;
+            cx<T>* A = fl ? A1 : A0;
+            const cx<T>* rr = P.rr + size_t(fl) * KD * Nmax;
+            const cx<T>* wv = P.w + size_t(fl) * KD * Nmax;
+            for (int p = threadIdx.x; p < N; p += NT) {
+                cx<T> w[KD > 0 ? KD : 1];
 #pragma unroll
-            for (int j = 0; j < KD; ++j) w[j] = j < P.n ? cx<T>{-wv[j * Nmax + p].x, -wv[j * Nmax + p].y} : cx<T>{T(0), T(0)};
-            int f = 0;
-            for (; f + 8 <= N; f += 8) {
-                cx<T> a[8];
+                for (int j = 0; j < KD; ++j) w[j] = j < P.n ? cx<T>{-wv[j * Nmax + p].x, -wv[j * Nmax + p].y} : cx<T>{T(0), T(0)};
+                int f = 0;
+                for (; f + 8 <= N; f += 8) {
+                    cx<T> a[8];
 #pragma unroll
-                for (int q = 0; q < 8; ++q) a[q] = A[size_t(f + q) * N + p];
+                    for (int q = 0; q < 8; ++q) a[q] = A[size_t(f + q) * N + p];
 #pragma unroll
-                for (int q = 0; q < 8; ++q) {
+                    for (int q = 0; q < 8; ++q) {
+#pragma unroll
+                        for (int j = 0; j < KD; ++j)
+                            if (j < P.n) cmac(a[q], w[j], rr[j * Nmax + f + q]);   // rows past n are not written yet
+                        A[size_t(f + q) * N + p] = a[q];
+                    }
+                }
+                for (; f < N; ++f) {
+                    cx<T> a = A[size_t(f) * N + p];
 #pragma unroll
                     for (int j = 0; j < KD; ++j)
-                        if (j < P.n) cmac(a[q], w[j], rr[j * Nmax + f + q]);   // rows past n are not written yet
-                    A[size_t(f + q) * N + p] = a[q];
+                        if (j < P.n) cmac(a, w[j], rr[j * Nmax + f]);
+                    A[size_t(f) * N + p] = a;
                 }
             }
-            for (; f < N; ++f) {
-                cx<T> a = A[size_t(f) * N + p];
-#pragma unroll
-                for (int j = 0; j < KD; ++j)
-                    if (j < P.n) cmac(a, w[j], rr[j * Nmax + f]);
-                A[size_t(f) * N + p] = a;
-            }
         }
+        P.n = 0;
+        __syncthreads();
     }
-    P.n = 0;
-    __syncthreads();
 }
 
 
