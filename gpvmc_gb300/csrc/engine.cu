@@ -26,6 +26,7 @@
 #include "kernels_trans.cuh"
 #include "kernels_res.cuh"
 #include "kernels_tc.cuh"
+#include "kernels_trans_res.cuh"
 #include "model.hpp"
 
 using namespace gv;
@@ -432,8 +433,34 @@ gv_status launch_walk_trans(gv_job* j, uint64_t nsteps)
     return GV_OK;
 }
 
+// On-chip exciton walk (GupT and the flavour-1 inverse in TMEM, the flavour-0
+// inverse in shared memory): mixed, Nexc <= 128, deferred re-inversion.
+bool trans_resident_ok(const gv_job* j, uint64_t nsteps)
+{
+    const int f = j->cfg.flags;
+    return nsteps > 0 && j->trans && j->cfg.precision == GV_PREC_MIXED &&
+           trans_res_fits(j->N[0], j->N[1], j->ch.Nexc) && (f & GV_FLAG_REINV_DEFERRED) &&
+           !(f & GV_FLAG_STREAM_INVERSES);
+}
+
+gv_status launch_walk_trans_res(gv_job* j, uint64_t nsteps)
+{
+    const TrResLayout lay = trans_res_layout(j->Ns, j->Nmax, j->N[0], j->ch.Nexc);
+    GV_CK(raise_smem_limit(k_walk_trans_res, lay.total));
+    GV_CK(cudaFuncSetAttribute(k_walk_trans_res, cudaFuncAttributePreferredSharedMemoryCarveout, 100));
+    int slot;
+    GV_CK(mark_begin(j, 0, &slot));
+    k_walk_trans_res<<<j->W, kTrThreads, lay.total, j->stream>>>(j->d, nsteps);
+    GV_CK(cudaGetLastError());
+    GV_CK(mark_end(j, slot));
+    ++j->last_launches;
+    ++j->total_launches;
+    return GV_OK;
+}
+
 gv_status walk_trans_dispatch(gv_job* j, uint64_t nsteps)
 {
+    if (trans_resident_ok(j, nsteps)) return launch_walk_trans_res(j, nsteps);
     return j->cfg.precision == GV_PREC_FP64 ? launch_walk_trans<double>(j, nsteps) : launch_walk_trans<float>(j, nsteps);
 }
 
