@@ -33,6 +33,23 @@ __host__ __device__ inline bool trans_res_fits(int N0, int N1, int Nexc)
     return Nexc <= 128 && N1 <= 127 && N0 <= 129;
 }
 
+// Column p of AiT0 in shared memory: sum_f AiT0[f][p] v[f], four independent
+// accumulators (short dependency chains), 8 loads in flight.
+__device__ __forceinline__ cx<float> smem_col_dot(const cx<float>* A, int N, int p, const cx<float>* v)
+{
+    cx<float> acc[4] = {{0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}};
+    int f = 0;
+    for (; f + 8 <= N; f += 8) {
+        cx<float> a[8];
+#pragma unroll
+        for (int k = 0; k < 8; ++k) a[k] = A[size_t(f + k) * N + p];
+#pragma unroll
+        for (int k = 0; k < 8; ++k) cmac(acc[k & 3], a[k], v[f + k]);
+    }
+    for (; f < N; ++f) cmac(acc[0], A[size_t(f) * N + p], v[f]);
+    return (acc[0] + acc[1]) + (acc[2] + acc[3]);
+}
+
 struct TrResLayout {
     size_t a0, g128, fock, part, wslot, worb, nbr, exu, exd, coef, C, rowc, g, Y, zp, phk, ru, rd, dk, ak, bk, X, Yv, zc,
         hrow, wpart, wa, red, tbase, total, used;
@@ -142,6 +159,7 @@ __global__ void __launch_bounds__(kTrThreads, 1) k_walk_trans_res(DevJob J, uint
     for (int i = tid; i < N1; i += NT) s_g[i] = gglob[i];
     if (N0 > 128)
         for (int k = tid; k < Nexc; k += NT) s_g128[k] = G[size_t(128) * Nexc + k];
+    for (int i = tid; i < 128; i += NT) s_hrow[i] = cx<T>{T(0), T(0)};   // read (times 0) before a first row change
     tmem_fence_before();
     __syncthreads();
     tmem_fence_after();
@@ -269,16 +287,19 @@ __global__ void __launch_bounds__(kTrThreads, 1) k_walk_trans_res(DevJob J, uint
             // Phase 2: Z_k = sum_f GupT[f][k] C0[f] along lane k's TMEM row; the
             // other warpgroup meanwhile forms phi_{exc_up[k]}(t).
             if (g == 0) {
-                cx<T> acc = {T(0), T(0)};
+                cx<T> a4[4] = {{T(0), T(0)}, {T(0), T(0)}, {T(0), T(0)}, {T(0), T(0)}};
                 for (int c = 0; c < 4; ++c) {
                     uint32_t r[64];
                     tmem_ld64(tl + 64 * c, r);
                     tmem_wait_ld(r);
+                    const cx<T>* cc = s_C + 32 * c;
+                    const bool full = 32 * c + 32 <= N0;   // whole chunk inside the matrix (uniform)
 #pragma unroll
                     for (int j = 0; j < 32; ++j)
-                        if (32 * c + j < N0)
-                            cmac(acc, cx<T>{__uint_as_float(r[2 * j]), __uint_as_float(r[2 * j + 1])}, s_C[32 * c + j]);
+                        if (full || 32 * c + j < N0)
+                            cmac(a4[j & 3], cx<T>{__uint_as_float(r[2 * j]), __uint_as_float(r[2 * j + 1])}, cc[j]);
                 }
+                cx<T> acc = (a4[0] + a4[1]) + (a4[2] + a4[3]);
                 if (N0 > 128 && lf < Nexc) cmac(acc, s_g128[lf], s_C[128]);
                 if (lf < Nexc) s_zp[lf] = acc;
             } else if (lf < Nexc) {
@@ -426,11 +447,28 @@ __global__ void __launch_bounds__(kTrThreads, 1) k_walk_trans_res(DevJob J, uint
                 __syncthreads();
                 // Stage 3: rank-2 updates.  AiT0 in shared memory, one column per
                 // thread: its entry in row r0 before the update, (A^-1 C)_p - [p == c].
-                for (int p = tid; p < N0; p += NT) {
-                    const cx<T> h = row ? A0s[size_t(r0) * N0 + p] : cx<T>{T(0), T(0)};
-                    cx<T> wa = col_dot<T>(A0s, N0, p, s_C);
-                    if (p == cu) wa.x -= T(1);
-                    col_update2<T>(A0s, N0, p, wa, s_X, h, s_Yv, row);
+                if (g == 0) {
+                    const int p = tid;
+                    if (p < N0) {
+                        const cx<T> h = row ? A0s[size_t(r0) * N0 + p] : cx<T>{T(0), T(0)};
+                        cx<T> wa = smem_col_dot(A0s, N0, p, s_C);
+                        if (p == cu) wa.x -= T(1);
+                        col_update2<T>(A0s, N0, p, wa, s_X, h, s_Yv, row);
+                    }
+                } else if (N0 > 128 && warp == 5) {
+                    // column 128 by one warp of the other warpgroup: rows split over lanes
+                    const cx<T> h = row ? A0s[size_t(r0) * N0 + 128] : cx<T>{T(0), T(0)};
+                    cx<T> wa = {T(0), T(0)};
+                    for (int f = lane; f < N0; f += 32) cmac(wa, A0s[size_t(f) * N0 + 128], s_C[f]);
+                    wa = warp_sum(wa);   // every lane has read its rows before any lane writes
+                    if (cu == 128) wa.x -= T(1);
+                    const cx<T> na = cneg(wa), nb = cneg(h);
+                    for (int f = lane; f < N0; f += 32) {
+                        cx<T> a = A0s[size_t(f) * N0 + 128];
+                        cmac(a, na, s_X[f]);
+                        if (row) cmac(a, nb, s_Yv[f]);
+                        A0s[size_t(f) * N0 + 128] = a;
+                    }
                 }
                 if (g) {
                     // AiT1 in TMEM: (A^-1 C1)_p summed over the lanes f (butterfly per
@@ -459,13 +497,14 @@ __global__ void __launch_bounds__(kTrThreads, 1) k_walk_trans_res(DevJob J, uint
                         uint32_t r[64];
                         tmem_ld64(tl + kA1Col + 64 * c, r);
                         tmem_wait_ld(r);
+                        const bool full = 32 * c + 32 <= N1;
 #pragma unroll
                         for (int j = 0; j < 32; ++j) {
                             const int p = 32 * c + j;
-                            if (p < N1) {
+                            if (full || p < N1) {
                                 cx<T> e = {__uint_as_float(r[2 * j]), __uint_as_float(r[2 * j + 1])};
                                 cmac(e, s_wa[p], nx);
-                                if (row) cmac(e, s_hrow[p], ny);
+                                cmac(e, s_hrow[p], ny);   // ny = 0 without a row change
                                 r[2 * j] = __float_as_uint(e.x);
                                 r[2 * j + 1] = __float_as_uint(e.y);
                             }
@@ -478,18 +517,20 @@ __global__ void __launch_bounds__(kTrThreads, 1) k_walk_trans_res(DevJob J, uint
                     const cx<T> dk = ok ? s_dk[lf] : cx<T>{T(0), T(0)};
                     const cx<T> na = ok ? cneg(s_ak[lf]) : cx<T>{T(0), T(0)};
                     const cx<T> nb = (ok && row) ? cneg(s_bk[lf]) : cx<T>{T(0), T(0)};
+                    // lanes past Nexc have zero coefficients and are never read
                     for (int c = 0; c < 4; ++c) {
                         uint32_t r[64];
                         tmem_ld64(tl + 64 * c, r);
                         tmem_wait_ld(r);
+                        const bool full = 32 * c + 32 <= N0;
 #pragma unroll
                         for (int j = 0; j < 32; ++j) {
                             const int f = 32 * c + j;
-                            if (ok && f < N0) {
+                            if (full || f < N0) {
                                 cx<T> v = {__uint_as_float(r[2 * j]), __uint_as_float(r[2 * j + 1])};
                                 cmac(v, dk, s_rowc[f]);
                                 cmac(v, na, s_X[f]);
-                                if (row) cmac(v, nb, s_Yv[f]);
+                                cmac(v, nb, s_Yv[f]);   // nb = 0 without a row change
                                 r[2 * j] = __float_as_uint(v.x);
                                 r[2 * j + 1] = __float_as_uint(v.y);
                             }
