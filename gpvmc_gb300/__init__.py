@@ -8,5 +8,6 @@ from ._lib import GvError, lib  # noqa: F401
 from .vmc import (Job, LatticeStepper, MetroMC, ProjHeis, SlaterDeterminant, SquareLattice,  # noqa: F401
                   StagFluxGroundState, StagFluxTransExciton, StagMagnTrack, StagMagnZ, StatSpinStruct, OverlapTrack, pi_phi)
 from .serving import Server  # noqa: F401
+from .output import FileManager, convert_tree, save_quantities, write_wavefunction  # noqa: F401
 
 __version__ = "0.1.0"

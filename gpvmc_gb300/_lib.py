@@ -126,6 +126,7 @@ _SIGS = {
                           ctypes.c_void_p],
     "gv_channel_orbitals": [ctypes.c_int32, ctypes.c_void_p, ctypes.c_int32, ctypes.c_void_p, ctypes.c_int32,
                             ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p],
+    "gv_fock_quantum_numbers": [ctypes.c_int32, ctypes.c_void_p, ctypes.c_void_p],
 }
 # exported names that take no status-returning signature above
 EXTRA_SYMBOLS = ["gv_version", "gv_status_string", "gv_philox4x32_10", "gv_uniform_at"]

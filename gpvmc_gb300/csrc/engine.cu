@@ -807,6 +807,21 @@ gv_status gv_channel_states(int32_t L, const double* bc, int32_t channel, const 
     return GV_OK;
 }
 
+gv_status gv_fock_quantum_numbers(int32_t L, const double* bc, int32_t* out)
+{
+    if (L < 2 || L > 64 || (L % 2) || !bc || !out) return GV_ERR_INVALID;
+    Orbitals o = make_orbitals(L, bc[0], bc[1]);
+    if (!o.ok) return GV_ERR_INVALID;
+    for (int i = 0; i < o.Nk; ++i)
+        for (int band = 0; band < 2; ++band) {
+            const int f = 2 * i + band;   // fock index: MBZ point i, band
+            out[3 * f] = o.kx[i];
+            out[3 * f + 1] = o.ky[i];
+            out[3 * f + 2] = band;
+        }
+    return GV_OK;
+}
+
 void gv_philox4x32_10(const uint32_t* c, const uint32_t* k, uint32_t* out)
 {
     philox4x32_10(c[0], c[1], c[2], c[3], k[0], k[1], out);

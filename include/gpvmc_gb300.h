@@ -316,6 +316,11 @@ gv_status gv_channel_orbitals(int32_t L, const double* phase_shift, int32_t chan
  * 0 and removes orbital exc_dn[k] from flavour 1 (Nexc entries each). */
 gv_status gv_channel_states(int32_t L, const double* phase_shift, int32_t channel, const int32_t* q,
                             int32_t* exc_up, int32_t* exc_dn);
+/* gv_fock_quantum_numbers: out[3*f + 0..2] = (kx, ky, band) of every fock
+ * orbital f < L*L, the integer labels StagFluxWaveFunction::quantum_numbers
+ * reports (StagFluxWaveFunction.cpp:81-87) and WaveFunction::Save writes as
+ * the states file's attributes (WaveFunction.cpp:85-137). */
+gv_status gv_fock_quantum_numbers(int32_t L, const double* phase_shift, int32_t* out);
 void gv_philox4x32_10(const uint32_t* ctr, const uint32_t* key, uint32_t* out);
 double gv_uniform_at(uint64_t seed, uint32_t walker, uint32_t stream, uint64_t k);
 
