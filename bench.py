@@ -96,8 +96,10 @@ def cpu_baseline(cores, sweeps):
 # GPU side
 
 class Clocks:
-    """nvidia-smi samples during the timed region."""
-    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+    """nvidia-smi samples (every 20 ms) kept when their timestamp falls inside
+    the timed region [t0, t1] (time.time()); the sampler is started before the
+    warm-up so that its own start-up does not eat the region."""
+    Q = ("timestamp,index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
          "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
          "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
 
@@ -108,10 +110,16 @@ class Clocks:
     def __enter__(self):
         try:
             self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.Q,
-                                          "--format=csv,noheader,nounits", "-lms", "50"],
+                                          "--format=csv,noheader,nounits", "-lms", "20"],
                                          stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
         except OSError:
             self.proc = None
+        self.first = ""
+        if self.proc:   # wait (3 s at most) until the sampler is producing
+            import select
+            r, _, _ = select.select([self.proc.stdout], [], [], 3.0)
+            if r:
+                self.first = self.proc.stdout.readline()
         return self
 
     def __exit__(self, *a):
@@ -122,26 +130,38 @@ class Clocks:
             except subprocess.TimeoutExpired:
                 self.proc.kill()
                 self.out, _ = self.proc.communicate()
+            self.out = self.first + (self.out or "")
 
-    def summary(self):
+    @staticmethod
+    def _epoch(ts):
+        try:
+            base, _, frac = ts.partition(".")
+            return time.mktime(time.strptime(base, "%Y/%m/%d %H:%M:%S")) + (float("0." + frac) if frac else 0.0)
+        except ValueError:
+            return None
+
+    def summary(self, t0=None, t1=None):
         if not self.proc:
             return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
         sm, mx, reasons = [], [], set()
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
         for line in (self.out or "").strip().splitlines():
             f = [x.strip() for x in line.split(",")]
-            if len(f) < 9:
+            if len(f) < 10:
+                continue
+            t = self._epoch(f[0])
+            if t0 is not None and t is not None and not (t0 - 0.01 <= t <= t1 + 0.01):
                 continue
             try:
-                sm.append(float(f[1]))
-                mx.append(float(f[2]))
+                sm.append(float(f[2]))
+                mx.append(float(f[3]))
             except ValueError:
                 continue
-            for n, v in zip(names, f[5:9]):
+            for n, v in zip(names, f[6:10]):
                 if v.lower().startswith("active"):
                     reasons.add(n)
         return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
-                "samples": len(sm), "reasons": sorted(reasons)}
+                "samples": len(sm), "reasons": sorted(reasons), "interval_ms": 20}
 
 
 def measured_peaks():
@@ -188,6 +208,9 @@ def delta_e(g, job, rank):
 def run_gpu(g, precision, steps, warmup, rank, clocks_index=None, policy="drift", check_delta=False):
     job = make_job(g, precision, rank, policy)
     job.init_walkers()
+    clk = Clocks(clocks_index) if clocks_index is not None else None
+    if clk:
+        clk.__enter__()
     for _ in range(THERM_SWEEPS):
         job.walk(SWEEP, 0, sync=False)
     for _ in range(warmup):
@@ -195,10 +218,8 @@ def run_gpu(g, precision, steps, warmup, rank, clocks_index=None, policy="drift"
     job.synchronize()
     c0 = job.counts().sum(axis=0)
     lat = []
-    clk = Clocks(clocks_index) if clocks_index is not None else None
-    if clk:
-        clk.__enter__()
     job.timer_start()
+    e0 = time.time()
     t0 = time.perf_counter()
     for _ in range(steps):
         t = time.perf_counter()
@@ -206,6 +227,7 @@ def run_gpu(g, precision, steps, warmup, rank, clocks_index=None, policy="drift"
         lat.append(t)
     ms, launches = job.timer_stop()
     wall = time.perf_counter() - t0
+    e1 = time.time()
     walk_ms, walk_n = job.kernel_ms(0)
     inv_ms, inv_n = job.kernel_ms(1)
     import numpy as np
@@ -224,7 +246,7 @@ def run_gpu(g, precision, steps, warmup, rank, clocks_index=None, policy="drift"
            "sweep_p99_ms": float(np.percentile(sweep_each, 99)) if len(sweep_each) else None,
            "checks_without_reinversion": int(nchecks.sum()), "max_drift_at_check": float(drift_seen.max()),
            "p_acc": d[1] / d[0], "p_ap": (d[1] + d[3]) / d[0], "reinv": float(d[4]), "e_site": e_site,
-           "clocks": clk.summary() if clk else None}
+           "clocks": clk.summary(e0, e1) if clk else None}
     if check_delta:
         res["delta_e_site"] = delta_e(g, job, rank)
     job.close()
@@ -588,7 +610,7 @@ def main():
     global WALKERS
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--steps", type=int, default=40)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
