@@ -278,6 +278,68 @@ def run_e2e(g, precision, steps, rank):
 
 
 # ---------------------------------------------------------------------------
+# Batched FP64 vs FP32 Sherman-Morrison at L=12: 4096 walkers, phi = 0.25 pi,
+# neel = 0.05, FP64 re-inversion every 64 accepted moves, ProjHeis every sweep.
+
+C2_L, C2_WALKERS, C2_NEEL, C2_REINV = 12, 4096, 0.05, 64
+
+
+def run_config2(g, sweeps=8):
+    """Both precisions on the same seeds (kernel time between CUDA events):
+    the plain FP64 engine without re-inversion, as the reference runs, and the
+    mixed form with the specified cadence (FP64 re-inversion every 64 accepted
+    moves) and with the drift-checked policy (every 64 accepted moves the
+    residual is estimated and the walker re-inverted only above 1e-5); the
+    mixed jobs' ||A A^-1 - I||_max at the end of the timed walk and their
+    E/site against an FP64 job started on the same configurations."""
+    import numpy as np
+    sweep = C2_L * C2_L
+    out = {"workload": "staggered-flux ground state L=12 (72x72 complex per spin), phi=0.25pi, neel=0.05, "
+                       "4096 walkers, ProjHeis every sweep, FP64 re-inversion every 64 accepted moves",
+           "unit": "steps/s", "sweeps": sweeps}
+    wav = g.StagFluxGroundState(C2_L, 0.25 * math.pi, C2_NEEL)
+    for key, prec, thr in (("mixed", "mixed", None), ("mixed_drift_checked", "mixed", DRIFT_THRESHOLD),
+                           ("fp64", "fp64", None)):
+        # the plain FP64 engine, as the headline's: no re-inversion (the reference never re-inverts)
+        job = g.Job(wav, walkers=C2_WALKERS, seed=SEED, precision=prec, reinv_every=C2_REINV if prec == "mixed" else 0,
+                    deferred_reinversion=True, drift_threshold=thr)
+        job.set_measurements(1)
+        job.init_walkers()
+        for _ in range(4):
+            job.walk(sweep, 0, sync=False)
+        job.synchronize()
+        c0 = job.counts().sum(axis=0)
+        job.timer_start()
+        for _ in range(sweeps):
+            job.walk(sweep, sweep, sync=False)
+        ms, _ = job.timer_stop()
+        wk, _ = job.kernel_ms(0)
+        rk, _ = job.kernel_ms(1)
+        d = (job.counts().sum(axis=0) - c0).astype(float)
+        out[key] = {"value": C2_WALKERS * sweep * sweeps / (ms * 1e-3), "ms_per_sweep": ms / sweeps,
+                    "walk_ms_per_sweep": wk / sweeps, "reinversion_ms_per_sweep": rk / sweeps,
+                    "reinversions_per_walker_sweep": d[4] / (C2_WALKERS * sweeps), "p_acc": d[1] / d[0]}
+        if prec == "mixed":
+            out[key]["inverse_residual_max"] = float(job.drift().max())
+            cfg = job.config()
+            job.reset_quantities()
+            job.measure()
+            pm, nm = job.projheis()
+            ref = g.Job(wav, walkers=C2_WALKERS, seed=SEED, precision="fp64")
+            ref.set_measurements(1)
+            ref.init_walkers(cfg)
+            ref.measure()
+            pr, nr = ref.projheis()
+            ref.close()
+            dd = np.abs(pm[:, 0].real / np.maximum(nm, 1) - pr[:, 0].real / np.maximum(nr, 1))
+            out[key]["delta_e_site_vs_fp64"] = {"max": float(dd.max()), "mean": float(dd.mean())}
+        job.close()
+    out["mixed_over_fp64"] = out["mixed"]["value"] / out["fp64"]["value"]
+    out["mixed_drift_checked_over_fp64"] = out["mixed_drift_checked"]["value"] / out["fp64"]["value"]
+    return out
+
+
+# ---------------------------------------------------------------------------
 # Exciton channel: transverse exciton L=16, q = (n, n) for n = 0..7, 512 walkers
 # per momentum (N0 = 129, N1 = 127, Nexc = 128), ProjHeis H / O every sweep.
 
@@ -621,7 +683,8 @@ def main():
     ap.add_argument("--walkers", type=int, default=WALKERS, help="walkers (profiling a smaller case)")
     ap.add_argument("--no-exciton", action="store_true", help="skip the exciton-channel section")
     ap.add_argument("--no-serving", action="store_true", help="skip the serving-stream section")
-    ap.add_argument("--no-pairs", action="store_true", help="skip the StatSpinStruct tensor-core section")
+    ap.add_argument("--no-pairs", action="store_true",
+                    help="skip the StatSpinStruct tensor-core, graphs, autotune and L=12 sections")
     args = ap.parse_args()
 
     rank = int(os.environ.get("RANK", "0"))
@@ -687,6 +750,7 @@ def main():
                   "reinversion_policy": "FP64 re-inversion every 128 accepted exchanges", "steps": k}
 
     exc = run_exciton(g, 4, 1) if (rank == 0 and not args.no_exciton) else None
+    c2 = run_config2(g) if (rank == 0 and not args.no_pairs) else None
     serving = run_serving(g) if (rank == 0 and world == 1 and not args.no_serving) else None
     pairs = run_pairs(g, WALKERS) if (rank == 0 and not args.no_pairs) else None
     graphs = run_graphs(g) if (rank == 0 and not args.no_pairs) else None
@@ -757,6 +821,8 @@ def main():
         out["cuda_graphs"] = graphs
     if tune:
         out["autotune"] = tune
+    if c2:
+        out["l12_batched"] = c2
     print(json.dumps(out))
 
 
