@@ -313,11 +313,16 @@ gv_status walk_dispatch(gv_job* j, uint64_t nsteps, uint64_t s0, uint64_t meas, 
 template <typename T, int NT>
 gv_status launch_check(gv_job* j, double threshold)
 {
-    const size_t sm = check_smem_bytes(j->Nmax, NT) + 64;
+    size_t sm = check_smem_bytes(j->Nmax, NT) + 64;
+    // Gauss-Jordan matrix in shared memory: always while two CTAs still fit per
+    // SM, and for the outright cadence (every due walker re-inverted) while it fits at all
+    const size_t msz = sizeof(cx<double>) * size_t(j->Nmax) * j->Nmax;
+    const int m_in_smem = (sm + msz <= size_t(113) * 1024 || (threshold < 0.0 && sm + msz <= size_t(200) * 1024)) ? 1 : 0;
+    if (m_in_smem) sm += msz;
     GV_CK(raise_smem_limit(k_check_reinvert<T, NT>, sm));
     int slot;
     GV_CK(mark_begin(j, 1, &slot));
-    k_check_reinvert<T, NT><<<j->W, NT, sm, j->stream>>>(j->d, threshold);
+    k_check_reinvert<T, NT><<<j->W, NT, sm, j->stream>>>(j->d, threshold, m_in_smem);
     GV_CK(cudaGetLastError());
     GV_CK(mark_end(j, slot));
     ++j->last_launches;
@@ -400,10 +405,13 @@ template <typename T, int NT>
 gv_status launch_invert(gv_job* j, int only_due)
 {
     size_t sm = gj_smem_bytes(j->Nmax, NT) + 64;
+    const size_t msz = sizeof(cx<double>) * size_t(j->Nmax) * j->Nmax;
+    const int m_in_smem = (sm + msz <= size_t(200) * 1024) ? 1 : 0;   // N <= 112
+    if (m_in_smem) sm += msz;
     GV_CK(raise_smem_limit(k_invert<T, NT>, sm));
     int slot;
     GV_CK(mark_begin(j, 1, &slot));
-    k_invert<T, NT><<<j->W, NT, sm, j->stream>>>(j->d, only_due);
+    k_invert<T, NT><<<j->W, NT, sm, j->stream>>>(j->d, only_due, m_in_smem);
     GV_CK(cudaGetLastError());
     GV_CK(mark_end(j, slot));
     ++j->total_launches;

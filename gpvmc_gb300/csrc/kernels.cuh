@@ -281,8 +281,11 @@ __device__ __noinline__ void trans_rebuild(const DevJob& J, int w, const int16_t
 
 // Initial inversion / re-inversion of every walker (only_due: only walkers
 // whose accepted-move count reached reinv_every, the deferred cadence).
+// m_in_smem: the Gauss-Jordan working matrix in shared memory (the launch
+// provides Nmax^2 complex FP64 after the GJ scratch) instead of the global
+// scratch, for matrices that fit: the N pivot passes then never leave the SM.
 template <typename T, int NT>
-__global__ void __launch_bounds__(NT) k_invert(DevJob J, int only_due)
+__global__ void __launch_bounds__(NT) k_invert(DevJob J, int only_due, int m_in_smem)
 {
     extern __shared__ __align__(16) char smem[];
     const int w = blockIdx.x;
@@ -292,7 +295,7 @@ __global__ void __launch_bounds__(NT) k_invert(DevJob J, int only_due)
     }
     char* p = smem;
     GJSmem S = carve_gj<NT>(p, J.Nmax);
-    cx<double>* M = J.scratch64 + size_t(w) * J.Nmax * J.Nmax;
+    cx<double>* M = m_in_smem ? reinterpret_cast<cx<double>*>(p) : J.scratch64 + size_t(w) * J.Nmax * J.Nmax;
     const int st = reinvert_walker<T, NT>(J, w, M, S, nullptr);
     if (J.channel == GV_CH_TRANS && st == GV_OK) trans_rebuild<T, NT>(J, w, nullptr, J.cur[w]);
     if (threadIdx.x == 0) {
@@ -1045,7 +1048,7 @@ __device__ __forceinline__ void ff_cmac(cx<float>& s, cx<float>& c, cx<float> ah
 // is 1/64 of its FP32 rate).  Walkers above the threshold (or
 // all of them when threshold < 0) get the FP64 Gauss-Jordan re-inversion.
 template <typename T, int NT>
-__global__ void __launch_bounds__(NT, 2) k_check_reinvert(DevJob J, double threshold)
+__global__ void __launch_bounds__(NT, 2) k_check_reinvert(DevJob J, double threshold, int m_in_smem)
 {
     extern __shared__ __align__(16) char smem[];
     constexpr int NR = 8;
@@ -1142,7 +1145,8 @@ __global__ void __launch_bounds__(NT, 2) k_check_reinvert(DevJob J, double thres
     const bool redo = threshold < 0.0 || drift > threshold;
     if (redo) {
         GJSmem S = carve_gj<NT>(gp, Nmax);
-        cx<double>* M = J.scratch64 + size_t(w) * Nmax * Nmax;
+        // the working matrix after the GJ scratch when the launch provides it (as k_invert)
+        cx<double>* M = m_in_smem ? reinterpret_cast<cx<double>*>(gp) : J.scratch64 + size_t(w) * Nmax * Nmax;
         const int st = reinvert_walker<T, NT>(J, w, M, S, nullptr);
         if (J.channel == GV_CH_TRANS && st == GV_OK) trans_rebuild<T, NT>(J, w, nullptr, J.cur[w]);
         if (tid == 0) { J.status[w] = st; J.counts[size_t(w) * 5 + 4] += 1; }
