@@ -49,6 +49,17 @@ __device__ __forceinline__ cx<T> phi_orb(const cx<T>* phase, const cx<T>* coef_f
     return cmul_rn(phase[size_t(s) * Nk + (o >> 1)], coef_fl[size_t(sublattice(s, L)) * Ns + o]);
 }
 
+// Exact FP32 -> FP64 widening in integer arithmetic (FP32 subnormals become
+// signed zeros), keeping epilogues off GB300's narrow FP64 pipe: products are
+// formed in FP32 and only running sums are FP64.
+__device__ __forceinline__ double f32_to_f64(float x)
+{
+    const uint32_t u = __float_as_uint(x), e = (u >> 23) & 0xFFu;
+    uint64_t d = uint64_t(u & 0x80000000u) << 32;
+    if (e) d |= (uint64_t(e == 0xFFu ? 0x7FFu : e + 896u) << 52) | (uint64_t(u & 0x7FFFFFu) << 29);
+    return __longlong_as_double(static_cast<long long>(d));
+}
+
 template <typename T>
 __device__ __forceinline__ cx<T> warp_sum(cx<T> v)
 {

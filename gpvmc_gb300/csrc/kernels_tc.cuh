@@ -213,17 +213,6 @@ __device__ __forceinline__ void tc_store_phi(char* base, const size_t* tiles, in
     }
 }
 
-// Exact FP32 -> FP64 widening in integer arithmetic (FP32 subnormals become
-// signed zeros), keeping the epilogue off GB300's narrow FP64 pipe: the pair
-// ratios are formed in FP32 and only the job-wide sums are FP64.
-__device__ __forceinline__ double f32_to_f64(float x)
-{
-    const uint32_t u = __float_as_uint(x), e = (u >> 23) & 0xFFu;
-    uint64_t d = uint64_t(u & 0x80000000u) << 32;
-    if (e) d |= (uint64_t(e == 0xFFu ? 0x7FFu : e + 896u) << 52) | (uint64_t(u & 0x7FFFFFu) << 29);
-    return __longlong_as_double(static_cast<long long>(d));
-}
-
 // Orbital operand with an explicit row -> coefficient table: row r, K value f
 // holds phase[site r][pcol f] coef[sub(site r) * cld + f] (rows r < nr, f < nk).
 __device__ __forceinline__ void tc_store_phi_cols(char* base, const size_t* tiles, int nt, const TcRegs& R,

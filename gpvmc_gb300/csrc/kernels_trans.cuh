@@ -779,6 +779,7 @@ __global__ void __launch_bounds__(NT) k_measure_trans(DevJob J, int mask, const 
                 }
                 const int rk = s_wslot[Ns + s_exd[k]];
                 cx<double> acc = s_S[k];
+                cx<T> part = {T(0), T(0)};   // FP32 form: the tile's bond products, added to acc once
 #pragma unroll
                 for (int tt = 0; tt < TT; ++tt) {
                     if (tt >= nt) break;
@@ -792,10 +793,22 @@ __global__ void __launch_bounds__(NT) k_measure_trans(DevJob J, int mask, const 
                             r0k = B[0] * s_Y[k] - B[1] * zc;
                             r1k = B[2] * s_g[rk] - s_arow[tt * Nexc + k] * B[3];
                         }
-                        const cx<double> r = to_d(r0k) * to_d(r1k);
-                        acc.x += r.x;
-                        acc.y += r.y;
+                        bool wide = true;
+                        if constexpr (sizeof(T) == 4) {
+                            // FP32 product unless it could come near the FP32 range (then FP64, as the plain form)
+                            wide = (fabsf(r0k.x) + fabsf(r0k.y)) * (fabsf(r1k.x) + fabsf(r1k.y)) > 1e30f;
+                            if (!wide) cmac(part, r0k, r1k);
+                        }
+                        if (wide) {
+                            const cx<double> r = to_d(r0k) * to_d(r1k);
+                            acc.x += r.x;
+                            acc.y += r.y;
+                        }
                     }
+                }
+                if constexpr (sizeof(T) == 4) {
+                    acc.x += f32_to_f64(part.x);
+                    acc.y += f32_to_f64(part.y);
                 }
                 s_S[k] = acc;
             }
