@@ -169,9 +169,14 @@ static int bigc_is_zero(bigc a) { zc z = bigc_z(a); return creal(z) == 0.0 && ci
 
 /* ------------------------------------------------------------------ */
 /* Hop sets: at most one hop per flavour (2 flavours). */
-typedef struct { int n[2]; int from[2]; int to[2]; } hopset;
+/* hop_path_t per flavour (defs.h:5-7): up to two hops (a long-exciton state
+ * differs from another by two orbital hops in one flavour); hop 0 in
+ * from/to, hop 1 in from2/to2. */
+typedef struct { int n[2]; int from[2]; int to[2]; int from2[2]; int to2[2]; } hopset;
 
 static hopset hopset_empty(void) { hopset h; memset(&h, 0, sizeof h); return h; }
+static int hop_from(const hopset* h, int fl, int i) { return i ? h->from2[fl] : h->from[fl]; }
+static int hop_to(const hopset* h, int fl, int i) { return i ? h->to2[fl] : h->to[fl]; }
 
 /* State (State.cpp): m_fock[fl][s] = particle or Npt, m_part[fl][p] = s. */
 typedef struct {
@@ -219,6 +224,23 @@ static int state_hopsign(const state_t* s, const hopset* h)   /* State.cpp:86-11
             int a = h->from[fl], b = h->to[fl];
             int mn = (a < b ? a : b) + 1, mx = a > b ? a : b;
             for (int x = mn; x < mx; ++x) odd = (odd != (s->fock[fl][x] != s->Npt[fl]));
+            if (h->n[fl] > 1) {
+                /* the second hop counts on a copy with the first applied (State.cpp:97-110) */
+                int* sf = (int*)malloc(sizeof(int) * s->Nfs[fl]);
+                memcpy(sf, s->fock[fl], sizeof(int) * s->Nfs[fl]);
+                int part = sf[a];
+                sf[a] = s->Npt[fl];
+                sf[b] = part;
+                for (int hh = 1; hh < h->n[fl]; ++hh) {
+                    int a2 = hop_from(h, fl, hh), b2 = hop_to(h, fl, hh);
+                    int mn2 = (a2 < b2 ? a2 : b2) + 1, mx2 = a2 > b2 ? a2 : b2;
+                    for (int x = mn2; x < mx2; ++x) odd = (odd != (sf[x] != s->Npt[fl]));
+                    part = sf[a2];
+                    if (part < s->Nfs[fl]) sf[part] = s->Npt[fl];   /* as State.cpp:107 writes it (by particle index) */
+                    sf[b2] = part;
+                }
+                free(sf);
+            }
         }
     }
     return 2 * (!odd) - 1;
@@ -227,14 +249,14 @@ static int state_hopsign(const state_t* s, const hopset* h)   /* State.cpp:86-11
 static void state_hop(state_t* s, const hopset* h)   /* State.cpp:73-84 */
 {
     s->sign *= state_hopsign(s, h);
-    for (int fl = 0; fl < 2; ++fl) {
-        if (h->n[fl]) {
-            int p = s->fock[fl][h->from[fl]];
-            s->fock[fl][h->from[fl]] = s->Npt[fl];
-            s->fock[fl][h->to[fl]] = p;
-            s->part[fl][p] = h->to[fl];
+    for (int fl = 0; fl < 2; ++fl)
+        for (int hh = 0; hh < h->n[fl]; ++hh) {
+            int f = hop_from(h, fl, hh), t = hop_to(h, fl, hh);
+            int p = s->fock[fl][f];
+            s->fock[fl][f] = s->Npt[fl];
+            s->fock[fl][t] = p;
+            s->part[fl][p] = t;
         }
-    }
 }
 
 static void state_initfock(state_t* s, int* const st[2])   /* State.cpp:29-41 */
@@ -254,13 +276,13 @@ static void state_initfock(state_t* s, int* const st[2])   /* State.cpp:29-41 */
 /* get_hop_path (State.cpp:213-231), one hop per flavour at most. */
 static int hop_path(const int* src, const int* dest, int n, int Npt, int* from, int* to)
 {
-    int np = 0, nh = 0, part = -1, hole = -1;
+    int np = 0, nh = 0, part[2] = {-1, -1}, hole[2] = {-1, -1};
     for (int x = 0; x < n; ++x) {
-        if (src[x] == Npt && dest[x] != Npt) { if (!np) part = x; ++np; }
-        if (src[x] != Npt && dest[x] == Npt) { if (!nh) hole = x; ++nh; }
+        if (src[x] == Npt && dest[x] != Npt) { if (np < 2) part[np] = x; ++np; }
+        if (src[x] != Npt && dest[x] == Npt) { if (nh < 2) hole[nh] = x; ++nh; }
     }
-    if (np > 1) return -1;
-    *from = hole; *to = part;
+    if (np > 2 || np != nh) return -1;
+    for (int h = 0; h < 2; ++h) { from[h] = hole[h]; to[h] = part[h]; }   /* pairs in ascending order */
     return np;
 }
 
@@ -395,15 +417,19 @@ static int wav_add_states(orc_job* j, int nst, int** st /* nst*2 vectors of Ns *
                 /* get_hop_state(m_exc[0][i][fl], m_fock[fl], ...) (State.cpp:233-244) */
                 memcpy(state, j->wav0.fock[fl], sizeof(int) * j->Ns);
                 const hopset* h0 = &j->exc[0 * nst + i];
-                if (h0->n[fl]) { state[h0->to[fl]] = state[h0->from[fl]]; state[h0->from[fl]] = Npt[fl]; }
+                for (int hh = 0; hh < h0->n[fl]; ++hh) {
+                    int f = hop_from(h0, fl, hh), t = hop_to(h0, fl, hh);
+                    state[t] = state[f];
+                    state[f] = Npt[fl];
+                }
                 hopset* ha = &j->exc[a * nst + i];
                 hopset* hb = &j->exc[i * nst + a];
-                int f1, t1, f2, t2;
-                int n1 = hop_path(st[a * 2 + fl], state, j->Ns, Npt[fl], &f1, &t1);
-                int n2 = hop_path(state, st[a * 2 + fl], j->Ns, Npt[fl], &f2, &t2);
+                int f1[2], t1[2], f2[2], t2[2];
+                int n1 = hop_path(st[a * 2 + fl], state, j->Ns, Npt[fl], f1, t1);
+                int n2 = hop_path(state, st[a * 2 + fl], j->Ns, Npt[fl], f2, t2);
                 if (n1 < 0 || n2 < 0) { free(state); return ORC_ERR_INVALID; }
-                ha->n[fl] = n1; ha->from[fl] = f1; ha->to[fl] = t1;
-                hb->n[fl] = n2; hb->from[fl] = f2; hb->to[fl] = t2;
+                ha->n[fl] = n1; ha->from[fl] = f1[0]; ha->to[fl] = t1[0]; ha->from2[fl] = f1[1]; ha->to2[fl] = t1[1];
+                hb->n[fl] = n2; hb->from[fl] = f2[0]; hb->to[fl] = t2[0]; hb->from2[fl] = f2[1]; hb->to2[fl] = t2[1];
             }
         }
     }
@@ -692,13 +718,148 @@ static bigc det_small(const zc* B, int M)
     return bigc_make(B[0] * B[3] - B[1] * B[2], 0);
 }
 
-/* linalg::DetUpdate (linalg.cpp:107-400), ranks rc, rr in {0,1}. */
+/* The plain-loop BLAS the reference build links (zgemm 'N','N', zgemv 'N',
+ * zgeru, zdotu), in the same loop order, for the rank-2 row branches. */
+static void zgemm_nn(int m, int n, int k, zc alpha, const zc* a, int lda, const zc* b, int ldb, zc beta, zc* c,
+                     int ldc)
+{
+    for (int jj = 0; jj < n; ++jj) {
+        for (int i = 0; i < m; ++i) {
+            zc* cij = &c[i + (size_t)jj * ldc];
+            *cij = (creal(beta) == 0.0 && cimag(beta) == 0.0) ? 0.0 : beta * *cij;
+        }
+        for (int l = 0; l < k; ++l) {
+            zc t = alpha * b[l + (size_t)jj * ldb];
+            for (int i = 0; i < m; ++i) c[i + (size_t)jj * ldc] += t * a[i + (size_t)l * lda];
+        }
+    }
+}
+
+static void zgemv_n(int m, int n, zc alpha, const zc* a, int lda, const zc* x, int incx, zc beta, zc* y, int incy)
+{
+    for (int i = 0; i < m; ++i) {
+        zc* yi = &y[(size_t)i * incy];
+        *yi = (creal(beta) == 0.0 && cimag(beta) == 0.0) ? 0.0 : beta * *yi;
+    }
+    for (int jj = 0; jj < n; ++jj) {
+        zc t = alpha * x[(size_t)jj * incx];
+        for (int i = 0; i < m; ++i) y[(size_t)i * incy] += t * a[i + (size_t)jj * lda];
+    }
+}
+
+static void zgeru_(int m, int n, zc alpha, const zc* x, int incx, const zc* y, int incy, zc* a, int lda)
+{
+    for (int jj = 0; jj < n; ++jj) {
+        zc t = alpha * y[(size_t)jj * incy];
+        for (int i = 0; i < m; ++i) a[i + (size_t)jj * lda] += x[(size_t)i * incx] * t;
+    }
+}
+
+static zc zdotu(int n, const zc* x, int incx, const zc* y, int incy)
+{
+    zc s = 0.0;
+    for (int i = 0; i < n; ++i) s += x[(size_t)i * incx] * y[(size_t)i * incy];
+    return s;
+}
+
+/* linalg::Det (linalg.cpp:46-73): closed forms up to M = 2, LU (zgetrf) above */
+static bigc det_any(const zc* B, int M)
+{
+    if (M <= 2) return det_small(B, M);
+    zc* AA = (zc*)malloc(sizeof(zc) * (size_t)M * M);
+    int* ipiv = (int*)malloc(sizeof(int) * M);
+    memcpy(AA, B, sizeof(zc) * (size_t)M * M);
+    lu_factor(AA, M, ipiv);
+    int perm = 1;
+    for (int i = 0; i < M; ++i) if (ipiv[i] != i + 1) perm *= -1;
+    bigc d = bigc_make((double)perm, 0);
+    for (int i = 0; i < M; ++i) bigc_muleq(&d, bigc_make(AA[(size_t)i * M + i], 0));
+    free(AA);
+    free(ipiv);
+    return d;
+}
+
+/* DetUpdate's B for one column (rc0 <= 1) and two rows of hop set r
+ * (linalg.cpp:139-258, the rr[r] > 1 arms). */
+static bigc det_update_rows2(const zc* A, const zc* Ai, int N, const zc* C, const int* ci, int rc0, zc EcAiC,
+                             const zc* RAiC, int Nr, const zc* R, int ldr, const int* ri, int rid)
+{
+    const int rr = 2, m = rc0 + rr;
+    zc B[9] = {0};
+    zc ErTAEcT[2] = {0, 0}, ErTC[2] = {0, 0};
+    for (int i = 0; i < rr; ++i)                       /* B22: zdotu R row . Ai column */
+        for (int jj = 0; jj < rr; ++jj)
+            B[rc0 + i + (size_t)(rc0 + jj) * m] = zdotu(N, &R[rid + i], ldr, &Ai[(size_t)ri[rid + jj] * N], 1);
+    if (rc0) B[0] = EcAiC;                             /* B11 */
+    if (rc0) {
+        for (int jj = 0; jj < rr; ++jj) B[(size_t)(rc0 + jj) * m] = Ai[ci[0] + (size_t)ri[rid + jj] * N];   /* B12 */
+        for (int i = 0; i < rr; ++i) {
+            ErTAEcT[i] = A[ri[rid + i] + (size_t)ci[0] * N];
+            ErTC[i] = C[ri[rid + i]];
+            B[rc0 + i] = RAiC[rid + i] - R[rid + i + (size_t)ci[0] * ldr];                             /* B21 */
+        }
+        zgemv_n(rr, rr, 1.0, &B[rc0 * m + rc0], m, ErTAEcT, 1, 1.0, &B[rc0], 1);
+        zgemv_n(rr, rr, 1.0, &B[rc0 * m + rc0], m, ErTC, 1, 1.0, &B[rc0], 1);
+        zc mem = zdotu(rr, &B[rc0 * m], m, ErTC, 1);
+        B[0] += mem;
+        mem = zdotu(rr, &B[rc0 * m], m, ErTAEcT, 1);
+        B[0] += mem;
+    }
+    (void)Nr;
+    return det_any(B, m);
+}
+
+/* DetUpdate's nr <= 1 branch with a two-row hop set (linalg.cpp:259-378, the
+ * rr[0] > 1 arms): one B per column hop set c. */
+static int det_update_cols_rows2(const zc* A, const zc* Ai, int N, const zc* C, int ldc, const int* ci,
+                                 const int* rc, int nc, const zc* R, int ldr, const int* ri, int nr, bigc* dets)
+{
+    const int rr = 2;
+    int* cid = (int*)malloc(sizeof(int) * nc);
+    int Nc = 0;
+    for (int c = 0; c < nc; ++c) { cid[c] = Nc; Nc += rc[c]; }
+    zc* RAi = (zc*)malloc(sizeof(zc) * rr * (size_t)N);
+    zc* RAiC = (zc*)malloc(sizeof(zc) * rr * (size_t)(Nc > 0 ? Nc : 1));
+    zc RAiEr[4];
+    zgemm_nn(rr, N, N, 1.0, R, ldr, Ai, N, 0.0, RAi, rr);                 /* R * Ai */
+    for (int i = 0; i < rr; ++i)
+        for (int jj = 0; jj < rr; ++jj) RAiEr[jj * rr + i] = RAi[i + (size_t)ri[jj] * rr];
+    if (Nc) zgemm_nn(rr, Nc, N, 1.0, RAi, rr, C, ldc, 0.0, RAiC, rr);     /* R * Ai * C */
+    for (int c = 0; c < nc; ++c) {
+        const int m = rc[c] + rr;
+        zc B[9] = {0};
+        zc ErTAEcT[2] = {0, 0}, REcT[2] = {0, 0};
+        if (rc[c]) B[0] = zdotu(N, &Ai[ci[cid[c]]], N, &C[(size_t)cid[c] * ldc], 1);   /* B11 */
+        for (int i = 0; i < rr; ++i)                                                   /* B22 */
+            for (int jj = 0; jj < rr; ++jj) B[(size_t)(rc[c] + jj) * m + rc[c] + i] = RAiEr[jj * rr + i];
+        if (rc[c]) {
+            for (int jj = 0; jj < rr; ++jj) B[(size_t)(rc[c] + jj) * m] = Ai[ci[cid[c]] + (size_t)ri[jj] * N];   /* B12 */
+            for (int i = 0; i < rr; ++i) {
+                ErTAEcT[i] = A[ri[i] + (size_t)ci[cid[c]] * N];
+                REcT[i] = R[i + (size_t)ci[cid[c]] * nr * rr];          /* row stride as linalg.cpp:322 */
+                B[rc[c] + i] = RAiC[i + (size_t)cid[c] * rr] - C[ri[i] + (size_t)cid[c] * ldc];   /* B21 */
+            }
+            for (int i = 0; i < rr; ++i) B[rc[c] + i] += (ErTAEcT[i] + REcT[i]) * B[0];
+            zgeru_(rr, rr, 1.0, REcT, 1, &B[(size_t)rc[c] * m], m, &B[(size_t)rc[c] * m + rc[c]], m);
+            zgeru_(rr, rr, 1.0, ErTAEcT, 1, &B[(size_t)rc[c] * m], m, &B[(size_t)rc[c] * m + rc[c]], m);
+        }
+        dets[c] = det_any(B, m);
+    }
+    free(cid);
+    free(RAi);
+    free(RAiC);
+    return ORC_OK;
+}
+
+/* linalg::DetUpdate (linalg.cpp:107-400), ranks rc in {0,1}, rr in {0,1,2}. */
 static int det_update(const zc* A, const zc* Ai, int N, const zc* C, int ldc, const int* ci,
                       const int* rc, int nc, const zc* R, int ldr, const int* ri, const int* rr,
                       int nr, bigc* dets, zc* work)
 {
     for (int c = 0; c < nc; ++c) if (rc[c] > 1) return ORC_ERR_INVALID;
-    for (int r = 0; r < nr; ++r) if (rr[r] > 1) return ORC_ERR_INVALID;
+    for (int r = 0; r < nr; ++r) if (rr[r] > 2) return ORC_ERR_INVALID;
+    if (nc > 1 && nr <= 1 && nr && rr[0] == 2)
+        return det_update_cols_rows2(A, Ai, N, C, ldc, ci, rc, nc, R, ldr, ri, nr, dets);
     if (nc <= 1) {
         int* rid = (int*)malloc(sizeof(int) * (nr > 0 ? nr : 1));
         int Nr = 0;
@@ -722,6 +883,10 @@ static int det_update(const zc* A, const zc* Ai, int N, const zc* C, int ldc, co
                 }
         }
         for (int r = 0; r < nr; ++r) {
+            if (rr[r] == 2) {
+                dets[r] = det_update_rows2(A, Ai, N, C, ci, nc ? rc0 : 0, EcAiC, RAiC, Nr, R, ldr, ri, rid[r]);
+                continue;
+            }
             zc B[4] = {0, 0, 0, 0};
             int m = rc0 + rr[r];
             if (rr[r]) {                                /* zdotu R row . Ai column ri */
@@ -794,11 +959,98 @@ static int det_update(const zc* A, const zc* Ai, int N, const zc* C, int ldc, co
     return ORC_ERR_INVALID;
 }
 
-/* linalg::InvUpdate (linalg.cpp:402-573), ranks rc, rr in {0,1}. */
+/* linalg::InvUpdate (linalg.cpp:402-573) as written there, through the
+ * plain-loop zgemm: used for two row changes (R is rr x N with leading
+ * dimension rr, C is N x rc). */
+static int inv_update_general(const zc* A, zc* Ai, int N, const zc* C, const int* ci, int rc,
+                              const zc* R, const int* ri, int rr, bigc* det)
+{
+    const int m = rc + rr;
+    const zc one = 1.0, zer = 0.0, mone = -1.0;
+    zc* EcAiC = (zc*)calloc((size_t)rc * rc + 1, sizeof(zc));
+    zc* RAiEr = (zc*)calloc((size_t)rr * rr + 1, sizeof(zc));
+    zc* B = (zc*)calloc((size_t)m * m, sizeof(zc));
+    zc* Bi = (zc*)calloc((size_t)m * m, sizeof(zc));
+    zc* RAiC = (zc*)calloc((size_t)rr * rc + 1, sizeof(zc));
+    zc* ErTAEcT = (zc*)calloc((size_t)rr * rc + 1, sizeof(zc));
+    zc* ErTC = (zc*)calloc((size_t)rr * rc + 1, sizeof(zc));
+    zc* REcT = (zc*)calloc((size_t)rr * rc + 1, sizeof(zc));
+    zc* AiC = (zc*)calloc((size_t)N * rc + 1, sizeof(zc));
+    zc* EcAi = (zc*)calloc((size_t)rc * N + 1, sizeof(zc));
+    zc* RAi = (zc*)calloc((size_t)rr * N + 1, sizeof(zc));
+    zc* AiEr = (zc*)calloc((size_t)N * rr + 1, sizeof(zc));
+    zc* mem = (zc*)calloc((size_t)(rc > rr ? rc : rr) * N + 1, sizeof(zc));
+    zc* lu = (zc*)calloc((size_t)m + 1, sizeof(zc));
+    if (rc) zgemm_nn(N, rc, N, one, Ai, N, C, N, zer, AiC, N);
+    if (rr) zgemm_nn(rr, N, N, one, R, rr, Ai, N, zer, RAi, rr);
+    for (int i = 0; i < rc; ++i)
+        for (int jj = 0; jj < rc; ++jj) EcAiC[jj * rc + i] = AiC[ci[i] + (size_t)jj * N];
+    for (int i = 0; i < rr; ++i)
+        for (int jj = 0; jj < rr; ++jj) RAiEr[i + jj * rr] = RAi[i + (size_t)ri[jj] * rr];
+    if (rc * rr) zgemm_nn(rr, rc, N, one, RAi, rr, C, N, zer, RAiC, rr);
+    for (int i = 0; i < rr; ++i)
+        for (int jj = 0; jj < rc; ++jj) {
+            ErTAEcT[i + jj * rr] = A[ri[i] + (size_t)ci[jj] * N];
+            ErTC[i + jj * rr] = C[ri[i] + (size_t)jj * N];
+            REcT[i + jj * rr] = R[i + (size_t)ci[jj] * rr];
+        }
+    for (int i = 0; i < rc; ++i)
+        for (int jj = 0; jj < rr; ++jj) B[i + (size_t)(rc + jj) * m] = Ai[ci[i] + (size_t)ri[jj] * N];   /* B12 */
+    for (int i = 0; i < rr; ++i)
+        for (int jj = 0; jj < rr; ++jj) B[(rc + i) + (size_t)(rc + jj) * m] = RAiEr[i + jj * rr];       /* B22 */
+    for (int i = 0; i < rc; ++i)
+        for (int jj = 0; jj < rc; ++jj) B[i + (size_t)jj * m] = EcAiC[i + jj * rc];                   /* B11 */
+    if (rr * rc) {
+        zgemm_nn(rc, rc, rr, mone, &B[(size_t)rc * m], m, ErTC, rr, one, B, m);
+        zgemm_nn(rc, rc, rr, one, &B[(size_t)rc * m], m, ErTAEcT, rr, one, B, m);
+    }
+    for (int i = 0; i < rr; ++i)
+        for (int jj = 0; jj < rc; ++jj) B[(rc + i) + (size_t)jj * m] = RAiC[i + jj * rr] - R[i + (size_t)ci[jj] * rr];
+    if (rr * rc) {
+        zgemm_nn(rr, rc, rr, one, &B[(size_t)rc * m + rc], m, ErTAEcT, rr, one, &B[rc], m);
+        zgemm_nn(rr, rc, rr, mone, &B[(size_t)rc * m + rc], m, ErTC, rr, one, &B[rc], m);
+    }
+    int st = ORC_OK;
+    if (!det_inv(B, Bi, m, det, lu)) {
+        for (int i = 0; i < N; ++i) {
+            for (int jj = 0; jj < rr; ++jj) AiEr[i + (size_t)jj * N] = Ai[i + (size_t)ri[jj] * N];
+            for (int jj = 0; jj < rc; ++jj) EcAi[jj + (size_t)i * rc] = Ai[ci[jj] + (size_t)i * N];
+        }
+        if (rr * rc) {
+            zgemm_nn(N, rc, rr, mone, AiEr, N, ErTC, rr, one, AiC, N);
+            zgemm_nn(N, rc, rr, one, AiEr, N, ErTAEcT, rr, one, AiC, N);
+        }
+        for (int c = 0; c < rc; ++c) AiC[ci[c] + (size_t)c * N] -= 1;
+        for (int r = 0; r < rr; ++r) RAi[r + (size_t)ri[r] * rr] -= 1;
+        if (rc) {
+            zgemm_nn(rc, N, rc, one, Bi, m, EcAi, rc, zer, mem, rc);
+            zgemm_nn(N, N, rc, mone, AiC, N, mem, rc, one, Ai, N);
+        }
+        if (rc * rr) {
+            zgemm_nn(rc, N, rr, one, &Bi[(size_t)rc * m], m, RAi, rr, zer, mem, rc);
+            zgemm_nn(N, N, rc, mone, AiC, N, mem, rc, one, Ai, N);
+            zgemm_nn(rr, N, rc, one, &Bi[rc], m, EcAi, rc, zer, mem, rr);
+            zgemm_nn(N, N, rr, mone, AiEr, N, mem, rr, one, Ai, N);
+        }
+        if (rr) {
+            zgemm_nn(rr, N, rr, one, &Bi[(size_t)rc * m + rc], m, RAi, rr, zer, mem, rr);
+            zgemm_nn(N, N, rr, mone, AiEr, N, mem, rr, one, Ai, N);
+        }
+    } else {
+        st = ORC_ERR_SINGULAR;
+    }
+    free(EcAiC); free(RAiEr); free(B); free(Bi); free(RAiC); free(ErTAEcT); free(ErTC); free(REcT);
+    free(AiC); free(EcAi); free(RAi); free(AiEr); free(mem); free(lu);
+    return st;
+}
+
+/* linalg::InvUpdate (linalg.cpp:402-573), ranks rc, rr in {0,1}; two rows
+ * through inv_update_general. */
 static int inv_update(const zc* A, zc* Ai, int N, const zc* C, const int* ci, int rc,
                       const zc* R, const int* ri, int rr, bigc* det, zc* work)
 {
     if (!rc && !rr) { *det = bigc_make(1.0, 0); return ORC_OK; }
+    if (rc <= 1 && rr == 2) return inv_update_general(A, Ai, N, C, ci, rc, R, ri, rr, det);
     if (rc > 1 || rr > 1) return ORC_ERR_INVALID;
     zc* AiC = work;            /* N */
     zc* RAi = work + N;        /* N */
@@ -910,9 +1162,9 @@ static int sd_virt_update(const orc_walker* w, int Nr, const hopset* rh, int Nk,
                 for (int f = 0; f < N; ++f)
                     V[(size_t)ridx[n] * N + f] = matel(j, w->wav.part[fl][f], rh[n].to[fl], fl);
         for (int n = 0; n < Nk; ++n)
-            if (kh[n].n[fl])
+            for (int r = 0; r < kh[n].n[fl]; ++r)
                 for (int f = 0; f < N; ++f)
-                    U[(size_t)f * Nkf + kidx[n]] = matel(j, kh[n].to[fl], w->lat.part[fl][f], fl);
+                    U[(size_t)f * Nkf + kidx[n] + r] = matel(j, hop_to(&kh[n], fl, r), w->lat.part[fl][f], fl);
         int* rfid = (int*)malloc(sizeof(int) * (Nrf > 0 ? Nrf : 1));
         int* kfid = (int*)malloc(sizeof(int) * (Nkf > 0 ? Nkf : 1));
         int* rfr = (int*)malloc(sizeof(int) * Nr);
@@ -923,37 +1175,39 @@ static int sd_virt_update(const orc_walker* w, int Nr, const hopset* rh, int Nk,
         }
         for (int nk = 0; nk < Nk; ++nk) {
             kfr[nk] = kh[nk].n[fl];
-            if (kh[nk].n[fl]) kfid[kidx[nk]] = w->wav.fock[fl][kh[nk].from[fl]];
+            for (int rk = 0; rk < kh[nk].n[fl]; ++rk) kfid[kidx[nk] + rk] = w->wav.fock[fl][hop_from(&kh[nk], fl, rk)];
         }
         if (Nk == NN) {
             for (int nr = 0; nr < Nr && !rc_all; ++nr) {
                 if (rh[nr].n[fl])
                     for (int nk = 0; nk < Nk; ++nk)
-                        if (kh[nk].n[fl])
-                            U[(size_t)rfid[ridx[nr]] * Nkf + kidx[nk]] = matel(j, kh[nk].to[fl], rh[nr].to[fl], fl);
+                        for (int rk = 0; rk < kh[nk].n[fl]; ++rk)
+                            U[(size_t)rfid[ridx[nr]] * Nkf + kidx[nk] + rk] =
+                                matel(j, hop_to(&kh[nk], fl, rk), rh[nr].to[fl], fl);
                 rc_all = det_update(w->mat[fl], w->mati[fl], N, &V[(size_t)ridx[nr] * N], N,
                                     &rfid[ridx[nr]], &rfr[nr], 1, U, Nkf, kfid, kfr, Nk, qq, w->work);
                 for (int nk = 0; nk < Nk; ++nk) bigc_muleq(&qs[nk * Nr + nr], qq[nk]);
                 if (rh[nr].n[fl])
                     for (int nk = 0; nk < Nk; ++nk)
-                        if (kh[nk].n[fl])
-                            U[(size_t)rfid[ridx[nr]] * Nkf + kidx[nk]] =
-                                matel(j, kh[nk].to[fl], w->lat.part[fl][rfid[ridx[nr]]], fl);
+                        for (int rk = 0; rk < kh[nk].n[fl]; ++rk)
+                            U[(size_t)rfid[ridx[nr]] * Nkf + kidx[nk] + rk] =
+                                matel(j, hop_to(&kh[nk], fl, rk), w->lat.part[fl][rfid[ridx[nr]]], fl);
             }
         } else {
             for (int nk = 0; nk < Nk && !rc_all; ++nk) {
-                if (kh[nk].n[fl])
+                for (int rk = 0; rk < kh[nk].n[fl]; ++rk)
                     for (int nr = 0; nr < Nr; ++nr)
                         if (rh[nr].n[fl])
-                            V[(size_t)ridx[nr] * N + kfid[kidx[nk]]] = matel(j, kh[nk].to[fl], rh[nr].to[fl], fl);
+                            V[(size_t)ridx[nr] * N + kfid[kidx[nk] + rk]] =
+                                matel(j, hop_to(&kh[nk], fl, rk), rh[nr].to[fl], fl);
                 rc_all = det_update(w->mat[fl], w->mati[fl], N, V, N, rfid, rfr, Nr,
                                     &U[kidx[nk]], Nkf, &kfid[kidx[nk]], &kfr[nk], 1, qq, w->work);
                 for (int nr = 0; nr < Nr; ++nr) bigc_muleq(&qs[nk * Nr + nr], qq[nr]);
-                if (kh[nk].n[fl])
+                for (int rk = 0; rk < kh[nk].n[fl]; ++rk)
                     for (int nr = 0; nr < Nr; ++nr)
                         if (rh[nr].n[fl])
-                            V[(size_t)ridx[nr] * N + kfid[kidx[nk]]] =
-                                matel(j, w->wav.part[fl][kfid[kidx[nk]]], rh[nr].to[fl], fl);
+                            V[(size_t)ridx[nr] * N + kfid[kidx[nk] + rk]] =
+                                matel(j, w->wav.part[fl][kfid[kidx[nk] + rk]], rh[nr].to[fl], fl);
             }
         }
         free(V); free(U); free(rfid); free(kfid); free(rfr); free(kfr); free(ridx); free(kidx);
@@ -971,16 +1225,17 @@ static int sd_update(orc_walker* w, const hopset* rh, const hopset* kh)
     for (int fl = 0; fl < 2; ++fl) {
         int N = j->N[fl];
         zc* V = w->work + 8 * (size_t)N + 16;
-        zc* U = V + N;
-        int rid = 0, kid = 0;
+        zc* U = V + N;   /* kh->n[fl] rows, U[f * n + r] */
+        const int nk = kh->n[fl];
+        int rid = 0, kid[2] = {0, 0};
         if (rh->n[fl])
             for (int f = 0; f < N; ++f) V[f] = matel(j, w->wav.part[fl][f], rh->to[fl], fl);
-        if (kh->n[fl])
-            for (int f = 0; f < N; ++f) U[f] = matel(j, kh->to[fl], w->lat.part[fl][f], fl);
-        if (kh->n[fl]) kid = w->wav.fock[fl][kh->to[fl]];
+        for (int r = 0; r < nk; ++r)
+            for (int f = 0; f < N; ++f) U[(size_t)f * nk + r] = matel(j, hop_to(kh, fl, r), w->lat.part[fl][f], fl);
+        for (int r = 0; r < nk; ++r) kid[r] = w->wav.fock[fl][hop_to(kh, fl, r)];
         if (rh->n[fl]) rid = w->lat.fock[fl][rh->to[fl]];
         bigc qq;
-        int rc = inv_update(w->mat[fl], w->mati[fl], N, V, &rid, rh->n[fl], U, &kid, kh->n[fl], &qq, w->work);
+        int rc = inv_update(w->mat[fl], w->mati[fl], N, V, &rid, rh->n[fl], U, kid, nk, &qq, w->work);
         if (rc) return rc;
         bigc_muleq(&w->amp, qq);
     }

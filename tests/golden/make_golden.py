@@ -116,7 +116,24 @@ def main():
     am, ae = r.amp()
     np.savez_compressed(os.path.join(HERE, "gs_L8_virt.npz"), config=r.config(), hops=hops, qm=qm, qe=qe,
                         amp=np.array([am.real, am.imag, ae]))
+    long_exciton()
     print("golden fixtures written to", HERE)
+
+
+def long_exciton():
+    """7. Longitudinal exciton channel (StagFluxLongExciton): states two
+    orbital hops apart in one flavour; q = (0, 0) adds the ground state."""
+    for L, q, steps in [(4, (2, 0), 1500), (4, (0, 0), 1500)]:
+        r = ol.RefChain(L, PHI, 0.1, channel=ol.LONG, q=q, seed=7, walker=3)
+        assert r.random_start() == 0
+        st0 = r.current_state()
+        t = r.walk(steps, trace=True)
+        r.walk(L * L * 6, meas=L * L, mask=ol.MEAS_PROJHEIS)
+        pj, n = r.projheis()
+        am, ae = r.amp()
+        np.savez_compressed(os.path.join(HERE, "long_L%d_q%d%d.npz" % (L, q[0], q[1])), q=np.array(q), state0=st0,
+                            state=r.current_state(), final=r.config(), amp=np.array([am.real, am.imag, ae]),
+                            pj=pj, n=n, **trace_arrays(t))
 
 
 if __name__ == "__main__":

@@ -121,6 +121,25 @@ def test_trans_exciton(oracle, L, steps):
         np.testing.assert_array_equal(o.config(), g["final"])
 
 
+@pytest.mark.parametrize("name,steps", [("long_L4_q20.npz", 1500), ("long_L4_q00.npz", 1500)])
+def test_long_exciton(oracle, name, steps):
+    """Longitudinal exciton: channel states two orbital hops apart (rank-2
+    row updates in linalg::DetUpdate / InvUpdate)."""
+    g = load(name)
+    L = 4
+    o = oracle.OracleChain(L, PHI, 0.1, channel=oracle.LONG, q=tuple(g["q"]), seed=7, walker=3)
+    assert o.random_start() == 0
+    assert o.current_state() == int(g["state0"])
+    whole = same_trace(o.walk(steps, trace=True), g)
+    o.walk(L * L * 6, meas=L * L, mask=oracle.MEAS_PROJHEIS)
+    pj, n = o.projheis()
+    assert n == int(g["n"])
+    if SAME_ARCH or (whole and o.current_state() == int(g["state"]) and (o.config() == g["final"]).all()):
+        assert o.current_state() == int(g["state"])
+        np.testing.assert_allclose(pj, g["pj"], rtol=RTOL, atol=RTOL * np.abs(g["pj"]).max())
+        np.testing.assert_array_equal(o.config(), g["final"])
+
+
 def test_virt_update(oracle):
     g = load("gs_L8_virt.npz")
     o = oracle.OracleChain(8, PHI, 0.1, seed=3, walker=0)

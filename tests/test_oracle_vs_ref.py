@@ -17,7 +17,9 @@ def ref(oracle):
 
 @pytest.mark.parametrize("L,channel,q,neel,steps", [
     (6, 0, (0, 0), 0.1, 3000), (8, 0, (0, 0), 0.0, 3000), (10, 0, (0, 0), 0.05, 2000),
-    (4, 1, (2, 2), 0.1, 2000), (8, 1, (2, 2), 0.1, 800)])
+    (4, 1, (2, 2), 0.1, 2000), (8, 1, (2, 2), 0.1, 800),
+    # long exciton: states two orbital hops apart in one flavour (rank-2 row updates)
+    (4, 2, (0, 0), 0.1, 1500), (4, 2, (2, 0), 0.1, 1500), (4, 2, (1, 1), 0.1, 1500), (6, 2, (2, 2), 0.1, 600)])
 def test_walk_bit_exact(ref, L, channel, q, neel, steps):
     o = ref.OracleChain(L, PHI, neel, channel=channel, q=q, seed=42, walker=1)
     r = ref.RefChain(L, PHI, neel, channel=channel, q=q, seed=42, walker=1)
