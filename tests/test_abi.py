@@ -51,6 +51,10 @@ def test_invalid_arguments_are_rejected(lib):
     h = ctypes.c_void_p()
     assert lib.gv_job_create(ctypes.byref(cfg), ctypes.byref(h)) == _lib.GV_OK + 1
     assert lib.gv_job_create(None, ctypes.byref(h)) == 1
+    # the longitudinal exciton (channel 2) is not served: rejected before any device call
+    cfg.L, cfg.channel = 8, 2
+    assert lib.gv_job_create(ctypes.byref(cfg), ctypes.byref(h)) == 1 and not h.value
+    cfg.channel = 0
     out = ctypes.c_uint64()
     cfg.L = 16
     cfg.n_walkers = 2048
