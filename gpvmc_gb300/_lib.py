@@ -80,6 +80,7 @@ _SIGS = {
     "gv_job_measure": [_P],
     "gv_job_reset_quantities": [_P],
     "gv_job_read_drift_checks": [_P, ctypes.c_void_p, ctypes.c_void_p],
+    "gv_job_set_wait_limit": [_P, ctypes.c_int32],
     "gv_slater_invert_noalloc": [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int32, ctypes.c_void_p, ctypes.c_void_p],
     "gv_job_walk": [_P, ctypes.c_uint64, ctypes.c_uint64],
     "gv_job_walk_traced": [_P, ctypes.c_uint64, ctypes.c_uint64, ctypes.c_int32, ctypes.c_void_p],

@@ -188,6 +188,7 @@ struct DevJob {
     void* gdn;                 // W*Nmax,    g[f] = sum_p phi_{exc_dn[cur]}(x_p) (A1^-1)(p, f)
     cx<double>* pjx;           // W*2*Nexc*Nexc ProjHeis H and O sums
     cx<float>* zbuf;           // W*N1*Nexc tensor-core Z[d][k] = sum_f GupT[f][k] phi_f(d) (mixed, or null)
+    int wait_limit;            // polls before a bounded mbarrier wait of the tensor-core kernels gives up
 };
 
 // Amplitude kept as (complex mantissa, base-2 exponent); renormalised

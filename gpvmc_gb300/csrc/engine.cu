@@ -970,6 +970,7 @@ gv_status gv_job_create(const gv_job_config* cfg, gv_job** out)
     d.precision = cfg->precision; d.channel = cfg->channel;
     d.seed = cfg->seed; d.walker_base = cfg->walker_base; d.reinv_every = cfg->reinv_every;
     d.trace = nullptr; d.trace_walker = -1;
+    d.wait_limit = kTcWaitLimit;
     const size_t es = cfg->precision == GV_PREC_FP64 ? sizeof(cx<double>) : sizeof(cx<float>);
     gv_status st = GV_OK;
     int32_t *nbr = nullptr, *edg = nullptr;
@@ -1108,6 +1109,16 @@ gv_status gv_job_measure(gv_job* j)
     if (!st && (mask & GV_MEAS_STATSPIN)) st = statspin_dispatch(j);
     if (!st && (mask & kTrackMask)) st = tracks_dispatch(j, mask);
     return st ? st : gv_job_synchronize(j);
+}
+
+gv_status gv_job_set_wait_limit(gv_job* j, int32_t polls)
+{
+    if (!j) return GV_ERR_INVALID;
+    GV_CK(cudaStreamSynchronize(j->stream));
+    j->d.wait_limit = polls < 0 ? kTcWaitLimit : polls;
+    for (auto& kv : j->graphs) cudaGraphExecDestroy(kv.second.exec);   // they hold the old limit
+    j->graphs.clear();
+    return GV_OK;
 }
 
 gv_status gv_job_read_drift_checks(gv_job* j, double* drift, uint64_t* checks)

@@ -266,9 +266,12 @@ __device__ __forceinline__ void tc_commit(uint32_t bar)
     asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar) : "memory");
 }
 
-__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity)
+// Poll the mbarrier phase up to `limit` times (a job's wait budget for the
+// waits whose failure the kernel reports; the drain wait before TMEM is freed
+// always takes the full kTcWaitLimit so that MMAs in flight finish first).
+__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity, int limit = kTcWaitLimit)
 {
-    for (int i = 0; i < kTcWaitLimit; ++i) {
+    for (int i = 0; i < limit; ++i) {
         uint32_t done;
         asm volatile(
             "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
@@ -409,7 +412,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_statspin_tc(DevJob J)
         for (int step = 0; step < 2 * KC; ++step) {
             const int gm = step / KC, kc = step % KC;
             if (!first) {   // the previous chunk's MMAs are done with the tiles
-                const bool ok = mbar_wait(bar, parity);
+                const bool ok = mbar_wait(bar, parity, J.wait_limit);
                 if (__syncthreads_or(!ok)) { failed = true; break; }
                 parity ^= 1u;
             }
@@ -442,7 +445,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_statspin_tc(DevJob J)
             break;
         }
         {
-            const bool ok = mbar_wait(bar, parity);
+            const bool ok = mbar_wait(bar, parity, J.wait_limit);
             if (__syncthreads_or(!ok)) {
                 failed = true;
                 if (tid == 0) J.status[w] = GV_ERR_TIMEOUT;
@@ -586,7 +589,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_trans_z_tc(DevJob J, cx<float
         const cx<float>* cf = s_cf + b * 2 * kTcMaxK;
         for (int kc = 0; kc < KC; ++kc) {
             if (!first) {
-                const bool ok = mbar_wait(bar, parity);
+                const bool ok = mbar_wait(bar, parity, J.wait_limit);
                 if (__syncthreads_or(!ok)) { failed = true; break; }
                 parity ^= 1u;
             }
@@ -614,7 +617,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_trans_z_tc(DevJob J, cx<float
             break;
         }
         {
-            const bool ok = mbar_wait(bar, parity);
+            const bool ok = mbar_wait(bar, parity, J.wait_limit);
             if (__syncthreads_or(!ok)) {
                 failed = true;
                 if (tid == 0) J.status[w] = GV_ERR_TIMEOUT;

@@ -19,7 +19,13 @@
 //    threads) race on the array: serialise them.
 //  * The device address of the array is looked up once per device, with
 //    that device current, on the first call made there; make that first call
-//    before any stream capture.
+//    before any stream capture.  The address stays valid for the life of the
+//    device's primary context: a caller that runs cudaDeviceReset must not
+//    call this entry point on that device afterwards.
+//  * A matrix that fails linalg::DetInv's singular test (Gauss-Jordan finds
+//    no pivot, or |det|^2 < 1e-9, linalg.cpp:23) reports GV_ERR_SINGULAR in
+//    info[3] with a zero determinant mantissa, as DetInv sets d = 0; d_Ai
+//    then holds whatever the elimination produced and must not be used.
 #include <cuda_runtime.h>
 
 #include <mutex>
@@ -80,8 +86,8 @@ __global__ void __launch_bounds__(kThreads) k_invert_noalloc(const cx<double>* _
     }
     for (int idx = threadIdx.x; idx < N * N; idx += kThreads) Ai[idx] = M[idx];
     if (threadIdx.x == 0) {
-        info[0] = S.flag[0] ? dm.x : 0.0;
-        info[1] = S.flag[0] ? dm.y : 0.0;
+        info[0] = status == GV_OK ? dm.x : 0.0;
+        info[1] = status == GV_OK ? dm.y : 0.0;
         info[2] = double(de);
         info[3] = double(status);
     }
@@ -98,6 +104,7 @@ extern "C" gv_status gv_slater_invert_noalloc(const double* d_A, double* d_Ai, i
     if (N < 1 || N > kMaxN) return GV_ERR_TOO_LARGE;
     if (!d_A || !d_Ai || !d_info) return GV_ERR_INVALID;
     if ((reinterpret_cast<uintptr_t>(d_A) | reinterpret_cast<uintptr_t>(d_Ai)) & 15) return GV_ERR_INVALID;
+    if (reinterpret_cast<uintptr_t>(d_info) & 7) return GV_ERR_INVALID;   // four doubles written by the kernel
     cx<double>* scratch = nullptr;
     gv_status st = scratch_address(&scratch);
     if (st) return st;

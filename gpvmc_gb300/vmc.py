@@ -255,6 +255,11 @@ class Job:
     def synchronize(self):
         check(_lib.lib().gv_job_synchronize(self._h), "gv_job_synchronize")
 
+    def set_wait_limit(self, polls):
+        """Poll budget of the tensor-core kernels' bounded mbarrier waits
+        (negative: the default)."""
+        check(_lib.lib().gv_job_set_wait_limit(self._h, int(polls)), "gv_job_set_wait_limit")
+
     def reinvert(self):
         check(_lib.lib().gv_job_reinvert(self._h), "gv_job_reinvert")
 

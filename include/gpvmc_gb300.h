@@ -146,6 +146,18 @@ gv_status gv_job_reset_quantities(gv_job* job);
  * number of checks that needed no re-inversion. */
 gv_status gv_job_read_drift_checks(gv_job* job, double* drift_seen, uint64_t* checks_without_reinversion);
 
+/* Bounded device waits.  The tensor-core kernels (StatSpinStruct pair
+ * ratios, exciton overlap rows) wait on an mbarrier for their MMAs with a
+ * poll budget; when it runs out the walker's status becomes GV_ERR_TIMEOUT,
+ * the kernel still lets the MMAs it issued finish before it frees its tensor
+ * memory, and the next calls on the job run normally (gv_job_init_walkers
+ * clears the status).  polls < 0 restores the default (4194304 polls);
+ * polls = 0 makes every such wait give up at once, which tests exercise.
+ * Applies to kernels enqueued after the call (cached CUDA graphs are
+ * dropped).  Diagnostic; it has no counterpart in the reference, whose
+ * CPU code never waits on a device. */
+gv_status gv_job_set_wait_limit(gv_job* job, int32_t polls);
+
 /* Start configurations.  up: n_walkers x Ns bytes, 1 where flavour 0 sits
  * (LatticeState::FockInit), or NULL for the reference's random start with up
  * to 10 retries (vmc.cpp:221-241), drawn from Philox stream 1.  A
@@ -333,15 +345,20 @@ double gv_uniform_at(uint64_t seed, uint32_t walker, uint32_t stream, uint64_t k
  *   d_A    device, N x N complex (interleaved re, im) in the reference's
  *          column-major m_mat layout, A[r*N + f] = A(f, r); not modified
  *   d_Ai   device output, the inverse in the m_mati layout (N x N complex)
- *   d_info device output, 4 doubles: det mantissa (re, im), det base-2
- *          exponent, status (GV_OK or GV_ERR_SINGULAR)
+ *   d_info device output, 4 doubles (8-byte aligned): det mantissa (re, im),
+ *          det base-2 exponent, status (GV_OK or GV_ERR_SINGULAR; singular:
+ *          zero mantissa as linalg::DetInv, and d_Ai is not an inverse)
+ * d_A and d_Ai must be 16-byte aligned; misaligned pointers are GV_ERR_INVALID
+ * before anything is enqueued.
  *   stream cudaStream_t to enqueue on (NULL: the default stream)
  * The only working memory is a static device array sized for
  * N <= GV_NOALLOC_MAX_N (256 KiB, held by every GPU that loads the library
  * until exit); larger N returns GV_ERR_TOO_LARGE.  The call allocates and
  * frees nothing.  Its first call on a device looks up that array's device
  * address (make that first call before any stream capture).  All calls share
- * the array: calls that overlap on the GPU race and must be serialised. */
+ * the array: calls that overlap on the GPU race and must be serialised.  The
+ * looked-up address lives as long as the device's primary context: do not
+ * call this entry point on a device after cudaDeviceReset. */
 #define GV_NOALLOC_MAX_N 128
 gv_status gv_slater_invert_noalloc(const double* d_A, double* d_Ai, int32_t N, double* d_info, void* stream);
 

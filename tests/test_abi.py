@@ -99,3 +99,15 @@ def test_python_api_lattice():
     np.testing.assert_array_equal(lat.neighbours, gold["nbr"])
     assert len(lat.edges) == 2 * 64
     assert g.pi_phi(0.25) == 0.25 * math.pi
+
+
+def test_noalloc_rejects_bad_pointers_before_any_launch(lib):
+    """gv_slater_invert_noalloc checks sizes and alignment on the host, before
+    it touches the device (these calls run without a GPU)."""
+    P = ctypes.c_void_p
+    assert lib.gv_slater_invert_noalloc(P(0x10000), P(0x20000), 4, P(0x30004), None) == 1   # d_info: 4-byte aligned
+    assert lib.gv_slater_invert_noalloc(P(0x10008), P(0x20000), 4, P(0x30000), None) == 1   # d_A: 8-byte aligned
+    assert lib.gv_slater_invert_noalloc(P(0x10000), P(0x20008), 4, P(0x30000), None) == 1   # d_Ai: 8-byte aligned
+    assert lib.gv_slater_invert_noalloc(None, P(0x20000), 4, P(0x30000), None) == 1
+    assert lib.gv_slater_invert_noalloc(P(0x10000), P(0x20000), 129, P(0x30000), None) == 10
+    assert lib.gv_slater_invert_noalloc(P(0x10000), P(0x20000), 0, P(0x30000), None) == 10

@@ -38,7 +38,7 @@ def _compare_traces(tg, to):
     return int(tie.sum())
 
 
-@pytest.mark.parametrize("L,neel", [(4, 0.1), (8, 0.1), (12, 0.05)])
+@pytest.mark.parametrize("L,neel", [(4, 0.1), (8, 0.1), (12, 0.05), (16, 0.1)])
 def test_start_and_inverse(engine, oracle, L, neel):
     job, orc = _pair(engine, oracle, L, neel)
     job.init_walkers()
@@ -53,7 +53,7 @@ def test_start_and_inverse(engine, oracle, L, neel):
         assert np.abs(gi - oi).max() < RTOL * np.abs(oi).max()
 
 
-@pytest.mark.parametrize("L,neel,steps", [(4, 0.1, 3000), (8, 0.1, 6000), (12, 0.05, 4000)])
+@pytest.mark.parametrize("L,neel,steps", [(4, 0.1, 3000), (8, 0.1, 6000), (12, 0.05, 4000), (16, 0.1, 3000)])
 def test_trace_parity(engine, oracle, L, neel, steps):
     job, orc = _pair(engine, oracle, L, neel, seed=77)
     job.init_walkers()
@@ -72,20 +72,25 @@ def test_trace_parity(engine, oracle, L, neel, steps):
     assert c[0] == steps and c[1] == int((to["accepted"] & (to["kind"] == 1)).sum())
 
 
-def test_measurements_parity(engine, oracle):
-    L, neel = 8, 0.1
+@pytest.mark.parametrize("L,therm,nmeas", [(8, 200, 30), (16, 20, 6)])
+def test_measurements_parity(engine, oracle, L, therm, nmeas):
+    """ProjHeis, StagMagnZ and StatSpinStruct sums over `nmeas` measured sweeps
+    after `therm` sweeps of thermalisation; L = 16 is the headline lattice
+    (N = 128 per flavour)."""
+    neel = 0.1
     job, orc = _pair(engine, oracle, L, neel, seed=5)
     job.set_measurements(7)
     job.init_walkers()
     orc.random_start()
-    job.walk(200 * L * L, 0)
-    orc.walk(200 * L * L)
-    tg = job.walk_traced(L * L * 30, L * L)
-    to = orc.walk(L * L * 30, meas=L * L, mask=7, trace=True)
+    job.walk(therm * L * L, 0)
+    orc.walk(therm * L * L)
+    tg = job.walk_traced(L * L * nmeas, L * L)
+    to = orc.walk(L * L * nmeas, meas=L * L, mask=7, trace=True)
     _compare_traces(tg, to)
+    assert (job.config()[0] == orc.config()).all()
     pj, n = job.projheis()
     opj, on = orc.projheis()
-    assert n[0] == on == 30
+    assert n[0] == on == nmeas
     assert abs(pj[0, 0] - opj[0, 0]) < RTOL * abs(opj[0, 0])
     assert pj[0, 1].real == opj[1, 0].real
     sm, sn = job.stagmagn()
@@ -93,7 +98,7 @@ def test_measurements_parity(engine, oracle):
     assert sn[0] == osn and abs(sm[0] - osm) < 1e-12 * max(1.0, abs(osm))
     ss, ssn = job.statspin()
     oss, ossn = orc.statspin()
-    assert ssn == ossn == 30
+    assert ssn == ossn == nmeas
     assert np.abs(ss - oss).max() < RTOL * np.abs(oss).max()
 
 

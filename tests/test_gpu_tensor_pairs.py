@@ -109,3 +109,34 @@ def test_exciton_overlap_rows_on_tensor_cores(engine, oracle, L, q):
     scale = np.abs(p64).max(axis=(1, 2), keepdims=True)
     assert (np.abs(pt - ps) / scale).max() < 2e-5
     assert (np.abs(pt - p64) / scale).max() < 1e-3
+
+
+def test_bounded_wait_gives_up_with_a_status(engine, oracle):
+    """The tensor-core kernel's mbarrier waits are bounded: with a poll budget
+    of zero every wait gives up at once, the walkers it reached report
+    GV_ERR_TIMEOUT (host-visible status, no hang, no fault: the MMAs issued
+    still finish before the kernel frees its tensor memory), and the same job
+    then measures normally again with the default budget."""
+    L, W = 8, 24
+    job = _mixed(engine, L, W, 3)
+    job.init_walkers()
+    job.walk(L * L * 2, 0)
+    job.reinvert()
+    cfg = job.config()
+    job.set_measurements(oracle.MEAS_STATSPIN)
+    job.reset_quantities()
+    job.set_wait_limit(0)
+    with pytest.raises(engine.GvError) as err:
+        job.measure()
+    assert err.value.status == 6
+    st = job.status()
+    assert (st == 6).any() and set(st.tolist()) <= {0, 6}
+    job.set_wait_limit(-1)
+    job.init_walkers(cfg)                 # clears the statuses, fresh FP64 inverses
+    ok, n = _measure(job, oracle)
+    assert n == 1 and (job.status() == 0).all()
+    ref = _mixed(engine, L, W, 3)
+    ref.init_walkers(cfg)
+    want, _ = _measure(ref, oracle)
+    # the job-wide sums are FP64 atomics over walkers: equal up to summation order
+    assert np.abs(ok - want).max() <= 1e-12 * np.abs(want).max()

@@ -27,7 +27,7 @@ pytestmark = pytest.mark.gpu
 
 PHI = 0.25 * math.pi
 RTOL = 1e-10
-CASES = [(4, (2, 2), 7, 3), (8, (4, 4), 7, 3), (8, (2, 0), 11, 0), (12, (6, 6), 5, 1)]
+CASES = [(4, (2, 2), 7, 3), (8, (4, 4), 7, 3), (8, (2, 0), 11, 0), (12, (6, 6), 5, 1), (16, (4, 4), 7, 3)]
 EMPTY = (-1, -1, -1, -1)
 
 
@@ -134,7 +134,8 @@ def test_trans_virt_update(engine, oracle, L, q, seed, walker):
 
 
 @pytest.mark.parametrize("L,q,seed,walker,steps", [(4, (2, 2), 7, 3, 2000), (8, (4, 4), 7, 3, 1500),
-                                                   (8, (2, 0), 11, 0, 2500), (12, (6, 6), 5, 1, 1200)])
+                                                   (8, (2, 0), 11, 0, 2500), (12, (6, 6), 5, 1, 1200),
+                                                   (16, (4, 4), 7, 3, 1500)])
 def test_trans_trace_parity(engine, oracle, L, q, seed, walker, steps):
     job, orc = _pair(engine, oracle, L, q, seed, walker)
     job.init_walkers()
@@ -156,7 +157,7 @@ def test_trans_trace_parity(engine, oracle, L, q, seed, walker, steps):
     assert c[0] == steps and c[1] == int((to["accepted"] & (to["kind"] == 1)).sum())
 
 
-@pytest.mark.parametrize("L,q,seed,walker", [(4, (2, 2), 7, 3), (8, (4, 4), 7, 3)])
+@pytest.mark.parametrize("L,q,seed,walker", [(4, (2, 2), 7, 3), (8, (4, 4), 7, 3), (16, (4, 4), 7, 3)])
 def test_trans_measurements(engine, oracle, L, q, seed, walker):
     mask = oracle.MEAS_PROJHEIS | oracle.MEAS_STAGMAGN | oracle.MEAS_STATSPIN
     job, orc = _pair(engine, oracle, L, q, seed, walker)

@@ -24,23 +24,32 @@ def load(name):
     return np.load(os.path.join(GOLD, name))
 
 
-def same_trace(t, g):
-    """Returns True when the whole trace agrees (no parting at a near-tie)."""
+def same_trace(t, g, states=False, min_agree=50):
+    """Returns True when the whole trace agrees (no parting at a near-tie).
+
+    Off the fixtures' architecture the chains may part, but only (a) after at
+    least `min_agree` agreeing steps, and (b) where a decision flips, at a
+    near-tie of the accept test (|ratio - u4| < 1e-9 in the fixture), or --
+    channels with several states (`states`) -- where the ratios drift apart
+    with the decisions still agreeing, which follows an arg-max between
+    channel states of equal weight picked by rounding."""
     n = len(g["v1"])
     assert (t["v1"] == g["v1"]).all() and (t["v2"] == g["v2"]).all()
     assert (t["u"][:, 3] == g["u4"]).all()
     real = g["kind"] == 1
     rel = np.where(real, np.abs(t["ratio"] - g["ratio"]) / np.maximum(np.abs(g["ratio"]), 1e-300), 0.0)
-    off = (t["kind"] != g["kind"]) | (t["accepted"] != g["accepted"]) | (rel > RTOL) & (np.abs(g["ratio"]) > 1e-13)
+    flip = (t["kind"] != g["kind"]) | (t["accepted"] != g["accepted"])
+    off = flip | (rel > RTOL) & (np.abs(g["ratio"]) > 1e-13)
     if not off.any():
         return True
     first = int(np.argmax(off))
     assert not SAME_ARCH, "trace differs at step %d on the fixtures' own architecture" % first
-    # the chains may only part after a step whose decision was a near-tie:
-    # an accept test within 1e-9, or (exciton channels) an arg-max between
-    # channel states of equal weight, which shows as ratios diverging while
-    # the decisions before agree
-    assert first > 0
+    assert first >= min(min_agree, n - 1), "chains part after only %d agreeing steps" % first
+    if flip[first]:
+        r, u = float(g["ratio"][first]), float(g["u4"][first])
+        assert abs(r - u) < 1e-9 * max(1.0, abs(r)), "decision flips at step %d, not a near-tie" % first
+    else:
+        assert states, "ratios part at step %d in a channel with one state" % first
     return False
 
 
@@ -111,7 +120,7 @@ def test_trans_exciton(oracle, L, steps):
     o = oracle.OracleChain(L, PHI, 0.1, channel=oracle.TRANS, q=tuple(g["q"]), seed=7, walker=3)
     assert o.random_start() == 0
     assert o.current_state() == int(g["state0"])
-    whole = same_trace(o.walk(steps, trace=True), g)
+    whole = same_trace(o.walk(steps, trace=True), g, states=True)
     o.walk(L * L * 6, meas=L * L, mask=oracle.MEAS_PROJHEIS)
     pj, n = o.projheis()
     assert n == int(g["n"])
@@ -130,7 +139,7 @@ def test_long_exciton(oracle, name, steps):
     o = oracle.OracleChain(L, PHI, 0.1, channel=oracle.LONG, q=tuple(g["q"]), seed=7, walker=3)
     assert o.random_start() == 0
     assert o.current_state() == int(g["state0"])
-    whole = same_trace(o.walk(steps, trace=True), g)
+    whole = same_trace(o.walk(steps, trace=True), g, states=True)
     o.walk(L * L * 6, meas=L * L, mask=oracle.MEAS_PROJHEIS)
     pj, n = o.projheis()
     assert n == int(g["n"])

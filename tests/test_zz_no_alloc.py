@@ -90,3 +90,31 @@ def test_noalloc_rejects_oversize(engine):
     p = ctypes.c_void_p(buf.data_ptr())
     assert lib.gv_slater_invert_noalloc(p, p, 129, ctypes.c_void_p(info.data_ptr()), None) == 10
     assert b"N <= 128" in lib.gv_status_string(10)
+
+
+def test_noalloc_singular_reports_zero_determinant(engine):
+    """linalg::DetInv's singular rule (|det|^2 < 1e-9, linalg.cpp:23): status
+    GV_ERR_SINGULAR with a zero mantissa; just above the bar the inverse and
+    determinant come back."""
+    torch = pytest.importorskip("torch")
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    lib = engine.lib()
+    stream = torch.cuda.current_stream().cuda_stream
+    for d4, want in ((1e-5, 2), (1e-4, 0), (0.0, 2)):
+        A = np.diag([1.0 + 0.5j, 2.0, 1.0j, d4]).astype(np.complex128)
+        A[0, 1] = 0.25
+        dA = torch.from_numpy(np.ascontiguousarray(A.T).view(np.float64).ravel().copy()).cuda()
+        dAi = torch.zeros(32, dtype=torch.float64, device="cuda")
+        dinfo = torch.full((4,), 7.0, dtype=torch.float64, device="cuda")
+        st = lib.gv_slater_invert_noalloc(ctypes.c_void_p(dA.data_ptr()), ctypes.c_void_p(dAi.data_ptr()), 4,
+                                          ctypes.c_void_p(dinfo.data_ptr()), ctypes.c_void_p(stream))
+        assert st == 0
+        torch.cuda.synchronize()
+        info = dinfo.cpu().numpy()
+        assert info[3] == want, (d4, info)
+        if want:
+            assert info[0] == 0.0 and info[1] == 0.0
+        else:
+            det = complex(info[0], info[1]) * 2.0 ** info[2]
+            assert abs(det - np.linalg.det(A)) < 1e-12 * abs(np.linalg.det(A))
