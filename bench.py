@@ -42,17 +42,23 @@ THERM_SWEEPS = 16   # untimed thermalisation before the warm-up steps, every GPU
 SEED = 20261203
 
 
-def workload_config(precision, policy="drift"):
-    pol = ("FP64 drift check every 128 accepted exchanges, FP64 re-inversion when ||A A^-1 - I||_max > %g"
-           % DRIFT_THRESHOLD) if policy == "drift" else (
-        "FP64 re-inversion every 128 accepted exchanges" if policy == "always" else "no re-inversion")
+PRECISION_MODES = {
+    "mixed": "mixed: FP32 inverses, ratios and Sherman-Morrison updates; FP64 drift check every 128 accepted "
+             "exchanges, FP64 re-inversion when ||A A^-1 - I||_max > %g" % DRIFT_THRESHOLD,
+    "fp64": "fp64: FP64 inverses, ratios and Sherman-Morrison updates, no re-inversion (as the reference: "
+            "vmc.cpp inverts only at the start)",
+}
+
+
+def workload_config(precision):
+    """The bench configuration; arms differ only in `precision` (which names
+    the re-inversion rule that belongs to each precision)."""
     return {"workload": "staggered-flux ground state L=16 (128x128 complex per spin), 2048 walkers, "
-                        "phi~U[0.1,0.4)pi, neel~U[0,0.15), ProjHeis every sweep, " + pol,
-            "L": L, "walkers": WALKERS, "sweep_steps": SWEEP, "precision": precision,
-            "reinv_every_accepted": REINV, "reinversion_policy": policy, "thermalisation_sweeps": THERM_SWEEPS,
-            "updates": "rank-1 Sherman-Morrison per accepted exchange",
+                        "phi~U[0.1,0.4)pi, neel~U[0,0.15), ProjHeis every sweep",
+            "L": L, "walkers": WALKERS, "sweep_steps": SWEEP, "precision": PRECISION_MODES[precision],
+            "thermalisation_sweeps": THERM_SWEEPS,
             "step": "one sweep of every walker (2048*256 Metropolis steps)",
-            "l2": "inputs larger than L2: walker inverses %d MiB" % (WALKERS * 2 * 128 * 128 * (8 if precision == "mixed" else 16) >> 20)}
+            "l2": "inputs larger than L2: walker inverses >= 512 MiB"}
 
 
 # ---------------------------------------------------------------------------
@@ -60,36 +66,42 @@ def workload_config(precision, policy="drift"):
 # the host cores.  Runs in spawned processes before any GPU work.
 
 def _cpu_chain(args):
-    walker, sweeps, measure = args
+    walker, sweeps, measure, reinv = args
     sys.path.insert(0, os.path.join(ROOT, "tests"))
-    import oracle_lib as ol
-    from gpvmc_gb300 import _lib
-    u_phi = _lib.lib().gv_uniform_at(SEED, walker, 2, 0)
-    u_neel = _lib.lib().gv_uniform_at(SEED, walker, 2, 1)
+    import oracle_lib as ol   # the oracle's own Philox: no engine library in this process
+    u_phi = ol.uniform_at(SEED, walker, 2, 0)
+    u_neel = ol.uniform_at(SEED, walker, 2, 1)
     phi = PHI_RANGE[0] + (PHI_RANGE[1] - PHI_RANGE[0]) * u_phi
     neel = NEEL_RANGE[0] + (NEEL_RANGE[1] - NEEL_RANGE[0]) * u_neel
-    o = ol.OracleChain(L, phi, neel, seed=SEED, walker=walker)
+    o = ol.OracleChain(L, phi, neel, seed=SEED, walker=walker, timing_build=True)
     if o.random_start():
         return 0, 0.0
     t0 = time.perf_counter()
     o.walk(SWEEP * sweeps, meas=SWEEP if measure else 0, mask=ol.MEAS_PROJHEIS if measure else 0,
-           reinv_every=REINV)
+           reinv_every=reinv)
     return SWEEP * sweeps, time.perf_counter() - t0
 
 
-def cpu_baseline(cores, sweeps):
+def cpu_baseline(cores, sweeps, reinv=0):
+    """The reference's CPU path (its algorithm restated in C, the timing build)
+    on every host core: one single-threaded chain per core, concurrently, as
+    the reference runs one chain per MPI rank; no re-inversion (reinv = 0), as
+    the reference."""
     subprocess.run(["make", "-s", "-C", os.path.join(ROOT, "oracle"), "all"], check=True)
     ctx = mp.get_context("spawn")
     with ctx.Pool(cores) as pool:
         t0 = time.perf_counter()
-        res = pool.map(_cpu_chain, [(w, sweeps, True) for w in range(cores)])
+        res = pool.map(_cpu_chain, [(w, sweeps, True, reinv) for w in range(cores)])
         wall = time.perf_counter() - t0
     rates = [r[0] / r[1] for r in res if r[1] > 0]
     # chains run concurrently, one per core: aggregate = sum of per-chain rates
     return {"value": sum(rates), "unit": "steps/s", "cores": cores, "kind": "port",
             "per_core": statistics.mean(rates), "wall_s": wall,
-            "sample": "%d independent L=16 chains (one per core, walkers 0..%d of the workload), %d sweeps "
-                      "each with ProjHeis per sweep and re-inversion every 128 accepted moves" % (cores, cores - 1, sweeps)}
+            "sample": "%d independent L=16 chains (one per core, walkers 0..%d of the workload, the same Philox "
+                      "streams), %d sweeps each with ProjHeis per sweep, %s; oracle/vmc_oracle.c timing build "
+                      "(-O3, inline complex arithmetic)" % (cores, cores - 1, sweeps,
+                                                            "no re-inversion" if not reinv else
+                                                            "re-inversion every %d accepted moves" % reinv)}
 
 
 # ---------------------------------------------------------------------------
@@ -256,8 +268,12 @@ def run_gpu(g, precision, steps, warmup, rank, clocks_index=None, policy="drift"
 def run_e2e(g, precision, steps, rank):
     """Through the public API with host buffers: job creation (host tables ->
     device), host random start configurations -> device, FP64 LU start, then
-    each step one sweep and a device->host read of the per-walker results."""
+    each step one sweep and a device->host read of the per-walker results.
+    Bytes are the library's own count of the host<->device copies it issued
+    inside the timed region (gv_transfer_bytes)."""
     import numpy as np
+    from gpvmc_gb300 import _lib
+    h0, d0 = _lib.transfer_bytes()
     t0 = time.perf_counter()
     job = make_job(g, precision, rank)
     job.init_walkers()
@@ -267,14 +283,13 @@ def run_e2e(g, precision, steps, rank):
         pj, n = job.projheis()
         results.append(pj[:, 0].real / np.maximum(n, 1))
     wall = time.perf_counter() - t0
+    h1, d1 = _lib.transfer_bytes()
     job.close()
-    ns = L * L
-    h2d = (ns * (ns // 2) * (16 + 8) + WALKERS * 4 * ns * (16 + 8) + WALKERS * (2 * ns + 2 * ns // 2) * 2 + 4 * ns * 4
-           + 4 * ns * 4)
-    d2h = WALKERS * (2 * 16 + 4)
-    return {"value": WALKERS * SWEEP * steps / wall, "unit": "steps/s", "h2d_bytes_per_step": int(h2d / steps),
-            "d2h_bytes_per_step": d2h, "wall_s": wall,
-            "includes": "job creation + start upload + FP64 LU start amortised over the steps"}
+    return {"value": WALKERS * SWEEP * steps / wall, "unit": "steps/s", "h2d_bytes_per_step": (h1 - h0) // steps,
+            "d2h_bytes_per_step": (d1 - d0) // steps, "wall_s": wall,
+            "h2d_bytes": h1 - h0, "d2h_bytes": d1 - d0,
+            "includes": "job creation + start upload + FP64 LU start amortised over the steps; bytes counted "
+                        "by the library at every copy it issued"}
 
 
 # ---------------------------------------------------------------------------
@@ -352,7 +367,7 @@ def _cpu_exciton_chain(args):
     sys.path.insert(0, os.path.join(ROOT, "tests"))
     import oracle_lib as ol
     q = EXC_QS[walker % len(EXC_QS)]
-    o = ol.OracleChain(L, 0.25 * math.pi, 0.1, channel=ol.TRANS, q=q, seed=SEED, walker=walker)
+    o = ol.OracleChain(L, 0.25 * math.pi, 0.1, channel=ol.TRANS, q=q, seed=SEED, walker=walker, timing_build=True)
     if o.random_start():
         return 0, 0.0
     t0 = time.perf_counter()
@@ -420,7 +435,14 @@ def run_exciton(g, sweeps, fp64_sweeps):
             p_acc, p_ap = d[1] / d[0], (d[1] + d[3]) / d[0]
             N0, N1, Nexc, sz = L * L // 2 + 1, L * L // 2 - 1, L * L // 2, 8
             bytes_step = p_ap * (Nexc * N0 + N0 + N1 + Nexc) * sz + p_acc * 2 * (N0 * N0 + N1 * N1 + N0 * Nexc) * sz
-            achieved = bytes_step * d[0] / (wk * 1e-3) / 1e9
+            # complex MACs: Z = GupT^T C and the two row dots per proposal; per accepted move the
+            # rank-2 updates of both inverses (column product + two rank-1 passes) and of GupT
+            flops_step = 8.0 * (p_ap * (Nexc * N0 + N0 + N1 + Nexc) + p_acc * (3 * (N0 * N0 + N1 * N1) + 3 * N0 * Nexc))
+            launches = max(1, wn)
+            steps_launch = d[0] / launches
+            ms_launch = wk / launches
+            res_bytes = EXC_WALKERS * 2 * (N0 * N0 + N1 * N1 + N0 * Nexc) * sz   # on-chip state in and out
+            achieved = res_bytes / (ms_launch * 1e-3) / 1e9
             peak, kind = measured_peaks()
             # the same walk on the streaming kernel (inverses and overlap rows re-read from L2 / HBM)
             jst = g.Job(g.StagFluxTransExciton(L, 0.25 * math.pi, 0.1, q=(4, 4)), walkers=EXC_WALKERS, seed=SEED,
@@ -435,11 +457,21 @@ def run_exciton(g, sweeps, fp64_sweeps):
             sk, _ = jst.kernel_ms(0)
             ds = (jst.counts().sum(axis=0) - s0).astype(float)
             jst.close()
-            out["roofline"] = {"kernel": "k_walk_trans_res", "bound": "on-chip (TMEM / shared memory); achieved = "
-                               "the streaming algorithm's bytes per step / time, against HBM",
-                               "achieved": achieved, "peak": peak,
-                               "unit": "GB/s", "frac": achieved / peak, "peak_kind": kind, "bytes_per_step": bytes_step,
-                               "walk_ms_per_sweep": wk / max(1, wn), "kernel_steps_per_s": d[0] / (wk * 1e-3),
+            f32_peak, mhz = fp32_peak_tflops(None)
+            f32 = flops_step * steps_launch / (ms_launch * 1e-3) / 1e12
+            stream_gbs = bytes_step * steps_launch / (ms_launch * 1e-3) / 1e9
+            out["roofline"] = {"kernel": "k_walk_trans_res", "bound": "hbm", "achieved": achieved, "peak": peak,
+                               "unit": "GB/s", "frac": achieved / peak, "peak_kind": kind,
+                               "algorithmic_bytes_per_launch": res_bytes,
+                               "algorithmic_bytes_what": "both inverses and the overlap rows GupT loaded at launch "
+                                                         "entry and stored at exit (FP32)",
+                               "binding_resource": "on-chip latency (profiles/k_walk_trans_res_L16_512walkers.md: "
+                                                   "issue-active 36 %, DRAM 0.9 % of peak)",
+                               "fp32": {"achieved_tflops": f32, "peak_tflops": f32_peak, "frac": f32 / f32_peak,
+                                        "flops_per_step": flops_step},
+                               "streaming_equivalent": {"bytes_per_step": bytes_step, "gbs": stream_gbs,
+                                                        "over_hbm_peak": stream_gbs / peak},
+                               "walk_ms_per_launch": ms_launch, "kernel_steps_per_s": d[0] / (wk * 1e-3),
                                "streaming_kernel_steps_per_s": ds[0] / (sk * 1e-3),
                                "p_acc": p_acc, "p_ap": p_ap, "q": [4, 4], "walkers": EXC_WALKERS}
             # H / O accuracy of the mixed form against FP64 on the same configurations
@@ -668,6 +700,87 @@ def run_serving(g):
                     "with fresh FP64 inverses"}
 
 
+# DRAM bytes per walker per walk launch of k_walk_gs_res (inverses in at entry,
+# out at exit, plus tables), from the full-size ncu capture summarised in
+# profiles/k_walk_gs_res_L16_2048walkers_dram.md
+RES_DRAM_BYTES_PER_WALKER = 108.8e6 / 304
+
+
+def sm_count():
+    try:
+        import torch
+        return int(torch.cuda.get_device_properties(0).multi_processor_count)
+    except Exception:
+        return 152
+
+
+def fp32_peak_tflops(clocks):
+    """Nominal FP32 CUDA-core peak at the SM clock sampled during the timed
+    region: SMs x 128 FP32 lanes x 2 flops (FMA) x clock."""
+    mhz = (clocks or {}).get("sm_mhz")
+    if not mhz:
+        try:
+            with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+                mhz = float(json.load(f)["sm_max_mhz"])
+        except Exception:
+            mhz = 2070.0
+    return sm_count() * 128 * 2 * mhz * 1e6 / 1e12, mhz
+
+
+def walk_roofline(res, precision):
+    """Roofline of the dominant kernel, the walk.
+
+    The on-chip kernel (k_walk_gs_res, mixed, N <= 128) keeps both inverses in
+    tensor memory for the whole launch: its algorithmic HBM bytes are the two
+    FP32 inverses in at entry and out at exit, 2 * 2 * N^2 * 8 B per walker
+    per launch, and it is bound by on-chip latency (one walker per SM), not by
+    HBM: the report gives that HBM fraction, the FP32 CUDA-core fraction of
+    its algorithmic flops, and the streaming formulation's bytes per step
+    (what an HBM-resident walk would move) under its own name.
+    The streaming kernel (k_walk_gs: FP64, or mixed with stream_inverses)
+    moves p_ap * (2 * 2 * N * s) + p_acc * (2 * 3 * N^2 * s) bytes per step."""
+    N, s_b = L * L // 2, (8 if precision == "mixed" else 16)
+    nl = max(1, res["walk_launches"])
+    ms_launch = res["walk_ms"] / nl
+    steps_launch = res["steps"] / nl
+    p_ap, p_acc = res["p_ap"], res["p_acc"]
+    stream_bytes = p_ap * (2 * 2 * N * s_b) + p_acc * (2 * 3 * N * N * s_b)
+    flops_step = p_ap * 2 * 8 * N + p_acc * 2 * 16 * N * N
+    peak, peak_kind = measured_peaks()
+    resident = precision == "mixed" and N <= 128
+    if resident:
+        alg = WALKERS * 2 * 2 * N * N * 8.0
+        alg_what = "both FP32 inverses loaded at launch entry and stored at exit: 2 flavours x 2 x N^2 x 8 B per walker"
+    else:
+        alg = stream_bytes * steps_launch
+        alg_what = "streaming formulation: p_ap*(2*2*N*s) + p_acc*(2*3*N^2*s) per Metropolis step"
+    achieved = alg / (ms_launch * 1e-3) / 1e9
+    f32_peak, mhz = fp32_peak_tflops(res.get("clocks"))
+    f32 = flops_step * steps_launch / (ms_launch * 1e-3) / 1e12
+    roof = {"bound": "hbm", "kernel": "k_walk_gs_res" if resident else "k_walk_gs",
+            "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak, "peak_kind": peak_kind,
+            "traffic": RES_DRAM_BYTES_PER_WALKER * WALKERS if resident else None,
+            "algorithmic_bytes_per_launch": alg, "algorithmic_bytes_what": alg_what,
+            "kernel_ms_per_launch": ms_launch, "steps_per_launch": steps_launch,
+            "fp32": {"achieved_tflops": f32, "peak_tflops": f32_peak, "frac": f32 / f32_peak,
+                     "flops_per_step": flops_step,
+                     "flops_what": "p_ap*2*8N (two ratio dots) + p_acc*2*16N^2 (A^-1 u and the rank-1 update, "
+                                   "both flavours)",
+                     "peak_kind": "nominal: %d SMs x 128 FP32 lanes x 2 flops x %.0f MHz (median sampled SM clock)"
+                                  % (sm_count(), mhz)},
+            "streaming_equivalent": {"bytes_per_step": stream_bytes,
+                                     "gbs": stream_bytes * steps_launch / (ms_launch * 1e-3) / 1e9,
+                                     "over_hbm_peak": stream_bytes * steps_launch / (ms_launch * 1e-3) / 1e9 / peak,
+                                     "what": "bytes an HBM-streaming walk would move per step, per second of this "
+                                             "kernel: the speed-up over that formulation's HBM bound, not a "
+                                             "bandwidth drawn"}}
+    if resident:
+        roof["binding_resource"] = ("on-chip latency with one walker (8 warps) per SM: ncu issue-active 38.5 %, "
+                                    "FMA pipe 17.3 %, top stalls wait / short scoreboard "
+                                    "(profiles/k_walk_gs_res_L16_304walkers.md)")
+    return roof
+
+
 def main():
     global WALKERS
     ap = argparse.ArgumentParser()
@@ -697,11 +810,11 @@ def main():
         if rank != 0:
             return
         cores = os.cpu_count() or 1
-        v = cpu_baseline(cores, args.cpu_sweeps)
+        v = cpu_baseline(cores, args.cpu_sweeps, reinv=0)
         out = {"metric": METRIC, "impl": "reference", "value": v["value"], "unit": "steps/s", "n_gpus": args.gpus,
                "steps": args.steps, "warmup": args.warmup, "higher_is_better": True, "scaling": "weak",
                "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-               "config": workload_config("fp64", "always"),
+               "config": workload_config("fp64"),
                "cpu_baseline": {"value": v["value"], "unit": "steps/s", "cores": v["cores"], "kind": v["kind"],
                                 "sample": v["sample"]},
                "e2e": {"value": v["value"], "unit": "steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
@@ -711,7 +824,7 @@ def main():
     WALKERS = args.walkers
     cpu = cpu_exc = None
     if rank == 0 and world == 1 and not args.no_cpu:
-        cpu = cpu_baseline(os.cpu_count() or 1, args.cpu_sweeps)
+        cpu = cpu_baseline(os.cpu_count() or 1, args.cpu_sweeps, reinv=0)
         if not args.no_exciton:
             cpu_exc = cpu_exciton_baseline(os.cpu_count() or 1, 4)
 
@@ -764,33 +877,15 @@ def main():
 
     if rank != 0:
         return
-    # Roofline of the walk kernel (HBM bound): algorithmic bytes per Metropolis
-    # step = p_ap * (2 spins * 2 * N * s) [inverse row + orbital column] +
-    #        p_acc * (2 spins * 3 * N^2 * s) [A^-1 u read, A^-1 read + write]
-    N, s = L * L // 2, (8 if args.precision == "mixed" else 16)
-    bytes_step = res["p_ap"] * (2 * 2 * N * s) + res["p_acc"] * (2 * 3 * N * N * s)
-    per_launch_steps = res["steps"] / max(1, res["walk_launches"])
-    ms_launch = res["walk_ms"] / max(1, res["walk_launches"])
-    achieved = bytes_step * per_launch_steps / (ms_launch * 1e-3) / 1e9
-    peak, peak_kind = measured_peaks()
-    resident = args.precision == "mixed" and L * L // 2 <= 128
+    roof = walk_roofline(res, args.precision)
     out = {"metric": METRIC, "value": value, "unit": "steps/s", "n_gpus": world, "steps": args.steps,
            "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
            "vs_baseline": None, "dtype": "f32" if args.precision == "mixed" else "f64", "data": "synthetic",
-           "config": workload_config(args.precision, "drift"),
+           "config": workload_config(args.precision),
            "e2e": ({k: e2e[k] for k in ("value", "unit", "h2d_bytes_per_step", "d2h_bytes_per_step", "includes")}
                    if e2e else None),
            "gpu_launches": int(res["launches"]),
-           "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                        "frac": achieved / peak, "peak_kind": peak_kind,
-                        # DRAM bytes per walk launch from one ncu capture of the same kernel at
-                        # 304 walkers (profiles/), scaled by walkers: each walker's inverses are
-                        # loaded and stored once per launch
-                        "traffic": (108.8e6 * WALKERS / 304) if resident else None,
-                        "kernel": "k_walk_gs_res" if resident else "k_walk_gs", "bytes_per_step": bytes_step,
-                        "bytes_per_step_meaning": "HBM bytes the streaming formulation of a Metropolis step moves "
-                                                  "(inverse rows and columns, accepted-move read-modify-write)",
-                        "kernel_ms_per_launch": ms_launch},
+           "roofline": roof,
            "kernel_share": {"walk_ms": res["walk_ms"], "reinversion_ms": res["inv_ms"],
                             "reinversion_launches": res["inv_launches"], "total_ms": res["ms"]},
            "acceptance": {"p_acc": res["p_acc"], "p_ap": res["p_ap"], "reinversions": res["reinv"],

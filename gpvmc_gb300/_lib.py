@@ -81,6 +81,7 @@ _SIGS = {
     "gv_job_reset_quantities": [_P],
     "gv_job_read_drift_checks": [_P, ctypes.c_void_p, ctypes.c_void_p],
     "gv_job_set_wait_limit": [_P, ctypes.c_int32],
+    "gv_transfer_bytes": [ctypes.POINTER(ctypes.c_uint64), ctypes.POINTER(ctypes.c_uint64)],
     "gv_slater_invert_noalloc": [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int32, ctypes.c_void_p, ctypes.c_void_p],
     "gv_job_walk": [_P, ctypes.c_uint64, ctypes.c_uint64],
     "gv_job_walk_traced": [_P, ctypes.c_uint64, ctypes.c_uint64, ctypes.c_int32, ctypes.c_void_p],
@@ -160,6 +161,13 @@ def lib():
     L.gv_uniform_at.argtypes = [ctypes.c_uint64, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint64]
     _lib = L
     return L
+
+
+def transfer_bytes():
+    """(host->device, device->host) bytes the library has copied so far."""
+    h, d = ctypes.c_uint64(), ctypes.c_uint64()
+    check(lib().gv_transfer_bytes(ctypes.byref(h), ctypes.byref(d)), "gv_transfer_bytes")
+    return int(h.value), int(d.value)
 
 
 def check(status, where):

@@ -12,6 +12,7 @@
 // assembled in registers, so a proposal reads one inverse row per flavour
 // from HBM and the phase column from L2.
 #include <algorithm>
+#include <atomic>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -76,6 +77,28 @@ struct gv_job {
 namespace {
 
 thread_local const char* g_last_cuda_error = "";
+
+// Bytes this library copied host -> device and device -> host (every copy
+// goes through copy_async / copy_sync), for end-to-end accounting.
+std::atomic<uint64_t> g_bytes_h2d{0}, g_bytes_d2h{0};
+
+void count_copy(size_t n, cudaMemcpyKind k)
+{
+    if (k == cudaMemcpyHostToDevice) g_bytes_h2d += n;
+    else if (k == cudaMemcpyDeviceToHost) g_bytes_d2h += n;
+}
+
+cudaError_t copy_async(void* dst, const void* src, size_t n, cudaMemcpyKind k, cudaStream_t s)
+{
+    count_copy(n, k);
+    return cudaMemcpyAsync(dst, src, n, k, s);
+}
+
+cudaError_t copy_sync(void* dst, const void* src, size_t n, cudaMemcpyKind k)
+{
+    count_copy(n, k);
+    return cudaMemcpy(dst, src, n, k);
+}
 
 // Status for a failed CUDA call, remembering its message for gv_last_cuda_error.
 gv_status cuda_status(cudaError_t e)
@@ -529,10 +552,10 @@ gv_status upload_wav(gv_job* j, const std::vector<WavHost>& ws)
         cur[w] = ws[w].cur;
         sign[w] = ws[w].sign;
     }
-    GV_CK(cudaMemcpyAsync(j->d.wslot, slot.data(), slot.size() * sizeof(int16_t), cudaMemcpyHostToDevice, j->stream));
-    GV_CK(cudaMemcpyAsync(j->d.worb, orb.data(), orb.size() * sizeof(int16_t), cudaMemcpyHostToDevice, j->stream));
-    GV_CK(cudaMemcpyAsync(j->d.cur, cur.data(), W * sizeof(int32_t), cudaMemcpyHostToDevice, j->stream));
-    GV_CK(cudaMemcpyAsync(j->d.wsign, sign.data(), W * sizeof(int32_t), cudaMemcpyHostToDevice, j->stream));
+    GV_CK(copy_async(j->d.wslot, slot.data(), slot.size() * sizeof(int16_t), cudaMemcpyHostToDevice, j->stream));
+    GV_CK(copy_async(j->d.worb, orb.data(), orb.size() * sizeof(int16_t), cudaMemcpyHostToDevice, j->stream));
+    GV_CK(copy_async(j->d.cur, cur.data(), W * sizeof(int32_t), cudaMemcpyHostToDevice, j->stream));
+    GV_CK(copy_async(j->d.wsign, sign.data(), W * sizeof(int32_t), cudaMemcpyHostToDevice, j->stream));
     GV_CK(cudaStreamSynchronize(j->stream));
     return GV_OK;
 }
@@ -546,7 +569,7 @@ gv_status virt_update_trans(gv_job* j, int walker, int nset, const int32_t* hops
     double* dout = nullptr;
     GV_CK(cudaMalloc(&dh, sizeof(int32_t) * 4 * nset));
     if (cudaMalloc(&dout, sizeof(double) * nout)) { cudaFree(dh); return GV_ERR_OOM; }
-    cudaError_t e = cudaMemcpyAsync(dh, hops, sizeof(int32_t) * 4 * nset, cudaMemcpyHostToDevice, j->stream);
+    cudaError_t e = copy_async(dh, hops, sizeof(int32_t) * 4 * nset, cudaMemcpyHostToDevice, j->stream);
     const size_t sm = (j->cfg.precision == GV_PREC_FP64 ? sizeof(cx<double>) : sizeof(cx<float>)) * 2 * j->Nmax +
                       sizeof(double) * 6 * 4 + 16;
     if (!e) {
@@ -554,7 +577,7 @@ gv_status virt_update_trans(gv_job* j, int walker, int nset, const int32_t* hops
         else k_virt_trans<float, 128><<<nset, 128, sm, j->stream>>>(j->d, walker, nset, dh, dout);
         e = cudaGetLastError();
     }
-    if (!e) e = cudaMemcpyAsync(out, dout, sizeof(double) * nout, cudaMemcpyDeviceToHost, j->stream);
+    if (!e) e = copy_async(out, dout, sizeof(double) * nout, cudaMemcpyDeviceToHost, j->stream);
     if (!e) e = cudaStreamSynchronize(j->stream);
     cudaFree(dh);
     cudaFree(dout);
@@ -571,7 +594,7 @@ gv_status inverse_max_abs(gv_job* j, double* out)
     if (j->cfg.precision == GV_PREC_FP64) k_inverse_max_abs<double, 256><<<j->W, 256, 0, j->stream>>>(j->d, d);
     else k_inverse_max_abs<float, 256><<<j->W, 256, 0, j->stream>>>(j->d, d);
     cudaError_t e = cudaGetLastError();
-    if (!e) e = cudaMemcpyAsync(out, d, sizeof(double) * j->W, cudaMemcpyDeviceToHost, j->stream);
+    if (!e) e = copy_async(out, d, sizeof(double) * j->W, cudaMemcpyDeviceToHost, j->stream);
     if (!e) e = cudaStreamSynchronize(j->stream);
     cudaFree(d);
     ++j->total_launches;
@@ -590,7 +613,7 @@ gv_status trans_start(gv_job* j)
     GV_CK(cudaMalloc(&dov, sizeof(double) * size_t(W) * Nexc));
     std::vector<double> ov(size_t(W) * Nexc);
     gv_status st = trans_overlaps(j, dov);
-    if (!st && (cudaMemcpyAsync(ov.data(), dov, ov.size() * sizeof(double), cudaMemcpyDeviceToHost, j->stream) ||
+    if (!st && (copy_async(ov.data(), dov, ov.size() * sizeof(double), cudaMemcpyDeviceToHost, j->stream) ||
                 cudaStreamSynchronize(j->stream)))
         st = GV_ERR_CUDA;
     cudaFree(dov);
@@ -639,8 +662,8 @@ gv_status upload_configs(gv_job* j, const std::vector<int8_t>& up)
         }
         if (pc[0] != j->N[0] || pc[1] != j->N[1]) return GV_ERR_INVALID;
     }
-    GV_CK(cudaMemcpyAsync(j->d.fock, fock.data(), fock.size() * sizeof(int16_t), cudaMemcpyHostToDevice, j->stream));
-    GV_CK(cudaMemcpyAsync(j->d.part, part.data(), part.size() * sizeof(int16_t), cudaMemcpyHostToDevice, j->stream));
+    GV_CK(copy_async(j->d.fock, fock.data(), fock.size() * sizeof(int16_t), cudaMemcpyHostToDevice, j->stream));
+    GV_CK(copy_async(j->d.part, part.data(), part.size() * sizeof(int16_t), cudaMemcpyHostToDevice, j->stream));
     return GV_OK;
 }
 
@@ -842,6 +865,13 @@ double gv_uniform_at(uint64_t seed, uint32_t walker, uint32_t stream, uint64_t k
 
 const char* gv_last_cuda_error(void) { return g_last_cuda_error; }
 
+gv_status gv_transfer_bytes(uint64_t* h2d, uint64_t* d2h)
+{
+    if (h2d) *h2d = g_bytes_h2d.load();
+    if (d2h) *d2h = g_bytes_d2h.load();
+    return GV_OK;
+}
+
 const char* gv_status_string(gv_status s)
 {
     switch (s) {
@@ -1025,16 +1055,16 @@ gv_status gv_job_create(const gv_job_config* cfg, gv_job** out)
         if (trans_z_tc_ok(j) && (st = dalloc(j, &d.zbuf, size_t(j->W) * j->N[1] * Nexc * sizeof(cx<float>))))
             return fail(st);
         d.exc_up = eu; d.exc_dn = ed;
-        if (cudaMemcpyAsync(eu, j->exu.data(), Nexc * sizeof(int16_t), cudaMemcpyHostToDevice, j->stream) ||
-            cudaMemcpyAsync(ed, j->exd.data(), Nexc * sizeof(int16_t), cudaMemcpyHostToDevice, j->stream))
+        if (copy_async(eu, j->exu.data(), Nexc * sizeof(int16_t), cudaMemcpyHostToDevice, j->stream) ||
+            copy_async(ed, j->exd.data(), Nexc * sizeof(int16_t), cudaMemcpyHostToDevice, j->stream))
             return fail(GV_ERR_CUDA);
     }
-    if (cudaMemcpyAsync(nbr, j->lat.nbr.data(), sizeof(int32_t) * 4 * j->Ns, cudaMemcpyHostToDevice, j->stream) ||
-        cudaMemcpyAsync(edg, edges.data(), edges.size() * sizeof(int32_t), cudaMemcpyHostToDevice, j->stream) ||
-        cudaMemcpyAsync(p64, ph64.data(), ph64.size() * sizeof(cx<double>), cudaMemcpyHostToDevice, j->stream) ||
-        cudaMemcpyAsync(p32, ph32.data(), ph32.size() * sizeof(cx<float>), cudaMemcpyHostToDevice, j->stream) ||
-        cudaMemcpyAsync(c64, cf64.data(), cf64.size() * sizeof(cx<double>), cudaMemcpyHostToDevice, j->stream) ||
-        cudaMemcpyAsync(c32, cf32.data(), cf32.size() * sizeof(cx<float>), cudaMemcpyHostToDevice, j->stream) ||
+    if (copy_async(nbr, j->lat.nbr.data(), sizeof(int32_t) * 4 * j->Ns, cudaMemcpyHostToDevice, j->stream) ||
+        copy_async(edg, edges.data(), edges.size() * sizeof(int32_t), cudaMemcpyHostToDevice, j->stream) ||
+        copy_async(p64, ph64.data(), ph64.size() * sizeof(cx<double>), cudaMemcpyHostToDevice, j->stream) ||
+        copy_async(p32, ph32.data(), ph32.size() * sizeof(cx<float>), cudaMemcpyHostToDevice, j->stream) ||
+        copy_async(c64, cf64.data(), cf64.size() * sizeof(cx<double>), cudaMemcpyHostToDevice, j->stream) ||
+        copy_async(c32, cf32.data(), cf32.size() * sizeof(cx<float>), cudaMemcpyHostToDevice, j->stream) ||
         cudaStreamSynchronize(j->stream))
         return fail(GV_ERR_CUDA);
     *out = j;
@@ -1125,8 +1155,8 @@ gv_status gv_job_read_drift_checks(gv_job* j, double* drift, uint64_t* checks)
 {
     if (!j) return GV_ERR_INVALID;
     GV_CK(cudaStreamSynchronize(j->stream));
-    if (drift) GV_CK(cudaMemcpy(drift, j->d.drift_seen, sizeof(double) * j->W, cudaMemcpyDeviceToHost));
-    if (checks) GV_CK(cudaMemcpy(checks, j->d.checks, sizeof(uint64_t) * j->W, cudaMemcpyDeviceToHost));
+    if (drift) GV_CK(copy_sync(drift, j->d.drift_seen, sizeof(double) * j->W, cudaMemcpyDeviceToHost));
+    if (checks) GV_CK(copy_sync(checks, j->d.checks, sizeof(uint64_t) * j->W, cudaMemcpyDeviceToHost));
     return GV_OK;
 }
 
@@ -1170,7 +1200,7 @@ gv_status gv_job_init_walkers(gv_job* j, const int8_t* up)
         if (st) return st;
         st = invert_all(j);
         if (st) return st;
-        GV_CK(cudaMemcpyAsync(status.data(), j->d.status, sizeof(int32_t) * W, cudaMemcpyDeviceToHost, j->stream));
+        GV_CK(copy_async(status.data(), j->d.status, sizeof(int32_t) * W, cudaMemcpyDeviceToHost, j->stream));
         GV_CK(cudaStreamSynchronize(j->stream));
         bool again = false;
         for (int w = 0; w < W; ++w)
@@ -1321,7 +1351,7 @@ gv_status gv_job_walk_traced(gv_job* j, uint64_t len, uint64_t meas, int32_t wal
     GV_CK(cudaMalloc(&dt, sizeof(gv_trace) * (len ? len : 1)));
     gv_status st = walk_impl(j, len, meas, dt, walker);
     if (!st) {
-        if (cudaMemcpyAsync(trace, dt, sizeof(gv_trace) * len, cudaMemcpyDeviceToHost, j->stream) ||
+        if (copy_async(trace, dt, sizeof(gv_trace) * len, cudaMemcpyDeviceToHost, j->stream) ||
             cudaStreamSynchronize(j->stream))
             st = GV_ERR_CUDA;
     }
@@ -1337,7 +1367,7 @@ gv_status gv_job_synchronize(gv_job* j)
     if (cudaEventElapsedTime(&ms, j->ev0, j->ev1) == cudaSuccess) j->last_ms = ms;
     else cudaGetLastError();   // no walk recorded yet: clear the (non-sticky) error
     std::vector<int32_t> status(j->W);
-    GV_CK(cudaMemcpy(status.data(), j->d.status, sizeof(int32_t) * j->W, cudaMemcpyDeviceToHost));
+    GV_CK(copy_sync(status.data(), j->d.status, sizeof(int32_t) * j->W, cudaMemcpyDeviceToHost));
     for (int32_t s : status)
         if (s) return s;
     return GV_OK;
@@ -1423,7 +1453,7 @@ gv_status gv_job_drift(gv_job* j, double* out)
     if (j->cfg.precision == GV_PREC_FP64) k_drift<double, 256><<<dim3(j->W, 2), 256, 0, j->stream>>>(j->d, d);
     else k_drift<float, 256><<<dim3(j->W, 2), 256, 0, j->stream>>>(j->d, d);
     cudaError_t e = cudaGetLastError();
-    if (!e) e = cudaMemcpyAsync(out, d, sizeof(double) * 2 * j->W, cudaMemcpyDeviceToHost, j->stream);
+    if (!e) e = copy_async(out, d, sizeof(double) * 2 * j->W, cudaMemcpyDeviceToHost, j->stream);
     if (!e) e = cudaStreamSynchronize(j->stream);
     cudaFree(d);
     return cuda_status(e);
@@ -1441,7 +1471,7 @@ gv_status gv_job_virt_update(gv_job* j, int32_t walker, int32_t nset, const int3
     double* dout = nullptr;
     GV_CK(cudaMalloc(&dh, sizeof(int32_t) * 4 * nset));
     if (cudaMalloc(&dout, sizeof(double) * 2 * nset)) { cudaFree(dh); return GV_ERR_OOM; }
-    cudaError_t e = cudaMemcpyAsync(dh, hops, sizeof(int32_t) * 4 * nset, cudaMemcpyHostToDevice, j->stream);
+    cudaError_t e = copy_async(dh, hops, sizeof(int32_t) * 4 * nset, cudaMemcpyHostToDevice, j->stream);
     const int per = 4;
     if (!e) {
         if (j->cfg.precision == GV_PREC_FP64)
@@ -1450,7 +1480,7 @@ gv_status gv_job_virt_update(gv_job* j, int32_t walker, int32_t nset, const int3
             k_virt_update<float><<<(nset + per - 1) / per, 32 * per, 0, j->stream>>>(j->d, walker, nset, dh, dout);
         e = cudaGetLastError();
     }
-    if (!e) e = cudaMemcpyAsync(out, dout, sizeof(double) * 2 * nset, cudaMemcpyDeviceToHost, j->stream);
+    if (!e) e = copy_async(out, dout, sizeof(double) * 2 * nset, cudaMemcpyDeviceToHost, j->stream);
     if (!e) e = cudaStreamSynchronize(j->stream);
     cudaFree(dh);
     cudaFree(dout);
@@ -1462,7 +1492,7 @@ gv_status gv_job_read_config(gv_job* j, int8_t* up)
     if (!j || !up) return GV_ERR_INVALID;
     GV_CK(cudaStreamSynchronize(j->stream));
     std::vector<int16_t> fock(size_t(j->W) * 2 * j->Ns);
-    GV_CK(cudaMemcpy(fock.data(), j->d.fock, fock.size() * sizeof(int16_t), cudaMemcpyDeviceToHost));
+    GV_CK(copy_sync(fock.data(), j->d.fock, fock.size() * sizeof(int16_t), cudaMemcpyDeviceToHost));
     for (int w = 0; w < j->W; ++w)
         for (int v = 0; v < j->Ns; ++v) up[size_t(w) * j->Ns + v] = fock[size_t(w) * 2 * j->Ns + v] >= 0 ? 1 : 0;
     return GV_OK;
@@ -1473,7 +1503,7 @@ gv_status gv_job_read_particles(gv_job* j, int32_t walker, int32_t fl, int32_t* 
     if (!j || !out || walker < 0 || walker >= j->W || fl < 0 || fl > 1) return GV_ERR_INVALID;
     GV_CK(cudaStreamSynchronize(j->stream));
     std::vector<int16_t> part(j->Nmax);
-    GV_CK(cudaMemcpy(part.data(), j->d.part + (size_t(walker) * 2 + fl) * j->Nmax, sizeof(int16_t) * j->Nmax,
+    GV_CK(copy_sync(part.data(), j->d.part + (size_t(walker) * 2 + fl) * j->Nmax, sizeof(int16_t) * j->Nmax,
                      cudaMemcpyDeviceToHost));
     for (int p = 0; p < j->N[fl]; ++p) out[p] = part[p];
     return GV_OK;
@@ -1485,9 +1515,9 @@ gv_status gv_job_read_amplitude(gv_job* j, double* mant, int32_t* exp10)
     GV_CK(cudaStreamSynchronize(j->stream));
     std::vector<cx<double>> m(j->W);
     std::vector<int32_t> e(j->W), sg(j->W, 1);
-    GV_CK(cudaMemcpy(m.data(), j->d.amp_m, sizeof(cx<double>) * j->W, cudaMemcpyDeviceToHost));
-    GV_CK(cudaMemcpy(e.data(), j->d.amp_e, sizeof(int32_t) * j->W, cudaMemcpyDeviceToHost));
-    if (j->trans) GV_CK(cudaMemcpy(sg.data(), j->d.wsign, sizeof(int32_t) * j->W, cudaMemcpyDeviceToHost));
+    GV_CK(copy_sync(m.data(), j->d.amp_m, sizeof(cx<double>) * j->W, cudaMemcpyDeviceToHost));
+    GV_CK(copy_sync(e.data(), j->d.amp_e, sizeof(int32_t) * j->W, cudaMemcpyDeviceToHost));
+    if (j->trans) GV_CK(copy_sync(sg.data(), j->d.wsign, sizeof(int32_t) * j->W, cudaMemcpyDeviceToHost));
     for (int w = 0; w < j->W; ++w) m[w] = m[w] * double(sg[w]);   // SlaterDeterminant::Amp (SlaterDeterminant.cpp:94)
     for (int w = 0; w < j->W; ++w) {
         const double a = std::hypot(m[w].x, m[w].y);
@@ -1512,11 +1542,11 @@ gv_status gv_job_read_inverse(gv_job* j, int32_t walker, int32_t fl, double* out
     const size_t n = size_t(N) * N;
     // AiT[f][p] = (A^-1)(p, f) is the reference's column-major m_mati[p + f*N].
     if (j->cfg.precision == GV_PREC_FP64) {
-        GV_CK(cudaMemcpy(out, static_cast<cx<double>*>(j->d.Ai[fl]) + size_t(walker) * n, n * sizeof(cx<double>),
+        GV_CK(copy_sync(out, static_cast<cx<double>*>(j->d.Ai[fl]) + size_t(walker) * n, n * sizeof(cx<double>),
                          cudaMemcpyDeviceToHost));
     } else {
         std::vector<cx<float>> a(n);
-        GV_CK(cudaMemcpy(a.data(), static_cast<cx<float>*>(j->d.Ai[fl]) + size_t(walker) * n, n * sizeof(cx<float>),
+        GV_CK(copy_sync(a.data(), static_cast<cx<float>*>(j->d.Ai[fl]) + size_t(walker) * n, n * sizeof(cx<float>),
                          cudaMemcpyDeviceToHost));
         for (size_t i = 0; i < n; ++i) { out[2 * i] = a[i].x; out[2 * i + 1] = a[i].y; }
     }
@@ -1527,7 +1557,7 @@ gv_status gv_job_read_counts(gv_job* j, uint64_t* counts)
 {
     if (!j || !counts) return GV_ERR_INVALID;
     GV_CK(cudaStreamSynchronize(j->stream));
-    GV_CK(cudaMemcpy(counts, j->d.counts, sizeof(uint64_t) * 5 * j->W, cudaMemcpyDeviceToHost));
+    GV_CK(copy_sync(counts, j->d.counts, sizeof(uint64_t) * 5 * j->W, cudaMemcpyDeviceToHost));
     return GV_OK;
 }
 
@@ -1539,7 +1569,7 @@ gv_status gv_job_read_state_index(gv_job* j, int32_t* state)
         return GV_OK;
     }
     GV_CK(cudaStreamSynchronize(j->stream));
-    GV_CK(cudaMemcpy(state, j->d.cur, sizeof(int32_t) * j->W, cudaMemcpyDeviceToHost));
+    GV_CK(copy_sync(state, j->d.cur, sizeof(int32_t) * j->W, cudaMemcpyDeviceToHost));
     return GV_OK;
 }
 
@@ -1548,11 +1578,11 @@ gv_status gv_job_read_projheis(gv_job* j, double* vals, int32_t* nmeas)
     if (!j || !vals) return GV_ERR_INVALID;
     GV_CK(cudaStreamSynchronize(j->stream));
     if (j->trans)
-        GV_CK(cudaMemcpy(vals, j->d.pjx, sizeof(cx<double>) * 2 * size_t(j->W) * j->ch.Nexc * j->ch.Nexc,
+        GV_CK(copy_sync(vals, j->d.pjx, sizeof(cx<double>) * 2 * size_t(j->W) * j->ch.Nexc * j->ch.Nexc,
                          cudaMemcpyDeviceToHost));
     else
-        GV_CK(cudaMemcpy(vals, j->d.pj, sizeof(cx<double>) * 2 * j->W, cudaMemcpyDeviceToHost));
-    if (nmeas) GV_CK(cudaMemcpy(nmeas, j->d.pj_n, sizeof(int32_t) * j->W, cudaMemcpyDeviceToHost));
+        GV_CK(copy_sync(vals, j->d.pj, sizeof(cx<double>) * 2 * j->W, cudaMemcpyDeviceToHost));
+    if (nmeas) GV_CK(copy_sync(nmeas, j->d.pj_n, sizeof(int32_t) * j->W, cudaMemcpyDeviceToHost));
     return GV_OK;
 }
 
@@ -1565,7 +1595,7 @@ gv_status gv_job_read_orbitals(gv_job* j, int32_t walker, int32_t fl, int32_t* o
     }
     GV_CK(cudaStreamSynchronize(j->stream));
     std::vector<int16_t> o(j->Nmax);
-    GV_CK(cudaMemcpy(o.data(), j->d.worb + (size_t(walker) * 2 + fl) * j->Nmax, sizeof(int16_t) * j->Nmax,
+    GV_CK(copy_sync(o.data(), j->d.worb + (size_t(walker) * 2 + fl) * j->Nmax, sizeof(int16_t) * j->Nmax,
                      cudaMemcpyDeviceToHost));
     for (int f = 0; f < j->N[fl]; ++f) orb[f] = o[f];
     return GV_OK;
@@ -1575,7 +1605,7 @@ gv_status gv_job_read_status(gv_job* j, int32_t* status)
 {
     if (!j || !status) return GV_ERR_INVALID;
     GV_CK(cudaStreamSynchronize(j->stream));
-    GV_CK(cudaMemcpy(status, j->d.status, sizeof(int32_t) * j->W, cudaMemcpyDeviceToHost));
+    GV_CK(copy_sync(status, j->d.status, sizeof(int32_t) * j->W, cudaMemcpyDeviceToHost));
     return GV_OK;
 }
 
@@ -1587,7 +1617,7 @@ gv_status gv_job_read_weight(gv_job* j, double* sigma)
         return GV_OK;
     }
     GV_CK(cudaStreamSynchronize(j->stream));
-    GV_CK(cudaMemcpy(sigma, j->d.sigma, sizeof(double) * j->W, cudaMemcpyDeviceToHost));
+    GV_CK(copy_sync(sigma, j->d.sigma, sizeof(double) * j->W, cudaMemcpyDeviceToHost));
     return GV_OK;
 }
 
@@ -1595,8 +1625,8 @@ gv_status gv_job_read_stagmagn(gv_job* j, double* vals, int32_t* nmeas)
 {
     if (!j || !vals) return GV_ERR_INVALID;
     GV_CK(cudaStreamSynchronize(j->stream));
-    GV_CK(cudaMemcpy(vals, j->d.sm, sizeof(cx<double>) * j->W, cudaMemcpyDeviceToHost));
-    if (nmeas) GV_CK(cudaMemcpy(nmeas, j->d.sm_n, sizeof(int32_t) * j->W, cudaMemcpyDeviceToHost));
+    GV_CK(copy_sync(vals, j->d.sm, sizeof(cx<double>) * j->W, cudaMemcpyDeviceToHost));
+    if (nmeas) GV_CK(copy_sync(nmeas, j->d.sm_n, sizeof(int32_t) * j->W, cudaMemcpyDeviceToHost));
     return GV_OK;
 }
 
@@ -1612,8 +1642,8 @@ gv_status gv_job_read_statspin(gv_job* j, double* vals, int32_t* nmeas)
     GV_CK(cudaStreamSynchronize(j->stream));
     const size_t Ns = size_t(j->Ns), n2 = Ns * Ns;
     std::vector<double> raw(3 * n2);
-    GV_CK(cudaMemcpy(raw.data(), j->d.ss, sizeof(double) * 3 * n2, cudaMemcpyDeviceToHost));
-    if (nmeas) GV_CK(cudaMemcpy(nmeas, j->d.ss_n, sizeof(int32_t), cudaMemcpyDeviceToHost));
+    GV_CK(copy_sync(raw.data(), j->d.ss, sizeof(double) * 3 * n2, cudaMemcpyDeviceToHost));
+    if (nmeas) GV_CK(copy_sync(nmeas, j->d.ss_n, sizeof(int32_t), cudaMemcpyDeviceToHost));
     const double* T = raw.data();
     const double* Aud = raw.data() + 2 * n2;
     std::vector<double> u(Ns, 0.0), dn(Ns, 0.0);
@@ -1781,9 +1811,9 @@ gv_status gv_job_read_tracks(gv_job* j, double* stagmagn, double* log10_weight, 
             for (int w = 0; w < j->W; ++w) n[w] = 0;
         return GV_OK;
     }
-    if (stagmagn) GV_CK(cudaMemcpy(stagmagn, j->d.track_sm, m * sizeof(double), cudaMemcpyDeviceToHost));
-    if (log10_weight) GV_CK(cudaMemcpy(log10_weight, j->d.track_lw, m * sizeof(double), cudaMemcpyDeviceToHost));
-    if (n) GV_CK(cudaMemcpy(n, j->d.track_n, sizeof(int32_t) * j->W, cudaMemcpyDeviceToHost));
+    if (stagmagn) GV_CK(copy_sync(stagmagn, j->d.track_sm, m * sizeof(double), cudaMemcpyDeviceToHost));
+    if (log10_weight) GV_CK(copy_sync(log10_weight, j->d.track_lw, m * sizeof(double), cudaMemcpyDeviceToHost));
+    if (n) GV_CK(copy_sync(n, j->d.track_n, sizeof(int32_t) * j->W, cudaMemcpyDeviceToHost));
     return GV_OK;
 }
 
@@ -1812,7 +1842,7 @@ gv_status gv_job_checkpoint(gv_job* j, int32_t flags, void* buf, uint64_t capaci
     unsigned char* out = static_cast<unsigned char*>(buf);
     unsigned char* p = out + sizeof(CkptHeader);
     for (const CkptSection& s : ckpt_sections(j, flags & GV_CKPT_INVERSES)) {
-        GV_CK(cudaMemcpyAsync(p, s.dev, s.bytes, cudaMemcpyDeviceToHost, j->stream));
+        GV_CK(copy_async(p, s.dev, s.bytes, cudaMemcpyDeviceToHost, j->stream));
         p += s.bytes;
     }
     GV_CK(cudaStreamSynchronize(j->stream));
@@ -1841,7 +1871,7 @@ gv_status gv_job_restore(gv_job* j, const void* buf, uint64_t size)
         return GV_ERR_INVALID;
     GV_CK(cudaStreamSynchronize(j->stream));
     for (const CkptSection& s : secs) {
-        GV_CK(cudaMemcpyAsync(s.dev, in, s.bytes, cudaMemcpyHostToDevice, j->stream));
+        GV_CK(copy_async(s.dev, in, s.bytes, cudaMemcpyHostToDevice, j->stream));
         in += s.bytes;
     }
     // The pageable source must outlive the copies: wait before returning.

@@ -362,6 +362,12 @@ double gv_uniform_at(uint64_t seed, uint32_t walker, uint32_t stream, uint64_t k
 #define GV_NOALLOC_MAX_N 128
 gv_status gv_slater_invert_noalloc(const double* d_A, double* d_Ai, int32_t N, double* d_info, void* stream);
 
+/* Bytes this library has copied host -> device and device -> host since the
+ * process loaded it (all jobs and threads), counted at every copy it issues:
+ * end-to-end accounting of what a workload moves over the host link.  No
+ * counterpart in the reference (a CPU program). */
+gv_status gv_transfer_bytes(uint64_t* h2d, uint64_t* d2h);
+
 /* Library version string. */
 const char* gv_version(void);
 /* Message for a status code. */

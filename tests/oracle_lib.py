@@ -20,6 +20,8 @@ import numpy as np
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 ORACLE_SO = os.path.join(ROOT, "oracle", "_build", "liboracle.so")
+# the same source built for timing (-O3, inline complex arithmetic): CPU-baseline legs only
+ORACLE_FAST_SO = os.path.join(ROOT, "oracle", "_build", "liboracle_fast.so")
 REF_SO = os.path.join(ROOT, "oracle", "_ref", "libgpvmc_ref.so")
 
 GROUNDSTATE, TRANS, LONG = 0, 1, 2
@@ -231,8 +233,8 @@ class _Chain:
 
 class OracleChain(_Chain):
     def __init__(self, L, phi, neel, neel_exp=0.0, bc=(1.0, 1.0), channel=GROUNDSTATE, q=(0, 0),
-                 seed=1234, walker=0):
-        self.lib = _load(ORACLE_SO, "orc")
+                 seed=1234, walker=0, timing_build=False):
+        self.lib = _load(ORACLE_FAST_SO if timing_build else ORACLE_SO, "orc")
         st = ctypes.c_int()
         self.job = self.lib.orc_job_create(L, phi, neel, neel_exp, bc[0], bc[1], channel, q[0], q[1],
                                            ctypes.byref(st))

@@ -22,18 +22,53 @@ def _pair(engine, oracle, L, neel, seed=1234, walkers=1, reinv=0, precision="fp6
     return job, orc
 
 
-def _compare_traces(tg, to):
+def exact_ratio(fresh_chain, i, v1, v2):
+    """The Metropolis ratio of step i from a freshly inverted FP64 state: a new
+    oracle chain replayed to step i and re-inverted from its configuration
+    (SlaterDeterminant::Init), then VirtUpdate of the exchange v1 <-> v2 and of
+    no move: sum_k |q_k(moved)|^2 / sum_k |q_k(current)|^2 over the channel
+    states (one state for the ground state)."""
+    o = fresh_chain()
+    if i:
+        o.walk(i)
+    assert o.reinit() == 0
+    up = o.config().astype(bool)
+    u, d = (v1, v2) if up[v1] else (v2, v1)
+    qm, qe = o.virt_update(np.array([(u, d, d, u), (-1, -1, -1, -1)], dtype=np.int32))
+    top = int(qe.max())
+    w = (np.abs(qm) ** 2 * 100.0 ** (qe - top).astype(float)).sum(axis=0)
+    return float(w[0] / w[1])
+
+
+def check_ratios(tg, to, fresh_chain=None):
+    """Ratios to 1e-10 relative (absolute floor 1e-13: ratios that vanish by
+    symmetry are rounding noise in both codes).  Where the engine and the
+    oracle differ by more, both running inverses carry the FP64
+    Sherman-Morrison drift of their own rounding (at L = 16 the oracle's
+    running inverse sits up to ~5e-11 relative from a fresh inversion after a
+    few hundred accepted moves); the engine's ratio must then be no further
+    from the exact one -- the same step from a freshly inverted state -- than
+    the oracle's, up to 1e-10 relative."""
+    real = np.flatnonzero(to["kind"] == 1)
+    err = np.abs(tg["ratio"][real] - to["ratio"][real])
+    bad = real[err > RTOL * np.abs(to["ratio"][real]) + 1e-13]
+    if len(bad) and fresh_chain is not None:
+        keep = []
+        for i in bad[:20]:
+            ex = exact_ratio(fresh_chain, int(i), int(to["v1"][i]), int(to["v2"][i]))
+            if abs(tg["ratio"][i] - ex) > abs(to["ratio"][i] - ex) + RTOL * abs(ex) + 1e-13:
+                keep.append(i)
+        bad = np.array(keep + list(bad[20:]), dtype=np.int64)
+    assert not len(bad), (bad[:5], to["ratio"][bad][:5], tg["ratio"][bad][:5])
+
+
+def _compare_traces(tg, to, fresh_chain=None):
     assert (tg["v1"] == to["v1"]).all()
     assert (tg["v2"] == to["v2"]).all()
     assert (tg["kind"] == to["kind"]).all()
     tie = np.abs(to["u"][:, 3] - to["ratio"]) < 1e-9
     assert ((tg["accepted"] == to["accepted"]) | tie).all()
-    real = to["kind"] == 1
-    # ratios that vanish by symmetry are rounding noise in both codes: the
-    # absolute floor 1e-13 is far below any ratio a uniform can accept
-    err = np.abs(tg["ratio"][real] - to["ratio"][real])
-    bad = err > RTOL * np.abs(to["ratio"][real]) + 1e-13
-    assert not bad.any(), (to["ratio"][real][bad][:5], tg["ratio"][real][bad][:5])
+    check_ratios(tg, to, fresh_chain)
     assert (tg["u4"] == to["u"][:, 3]).all()
     return int(tie.sum())
 
@@ -60,7 +95,12 @@ def test_trace_parity(engine, oracle, L, neel, steps):
     orc.random_start()
     tg = job.walk_traced(steps, 0)
     to = orc.walk(steps, trace=True)
-    _compare_traces(tg, to)
+
+    def fresh():
+        o = oracle.OracleChain(L, PHI, neel, seed=77, walker=0)
+        o.random_start()
+        return o
+    _compare_traces(tg, to, fresh)
     assert (job.config()[0] == orc.config()).all()
     m, e = job.amplitude()
     om, oe = orc.amp()
@@ -86,7 +126,13 @@ def test_measurements_parity(engine, oracle, L, therm, nmeas):
     orc.walk(therm * L * L)
     tg = job.walk_traced(L * L * nmeas, L * L)
     to = orc.walk(L * L * nmeas, meas=L * L, mask=7, trace=True)
-    _compare_traces(tg, to)
+
+    def fresh():
+        o = oracle.OracleChain(L, PHI, neel, seed=5, walker=0)
+        o.random_start()
+        o.walk(therm * L * L)
+        return o
+    _compare_traces(tg, to, fresh)
     assert (job.config()[0] == orc.config()).all()
     pj, n = job.projheis()
     opj, on = orc.projheis()
