@@ -82,6 +82,12 @@ _SIGS = {
     "gv_job_read_drift_checks": [_P, ctypes.c_void_p, ctypes.c_void_p],
     "gv_job_set_wait_limit": [_P, ctypes.c_int32],
     "gv_transfer_bytes": [ctypes.POINTER(ctypes.c_uint64), ctypes.POINTER(ctypes.c_uint64)],
+    "gv_job_trystep": [_P, ctypes.c_int32, ctypes.c_void_p, ctypes.POINTER(ctypes.c_double),
+                       ctypes.POINTER(ctypes.c_int32), ctypes.POINTER(ctypes.c_int32)],
+    "gv_job_yesno": [_P, ctypes.c_int32, ctypes.c_double, ctypes.POINTER(ctypes.c_int32)],
+    "gv_job_step": [_P, ctypes.c_int32],
+    "gv_job_update": [_P, ctypes.c_int32, ctypes.c_void_p, ctypes.c_int32],
+    "gv_job_stepper_weight": [_P, ctypes.c_int32, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_int32)],
     "gv_slater_invert_noalloc": [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int32, ctypes.c_void_p, ctypes.c_void_p],
     "gv_job_walk": [_P, ctypes.c_uint64, ctypes.c_uint64],
     "gv_job_walk_traced": [_P, ctypes.c_uint64, ctypes.c_uint64, ctypes.c_int32, ctypes.c_void_p],

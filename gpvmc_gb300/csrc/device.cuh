@@ -189,6 +189,13 @@ struct DevJob {
     cx<double>* pjx;           // W*2*Nexc*Nexc ProjHeis H and O sums
     cx<float>* zbuf;           // W*N1*Nexc tensor-core Z[d][k] = sum_f GupT[f][k] phi_f(d) (mixed, or null)
     int wait_limit;            // polls before a bounded mbarrier wait of the tensor-core kernels gives up
+    // Single-walker stepping (gv_job_trystep / gv_job_step, LatticeStepper::trystep / step):
+    // when forced_walker >= 0 the streaming walk kernels run that walker only, take the
+    // proposal (forced_v1, forced_v2) instead of drawing it and leave its Philox position
+    // alone; forced_accept = 1 applies the move (LatticeStepper::step), 0 only evaluates it
+    // into the trace record and writes nothing back; forced_khop >= 0 picks that channel
+    // state instead of the arg-max.
+    int forced_walker, forced_v1, forced_v2, forced_accept, forced_khop;
 };
 
 // Amplitude kept as (complex mantissa, base-2 exponent); renormalised

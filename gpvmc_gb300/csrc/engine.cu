@@ -72,6 +72,11 @@ struct gv_job {
     bool graphs_off = false;
     int64_t graph_replays = 0;
     std::vector<int16_t> exu, exd;       // channel tables (Channel::exc_up / exc_dn)
+    // single-walker stepping: the proposal gv_job_trystep evaluated, waiting for gv_job_step
+    struct Pending {
+        int w = -1, v1 = 0, v2 = 0, khop = -1;
+    } pend;
+    gv_trace* step_trace = nullptr;      // device record of a single-walker step
 };
 
 namespace {
@@ -1001,6 +1006,7 @@ gv_status gv_job_create(const gv_job_config* cfg, gv_job** out)
     d.seed = cfg->seed; d.walker_base = cfg->walker_base; d.reinv_every = cfg->reinv_every;
     d.trace = nullptr; d.trace_walker = -1;
     d.wait_limit = kTcWaitLimit;
+    d.forced_walker = -1; d.forced_v1 = d.forced_v2 = 0; d.forced_accept = 0; d.forced_khop = -1;
     const size_t es = cfg->precision == GV_PREC_FP64 ? sizeof(cx<double>) : sizeof(cx<float>);
     gv_status st = GV_OK;
     int32_t *nbr = nullptr, *edg = nullptr;
@@ -1357,6 +1363,162 @@ gv_status gv_job_walk_traced(gv_job* j, uint64_t len, uint64_t meas, int32_t wal
     }
     cudaFree(dt);
     return st ? st : gv_job_synchronize(j);
+}
+
+// ---- Single-walker stepping: LatticeStepper::trystep / step, MetroMC::YesNo ----
+// One streaming walk launch that runs walker w only, on the given proposal
+// (v1, v2): accept = 0 evaluates it (ratio and arg-max channel state into
+// *rec) and changes nothing; accept = 1 applies it with channel state khop
+// (-1: the arg-max), exactly as an accepted step of gv_job_walk.
+static gv_status forced_walk(gv_job* j, int w, int v1, int v2, int accept, int khop, gv_trace* rec)
+{
+    if (!j->step_trace) {
+        gv_status st = dalloc(j, &j->step_trace, sizeof(gv_trace));
+        if (st) return st;
+    }
+    DevJob& d = j->d;
+    d.forced_walker = w; d.forced_v1 = v1; d.forced_v2 = v2; d.forced_accept = accept; d.forced_khop = khop;
+    d.trace = j->step_trace;
+    d.trace_walker = w;
+    const bool fp64 = j->cfg.precision == GV_PREC_FP64;
+    gv_status st;
+    if (j->trans) st = fp64 ? launch_walk_trans<double>(j, 1) : launch_walk_trans<float>(j, 1);
+    else if (j->nt == 128) st = fp64 ? launch_walk<double, 128, 0>(j, 1, 0, 0, 0, 0) : launch_walk<float, 128, 0>(j, 1, 0, 0, 0, 0);
+    else st = fp64 ? launch_walk<double, 256, 0>(j, 1, 0, 0, 0, 0) : launch_walk<float, 256, 0>(j, 1, 0, 0, 0, 0);
+    d.forced_walker = -1;
+    d.forced_khop = -1;
+    d.trace = nullptr;
+    d.trace_walker = -1;
+    if (st) return st;
+    if (rec) GV_CK(copy_async(rec, j->step_trace, sizeof(gv_trace), cudaMemcpyDeviceToHost, j->stream));
+    GV_CK(cudaStreamSynchronize(j->stream));
+    int32_t status = GV_OK;
+    GV_CK(copy_sync(&status, j->d.status + w, sizeof(int32_t), cudaMemcpyDeviceToHost));
+    return status;
+}
+
+// |Amp|^2 sigma of walker w (LatticeStepper::weight) as mantissa * 2^e2.
+static gv_status walker_weight(gv_job* j, int w, double* mant, int32_t* e2)
+{
+    cx<double> m;
+    int32_t e = 0;
+    double sigma = 1.0;
+    GV_CK(cudaStreamSynchronize(j->stream));
+    GV_CK(copy_sync(&m, j->d.amp_m + w, sizeof(m), cudaMemcpyDeviceToHost));
+    GV_CK(copy_sync(&e, j->d.amp_e + w, sizeof(e), cudaMemcpyDeviceToHost));
+    if (j->trans) GV_CK(copy_sync(&sigma, j->d.sigma + w, sizeof(double), cudaMemcpyDeviceToHost));
+    int k = 0;
+    *mant = std::frexp((m.x * m.x + m.y * m.y) * sigma, &k);
+    *e2 = 2 * e + k;
+    return GV_OK;
+}
+
+static gv_status walker_rng(gv_job* j, int w, uint64_t* k)
+{
+    GV_CK(cudaStreamSynchronize(j->stream));
+    GV_CK(copy_sync(k, j->d.rng_next + w, sizeof(uint64_t), cudaMemcpyDeviceToHost));
+    return GV_OK;
+}
+
+gv_status gv_job_stepper_weight(gv_job* j, int32_t walker, double* mant, int32_t* exp2)
+{
+    if (!j || !mant || !exp2 || walker < 0 || walker >= j->W) return GV_ERR_INVALID;
+    if (!j->ready) return GV_ERR_NOT_READY;
+    return walker_weight(j, walker, mant, exp2);
+}
+
+gv_status gv_job_trystep(gv_job* j, int32_t walker, int32_t* v, double* weight_mant, int32_t* weight_exp2,
+                         int32_t* khop)
+{
+    if (!j || walker < 0 || walker >= j->W) return GV_ERR_INVALID;
+    if (!j->ready) return GV_ERR_NOT_READY;
+    uint64_t k = 0;
+    gv_status st = walker_rng(j, walker, &k);
+    if (st) return st;
+    // u1 -> vertex, u2 -> neighbour slot (LatticeStepper.cpp:45-47), integer-exact as in the walk kernels
+    uint32_t x[4];
+    philox_call(j->cfg.seed, j->cfg.walker_base + uint32_t(walker), 0, k >> 1, x);
+    const int v1 = scaled_floor(uint32_t(j->Ns), u52(x[0], x[1]));
+    const int v2 = j->lat.nbr[size_t(v1) * 4 + int(u52(x[2], x[3]) >> 50)];
+    gv_trace t{};
+    st = forced_walk(j, walker, v1, v2, 0, -1, &t);
+    if (st) return st;
+    double m = 0.0;
+    int32_t e2 = 0;
+    st = walker_weight(j, walker, &m, &e2);
+    if (st) return st;
+    if (t.kind) {   // the proposal's weight: its ratio times the current weight
+        int kk = 0;
+        m = std::frexp(m * t.ratio, &kk);
+        e2 += kk;
+    }
+    j->pend.w = walker;
+    j->pend.v1 = v1;
+    j->pend.v2 = v2;
+    j->pend.khop = t.kind ? t.khop : -1;
+    if (v) { v[0] = v1; v[1] = v2; }
+    if (weight_mant) *weight_mant = m;
+    if (weight_exp2) *weight_exp2 = e2;
+    if (khop) *khop = j->pend.khop;
+    return GV_OK;
+}
+
+gv_status gv_job_yesno(gv_job* j, int32_t walker, double ratio, int32_t* accepted)
+{
+    if (!j || !accepted || walker < 0 || walker >= j->W) return GV_ERR_INVALID;
+    if (!j->ready) return GV_ERR_NOT_READY;
+    uint64_t k = 0;
+    gv_status st = walker_rng(j, walker, &k);
+    if (st) return st;
+    // u4, the step's fourth uniform (MetroMC.cpp:41); the stream then moves to the next step
+    const double u4 = uniform_at(j->cfg.seed, j->cfg.walker_base + uint32_t(walker), 0, k + 3);
+    const int acc = ratio > 1.0 ? (u4 < 1.0) : (u4 < ratio);
+    const uint64_t next = k + 4;
+    GV_CK(copy_sync(j->d.rng_next + walker, &next, sizeof(uint64_t), cudaMemcpyHostToDevice));
+    if (!acc) {   // a rejected step: counted here (an accepted one by gv_job_step)
+        uint64_t c[5];
+        GV_CK(copy_sync(c, j->d.counts + size_t(walker) * 5, sizeof(c), cudaMemcpyDeviceToHost));
+        c[0] += 1;
+        c[3] += 1;
+        GV_CK(copy_sync(j->d.counts + size_t(walker) * 5, c, sizeof(c), cudaMemcpyHostToDevice));
+        if (j->pend.w == walker) j->pend.w = -1;
+    }
+    *accepted = acc;
+    return GV_OK;
+}
+
+gv_status gv_job_step(gv_job* j, int32_t walker)
+{
+    if (!j || walker < 0 || walker >= j->W) return GV_ERR_INVALID;
+    if (!j->ready) return GV_ERR_NOT_READY;
+    if (j->pend.w != walker) return GV_ERR_INVALID;   // no evaluated proposal for this walker
+    const gv_job::Pending p = j->pend;
+    j->pend.w = -1;
+    gv_status st = forced_walk(j, walker, p.v1, p.v2, 1, p.khop, nullptr);
+    if (!st && (j->cfg.flags & GV_FLAG_REINV_DEFERRED) && j->cfg.reinv_every > 0) {
+        st = deferred_reinversion(j);
+        if (!st) st = gv_job_synchronize(j);
+    }
+    return st;
+}
+
+gv_status gv_job_update(gv_job* j, int32_t walker, const int32_t* hop, int32_t state)
+{
+    if (!j || !hop || walker < 0 || walker >= j->W) return GV_ERR_INVALID;
+    if (!j->ready) return GV_ERR_NOT_READY;
+    for (int i = 0; i < 4; ++i)
+        if (hop[i] < -1 || hop[i] >= j->Ns) return GV_ERR_INVALID;
+    if (hop[0] < 0 && hop[1] < 0 && hop[2] < 0 && hop[3] < 0) return GV_OK;   // the empty hop set
+    // a nearest-neighbour exchange: flavour 0 from a to b, flavour 1 from b to a
+    if (hop[0] < 0 || hop[1] < 0 || hop[2] != hop[1] || hop[3] != hop[0]) return GV_ERR_INVALID;
+    if (state < -1 || state >= j->ch.Nexc) return GV_ERR_INVALID;
+    std::vector<int16_t> fock(2 * size_t(j->Ns));
+    GV_CK(cudaStreamSynchronize(j->stream));
+    GV_CK(copy_sync(fock.data(), j->d.fock + size_t(walker) * 2 * j->Ns, fock.size() * sizeof(int16_t),
+                    cudaMemcpyDeviceToHost));
+    if (fock[hop[0]] < 0 || fock[j->Ns + hop[1]] < 0) return GV_ERR_INVALID;   // the hop's particles are absent
+    if (j->pend.w == walker) j->pend.w = -1;
+    return forced_walk(j, walker, hop[0], hop[1], 1, state, nullptr);
 }
 
 gv_status gv_job_synchronize(gv_job* j)

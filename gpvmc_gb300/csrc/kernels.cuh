@@ -732,6 +732,8 @@ __global__ void __launch_bounds__(NT, 768 / NT) k_walk_gs(DevJob J, uint64_t nst
     const int w = blockIdx.x;
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     if (w >= J.W || J.status[w] != GV_OK) return;
+    const bool forced = J.forced_walker >= 0;
+    if (forced && w != J.forced_walker) return;
     const int Ns = J.Ns, Nmax = J.Nmax, L = J.L, Nk = J.Nk;
     const int N0 = J.N[0], N1 = J.N[1];
     const WalkLayout lay = walk_layout<T, NT, KD>(Ns, Nmax, (mask & GV_MEAS_PROJHEIS) != 0, inkernel_reinv != 0);
@@ -782,8 +784,9 @@ __global__ void __launch_bounds__(NT, 768 / NT) k_walk_gs(DevJob J, uint64_t nst
         // vertex and slot are computed in integers, bit-identical to
         // size_t(n * uniform()) (LatticeStepper.cpp:45-47).
         const uint64_t m4 = u52(y[2], y[3]);
-        const int v1 = scaled_floor(uint32_t(Ns), u52(x[0], x[1]));
-        const int v2 = s_nbr[v1 * 4 + int(u52(x[2], x[3]) >> 50)];
+        int v1 = scaled_floor(uint32_t(Ns), u52(x[0], x[1]));
+        int v2 = s_nbr[v1 * 4 + int(u52(x[2], x[3]) >> 50)];
+        if (forced) { v1 = J.forced_v1; v2 = J.forced_v2; }
         const int f1 = s_fock[v1] >= 0 ? 0 : 1;
         const int f2 = s_fock[v2] >= 0 ? 0 : 1;
         int kind = 0, accepted;
@@ -833,7 +836,7 @@ __global__ void __launch_bounds__(NT, 768 / NT) k_walk_gs(DevJob J, uint64_t nst
             ratio = Accept<T>::ratio(ru, rd);
             if (!isfinite(ratio)) { status = GV_ERR_NAN; break; }
             // MetroMC::YesNo (MetroMC.cpp:41): ratio > 1 draws u4 < 1, always true here
-            accepted = ratio > T(1) ? 1 : (Accept<T>::uniform(m4) < ratio);
+            accepted = forced ? J.forced_accept : (ratio > T(1) ? 1 : (Accept<T>::uniform(m4) < ratio));
             if (!accepted) {
                 ++c_rej;
             } else {
@@ -891,6 +894,7 @@ __global__ void __launch_bounds__(NT, 768 / NT) k_walk_gs(DevJob J, uint64_t nst
             t.ratio = double(ratio); t.u4 = u01(y[2], y[3]);
             J.trace[s] = t;
         }
+        if (forced && !J.forced_accept) return;   // evaluation only: nothing was changed, nothing to write
         const uint64_t gs = s0 + s;
         if (meas && (meas == 1 || gs % meas == 0) && mask) {
             flush_pending<T, NT, KD>(P, A0, A1, N0, N1, Nmax);
@@ -902,7 +906,7 @@ __global__ void __launch_bounds__(NT, 768 / NT) k_walk_gs(DevJob J, uint64_t nst
     for (int i = tid; i < 2 * Ns; i += NT) J.fock[size_t(w) * 2 * Ns + i] = s_fock[i];
     for (int i = tid; i < 2 * Nmax; i += NT) J.part[size_t(w) * 2 * Nmax + i] = s_part[i];
     if (tid == 0) {
-        J.rng_next[w] = k;
+        if (!forced) J.rng_next[w] = k;   // single-walker stepping draws its uniforms itself
         unsigned long long* c = J.counts + size_t(w) * 5;
         c[0] += c_acc + c_noop + c_rej;
         c[1] += c_acc;

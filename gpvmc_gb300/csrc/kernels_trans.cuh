@@ -202,6 +202,8 @@ __global__ void __launch_bounds__(NT, 2) k_walk_trans(DevJob J, uint64_t nsteps,
     const int w = blockIdx.x;
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     if (w >= J.W || J.status[w] != GV_OK) return;
+    const bool forced = J.forced_walker >= 0;
+    if (forced && w != J.forced_walker) return;
     const int Ns = J.Ns, Nmax = J.Nmax, L = J.L, Nk = J.Nk, Nexc = J.Nexc;
     const int N0 = J.N[0], N1 = J.N[1];
     const TransLayout lay = trans_layout<T, NT>(Ns, Nmax, Nexc, inkernel_reinv != 0);
@@ -271,8 +273,9 @@ __global__ void __launch_bounds__(NT, 2) k_walk_trans(DevJob J, uint64_t nsteps,
         philox_call(J.seed, wid, 0, kk >> 1, x);
         philox_call(J.seed, wid, 0, (kk >> 1) + 1, y);
         const uint64_t m4 = u52(y[2], y[3]);
-        const int v1 = scaled_floor(uint32_t(Ns), u52(x[0], x[1]));
-        const int v2 = s_nbr[v1 * 4 + int(u52(x[2], x[3]) >> 50)];
+        int v1 = scaled_floor(uint32_t(Ns), u52(x[0], x[1]));
+        int v2 = s_nbr[v1 * 4 + int(u52(x[2], x[3]) >> 50)];
+        if (forced) { v1 = J.forced_v1; v2 = J.forced_v2; }
         const int f1 = s_fock[v1] >= 0 ? 0 : 1;
         const int f2 = s_fock[v2] >= 0 ? 0 : 1;
         int kind = 0, accepted, khop = -1;
@@ -383,10 +386,10 @@ __global__ void __launch_bounds__(NT, 2) k_walk_trans(DevJob J, uint64_t nsteps,
                     kbest = rbi[q];
                 }
             }
-            khop = kbest;
+            khop = (forced && J.forced_khop >= 0 && J.forced_khop < Nexc) ? J.forced_khop : kbest;
             ratio = wsum / T(sigma);
             if (!isfinite(ratio) || khop >= Nexc) { status = GV_ERR_NAN; break; }
-            accepted = ratio > T(1) ? 1 : (Accept<T>::uniform(m4) < ratio);
+            accepted = forced ? J.forced_accept : (ratio > T(1) ? 1 : (Accept<T>::uniform(m4) < ratio));
             if (!accepted) {
                 ++c_rej;
             } else {
@@ -546,6 +549,7 @@ __global__ void __launch_bounds__(NT, 2) k_walk_trans(DevJob J, uint64_t nsteps,
             t.ratio = double(ratio); t.u4 = u01(y[2], y[3]);
             J.trace[s] = t;
         }
+        if (forced && !J.forced_accept) return;   // evaluation only: nothing was changed, nothing to write
     }
     __syncthreads();
     for (int i = tid; i < 2 * Ns; i += NT) {
@@ -559,7 +563,7 @@ __global__ void __launch_bounds__(NT, 2) k_walk_trans(DevJob J, uint64_t nsteps,
     cx<T>* gout = static_cast<cx<T>*>(J.gdn) + size_t(w) * Nmax;
     for (int i = tid; i < N1; i += NT) gout[i] = s_g[i];
     if (tid == 0) {
-        J.rng_next[w] = kk;
+        if (!forced) J.rng_next[w] = kk;   // single-walker stepping draws its uniforms itself
         unsigned long long* c = J.counts + size_t(w) * 5;
         c[0] += c_acc + c_noop + c_rej;
         c[1] += c_acc;

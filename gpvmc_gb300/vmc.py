@@ -263,6 +263,41 @@ class Job:
     def reinvert(self):
         check(_lib.lib().gv_job_reinvert(self._h), "gv_job_reinvert")
 
+    # ---- single-walker stepping (LatticeStepper::trystep / step, MetroMC::YesNo) ----
+    def trystep(self, walker=0):
+        """LatticeStepper::trystep on one walker: ((v1, v2), weight as
+        (mantissa, base-2 exponent), arg-max channel state or -1 for a
+        same-flavour proposal).  The proposal stays pending for step()."""
+        v = np.zeros(2, dtype=np.int32)
+        m, e, k = ctypes.c_double(), ctypes.c_int32(), ctypes.c_int32()
+        check(_lib.lib().gv_job_trystep(self._h, walker, _p(v), ctypes.byref(m), ctypes.byref(e), ctypes.byref(k)),
+              "gv_job_trystep")
+        return (int(v[0]), int(v[1])), (m.value, e.value), k.value
+
+    def yesno(self, walker, ratio):
+        """MetroMC::YesNo with the walker's u4; moves its stream to the next step."""
+        a = ctypes.c_int32()
+        check(_lib.lib().gv_job_yesno(self._h, walker, float(ratio), ctypes.byref(a)), "gv_job_yesno")
+        return bool(a.value)
+
+    def step(self, walker=0):
+        """LatticeStepper::step: apply the walker's pending proposal."""
+        check(_lib.lib().gv_job_step(self._h, walker), "gv_job_step")
+
+    def update(self, walker, hop, state=-1):
+        """Lattice hop + wavefunction hop + SlaterDeterminant::Update for the
+        exchange hop = (up_from, up_to, dn_from, dn_to) and channel state
+        `state` (-1: the arg-max)."""
+        h = np.ascontiguousarray(hop, dtype=np.int32)
+        check(_lib.lib().gv_job_update(self._h, walker, _p(h), int(state)), "gv_job_update")
+
+    def stepper_weight(self, walker=0):
+        """LatticeStepper::weight of one walker as (mantissa, base-2 exponent)."""
+        m, e = ctypes.c_double(), ctypes.c_int32()
+        check(_lib.lib().gv_job_stepper_weight(self._h, walker, ctypes.byref(m), ctypes.byref(e)),
+              "gv_job_stepper_weight")
+        return m.value, e.value
+
     def drift(self):
         out = np.zeros(2 * self.walkers)
         check(_lib.lib().gv_job_drift(self._h, _p(out)), "gv_job_drift")
@@ -403,13 +438,35 @@ class SlaterDeterminant:
 
 
 class LatticeStepper:
-    """LatticeStepper (LatticeStepper.h:16-37): nearest-neighbour exchanges."""
+    """LatticeStepper (LatticeStepper.h:16-37): nearest-neighbour exchanges.
+    Step-level calls (Stepper.h:13-34) act on one walker of the job; weights
+    are (mantissa, base-2 exponent) pairs (the reference's BigDouble)."""
 
-    def __init__(self, job):
+    def __init__(self, job, walker=0):
         self.job = job
+        self.walker = walker
+        self.prev = None
+        self.khop = -1
 
     def GetAmp(self):
         return SlaterDeterminant(self.job)
+
+    def Reset(self):
+        self.prev, self.khop = None, -1
+
+    def trystep(self):
+        self.prev, w, self.khop = self.job.trystep(self.walker)
+        return w
+
+    def step(self):
+        self.job.step(self.walker)
+        self.prev, self.khop = None, -1
+
+    def weight(self):
+        return self.job.stepper_weight(self.walker)
+
+    def transprob(self):
+        return 1.0
 
 
 class Quantity:
@@ -503,11 +560,27 @@ class OverlapTrack(Quantity):
 
 
 class MetroMC:
-    """MetroMC (MetroMC.h:11-45): Walk(len, meas), Rejection()."""
+    """MetroMC (MetroMC.h:11-45): Walk(len, meas) on every walker of the job,
+    Step(meas) / YesNo(ratio) on the stepper's walker, Rejection()."""
 
     def __init__(self, stepper):
         self.job = stepper.job
+        self.stepper = stepper
         self.quantities = []
+        self._state_weight = None
+
+    def YesNo(self, ratio):
+        return self.job.yesno(self.stepper.walker, ratio)
+
+    def Step(self, meas=False):
+        """MetroMC::Step (MetroMC.cpp:90-103)."""
+        if self._state_weight is None:
+            self._state_weight = self.stepper.weight()
+        new = self.stepper.trystep()
+        ratio = math.ldexp(new[0] / self._state_weight[0], new[1] - self._state_weight[1])
+        if self.YesNo(ratio):
+            self.stepper.step()
+            self._state_weight = new
 
     def AddQuantity(self, q):
         self.quantities.append(q)
@@ -526,6 +599,7 @@ class MetroMC:
             if self.job.track_capacity < need:
                 self.job.set_track_capacity(need)
         self.job.walk(length, meas)
+        self._state_weight = None   # the walk moved the stepper's walker too
 
     def Rejection(self):
         c = self.job.counts().astype(np.float64)

@@ -201,6 +201,42 @@ gv_status gv_job_stream(gv_job* job, void** stream);
 /* As gv_job_walk, also recording walker `walker`'s per-step trace into the
  * host array trace[len] (synchronous). */
 gv_status gv_job_walk_traced(gv_job* job, uint64_t len, uint64_t meas, int32_t walker, gv_trace* trace);
+/* Single-walker stepping, the reference's step-level API for one chain
+ * (callers that drive MetroMC::Step themselves, or a Stepper of their own).
+ * The walker's Metropolis stream is the one gv_job_walk draws from, so
+ * stepping and walking can be mixed.  Slow path: every call synchronises.
+ *   gv_job_trystep   LatticeStepper::trystep (LatticeStepper.cpp:36-100): draws
+ *                    u1, u2, u3 of the walker's next step, proposes the
+ *                    exchange v[0] = floor(Ns u1) <-> v[1] = its neighbour
+ *                    floor(deg u2) (u3 drawn and unused), evaluates
+ *                    SlaterDeterminant::VirtUpdate over every channel state
+ *                    and returns the proposal's weight sum_k |q_k|^2 as
+ *                    weight_mant * 2^weight_exp2 (the current weight for a
+ *                    same-flavour proposal) and the arg-max channel state
+ *                    khop (-1 for a same-flavour proposal).  The proposal
+ *                    stays pending for gv_job_step.
+ *   gv_job_yesno     MetroMC::YesNo (MetroMC.cpp:27-43) with the step's u4:
+ *                    accepted = ratio > 1 ? u4 < 1 : u4 < ratio; moves the
+ *                    stream to the next step and counts a rejection.
+ *   gv_job_step      LatticeStepper::step (LatticeStepper.cpp:102-147): applies
+ *                    the pending proposal -- the lattice hop, the wavefunction
+ *                    hop to its arg-max state, SlaterDeterminant::Update of
+ *                    both inverses (linalg::InvUpdate) and the amplitude -- with
+ *                    the same kernel code as an accepted step of gv_job_walk.
+ *   gv_job_update    LatticeState::Hop + WaveFunction::Hop + SlaterDeterminant::
+ *                    Update (SlaterDeterminant.cpp:270-326) for a given
+ *                    exchange hop = (up_from, up_to, dn_from, dn_to) with
+ *                    up_to = dn_from and dn_to = up_from (all -1: nothing)
+ *                    and channel state `state` (-1: the arg-max).
+ *   gv_job_stepper_weight  LatticeStepper::weight (LatticeStepper.cpp:149-169):
+ *                    sum_k |q_k|^2 as mant * 2^exp2. */
+gv_status gv_job_trystep(gv_job* job, int32_t walker, int32_t* v, double* weight_mant, int32_t* weight_exp2,
+                         int32_t* khop);
+gv_status gv_job_yesno(gv_job* job, int32_t walker, double ratio, int32_t* accepted);
+gv_status gv_job_step(gv_job* job, int32_t walker);
+gv_status gv_job_update(gv_job* job, int32_t walker, const int32_t* hop, int32_t state);
+gv_status gv_job_stepper_weight(gv_job* job, int32_t walker, double* mant, int32_t* exp2);
+
 /* Wait for the job's stream; returns the first walker error status if any. */
 gv_status gv_job_synchronize(gv_job* job);
 

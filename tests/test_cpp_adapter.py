@@ -9,15 +9,16 @@ import pytest
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 DRIVER = os.path.join(ROOT, "tests", "cpp", "vmc_driver.cpp")
+STEP_DRIVER = os.path.join(ROOT, "tests", "cpp", "step_driver.cpp")
 
 
-def build_driver(tmp_path):
+def build_driver(tmp_path, src=DRIVER):
     from gpvmc_gb300 import build as b
     if not os.path.exists(b.LIB):
         b.build()
-    exe = str(tmp_path / "vmc_driver")
+    exe = str(tmp_path / os.path.splitext(os.path.basename(src))[0])
     cuda_lib = "/usr/local/cuda/lib64"
-    cmd = ["g++", "-O2", "-std=c++17", "-I" + os.path.join(ROOT, "include"), DRIVER, "-o", exe,
+    cmd = ["g++", "-O2", "-std=c++17", "-I" + os.path.join(ROOT, "include"), src, "-o", exe,
            "-L" + os.path.dirname(b.LIB), "-lgpvmc_gb300", "-L" + cuda_lib, "-lcudart",
            "-Wl,-rpath," + os.path.dirname(b.LIB) + ":" + cuda_lib]
     subprocess.run(cmd, check=True, capture_output=True, text=True)
@@ -25,9 +26,10 @@ def build_driver(tmp_path):
 
 
 def test_adapter_compiles_and_links(tmp_path):
-    exe = build_driver(tmp_path)
-    r = subprocess.run([exe], capture_output=True, text=True)
-    assert r.returncode == 2 and "usage" in r.stderr
+    for src in (DRIVER, STEP_DRIVER):
+        exe = build_driver(tmp_path, src)
+        r = subprocess.run([exe], capture_output=True, text=True)
+        assert r.returncode == 2 and "usage" in r.stderr
 
 
 @pytest.mark.gpu
@@ -47,3 +49,61 @@ def test_driver_matches_python_api(tmp_path, engine):
     pj, n = job.projheis()
     np.testing.assert_allclose(e_cpp, pj[:, 0].real / n, rtol=0, atol=1e-14)
     assert int(tok[-1]) == 10
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("channel,L,q,steps", [("gs", 8, (0, 0), 1000), ("gs", 16, (0, 0), 400),
+                                               ("trans", 8, (4, 4), 400), ("trans", 4, (2, 2), 600)])
+def test_step_driver_matches_oracle(tmp_path, engine, oracle, channel, L, q, steps):
+    """The step-level adapter (LatticeStepper::trystep / step, MetroMC::YesNo,
+    MetroMC::Step, SlaterDeterminant::VirtUpdate(rhop, khop, qs)) driven by C++
+    like MetroMC::Walk reproduces the oracle's chain: proposals, decisions up
+    to flagged near-ties, ratios (1e-10, or no further than the oracle from a
+    freshly inverted state), VirtUpdate amplitudes of every channel state to
+    1e-9 and the final configuration."""
+    import math
+    from test_gpu_parity import check_ratios
+    exe = build_driver(tmp_path, STEP_DRIVER)
+    seed = 7
+    r = subprocess.run([exe, channel, str(L), "0.25", "0.1", str(seed), str(steps), str(q[0]), str(q[1]), "fp64"],
+                       capture_output=True, text=True, check=True)
+    lines = r.stdout.splitlines()
+    S = [ln.split()[1:] for ln in lines if ln.startswith("S ")]
+    t = np.zeros(len(S), dtype=[("v1", "<i4"), ("v2", "<i4"), ("kind", "<i4"), ("accepted", "<i4"), ("ratio", "<f8")])
+    for i, x in enumerate(S):
+        t[i] = (int(x[0]), int(x[1]), int(int(x[2]) >= 0), int(x[3]), float(x[4]))
+    ch = oracle.TRANS if channel == "trans" else oracle.GROUNDSTATE
+
+    def fresh():
+        o = oracle.OracleChain(L, 0.25 * math.pi, 0.1, channel=ch, q=q, seed=seed, walker=0)
+        assert o.random_start() == 0
+        return o
+    orc = fresh()
+    to = orc.walk(steps // 2, trace=True)
+    assert (t["v1"] == to["v1"]).all() and (t["v2"] == to["v2"]).all() and (t["kind"] == to["kind"]).all()
+    tie = np.abs(to["u"][:, 3] - to["ratio"]) < 1e-9
+    assert ((t["accepted"] == to["accepted"]) | tie).all()
+    assert not tie.any(), "pick a tie-free seed"
+    check_ratios(t, to, fresh)
+    # VirtUpdate(rhop, khop, qs) at the half-way point against the oracle's
+    V = next(ln.split()[1:] for ln in lines if ln.startswith("V "))
+    K, Nr = int(V[0]), int(V[1])
+    vals = np.array(V[2:], dtype=float).reshape(K, Nr, 3)
+    up = orc.config().astype(bool)
+    hops = [(-1, -1, -1, -1)]
+    for y in range(L):
+        for x in range(L):
+            a, b = y * L + x, y * L + (x + 1) % L
+            if len(hops) < 2 and up[a] != up[b]:
+                u, d = (a, b) if up[a] else (b, a)
+                hops.append((u, d, d, u))
+    assert Nr == len(hops) and K == orc.Nexc
+    qm, qe = orc.virt_update(np.array(hops, dtype=np.int32))     # (Nexc, Nr)
+    top = int(qe.max())
+    want = qm * 10.0 ** (qe - top).astype(float)
+    got = (vals[..., 0] + 1j * vals[..., 1]) * 10.0 ** (vals[..., 2] - top)
+    assert np.abs(got - want).max() < 1e-9 * np.abs(want).max()
+    # the second half through MetroMC::Step itself: same final configuration
+    orc.walk(steps - steps // 2)
+    C = next(ln.split()[1:] for ln in lines if ln.startswith("C "))
+    assert (np.array(C, dtype=np.int8) == orc.config()).all()
