@@ -6,7 +6,7 @@ gpvmc_gb300.vmc for the reference-named API.
 """
 from ._lib import GvError, lib  # noqa: F401
 from .vmc import (Job, LatticeStepper, MetroMC, ProjHeis, SlaterDeterminant, SquareLattice,  # noqa: F401
-                  StagFluxGroundState, StagFluxTransExciton, StagMagnTrack, StagMagnZ, StatSpinStruct, OverlapTrack, pi_phi)
+                  StagFluxGroundState, StagFluxTransExciton, StagFluxLongExciton, StagMagnTrack, StagMagnZ, StatSpinStruct, OverlapTrack, pi_phi)
 from .serving import Server  # noqa: F401
 from .output import FileManager, convert_tree, save_quantities, write_wavefunction  # noqa: F401
 

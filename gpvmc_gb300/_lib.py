@@ -16,7 +16,7 @@ GV_REQ_PENDING, GV_REQ_RUNNING, GV_REQ_DONE = 0, 1, 2
 STATUS_NAMES = {0: "ok", 1: "invalid", 2: "singular", 3: "nan", 4: "zero amplitude", 5: "drift",
                 6: "timeout", 7: "out of memory", 8: "cuda error", 9: "not ready", 10: "too large"}
 
-GV_CH_GROUNDSTATE, GV_CH_TRANS = 0, 1
+GV_CH_GROUNDSTATE, GV_CH_TRANS, GV_CH_LONG = 0, 1, 2
 GV_PREC_FP64, GV_PREC_MIXED = 0, 1
 GV_MEAS_PROJHEIS, GV_MEAS_STAGMAGN, GV_MEAS_STATSPIN = 1, 2, 4
 GV_MEAS_STAGMAGN_TRACK, GV_MEAS_OVERLAP_TRACK = 8, 16

@@ -25,6 +25,7 @@
 #include "device.cuh"
 #include "kernels.cuh"
 #include "kernels_trans.cuh"
+#include "kernels_long.cuh"
 #include "kernels_res.cuh"
 #include "kernels_tc.cuh"
 #include "kernels_trans_res.cuh"
@@ -64,6 +65,7 @@ struct gv_job {
     std::vector<uint64_t> start_draws;   // Philox stream-1 uniform index per walker
     int n_sm = 1;                        // SMs of the job's device (persistent grids)
     bool trans = false;                  // transverse-exciton channel
+    bool lng = false;                    // longitudinal-exciton channel
     struct WalkGraph {
         cudaGraphExec_t exec;
         int64_t launches;
@@ -135,8 +137,9 @@ bool valid_config(const gv_job_config* c)
     if (!c) return false;
     if (c->L < 4 || c->L > 64 || (c->L % 2)) return false;
     if (c->channel == GV_CH_TRANS && c->L > 32) return false;
-    if (c->channel != GV_CH_GROUNDSTATE && c->channel != GV_CH_TRANS) return false;
-    if (c->channel == GV_CH_TRANS && (c->flags & GV_FLAG_DELAYED_UPDATES)) return false;
+    if (c->channel == GV_CH_LONG && c->L > 24) return false;   // its walk stages 3 x 2 x L^2 orbitals on chip
+    if (c->channel != GV_CH_GROUNDSTATE && c->channel != GV_CH_TRANS && c->channel != GV_CH_LONG) return false;
+    if (c->channel != GV_CH_GROUNDSTATE && (c->flags & GV_FLAG_DELAYED_UPDATES)) return false;
     if (c->n_walkers < 1 || c->n_walkers > (1 << 20)) return false;
     if (c->precision != GV_PREC_FP64 && c->precision != GV_PREC_MIXED) return false;
     if (c->reinv_every < 0) return false;
@@ -149,6 +152,10 @@ bool valid_config(const gv_job_config* c)
 }
 
 int pick_threads(int Nmax) { return Nmax > 128 ? 256 : 128; }
+
+// Either exciton channel: a wavefunction with several states, its Fock state,
+// sign, current state and weight kept per walker.
+inline bool exc(const gv_job* j) { return j->trans || j->lng; }
 
 // Exciton channel tables, checked against the channel's hop table
 // (WaveFunction::m_exc, WaveFunction.cpp:39-67): from state a, state b != a
@@ -218,6 +225,33 @@ void wav_hop(const gv_job* j, WavHost& s, int k)
         s.slot[fl][to] = p;
         s.orb[fl][p] = int16_t(to);
     }
+    s.cur = k;
+}
+
+// WaveFunction::Hop in the longitudinal channel: up to two hops per flavour
+// (State::get_hop_path pairs, State::HopSign with the second hop counted after
+// the first, State.cpp:73-115).
+void long_wav_hop(const gv_job* j, WavHost& s, int k)
+{
+    int odd = 0;
+    for (int fl = 0; fl < 2; ++fl) {
+        int V[2], F[2];
+        const int n = long_hops(s.cur, k, fl, j->exu.data(), j->exd.data(), j->Ns, V, F);
+        std::vector<int16_t> sl = s.slot[fl];
+        for (int i = 0; i < n; ++i) {
+            for (int x = std::min(V[i], F[i]) + 1; x < std::max(V[i], F[i]); ++x) odd ^= sl[x] >= 0 ? 1 : 0;
+            const int16_t r = sl[V[i]];
+            sl[V[i]] = -1;
+            sl[F[i]] = r;
+        }
+        for (int i = 0; i < n; ++i) {
+            const int16_t r = s.slot[fl][V[i]];
+            s.slot[fl][V[i]] = -1;
+            s.slot[fl][F[i]] = r;
+            s.orb[fl][r] = int16_t(F[i]);
+        }
+    }
+    s.sign *= odd ? -1 : 1;
     s.cur = k;
 }
 
@@ -300,7 +334,7 @@ constexpr int kDelay = GV_DELAY_DEPTH;
 bool resident_ok(const gv_job* j, uint64_t nsteps)
 {
     const int f = j->cfg.flags;
-    return nsteps > 0 && !j->trans && j->cfg.precision == GV_PREC_MIXED && j->N[0] == j->N[1] && j->Nmax <= 128 &&
+    return nsteps > 0 && !exc(j) && j->cfg.precision == GV_PREC_MIXED && j->N[0] == j->N[1] && j->Nmax <= 128 &&
            (f & GV_FLAG_REINV_DEFERRED) && !(f & GV_FLAG_DELAYED_UPDATES) && !(f & GV_FLAG_STREAM_INVERSES);
 }
 
@@ -393,7 +427,7 @@ bool trans_z_tc_ok(const gv_job* j)
 // Tensor-core StatSpinStruct: mixed ground state with N_0 = N_1 <= 128.
 bool statspin_tc_ok(const gv_job* j)
 {
-    return !j->trans && j->cfg.precision == GV_PREC_MIXED && j->N[0] == j->N[1] && j->N[0] <= kTcM &&
+    return !exc(j) && j->cfg.precision == GV_PREC_MIXED && j->N[0] == j->N[1] && j->N[0] <= kTcM &&
            !(j->cfg.flags & GV_FLAG_SCALAR_PAIRS);
 }
 
@@ -535,6 +569,98 @@ gv_status measure_trans_dispatch(gv_job* j, int mask)
 }
 
 // sigma (and, with out, every state's |rho0_k|^2) of every walker.
+// Longitudinal exciton: the walk, the ProjHeis / StagMagnZ measurement, the
+// state overlaps (start-state pick, weight) and VirtUpdate.
+template <typename T>
+gv_status launch_walk_long(gv_job* j, uint64_t nsteps)
+{
+    constexpr int NT = 256;
+    const bool inkernel = !(j->cfg.flags & GV_FLAG_REINV_DEFERRED);
+    const LongLayout lay = long_layout<T, NT>(j->Ns, j->Nmax, j->ch.Nexc, inkernel);
+    GV_CK(raise_smem_limit(k_walk_long<T, NT>, lay.total));
+    int slot;
+    GV_CK(mark_begin(j, 0, &slot));
+    k_walk_long<T, NT><<<j->W, NT, lay.total, j->stream>>>(j->d, nsteps, inkernel ? 1 : 0);
+    GV_CK(cudaGetLastError());
+    GV_CK(mark_end(j, slot));
+    ++j->last_launches;
+    ++j->total_launches;
+    return GV_OK;
+}
+
+gv_status walk_long_dispatch(gv_job* j, uint64_t nsteps)
+{
+    return j->cfg.precision == GV_PREC_FP64 ? launch_walk_long<double>(j, nsteps) : launch_walk_long<float>(j, nsteps);
+}
+
+template <typename T>
+gv_status launch_measure_long(gv_job* j, int mask)
+{
+    constexpr int NT = 256;
+    const LongMeasLayout lay = long_meas_layout<T, NT>(j->Ns, j->Nmax, j->ch.Nexc);
+    GV_CK(raise_smem_limit(k_measure_long<T, NT>, lay.total));
+    int slot;
+    GV_CK(mark_begin(j, 2, &slot));
+    k_measure_long<T, NT><<<j->W, NT, lay.total, j->stream>>>(j->d, mask);
+    GV_CK(cudaGetLastError());
+    GV_CK(mark_end(j, slot));
+    ++j->last_launches;
+    ++j->total_launches;
+    return GV_OK;
+}
+
+gv_status measure_long_dispatch(gv_job* j, int mask)
+{
+    return j->cfg.precision == GV_PREC_FP64 ? launch_measure_long<double>(j, mask) : launch_measure_long<float>(j, mask);
+}
+
+gv_status long_states(gv_job* j, double* out)
+{
+    constexpr int NT = 256;
+    const size_t sm = ((sizeof(int16_t) * (4 * size_t(j->Ns) + 2) + 15) & ~size_t(15)) + sizeof(double) * (NT / 32);
+    if (j->cfg.precision == GV_PREC_FP64) k_long_states<double, NT><<<j->W, NT, sm, j->stream>>>(j->d, out);
+    else k_long_states<float, NT><<<j->W, NT, sm, j->stream>>>(j->d, out);
+    GV_CK(cudaGetLastError());
+    ++j->total_launches;
+    return GV_OK;
+}
+
+gv_status virt_update_long(gv_job* j, int walker, int nset, const int32_t* hops, double* out)
+{
+    for (int i = 0; i < nset; ++i) {
+        const int32_t* h = hops + 4 * i;
+        const bool empty = h[0] < 0 && h[1] < 0 && h[2] < 0 && h[3] < 0;
+        for (int q = 0; q < 4; ++q)
+            if (h[q] < -1 || h[q] >= j->Ns) return GV_ERR_INVALID;
+        if (!empty && (h[0] < 0 || h[1] < 0 || h[2] != h[1] || h[3] != h[0])) return GV_ERR_INVALID;   // exchanges only
+    }
+    if (nset == 0) return GV_OK;
+    constexpr int NT = 256;
+    int32_t* dh = nullptr;
+    double* dout = nullptr;
+    const size_t nout = size_t(2) * nset * j->ch.Nexc;
+    GV_CK(cudaMalloc(&dh, sizeof(int32_t) * 4 * nset));
+    if (cudaMalloc(&dout, sizeof(double) * nout)) { cudaFree(dh); return GV_ERR_OOM; }
+    cudaError_t e = copy_async(dh, hops, sizeof(int32_t) * 4 * nset, cudaMemcpyHostToDevice, j->stream);
+    if (!e) {
+        if (j->cfg.precision == GV_PREC_FP64) {
+            const size_t sm = long_meas_layout<double, NT>(j->Ns, j->Nmax, j->ch.Nexc).total;
+            e = raise_smem_limit(k_virt_long<double, NT>, sm);
+            if (!e) k_virt_long<double, NT><<<1, NT, sm, j->stream>>>(j->d, walker, nset, dh, dout);
+        } else {
+            const size_t sm = long_meas_layout<float, NT>(j->Ns, j->Nmax, j->ch.Nexc).total;
+            e = raise_smem_limit(k_virt_long<float, NT>, sm);
+            if (!e) k_virt_long<float, NT><<<1, NT, sm, j->stream>>>(j->d, walker, nset, dh, dout);
+        }
+        if (!e) e = cudaGetLastError();
+    }
+    if (!e) e = copy_async(out, dout, sizeof(double) * nout, cudaMemcpyDeviceToHost, j->stream);
+    if (!e) e = cudaStreamSynchronize(j->stream);
+    cudaFree(dh);
+    cudaFree(dout);
+    return cuda_status(e);
+}
+
 gv_status trans_overlaps(gv_job* j, double* out)
 {
     if (j->cfg.precision == GV_PREC_FP64) k_trans_overlaps<double, 128><<<j->W, 128, 0, j->stream>>>(j->d, out);
@@ -638,6 +764,38 @@ gv_status trans_start(gv_job* j)
     return trans_overlaps(j, nullptr);
 }
 
+// vmc.cpp:243-263 in the longitudinal channel: overlaps of every state from
+// the walker's state-0 inverses and R (the determinant lemma, no LU per
+// state), the first state of largest |Amp|, the reference's hop path
+// 0 -> 1 -> ... -> Nexc-1 -> kmax replayed on the host (Slater rows, sign),
+// then the inverses, R and the weight in that state.
+gv_status long_start(gv_job* j)
+{
+    const int W = j->W, Nexc = j->ch.Nexc;
+    double* dov = nullptr;
+    GV_CK(cudaMalloc(&dov, sizeof(double) * size_t(W) * Nexc));
+    std::vector<double> ov(size_t(W) * Nexc);
+    gv_status st = long_states(j, dov);
+    if (!st && (copy_async(ov.data(), dov, ov.size() * sizeof(double), cudaMemcpyDeviceToHost, j->stream) ||
+                cudaStreamSynchronize(j->stream)))
+        st = GV_ERR_CUDA;
+    cudaFree(dov);
+    if (st) return st;
+    WavHost base = wav_state0(j);
+    for (int k = 0; k < Nexc; ++k) long_wav_hop(j, base, k);
+    std::vector<WavHost> ws(W, base);
+    for (int w = 0; w < W; ++w) {
+        int kmax = 0;
+        double best = ov[size_t(w) * Nexc];
+        for (int k = 1; k < Nexc; ++k)
+            if (ov[size_t(w) * Nexc + k] > best) { best = ov[size_t(w) * Nexc + k]; kmax = k; }
+        long_wav_hop(j, ws[w], kmax);
+    }
+    if ((st = upload_wav(j, ws))) return st;
+    if ((st = invert_all(j))) return st;
+    return long_states(j, nullptr);
+}
+
 // LatticeState::RanInit (LatticeState.cpp:37-82) for the two-flavour
 // half-filled lattice: flavour-0 sites drawn uniformly (Philox stream 1)
 // until N0 distinct, the rest flavour 1.
@@ -716,7 +874,7 @@ std::vector<CkptSection> ckpt_sections(gv_job* j, bool inverses)
         {d.ss_n, sizeof(int32_t)},
     };
     const size_t Nexc = size_t(j->ch.Nexc);
-    if (j->trans) {
+    if (exc(j)) {
         s.push_back({d.worb, W * 2 * Nmax * sizeof(int16_t)});
         s.push_back({d.wslot, W * 2 * Ns * sizeof(int16_t)});
         s.push_back({d.cur, W * sizeof(int32_t)});
@@ -732,6 +890,7 @@ std::vector<CkptSection> ckpt_sections(gv_job* j, bool inverses)
             s.push_back({d.gup, W * size_t(j->N[0]) * Nexc * es});
             s.push_back({d.gdn, W * Nmax * es});
         }
+        if (j->lng) s.push_back({d.gup, W * 2 * Nmax * size_t(Ns) * es});   // the overlap tables R
     }
     return s;
 }
@@ -817,7 +976,7 @@ gv_status gv_channel_orbitals(int32_t L, const double* bc, int32_t channel, cons
                               int32_t* orb, int32_t* N, int32_t* Nexc)
 {
     if (L < 2 || L > 64 || (L % 2) || !bc || !q || fl < 0 || fl > 1) return GV_ERR_INVALID;
-    if (channel != GV_CH_GROUNDSTATE && channel != GV_CH_TRANS) return GV_ERR_INVALID;
+    if (channel != GV_CH_GROUNDSTATE && channel != GV_CH_TRANS && channel != GV_CH_LONG) return GV_ERR_INVALID;
     Orbitals o = make_orbitals(L, bc[0], bc[1]);
     if (!o.ok) return GV_ERR_INVALID;
     Channel ch = make_channel(o, channel, q[0], q[1]);
@@ -833,10 +992,16 @@ gv_status gv_channel_orbitals(int32_t L, const double* bc, int32_t channel, cons
 gv_status gv_channel_states(int32_t L, const double* bc, int32_t channel, const int32_t* q, int32_t* exc_up,
                             int32_t* exc_dn)
 {
-    if (L < 4 || L > 32 || (L % 2) || !bc || !q || !exc_up || !exc_dn || channel != GV_CH_TRANS) return GV_ERR_INVALID;
+    if (L < 4 || L > 32 || (L % 2) || !bc || !q || !exc_up || !exc_dn) return GV_ERR_INVALID;
+    if (channel != GV_CH_TRANS && channel != GV_CH_LONG) return GV_ERR_INVALID;
     Orbitals o = make_orbitals(L, bc[0], bc[1]);
     if (!o.ok) return GV_ERR_INVALID;
     Channel ch = make_channel(o, channel, q[0], q[1]);
+    if (channel == GV_CH_LONG) {
+        if (!ch.ok) return GV_ERR_INVALID;
+        for (int k = 0; k < ch.Nexc; ++k) { exc_up[k] = ch.exc_up[k]; exc_dn[k] = ch.exc_dn[k]; }
+        return GV_OK;
+    }
     std::vector<int16_t> up, dn;
     if (!ch.ok || !trans_tables(ch, up, dn)) return GV_ERR_INVALID;
     for (int k = 0; k < ch.Nexc; ++k) { exc_up[k] = up[k]; exc_dn[k] = dn[k]; }
@@ -899,9 +1064,9 @@ gv_status gv_job_footprint(const gv_job_config* c, uint64_t* bytes)
 {
     if (!valid_config(c) || !bytes) return GV_ERR_INVALID;
     const uint64_t Ns = uint64_t(c->L) * c->L, Nk = Ns / 2, W = c->n_walkers;
-    const bool tr = c->channel == GV_CH_TRANS;
+    const bool tr = c->channel == GV_CH_TRANS, lg = c->channel == GV_CH_LONG;
     const uint64_t N0 = tr ? Ns / 2 + 1 : Ns / 2, N1 = tr ? Ns / 2 - 1 : Ns / 2, Nmax = std::max(N0, N1);
-    const uint64_t Nexc = tr ? Ns / 2 : 1;
+    const uint64_t Nexc = tr ? Ns / 2 : lg ? Ns + 1 : 1;
     const uint64_t es = c->precision == GV_PREC_FP64 ? 16 : 8;
     uint64_t b = 0;
     b += Ns * Nk * (16 + 8);                 // phase tables
@@ -917,6 +1082,11 @@ gv_status gv_job_footprint(const gv_job_config* c, uint64_t* bytes)
         b += W * (2 * Ns + 2 * Nmax) * 2;    // wavefunction Fock state
         b += W * 2 * Nexc * Nexc * 16;       // ProjHeis H and O sums
         if (c->precision == GV_PREC_MIXED) b += W * N1 * Nexc * 8;   // tensor-core overlap rows
+    }
+    if (lg) {
+        b += W * 2 * Nmax * Ns * es;         // overlap table R of both flavours
+        b += W * (2 * Ns + 2 * Nmax) * 2;    // wavefunction Fock state
+        b += W * 2 * Nexc * Nexc * 16;       // ProjHeis H and O sums
     }
     *bytes = b;
     return GV_OK;
@@ -936,7 +1106,12 @@ gv_status gv_job_create(const gv_job_config* cfg, gv_job** out)
     j->ch = make_channel(j->orb, cfg->channel, cfg->q[0], cfg->q[1]);
     if (!j->ch.ok) { delete j; return GV_ERR_INVALID; }
     j->trans = cfg->channel == GV_CH_TRANS;
+    j->lng = cfg->channel == GV_CH_LONG;
     if (j->trans && !trans_tables(j->ch, j->exu, j->exd)) { delete j; return GV_ERR_INVALID; }
+    if (j->lng) {
+        j->exu.assign(j->ch.exc_up.begin(), j->ch.exc_up.end());
+        j->exd.assign(j->ch.exc_dn.begin(), j->ch.exc_dn.end());
+    }
     j->Ns = L * L;
     j->Nk = j->orb.Nk;
     j->N[0] = j->ch.N[0];
@@ -1044,8 +1219,10 @@ gv_status gv_job_create(const gv_job_config* cfg, gv_job** out)
     d.worb = nullptr; d.wslot = nullptr; d.exc_up = nullptr; d.exc_dn = nullptr; d.cur = nullptr; d.wsign = nullptr;
     d.sigma = nullptr; d.gup = nullptr; d.gdn = nullptr; d.pjx = nullptr; d.zbuf = nullptr;
     d.track_sm = nullptr; d.track_lw = nullptr; d.track_n = nullptr; d.track_cap = 0;
-    if (j->trans) {
+    if (exc(j)) {
         const int Nexc = j->ch.Nexc;
+        // overlap rows: GupT and g (transverse); R of both flavours over every orbital (longitudinal)
+        const size_t gup = j->lng ? size_t(2) * j->Nmax * j->Ns : size_t(j->N[0]) * Nexc;
         int16_t *eu = nullptr, *ed = nullptr;
         if ((st = dalloc(j, &d.worb, size_t(j->W) * 2 * j->Nmax * sizeof(int16_t))) ||
             (st = dalloc(j, &d.wslot, size_t(j->W) * 2 * j->Ns * sizeof(int16_t))) ||
@@ -1054,7 +1231,7 @@ gv_status gv_job_create(const gv_job_config* cfg, gv_job** out)
             (st = dalloc(j, &d.cur, size_t(j->W) * sizeof(int32_t))) ||
             (st = dalloc(j, &d.wsign, size_t(j->W) * sizeof(int32_t))) ||
             (st = dalloc(j, &d.sigma, size_t(j->W) * sizeof(double))) ||
-            (st = dalloc(j, &d.gup, size_t(j->W) * j->N[0] * Nexc * es)) ||
+            (st = dalloc(j, &d.gup, size_t(j->W) * gup * es)) ||
             (st = dalloc(j, &d.gdn, size_t(j->W) * j->Nmax * es)) ||
             (st = dalloc(j, &d.pjx, size_t(j->W) * 2 * Nexc * Nexc * sizeof(cx<double>))))
             return fail(st);
@@ -1121,7 +1298,7 @@ static gv_status reset_quantities(gv_job* j)
     GV_CK(cudaMemsetAsync(j->d.sm_n, 0, sizeof(int32_t) * j->W, j->stream));
     GV_CK(cudaMemsetAsync(j->d.ss, 0, sizeof(double) * 10 * j->Ns * j->Ns, j->stream));
     GV_CK(cudaMemsetAsync(j->d.ss_n, 0, sizeof(int32_t), j->stream));
-    if (j->trans)
+    if (exc(j))
         GV_CK(cudaMemsetAsync(j->d.pjx, 0, sizeof(cx<double>) * 2 * size_t(j->W) * j->ch.Nexc * j->ch.Nexc, j->stream));
     if (j->d.track_n) GV_CK(cudaMemsetAsync(j->d.track_n, 0, sizeof(int32_t) * j->W, j->stream));
     return GV_OK;
@@ -1141,7 +1318,8 @@ gv_status gv_job_measure(gv_job* j)
     gv_status st = GV_OK;
     const int inner = mask & kInnerMask;
     if (inner)
-        st = j->trans ? measure_trans_dispatch(j, inner) : walk_dispatch(j, 0, 0, 1, inner, 1);
+        st = j->trans ? measure_trans_dispatch(j, inner)
+             : j->lng ? measure_long_dispatch(j, inner) : walk_dispatch(j, 0, 0, 1, inner, 1);
     if (!st && (mask & GV_MEAS_STATSPIN)) st = statspin_dispatch(j);
     if (!st && (mask & kTrackMask)) st = tracks_dispatch(j, mask);
     return st ? st : gv_job_synchronize(j);
@@ -1198,7 +1376,7 @@ gv_status gv_job_init_walkers(gv_job* j, const int8_t* up)
     const bool screen = j->cfg.precision == GV_PREC_MIXED && !up;
     std::vector<double> amax(W);
     for (int attempt = 0; attempt < 10; ++attempt) {
-        if (j->trans) {   // every walker starts in channel state 0
+        if (exc(j)) {   // every walker starts in channel state 0
             gv_status st = upload_wav(j, std::vector<WavHost>(W, wav_state0(j)));
             if (st) return st;
         }
@@ -1211,10 +1389,10 @@ gv_status gv_job_init_walkers(gv_job* j, const int8_t* up)
         bool again = false;
         for (int w = 0; w < W; ++w)
             if (status[w] == GV_ERR_SINGULAR && !up) { ran_init(j, w, &cfg[size_t(w) * Ns]); again = true; }
-        if (!again && j->trans) {
+        if (!again && exc(j)) {
             for (int w = 0; w < W; ++w)
                 if (status[w] != GV_OK) { j->ready = true; return status[w]; }
-            if ((st = trans_start(j))) return st;
+            if ((st = j->trans ? trans_start(j) : long_start(j))) return st;
         }
         if (!again && screen) {
             if ((st = inverse_max_abs(j, amax.data()))) return st;
@@ -1231,7 +1409,7 @@ gv_status gv_job_init_walkers(gv_job* j, const int8_t* up)
     for (int w = 0; w < W; ++w)
         if (status[w] != GV_OK) { j->ready = true; return status[w]; }
     j->ready = true;
-    return j->trans ? gv_job_synchronize(j) : GV_OK;
+    return exc(j) ? gv_job_synchronize(j) : GV_OK;
 }
 
 // The kernels of one MetroMC::Walk(len, meas) call, enqueued on the job's stream.
@@ -1243,8 +1421,10 @@ static gv_status enqueue_walk(gv_job* j, uint64_t len, uint64_t meas, int mask, 
     }
     gv_status st = GV_OK;
     const int inner = mask & kInnerMask;
-    if (!(mask & (GV_MEAS_STATSPIN | kTrackMask)) && !(j->trans && mask)) {
-        st = j->trans ? walk_trans_dispatch(j, len) : walk_dispatch(j, len, 0, meas, mask);
+    // the exciton walks measure in kernels of their own, between walk launches
+    auto exc_walk = [&](uint64_t n) { return j->trans ? walk_trans_dispatch(j, n) : walk_long_dispatch(j, n); };
+    if (!(mask & (GV_MEAS_STATSPIN | kTrackMask)) && !(exc(j) && mask)) {
+        st = exc(j) ? exc_walk(len) : walk_dispatch(j, len, 0, meas, mask);
     } else {
         // Split at the measurement points: steps [a, m] then measure after step m.
         uint64_t a = 0;
@@ -1252,14 +1432,14 @@ static gv_status enqueue_walk(gv_job* j, uint64_t len, uint64_t meas, int mask, 
             uint64_t m = (a == 0) ? 0 : ((a + meas - 1) / meas) * meas;   // next s with s % meas == 0, s >= a
             if (j->d.trace) j->d.trace = dtrace + a;
             if (m >= len) {
-                st = j->trans ? walk_trans_dispatch(j, len - a) : walk_dispatch(j, len - a, a, 0, 0);
+                st = exc(j) ? exc_walk(len - a) : walk_dispatch(j, len - a, a, 0, 0);
                 a = len;
                 break;
             }
             const uint64_t nsteps = m - a + 1;
-            if (j->trans) {
-                st = walk_trans_dispatch(j, nsteps);
-                if (!st && inner) st = measure_trans_dispatch(j, inner);
+            if (exc(j)) {
+                st = exc_walk(nsteps);
+                if (!st && inner) st = j->trans ? measure_trans_dispatch(j, inner) : measure_long_dispatch(j, inner);
             } else {
                 // ground state: ProjHeis / StagMagnZ inside the walk kernel at step m
                 st = walk_dispatch(j, nsteps, a, meas, inner);
@@ -1383,6 +1563,7 @@ static gv_status forced_walk(gv_job* j, int w, int v1, int v2, int accept, int k
     const bool fp64 = j->cfg.precision == GV_PREC_FP64;
     gv_status st;
     if (j->trans) st = fp64 ? launch_walk_trans<double>(j, 1) : launch_walk_trans<float>(j, 1);
+    else if (j->lng) st = fp64 ? launch_walk_long<double>(j, 1) : launch_walk_long<float>(j, 1);
     else if (j->nt == 128) st = fp64 ? launch_walk<double, 128, 0>(j, 1, 0, 0, 0, 0) : launch_walk<float, 128, 0>(j, 1, 0, 0, 0, 0);
     else st = fp64 ? launch_walk<double, 256, 0>(j, 1, 0, 0, 0, 0) : launch_walk<float, 256, 0>(j, 1, 0, 0, 0, 0);
     d.forced_walker = -1;
@@ -1406,7 +1587,7 @@ static gv_status walker_weight(gv_job* j, int w, double* mant, int32_t* e2)
     GV_CK(cudaStreamSynchronize(j->stream));
     GV_CK(copy_sync(&m, j->d.amp_m + w, sizeof(m), cudaMemcpyDeviceToHost));
     GV_CK(copy_sync(&e, j->d.amp_e + w, sizeof(e), cudaMemcpyDeviceToHost));
-    if (j->trans) GV_CK(copy_sync(&sigma, j->d.sigma + w, sizeof(double), cudaMemcpyDeviceToHost));
+    if (exc(j)) GV_CK(copy_sync(&sigma, j->d.sigma + w, sizeof(double), cudaMemcpyDeviceToHost));
     int k = 0;
     *mant = std::frexp((m.x * m.x + m.y * m.y) * sigma, &k);
     *e2 = 2 * e + k;
@@ -1626,6 +1807,7 @@ gv_status gv_job_virt_update(gv_job* j, int32_t walker, int32_t nset, const int3
     if (!j || !hops || !out || walker < 0 || walker >= j->W || nset < 0) return GV_ERR_INVALID;
     if (!j->ready) return GV_ERR_NOT_READY;
     if (j->trans) return virt_update_trans(j, walker, nset, hops, out);
+    if (j->lng) return virt_update_long(j, walker, nset, hops, out);
     if (nset == 0) return GV_OK;
     for (int i = 0; i < 4 * nset; ++i)
         if (hops[i] < -1 || hops[i] >= j->Ns) return GV_ERR_INVALID;
@@ -1679,7 +1861,7 @@ gv_status gv_job_read_amplitude(gv_job* j, double* mant, int32_t* exp10)
     std::vector<int32_t> e(j->W), sg(j->W, 1);
     GV_CK(copy_sync(m.data(), j->d.amp_m, sizeof(cx<double>) * j->W, cudaMemcpyDeviceToHost));
     GV_CK(copy_sync(e.data(), j->d.amp_e, sizeof(int32_t) * j->W, cudaMemcpyDeviceToHost));
-    if (j->trans) GV_CK(copy_sync(sg.data(), j->d.wsign, sizeof(int32_t) * j->W, cudaMemcpyDeviceToHost));
+    if (exc(j)) GV_CK(copy_sync(sg.data(), j->d.wsign, sizeof(int32_t) * j->W, cudaMemcpyDeviceToHost));
     for (int w = 0; w < j->W; ++w) m[w] = m[w] * double(sg[w]);   // SlaterDeterminant::Amp (SlaterDeterminant.cpp:94)
     for (int w = 0; w < j->W; ++w) {
         const double a = std::hypot(m[w].x, m[w].y);
@@ -1726,7 +1908,7 @@ gv_status gv_job_read_counts(gv_job* j, uint64_t* counts)
 gv_status gv_job_read_state_index(gv_job* j, int32_t* state)
 {
     if (!j || !state) return GV_ERR_INVALID;
-    if (!j->trans) {
+    if (!exc(j)) {
         for (int w = 0; w < j->W; ++w) state[w] = 0;
         return GV_OK;
     }
@@ -1739,7 +1921,7 @@ gv_status gv_job_read_projheis(gv_job* j, double* vals, int32_t* nmeas)
 {
     if (!j || !vals) return GV_ERR_INVALID;
     GV_CK(cudaStreamSynchronize(j->stream));
-    if (j->trans)
+    if (exc(j))
         GV_CK(copy_sync(vals, j->d.pjx, sizeof(cx<double>) * 2 * size_t(j->W) * j->ch.Nexc * j->ch.Nexc,
                          cudaMemcpyDeviceToHost));
     else
@@ -1751,7 +1933,7 @@ gv_status gv_job_read_projheis(gv_job* j, double* vals, int32_t* nmeas)
 gv_status gv_job_read_orbitals(gv_job* j, int32_t walker, int32_t fl, int32_t* orb)
 {
     if (!j || !orb || walker < 0 || walker >= j->W || fl < 0 || fl > 1) return GV_ERR_INVALID;
-    if (!j->trans) {
+    if (!exc(j)) {
         for (int f = 0; f < j->N[fl]; ++f) orb[f] = 2 * f;
         return GV_OK;
     }
@@ -1774,7 +1956,7 @@ gv_status gv_job_read_status(gv_job* j, int32_t* status)
 gv_status gv_job_read_weight(gv_job* j, double* sigma)
 {
     if (!j || !sigma) return GV_ERR_INVALID;
-    if (!j->trans) {
+    if (!exc(j)) {
         for (int w = 0; w < j->W; ++w) sigma[w] = 1.0;
         return GV_OK;
     }
@@ -1852,7 +2034,7 @@ constexpr int kTunable = GV_FLAG_DELAYED_UPDATES | GV_FLAG_STREAM_INVERSES;
 // at 256 threads; 2 / 3 as 0 / 1 with delayed updates; 4 on-chip (TMEM).
 bool tune_applicable(const gv_job* j, int v)
 {
-    if (j->trans) return false;
+    if (exc(j)) return false;
     const int dflt = pick_threads(j->Nmax);
     const int nt = (v == 1 || v == 3) ? 256 : dflt;
     if ((v == 1 || v == 3) && dflt == 256) return false;   // same as 0 / 2
@@ -1882,7 +2064,7 @@ gv_status gv_job_autotune(gv_job* j, uint64_t steps, int32_t* choice, double* us
     if (us_per_step)
         for (int v = 0; v < kTuneVariants; ++v) us_per_step[v] = -1.0;
     if (choice) *choice = -1;
-    if (j->trans) return GV_OK;   // one exciton walk kernel: nothing to choose
+    if (exc(j)) return GV_OK;   // one exciton walk kernel per channel: nothing to choose
     int dev = 0;
     GV_CK(cudaGetDevice(&dev));
     int wlog = 0;

@@ -290,6 +290,29 @@ __device__ __noinline__ void trans_rebuild(const DevJob& J, int w, const int16_t
     __syncthreads();
 }
 
+// Longitudinal exciton channel: rebuild R of both flavours of a freshly inverted walker from its stored
+// inverses: R[f][o] = sum_p phi_o(x_p) (A^-1)(p, f) for every orbital o
+// (the R A^-1 products of linalg::DetUpdate for every row a state can bring in).
+template <typename T, int NT>
+__device__ __noinline__ void long_rebuild(const DevJob& J, int w, const int16_t* part_s)
+{
+    const int N = J.N[0], Ns = J.Ns, Nk = J.Nk, L = J.L;
+    const cx<T>* phase = Tab<T>::phase(J);
+    for (int fl = 0; fl < 2; ++fl) {
+        const int16_t* part = part_s ? part_s + fl * J.Nmax : J.part + (size_t(w) * 2 + fl) * J.Nmax;
+        const cx<T>* cf = Tab<T>::coef(J) + (size_t(w) * 2 + fl) * 2 * Ns;
+        const cx<T>* A = ai_ptr<T>(J, fl, w);
+        cx<T>* R = static_cast<cx<T>*>(J.gup) + (size_t(w) * 2 + fl) * size_t(J.Nmax) * Ns;
+        for (int idx = threadIdx.x; idx < N * Ns; idx += NT) {
+            const int f = idx / Ns, o = idx % Ns;
+            cx<T> acc = {T(0), T(0)};
+            for (int p = 0; p < N; ++p) cmac(acc, phi_orb<T>(phase, cf, Nk, Ns, L, part[p], o), A[size_t(f) * N + p]);
+            R[idx] = acc;
+        }
+    }
+    __syncthreads();
+}
+
 // Initial inversion / re-inversion of every walker (only_due: only walkers
 // whose accepted-move count reached reinv_every, the deferred cadence).
 // m_in_smem: the Gauss-Jordan working matrix in shared memory (the launch
@@ -309,6 +332,7 @@ __global__ void __launch_bounds__(NT) k_invert(DevJob J, int only_due, int m_in_
     cx<double>* M = m_in_smem ? reinterpret_cast<cx<double>*>(p) : J.scratch64 + size_t(w) * J.Nmax * J.Nmax;
     const int st = reinvert_walker<T, NT>(J, w, M, S, nullptr);
     if (J.channel == GV_CH_TRANS && st == GV_OK) trans_rebuild<T, NT>(J, w, nullptr, J.cur[w]);
+    if (J.channel == GV_CH_LONG && st == GV_OK) long_rebuild<T, NT>(J, w, nullptr);
     if (threadIdx.x == 0) {
         J.status[w] = st;
         if (only_due) { J.since_reinv[w] = 0; J.counts[size_t(w) * 5 + 4] += 1; }
@@ -947,7 +971,7 @@ __global__ void k_tracks(DevJob J, int mask)
             const cx<double> a = J.amp_m[w];
             const double mag = hypot(a.x, a.y);
             double lw = mag > 0.0 ? 2.0 * (log10(mag) + double(J.amp_e[w]) * 0.30102999566398119521) : -INFINITY;
-            if (J.channel == GV_CH_TRANS) lw += log10(J.sigma[w]);
+            if (J.channel != GV_CH_GROUNDSTATE) lw += log10(J.sigma[w]);
             J.track_lw[at] = lw;
         }
         J.track_n[w] = n + 1;
@@ -999,7 +1023,7 @@ __global__ void __launch_bounds__(NT) k_statspin(DevJob J)
         if (!sub) pcol[fl * Nmax + f] = int16_t(o >> 1);
     }
     __syncthreads();
-    const bool scaled = J.channel == GV_CH_TRANS;
+    const bool scaled = J.channel != GV_CH_GROUNDSTATE;
     const double inv_sigma = scaled ? 1.0 / J.sigma[w] : 1.0;
     const cx<T>* A0 = ai_ptr<T>(J, 0, w);
     const cx<T>* A1 = ai_ptr<T>(J, 1, w);
@@ -1164,6 +1188,7 @@ __global__ void __launch_bounds__(NT, 2) k_check_reinvert(DevJob J, double thres
         cx<double>* M = m_in_smem ? reinterpret_cast<cx<double>*>(gp) : J.scratch64 + size_t(w) * Nmax * Nmax;
         const int st = reinvert_walker<T, NT>(J, w, M, S, nullptr);
         if (J.channel == GV_CH_TRANS && st == GV_OK) trans_rebuild<T, NT>(J, w, nullptr, J.cur[w]);
+        if (J.channel == GV_CH_LONG && st == GV_OK) long_rebuild<T, NT>(J, w, nullptr);
         if (tid == 0) { J.status[w] = st; J.counts[size_t(w) * 5 + 4] += 1; }
     } else if (tid == 0) {
         J.checks[w] += 1;

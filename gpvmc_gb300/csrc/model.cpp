@@ -183,6 +183,48 @@ Channel make_channel(const Orbitals& o, int kind, int qx, int qy)
             ch.exc_up.push_back(2 * fe + 1);
             ch.exc_dn.push_back(hole);
         }
+    } else if (kind == 2) {
+        // StagFluxLongExciton.cpp:6-66: for every upper-band orbital 2fe+1 the
+        // particle-hole pair (2fe+1, hole of k - q) in flavour 0 (state 2fe) or
+        // in flavour 1 (state 2fe+1); at q = 0 or (pi, pi) also the ground
+        // state (state Ns).  The states differ by up to two orbital hops in one
+        // flavour, so the single-hop table below is not built for this channel.
+        ch.N[0] = ch.N[1] = Ns / 2;
+        for (int fe = 0; fe < Ns / 2; ++fe) {
+            int Qk[2] = {((o.kx[fe] - qx) % L + L) % L, ((o.ky[fe] - qy) % L + L) % L};
+            mbz_fold(o, Qk);
+            const int hole = o.qn2fock[(Qk[0] * L + Qk[1]) * 2];
+            std::vector<char> full(Ns, 0), holed(Ns, 0);
+            for (int f = 0; f < Ns / 2; ++f) {
+                full[2 * f] = 1;
+                if (hole != 2 * f) holed[2 * f] = 1;
+            }
+            holed[2 * fe + 1] = 1;
+            for (int which = 0; which < 2; ++which) {
+                occ[0].push_back(which == 0 ? holed : full);
+                occ[1].push_back(which == 0 ? full : holed);
+                ch.exc_up.push_back(2 * fe + 1);
+                ch.exc_dn.push_back(hole);
+            }
+        }
+        if ((qx == 0 && qy == 0) || (qx == L / 2 && qy == L / 2)) {
+            std::vector<char> full(Ns, 0);
+            for (int f = 0; f < Ns / 2; ++f) full[2 * f] = 1;
+            occ[0].push_back(full);
+            occ[1].push_back(full);
+            ch.exc_up.push_back(-1);
+            ch.exc_dn.push_back(-1);
+        }
+        ch.Nexc = int(occ[0].size());
+        for (int fl = 0; fl < 2; ++fl) {
+            ch.fock0[fl].assign(Ns, ch.N[fl]);
+            int p = 0;
+            for (int x = 0; x < Ns; ++x)
+                if (occ[fl][0][x]) ch.fock0[fl][x] = p++;
+            if (p != ch.N[fl]) return ch;
+        }
+        ch.ok = true;
+        return ch;
     } else {
         return ch;
     }

@@ -58,12 +58,14 @@ zd phi_elem(const zd& phase, const zd& coef);
 // is the one-orbital hop (from, to) of flavour fl going from state a to b,
 // (-1,-1) if none (WaveFunction::AddState, WaveFunction.cpp:39-67).
 struct Channel {
-    int kind = 0;          // 0 groundstate, 1 transverse exciton
+    int kind = 0;          // 0 groundstate, 1 transverse exciton, 2 longitudinal exciton
     int N[2] = {0, 0};
     int Nexc = 0;
     std::vector<int32_t> fock0[2];        // state 0 Fock vectors: orbital -> particle or N
     std::vector<int32_t> hop_from, hop_to; // (a*Nexc + b)*2 + fl
-    // transverse exciton: flavour-0 upper-band orbital and flavour-1 hole of state k
+    // transverse exciton: flavour-0 upper-band orbital and flavour-1 hole of state k;
+    // longitudinal exciton: the particle-hole pair (exc_up, exc_dn) of state k, in
+    // flavour k % 2 for k < Ns, and -1 for the ground state (k = Ns)
     std::vector<int32_t> exc_up, exc_dn;
     bool ok = false;
 };

@@ -26,7 +26,7 @@ import numpy as np
 from . import _lib
 from ._lib import GvError, check
 
-CHANNELS = {"groundstate": _lib.GV_CH_GROUNDSTATE, "trans": _lib.GV_CH_TRANS}
+CHANNELS = {"groundstate": _lib.GV_CH_GROUNDSTATE, "trans": _lib.GV_CH_TRANS, "long": _lib.GV_CH_LONG}
 PRECISIONS = {"fp64": _lib.GV_PREC_FP64, "mixed": _lib.GV_PREC_MIXED}
 
 
@@ -82,6 +82,13 @@ class StagFluxGroundState(StagFluxWaveFunction):
 
 class StagFluxTransExciton(StagFluxWaveFunction):
     channel = "trans"
+
+
+class StagFluxLongExciton(StagFluxWaveFunction):
+    """StagFluxLongExciton (StagFluxLongExciton.cpp:6-66): a particle-hole pair
+    of momentum q in one flavour, L^2 states (+ the ground state at q = 0 or
+    (pi, pi))."""
+    channel = "long"
 
 
 class Job:
@@ -611,5 +618,6 @@ def pi_phi(phi_over_pi):
     return phi_over_pi * math.pi
 
 
-__all__ = ["SquareLattice", "StagFluxGroundState", "StagFluxTransExciton", "Job", "SlaterDeterminant",
+__all__ = ["SquareLattice", "StagFluxGroundState", "StagFluxTransExciton", "StagFluxLongExciton", "Job",
+           "SlaterDeterminant",
            "LatticeStepper", "MetroMC", "ProjHeis", "StagMagnZ", "StatSpinStruct", "GvError", "pi_phi"]

@@ -55,6 +55,7 @@ typedef int32_t gv_status;
 
 #define GV_CH_GROUNDSTATE 0   /* StagFluxGroundState */
 #define GV_CH_TRANS 1         /* StagFluxTransExciton */
+#define GV_CH_LONG 2          /* StagFluxLongExciton */
 
 #define GV_PREC_FP64 0        /* plain form: FP64 inverses, FP64 Sherman-Morrison */
 #define GV_PREC_MIXED 1       /* FP32 inverses/updates, FP64 periodic re-inversion */
@@ -359,9 +360,13 @@ gv_status gv_phi_table(int32_t L, double phi, double neel, double neel_exp, cons
 gv_status gv_lattice_neighbours(int32_t L, int32_t* nbr);
 gv_status gv_channel_orbitals(int32_t L, const double* phase_shift, int32_t channel, const int32_t* q,
                               int32_t fl, int32_t* orb, int32_t* N, int32_t* Nexc);
-/* gv_channel_states: the channel's state table, exciton channel only
- * (StagFluxTransExciton.cpp:7-44): state k adds orbital exc_up[k] to flavour
- * 0 and removes orbital exc_dn[k] from flavour 1 (Nexc entries each). */
+/* gv_channel_states: the channel's state table, exciton channels only.
+ * Transverse (StagFluxTransExciton.cpp:7-44): state k adds orbital exc_up[k]
+ * to flavour 0 and removes orbital exc_dn[k] from flavour 1.  Longitudinal
+ * (StagFluxLongExciton.cpp:6-66): state k < Ns replaces the lower-band
+ * orbital exc_dn[k] by the upper-band orbital exc_up[k] in flavour k % 2 (the
+ * other flavour fills the lower band); state Ns, present at q = 0 and
+ * q = (L/2, L/2), is the ground state (-1, -1).  Nexc entries each. */
 gv_status gv_channel_states(int32_t L, const double* phase_shift, int32_t channel, const int32_t* q,
                             int32_t* exc_up, int32_t* exc_dn);
 /* gv_fock_quantum_numbers: out[3*f + 0..2] = (kx, ky, band) of every fock

@@ -51,9 +51,14 @@ def test_invalid_arguments_are_rejected(lib):
     h = ctypes.c_void_p()
     assert lib.gv_job_create(ctypes.byref(cfg), ctypes.byref(h)) == _lib.GV_OK + 1
     assert lib.gv_job_create(None, ctypes.byref(h)) == 1
-    # the longitudinal exciton (channel 2) is not served: rejected before any device call
-    cfg.L, cfg.channel = 8, 2
+    # an unknown channel, and the longitudinal exciton beyond L = 24: rejected before any device call
+    cfg.L, cfg.channel = 8, 3
     assert lib.gv_job_create(ctypes.byref(cfg), ctypes.byref(h)) == 1 and not h.value
+    cfg.L, cfg.channel = 26, 2
+    assert lib.gv_job_create(ctypes.byref(cfg), ctypes.byref(h)) == 1 and not h.value
+    cfg.L = 16
+    assert lib.gv_job_footprint(ctypes.byref(cfg), ctypes.byref(out := ctypes.c_uint64())) == 0
+    assert out.value > 2 * 128 * 256 * 16                      # the overlap tables R per walker
     cfg.channel = 0
     out = ctypes.c_uint64()
     cfg.L = 16
@@ -111,3 +116,36 @@ def test_noalloc_rejects_bad_pointers_before_any_launch(lib):
     assert lib.gv_slater_invert_noalloc(None, P(0x20000), 4, P(0x30000), None) == 1
     assert lib.gv_slater_invert_noalloc(P(0x10000), P(0x20000), 129, P(0x30000), None) == 10
     assert lib.gv_slater_invert_noalloc(P(0x10000), P(0x20000), 0, P(0x30000), None) == 10
+
+
+@pytest.mark.parametrize("L,q", [(4, (2, 0)), (4, (0, 0)), (8, (4, 4)), (8, (2, 2)), (16, (8, 8))])
+def test_long_exciton_state_table(lib, L, q):
+    """StagFluxLongExciton.cpp:6-66: states 2fe / 2fe + 1 put the pair (2fe + 1,
+    hole at k - q) into flavour 0 / 1, the ground state is added at q = 0 and
+    (pi, pi); every hole is a lower-band orbital, each once per flavour, and the
+    pair carries momentum q up to the (pi, pi) fold."""
+    bc = (ctypes.c_double * 2)(1.0, 1.0)
+    qq = (ctypes.c_int32 * 2)(*q)
+    Ns = L * L
+    N, K = ctypes.c_int32(), ctypes.c_int32()
+    orb = np.zeros(Ns, dtype=np.int32)
+    assert lib.gv_channel_orbitals(L, bc, 2, qq, 0, orb.ctypes.data_as(ctypes.c_void_p), ctypes.byref(N),
+                                   ctypes.byref(K)) == 0
+    extra = q in ((0, 0), (L // 2, L // 2))
+    assert N.value == Ns // 2 and K.value == Ns + (1 if extra else 0)
+    up = np.zeros(K.value, dtype=np.int32)
+    dn = np.zeros(K.value, dtype=np.int32)
+    assert lib.gv_channel_states(L, bc, 2, qq, up.ctypes.data_as(ctypes.c_void_p),
+                                 dn.ctypes.data_as(ctypes.c_void_p)) == 0
+    fe = np.arange(Ns // 2)
+    assert (up[0:Ns:2] == 2 * fe + 1).all() and (up[1:Ns:2] == 2 * fe + 1).all()
+    assert (dn[0:Ns:2] == dn[1:Ns:2]).all() and (dn[:Ns] % 2 == 0).all()
+    assert sorted(dn[0:Ns:2].tolist()) == list(range(0, Ns, 2))
+    if extra:
+        assert up[Ns] == -1 and dn[Ns] == -1
+    qn = np.zeros(3 * Ns, dtype=np.int32)
+    assert lib.gv_fock_quantum_numbers(L, bc, qn.ctypes.data_as(ctypes.c_void_p)) == 0
+    qn = qn.reshape(Ns, 3)
+    for k in range(0, Ns, 2):
+        d = (qn[up[k], :2] - qn[dn[k], :2] - np.array(q)) % L
+        assert tuple(d) in ((0, 0), (L // 2, L // 2))
