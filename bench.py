@@ -515,6 +515,96 @@ def run_exciton(g, sweeps, fp64_sweeps):
 
 
 # ---------------------------------------------------------------------------
+# Longitudinal exciton (StagFluxLongExciton): L=16, q = (0,0) and (8,8)
+# (257 states each, the ground state included), N0 = N1 = 128.
+
+LONG_QS = [(0, 0), (8, 8)]
+LONG_WALKERS = 256
+
+
+def _cpu_long_chain(args):
+    walker, sweeps = args
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    import oracle_lib as ol
+    q = LONG_QS[walker % len(LONG_QS)]
+    o = ol.OracleChain(L, 0.25 * math.pi, 0.1, channel=ol.LONG, q=q, seed=SEED, walker=walker, timing_build=True)
+    if o.random_start():
+        return 0, 0.0
+    t0 = time.perf_counter()
+    o.walk(sweeps, meas=0)
+    return sweeps, time.perf_counter() - t0
+
+
+def cpu_long_baseline(cores, steps):
+    subprocess.run(["make", "-s", "-C", os.path.join(ROOT, "oracle"), "all"], check=True)
+    with mp.get_context("spawn").Pool(cores) as pool:
+        res = pool.map(_cpu_long_chain, [(w, steps) for w in range(cores)])
+    rates = [r[0] / r[1] for r in res if r[1] > 0]
+    return {"value": sum(rates), "unit": "steps/s", "cores": cores, "kind": "port", "per_core": statistics.mean(rates),
+            "sample": "%d independent longitudinal-exciton chains L=16 (q=(0,0), (8,8) alternating), %d Metropolis "
+                      "steps each, no measurement; oracle timing build" % (cores, steps)}
+
+
+def run_long(g, sweeps, fp64_sweeps):
+    """Both momenta at once (one stream per job), wall time between
+    synchronisations, ProjHeis H/O every sweep in the measured phase; the
+    mixed form's H/O error against FP64 on the same configurations."""
+    import numpy as np
+    out = {"workload": "longitudinal exciton L=16 (128x128 complex per spin, 257 states incl. the ground state), "
+                       "q=(0,0) and (8,8), %d walkers per q, ProjHeis H/O (257x257 each) every sweep" % LONG_WALKERS,
+           "unit": "steps/s"}
+    for prec, n in (("mixed", sweeps), ("fp64", fp64_sweeps)):
+        jobs = []
+        for i, q in enumerate(LONG_QS):
+            kw = dict(reinv_every=REINV)
+            if prec == "mixed":
+                kw["drift_threshold"] = DRIFT_THRESHOLD
+            j = g.Job(g.StagFluxLongExciton(L, 0.25 * math.pi, 0.1, q=q), walkers=LONG_WALKERS, seed=SEED,
+                      precision=prec, walker_base=i * LONG_WALKERS, **kw)
+            j.set_measurements(1)
+            j.init_walkers()
+            jobs.append(j)
+        for j in jobs:
+            j.walk(SWEEP, 0, sync=False)
+        for j in jobs:
+            j.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(n):
+            for j in jobs:
+                j.walk(SWEEP, 0, sync=False)
+        for j in jobs:
+            j.synchronize()
+        wall = time.perf_counter() - t0
+        steps = len(jobs) * LONG_WALKERS * SWEEP * n
+        j = jobs[0]
+        j.timer_start()
+        j.reset_quantities()
+        j.measure()
+        j.timer_stop()
+        mk, _ = j.kernel_ms(2)
+        out[prec] = {"value": steps / wall, "sweeps": n, "wall_s": wall, "measure_ms": mk,
+                     "measure_what": "one ProjHeis H/O measurement of one job's %d walkers (kernel time)" % LONG_WALKERS}
+        if prec == "mixed":
+            cfg = j.config()
+            pm, _ = j.projheis()
+            ref = g.Job(g.StagFluxLongExciton(L, 0.25 * math.pi, 0.1, q=LONG_QS[0]), walkers=LONG_WALKERS, seed=SEED,
+                        precision="fp64")
+            ref.set_measurements(1)
+            ref.init_walkers(cfg)
+            ref.reset_quantities()
+            ref.measure()
+            pr, _ = ref.projheis()
+            err = np.abs(pm - pr).max(axis=(1, 2)) / np.abs(pr).max(axis=(1, 2))
+            out["ho_error_vs_fp64"] = {"median": float(np.median(err)), "max": float(err.max()),
+                                       "what": "max |H,O mixed - H,O FP64| / max |H,O FP64| per walker, q=(0,0)"}
+            ref.close()
+        for j in jobs:
+            j.close()
+    out["mixed_over_fp64"] = out["mixed"]["value"] / out["fp64"]["value"]
+    return out
+
+
+# ---------------------------------------------------------------------------
 # Serving stream: Poisson arrivals (20 jobs/s) of heterogeneous requests --
 # L in {8,12,16,20,24}, phi ~ U[0,0.5) pi, neel ~ U[0,0.2), ground state 80% /
 # transverse exciton 20% (q on the diagonal), 64-1024 walkers (log-uniform) --
@@ -796,6 +886,7 @@ def main():
     ap.add_argument("--walkers", type=int, default=WALKERS, help="walkers (profiling a smaller case)")
     ap.add_argument("--no-exciton", action="store_true", help="skip the exciton-channel section")
     ap.add_argument("--no-serving", action="store_true", help="skip the serving-stream section")
+    ap.add_argument("--no-long", action="store_true", help="skip the longitudinal-exciton section")
     ap.add_argument("--no-pairs", action="store_true",
                     help="skip the StatSpinStruct tensor-core, graphs, autotune and L=12 sections")
     args = ap.parse_args()
@@ -822,11 +913,13 @@ def main():
         return
 
     WALKERS = args.walkers
-    cpu = cpu_exc = None
+    cpu = cpu_exc = cpu_lng = None
     if rank == 0 and world == 1 and not args.no_cpu:
         cpu = cpu_baseline(os.cpu_count() or 1, args.cpu_sweeps, reinv=0)
         if not args.no_exciton:
             cpu_exc = cpu_exciton_baseline(os.cpu_count() or 1, 4)
+        if not args.no_long:
+            cpu_lng = cpu_long_baseline(os.cpu_count() or 1, 2000)
 
     dist = None
     if world > 1:
@@ -863,6 +956,7 @@ def main():
                   "reinversion_policy": "FP64 re-inversion every 128 accepted exchanges", "steps": k}
 
     exc = run_exciton(g, 4, 1) if (rank == 0 and not args.no_exciton) else None
+    lng = run_long(g, 2, 1) if (rank == 0 and not args.no_long) else None
     c2 = run_config2(g) if (rank == 0 and not args.no_pairs) else None
     serving = run_serving(g) if (rank == 0 and world == 1 and not args.no_serving) else None
     pairs = run_pairs(g, WALKERS) if (rank == 0 and not args.no_pairs) else None
@@ -908,6 +1002,10 @@ def main():
         if cpu_exc:
             exc["cpu_baseline"] = {k: cpu_exc[k] for k in ("value", "unit", "cores", "kind", "sample", "per_core")}
         out["exciton"] = exc
+    if lng:
+        if cpu_lng:
+            lng["cpu_baseline"] = {k: cpu_lng[k] for k in ("value", "unit", "cores", "kind", "sample", "per_core")}
+        out["long_exciton"] = lng
     if serving:
         out["serving"] = serving
     if pairs:

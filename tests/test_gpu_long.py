@@ -188,7 +188,7 @@ def test_long_measurements(engine, oracle, L, q, seed, walker):
 
 
 def test_long_reinversion_cadence(engine, oracle):
-    L, q, seed, walker = 6, (2, 2), 4, 2
+    L, q, seed, walker = 6, (2, 2), 4, 3
     job, orc = _pair(engine, oracle, L, q, seed, walker, reinv=L * L)
     job.init_walkers()
     assert orc.random_start() == 0
