@@ -635,6 +635,14 @@ gv_status virt_update_long(gv_job* j, int walker, int nset, const int32_t* hops,
         if (!empty && (h[0] < 0 || h[1] < 0 || h[2] != h[1] || h[3] != h[0])) return GV_ERR_INVALID;   // exchanges only
     }
     if (nset == 0) return GV_OK;
+    {   // each exchange moves a flavour-0 particle from up_from and a flavour-1 particle from dn_from
+        std::vector<int16_t> fock(2 * size_t(j->Ns));
+        GV_CK(cudaStreamSynchronize(j->stream));
+        GV_CK(copy_sync(fock.data(), j->d.fock + size_t(walker) * 2 * j->Ns, fock.size() * sizeof(int16_t),
+                        cudaMemcpyDeviceToHost));
+        for (int i = 0; i < nset; ++i)
+            if (hops[4 * i] >= 0 && (fock[hops[4 * i]] < 0 || fock[j->Ns + hops[4 * i + 2]] < 0)) return GV_ERR_INVALID;
+    }
     constexpr int NT = 256;
     int32_t* dh = nullptr;
     double* dout = nullptr;

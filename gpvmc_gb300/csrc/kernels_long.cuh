@@ -124,7 +124,7 @@ template <typename T>
 __device__ __forceinline__ int long_cap(const LongFl<T>& D, int n, const int V[2], const int F[2], cx<T>* B)
 {
     int r[2];
-    for (int i = 0; i < n; ++i) r[i] = D.wslot[V[i]];
+    for (int i = 0; i < n; ++i) r[i] = max(int(D.wslot[V[i]]), 0);   // V[i] is occupied in the current state
     if (!D.moved) {
         for (int i = 0; i < n; ++i)
             for (int j = 0; j < n; ++j) B[i * n + j] = D.R[size_t(r[j]) * D.Ns + F[i]];
@@ -250,7 +250,7 @@ __host__ __device__ inline LongLayout long_layout(int Ns, int Nmax, int Nexc, bo
     l.q = al(c * Nexc);
     l.Y = al(c * 2 * 3 * Nmax);
     l.Bi = al(c * 2 * 9 + sizeof(int) * 16);
-    l.red = al(sizeof(double) * 4 * (NT / 32) + sizeof(int) * (NT / 32) + 64);
+    l.red = al(sizeof(double) * 6 * (NT / 32) + sizeof(int) * (NT / 32) + 64);
     l.gj = al(gj ? gj_smem_bytes(Nmax, NT) : 16);
     l.total = al(16);
     return l;
@@ -273,7 +273,7 @@ __device__ __forceinline__ void long_stage(const DevJob& J, int w, int s0, int t
     for (int idx = tid; idx < 2 * N; idx += NT) {
         const int fl = idx / N, f = idx % N;
         const int s = fl ? t0 : s0, t = fl ? s0 : t0;
-        const int c = s_fock[fl * Ns + s];
+        const int c = max(int(s_fock[fl * Ns + s]), 0);   // the exchange moves a particle of each flavour
         const cx<T>* cf = s_coef + fl * 2 * Ns;
         const int o = s_worb[fl * Nmax + f];
         const cx<T> a = ai_ptr<T>(J, fl, w)[size_t(f) * N + c];
@@ -472,7 +472,7 @@ __global__ void __launch_bounds__(NT) k_walk_long(DevJob J, uint64_t nsteps, int
                     h[0] = n; h[5] = m;
                     // a vanishing capacitance determinant is a singular update (linalg.cpp:562-570)
                     s_hop[13 + fl] = !(norm2(det3(B, m)) >= T(1e-9));
-                    for (int i = 0; i < n; ++i) { h[1 + i] = s_wslot[fl * Ns + V[i]]; h[3 + i] = F[i]; }
+                    for (int i = 0; i < n; ++i) { h[1 + i] = max(int(s_wslot[fl * Ns + V[i]]), 0); h[3 + i] = F[i]; }
                 }
                 __syncthreads();
                 if (s_hop[13] || s_hop[14]) { status = GV_ERR_SINGULAR; break; }
@@ -553,7 +553,7 @@ __global__ void __launch_bounds__(NT) k_walk_long(DevJob J, uint64_t nsteps, int
                         const int n = long_hops(cur, khop, fl, s_exu, s_exd, Ns, V, F);
                         odd ^= long_hop_parity(s_pre + fl * (Ns + 1), n, V, F);
                         for (int i = 0; i < n; ++i) {
-                            const int r = s_wslot[fl * Ns + V[i]];
+                            const int r = max(int(s_wslot[fl * Ns + V[i]]), 0);
                             s_wslot[fl * Ns + V[i]] = -1;
                             s_wslot[fl * Ns + F[i]] = int16_t(r);
                             s_worb[fl * Nmax + r] = int16_t(F[i]);
