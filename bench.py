@@ -690,6 +690,65 @@ def run_pairs(g, walkers):
             "error_what": "max |s+-, s-+ (engine) - same from fresh FP64 inverses| / max |s+-, s-+|"}
 
 
+def run_tc_projheis(g, walkers):
+    """Config 3: every sweep's ProjHeis from the split-TF32 tensor-core products
+    G = Phi A^-1 (GV_FLAG_TC_PROJHEIS; the nearest-neighbour pairs of G_up G_dn^T
+    are the bond ratios): time per measurement of all walkers, executed
+    tensor-pipe rate, and the E/site error against fresh FP64 inverses of the
+    same configurations; and the headline walk with ProjHeis taken that way."""
+    import numpy as np
+    from gpvmc_gb300.replicas import walker_base
+    wav = g.StagFluxGroundState(L, 0.25 * math.pi, 0.0)
+    common = dict(walkers=walkers, seed=SEED, reinv_every=REINV, walker_base=walker_base(0, walkers),
+                  phi_range=PHI_RANGE, neel_range=NEEL_RANGE, deferred_reinversion=True)
+    job = g.Job(wav, precision="mixed", drift_threshold=DRIFT_THRESHOLD, tc_projheis=True, **common)
+    job.set_measurements(1)
+    job.init_walkers()
+    for _ in range(4):
+        job.walk(SWEEP, 0, sync=False)
+    job.synchronize()
+    c0 = job.counts().sum(axis=0)
+    job.timer_start()
+    n = 8
+    for _ in range(n):
+        job.walk(SWEEP, SWEEP, sync=False)
+    ms, _ = job.timer_stop()
+    walk_steps = float((job.counts().sum(axis=0) - c0)[0])
+    meas_ms, meas_n = job.kernel_ms(2)
+    cfg = job.config()
+    job.reset_quantities()
+    job.measure()
+    e_tc = job.projheis()[0][:, 0].real
+    j64 = g.Job(wav, precision="fp64", **common)
+    j64.set_measurements(1)
+    j64.init_walkers(cfg)
+    j64.measure()
+    e64 = j64.projheis()[0][:, 0].real
+    j64.close()
+    job.close()
+    N = L * L // 2
+    per = meas_ms / max(1, meas_n)
+    useful = 2 * 8.0 * N ** 3 * walkers                # the two complex N^3 products restricted to used columns
+    full_g = 2 * 8.0 * (L * L) * N * N * walkers        # G = Phi(Ns x N) A^-1(N x N) per spin, in full
+    executed = 2 * 3 * 4 * 2.0 * 128 * N * N * walkers
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            peak_tf32 = float(json.load(f)["bf16_tflops"]) / 2
+    except Exception:
+        peak_tf32 = 1900.0 / 2
+    tens = executed / (per * 1e-3) / 1e12
+    d = np.abs(e_tc - e64)
+    return {"workload": "ProjHeis of %d walkers at L=16 from tensor-core pair products, per-walker phi/neel, "
+                        "every sweep of the headline walk" % walkers,
+            "kernel": "k_statspin_tc (mode ProjHeis): tcgen05.mma kind::tf32, split precision, FP32 accumulation",
+            "ms_per_measurement": per, "walk_with_tc_projheis_steps_per_s": walk_steps / (ms * 1e-3),
+            "useful_tflops": useful / (per * 1e-3) / 1e12,
+            "full_g_equivalent_tflops": full_g / (per * 1e-3) / 1e12,
+            "tensor_tflops_executed": tens, "tensor_peak_tflops": peak_tf32, "tensor_frac": tens / peak_tf32,
+            "tensor_peak_kind": "TF32 dense = half the measured bf16 dense burst (the nominal ratio)",
+            "e_site_error_vs_fp64": {"max": float(d.max()), "mean": float(d.mean()), "bar": 1e-5}}
+
+
 def run_graphs(g, calls=200):
     """Walk calls of a small job (L=8, 64 walkers, one sweep per call with
     ProjHeis, StagMagnZ and StatSpinStruct measured), enqueued kernel by
@@ -960,6 +1019,7 @@ def main():
     c2 = run_config2(g) if (rank == 0 and not args.no_pairs) else None
     serving = run_serving(g) if (rank == 0 and world == 1 and not args.no_serving) else None
     pairs = run_pairs(g, WALKERS) if (rank == 0 and not args.no_pairs) else None
+    tcph = run_tc_projheis(g, WALKERS) if (rank == 0 and not args.no_pairs) else None
     graphs = run_graphs(g) if (rank == 0 and not args.no_pairs) else None
     tune = run_autotune(g) if (rank == 0 and not args.no_pairs) else None
     e2e = run_e2e(g, args.precision, args.steps, rank) if not args.no_e2e else None
@@ -1010,6 +1070,8 @@ def main():
         out["serving"] = serving
     if pairs:
         out["statspin_tensor_cores"] = pairs
+    if tcph:
+        out["projheis_tensor_cores"] = tcph
     if graphs:
         out["cuda_graphs"] = graphs
     if tune:

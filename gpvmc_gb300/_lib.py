@@ -26,6 +26,7 @@ GV_FLAG_DELAYED_UPDATES = 4
 GV_FLAG_STREAM_INVERSES = 8
 GV_FLAG_SCALAR_PAIRS = 16
 GV_FLAG_CUDA_GRAPHS = 32
+GV_FLAG_TC_PROJHEIS = 64
 GV_CKPT_INVERSES = 1
 
 

@@ -144,7 +144,12 @@ bool valid_config(const gv_job_config* c)
     if (c->precision != GV_PREC_FP64 && c->precision != GV_PREC_MIXED) return false;
     if (c->reinv_every < 0) return false;
     if (c->flags & ~(GV_FLAG_REINV_DEFERRED | GV_FLAG_REINV_ON_DRIFT | GV_FLAG_DELAYED_UPDATES | GV_FLAG_STREAM_INVERSES |
-                     GV_FLAG_SCALAR_PAIRS | GV_FLAG_CUDA_GRAPHS))
+                     GV_FLAG_SCALAR_PAIRS | GV_FLAG_CUDA_GRAPHS | GV_FLAG_TC_PROJHEIS))
+        return false;
+    // ProjHeis from the tensor-core pair products: mixed ground state, N <= 128
+    if ((c->flags & GV_FLAG_TC_PROJHEIS) &&
+        (c->channel != GV_CH_GROUNDSTATE || c->precision != GV_PREC_MIXED || c->L * c->L / 2 > kTcM ||
+         (c->flags & GV_FLAG_SCALAR_PAIRS)))
         return false;
     if ((c->flags & GV_FLAG_REINV_ON_DRIFT) && (!(c->flags & GV_FLAG_REINV_DEFERRED) || !(c->drift_threshold > 0.0)))
         return false;
@@ -431,20 +436,24 @@ bool statspin_tc_ok(const gv_job* j)
            !(j->cfg.flags & GV_FLAG_SCALAR_PAIRS);
 }
 
-gv_status statspin_dispatch(gv_job* j)
+// mode bit 0: StatSpinStruct; bit 1: ProjHeis from the tensor-core pair products
+// (GV_FLAG_TC_PROJHEIS).
+gv_status statspin_dispatch(gv_job* j, int mode = 1)
 {
     if (statspin_tc_ok(j)) {
         const TcLayout lay = tc_layout(j->N[0]);
         GV_CK(raise_smem_limit(k_statspin_tc, lay.total));
         int slot;
         GV_CK(mark_begin(j, 2, &slot));
-        const int cells = j->Ns * ((j->W + 31) / 32);
-        k_occ_bits<<<(cells + 255) / 256, 256, 0, j->stream>>>(j->d, j->d.occ);
-        k_occ_pairs<<<j->Ns, 256, 0, j->stream>>>(j->d, j->d.occ);
-        k_statspin_tc<<<std::min(j->W, j->n_sm), kTcThreads, lay.total, j->stream>>>(j->d);
+        if (mode & 1) {   // antiparallel counts from occupation bitsets
+            const int cells = j->Ns * ((j->W + 31) / 32);
+            k_occ_bits<<<(cells + 255) / 256, 256, 0, j->stream>>>(j->d, j->d.occ);
+            k_occ_pairs<<<j->Ns, 256, 0, j->stream>>>(j->d, j->d.occ);
+            j->last_launches += 2;
+            j->total_launches += 2;
+        }
+        k_statspin_tc<<<std::min(j->W, j->n_sm), kTcThreads, lay.total, j->stream>>>(j->d, mode);
         GV_CK(cudaGetLastError());
-        j->last_launches += 2;
-        j->total_launches += 2;
         GV_CK(mark_end(j, slot));
         ++j->last_launches;
         ++j->total_launches;
@@ -1324,11 +1333,13 @@ gv_status gv_job_measure(gv_job* j)
     if (!j->ready) return GV_ERR_NOT_READY;
     const int mask = j->cfg.meas_mask;
     gv_status st = GV_OK;
-    const int inner = mask & kInnerMask;
+    const bool tcph = (j->cfg.flags & GV_FLAG_TC_PROJHEIS) && (mask & GV_MEAS_PROJHEIS);
+    const int inner = mask & kInnerMask & (tcph ? ~GV_MEAS_PROJHEIS : ~0);
+    const int pairs = ((mask & GV_MEAS_STATSPIN) ? 1 : 0) | (tcph ? 2 : 0);
     if (inner)
         st = j->trans ? measure_trans_dispatch(j, inner)
              : j->lng ? measure_long_dispatch(j, inner) : walk_dispatch(j, 0, 0, 1, inner, 1);
-    if (!st && (mask & GV_MEAS_STATSPIN)) st = statspin_dispatch(j);
+    if (!st && pairs) st = statspin_dispatch(j, pairs);
     if (!st && (mask & kTrackMask)) st = tracks_dispatch(j, mask);
     return st ? st : gv_job_synchronize(j);
 }
@@ -1428,10 +1439,13 @@ static gv_status enqueue_walk(gv_job* j, uint64_t len, uint64_t meas, int mask, 
         if (rs) return rs;
     }
     gv_status st = GV_OK;
-    const int inner = mask & kInnerMask;
+    // GV_FLAG_TC_PROJHEIS: ProjHeis from the tensor-core pair pass instead of inside the walk
+    const bool tcph = (j->cfg.flags & GV_FLAG_TC_PROJHEIS) && (mask & GV_MEAS_PROJHEIS);
+    const int inner = mask & kInnerMask & (tcph ? ~GV_MEAS_PROJHEIS : ~0);
+    const int pairs = ((mask & GV_MEAS_STATSPIN) ? 1 : 0) | (tcph ? 2 : 0);
     // the exciton walks measure in kernels of their own, between walk launches
     auto exc_walk = [&](uint64_t n) { return j->trans ? walk_trans_dispatch(j, n) : walk_long_dispatch(j, n); };
-    if (!(mask & (GV_MEAS_STATSPIN | kTrackMask)) && !(exc(j) && mask)) {
+    if (!(mask & (GV_MEAS_STATSPIN | kTrackMask)) && !(exc(j) && mask) && !tcph) {
         st = exc(j) ? exc_walk(len) : walk_dispatch(j, len, 0, meas, mask);
     } else {
         // Split at the measurement points: steps [a, m] then measure after step m.
@@ -1452,7 +1466,7 @@ static gv_status enqueue_walk(gv_job* j, uint64_t len, uint64_t meas, int mask, 
                 // ground state: ProjHeis / StagMagnZ inside the walk kernel at step m
                 st = walk_dispatch(j, nsteps, a, meas, inner);
             }
-            if (!st && (mask & GV_MEAS_STATSPIN)) st = statspin_dispatch(j);
+            if (!st && pairs) st = statspin_dispatch(j, pairs);
             if (!st && (mask & kTrackMask)) st = tracks_dispatch(j, mask);
             a = m + 1;
         }

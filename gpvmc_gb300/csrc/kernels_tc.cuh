@@ -45,7 +45,7 @@ constexpr int kTcWaitLimit = 1 << 22;     // mbarrier polls before a wait gives 
 __host__ __device__ inline int tc_ncols(int N) { return (N + 15) & ~15; }
 
 struct TcLayout {
-    size_t a[4], b[6], site, coef, bar, tbase, total;
+    size_t a[4], b[6], site, coef, bar, tbase, red, total;
 };
 
 // Operand tiles at 1024-byte multiples from a 1024-aligned base:
@@ -66,6 +66,8 @@ __host__ __device__ inline TcLayout tc_layout(int N)
     o += 8;
     l.tbase = o;
     o += 8;
+    l.red = o;                                 // per-warp ProjHeis partial sums
+    o += sizeof(double) * 4 * (kTcThreads / 32);
     l.total = o + 1024;   // room to align the base
     return l;
 }
@@ -343,7 +345,12 @@ __device__ __forceinline__ int tc_next_walker(const DevJob& J, int w)
     return -1;
 }
 
-__global__ void __launch_bounds__(kTcThreads, 1) k_statspin_tc(DevJob J)
+// mode bit 0: StatSpinStruct pair sums (StatSpinStruct.cpp:16-135); bit 1:
+// ProjHeis (ProjHeis.cpp:40-158) from the same products: the pairs whose up
+// and down sites are nearest neighbours are the antiparallel bonds, and with
+// n_anti of them E/site = (Ns / 2 - n_anti / 2 - sum_bonds r / 2) / Ns per
+// walker (parallel bonds +1/4, antiparallel -1/4 - r/2).
+__global__ void __launch_bounds__(kTcThreads, 1) k_statspin_tc(DevJob J, int mode)
 {
     extern __shared__ __align__(16) char smem_raw[];
     const uint32_t raw = smem_addr(smem_raw);
@@ -356,6 +363,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_statspin_tc(DevJob J)
     cx<float>* s_coef = reinterpret_cast<cx<float>*>(base + lay.coef);  // [buf][fl][sub][f]
     uint64_t* s_bar = reinterpret_cast<uint64_t*>(base + lay.bar);
     uint32_t* s_tbase = reinterpret_cast<uint32_t*>(base + lay.tbase);
+    double* s_red = reinterpret_cast<double*>(base + lay.red);
     const uint32_t bar = smem_addr(s_bar);
     double* T = J.ss;
 
@@ -459,6 +467,11 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_statspin_tc(DevJob J)
         const int lg = warp & 3, c = 32 * lg + lane;
         const bool crow = c < N;
         const int si = crow ? st[c] : 0;
+        int nb[4];
+#pragma unroll
+        for (int k = 0; k < 4; ++k) nb[k] = J.nbr[si * 4 + k];
+        cx<double> eb = {0.0, 0.0};   // sum of the bond ratios of this thread's pairs
+        int nanti = 0;
         for (int cc = warp >> 2; cc < Nt / 16; cc += 2) {
             uint32_t r[64];
             const uint32_t ta = tbase + (uint32_t(32 * lg) << 16) + uint32_t(16 * cc);
@@ -475,15 +488,42 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_statspin_tc(DevJob J)
                         const cx<float> gu = {__uint_as_float(r[t]), __uint_as_float(r[16 + t])};
                         const cx<float> gd = {__uint_as_float(r[32 + t]), __uint_as_float(r[48 + t])};
                         const cx<float> v = cmul_rn(gu, gd);
-                        const size_t ij = size_t(si) * Ns + st[kTcM + q];
-                        atomicAdd(&T[2 * ij], f32_to_f64(v.x));
-                        atomicAdd(&T[2 * ij + 1], f32_to_f64(v.y));
+                        const int sj = st[kTcM + q];
+                        if (mode & 1) {
+                            const size_t ij = size_t(si) * Ns + sj;
+                            atomicAdd(&T[2 * ij], f32_to_f64(v.x));
+                            atomicAdd(&T[2 * ij + 1], f32_to_f64(v.y));
+                        }
+                        if ((mode & 2) && (sj == nb[0] || sj == nb[1] || sj == nb[2] || sj == nb[3])) {
+                            eb.x += f32_to_f64(v.x);
+                            eb.y += f32_to_f64(v.y);
+                            ++nanti;
+                        }
                     }
                 }
             }
         }
         tmem_fence_before();
-        if (tid == 0) atomicAdd(J.ss_n, w == 0 ? 1 : 0);
+        if (mode & 2) {   // the walker's ProjHeis sample
+#pragma unroll
+            for (int o = 16; o; o >>= 1) {
+                eb.x += __shfl_xor_sync(0xffffffffu, eb.x, o);
+                eb.y += __shfl_xor_sync(0xffffffffu, eb.y, o);
+                nanti += __shfl_xor_sync(0xffffffffu, nanti, o);
+            }
+            if (lane == 0) { s_red[warp * 4] = eb.x; s_red[warp * 4 + 1] = eb.y; s_red[warp * 4 + 2] = double(nanti); }
+            __syncthreads();
+            if (tid == 0) {
+                double ex = 0.0, ey = 0.0, na = 0.0;
+                for (int q = 0; q < kTcThreads / 32; ++q) { ex += s_red[q * 4]; ey += s_red[q * 4 + 1]; na += s_red[q * 4 + 2]; }
+                const double inv_ns = 1.0 / double(Ns);
+                J.pj[size_t(w) * 2].x += (0.5 * Ns - 0.5 * na - 0.5 * ex) * inv_ns;
+                J.pj[size_t(w) * 2].y += -0.5 * ey * inv_ns;
+                J.pj[size_t(w) * 2 + 1].x += 1.0;
+                J.pj_n[w] += 1;
+            }
+        }
+        if (tid == 0 && (mode & 1)) atomicAdd(J.ss_n, w == 0 ? 1 : 0);
         first = true;   // the next walker's first MMAs follow the __syncthreads of its first chunk
         w = wn;
         b ^= 1;

@@ -96,7 +96,8 @@ class Job:
 
     def __init__(self, wav, walkers=1, seed=1234, precision="fp64", reinv_every=0, walker_base=0,
                  phi_range=None, neel_range=None, deferred_reinversion=False, drift_threshold=None,
-                 delayed_updates=False, stream_inverses=False, scalar_pairs=False, cuda_graphs=False):
+                 delayed_updates=False, stream_inverses=False, scalar_pairs=False, cuda_graphs=False,
+                 tc_projheis=False):
         L = _lib.lib()
         cfg = _lib.JobConfig()
         cfg.L = wav.L
@@ -126,6 +127,8 @@ class Job:
             cfg.flags |= _lib.GV_FLAG_SCALAR_PAIRS
         if cuda_graphs:
             cfg.flags |= _lib.GV_FLAG_CUDA_GRAPHS
+        if tc_projheis:
+            cfg.flags |= _lib.GV_FLAG_TC_PROJHEIS
         self.cfg = cfg
         self.wav = wav
         self.walkers = walkers

@@ -77,6 +77,11 @@ typedef int32_t gv_status;
                                      quantities) into a CUDA graph once and replay it: one
                                      launch per call instead of one per kernel (not while a
                                      job timer runs or a walk is traced) */
+#define GV_FLAG_TC_PROJHEIS 64    /* mixed ground state, N <= 128: ProjHeis from the split-TF32
+                                     tensor-core products G = Phi A^-1 of every antiparallel
+                                     pair (the nearest-neighbour pairs are the bonds) instead
+                                     of the per-particle FP32 dot products in the walk kernel;
+                                     GV_ERR_INVALID at creation where it does not apply */
 #define GV_FLAG_SCALAR_PAIRS 16   /* mixed precision: StatSpinStruct pair ratios (ground state)
                                      and the exciton ProjHeis overlap rows Z = GupT^T Phi from
                                      FP32 dot products on the CUDA cores instead of split-TF32

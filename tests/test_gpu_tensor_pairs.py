@@ -140,3 +140,43 @@ def test_bounded_wait_gives_up_with_a_status(engine, oracle):
     want, _ = _measure(ref, oracle)
     # the job-wide sums are FP64 atomics over walkers: equal up to summation order
     assert np.abs(ok - want).max() <= 1e-12 * np.abs(want).max()
+
+
+@pytest.mark.parametrize("L,W", [(8, 24), (16, 40)])
+def test_tensor_core_projheis(engine, oracle, L, W):
+    """GV_FLAG_TC_PROJHEIS: ProjHeis from the split-TF32 tensor-core pair
+    products (G = Phi A^-1, nearest-neighbour pairs) equals the per-particle
+    FP32 dot products on the same FP32 inverses to 5e-6 in E/site, and fresh
+    FP64 inverses of the same configurations to 1e-5; in a walk it measures
+    once per measurement point."""
+    jt = _mixed(engine, L, W, 5, tc_projheis=True)
+    jt.set_measurements(oracle.MEAS_PROJHEIS | oracle.MEAS_STAGMAGN)
+    jt.init_walkers()
+    jt.walk(L * L * 4, L * L)
+    pj, n = jt.projheis()
+    sm, ns = jt.stagmagn()
+    assert (n == 4).all() and (ns == 4).all() and np.isfinite(pj).all()
+    jt.reinvert()
+    cfg = jt.config()
+    jt.reset_quantities()
+    jt.measure()
+    e_tc = jt.projheis()[0][:, 0].real
+    jc = _mixed(engine, L, W, 5)
+    jc.set_measurements(oracle.MEAS_PROJHEIS)
+    jc.init_walkers(cfg)
+    jc.measure()
+    e_cc = jc.projheis()[0][:, 0].real
+    j64 = engine.Job(engine.StagFluxGroundState(L, PHI, 0.1), walkers=W, seed=5, precision="fp64")
+    j64.set_measurements(oracle.MEAS_PROJHEIS)
+    j64.init_walkers(cfg)
+    j64.measure()
+    e64 = j64.projheis()[0][:, 0].real
+    assert np.abs(e_tc - e_cc).max() < 5e-6
+    assert np.abs(e_tc - e64).max() < 1e-5
+
+
+def test_tensor_core_projheis_rejected_where_it_does_not_apply(engine):
+    with pytest.raises(engine.GvError):
+        engine.Job(engine.StagFluxGroundState(8, PHI, 0.1), walkers=2, seed=1, precision="fp64", tc_projheis=True)
+    with pytest.raises(engine.GvError):
+        engine.Job(engine.StagFluxGroundState(20, PHI, 0.1), walkers=2, seed=1, precision="mixed", tc_projheis=True)
