@@ -789,7 +789,7 @@ def run_autotune(g):
                     "min(walkers, 4 x SMs) walkers, one timed sweep after one warm-up sweep"}
 
 
-def serving_requests(g, n=SERVE_JOBS):
+def serving_requests(g, n=SERVE_JOBS, scale=SERVE_SWEEP_SCALE):
     import numpy as np
     rng = np.random.default_rng(SEED)
     reqs, t = [], 0.0
@@ -803,9 +803,9 @@ def serving_requests(g, n=SERVE_JOBS):
         else:
             wav = g.StagFluxGroundState(L, phi, neel)
         walkers = int(round(math.exp(rng.uniform(math.log(64), math.log(1024)))))
-        sweeps = max(1, int(round(math.exp(rng.uniform(math.log(1e3), math.log(1e4))) / SERVE_SWEEP_SCALE)))
+        sweeps = max(1, int(round(math.exp(rng.uniform(math.log(1e3), math.log(1e4))) / scale)))
         reqs.append((t, dict(wav=wav, walkers=walkers, sweeps=sweeps, therm_sweeps=max(1, sweeps // 5),
-                             seed=SEED + i, walker_base=0, precision="mixed", validate=(i % 6 == 0))))
+                             seed=SEED + i, walker_base=0, precision="mixed", validate=True)))
     return reqs
 
 
@@ -832,6 +832,14 @@ def run_serving(g):
               if r["status"] == 0 and r["validation_error"] >= 0 and q["wav"].channel == "groundstate"]
     tr_err = [r["validation_error"] for (t, q), r in zip(reqs, res)
               if r["status"] == 0 and r["validation_error"] >= 0 and q["wav"].channel == "trans"]
+    # The sustained arrival rate for the unscaled request distribution (1e3-1e4
+    # sweeps): the stream kept the device saturated (queue p99 above), so its
+    # steps/s is the mix's service capacity, and a queue stays bounded while
+    # rate x mean steps per request < capacity.
+    unscaled = serving_requests(g, n=4000, scale=1)
+    mean_steps = float(np.mean([q["walkers"] * (q["sweeps"] + q["therm_sweeps"]) * q["wav"].L ** 2
+                                for _, q in unscaled]))
+    cap = steps / span
     return {"workload": "%d requests, Poisson arrivals at %g/s, L~U{8,12,16,20,24}, phi~U[0,0.5)pi, "
                         "neel~U[0,0.2), ground state 80%% / transverse exciton 20%% (q on the diagonal), "
                         "64-1024 walkers log-uniform, sweeps log-uniform [1e3,1e4] scaled by 1/%d, mixed "
@@ -844,6 +852,13 @@ def run_serving(g):
             "e_site_error_vs_fp64_max": max(gs_err) if gs_err else None,
             "exciton_ho_error_vs_fp64_max": max(tr_err) if tr_err else None,
             "validated_jobs": len(gs_err) + len(tr_err),
+            "unscaled": {"mean_steps_per_request": mean_steps,
+                         "sustained_rate_jobs_per_s": cap / mean_steps,
+                         "rate_at_80pct_load_jobs_per_s": 0.8 * cap / mean_steps,
+                         "requested_rate_jobs_per_s": SERVE_RATE,
+                         "what": "the unscaled distribution (1e3-1e4 sweeps log-uniform, thermalisation a fifth of "
+                                 "that) needs mean_steps_per_request Metropolis steps per request; at the stream's "
+                                 "saturated service rate the queue stays bounded below sustained_rate"},
             "what": "latency = done - submitted (host clock, includes queueing, walker start and FP64 start "
                     "inversions); error: the job's final configurations measured with its own inverses and "
                     "with fresh FP64 inverses"}
@@ -946,6 +961,7 @@ def main():
     ap.add_argument("--no-exciton", action="store_true", help="skip the exciton-channel section")
     ap.add_argument("--no-serving", action="store_true", help="skip the serving-stream section")
     ap.add_argument("--no-long", action="store_true", help="skip the longitudinal-exciton section")
+    ap.add_argument("--serving-only", action="store_true", help="only the serving stream (profiling runs)")
     ap.add_argument("--no-pairs", action="store_true",
                     help="skip the StatSpinStruct tensor-core, graphs, autotune and L=12 sections")
     args = ap.parse_args()
@@ -972,6 +988,10 @@ def main():
         return
 
     WALKERS = args.walkers
+    if args.serving_only:
+        import gpvmc_gb300 as g
+        print(json.dumps({"serving": run_serving(g)}))
+        return
     cpu = cpu_exc = cpu_lng = None
     if rank == 0 and world == 1 and not args.no_cpu:
         cpu = cpu_baseline(os.cpu_count() or 1, args.cpu_sweeps, reinv=0)

@@ -6,8 +6,8 @@
 //   step_driver gs|trans L phi_over_pi neel seed steps qx qy fp64|mixed
 // Output lines:
 //   S v1 v2 khop accepted ratio        one per step of the first half
-//   V <re im exp10 of VirtUpdate(rhop, khop, qs) for every state, no hop and the
-//      first antiparallel bond> after the first half
+//   V K Nr state <re im exp10 of VirtUpdate(rhop, khop, qs) for every state, no hop
+//      and the first antiparallel bond> after the first half, with the current state
 //   C <occupation of the sites>        final configuration (1 = flavour 0)
 //   A re im exp10 state                final amplitude and channel state
 #include <cstdio>
@@ -42,12 +42,13 @@ int main(int argc, char** argv)
         for (int s = 0; s < steps / 2; ++s) {
             const gv::BigDouble new_weight = stepper.trystep();
             const gv::BigDouble ratio = new_weight / state_weight;
+            const int khop = stepper.Khop();   // the proposal's arg-max state, before step() clears it
             const bool acc = varmc.YesNo(ratio);
             if (acc) {
                 stepper.step();
                 state_weight = new_weight;
             }
-            std::printf("S %d %d %d %d %.17e\n", stepper.Proposal(0), stepper.Proposal(1), stepper.Khop(), int(acc),
+            std::printf("S %d %d %d %d %.17e\n", stepper.Proposal(0), stepper.Proposal(1), khop, int(acc),
                         double(ratio));
         }
         // SlaterDeterminant::VirtUpdate with the reference's hop-path sets: the
@@ -70,7 +71,7 @@ int main(int argc, char** argv)
             const auto khop = stepper.GetWaveFunction()->GetHops();
             std::vector<gv::BigComplex> qs;
             stepper.GetAmp()->VirtUpdate(rhop, khop, qs);
-            std::printf("V %d %d", int(khop.size()), int(rhop.size()));
+            std::printf("V %d %d %d", int(khop.size()), int(rhop.size()), stepper.GetWaveFunction()->GetCurrentState());
             for (const auto& q : qs) std::printf(" %.17e %.17e %d", q.mantissa().real(), q.mantissa().imag(), q.exponent10());
             std::printf("\n");
         }

@@ -132,10 +132,12 @@ def test_long_trace_parity(engine, oracle, L, q, seed, walker, steps):
 
 @pytest.mark.parametrize("name,steps", [("long_L4_q20.npz", 1500), ("long_L4_q00.npz", 1500)])
 def test_long_matches_reference_fixture(engine, name, steps):
-    """The engine against the reference build's own trace (tests/golden,
+    """The engine against the reference build's own run (tests/golden,
     generated by tests/golden/make_golden.py from the reference compiled with
-    its shims): proposals, decisions and ratios (1e-9: the fixtures are
-    x86_64 libm tables, the engine's host tables use this machine's libm)."""
+    its shims): proposals, decisions and ratios over 1500 steps, then the
+    ProjHeis H / O sums of six measured sweeps and the final configuration
+    (1e-9: the fixtures are x86_64 libm tables, the engine's host tables use
+    this machine's libm)."""
     g = np.load(os.path.join(GOLD, name))
     L = 4
     job = engine.Job(engine.StagFluxLongExciton(L, PHI, 0.1, q=tuple(g["q"])), walkers=1, seed=7, walker_base=3)
@@ -151,7 +153,13 @@ def test_long_matches_reference_fixture(engine, name, steps):
         real = g["kind"] == 1
         err = np.abs(tg["ratio"][real] - g["ratio"][real])
         assert (err <= 1e-9 * np.abs(g["ratio"][real]) + 1e-13).all()
+        # then six measured sweeps: the reference's ProjHeis H / O sums and final configuration
+        job.set_measurements(1)
+        job.walk(L * L * 6, L * L)
+        pj, nm = job.projheis()
+        assert nm[0] == int(g["n"])
         assert (job.config()[0] == g["final"]).all()
+        assert np.abs(pj[0] - g["pj"]).max() < 1e-9 * np.abs(g["pj"]).max()
 
 
 @pytest.mark.parametrize("L,q,seed,walker", [(4, (2, 0), 7, 3), (6, (2, 2), 2, 3), (8, (4, 4), 3, 3)])
