@@ -79,6 +79,8 @@ struct gv_job {
         int w = -1, v1 = 0, v2 = 0, khop = -1;
     } pend;
     gv_trace* step_trace = nullptr;      // device record of a single-walker step
+    void* diag = nullptr;                // scratch of the diagnostic entry points (grown on demand)
+    size_t diag_bytes = 0;
 };
 
 namespace {
@@ -129,6 +131,40 @@ gv_status dalloc(gv_job* j, P** ptr, size_t bytes)
     GV_CK(cudaMemsetAsync(p, 0, bytes ? bytes : 16, j->stream));
     j->allocs.push_back(p);
     *ptr = static_cast<P*>(p);
+    return GV_OK;
+}
+
+// Device scratch for the diagnostic entry points (VirtUpdate, drift, traces,
+// start-state overlaps): allocated once and grown when a call needs more, so
+// that repeated calls allocate nothing.  Every user finishes (synchronises)
+// before it returns, so one buffer per job serves them all.
+gv_status diag_scratch(gv_job* j, size_t bytes, void** out)
+{
+    bytes = (bytes + 255) & ~size_t(255);
+    if (bytes > j->diag_bytes) {
+        if (j->diag) {
+            GV_CK(cudaStreamSynchronize(j->stream));
+            cudaFree(j->diag);
+            j->diag = nullptr;
+            j->diag_bytes = 0;
+        }
+        GV_CK(cudaMalloc(&j->diag, bytes));
+        j->diag_bytes = bytes;
+    }
+    *out = j->diag;
+    return GV_OK;
+}
+
+// Two regions of one diagnostic scratch: a at offset 0, b at the next 256-byte boundary.
+template <typename A, typename B>
+gv_status diag_pair(gv_job* j, size_t na, size_t nb, A** a, B** b)
+{
+    const size_t off = (sizeof(A) * na + 255) & ~size_t(255);
+    void* p = nullptr;
+    gv_status st = diag_scratch(j, off + sizeof(B) * nb, &p);
+    if (st) return st;
+    *a = static_cast<A*>(p);
+    *b = reinterpret_cast<B*>(static_cast<char*>(p) + off);
     return GV_OK;
 }
 
@@ -656,8 +692,8 @@ gv_status virt_update_long(gv_job* j, int walker, int nset, const int32_t* hops,
     int32_t* dh = nullptr;
     double* dout = nullptr;
     const size_t nout = size_t(2) * nset * j->ch.Nexc;
-    GV_CK(cudaMalloc(&dh, sizeof(int32_t) * 4 * nset));
-    if (cudaMalloc(&dout, sizeof(double) * nout)) { cudaFree(dh); return GV_ERR_OOM; }
+    gv_status st = diag_pair(j, size_t(4) * nset, nout, &dh, &dout);
+    if (st) return st;
     cudaError_t e = copy_async(dh, hops, sizeof(int32_t) * 4 * nset, cudaMemcpyHostToDevice, j->stream);
     if (!e) {
         if (j->cfg.precision == GV_PREC_FP64) {
@@ -673,8 +709,6 @@ gv_status virt_update_long(gv_job* j, int walker, int nset, const int32_t* hops,
     }
     if (!e) e = copy_async(out, dout, sizeof(double) * nout, cudaMemcpyDeviceToHost, j->stream);
     if (!e) e = cudaStreamSynchronize(j->stream);
-    cudaFree(dh);
-    cudaFree(dout);
     return cuda_status(e);
 }
 
@@ -715,8 +749,8 @@ gv_status virt_update_trans(gv_job* j, int walker, int nset, const int32_t* hops
     const size_t nout = size_t(nset) * j->ch.Nexc * 2;
     int32_t* dh = nullptr;
     double* dout = nullptr;
-    GV_CK(cudaMalloc(&dh, sizeof(int32_t) * 4 * nset));
-    if (cudaMalloc(&dout, sizeof(double) * nout)) { cudaFree(dh); return GV_ERR_OOM; }
+    gv_status st = diag_pair(j, size_t(4) * nset, nout, &dh, &dout);
+    if (st) return st;
     cudaError_t e = copy_async(dh, hops, sizeof(int32_t) * 4 * nset, cudaMemcpyHostToDevice, j->stream);
     const size_t sm = (j->cfg.precision == GV_PREC_FP64 ? sizeof(cx<double>) : sizeof(cx<float>)) * 2 * j->Nmax +
                       sizeof(double) * 6 * 4 + 16;
@@ -727,8 +761,6 @@ gv_status virt_update_trans(gv_job* j, int walker, int nset, const int32_t* hops
     }
     if (!e) e = copy_async(out, dout, sizeof(double) * nout, cudaMemcpyDeviceToHost, j->stream);
     if (!e) e = cudaStreamSynchronize(j->stream);
-    cudaFree(dh);
-    cudaFree(dout);
     return cuda_status(e);
 }
 
@@ -737,14 +769,15 @@ constexpr double kMixedMaxInverse = 1e6;
 // Largest |(A^-1)_ij| over both flavours of every walker (stored precision).
 gv_status inverse_max_abs(gv_job* j, double* out)
 {
-    double* d = nullptr;
-    GV_CK(cudaMalloc(&d, sizeof(double) * j->W));
+    void* p = nullptr;
+    gv_status st = diag_scratch(j, sizeof(double) * j->W, &p);
+    if (st) return st;
+    double* d = static_cast<double*>(p);
     if (j->cfg.precision == GV_PREC_FP64) k_inverse_max_abs<double, 256><<<j->W, 256, 0, j->stream>>>(j->d, d);
     else k_inverse_max_abs<float, 256><<<j->W, 256, 0, j->stream>>>(j->d, d);
     cudaError_t e = cudaGetLastError();
     if (!e) e = copy_async(out, d, sizeof(double) * j->W, cudaMemcpyDeviceToHost, j->stream);
     if (!e) e = cudaStreamSynchronize(j->stream);
-    cudaFree(d);
     ++j->total_launches;
     return cuda_status(e);
 }
@@ -757,14 +790,15 @@ gv_status inverse_max_abs(gv_job* j, double* out)
 gv_status trans_start(gv_job* j)
 {
     const int W = j->W, Nexc = j->ch.Nexc;
-    double* dov = nullptr;
-    GV_CK(cudaMalloc(&dov, sizeof(double) * size_t(W) * Nexc));
+    void* p = nullptr;
+    gv_status st = diag_scratch(j, sizeof(double) * size_t(W) * Nexc, &p);
+    if (st) return st;
+    double* dov = static_cast<double*>(p);
     std::vector<double> ov(size_t(W) * Nexc);
-    gv_status st = trans_overlaps(j, dov);
+    st = trans_overlaps(j, dov);
     if (!st && (copy_async(ov.data(), dov, ov.size() * sizeof(double), cudaMemcpyDeviceToHost, j->stream) ||
                 cudaStreamSynchronize(j->stream)))
         st = GV_ERR_CUDA;
-    cudaFree(dov);
     if (st) return st;
     WavHost base = wav_state0(j);
     for (int k = 0; k < Nexc; ++k) wav_hop(j, base, k);
@@ -789,14 +823,15 @@ gv_status trans_start(gv_job* j)
 gv_status long_start(gv_job* j)
 {
     const int W = j->W, Nexc = j->ch.Nexc;
-    double* dov = nullptr;
-    GV_CK(cudaMalloc(&dov, sizeof(double) * size_t(W) * Nexc));
+    void* p = nullptr;
+    gv_status st = diag_scratch(j, sizeof(double) * size_t(W) * Nexc, &p);
+    if (st) return st;
+    double* dov = static_cast<double*>(p);
     std::vector<double> ov(size_t(W) * Nexc);
-    gv_status st = long_states(j, dov);
+    st = long_states(j, dov);
     if (!st && (copy_async(ov.data(), dov, ov.size() * sizeof(double), cudaMemcpyDeviceToHost, j->stream) ||
                 cudaStreamSynchronize(j->stream)))
         st = GV_ERR_CUDA;
-    cudaFree(dov);
     if (st) return st;
     WavHost base = wav_state0(j);
     for (int k = 0; k < Nexc; ++k) long_wav_hop(j, base, k);
@@ -1277,6 +1312,7 @@ gv_status gv_job_destroy(gv_job* j)
     if (j->stream) cudaStreamSynchronize(j->stream);
     for (auto& kv : j->graphs) cudaGraphExecDestroy(kv.second.exec);
     for (void* p : j->allocs) cudaFree(p);
+    cudaFree(j->diag);
     cudaFree(j->d.track_sm);
     cudaFree(j->d.track_lw);
     cudaFree(j->d.track_n);
@@ -1555,15 +1591,16 @@ gv_status gv_job_stream(gv_job* j, void** stream)
 gv_status gv_job_walk_traced(gv_job* j, uint64_t len, uint64_t meas, int32_t walker, gv_trace* trace)
 {
     if (!j || !trace || walker < 0 || walker >= j->W) return GV_ERR_INVALID;
-    gv_trace* dt = nullptr;
-    GV_CK(cudaMalloc(&dt, sizeof(gv_trace) * (len ? len : 1)));
-    gv_status st = walk_impl(j, len, meas, dt, walker);
+    void* p = nullptr;
+    gv_status st = diag_scratch(j, sizeof(gv_trace) * (len ? len : 1), &p);
+    if (st) return st;
+    gv_trace* dt = static_cast<gv_trace*>(p);
+    st = walk_impl(j, len, meas, dt, walker);
     if (!st) {
         if (copy_async(trace, dt, sizeof(gv_trace) * len, cudaMemcpyDeviceToHost, j->stream) ||
             cudaStreamSynchronize(j->stream))
             st = GV_ERR_CUDA;
     }
-    cudaFree(dt);
     return st ? st : gv_job_synchronize(j);
 }
 
@@ -1813,14 +1850,15 @@ gv_status gv_job_drift(gv_job* j, double* out)
 {
     if (!j || !out) return GV_ERR_INVALID;
     if (!j->ready) return GV_ERR_NOT_READY;
-    double* d = nullptr;
-    GV_CK(cudaMalloc(&d, sizeof(double) * 2 * j->W));
+    void* p = nullptr;
+    gv_status st = diag_scratch(j, sizeof(double) * 2 * j->W, &p);
+    if (st) return st;
+    double* d = static_cast<double*>(p);
     if (j->cfg.precision == GV_PREC_FP64) k_drift<double, 256><<<dim3(j->W, 2), 256, 0, j->stream>>>(j->d, d);
     else k_drift<float, 256><<<dim3(j->W, 2), 256, 0, j->stream>>>(j->d, d);
     cudaError_t e = cudaGetLastError();
     if (!e) e = copy_async(out, d, sizeof(double) * 2 * j->W, cudaMemcpyDeviceToHost, j->stream);
     if (!e) e = cudaStreamSynchronize(j->stream);
-    cudaFree(d);
     return cuda_status(e);
 }
 
@@ -1835,8 +1873,8 @@ gv_status gv_job_virt_update(gv_job* j, int32_t walker, int32_t nset, const int3
         if (hops[i] < -1 || hops[i] >= j->Ns) return GV_ERR_INVALID;
     int32_t* dh = nullptr;
     double* dout = nullptr;
-    GV_CK(cudaMalloc(&dh, sizeof(int32_t) * 4 * nset));
-    if (cudaMalloc(&dout, sizeof(double) * 2 * nset)) { cudaFree(dh); return GV_ERR_OOM; }
+    gv_status st = diag_pair(j, size_t(4) * nset, size_t(2) * nset, &dh, &dout);
+    if (st) return st;
     cudaError_t e = copy_async(dh, hops, sizeof(int32_t) * 4 * nset, cudaMemcpyHostToDevice, j->stream);
     const int per = 4;
     if (!e) {
@@ -1848,8 +1886,6 @@ gv_status gv_job_virt_update(gv_job* j, int32_t walker, int32_t nset, const int3
     }
     if (!e) e = copy_async(out, dout, sizeof(double) * 2 * nset, cudaMemcpyDeviceToHost, j->stream);
     if (!e) e = cudaStreamSynchronize(j->stream);
-    cudaFree(dh);
-    cudaFree(dout);
     return cuda_status(e);
 }
 
