@@ -19,6 +19,7 @@
 #include <map>
 #include <mutex>
 #include <string>
+#include <thread>
 #include <tuple>
 #include <vector>
 
@@ -1186,24 +1187,51 @@ gv_status gv_job_create(const gv_job_config* cfg, gv_job** out)
     // Host tables.
     std::vector<zd> ph;
     phase_table(j->orb, ph);
-    std::vector<zd> coef(size_t(j->W) * 4 * j->Ns);
-    for (int w = 0; w < j->W; ++w)
+    // U_k / V_k of every walker (StagFluxWaveFunction.cpp:121-163): computed
+    // once when the walkers share (phi, neel), else per walker on host threads
+    // (each walker's table is the same whichever thread computes it).
+    const size_t per_walker = size_t(4) * j->Ns;
+    std::vector<cx<double>> cf64(size_t(j->W) * per_walker);
+    std::vector<cx<float>> cf32(cf64.size());
+    const bool shared = !(cfg->phi_range[1] > cfg->phi_range[0]) && !(cfg->neel_range[1] > cfg->neel_range[0]);
+    auto fill = [&](int w) {
+        std::vector<zd> c(per_walker);
         for (int fl = 0; fl < 2; ++fl)
-            if (!stagflux_coefs(j->orb, j->wphi[w], j->wneel[w], cfg->neel_exp, fl, &coef[(size_t(w) * 2 + fl) * 2 * j->Ns])) {
-                delete j;
-                return GV_ERR_NAN;
-            }
+            if (!stagflux_coefs(j->orb, j->wphi[w], j->wneel[w], cfg->neel_exp, fl, &c[size_t(fl) * 2 * j->Ns])) return false;
+        for (size_t i = 0; i < per_walker; ++i) {
+            cf64[size_t(w) * per_walker + i] = {c[i].real(), c[i].imag()};
+            cf32[size_t(w) * per_walker + i] = {float(c[i].real()), float(c[i].imag())};
+        }
+        return true;
+    };
+    bool coef_ok = true;
+    if (shared) {
+        coef_ok = fill(0);
+        for (int w = 1; coef_ok && w < j->W; ++w) {
+            std::copy(cf64.begin(), cf64.begin() + per_walker, cf64.begin() + size_t(w) * per_walker);
+            std::copy(cf32.begin(), cf32.begin() + per_walker, cf32.begin() + size_t(w) * per_walker);
+        }
+    } else {
+        const int nth = std::max(1, std::min(16, int(std::thread::hardware_concurrency())));
+        std::vector<std::thread> pool;
+        std::atomic<bool> ok_all{true};
+        for (int t = 0; t < nth; ++t)
+            pool.emplace_back([&, t] {
+                for (int w = t; w < j->W; w += nth)
+                    if (!fill(w)) ok_all = false;
+            });
+        for (auto& th : pool) th.join();
+        coef_ok = ok_all;
+    }
+    if (!coef_ok) {
+        delete j;
+        return GV_ERR_NAN;
+    }
     std::vector<cx<double>> ph64(ph.size());
     std::vector<cx<float>> ph32(ph.size());
     for (size_t i = 0; i < ph.size(); ++i) {
         ph64[i] = {ph[i].real(), ph[i].imag()};
         ph32[i] = {float(ph[i].real()), float(ph[i].imag())};
-    }
-    std::vector<cx<double>> cf64(coef.size());
-    std::vector<cx<float>> cf32(coef.size());
-    for (size_t i = 0; i < coef.size(); ++i) {
-        cf64[i] = {coef[i].real(), coef[i].imag()};
-        cf32[i] = {float(coef[i].real()), float(coef[i].imag())};
     }
     std::vector<int32_t> edges(size_t(2) * j->Ns * 4);
     for (int e = 0; e < 2 * j->Ns; ++e) {
