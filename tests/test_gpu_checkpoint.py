@@ -35,6 +35,13 @@ def _trans(engine, precision, L=8, W=8, seed=7, **kw):
                       precision=precision, **kw)
 
 
+def _long(engine, precision, L=8, W=8, seed=3, **kw):
+    kw.setdefault("reinv_every", 64)
+    kw.setdefault("deferred_reinversion", True)
+    return engine.Job(engine.StagFluxLongExciton(L, PHI, 0.1, q=(2, 2)), walkers=W, seed=seed,
+                      precision=precision, **kw)
+
+
 def _snapshot(job, statspin=False):
     s = {
         "config": job.config(),
@@ -120,6 +127,17 @@ def test_exciton_walk_resumes_exactly(engine, oracle, precision, inverses):
     mask = oracle.MEAS_PROJHEIS | oracle.MEAS_STAGMAGN
     a, b = _split_run(lambda: _trans(engine, precision), mask, inverses)
     _assert_same(a, b)
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+@pytest.mark.parametrize("inverses", [True, False])
+def test_long_exciton_walk_resumes_exactly(engine, oracle, precision, inverses):
+    """The longitudinal channel also carries its overlap tables R; without
+    stored inverses the restore rebuilds them with the FP64 inversion."""
+    mask = oracle.MEAS_PROJHEIS | oracle.MEAS_STAGMAGN
+    a, b = _split_run(lambda: _long(engine, precision), mask, inverses)
+    _assert_same(a, b)
+    assert (a["pj"][1] == 6).all()
 
 
 def test_restore_refuses_foreign_or_damaged_blobs(engine, tmp_path):
