@@ -704,7 +704,7 @@ def run_tc_projheis(g, walkers):
     job = g.Job(wav, precision="mixed", drift_threshold=DRIFT_THRESHOLD, tc_projheis=True, **common)
     job.set_measurements(1)
     job.init_walkers()
-    for _ in range(4):
+    for _ in range(THERM_SWEEPS):   # thermalised as the headline walk, so that the walks compare
         job.walk(SWEEP, 0, sync=False)
     job.synchronize()
     c0 = job.counts().sum(axis=0)
@@ -865,9 +865,11 @@ def run_serving(g):
 
 
 # DRAM bytes per walker per walk launch of k_walk_gs_res (inverses in at entry,
-# out at exit, plus tables), from the full-size ncu capture summarised in
+# out at exit, plus tables): dram__bytes_read.sum + dram__bytes_write.sum of
+# one measured sweep of the 2048-walker workload (557.43 MB + 484.71 MB, a
+# one-pass ncu capture), summarised in
 # profiles/k_walk_gs_res_L16_2048walkers_dram.md
-RES_DRAM_BYTES_PER_WALKER = 108.8e6 / 304
+RES_DRAM_BYTES_PER_WALKER = (557.43e6 + 484.71e6) / 2048
 
 
 def sm_count():
