@@ -372,12 +372,14 @@ gv_status launch_walk(gv_job* j, uint64_t nsteps, uint64_t s0, uint64_t meas, in
 constexpr int kDelay = GV_DELAY_DEPTH;
 
 // On-chip walk (both FP32 inverses in TMEM / shared memory for the whole call):
-// mixed ground state, N <= 128, deferred re-inversion, no delayed updates.
+// mixed ground state, N <= 128 and even (rows of the inverses and of the phase
+// table are copied in 16-byte pieces), deferred re-inversion, no delayed updates.
 bool resident_ok(const gv_job* j, uint64_t nsteps)
 {
     const int f = j->cfg.flags;
     return nsteps > 0 && !exc(j) && j->cfg.precision == GV_PREC_MIXED && j->N[0] == j->N[1] && j->Nmax <= 128 &&
-           (f & GV_FLAG_REINV_DEFERRED) && !(f & GV_FLAG_DELAYED_UPDATES) && !(f & GV_FLAG_STREAM_INVERSES);
+           j->Nmax % 2 == 0 && j->Nk % 2 == 0 && (f & GV_FLAG_REINV_DEFERRED) && !(f & GV_FLAG_DELAYED_UPDATES) &&
+           !(f & GV_FLAG_STREAM_INVERSES);
 }
 
 gv_status launch_walk_res(gv_job* j, uint64_t nsteps, uint64_t s0, uint64_t meas, int mask)

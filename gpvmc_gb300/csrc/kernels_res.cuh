@@ -76,6 +76,26 @@ __device__ __forceinline__ void tmem_wait_ld(uint32_t (&r)[8])
     asm volatile("tcgen05.wait::ld.sync.aligned;"
                  : "+r"(r[0]), "+r"(r[1]), "+r"(r[2]), "+r"(r[3]), "+r"(r[4]), "+r"(r[5]), "+r"(r[6]), "+r"(r[7])::"memory");
 }
+__device__ __forceinline__ void tmem_wait_ld(uint32_t (&r)[16])
+{
+    asm volatile("tcgen05.wait::ld.sync.aligned;"
+                 : "+r"(r[0]), "+r"(r[1]), "+r"(r[2]), "+r"(r[3]), "+r"(r[4]), "+r"(r[5]), "+r"(r[6]), "+r"(r[7]),
+                   "+r"(r[8]), "+r"(r[9]), "+r"(r[10]), "+r"(r[11]), "+r"(r[12]), "+r"(r[13]), "+r"(r[14]),
+                   "+r"(r[15])::"memory");
+}
+// 16-byte asynchronous global -> shared copies (zero fill when !valid; the
+// source is then not read)
+__device__ __forceinline__ void cp_async16(void* smem_dst, const void* gsrc, bool valid)
+{
+    const uint32_t d = static_cast<uint32_t>(__cvta_generic_to_shared(smem_dst));
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;" ::"r"(d), "l"(gsrc), "r"(valid ? 16 : 0) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+template <int n>
+__device__ __forceinline__ void cp_async_wait()
+{
+    asm volatile("cp.async.wait_group %0;" ::"n"(n) : "memory");
+}
 __device__ __forceinline__ void tmem_st64(uint32_t taddr, const uint32_t (&r)[64])
 {
     asm volatile("tcgen05.st.sync.aligned.32x32b.x64.b32 [%0], {%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31,%32,%33,%34,%35,%36,%37,%38,%39,%40,%41,%42,%43,%44,%45,%46,%47,%48,%49,%50,%51,%52,%53,%54,%55,%56,%57,%58,%59,%60,%61,%62,%63,%64};" ::"r"(taddr), "r"(r[0]), "r"(r[1]), "r"(r[2]), "r"(r[3]), "r"(r[4]), "r"(r[5]), "r"(r[6]), "r"(r[7]), "r"(r[8]), "r"(r[9]), "r"(r[10]), "r"(r[11]), "r"(r[12]), "r"(r[13]), "r"(r[14]), "r"(r[15]), "r"(r[16]), "r"(r[17]), "r"(r[18]), "r"(r[19]), "r"(r[20]), "r"(r[21]), "r"(r[22]), "r"(r[23]), "r"(r[24]), "r"(r[25]), "r"(r[26]), "r"(r[27]), "r"(r[28]), "r"(r[29]), "r"(r[30]), "r"(r[31]), "r"(r[32]), "r"(r[33]), "r"(r[34]), "r"(r[35]), "r"(r[36]), "r"(r[37]), "r"(r[38]), "r"(r[39]), "r"(r[40]), "r"(r[41]), "r"(r[42]), "r"(r[43]), "r"(r[44]), "r"(r[45]), "r"(r[46]), "r"(r[47]), "r"(r[48]), "r"(r[49]), "r"(r[50]), "r"(r[51]), "r"(r[52]), "r"(r[53]), "r"(r[54]), "r"(r[55]), "r"(r[56]), "r"(r[57]), "r"(r[58]), "r"(r[59]), "r"(r[60]), "r"(r[61]), "r"(r[62]), "r"(r[63]) : "memory");
@@ -87,10 +107,11 @@ constexpr int kResThreads = 256;
 constexpr int kResTmemCols = 512;                 // both flavours, 128 complex FP32 per lane each
 constexpr size_t kResMinSmem = 116 * 1024;        // over half an SM's shared memory: one CTA per SM
 constexpr int kResRngBatch = 32;
-constexpr int kResSpec = 2;                       // proposals evaluated per barrier
+constexpr int kResSpec = 8;                       // proposals evaluated per barrier (<= 32: one lane each)
+constexpr int kResStageRow = 34;                  // complex per staged row segment: 32 + 2 (272 B rows: no bank conflicts)
 
 struct ResLayout {
-    size_t fock, part, nbr, sub, coef, red, wpart, w, rv, ru4, ru4d, racc, rq, rqp, nb, redm, tbase, total, used;
+    size_t fock, part, nbr, sub, coef, red, wpart, w, rv, ru4, ru4d, racc, rq, rqp, nb, redm, ph, tbase, total, used;
 };
 
 __host__ __device__ inline ResLayout res_layout(int Ns, int N, bool projheis)
@@ -107,14 +128,20 @@ __host__ __device__ inline ResLayout res_layout(int Ns, int N, bool projheis)
     l.red = al(sizeof(float) * 2 * 16 * kResSpec);
     l.wpart = al(c * 2 * 4 * 128);
     l.w = al(c * 2 * 128);
-    l.rv = al(sizeof(int16_t) * 2 * kResRngBatch);
-    l.ru4 = al(sizeof(float) * kResRngBatch);
-    l.ru4d = al(sizeof(double) * kResRngBatch);
+    l.rv = al(sizeof(int16_t) * 2 * 2 * kResRngBatch);   // [batch parity][step][v1, v2]
+    l.ru4 = al(sizeof(float) * 2 * kResRngBatch);
+    l.ru4d = al(sizeof(double) * 2 * kResRngBatch);
     l.racc = al(sizeof(cx<float>) * 2 * kResRngBatch);   // accepted ratio pairs of the batch
     l.rq = al(projheis ? c * 4 * Ns : 16);
     l.rqp = al(projheis ? c * 2 * 4 * 4 * 128 : 16);   // [g][warp][slot][p] partial bond ratios
     l.nb = al(projheis ? sizeof(int32_t) * 2 * 4 * 128 : 16);   // [g][bond] particle, slot and site
     l.redm = al(sizeof(double) * 4 * (kResThreads / 32));
+    // phase rows of both sites of every proposal of two uniform batches
+    // ([parity][step][site][N]); at launch entry and exit the same bytes hold two
+    // staging tiles of the inverses ([buffer][flavour][row][kResStageRow])
+    const size_t ph_rows = c * 2 * kResRngBatch * 2 * size_t(N);
+    const size_t stage = c * 2 * 2 * 128 * kResStageRow;   // two buffers
+    l.ph = al(ph_rows > stage ? ph_rows : stage);
     l.tbase = al(sizeof(uint32_t));
     l.used = al(16);
     l.total = l.used < kResMinSmem ? kResMinSmem : l.used;
@@ -195,18 +222,39 @@ __global__ void __launch_bounds__(kResThreads, 1) k_walk_gs_res(DevJob J, uint64
     const int g = tid >> 7;                       // warpgroup = flavour
     const int f = tid & 127;                      // TMEM lane = Slater row of this thread
     const uint32_t trow = tbase + ((uint32_t(warp & 3) * 32) << 16) + uint32_t(256 * g);
-    cx<T>* Ag = ai_ptr<T>(J, g, w);
-    // inverse of flavour g -> TMEM: lane f = row f of AiT (contiguous in HBM), zero padding
+    // both inverses -> TMEM (lane f = row f of AiT, zero padding), 32 particles
+    // at a time: coalesced 16-byte copies of the rows' segments into a shared
+    // tile (N is even: a 16-byte piece never straddles two rows), then each
+    // thread moves its own row segment into its TMEM lane
+    cx<T>* s_stage = reinterpret_cast<cx<T>*>(smem + lay.ph);
+    constexpr int kTile = 2 * 128 * kResStageRow;   // complex per staging tile
+    auto stage_segment = [&](int c, int b) {   // particles 32c .. 32c + 31 of both inverses -> tile b
+        for (int i = tid; i < 2 * 128 * 16; i += kResThreads) {
+            const int fl = i >> 11, row = (i >> 4) & 127, kp = i & 15, p = 32 * c + 2 * kp;
+            const bool ok = row < N && p < N;
+            const cx<T>* src = ai_ptr<T>(J, fl, w) + (ok ? size_t(row) * N + p : 0);
+            cp_async16(s_stage + b * kTile + (fl * 128 + row) * kResStageRow + 2 * kp, src, ok);
+        }
+        cp_async_commit();
+    };
+    stage_segment(0, 0);   // two segments in flight
+    if (NCH > 1) stage_segment(1, 1);
     for (int c = 0; c < NCH; ++c) {
+        if (c + 1 < NCH) cp_async_wait<1>();
+        else cp_async_wait<0>();
+        __syncthreads();
+        const cx<T>* my_seg = s_stage + (c & 1) * kTile + (g * 128 + f) * kResStageRow;
         uint32_t r[64];
 #pragma unroll
-        for (int j = 0; j < 32; ++j) {
-            const int p = 32 * c + j;
-            cx<T> a = {0.f, 0.f};
-            if (f < N && p < N) a = Ag[size_t(f) * N + p];
-            r[2 * j] = __float_as_uint(a.x);
-            r[2 * j + 1] = __float_as_uint(a.y);
+        for (int j = 0; j < 16; ++j) {
+            const float4 q = reinterpret_cast<const float4*>(my_seg)[j];
+            r[4 * j] = __float_as_uint(q.x);
+            r[4 * j + 1] = __float_as_uint(q.y);
+            r[4 * j + 2] = __float_as_uint(q.z);
+            r[4 * j + 3] = __float_as_uint(q.w);
         }
+        __syncthreads();   // the tile is free for segment c + 2
+        if (c + 2 < NCH) stage_segment(c + 2, c & 1);
         tmem_st64(trow + 64 * c, r);
     }
     tmem_wait_st();
@@ -229,22 +277,69 @@ __global__ void __launch_bounds__(kResThreads, 1) k_walk_gs_res(DevJob J, uint64
                           phase, ai_ptr<T>(J, 0, w), ai_ptr<T>(J, 1, w)};
     // Proposals are evaluated kResSpec at a time: every thread forms its terms
     // of the next kb proposals' ratios (same inverse, same occupancy), one
-    // barrier combines them, and the steps are then resolved in order until
-    // the first accepted move, whose update invalidates the rest (they are
-    // evaluated again, from the new inverse, in the next round).  A round
-    // never crosses a uniform batch or a measurement step.
-    // phase rows of both sites of the next round's proposals, fetched during the
-    // current round (whichever site a proposal's particle moves to, its row is there)
-    cx<T> pf[kResSpec][2];
-    int pf_bi = -1;   // first proposal index of the prefetched rows, -1: none
+    // barrier combines them, lane i of every warp resolves proposal i, and a
+    // ballot finds the first step that ends the round -- an accepted exchange,
+    // whose update invalidates the later proposals (they are evaluated again,
+    // from the new inverse, in the next round), or an error.  A round never
+    // crosses a uniform batch or a measurement step.
+    // The uniforms of a batch and the phase rows of both sites of its
+    // proposals (whichever site a particle moves to, its row is there) are in
+    // shared memory before the batch starts: batch b + 1 is drawn and its rows
+    // copied asynchronously while batch b runs (the Metropolis stream does not
+    // depend on the walk).
+    cx<T>* s_ph = reinterpret_cast<cx<T>*>(smem + lay.ph);
+    const int half = N / 2;   // 16-byte pieces per phase row
+    // warp 0: steps sb .. sb + 31 into parity par; a step past the call's end
+    // gets the sites (0, 0), so that every entry is a valid site index
+    auto draw_batch = [&](uint64_t sb, int par) {
+        if (warp == 0) {
+            int v1 = 0, v2 = 0;
+            float ru = 0.f;
+            double rud = 0.0;
+            if (sb + lane < nsteps) {
+                const uint64_t kl = k + 4 * (sb + uint64_t(lane));
+                uint32_t x[4], y[4];
+                philox_call(J.seed, wid, 0, kl >> 1, x);
+                philox_call(J.seed, wid, 0, (kl >> 1) + 1, y);
+                v1 = scaled_floor(uint32_t(Ns), u52(x[0], x[1]));
+                v2 = s_nbr[v1 * 4 + int(u52(x[2], x[3]) >> 50)];
+                ru = Accept<T>::uniform(u52(y[2], y[3]));
+                rud = u01(y[2], y[3]);
+            }
+            s_rv[(par * kResRngBatch + lane) * 2] = int16_t(v1);
+            s_rv[(par * kResRngBatch + lane) * 2 + 1] = int16_t(v2);
+            s_ru4[par * kResRngBatch + lane] = ru;
+            s_ru4d[par * kResRngBatch + lane] = rud;
+        }
+    };
+    // all threads, one commit group: thread t copies 16-byte piece t % 64 of
+    // rows t / 64 + 4 j (row = 2 step + site) of parity par
+    static_assert(kResThreads == 256 && 2 * kResRngBatch == 64, "row fetch mapping");
+    auto fetch_batch_rows = [&](uint64_t sb, int par) {
+        const int kp = tid & 63;
+        if (kp < half) {
+#pragma unroll
+            for (int j = 0; j < 16; ++j) {
+                const int row = (tid >> 6) + 4 * j, step = row >> 1;
+                const int site = s_rv[(par * kResRngBatch + step) * 2 + (row & 1)];
+                cp_async16(s_ph + (size_t(par) * 2 * kResRngBatch + row) * N + 2 * kp,
+                           phase + size_t(site) * Nk + 2 * kp, sb + uint64_t(step) < nsteps);
+            }
+        }
+        cp_async_commit();
+    };
+    draw_batch(0, 0);
+    __syncthreads();
+    fetch_batch_rows(0, 0);
     const bool measuring = meas != 0 && mask != 0;
     // steps from s to the next measuring step (0: s itself is measured)
     uint64_t to_meas = measuring ? (meas == 1 ? 0 : (meas - (s0 % meas)) % meas) : ~uint64_t(0);
     uint64_t s = 0;
     while (s < nsteps) {
         const int bi0 = int(s % kResRngBatch);
-        if (bi0 == 0) {   // the next batch of proposals and accept uniforms (one lane per step)
-            __syncthreads();   // every thread is done with the previous batch
+        const int par = int(s / kResRngBatch) & 1;
+        if (bi0 == 0) {
+            __syncthreads();   // every thread is done with the previous batch and its buffers
             // the amplitude (FP64, off the per-step path): the previous batch's accepted ratios
             if (tid == 32) {
                 for (int i = 0; i < nacc; ++i) {
@@ -253,19 +348,14 @@ __global__ void __launch_bounds__(kResThreads, 1) k_walk_gs_res(DevJob J, uint64
                 }
             }
             nacc = 0;
-            if (warp == 0 && s + lane < nsteps) {
-                const uint64_t kl = k + 4 * (s + uint64_t(lane));
-                uint32_t x[4], y[4];
-                philox_call(J.seed, wid, 0, kl >> 1, x);
-                philox_call(J.seed, wid, 0, (kl >> 1) + 1, y);
-                const int v1 = scaled_floor(uint32_t(Ns), u52(x[0], x[1]));
-                s_rv[2 * lane] = int16_t(v1);
-                s_rv[2 * lane + 1] = s_nbr[v1 * 4 + int(u52(x[2], x[3]) >> 50)];
-                s_ru4[lane] = Accept<T>::uniform(u52(y[2], y[3]));
-                s_ru4d[lane] = u01(y[2], y[3]);
-            }
+            draw_batch(s + kResRngBatch, par ^ 1);
+            __syncthreads();
+            fetch_batch_rows(s + kResRngBatch, par ^ 1);
+            cp_async_wait<1>();   // this batch's rows (the group before) have landed
             __syncthreads();
         }
+        const int16_t* rv = s_rv + par * 2 * kResRngBatch;
+        const cx<T>* prow = s_ph + size_t(par) * 2 * kResRngBatch * N;
         uint64_t kb64 = nsteps - s;
         if (kb64 > uint64_t(kResRngBatch - bi0)) kb64 = uint64_t(kResRngBatch - bi0);
         if (kb64 > uint64_t(kResSpec)) kb64 = kResSpec;
@@ -277,145 +367,174 @@ __global__ void __launch_bounds__(kResThreads, 1) k_walk_gs_res(DevJob J, uint64
         cx<T> pa[kResSpec], pu[kResSpec];
         uint32_t rr[2 * kResSpec];
         int psite[kResSpec], ppart[kResSpec];   // (upf | upt << 16), (cu | cd << 16) of proposal i
-        int anti = 0;   // bit i: proposal i exchanges antiparallel spins
+        unsigned anti = 0;   // bit i: proposal i exchanges antiparallel spins
+        // branch-free, so that the kResSpec chains interleave: every proposal slot
+        // loads and multiplies (slots past kb, or exchanging parallel spins,
+        // carry u = 0 and are ignored)
+        const int fi = f < N ? f : N - 1;
 #pragma unroll
         for (int i = 0; i < kResSpec; ++i) {
-            pu[i] = cx<T>{0.f, 0.f};
-            rr[2 * i] = rr[2 * i + 1] = 0u;
-            psite[i] = ppart[i] = 0;
-            if (i < kb) {
-                const int v1 = s_rv[2 * (bi0 + i)], v2 = s_rv[2 * (bi0 + i) + 1];
-                const bool up1 = s_fock[v1] >= 0, up2 = s_fock[v2] >= 0;
-                if (up1 != up2) {
-                    anti |= 1 << i;
-                    const int upf = up1 ? v1 : v2, upt = up1 ? v2 : v1;
-                    const int cu = s_fock[upf], cd = s_fock[Ns + upt];
-                    psite[i] = upf | (upt << 16);
-                    ppart[i] = cu | (cd << 16);
-                    const int cg = g ? cd : cu;     // this flavour's particle
-                    const int tg = g ? upf : upt;   // and its destination
-                    uint32_t r2[2];
-                    tmem_ld2(trow + 2 * cg, r2);
-                    rr[2 * i] = r2[0];
-                    rr[2 * i + 1] = r2[1];
-                    if (f < N) {
-                        const cx<T> ph = pf_bi == bi0 ? (tg == v1 ? pf[i][0] : pf[i][1]) : phase[size_t(tg) * Nk + f];
-                        pu[i] = cmul_rn(ph, cf[s_sub[tg] * N + f]);
-                    }
-                }
-            }
-        }
-        {   // the next round's rows, assuming it starts right after this one
-            const int nb0 = bi0 + kb;
-            pf_bi = -1;
-            if (nb0 < kResRngBatch && s + uint64_t(kb) < nsteps) {
-#pragma unroll
-                for (int i = 0; i < kResSpec; ++i)
-                    if (nb0 + i < kResRngBatch && s + uint64_t(kb + i) < nsteps && f < N) {
-                        pf[i][0] = phase[size_t(s_rv[2 * (nb0 + i)]) * Nk + f];
-                        pf[i][1] = phase[size_t(s_rv[2 * (nb0 + i) + 1]) * Nk + f];
-                    }
-                pf_bi = nb0;
-            }
+            const int bi = bi0 + i < kResRngBatch ? bi0 + i : kResRngBatch - 1;
+            const int v1 = rv[2 * bi], v2 = rv[2 * bi + 1];
+            const int u1 = s_fock[v1], u2 = s_fock[v2], d1 = s_fock[Ns + v1], d2 = s_fock[Ns + v2];
+            const bool up1 = u1 >= 0, up2 = u2 >= 0;
+            const bool an = i < kb && up1 != up2;
+            anti |= unsigned(an) << i;
+            const int upf = up1 ? v1 : v2, upt = up1 ? v2 : v1;
+            const int cu = up1 ? u1 : u2, cd = up1 ? d2 : d1;   // the up particle at upf, the down one at upt
+            psite[i] = upf | (upt << 16);
+            ppart[i] = (cu & 0xFFFF) | (cd << 16);
+            int cg = g ? cd : cu;             // this flavour's particle
+            cg = cg < 0 ? 0 : cg;
+            const int tg = g ? upf : upt;     // and its destination
+            uint32_t r2[2];
+            tmem_ld2(trow + 2 * cg, r2);
+            rr[2 * i] = r2[0];
+            rr[2 * i + 1] = r2[1];
+            const cx<T> uu = cmul_rn(prow[size_t(2 * bi + (tg == v1 ? 0 : 1)) * N + fi], cf[s_sub[tg] * N + fi]);
+            pu[i] = (an && f < N) ? uu : cx<T>{0.f, 0.f};
         }
         tmem_wait_ld(rr);
         T* rb = s_red + rbuf * 16 * kResSpec;
         rbuf ^= 1;
+        {   // the kResSpec warp sums at once: a butterfly that leaves proposal
+            // (lane >> 2)'s sum in lanes 4 i .. 4 i + 3 (the pairs and their order
+            // are those of warp_sum, so the sums are the same)
+            static_assert(kResSpec == 8, "the butterfly below sums eight proposals");
+            cx<T> x[8];
 #pragma unroll
-        for (int i = 0; i < kResSpec; ++i) {
-            pa[i] = cx<T>{__uint_as_float(rr[2 * i]), __uint_as_float(rr[2 * i + 1])};
-            if (anti & (1 << i)) {
-                const cx<T> part = warp_sum(pa[i] * pu[i]);
-                if (lane == 0) { rb[16 * i + warp * 2] = part.x; rb[16 * i + warp * 2 + 1] = part.y; }
+            for (int i = 0; i < 8; ++i) {
+                pa[i] = cx<T>{__uint_as_float(rr[2 * i]), __uint_as_float(rr[2 * i + 1])};
+                x[i] = pa[i] * pu[i];
+            }
+#pragma unroll
+            for (int o = 16, n = 4; o >= 4; o >>= 1, n >>= 1) {
+                const bool hi = (lane & o) != 0;
+#pragma unroll
+                for (int t = 0; t < n; ++t) {
+                    const cx<T> keep = hi ? x[n + t] : x[t];
+                    cx<T> send = hi ? x[t] : x[n + t];
+                    send.x = __shfl_xor_sync(0xffffffffu, send.x, o);
+                    send.y = __shfl_xor_sync(0xffffffffu, send.y, o);
+                    x[t] = keep + send;
+                }
+            }
+#pragma unroll
+            for (int o = 2; o; o >>= 1) {
+                const cx<T> y = {__shfl_xor_sync(0xffffffffu, x[0].x, o), __shfl_xor_sync(0xffffffffu, x[0].y, o)};
+                x[0] = x[0] + y;
+            }
+            if ((lane & 3) == 0) {
+                const int i = lane >> 2;
+                rb[16 * i + warp * 2] = x[0].x;
+                rb[16 * i + warp * 2 + 1] = x[0].y;
             }
         }
         __syncthreads();
-        int done = kb;
-#pragma unroll
-        for (int i = 0; i < kResSpec; ++i) {
-            if (i >= kb || done < kb) continue;
-            const int bi = bi0 + i;
-            const int v1 = s_rv[2 * bi], v2 = s_rv[2 * bi + 1];
-            int kind = 0, accepted;
-            T ratio = T(1);
-            if (!(anti & (1 << i))) {
-                accepted = 1;   // m_weight / m_state_weight = 1 (MetroMC.cpp:41)
-                ++c_noop;
-            } else {
-                kind = 1;
-                const T* q = rb + 16 * i;
-                const cx<T> ru = {q[0] + q[2] + q[4] + q[6], q[1] + q[3] + q[5] + q[7]};
-                const cx<T> rd = {q[8] + q[10] + q[12] + q[14], q[9] + q[11] + q[13] + q[15]};
-                ratio = Accept<T>::ratio(ru, rd);
-                if (!isfinite(ratio)) { status = GV_ERR_NAN; done = -1 - i; continue; }
-                accepted = ratio > T(1) ? 1 : (s_ru4[bi] < ratio);
-                if (!accepted) {
-                    ++c_rej;
-                } else {
-                    if (norm2(ru) < T(1e-9) || norm2(rd) < T(1e-9)) { status = GV_ERR_SINGULAR; done = -1 - i; continue; }
-                    // occupancy of this step as read before the round's barrier
-                    const int upf = psite[i] & 0xFFFF, upt = psite[i] >> 16;
-                    const int dnf = upt, dnt = upf;
-                    const int cu = ppart[i] & 0xFFFF, cd = ppart[i] >> 16;
-                    const int cg = g ? cd : cu;
-                    const cx<T> u = pu[i], a = pa[i];
-                    const cx<T> ir = cinv(g ? rd : ru);
-                    // w = A^-1 u: this warp's 32 rows times u_f, summed over lanes per particle
-                    cx<T>* wpart = s_wpart + (g * 4 + (warp & 3)) * 128;
-                    for (int c = 0; c < NCH; ++c) {
-                        uint32_t r[64];
-                        tmem_ld64(trow + 64 * c, r);
-                        tmem_wait_ld(r);
-                        cx<T> v[32];
-#pragma unroll
-                        for (int j = 0; j < 32; ++j) v[j] = cx<T>{__uint_as_float(r[2 * j]), __uint_as_float(r[2 * j + 1])} * u;
-                        wpart[32 * c + lane] = warp_reduce_scatter(v);
-                    }
-                    wg_sync(g);
-                    if (f < 32 * NCH) {   // w_p - [p == c]
-                        const cx<T>* wp0 = s_wpart + g * 4 * 128;
-                        cx<T> wq = wp0[f] + wp0[128 + f] + wp0[256 + f] + wp0[384 + f];
-                        if (f == cg) wq.x -= 1.f;
-                        s_w[g * 128 + f] = wq;
-                    }
-                    wg_sync(g);
-                    // row update: AiT[f][p] -= (w_p - [p == c]) * (A^-1)(c, f) / r
-                    const cx<T> coef = cneg(a * ir);
-                    const cx<T>* wv = s_w + g * 128;
-                    for (int c = 0; c < NCH; ++c) {
-                        uint32_t r[64];
-                        tmem_ld64(trow + 64 * c, r);
-                        tmem_wait_ld(r);
-#pragma unroll
-                        for (int j = 0; j < 32; ++j) {
-                            const int p = 32 * c + j;
-                            cx<T> e = {__uint_as_float(r[2 * j]), __uint_as_float(r[2 * j + 1])};
-                            cmac(e, wv[p], coef);
-                            r[2 * j] = __float_as_uint(e.x);
-                            r[2 * j + 1] = __float_as_uint(e.y);
-                        }
-                        tmem_st64(trow + 64 * c, r);
-                    }
-                    tmem_wait_st();
-                    if (tid == 0) {
-                        s_fock[upt] = int16_t(cu); s_fock[upf] = -1; s_part[cu] = int16_t(upt);
-                        s_fock[Ns + dnt] = int16_t(cd); s_fock[Ns + dnf] = -1; s_part[N + cd] = int16_t(dnt);
-                        s_racc[2 * nacc] = ru;
-                        s_racc[2 * nacc + 1] = rd;
-                    }
-                    ++nacc;
-                    ++c_acc;
-                    ++since;
-                    __syncthreads();
-                    done = i + 1;   // the later proposals saw the old inverse and occupancy
+        // lane i (i < kb) resolves proposal i; every warp does the same
+        T ratio = T(1);
+        int stop = 0;   // 1: accepted exchange, 2: non-finite ratio, 3: accepted with a vanishing ratio
+        if (lane < kb && (anti & (1u << lane))) {
+            const T* q = rb + 16 * lane;
+            const cx<T> ru = {q[0] + q[2] + q[4] + q[6], q[1] + q[3] + q[5] + q[7]};
+            const cx<T> rd = {q[8] + q[10] + q[12] + q[14], q[9] + q[11] + q[13] + q[15]};
+            ratio = Accept<T>::ratio(ru, rd);
+            if (!isfinite(ratio)) {
+                stop = 2;
+            } else if (ratio > T(1) || s_ru4[par * kResRngBatch + bi0 + lane] < ratio) {
+                stop = (norm2(ru) < T(1e-9) || norm2(rd) < T(1e-9)) ? 3 : 1;
+            }
+        }
+        const unsigned stops = __ballot_sync(0xffffffffu, stop != 0);
+        const int first = stops ? __ffs(stops) - 1 : kb;
+        const int first_kind = __shfl_sync(0xffffffffu, stop, first & 31);
+        const unsigned before = (1u << first) - 1u;   // first <= kb <= kResSpec < 32
+        c_noop += __popc(~anti & before);
+        c_rej += __popc(anti & before);
+        int done;
+        if (first == kb) {
+            done = kb;
+        } else if (first_kind != 1) {
+            status = first_kind == 2 ? GV_ERR_NAN : GV_ERR_SINGULAR;
+            done = -1 - first;
+        } else {
+            done = first + 1;   // the later proposals saw the old inverse and occupancy
+        }
+        if (J.trace && w == J.trace_walker) {   // block-uniform
+            const int nt = done < 0 ? -1 - done : done;
+            for (int i = 0; i < nt; ++i) {
+                const T ri = __shfl_sync(0xffffffffu, ratio, i);
+                if (tid == 0) {
+                    const int kind = (anti >> i) & 1;
+                    gv_trace t;
+                    t.v1 = rv[2 * (bi0 + i)]; t.v2 = rv[2 * (bi0 + i) + 1];
+                    t.kind = kind; t.accepted = (!kind || i == first) ? 1 : 0; t.khop = kind ? 0 : -1; t.pad = 0;
+                    t.ratio = kind ? double(ri) : 1.0; t.u4 = s_ru4d[par * kResRngBatch + bi0 + i];
+                    J.trace[s + i] = t;
                 }
             }
-            if (J.trace && w == J.trace_walker && tid == 0) {
-                gv_trace t;
-                t.v1 = v1; t.v2 = v2; t.kind = kind; t.accepted = accepted; t.khop = kind ? 0 : -1; t.pad = 0;
-                t.ratio = double(ratio); t.u4 = s_ru4d[bi];
-                J.trace[s + i] = t;
+        }
+        if (done > 0 && first < kb) {   // the accepted exchange of step s + first
+            int ps = 0, pp = 0;
+            cx<T> u = {0.f, 0.f}, a = {0.f, 0.f};
+#pragma unroll
+            for (int i = 0; i < kResSpec; ++i)
+                if (i == first) { ps = psite[i]; pp = ppart[i]; u = pu[i]; a = pa[i]; }
+            const T* q = rb + 16 * first;
+            const cx<T> ru = {q[0] + q[2] + q[4] + q[6], q[1] + q[3] + q[5] + q[7]};
+            const cx<T> rd = {q[8] + q[10] + q[12] + q[14], q[9] + q[11] + q[13] + q[15]};
+            const int upf = ps & 0xFFFF, upt = ps >> 16;
+            const int dnf = upt, dnt = upf;
+            const int cu = pp & 0xFFFF, cd = pp >> 16;
+            const int cg = g ? cd : cu;
+            const cx<T> ir = cinv(g ? rd : ru);
+            // w = A^-1 u: this warp's 32 rows times u_f, summed over lanes per particle
+            cx<T>* wpart = s_wpart + (g * 4 + (warp & 3)) * 128;
+            for (int c = 0; c < NCH; ++c) {
+                uint32_t r[64];
+                tmem_ld64(trow + 64 * c, r);
+                tmem_wait_ld(r);
+                cx<T> v[32];
+#pragma unroll
+                for (int j = 0; j < 32; ++j) v[j] = cx<T>{__uint_as_float(r[2 * j]), __uint_as_float(r[2 * j + 1])} * u;
+                wpart[32 * c + lane] = warp_reduce_scatter(v);
             }
+            wg_sync(g);
+            if (f < 32 * NCH) {   // w_p - [p == c]
+                const cx<T>* wp0 = s_wpart + g * 4 * 128;
+                cx<T> wq = wp0[f] + wp0[128 + f] + wp0[256 + f] + wp0[384 + f];
+                if (f == cg) wq.x -= 1.f;
+                s_w[g * 128 + f] = wq;
+            }
+            wg_sync(g);
+            // row update: AiT[f][p] -= (w_p - [p == c]) * (A^-1)(c, f) / r
+            const cx<T> coef = cneg(a * ir);
+            const cx<T>* wv = s_w + g * 128;
+            for (int c = 0; c < NCH; ++c) {
+                uint32_t r[64];
+                tmem_ld64(trow + 64 * c, r);
+                tmem_wait_ld(r);
+#pragma unroll
+                for (int j = 0; j < 32; ++j) {
+                    const int p = 32 * c + j;
+                    cx<T> e = {__uint_as_float(r[2 * j]), __uint_as_float(r[2 * j + 1])};
+                    cmac(e, wv[p], coef);
+                    r[2 * j] = __float_as_uint(e.x);
+                    r[2 * j + 1] = __float_as_uint(e.y);
+                }
+                tmem_st64(trow + 64 * c, r);
+            }
+            tmem_wait_st();
+            if (tid == 0) {
+                s_fock[upt] = int16_t(cu); s_fock[upf] = -1; s_part[cu] = int16_t(upt);
+                s_fock[Ns + dnt] = int16_t(cd); s_fock[Ns + dnf] = -1; s_part[N + cd] = int16_t(dnt);
+                s_racc[2 * nacc] = ru;
+                s_racc[2 * nacc + 1] = rd;
+            }
+            ++nacc;
+            ++c_acc;
+            ++since;
+            __syncthreads();
         }
         if (done < 0) {   // stopped at step s - 1 - done: the walker takes no further steps
             s += uint64_t(-1 - done);
@@ -501,6 +620,7 @@ __global__ void __launch_bounds__(kResThreads, 1) k_walk_gs_res(DevJob J, uint64
         }
     }
     k += 4 * s;
+    cp_async_wait<0>();   // the rows of a batch not reached may still be landing in the tile's bytes
     __syncthreads();
     if (tid == 32) {
         for (int i = 0; i < nacc; ++i) {
@@ -508,15 +628,25 @@ __global__ void __launch_bounds__(kResThreads, 1) k_walk_gs_res(DevJob J, uint64
             amp_normalise(am, ae);
         }
     }
-    // write back: both inverses from TMEM, occupancy, counters
+    // write back: both inverses from TMEM through the shared tile (each thread
+    // stores its row segment, then coalesced 16-byte stores), occupancy, counters
     for (int c = 0; c < NCH; ++c) {
         uint32_t r[64];
         tmem_ld64(trow + 64 * c, r);
         tmem_wait_ld(r);
+        // tile c & 1: its previous readers (segment c - 2) passed the barrier of segment c - 1
+        cx<T>* tile = s_stage + (c & 1) * kTile;
+        float4* seg = reinterpret_cast<float4*>(tile + (g * 128 + f) * kResStageRow);
 #pragma unroll
-        for (int j = 0; j < 32; ++j) {
-            const int p = 32 * c + j;
-            if (f < N && p < N) Ag[size_t(f) * N + p] = cx<T>{__uint_as_float(r[2 * j]), __uint_as_float(r[2 * j + 1])};
+        for (int j = 0; j < 16; ++j)
+            seg[j] = make_float4(__uint_as_float(r[4 * j]), __uint_as_float(r[4 * j + 1]), __uint_as_float(r[4 * j + 2]),
+                                 __uint_as_float(r[4 * j + 3]));
+        __syncthreads();
+        for (int i = tid; i < 2 * 128 * 16; i += kResThreads) {
+            const int fl = i >> 11, row = (i >> 4) & 127, kp = i & 15, p = 32 * c + 2 * kp;
+            if (row < N && p < N)
+                *reinterpret_cast<float4*>(ai_ptr<T>(J, fl, w) + size_t(row) * N + p) =
+                    reinterpret_cast<const float4*>(tile + (fl * 128 + row) * kResStageRow)[kp];
         }
     }
     for (int i = tid; i < 2 * Ns; i += kResThreads) J.fock[size_t(w) * 2 * Ns + i] = s_fock[i];
