@@ -83,23 +83,62 @@ __device__ __forceinline__ void tmem_wait_ld(uint32_t (&r)[16])
                    "+r"(r[8]), "+r"(r[9]), "+r"(r[10]), "+r"(r[11]), "+r"(r[12]), "+r"(r[13]), "+r"(r[14]),
                    "+r"(r[15])::"memory");
 }
-// 16-byte asynchronous global -> shared copies (zero fill when !valid; the
-// source is then not read)
-__device__ __forceinline__ void cp_async16(void* smem_dst, const void* gsrc, bool valid)
-{
-    const uint32_t d = static_cast<uint32_t>(__cvta_generic_to_shared(smem_dst));
-    asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;" ::"r"(d), "l"(gsrc), "r"(valid ? 16 : 0) : "memory");
-}
-__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
-template <int n>
-__device__ __forceinline__ void cp_async_wait()
-{
-    asm volatile("cp.async.wait_group %0;" ::"n"(n) : "memory");
-}
 __device__ __forceinline__ void tmem_st64(uint32_t taddr, const uint32_t (&r)[64])
 {
     asm volatile("tcgen05.st.sync.aligned.32x32b.x64.b32 [%0], {%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31,%32,%33,%34,%35,%36,%37,%38,%39,%40,%41,%42,%43,%44,%45,%46,%47,%48,%49,%50,%51,%52,%53,%54,%55,%56,%57,%58,%59,%60,%61,%62,%63,%64};" ::"r"(taddr), "r"(r[0]), "r"(r[1]), "r"(r[2]), "r"(r[3]), "r"(r[4]), "r"(r[5]), "r"(r[6]), "r"(r[7]), "r"(r[8]), "r"(r[9]), "r"(r[10]), "r"(r[11]), "r"(r[12]), "r"(r[13]), "r"(r[14]), "r"(r[15]), "r"(r[16]), "r"(r[17]), "r"(r[18]), "r"(r[19]), "r"(r[20]), "r"(r[21]), "r"(r[22]), "r"(r[23]), "r"(r[24]), "r"(r[25]), "r"(r[26]), "r"(r[27]), "r"(r[28]), "r"(r[29]), "r"(r[30]), "r"(r[31]), "r"(r[32]), "r"(r[33]), "r"(r[34]), "r"(r[35]), "r"(r[36]), "r"(r[37]), "r"(r[38]), "r"(r[39]), "r"(r[40]), "r"(r[41]), "r"(r[42]), "r"(r[43]), "r"(r[44]), "r"(r[45]), "r"(r[46]), "r"(r[47]), "r"(r[48]), "r"(r[49]), "r"(r[50]), "r"(r[51]), "r"(r[52]), "r"(r[53]), "r"(r[54]), "r"(r[55]), "r"(r[56]), "r"(r[57]), "r"(r[58]), "r"(r[59]), "r"(r[60]), "r"(r[61]), "r"(r[62]), "r"(r[63]) : "memory");
 }
+constexpr int kTcWaitLimit = 1 << 22;     // mbarrier polls before a wait gives up
+
+// Poll the mbarrier phase up to `limit` times (a job's wait budget for the
+// waits whose failure the kernel reports; the drain wait before TMEM is freed
+// always takes the full kTcWaitLimit so that MMAs in flight finish first).
+__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity, int limit = kTcWaitLimit)
+{
+    for (int i = 0; i < limit; ++i) {
+        uint32_t done;
+        asm volatile(
+            "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+            "selp.b32 %0, 1, 0, p;\n\t}"
+            : "=r"(done)
+            : "r"(bar), "r"(parity)
+            : "memory");
+        if (done) return true;
+    }
+    return false;
+}
+
+// ---- mbarriers and bulk (TMA) copies ----
+__device__ __forceinline__ uint32_t smem_u32(const void* p) { return static_cast<uint32_t>(__cvta_generic_to_shared(p)); }
+__device__ __forceinline__ void mbar_init(uint32_t bar, uint32_t count)
+{
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count) : "memory");
+}
+// one arrival that also announces the bytes the phase's bulk copies will deliver
+__device__ __forceinline__ void mbar_expect_tx(uint32_t bar, uint32_t bytes)
+{
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
+}
+// global -> shared bulk copy completing on an mbarrier (16-byte aligned, bytes % 16 == 0)
+__device__ __forceinline__ void bulk_g2s(uint32_t dst, const void* src, uint32_t bytes, uint32_t bar)
+{
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
+                 ::"r"(dst), "l"(src), "r"(bytes), "r"(bar) : "memory");
+}
+// shared -> global bulk copy in this thread's bulk group
+__device__ __forceinline__ void bulk_s2g(void* dst, uint32_t src, uint32_t bytes)
+{
+    asm volatile("cp.async.bulk.global.shared::cta.bulk_group [%0], [%1], %2;" ::"l"(dst), "r"(src), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ void bulk_commit() { asm volatile("cp.async.bulk.commit_group;" ::: "memory"); }
+template <int n>
+__device__ __forceinline__ void bulk_wait_read()
+{
+    asm volatile("cp.async.bulk.wait_group.read %0;" ::"n"(n) : "memory");
+}
+__device__ __forceinline__ void bulk_wait_all() { asm volatile("cp.async.bulk.wait_group 0;" ::: "memory"); }
+// generic-proxy shared-memory accesses of this thread before its later bulk copies
+__device__ __forceinline__ void fence_proxy_async() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
+
 // barrier over one warpgroup (ids 1, 2; id 0 is __syncthreads)
 __device__ __forceinline__ void wg_sync(int g) { asm volatile("bar.sync %0, 128;" ::"r"(1 + g) : "memory"); }
 
@@ -108,10 +147,11 @@ constexpr int kResTmemCols = 512;                 // both flavours, 128 complex 
 constexpr size_t kResMinSmem = 116 * 1024;        // over half an SM's shared memory: one CTA per SM
 constexpr int kResRngBatch = 32;
 constexpr int kResSpec = 8;                       // proposals evaluated per barrier (<= 32: one lane each)
+constexpr int kResAccCap = 128;                   // accepted ratio pairs held before their product is taken
 constexpr int kResStageRow = 34;                  // complex per staged row segment: 32 + 2 (272 B rows: no bank conflicts)
 
 struct ResLayout {
-    size_t fock, part, nbr, sub, coef, red, wpart, w, rv, ru4, ru4d, racc, rq, rqp, nb, redm, ph, tbase, total, used;
+    size_t fock, part, nbr, sub, coef, red, wpart, w, rv, ru4, ru4d, racc, rq, rqp, nb, redm, ph, bars, tbase, total, used;
 };
 
 __host__ __device__ inline ResLayout res_layout(int Ns, int N, bool projheis)
@@ -128,10 +168,10 @@ __host__ __device__ inline ResLayout res_layout(int Ns, int N, bool projheis)
     l.red = al(sizeof(float) * 2 * 16 * kResSpec);
     l.wpart = al(c * 2 * 4 * 128);
     l.w = al(c * 2 * 128);
-    l.rv = al(sizeof(int16_t) * 2 * 2 * kResRngBatch);   // [batch parity][step][v1, v2]
-    l.ru4 = al(sizeof(float) * 2 * kResRngBatch);
-    l.ru4d = al(sizeof(double) * 2 * kResRngBatch);
-    l.racc = al(sizeof(cx<float>) * 2 * kResRngBatch);   // accepted ratio pairs of the batch
+    l.rv = al(sizeof(int16_t) * 3 * 2 * kResRngBatch);   // [batch % 3][step][v1, v2]
+    l.ru4 = al(sizeof(float) * 3 * kResRngBatch);
+    l.ru4d = al(sizeof(double) * 3 * kResRngBatch);
+    l.racc = al(sizeof(cx<float>) * 2 * kResAccCap);     // accepted ratio pairs not yet in the amplitude
     l.rq = al(projheis ? c * 4 * Ns : 16);
     l.rqp = al(projheis ? c * 2 * 4 * 4 * 128 : 16);   // [g][warp][slot][p] partial bond ratios
     l.nb = al(projheis ? sizeof(int32_t) * 2 * 4 * 128 : 16);   // [g][bond] particle, slot and site
@@ -142,6 +182,7 @@ __host__ __device__ inline ResLayout res_layout(int Ns, int N, bool projheis)
     const size_t ph_rows = c * 2 * kResRngBatch * 2 * size_t(N);
     const size_t stage = c * 2 * 2 * 128 * kResStageRow;   // two buffers
     l.ph = al(ph_rows > stage ? ph_rows : stage);
+    l.bars = al(sizeof(uint64_t) * 4);   // mbarriers: the two staging tiles, the two row buffers
     l.tbase = al(sizeof(uint32_t));
     l.used = al(16);
     l.total = l.used < kResMinSmem ? kResMinSmem : l.used;
@@ -199,8 +240,14 @@ __global__ void __launch_bounds__(kResThreads, 1) k_walk_gs_res(DevJob J, uint64
     int32_t* s_nb = reinterpret_cast<int32_t*>(smem + lay.nb);
     double* s_redm = reinterpret_cast<double*>(smem + lay.redm);
     uint32_t* s_tbase = reinterpret_cast<uint32_t*>(smem + lay.tbase);
+    uint64_t* s_bar = reinterpret_cast<uint64_t*>(smem + lay.bars);
+    const uint32_t ebar0 = smem_u32(s_bar), rbar0 = smem_u32(s_bar + 2);
 
     if (warp == 0) tmem_alloc(s_tbase, kResTmemCols);
+    if (tid == 32) {
+        for (int i = 0; i < 4; ++i) mbar_init(smem_u32(s_bar + i), 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
     for (int i = tid; i < 2 * Ns; i += kResThreads) s_fock[i] = J.fock[size_t(w) * 2 * Ns + i];
     for (int i = tid; i < 2 * N; i += kResThreads) {
         const int fl = i / N, p = i % N;
@@ -223,44 +270,52 @@ __global__ void __launch_bounds__(kResThreads, 1) k_walk_gs_res(DevJob J, uint64
     const int f = tid & 127;                      // TMEM lane = Slater row of this thread
     const uint32_t trow = tbase + ((uint32_t(warp & 3) * 32) << 16) + uint32_t(256 * g);
     // both inverses -> TMEM (lane f = row f of AiT, zero padding), 32 particles
-    // at a time: coalesced 16-byte copies of the rows' segments into a shared
-    // tile (N is even: a 16-byte piece never straddles two rows), then each
-    // thread moves its own row segment into its TMEM lane
+    // at a time: every thread copies its own row segment (256 B; N is even, so
+    // 16-byte multiples) into a shared tile with one bulk (TMA) copy completing
+    // on the tile's mbarrier, two segments in flight, then moves it into its
+    // TMEM lane.  Every wait is bounded (J.wait_limit polls); a wait that gives
+    // up ends the walker with GV_ERR_TIMEOUT after the copies in flight drained.
     cx<T>* s_stage = reinterpret_cast<cx<T>*>(smem + lay.ph);
     constexpr int kTile = 2 * 128 * kResStageRow;   // complex per staging tile
-    auto stage_segment = [&](int c, int b) {   // particles 32c .. 32c + 31 of both inverses -> tile b
-        for (int i = tid; i < 2 * 128 * 16; i += kResThreads) {
-            const int fl = i >> 11, row = (i >> 4) & 127, kp = i & 15, p = 32 * c + 2 * kp;
-            const bool ok = row < N && p < N;
-            const cx<T>* src = ai_ptr<T>(J, fl, w) + (ok ? size_t(row) * N + p : 0);
-            cp_async16(s_stage + b * kTile + (fl * 128 + row) * kResStageRow + 2 * kp, src, ok);
+    int ne_issued = 0, ne_done = 0;                 // staging phases issued / waited for
+    auto stage_segment = [&](int c) {   // particles 32c .. 32c + 31 of row f of flavour g -> tile c & 1
+        const int np = N - 32 * c < 32 ? N - 32 * c : 32;
+        const uint32_t bar = ebar0 + 8 * (c & 1);
+        if (tid == 0) mbar_expect_tx(bar, uint32_t(2 * N) * uint32_t(np) * 8u);
+        if (f < N) {
+            fence_proxy_async();
+            bulk_g2s(smem_u32(s_stage + (c & 1) * kTile + (g * 128 + f) * kResStageRow),
+                     ai_ptr<T>(J, g, w) + size_t(f) * N + 32 * c, uint32_t(np) * 8u, bar);
         }
-        cp_async_commit();
+        ++ne_issued;
     };
-    stage_segment(0, 0);   // two segments in flight
-    if (NCH > 1) stage_segment(1, 1);
-    for (int c = 0; c < NCH; ++c) {
-        if (c + 1 < NCH) cp_async_wait<1>();
-        else cp_async_wait<0>();
-        __syncthreads();
+    bool lost = false;   // a bounded wait gave up (block-uniform after each check)
+    stage_segment(0);
+    if (NCH > 1) stage_segment(1);
+    for (int c = 0; c < NCH && !lost; ++c) {
+        lost = !mbar_wait(ebar0 + 8 * (c & 1), (c >> 1) & 1, J.wait_limit);
+        lost = __syncthreads_or(lost);   // also: every wait on this phase is over before it is armed again
+        if (lost) break;
+        ++ne_done;
         const cx<T>* my_seg = s_stage + (c & 1) * kTile + (g * 128 + f) * kResStageRow;
         uint32_t r[64];
 #pragma unroll
-        for (int j = 0; j < 16; ++j) {
-            const float4 q = reinterpret_cast<const float4*>(my_seg)[j];
+        for (int j = 0; j < 16; ++j) {   // particles 32c + 2j, 32c + 2j + 1 (both < N or both >= N)
+            const bool in = f < N && 32 * c + 2 * j < N;
+            const float4 q = in ? reinterpret_cast<const float4*>(my_seg)[j] : make_float4(0.f, 0.f, 0.f, 0.f);
             r[4 * j] = __float_as_uint(q.x);
             r[4 * j + 1] = __float_as_uint(q.y);
             r[4 * j + 2] = __float_as_uint(q.z);
             r[4 * j + 3] = __float_as_uint(q.w);
         }
-        __syncthreads();   // the tile is free for segment c + 2
-        if (c + 2 < NCH) stage_segment(c + 2, c & 1);
+        if (c + 2 < NCH) stage_segment(c + 2);   // this thread's segment of the tile is read
         tmem_st64(trow + 64 * c, r);
     }
     tmem_wait_st();
     tmem_fence_before();
     __syncthreads();
     tmem_fence_after();
+    const bool loaded = !lost;   // both inverses are in TMEM
 
     const cx<T>* phase = J.phase32;
     const cx<T>* cf = s_coef + g * 2 * N;         // this flavour's [sub][f]
@@ -272,7 +327,36 @@ __global__ void __launch_bounds__(kResThreads, 1) k_walk_gs_res(DevJob J, uint64
     int ae = J.amp_e[w];
     int status = GV_OK;
     int rbuf = 0;
-    int nacc = 0;   // accepted ratio pairs waiting to be multiplied into the amplitude
+    int nacc = 0;   // accepted ratio pairs waiting to be multiplied into the amplitude (block-uniform)
+    // The amplitude (FP64 mantissa, base-2 exponent; LatticeStepper's running
+    // product of the accepted ratios) is brought up to date only when the
+    // pairs' buffer could fill within the next batch, and at the end of the
+    // call: warp 1 multiplies the pending pairs as a tree (lane products, then
+    // five shuffle levels, each product renormalised), so that the slow FP64
+    // pipe sits on the per-step path only once every few sweeps.
+    auto flush_amp = [&]() {
+        if (warp == 1) {
+            cx<double> v = {1.0, 0.0};
+            int e = 0;
+            for (int i = lane; i < nacc; i += 32) {
+                v = v * (to_d(s_racc[2 * i]) * to_d(s_racc[2 * i + 1]));
+                amp_normalise(v, e);
+            }
+#pragma unroll
+            for (int o = 16; o; o >>= 1) {
+                const cx<double> u = {__shfl_xor_sync(0xffffffffu, v.x, o), __shfl_xor_sync(0xffffffffu, v.y, o)};
+                e += __shfl_xor_sync(0xffffffffu, e, o);
+                v = v * u;
+                amp_normalise(v, e);
+            }
+            if (lane == 0) {   // thread 32 holds the amplitude
+                am = am * v;
+                ae += e;
+                amp_normalise(am, ae);
+            }
+        }
+        nacc = 0;
+    };
     const WalkCtx<T> C = {&J, w, Ns, N, L, Nk, N, N, s_fock, s_part, s_nbr, s_coef, s_rq, s_redm,
                           phase, ai_ptr<T>(J, 0, w), ai_ptr<T>(J, 1, w)};
     // Proposals are evaluated kResSpec at a time: every thread forms its terms
@@ -284,77 +368,80 @@ __global__ void __launch_bounds__(kResThreads, 1) k_walk_gs_res(DevJob J, uint64
     // crosses a uniform batch or a measurement step.
     // The uniforms of a batch and the phase rows of both sites of its
     // proposals (whichever site a particle moves to, its row is there) are in
-    // shared memory before the batch starts: batch b + 1 is drawn and its rows
-    // copied asynchronously while batch b runs (the Metropolis stream does not
-    // depend on the walk).
+    // shared memory before the batch starts: at the start of batch b, warp 0
+    // draws batch b + 2 while every warp issues bulk copies of batch b + 1's
+    // rows (drawn a batch earlier), which land while batch b runs (the
+    // Metropolis stream does not depend on the walk).
     cx<T>* s_ph = reinterpret_cast<cx<T>*>(smem + lay.ph);
-    const int half = N / 2;   // 16-byte pieces per phase row
-    // warp 0: steps sb .. sb + 31 into parity par; a step past the call's end
-    // gets the sites (0, 0), so that every entry is a valid site index
-    auto draw_batch = [&](uint64_t sb, int par) {
+    // warp 0: steps sb .. sb + 31 into slot rs; a step past the call's end
+    // gets the sites (0, 0), so that every entry is a valid site index (the
+    // FP64 uniform is kept for the trace only)
+    auto draw_batch = [&](uint64_t sb, int rs) {
+        int v1 = 0, v2 = 0;
+        float ru = 0.f;
+        double rud = 0.0;
+        if (sb + lane < nsteps) {
+            const uint64_t kl = k + 4 * (sb + uint64_t(lane));
+            uint32_t x[4], y[4];
+            philox_call(J.seed, wid, 0, kl >> 1, x);
+            philox_call(J.seed, wid, 0, (kl >> 1) + 1, y);
+            v1 = scaled_floor(uint32_t(Ns), u52(x[0], x[1]));
+            v2 = s_nbr[v1 * 4 + int(u52(x[2], x[3]) >> 50)];
+            ru = Accept<T>::uniform(u52(y[2], y[3]));
+            if (J.trace) rud = u01(y[2], y[3]);
+        }
+        s_rv[(rs * kResRngBatch + lane) * 2] = int16_t(v1);
+        s_rv[(rs * kResRngBatch + lane) * 2 + 1] = int16_t(v2);
+        s_ru4[rs * kResRngBatch + lane] = ru;
+        s_ru4d[rs * kResRngBatch + lane] = rud;
+    };
+    // all warps: the 2 x 32 phase rows of the batch in slot rs (row 2 step +
+    // site, 8N bytes each) into row buffer par, one bulk copy by each of lanes
+    // 0..7 of every warp, completing on that buffer's mbarrier
+    static_assert(kResThreads == 256 && 2 * kResRngBatch == 64, "eight row copies per warp");
+    auto fetch_batch_rows = [&](int rs, int par) {
+        const uint32_t bar = rbar0 + 8 * par, rowb = uint32_t(N) * 8u;
+        if (tid == 0) mbar_expect_tx(bar, uint32_t(2 * kResRngBatch) * rowb);
+        if (lane < 8) {
+            const int q = warp * 8 + lane;
+            const int site = s_rv[(rs * kResRngBatch + (q >> 1)) * 2 + (q & 1)];
+            fence_proxy_async();
+            bulk_g2s(smem_u32(s_ph + (size_t(par) * 2 * kResRngBatch + q) * N), phase + size_t(site) * Nk, rowb, bar);
+        }
+    };
+    uint32_t nb_issued = 0, nb_waited = 0;   // row batches copied / waited for
+    int rs_cur = 0;                          // uniform slot of the current batch
+    if (!lost) {
         if (warp == 0) {
-            int v1 = 0, v2 = 0;
-            float ru = 0.f;
-            double rud = 0.0;
-            if (sb + lane < nsteps) {
-                const uint64_t kl = k + 4 * (sb + uint64_t(lane));
-                uint32_t x[4], y[4];
-                philox_call(J.seed, wid, 0, kl >> 1, x);
-                philox_call(J.seed, wid, 0, (kl >> 1) + 1, y);
-                v1 = scaled_floor(uint32_t(Ns), u52(x[0], x[1]));
-                v2 = s_nbr[v1 * 4 + int(u52(x[2], x[3]) >> 50)];
-                ru = Accept<T>::uniform(u52(y[2], y[3]));
-                rud = u01(y[2], y[3]);
-            }
-            s_rv[(par * kResRngBatch + lane) * 2] = int16_t(v1);
-            s_rv[(par * kResRngBatch + lane) * 2 + 1] = int16_t(v2);
-            s_ru4[par * kResRngBatch + lane] = ru;
-            s_ru4d[par * kResRngBatch + lane] = rud;
+            draw_batch(0, 0);
+            draw_batch(kResRngBatch, 1);
         }
-    };
-    // all threads, one commit group: thread t copies 16-byte piece t % 64 of
-    // rows t / 64 + 4 j (row = 2 step + site) of parity par
-    static_assert(kResThreads == 256 && 2 * kResRngBatch == 64, "row fetch mapping");
-    auto fetch_batch_rows = [&](uint64_t sb, int par) {
-        const int kp = tid & 63;
-        if (kp < half) {
-#pragma unroll
-            for (int j = 0; j < 16; ++j) {
-                const int row = (tid >> 6) + 4 * j, step = row >> 1;
-                const int site = s_rv[(par * kResRngBatch + step) * 2 + (row & 1)];
-                cp_async16(s_ph + (size_t(par) * 2 * kResRngBatch + row) * N + 2 * kp,
-                           phase + size_t(site) * Nk + 2 * kp, sb + uint64_t(step) < nsteps);
-            }
-        }
-        cp_async_commit();
-    };
-    draw_batch(0, 0);
-    __syncthreads();
-    fetch_batch_rows(0, 0);
+        __syncthreads();
+        fetch_batch_rows(0, 0);
+        nb_issued = 1;
+    }
     const bool measuring = meas != 0 && mask != 0;
     // steps from s to the next measuring step (0: s itself is measured)
     uint64_t to_meas = measuring ? (meas == 1 ? 0 : (meas - (s0 % meas)) % meas) : ~uint64_t(0);
     uint64_t s = 0;
-    while (s < nsteps) {
+    while (!lost && s < nsteps) {
         const int bi0 = int(s % kResRngBatch);
         const int par = int(s / kResRngBatch) & 1;
+        if (bi0 == 0 && s > 0) rs_cur = rs_cur == 2 ? 0 : rs_cur + 1;
+        const int rs1 = rs_cur == 2 ? 0 : rs_cur + 1, rs2 = rs1 == 2 ? 0 : rs1 + 1;
         if (bi0 == 0) {
             __syncthreads();   // every thread is done with the previous batch and its buffers
-            // the amplitude (FP64, off the per-step path): the previous batch's accepted ratios
-            if (tid == 32) {
-                for (int i = 0; i < nacc; ++i) {
-                    am = am * (to_d(s_racc[2 * i]) * to_d(s_racc[2 * i + 1]));
-                    amp_normalise(am, ae);
-                }
-            }
-            nacc = 0;
-            draw_batch(s + kResRngBatch, par ^ 1);
-            __syncthreads();
-            fetch_batch_rows(s + kResRngBatch, par ^ 1);
-            cp_async_wait<1>();   // this batch's rows (the group before) have landed
-            __syncthreads();
+            if (nacc > kResAccCap - kResRngBatch) flush_amp();   // a batch accepts at most 32
+            fetch_batch_rows(rs1, par ^ 1);                              // batch b + 1's rows in flight
+            if (warp == 0) draw_batch(s + 2 * kResRngBatch, rs2);        // batch b + 2's uniforms
+            ++nb_issued;
+            // this batch's rows (its barrier is armed again only after the next
+            // batch boundary, which every thread reaches after this wait)
+            const bool ok = mbar_wait(rbar0 + 8 * (nb_waited & 1), (nb_waited >> 1) & 1, J.wait_limit);
+            ++nb_waited;
+            if (__syncthreads_or(!ok)) { status = GV_ERR_TIMEOUT; lost = true; break; }
         }
-        const int16_t* rv = s_rv + par * 2 * kResRngBatch;
+        const int16_t* rv = s_rv + rs_cur * 2 * kResRngBatch;
         const cx<T>* prow = s_ph + size_t(par) * 2 * kResRngBatch * N;
         uint64_t kb64 = nsteps - s;
         if (kb64 > uint64_t(kResRngBatch - bi0)) kb64 = uint64_t(kResRngBatch - bi0);
@@ -441,7 +528,7 @@ __global__ void __launch_bounds__(kResThreads, 1) k_walk_gs_res(DevJob J, uint64
             ratio = Accept<T>::ratio(ru, rd);
             if (!isfinite(ratio)) {
                 stop = 2;
-            } else if (ratio > T(1) || s_ru4[par * kResRngBatch + bi0 + lane] < ratio) {
+            } else if (ratio > T(1) || s_ru4[rs_cur * kResRngBatch + bi0 + lane] < ratio) {
                 stop = (norm2(ru) < T(1e-9) || norm2(rd) < T(1e-9)) ? 3 : 1;
             }
         }
@@ -469,7 +556,7 @@ __global__ void __launch_bounds__(kResThreads, 1) k_walk_gs_res(DevJob J, uint64
                     gv_trace t;
                     t.v1 = rv[2 * (bi0 + i)]; t.v2 = rv[2 * (bi0 + i) + 1];
                     t.kind = kind; t.accepted = (!kind || i == first) ? 1 : 0; t.khop = kind ? 0 : -1; t.pad = 0;
-                    t.ratio = kind ? double(ri) : 1.0; t.u4 = s_ru4d[par * kResRngBatch + bi0 + i];
+                    t.ratio = kind ? double(ri) : 1.0; t.u4 = s_ru4d[rs_cur * kResRngBatch + bi0 + i];
                     J.trace[s + i] = t;
                 }
             }
@@ -579,10 +666,10 @@ __global__ void __launch_bounds__(kResThreads, 1) k_walk_gs_res(DevJob J, uint64
                     uint32_t rr[64];
                     int ent[32];
 #pragma unroll
-                    for (int t = 0; t < 32; ++t) {
+                    for (int t = 0; t < 32; ++t) {   // branch-free: a bond without a ratio loads particle 0
                         ent[t] = e0 + t < NE ? tab[e0 + t] : -1;
-                        uint32_t r2[2] = {0u, 0u};
-                        if (ent[t] >= 0) tmem_ld2(trow + 2 * (ent[t] & 0xFF), r2);
+                        uint32_t r2[2];
+                        tmem_ld2(trow + 2 * (ent[t] >= 0 ? (ent[t] & 0xFF) : 0), r2);
                         rr[2 * t] = r2[0];
                         rr[2 * t + 1] = r2[1];
                     }
@@ -620,34 +707,37 @@ __global__ void __launch_bounds__(kResThreads, 1) k_walk_gs_res(DevJob J, uint64
         }
     }
     k += 4 * s;
-    cp_async_wait<0>();   // the rows of a batch not reached may still be landing in the tile's bytes
-    __syncthreads();
-    if (tid == 32) {
-        for (int i = 0; i < nacc; ++i) {
-            am = am * (to_d(s_racc[2 * i]) * to_d(s_racc[2 * i + 1]));
-            amp_normalise(am, ae);
-        }
-    }
-    // write back: both inverses from TMEM through the shared tile (each thread
-    // stores its row segment, then coalesced 16-byte stores), occupancy, counters
-    for (int c = 0; c < NCH; ++c) {
-        uint32_t r[64];
-        tmem_ld64(trow + 64 * c, r);
-        tmem_wait_ld(r);
-        // tile c & 1: its previous readers (segment c - 2) passed the barrier of segment c - 1
-        cx<T>* tile = s_stage + (c & 1) * kTile;
-        float4* seg = reinterpret_cast<float4*>(tile + (g * 128 + f) * kResStageRow);
+    // the copies still in flight land before their bytes are used again (bounded)
+    bool drained = true;
+    for (; nb_waited < nb_issued; ++nb_waited)
+        drained = mbar_wait(rbar0 + 8 * (nb_waited & 1), (nb_waited >> 1) & 1) && drained;
+    for (; ne_done < ne_issued; ++ne_done)
+        drained = mbar_wait(ebar0 + 8 * (ne_done & 1), (ne_done >> 1) & 1) && drained;
+    drained = !__syncthreads_or(!drained);
+    if (lost) status = GV_ERR_TIMEOUT;
+    flush_amp();
+    // write back (unless the inverses were not all loaded, or the tiles' bytes
+    // may still be written by a copy that was not seen to land): each thread
+    // moves its row segment from TMEM to its slot of a tile and stores it with
+    // one bulk copy; the slot is written again two segments later, once that
+    // copy has read it
+    if (loaded && drained) {
+        for (int c = 0; c < NCH; ++c) {
+            uint32_t r[64];
+            tmem_ld64(trow + 64 * c, r);
+            tmem_wait_ld(r);
+            if (c >= 2) bulk_wait_read<1>();
+            float4* seg = reinterpret_cast<float4*>(s_stage + (c & 1) * kTile + (g * 128 + f) * kResStageRow);
 #pragma unroll
-        for (int j = 0; j < 16; ++j)
-            seg[j] = make_float4(__uint_as_float(r[4 * j]), __uint_as_float(r[4 * j + 1]), __uint_as_float(r[4 * j + 2]),
-                                 __uint_as_float(r[4 * j + 3]));
-        __syncthreads();
-        for (int i = tid; i < 2 * 128 * 16; i += kResThreads) {
-            const int fl = i >> 11, row = (i >> 4) & 127, kp = i & 15, p = 32 * c + 2 * kp;
-            if (row < N && p < N)
-                *reinterpret_cast<float4*>(ai_ptr<T>(J, fl, w) + size_t(row) * N + p) =
-                    reinterpret_cast<const float4*>(tile + (fl * 128 + row) * kResStageRow)[kp];
+            for (int j = 0; j < 16; ++j)
+                seg[j] = make_float4(__uint_as_float(r[4 * j]), __uint_as_float(r[4 * j + 1]),
+                                     __uint_as_float(r[4 * j + 2]), __uint_as_float(r[4 * j + 3]));
+            fence_proxy_async();
+            const int np = N - 32 * c < 32 ? N - 32 * c : 32;
+            if (f < N) bulk_s2g(ai_ptr<T>(J, g, w) + size_t(f) * N + 32 * c, smem_u32(seg), uint32_t(np) * 8u);
+            bulk_commit();
         }
+        bulk_wait_all();
     }
     for (int i = tid; i < 2 * Ns; i += kResThreads) J.fock[size_t(w) * 2 * Ns + i] = s_fock[i];
     for (int i = tid; i < 2 * N; i += kResThreads) {

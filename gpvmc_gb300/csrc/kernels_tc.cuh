@@ -40,7 +40,6 @@ namespace {
 
 constexpr int kTcThreads = 256;
 constexpr int kTcM = 128;                 // MMA rows (up particles, zero padded)
-constexpr int kTcWaitLimit = 1 << 22;     // mbarrier polls before a wait gives up
 
 __host__ __device__ inline int tc_ncols(int N) { return (N + 15) & ~15; }
 
@@ -268,23 +267,6 @@ __device__ __forceinline__ void tc_commit(uint32_t bar)
     asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar) : "memory");
 }
 
-// Poll the mbarrier phase up to `limit` times (a job's wait budget for the
-// waits whose failure the kernel reports; the drain wait before TMEM is freed
-// always takes the full kTcWaitLimit so that MMAs in flight finish first).
-__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity, int limit = kTcWaitLimit)
-{
-    for (int i = 0; i < limit; ++i) {
-        uint32_t done;
-        asm volatile(
-            "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
-            "selp.b32 %0, 1, 0, p;\n\t}"
-            : "=r"(done)
-            : "r"(bar), "r"(parity)
-            : "memory");
-        if (done) return true;
-    }
-    return false;
-}
 
 __device__ __forceinline__ void tmem_wait_ld(uint32_t (&r)[32])
 {

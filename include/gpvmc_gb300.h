@@ -153,11 +153,12 @@ gv_status gv_job_reset_quantities(gv_job* job);
 gv_status gv_job_read_drift_checks(gv_job* job, double* drift_seen, uint64_t* checks_without_reinversion);
 
 /* Bounded device waits.  The tensor-core kernels (StatSpinStruct pair
- * ratios, exciton overlap rows) wait on an mbarrier for their MMAs with a
- * poll budget; when it runs out the walker's status becomes GV_ERR_TIMEOUT,
- * the kernel still lets the MMAs it issued finish before it frees its tensor
- * memory, and the next calls on the job run normally (gv_job_init_walkers
- * clears the status).  polls < 0 restores the default (4194304 polls);
+ * ratios, exciton overlap rows) wait on an mbarrier for their MMAs, and the
+ * on-chip ground-state walk for its bulk (TMA) copies of the inverses and of
+ * the proposals' phase rows, with a poll budget; when it runs out the
+ * walker's status becomes GV_ERR_TIMEOUT, the kernel still lets the MMAs or
+ * copies it issued finish before it frees its tensor memory, and the next
+ * calls on the job run normally (gv_job_init_walkers clears the status).  polls < 0 restores the default (4194304 polls);
  * polls = 0 makes every such wait give up at once, which tests exercise.
  * Applies to kernels enqueued after the call (cached CUDA graphs are
  * dropped).  Diagnostic; it has no counterpart in the reference, whose
