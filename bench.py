@@ -866,10 +866,10 @@ def run_serving(g):
 
 # DRAM bytes per walker per walk launch of k_walk_gs_res (inverses in at entry,
 # out at exit, plus tables): dram__bytes_read.sum + dram__bytes_write.sum of
-# one measured sweep of the 2048-walker workload (557.43 MB + 484.71 MB, a
+# one measured sweep of the 2048-walker workload (557.59 MB + 478.38 MB, a
 # one-pass ncu capture), summarised in
 # profiles/k_walk_gs_res_L16_2048walkers_dram.md
-RES_DRAM_BYTES_PER_WALKER = (557.43e6 + 484.71e6) / 2048
+RES_DRAM_BYTES_PER_WALKER = (557.59e6 + 478.38e6) / 2048
 
 
 def sm_count():
@@ -941,8 +941,9 @@ def walk_roofline(res, precision):
                                              "kernel: the speed-up over that formulation's HBM bound, not a "
                                              "bandwidth drawn"}}
     if resident:
-        roof["binding_resource"] = ("on-chip latency with one walker (8 warps) per SM: ncu issue-active 38.5 %, "
-                                    "FMA pipe 17.3 %, top stalls wait / short scoreboard "
+        roof["binding_resource"] = ("instruction issue and short dependency chains with one walker (8 warps) per "
+                                    "SM: ncu issue-active 53.8 %, ALU pipe 37.6 %, FMA pipe 25.5 %, stalls per "
+                                    "issue wait 0.71 / short scoreboard 0.66 / not selected 0.48 "
                                     "(profiles/k_walk_gs_res_L16_304walkers.md)")
     return roof
 
