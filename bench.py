@@ -408,8 +408,9 @@ def run_exciton(g, sweeps, fp64_sweeps):
            "unit": "steps/s"}
     for prec, n in (("mixed", sweeps), ("fp64", fp64_sweeps)):
         jobs = exciton_jobs(g, prec)
-        for j in jobs:
-            j.walk(SWEEP, 0, sync=False)
+        for _ in range(THERM_SWEEPS):   # thermalised as the headline walk, both arms alike
+            for j in jobs:
+                j.walk(SWEEP, 0, sync=False)
         for j in jobs:
             j.synchronize()
         t0 = time.perf_counter()

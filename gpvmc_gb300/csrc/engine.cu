@@ -553,17 +553,21 @@ gv_status launch_walk_trans(gv_job* j, uint64_t nsteps)
 
 // On-chip exciton walk (GupT and the flavour-1 inverse in TMEM, the flavour-0
 // inverse in shared memory): mixed, Nexc <= 128, deferred re-inversion.
+constexpr size_t kMaxSmemPerBlock = 227 * 1024;   // opt-in dynamic shared memory per block on sm_100 / sm_103
+
 bool trans_resident_ok(const gv_job* j, uint64_t nsteps)
 {
     const int f = j->cfg.flags;
+    // the staged phase rows are copied whole (8 Nk bytes: a multiple of 16)
     return nsteps > 0 && j->trans && j->cfg.precision == GV_PREC_MIXED &&
-           trans_res_fits(j->N[0], j->N[1], j->ch.Nexc) && (f & GV_FLAG_REINV_DEFERRED) &&
-           !(f & GV_FLAG_STREAM_INVERSES);
+           trans_res_fits(j->N[0], j->N[1], j->ch.Nexc) && j->Nk % 2 == 0 &&
+           trans_res_layout(j->Ns, j->Nk, j->Nmax, j->N[0], j->ch.Nexc).total <= kMaxSmemPerBlock &&
+           (f & GV_FLAG_REINV_DEFERRED) && !(f & GV_FLAG_STREAM_INVERSES);
 }
 
 gv_status launch_walk_trans_res(gv_job* j, uint64_t nsteps)
 {
-    const TrResLayout lay = trans_res_layout(j->Ns, j->Nmax, j->N[0], j->ch.Nexc);
+    const TrResLayout lay = trans_res_layout(j->Ns, j->Nk, j->Nmax, j->N[0], j->ch.Nexc);
     GV_CK(raise_smem_limit(k_walk_trans_res, lay.total));
     GV_CK(cudaFuncSetAttribute(k_walk_trans_res, cudaFuncAttributePreferredSharedMemoryCarveout, 100));
     int slot;

@@ -27,6 +27,8 @@ namespace {
 constexpr int kTrThreads = 256;
 constexpr size_t kTrMinSmem = 116 * 1024;   // over half an SM's shared memory: one CTA per SM
 constexpr uint32_t kA1Col = 256;            // first TMEM column of AiT1
+constexpr int kTrBatch = 8;                 // steps per uniform batch (phase rows staged per batch)
+constexpr int kTrAccCap = 64;               // accepted ratio pairs held before their product is taken
 
 __host__ __device__ inline bool trans_res_fits(int N0, int N1, int Nexc)
 {
@@ -52,10 +54,10 @@ __device__ __forceinline__ cx<float> smem_col_dot(const cx<float>* A, int N, int
 
 struct TrResLayout {
     size_t a0, g128, fock, part, wslot, worb, nbr, exu, exd, coef, C, rowc, g, Y, zp, phk, ru, rd, dk, ak, bk, X, Yv, zc,
-        hrow, wpart, wa, red, tbase, total, used;
+        hrow, wpart, wa, red, brv, bu4, bu4d, bph, bacc, bbar, tbase, total, used;
 };
 
-__host__ __device__ inline TrResLayout trans_res_layout(int Ns, int Nmax, int N0, int Nexc)
+__host__ __device__ inline TrResLayout trans_res_layout(int Ns, int Nk, int Nmax, int N0, int Nexc)
 {
     TrResLayout l;
     size_t b = 0;
@@ -89,6 +91,12 @@ __host__ __device__ inline TrResLayout trans_res_layout(int Ns, int Nmax, int N0
     l.wpart = al(c * 4 * 128);
     l.wa = al(c * 128);
     l.red = al(sizeof(float) * 2 * 8 * (kTrThreads / 32) + sizeof(int) * (kTrThreads / 32) + 64);
+    l.brv = al(sizeof(int16_t) * 3 * 2 * kTrBatch);            // [batch % 3][step][v1, v2]
+    l.bu4 = al(sizeof(float) * 3 * kTrBatch);
+    l.bu4d = al(sizeof(double) * 3 * kTrBatch);
+    l.bph = al(c * 2 * 2 * kTrBatch * size_t(Nk));             // [batch parity][2 step + site][Nk] phase rows
+    l.bacc = al(c * 2 * kTrAccCap);                            // accepted ratio pairs not yet in the amplitude
+    l.bbar = al(sizeof(uint64_t) * 2);                         // the row buffers' mbarriers
     l.tbase = al(16);
     l.used = al(16);
     l.total = l.used < kTrMinSmem ? kTrMinSmem : l.used;
@@ -105,7 +113,7 @@ __global__ void __launch_bounds__(kTrThreads, 1) k_walk_trans_res(DevJob J, uint
     if (w >= J.W || J.status[w] != GV_OK) return;   // before any TMEM allocation
     const int Ns = J.Ns, Nmax = J.Nmax, L = J.L, Nk = J.Nk, Nexc = J.Nexc;
     const int N0 = J.N[0], N1 = J.N[1];
-    const TrResLayout lay = trans_res_layout(Ns, Nmax, N0, Nexc);
+    const TrResLayout lay = trans_res_layout(Ns, Nk, Nmax, N0, Nexc);
     cx<T>* A0s = reinterpret_cast<cx<T>*>(smem + lay.a0);
     cx<T>* s_g128 = reinterpret_cast<cx<T>*>(smem + lay.g128);   // GupT[128][k]
     int16_t* s_fock = reinterpret_cast<int16_t*>(smem + lay.fock);
@@ -135,8 +143,20 @@ __global__ void __launch_bounds__(kTrThreads, 1) k_walk_trans_res(DevJob J, uint
     cx<T>* s_wa = reinterpret_cast<cx<T>*>(smem + lay.wa);
     T* s_red = reinterpret_cast<T*>(smem + lay.red);
     uint32_t* s_tbase = reinterpret_cast<uint32_t*>(smem + lay.tbase);
+    int16_t* b_rv = reinterpret_cast<int16_t*>(smem + lay.brv);
+    float* b_u4 = reinterpret_cast<float*>(smem + lay.bu4);
+    double* b_u4d = reinterpret_cast<double*>(smem + lay.bu4d);
+    cx<T>* b_ph = reinterpret_cast<cx<T>*>(smem + lay.bph);
+    cx<T>* b_acc = reinterpret_cast<cx<T>*>(smem + lay.bacc);
+    uint64_t* b_bar = reinterpret_cast<uint64_t*>(smem + lay.bbar);
+    const uint32_t rbar0 = smem_u32(b_bar);
 
     if (warp == 0) tmem_alloc(s_tbase, 512);
+    if (tid == 32) {
+        mbar_init(rbar0, 1);
+        mbar_init(rbar0 + 8, 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
     for (int i = tid; i < 2 * Ns; i += NT) {
         s_fock[i] = J.fock[size_t(w) * 2 * Ns + i];
         s_wslot[i] = J.wslot[size_t(w) * 2 * Ns + i];
@@ -215,14 +235,101 @@ __global__ void __launch_bounds__(kTrThreads, 1) k_walk_trans_res(DevJob J, uint
     double sigma = J.sigma[w];
     int status = GV_OK;
     int rbuf = 0;
+    // Uniform batches of kTrBatch steps: warp 0 draws batch b + 2 while the
+    // phase rows phi(v1), phi(v2) of batch b + 1 (drawn a batch earlier) come
+    // into shared memory as bulk copies on that buffer's mbarrier, so that no
+    // step computes Philox numbers or reads the phase table in global memory
+    // (every site a step's formulas name is v1 or v2).
+    const uint64_t kk0 = kk;
+    auto draw_batch = [&](uint64_t sb, int rs) {   // warp 0; a step past the call's end gets sites (0, 0)
+        if (lane < kTrBatch) {
+            int a1 = 0, a2 = 0;
+            float u = 0.f;
+            double ud = 0.0;
+            if (sb + lane < nsteps) {
+                const uint64_t kl = kk0 + 4 * (sb + uint64_t(lane));
+                uint32_t x[4], y[4];
+                philox_call(J.seed, wid, 0, kl >> 1, x);
+                philox_call(J.seed, wid, 0, (kl >> 1) + 1, y);
+                a1 = scaled_floor(uint32_t(Ns), u52(x[0], x[1]));
+                a2 = s_nbr[a1 * 4 + int(u52(x[2], x[3]) >> 50)];
+                u = Accept<T>::uniform(u52(y[2], y[3]));
+                if (J.trace) ud = u01(y[2], y[3]);
+            }
+            b_rv[(rs * kTrBatch + lane) * 2] = int16_t(a1);
+            b_rv[(rs * kTrBatch + lane) * 2 + 1] = int16_t(a2);
+            b_u4[rs * kTrBatch + lane] = u;
+            b_u4d[rs * kTrBatch + lane] = ud;
+        }
+    };
+    auto fetch_rows = [&](int rs, int par) {   // threads 0 .. 2 kTrBatch - 1: one row (8 Nk bytes) each
+        const uint32_t bar = rbar0 + 8 * par, rowb = uint32_t(Nk) * 8u;
+        if (tid == 0) mbar_expect_tx(bar, uint32_t(2 * kTrBatch) * rowb);
+        if (tid < 2 * kTrBatch) {
+            const int site = b_rv[(rs * kTrBatch + (tid >> 1)) * 2 + (tid & 1)];
+            fence_proxy_async();
+            bulk_g2s(smem_u32(b_ph + (size_t(par) * 2 * kTrBatch + tid) * Nk), phase + size_t(site) * Nk, rowb, bar);
+        }
+    };
+    // The amplitude's FP64 products of the accepted ratio pairs, as a warp tree
+    // once the pairs' buffer could fill within the next batch and at the end
+    // (thread 0 holds the amplitude)
+    int nacc = 0;
+    auto flush_amp = [&]() {
+        if (warp == 0) {
+            cx<double> v = {1.0, 0.0};
+            int e = 0;
+            for (int i = lane; i < nacc; i += 32) {
+                v = v * (to_d(b_acc[2 * i]) * to_d(b_acc[2 * i + 1]));
+                amp_normalise(v, e);
+            }
+#pragma unroll
+            for (int o = 16; o; o >>= 1) {
+                const cx<double> u = {__shfl_xor_sync(0xffffffffu, v.x, o), __shfl_xor_sync(0xffffffffu, v.y, o)};
+                e += __shfl_xor_sync(0xffffffffu, e, o);
+                v = v * u;
+                amp_normalise(v, e);
+            }
+            if (lane == 0) {
+                am = am * v;
+                ae += e;
+                amp_normalise(am, ae);
+            }
+        }
+        nacc = 0;
+    };
+    uint32_t nb_issued = 0, nb_waited = 0;
+    int rs_cur = 0;
+    if (warp == 0) {
+        draw_batch(0, 0);
+        draw_batch(kTrBatch, 1);
+    }
+    __syncthreads();
+    fetch_rows(0, 0);
+    nb_issued = 1;
 
     for (uint64_t s = 0; s < nsteps; ++s, kk += 4) {
-        uint32_t x[4], y[4];
-        philox_call(J.seed, wid, 0, kk >> 1, x);
-        philox_call(J.seed, wid, 0, (kk >> 1) + 1, y);
-        const uint64_t m4 = u52(y[2], y[3]);
-        const int v1 = scaled_floor(uint32_t(Ns), u52(x[0], x[1]));
-        const int v2 = s_nbr[v1 * 4 + int(u52(x[2], x[3]) >> 50)];
+        const int bi = int(s % kTrBatch);
+        const int par = int(s / kTrBatch) & 1;
+        if (bi == 0) {
+            if (s > 0) rs_cur = rs_cur == 2 ? 0 : rs_cur + 1;
+            const int rs1 = rs_cur == 2 ? 0 : rs_cur + 1, rs2 = rs1 == 2 ? 0 : rs1 + 1;
+            __syncthreads();   // every thread is done with batch b - 1 and its buffers
+            if (nacc > kTrAccCap - kTrBatch) flush_amp();
+            fetch_rows(rs1, par ^ 1);
+            if (warp == 0) draw_batch(s + 2 * kTrBatch, rs2);
+            ++nb_issued;
+            const bool ok = mbar_wait(rbar0 + 8 * (nb_waited & 1), (nb_waited >> 1) & 1, J.wait_limit);
+            ++nb_waited;
+            if (__syncthreads_or(!ok)) { status = GV_ERR_TIMEOUT; break; }
+        }
+        const int v1 = b_rv[(rs_cur * kTrBatch + bi) * 2], v2 = b_rv[(rs_cur * kTrBatch + bi) * 2 + 1];
+        const cx<T>* row1 = b_ph + (size_t(par) * 2 * kTrBatch + 2 * bi) * Nk;   // phase row of v1, then of v2
+        // phi_o(site) of orbital o from the staged rows (site is v1 or v2)
+        auto phi_st = [&](const cx<T>* cfx, int site, int o) {
+            const cx<T>* row = site == v1 ? row1 : row1 + Nk;
+            return cmul_rn(row[o >> 1], cfx[size_t(sublattice(site, L)) * Ns + o]);
+        };
         const int f1 = s_fock[v1] >= 0 ? 0 : 1;
         const int f2 = s_fock[v2] >= 0 ? 0 : 1;
         int kind = 0, accepted, khop = -1;
@@ -243,7 +350,7 @@ __global__ void __launch_bounds__(kTrThreads, 1) k_walk_trans_res(DevJob J, uint
             cx<T> m11u = {T(0), T(0)}, m11d = {T(0), T(0)}, gc = {T(0), T(0)};
             for (int f = tid; f < N0; f += NT) {
                 const cx<T> a = A0s[size_t(f) * N0 + cu];
-                const cx<T> c = phi_orb<T>(phase, cf0, Nk, Ns, L, upt, s_worb[f]);
+                const cx<T> c = phi_st(cf0, upt, s_worb[f]);
                 s_rowc[f] = a;
                 s_C[f] = c;
                 cmac(m11u, a, c);
@@ -255,7 +362,7 @@ __global__ void __launch_bounds__(kTrThreads, 1) k_walk_trans_res(DevJob J, uint
                 const cx<T> v = {__uint_as_float(r2[0]), __uint_as_float(r2[1])};
                 if (g) {
                     if (lf < N1) {
-                        const cx<T> c = phi_orb<T>(phase, cf1, Nk, Ns, L, dnt, s_worb[Nmax + lf]);
+                        const cx<T> c = phi_st(cf1, dnt, s_worb[Nmax + lf]);
                         s_rowc[Nmax + lf] = v;
                         s_C[Nmax + lf] = c;
                         cmac(m11d, v, c);
@@ -303,12 +410,12 @@ __global__ void __launch_bounds__(kTrThreads, 1) k_walk_trans_res(DevJob J, uint
                 if (N0 > 128 && lf < Nexc) cmac(acc, s_g128[lf], s_C[128]);
                 if (lf < Nexc) s_zp[lf] = acc;
             } else if (lf < Nexc) {
-                s_phk[lf] = phi_orb<T>(phase, cf0, Nk, Ns, L, upt, s_exu[lf]);
+                s_phk[lf] = phi_st(cf0, upt, s_exu[lf]);
             }
             __syncthreads();
             // Phase 3: per-state ratios, their sum and the first arg-max.
             const cx<T> M12 = s_rowc[r0];
-            const cx<T> gcd = gC - phi_orb<T>(phase, cf1, Nk, Ns, L, dnt, hcur);
+            const cx<T> gcd = gC - phi_st(cf1, dnt, hcur);
             T wsum = T(0), wbest = T(-1);
             int kbest = Nexc;
             for (int k = tid; k < Nexc; k += NT) {
@@ -350,7 +457,7 @@ __global__ void __launch_bounds__(kTrThreads, 1) k_walk_trans_res(DevJob J, uint
             khop = kbest;
             ratio = wsum / T(sigma);
             if (!isfinite(ratio) || khop >= Nexc) { status = GV_ERR_NAN; break; }
-            accepted = ratio > T(1) ? 1 : (Accept<T>::uniform(m4) < ratio);
+            accepted = ratio > T(1) ? 1 : (b_u4[rs_cur * kTrBatch + bi] < ratio);
             if (!accepted) {
                 ++c_rej;
             } else {
@@ -363,7 +470,7 @@ __global__ void __launch_bounds__(kTrThreads, 1) k_walk_trans_res(DevJob J, uint
                 // copied to shared memory by their lanes.
                 for (int k = tid; k < Nexc; k += NT) {
                     const cx<T> Z = s_zp[k];
-                    const cx<T> dk = s_phk[k] - phi_orb<T>(phase, cf0, Nk, Ns, L, upf, s_exu[k]);
+                    const cx<T> dk = s_phk[k] - phi_st(cf0, upf, s_exu[k]);
                     s_dk[k] = dk;
                     s_ak[k] = Z + dk * M11u - s_phk[k];
                     s_bk[k] = s_Y[k] + dk * M12;
@@ -398,11 +505,11 @@ __global__ void __launch_bounds__(kTrThreads, 1) k_walk_trans_res(DevJob J, uint
                 cx<T> Mui[4], Mdi[4];
                 cx<T> delu = {T(0), T(0)}, deld = {T(0), T(0)}, Dh;
                 {
-                    const cx<T> phc_t = phi_orb<T>(phase, cf1, Nk, Ns, L, dnt, hcur);
-                    Dh = phc_t - phi_orb<T>(phase, cf1, Nk, Ns, L, dnf, hcur);
+                    const cx<T> phc_t = phi_st(cf1, dnt, hcur);
+                    Dh = phc_t - phi_st(cf1, dnf, hcur);
                     if (row) {
                         cx<T> Mu[4], Md[4];
-                        delu = s_C[r0] - phi_orb<T>(phase, cf0, Nk, Ns, L, upf, ocur);
+                        delu = s_C[r0] - phi_st(cf0, upf, ocur);
                         const cx<T> Zk = s_zp[khop];
                         const cx<T> dkh = s_dk[khop];
                         const cx<T> raic = Zk + dkh * M11u, raier = s_Y[khop] + dkh * M12;
@@ -411,7 +518,7 @@ __global__ void __launch_bounds__(kTrThreads, 1) k_walk_trans_res(DevJob J, uint
                         Mu[3] = raier - delu * M12;
                         inv2(Mu, Mui);
                         const cx<T> M12d = s_rowc[Nmax + rp];
-                        deld = s_C[Nmax + rp] - phi_orb<T>(phase, cf1, Nk, Ns, L, dnf, s_exd[khop]);
+                        deld = s_C[Nmax + rp] - phi_st(cf1, dnf, s_exd[khop]);
                         const cx<T> raicd = gC + Dh * M11d, raierd = s_g[rp] + Dh * M12d;
                         Md[0] = M11d; Md[1] = M12d;
                         Md[2] = raicd - phc_t - deld * M11d;
@@ -549,7 +656,7 @@ __global__ void __launch_bounds__(kTrThreads, 1) k_walk_trans_res(DevJob J, uint
                 __syncthreads();   // the column pass is done with s_C, s_X, s_Yv, s_rowc
                 // g of the state after the move (its hole orbital).
                 {
-                    const cx<T> ah = gC + Dh * M11d - phi_orb<T>(phase, cf1, Nk, Ns, L, dnt, hcur);
+                    const cx<T> ah = gC + Dh * M11d - phi_st(cf1, dnt, hcur);
                     const cx<T> M12d = row ? s_rowc[Nmax + rp] : cx<T>{T(0), T(0)};
                     const cx<T> q0 = deld * M11d;
                     cx<T> q1 = deld * M12d;
@@ -582,11 +689,12 @@ __global__ void __launch_bounds__(kTrThreads, 1) k_walk_trans_res(DevJob J, uint
                         s_worb[r0] = int16_t(onew); s_wslot[onew] = int16_t(r0); s_wslot[ocur] = -1;
                         s_worb[Nmax + rp] = int16_t(hcur); s_wslot[Ns + hcur] = int16_t(rp); s_wslot[Ns + hnew] = -1;
                     }
-                    am = am * (to_d(rho_u) * to_d(rho_d));
-                    amp_normalise(am, ae);
+                    b_acc[2 * nacc] = rho_u;
+                    b_acc[2 * nacc + 1] = rho_d;
                 }
+                ++nacc;
                 if (row) { cur = khop; wsign *= hs; }
-                sigma = double(wsum) / double(Accept<T>::ratio(rho_u, rho_d));
+                sigma = double(wsum / Accept<T>::ratio(rho_u, rho_d));   // in FP32: only T(sigma) is used
                 ++c_acc;
                 ++since;
                 __syncthreads();
@@ -595,11 +703,16 @@ __global__ void __launch_bounds__(kTrThreads, 1) k_walk_trans_res(DevJob J, uint
         if (J.trace && w == J.trace_walker && tid == 0) {
             gv_trace t;
             t.v1 = v1; t.v2 = v2; t.kind = kind; t.accepted = accepted; t.khop = kind ? khop : -1; t.pad = 0;
-            t.ratio = double(ratio); t.u4 = u01(y[2], y[3]);
+            t.ratio = double(ratio); t.u4 = b_u4d[rs_cur * kTrBatch + bi];
             J.trace[s] = t;
         }
     }
-    __syncthreads();
+    // the row copies still in flight land before the block exits (bounded)
+    bool drained = true;
+    for (; nb_waited < nb_issued; ++nb_waited)
+        drained = mbar_wait(rbar0 + 8 * (nb_waited & 1), (nb_waited >> 1) & 1) && drained;
+    if (__syncthreads_or(!drained)) status = GV_ERR_TIMEOUT;
+    flush_amp();
     // write back: AiT0 from shared memory, GupT and AiT1 from TMEM, the rest
     for (int i = tid; i < N0 * N0; i += NT) A0[i] = A0s[i];
     if (g == 0) {
