@@ -165,6 +165,7 @@ struct DevJob {
                                // Aud (Ns*Ns real) in a 10*Ns*Ns-double buffer
     int32_t* ss_n;
     uint32_t* occ;             // 2*Ns*ceil(W/32) occupation bitsets (tensor-core StatSpinStruct)
+    float2* ss32;              // Ns*Ns FP32 staging sums of one tensor-core StatSpinStruct measurement
     double* track_sm;          // W*track_cap StagMagnTrack values
     double* track_lw;          // W*track_cap OverlapTrack log10 weights
     int32_t* track_n;          // W entries recorded

@@ -493,6 +493,12 @@ gv_status statspin_dispatch(gv_job* j, int mode = 1)
         }
         k_statspin_tc<<<std::min(j->W, j->n_sm), kTcThreads, lay.total, j->stream>>>(j->d, mode);
         GV_CK(cudaGetLastError());
+        if (mode & 1) {
+            k_fold_ss<<<j->n_sm, 256, 0, j->stream>>>(j->d);
+            GV_CK(cudaGetLastError());
+            ++j->last_launches;
+            ++j->total_launches;
+        }
         GV_CK(mark_end(j, slot));
         ++j->last_launches;
         ++j->total_launches;
@@ -1136,6 +1142,7 @@ gv_status gv_job_footprint(const gv_job_config* c, uint64_t* bytes)
     b += W * Nmax * Nmax * 16;               // FP64 re-inversion scratch
     b += 5 * Ns * Ns * 16;                   // StatSpinStruct sums
     b += 2 * Ns * ((W + 31) / 32) * 4;       // occupation bitsets
+    b += Ns * Ns * 8;                        // FP32 staging sums of a tensor-core StatSpinStruct measurement
     if (tr) {
         b += W * (N0 * Nexc + Nmax) * es;    // overlap rows GupT and g
         b += W * (2 * Ns + 2 * Nmax) * 2;    // wavefunction Fock state
@@ -1298,6 +1305,7 @@ gv_status gv_job_create(const gv_job_config* cfg, gv_job** out)
         (st = dalloc(j, &d.ss, size_t(5) * j->Ns * j->Ns * 2 * sizeof(double))) ||
         (st = dalloc(j, &d.ss_n, sizeof(int32_t))) ||
         (st = dalloc(j, &d.occ, sizeof(uint32_t) * 2 * j->Ns * ((j->W + 31) / 32))) ||
+        (st = dalloc(j, &d.ss32, sizeof(float2) * j->Ns * j->Ns)) ||
         (st = dalloc(j, &d.scratch64, scratch_walkers(j) * j->Nmax * j->Nmax * sizeof(cx<double>))))
         return fail(st);
     d.nbr = nbr; d.edges = reinterpret_cast<const int4*>(edg); d.phase64 = p64; d.phase32 = p32; d.coef64 = c64; d.coef32 = c32;
@@ -1385,6 +1393,7 @@ static gv_status reset_quantities(gv_job* j)
     GV_CK(cudaMemsetAsync(j->d.sm_n, 0, sizeof(int32_t) * j->W, j->stream));
     GV_CK(cudaMemsetAsync(j->d.ss, 0, sizeof(double) * 10 * j->Ns * j->Ns, j->stream));
     GV_CK(cudaMemsetAsync(j->d.ss_n, 0, sizeof(int32_t), j->stream));
+    GV_CK(cudaMemsetAsync(j->d.ss32, 0, sizeof(float2) * j->Ns * j->Ns, j->stream));
     if (exc(j))
         GV_CK(cudaMemsetAsync(j->d.pjx, 0, sizeof(cx<double>) * 2 * size_t(j->W) * j->ch.Nexc * j->ch.Nexc, j->stream));
     if (j->d.track_n) GV_CK(cudaMemsetAsync(j->d.track_n, 0, sizeof(int32_t) * j->W, j->stream));

@@ -623,7 +623,7 @@ __global__ void __launch_bounds__(NT) k_walk_long(DevJob J, uint64_t nsteps, int
 
 // Shared-memory pieces of the measurement and VirtUpdate kernels.
 struct LongMeasLayout {
-    size_t fock, part, wslot, worb, exu, exd, pre, coef, rowc, del, C, Z, pt, dd, S, a, hh, red, total;
+    size_t fock, part, wslot, worb, exu, exd, pre, coef, rowc, del, C, Z, pt, dd, S, a, hh, f32, red, total;
 };
 
 template <typename T, int NT>
@@ -650,6 +650,7 @@ __host__ __device__ inline LongMeasLayout long_meas_layout(int Ns, int Nmax, int
     l.S = al(sizeof(cx<double>) * Nexc);
     l.a = al(sizeof(cx<double>) * Nexc);
     l.hh = al(sizeof(cx<double>) * Nexc);
+    l.f32 = l.Z;   // FP32 factors of the H / O outer products (mixed form): over Z, pt, dd, dead by then
     l.red = al(sizeof(double) * 4 * (NT / 32) + 64);
     l.total = al(16);
     return l;
@@ -773,12 +774,43 @@ __global__ void __launch_bounds__(NT) k_measure_long(DevJob J, int mask)
         const double iw = 1.0 / wsum;
         cx<double>* H = J.pjx + size_t(w) * 2 * Nexc * Nexc;
         cx<double>* O = H + size_t(Nexc) * Nexc;
-        for (int idx = tid; idx < Nexc * Nexc; idx += NT) {
-            const int k1 = idx / Nexc, k2 = idx % Nexc;
-            const cx<double> ca = {s_a[k1].x, -s_a[k1].y};
-            const cx<double> hv = ca * s_hh[k2], ov = ca * s_a[k2];
-            H[idx].x += hv.x * iw; H[idx].y += hv.y * iw;
-            O[idx].x += ov.x * iw; O[idx].y += ov.y * iw;
+        // Mixed form: the outer products in FP32, widened exactly and summed in
+        // FP64 (as the transverse channel's measurement; FP64 products for a
+        // walker whose factors exceed 1e15)
+        bool narrow = false;
+        if constexpr (sizeof(T) == 4) {
+            cx<float>* s_caf = reinterpret_cast<cx<float>*>(smem + lay.f32);
+            cx<float>* s_hf = s_caf + Nexc;
+            cx<float>* s_af = s_hf + Nexc;
+            bool big = false;
+            for (int k = tid; k < Nexc; k += NT) {
+                const double m = fmax(fmax(fabs(s_a[k].x), fabs(s_a[k].y)), fmax(fabs(s_hh[k].x), fabs(s_hh[k].y)));
+                big = big || !(m <= 1e15) || !(fmax(fabs(s_a[k].x), fabs(s_a[k].y)) * iw <= 1e15);
+                s_caf[k] = cx<float>{float(s_a[k].x * iw), float(-s_a[k].y * iw)};
+                s_hf[k] = cx<float>{float(s_hh[k].x), float(s_hh[k].y)};
+                s_af[k] = cx<float>{float(s_a[k].x), float(s_a[k].y)};
+            }
+            narrow = !__syncthreads_or(big);
+        }
+        if (narrow) {
+            const cx<float>* s_caf = reinterpret_cast<const cx<float>*>(smem + lay.f32);
+            const cx<float>* s_hf = s_caf + Nexc;
+            const cx<float>* s_af = s_hf + Nexc;
+            for (int idx = tid; idx < Nexc * Nexc; idx += NT) {
+                const int k1 = idx / Nexc, k2 = idx % Nexc;
+                const cx<float> ca = s_caf[k1];
+                const cx<float> hv = cmul_rn(ca, s_hf[k2]), ov = cmul_rn(ca, s_af[k2]);
+                H[idx].x += f32_to_f64(hv.x); H[idx].y += f32_to_f64(hv.y);
+                O[idx].x += f32_to_f64(ov.x); O[idx].y += f32_to_f64(ov.y);
+            }
+        } else {
+            for (int idx = tid; idx < Nexc * Nexc; idx += NT) {
+                const int k1 = idx / Nexc, k2 = idx % Nexc;
+                const cx<double> ca = {s_a[k1].x, -s_a[k1].y};
+                const cx<double> hv = ca * s_hh[k2], ov = ca * s_a[k2];
+                H[idx].x += hv.x * iw; H[idx].y += hv.y * iw;
+                O[idx].x += ov.x * iw; O[idx].y += ov.y * iw;
+            }
         }
         if (tid == 0) J.pj_n[w] += 1;
         __syncthreads();

@@ -288,11 +288,15 @@ __device__ __forceinline__ void tmem_ld16(uint32_t taddr, uint32_t* r)
 // The 48 MMAs of one K chunk into the accumulator pair at column dcol:
 // Re += Ar Br + Ai (-Bi), Im += Ar Bi + Ai Br, each real product as three
 // split-precision terms, K = 8 per instruction (32 bytes along the row).
+// With neg_bit the -Bi terms read the Bi tiles through the instruction
+// descriptor's negate-B bit (bit 14), so the negated tiles need not be built.
 __device__ __forceinline__ void tc_issue_chunk(uint32_t tbase, uint32_t dcol, uint32_t sbase, const TcLayout& lay,
-                                               uint32_t idesc, bool first)
+                                               uint32_t idesc, bool first, bool neg_bit = false)
 {
     enum { RH = 0, RL = 1, IH = 2, IL = 3, NH = 4, NL = 5 };
-    const int re_terms[6][2] = {{RH, RH}, {RH, RL}, {RL, RH}, {IH, NH}, {IH, NL}, {IL, NH}};
+    const int re_terms[6][2] = {{RH, RH}, {RH, RL}, {RL, RH}, {IH, neg_bit ? IH : NH}, {IH, neg_bit ? IL : NL},
+                                {IL, neg_bit ? IH : NH}};
+    const uint32_t idesc_neg = idesc | (neg_bit ? (1u << 14) : 0u);
     const int im_terms[6][2] = {{RH, IH}, {RH, IL}, {RL, IH}, {IH, RH}, {IH, RL}, {IL, RH}};
 #pragma unroll
     for (int kk = 0; kk < 4; ++kk) {
@@ -300,7 +304,7 @@ __device__ __forceinline__ void tc_issue_chunk(uint32_t tbase, uint32_t dcol, ui
         for (int t = 0; t < 6; ++t) {
             const uint32_t acc = (first && kk == 0 && t == 0) ? 0u : 1u;
             tc_mma(tbase + dcol, tc_desc(sbase + uint32_t(lay.a[re_terms[t][0]]) + 32 * kk),
-                   tc_desc(sbase + uint32_t(lay.b[re_terms[t][1]]) + 32 * kk), idesc, acc);
+                   tc_desc(sbase + uint32_t(lay.b[re_terms[t][1]]) + 32 * kk), t >= 3 ? idesc_neg : idesc, acc);
             tc_mma(tbase + dcol + 128, tc_desc(sbase + uint32_t(lay.a[im_terms[t][0]]) + 32 * kk),
                    tc_desc(sbase + uint32_t(lay.b[im_terms[t][1]]) + 32 * kk), idesc, acc);
         }
@@ -327,6 +331,21 @@ __device__ __forceinline__ int tc_next_walker(const DevJob& J, int w)
     return -1;
 }
 
+// The FP32 staging sums of one StatSpinStruct measurement (vector atomics of
+// k_statspin_tc) into the FP64 job-wide sums T, and back to zero.
+__global__ void k_fold_ss(DevJob J)
+{
+    const size_t n = size_t(J.Ns) * J.Ns;
+    for (size_t i = size_t(blockIdx.x) * blockDim.x + threadIdx.x; i < n; i += size_t(gridDim.x) * blockDim.x) {
+        const float2 v = J.ss32[i];
+        if (v.x != 0.f || v.y != 0.f) {
+            J.ss[2 * i] += f32_to_f64(v.x);
+            J.ss[2 * i + 1] += f32_to_f64(v.y);
+            J.ss32[i] = make_float2(0.f, 0.f);
+        }
+    }
+}
+
 // mode bit 0: StatSpinStruct pair sums (StatSpinStruct.cpp:16-135); bit 1:
 // ProjHeis (ProjHeis.cpp:40-158) from the same products: the pairs whose up
 // and down sites are nearest neighbours are the antiparallel bonds, and with
@@ -347,7 +366,6 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_statspin_tc(DevJob J, int mod
     uint32_t* s_tbase = reinterpret_cast<uint32_t*>(base + lay.tbase);
     double* s_red = reinterpret_cast<double*>(base + lay.red);
     const uint32_t bar = smem_addr(s_bar);
-    double* T = J.ss;
 
     if (warp == 0) tmem_alloc(s_tbase, 512);
     if (tid == 0) {
@@ -409,17 +427,17 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_statspin_tc(DevJob J, int mod
             first = false;
             if (gm == 0) {   // G_up: A = AiT_up^T (rows c), B = Phi_up at the down sites (rows q)
                 tc_store_inverse(base, lay.a, 4, R, kTcM);
-                tc_store_phi(base, lay.b, 6, R, sc, st + kTcM, N, L, Nt, kc);
+                tc_store_phi(base, lay.b, 4, R, sc, st + kTcM, N, L, Nt, kc);
             } else {         // G_dn^T: A = Phi_dn at the up sites (rows c), B = AiT_dn^T (rows q)
                 tc_store_phi(base, lay.a, 4, R, sc + 2 * N, st, N, L, kTcM, kc);
-                tc_store_inverse(base, lay.b, 6, R, Nt);
+                tc_store_inverse(base, lay.b, 4, R, Nt);
             }
             asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
             tmem_fence_before();
             __syncthreads();
             if (tid == 0) {
                 tmem_fence_after();
-                tc_issue_chunk(tbase, uint32_t(256 * gm), sbase, lay, idesc, kc == 0);
+                tc_issue_chunk(tbase, uint32_t(256 * gm), sbase, lay, idesc, kc == 0, true);
                 tc_commit(bar);
             }
             if (step + 1 < 2 * KC) {
@@ -471,11 +489,8 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_statspin_tc(DevJob J, int mod
                         const cx<float> gd = {__uint_as_float(r[32 + t]), __uint_as_float(r[48 + t])};
                         const cx<float> v = cmul_rn(gu, gd);
                         const int sj = st[kTcM + q];
-                        if (mode & 1) {
-                            const size_t ij = size_t(si) * Ns + sj;
-                            atomicAdd(&T[2 * ij], f32_to_f64(v.x));
-                            atomicAdd(&T[2 * ij + 1], f32_to_f64(v.y));
-                        }
+                        if (mode & 1)   // FP32 staging sums, folded into the FP64 sums after the launch
+                            atomicAdd(J.ss32 + size_t(si) * Ns + sj, make_float2(v.x, v.y));
                         if ((mode & 2) && (sj == nb[0] || sj == nb[1] || sj == nb[2] || sj == nb[3])) {
                             eb.x += f32_to_f64(v.x);
                             eb.y += f32_to_f64(v.y);

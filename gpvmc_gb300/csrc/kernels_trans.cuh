@@ -594,7 +594,7 @@ __global__ void __launch_bounds__(NT, 2) k_walk_trans(DevJob J, uint64_t nsteps,
 constexpr int kMeasTile = 8;
 
 struct MeasLayout {
-    size_t fock, part, wslot, worb, nbr, exu, exd, coef, rq, h, Y, g, gcs, Ct, arow, bond, S, a, hh, red, total;
+    size_t fock, part, wslot, worb, nbr, exu, exd, coef, rq, h, Y, g, gcs, Ct, arow, bond, S, a, hh, f32, red, total;
 };
 
 template <typename T, int NT>
@@ -623,6 +623,7 @@ __host__ __device__ inline MeasLayout meas_layout(int Ns, int Nmax, int Nexc)
     l.S = al(sizeof(cx<double>) * Nexc);
     l.a = al(sizeof(cx<double>) * Nexc);
     l.hh = al(sizeof(cx<double>) * Nexc);
+    l.f32 = al(sizeof(cx<float>) * 3 * Nexc);   // FP32 factors of the H / O outer products (mixed form)
     l.red = al(sizeof(double) * 4 * (NT / 32) + 16);
     l.total = al(16);
     return l;
@@ -858,12 +859,46 @@ __global__ void __launch_bounds__(NT) k_measure_trans(DevJob J, int mask, const 
         const double iw = 1.0 / wsum;
         cx<double>* H = J.pjx + size_t(w) * 2 * Nexc * Nexc;
         cx<double>* O = H + size_t(Nexc) * Nexc;
-        for (int idx = tid; idx < Nexc * Nexc; idx += NT) {
-            const int k1 = idx / Nexc, k2 = idx % Nexc;
-            const cx<double> ca = {s_a[k1].x, -s_a[k1].y};
-            const cx<double> hv = ca * s_hh[k2], ov = ca * s_a[k2];
-            H[idx].x += hv.x * iw; H[idx].y += hv.y * iw;
-            O[idx].x += ov.x * iw; O[idx].y += ov.y * iw;
+        bool narrow = false;
+        if constexpr (sizeof(T) == 4) {
+            // Mixed form: the Nexc^2 outer products in FP32 (their factors come
+            // from FP32 ratios; conj(a_k1) / sum|a|^2 rounded once per state),
+            // widened exactly and summed into the FP64 sums: four FP64 adds per
+            // entry instead of sixteen FP64 operations on GB300's narrow FP64
+            // pipe.  A walker whose factors could take a product near the FP32
+            // range (any |factor| > 1e15) keeps the FP64 products.
+            cx<float>* s_caf = reinterpret_cast<cx<float>*>(smem + lay.f32);
+            cx<float>* s_hf = s_caf + Nexc;
+            cx<float>* s_af = s_hf + Nexc;
+            bool big = false;
+            for (int k = tid; k < Nexc; k += NT) {
+                const double m = fmax(fmax(fabs(s_a[k].x), fabs(s_a[k].y)), fmax(fabs(s_hh[k].x), fabs(s_hh[k].y)));
+                big = big || !(m <= 1e15) || !(fmax(fabs(s_a[k].x), fabs(s_a[k].y)) * iw <= 1e15);
+                s_caf[k] = cx<float>{float(s_a[k].x * iw), float(-s_a[k].y * iw)};
+                s_hf[k] = cx<float>{float(s_hh[k].x), float(s_hh[k].y)};
+                s_af[k] = cx<float>{float(s_a[k].x), float(s_a[k].y)};
+            }
+            narrow = !__syncthreads_or(big);
+        }
+        if (narrow) {
+            const cx<float>* s_caf = reinterpret_cast<const cx<float>*>(smem + lay.f32);
+            const cx<float>* s_hf = s_caf + Nexc;
+            const cx<float>* s_af = s_hf + Nexc;
+            for (int idx = tid; idx < Nexc * Nexc; idx += NT) {
+                const int k1 = idx / Nexc, k2 = idx % Nexc;
+                const cx<float> ca = s_caf[k1];
+                const cx<float> hv = cmul_rn(ca, s_hf[k2]), ov = cmul_rn(ca, s_af[k2]);
+                H[idx].x += f32_to_f64(hv.x); H[idx].y += f32_to_f64(hv.y);
+                O[idx].x += f32_to_f64(ov.x); O[idx].y += f32_to_f64(ov.y);
+            }
+        } else {
+            for (int idx = tid; idx < Nexc * Nexc; idx += NT) {
+                const int k1 = idx / Nexc, k2 = idx % Nexc;
+                const cx<double> ca = {s_a[k1].x, -s_a[k1].y};
+                const cx<double> hv = ca * s_hh[k2], ov = ca * s_a[k2];
+                H[idx].x += hv.x * iw; H[idx].y += hv.y * iw;
+                O[idx].x += ov.x * iw; O[idx].y += ov.y * iw;
+            }
         }
         if (tid == 0) J.pj_n[w] += 1;
         __syncthreads();

@@ -138,8 +138,9 @@ def test_bounded_wait_gives_up_with_a_status(engine, oracle):
     ref = _mixed(engine, L, W, 3)
     ref.init_walkers(cfg)
     want, _ = _measure(ref, oracle)
-    # the job-wide sums are FP64 atomics over walkers: equal up to summation order
-    assert np.abs(ok - want).max() <= 1e-12 * np.abs(want).max()
+    # the job-wide sums go through FP32 staging atomics over walkers (folded into
+    # FP64 after each measurement): equal up to FP32 summation order
+    assert np.abs(ok - want).max() <= 1e-6 * np.abs(want).max()
 
 
 @pytest.mark.parametrize("L,W", [(8, 24), (16, 40)])
