@@ -152,3 +152,36 @@ def test_double_float_drift_check_matches_fp64(engine):
     assert (n > 0).all()
     assert (seen <= full * (1 + 1e-6) + 1e-12).all()
     assert np.median(seen / full) > 0.05
+
+
+@pytest.mark.parametrize("channel", ["gs", "trans"])
+def test_bulk_copy_waits_are_bounded(engine, channel):
+    """The on-chip walks wait for their bulk (TMA) copies -- the inverses'
+    staging tiles, the batches' phase rows -- on mbarriers with the job's poll
+    budget.  With a budget of zero every walker gives up at its first wait and
+    reports GV_ERR_TIMEOUT: no hang and no fault (the copies in flight land
+    before the block exits), no step taken, and an inverse that was not fully
+    loaded is not written back.  The job then walks normally again."""
+    L, W = 8, 12
+    if channel == "gs":
+        job = _job(engine, L, W, 5)
+    else:
+        job = engine.Job(engine.StagFluxTransExciton(L, PHI, 0.1, q=(4, 4)), walkers=W, seed=5, precision="mixed",
+                         reinv_every=128, deferred_reinversion=True)
+    job.init_walkers()
+    job.walk(L * L, 0)
+    cfg, counts = job.config(), job.counts()
+    inv = [job.inverse(w, 0) for w in (0, W - 1)]
+    job.set_wait_limit(0)
+    with pytest.raises(engine.GvError) as err:
+        job.walk(L * L, 0)
+    assert err.value.status == 6
+    assert (job.status() == 6).all()
+    assert np.array_equal(job.config(), cfg) and np.array_equal(job.counts(), counts)
+    for w, a in zip((0, W - 1), inv):
+        assert np.array_equal(job.inverse(w, 0), a)
+    job.set_wait_limit(-1)
+    job.init_walkers(cfg)   # clears the statuses, fresh FP64 inverses
+    job.walk(L * L, 0)
+    assert (job.status() == 0).all()
+    assert (job.counts()[:, 0] == L * L).all()   # the counters restart with the walkers
