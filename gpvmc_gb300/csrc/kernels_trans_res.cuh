@@ -577,6 +577,37 @@ __global__ void __launch_bounds__(kTrThreads, 1) k_walk_trans_res(DevJob J, uint
                         A0s[size_t(f) * N0 + 128] = a;
                     }
                 }
+                // GupT[f][k] += d_k row_c[f] - a_k X[f] - b_k Y[f] along lane k's row, 32
+                // Slater rows per chunk; either warpgroup can reach every TMEM lane
+                // (a warp's lane quarter is warp % 4), so the chunks are shared out
+                // to balance the stage: warpgroup 0 also rewrites AiT0, warpgroup 1
+                // AiT1
+                const bool gok = lf < Nexc;
+                const cx<T> gdk = gok ? s_dk[lf] : cx<T>{T(0), T(0)};
+                const cx<T> gna = gok ? cneg(s_ak[lf]) : cx<T>{T(0), T(0)};
+                const cx<T> gnb = (gok && row) ? cneg(s_bk[lf]) : cx<T>{T(0), T(0)};
+                // lanes past Nexc have zero coefficients and are never read
+                auto gupt_chunks = [&](int c0, int c1) {
+                    for (int c = c0; c < c1; ++c) {
+                        uint32_t r[64];
+                        tmem_ld64(tl + 64 * c, r);
+                        tmem_wait_ld(r);
+                        const bool full = 32 * c + 32 <= N0;
+#pragma unroll
+                        for (int j = 0; j < 32; ++j) {
+                            const int f = 32 * c + j;
+                            if (full || f < N0) {
+                                cx<T> v = {__uint_as_float(r[2 * j]), __uint_as_float(r[2 * j + 1])};
+                                cmac(v, gdk, s_rowc[f]);
+                                cmac(v, gna, s_X[f]);
+                                cmac(v, gnb, s_Yv[f]);   // gnb = 0 without a row change
+                                r[2 * j] = __float_as_uint(v.x);
+                                r[2 * j + 1] = __float_as_uint(v.y);
+                            }
+                        }
+                        tmem_st64(tl + 64 * c, r);
+                    }
+                };
                 if (g) {
                     // AiT1 in TMEM: (A^-1 C1)_p summed over the lanes f (butterfly per
                     // warp, the four warps in shared memory), then every lane updates
@@ -618,37 +649,14 @@ __global__ void __launch_bounds__(kTrThreads, 1) k_walk_trans_res(DevJob J, uint
                         }
                         tmem_st64(tl + kA1Col + 64 * c, r);
                     }
+                    gupt_chunks(2, 4);
                 } else {
-                    // GupT[f][k] += d_k row_c[f] - a_k X[f] - b_k Y[f] along lane k's row
-                    const bool ok = lf < Nexc;
-                    const cx<T> dk = ok ? s_dk[lf] : cx<T>{T(0), T(0)};
-                    const cx<T> na = ok ? cneg(s_ak[lf]) : cx<T>{T(0), T(0)};
-                    const cx<T> nb = (ok && row) ? cneg(s_bk[lf]) : cx<T>{T(0), T(0)};
-                    // lanes past Nexc have zero coefficients and are never read
-                    for (int c = 0; c < 4; ++c) {
-                        uint32_t r[64];
-                        tmem_ld64(tl + 64 * c, r);
-                        tmem_wait_ld(r);
-                        const bool full = 32 * c + 32 <= N0;
-#pragma unroll
-                        for (int j = 0; j < 32; ++j) {
-                            const int f = 32 * c + j;
-                            if (full || f < N0) {
-                                cx<T> v = {__uint_as_float(r[2 * j]), __uint_as_float(r[2 * j + 1])};
-                                cmac(v, dk, s_rowc[f]);
-                                cmac(v, na, s_X[f]);
-                                cmac(v, nb, s_Yv[f]);   // nb = 0 without a row change
-                                r[2 * j] = __float_as_uint(v.x);
-                                r[2 * j + 1] = __float_as_uint(v.y);
-                            }
-                        }
-                        tmem_st64(tl + 64 * c, r);
-                    }
-                    if (N0 > 128 && ok) {
+                    gupt_chunks(0, 2);
+                    if (N0 > 128 && gok) {
                         cx<T> v = s_g128[lf];
-                        cmac(v, dk, s_rowc[128]);
-                        cmac(v, na, s_X[128]);
-                        if (row) cmac(v, nb, s_Yv[128]);
+                        cmac(v, gdk, s_rowc[128]);
+                        cmac(v, gna, s_X[128]);
+                        if (row) cmac(v, gnb, s_Yv[128]);
                         s_g128[lf] = v;
                     }
                 }
