@@ -565,14 +565,15 @@ def run_long(g, sweeps, fp64_sweeps):
             j.set_measurements(1)
             j.init_walkers()
             jobs.append(j)
-        for j in jobs:
-            j.walk(SWEEP, 0, sync=False)
+        for _ in range(THERM_SWEEPS):   # thermalised as the headline walk, both arms alike
+            for j in jobs:
+                j.walk(SWEEP, 0, sync=False)
         for j in jobs:
             j.synchronize()
         t0 = time.perf_counter()
         for _ in range(n):
             for j in jobs:
-                j.walk(SWEEP, 0, sync=False)
+                j.walk(SWEEP, SWEEP, sync=False)   # ProjHeis H / O once per sweep
         for j in jobs:
             j.synchronize()
         wall = time.perf_counter() - t0

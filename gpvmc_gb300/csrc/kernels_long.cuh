@@ -256,9 +256,30 @@ __host__ __device__ inline LongLayout long_layout(int Ns, int Nmax, int Nexc, bo
     return l;
 }
 
+// phi_o(t) and phi_o(t) - phi_o(s) of every orbital of both flavours, for the
+// exchange moving flavour 0 from s0 to t0 and flavour 1 from t0 to s0
+template <typename T, int NT>
+__device__ __forceinline__ void long_stage_phi(const DevJob& J, int s0, int t0, const cx<T>* s_coef, cx<T>* s_pt,
+                                               cx<T>* s_dd)
+{
+    const int tid = threadIdx.x;
+    const int Ns = J.Ns, Nk = J.Nk, L = J.L;
+    const cx<T>* phase = Tab<T>::phase(J);
+    for (int idx = tid; idx < 2 * Ns; idx += NT) {
+        const int fl = idx / Ns, o = idx % Ns;
+        const int s = fl ? t0 : s0, t = fl ? s0 : t0;
+        const cx<T>* cf = s_coef + fl * 2 * Ns;
+        const cx<T> pt = phi_orb<T>(phase, cf, Nk, Ns, L, t, o);
+        s_pt[idx] = pt;
+        s_dd[idx] = pt - phi_orb<T>(phase, cf, Nk, Ns, L, s, o);
+    }
+    __syncthreads();
+}
+
 // Stage one exchange for both flavours: flavour 0 moves from s0 to t0 and
 // flavour 1 from t0 to s0 (rowc, the new column C, delta, phi(t), d, M11,
-// and Z over all orbitals).  Ends with the CTA synchronised and M11 of both flavours in m11[].
+// and Z over all orbitals; s_Z == nullptr: Z already staged by the caller).
+// Ends with the CTA synchronised and M11 of both flavours in m11[].
 template <typename T, int NT>
 __device__ __forceinline__ void long_stage(const DevJob& J, int w, int s0, int t0, const int16_t* s_fock,
                                            const int16_t* s_worb, const cx<T>* s_coef, cx<T>* s_rowc, cx<T>* s_del,
@@ -294,6 +315,10 @@ __device__ __forceinline__ void long_stage(const DevJob& J, int w, int s0, int t
         for (int q = 0; q < NW; ++q) { m.x += T(s_red[q * 4 + 2 * i]); m.y += T(s_red[q * 4 + 2 * i + 1]); }
         m11[i] = m;
     }
+    if (s_Z == nullptr) {   // Z staged by the caller (batched bonds): the orbital rows only
+        long_stage_phi<T, NT>(J, s0, t0, s_coef, s_pt, s_dd);
+        return;
+    }
     // Z_o = sum_f R[f][o] C[f] for every orbital of both flavours
     for (int idx = tid; idx < 2 * Ns; idx += NT) {
         const int fl = idx / Ns, o = idx % Ns;
@@ -312,15 +337,7 @@ __device__ __forceinline__ void long_stage(const DevJob& J, int w, int s0, int t
         s_Z[idx] = z;
     }
     __syncthreads();
-    for (int idx = tid; idx < 2 * Ns; idx += NT) {
-        const int fl = idx / Ns, o = idx % Ns;
-        const int s = fl ? t0 : s0, t = fl ? s0 : t0;
-        const cx<T>* cf = s_coef + fl * 2 * Ns;
-        const cx<T> pt = phi_orb<T>(phase, cf, Nk, Ns, L, t, o);
-        s_pt[idx] = pt;
-        s_dd[idx] = pt - phi_orb<T>(phase, cf, Nk, Ns, L, s, o);
-    }
-    __syncthreads();
+    long_stage_phi<T, NT>(J, s0, t0, s_coef, s_pt, s_dd);
 }
 
 // ------------------------------------------------------------------------
@@ -622,8 +639,10 @@ __global__ void __launch_bounds__(NT) k_walk_long(DevJob J, uint64_t nsteps, int
 }
 
 // Shared-memory pieces of the measurement and VirtUpdate kernels.
+constexpr int kLongBonds = 8;   // bonds whose overlap sums Z share one pass over R in a measurement
+
 struct LongMeasLayout {
-    size_t fock, part, wslot, worb, exu, exd, pre, coef, rowc, del, C, Z, pt, dd, S, a, hh, f32, red, total;
+    size_t fock, part, wslot, worb, exu, exd, pre, coef, rowc, del, C, Z, pt, dd, S, a, hh, f32, bl, Cb, Zb, red, total;
 };
 
 template <typename T, int NT>
@@ -651,6 +670,9 @@ __host__ __device__ inline LongMeasLayout long_meas_layout(int Ns, int Nmax, int
     l.a = al(sizeof(cx<double>) * Nexc);
     l.hh = al(sizeof(cx<double>) * Nexc);
     l.f32 = l.Z;   // FP32 factors of the H / O outer products (mixed form): over Z, pt, dd, dead by then
+    l.bl = al(sizeof(int32_t) * 2 * Ns);                    // antiparallel bonds (s0 | t0 << 16), creation order
+    l.Cb = al(c * kLongBonds * 2 * Nmax);                   // [bond][fl][f] new columns of a batch of bonds
+    l.Zb = al(c * kLongBonds * 2 * Ns);                     // [bond][fl][o] their overlap sums
     l.red = al(sizeof(double) * 4 * (NT / 32) + 64);
     l.total = al(16);
     return l;
@@ -740,23 +762,94 @@ __global__ void __launch_bounds__(NT) k_measure_long(DevJob J, int mask)
         }
         wsum = block_sum_d<NT>(wsum, s_red);
         D[0].moved = D[1].moved = true;
+        // The antiparallel bonds in creation order (SquareLattice.cpp:9-28),
+        // compacted: each warp ballots its 32 bonds, the warps' counts are
+        // prefix-summed in shared memory.
+        int32_t* s_bl = reinterpret_cast<int32_t*>(smem + lay.bl);
+        int* s_cnt = reinterpret_cast<int*>(s_red);
         int nanti = 0;
-        for (int e = 0; e < 2 * Ns; ++e) {   // the bonds in creation order (SquareLattice.cpp:9-28)
-            const int4 E = J.edges[e];
-            const bool ua = s_fock[E.x] >= 0, ub = s_fock[E.y] >= 0;
-            if (ua == ub) continue;
-            ++nanti;
-            const int s0 = ua ? E.x : E.y, t0 = ua ? E.y : E.x;
-            cx<T> m11[2];
-            long_stage<T, NT>(J, w, s0, t0, s_fock, s_worb, s_coef, s_rowc, s_del, s_C, s_Z, s_pt, s_dd, s_red, m11);
-            D[0].M11 = m11[0];
-            D[1].M11 = m11[1];
-            for (int k = tid; k < Nexc; k += NT) {
-                const cx<double> q = to_d(long_state_ratio<T>(D, cur, k, s_exu, s_exd, s_pre, Ns, nullptr));
-                s_S[k].x += q.x;
-                s_S[k].y += q.y;
+        for (int e0 = 0; e0 < 2 * Ns; e0 += NT) {
+            const int e = e0 + tid;
+            bool anti = false;
+            int code = 0;
+            if (e < 2 * Ns) {
+                const int4 E = J.edges[e];
+                const bool ua = s_fock[E.x] >= 0, ub = s_fock[E.y] >= 0;
+                anti = ua != ub;
+                code = ua ? (E.x | (E.y << 16)) : (E.y | (E.x << 16));   // s0 | t0 << 16
             }
-            __syncthreads();   // the next bond restages
+            const unsigned bal = __ballot_sync(0xffffffffu, anti);
+            if (lane == 0) s_cnt[warp] = __popc(bal);
+            __syncthreads();
+            int off = nanti, tot = 0;
+            for (int q = 0; q < NW; ++q) {
+                if (q < warp) off += s_cnt[q];
+                tot += s_cnt[q];
+            }
+            if (anti) s_bl[off + __popc(bal & ((1u << lane) - 1u))] = code;
+            nanti += tot;
+            __syncthreads();
+        }
+        cx<T>* s_Cb = reinterpret_cast<cx<T>*>(smem + lay.Cb);
+        cx<T>* s_Zb = reinterpret_cast<cx<T>*>(smem + lay.Zb);
+        const int N = J.N[0], Nk = J.Nk;
+        const cx<T>* phase = Tab<T>::phase(J);
+        for (int b0 = 0; b0 < nanti; b0 += kLongBonds) {
+            const int nb = nanti - b0 < kLongBonds ? nanti - b0 : kLongBonds;
+            // the new columns C of the batch's bonds (as long_stage forms them)
+            for (int idx = tid; idx < nb * 2 * N; idx += NT) {
+                const int j = idx / (2 * N), fl = (idx / N) & 1, f = idx % N;
+                const int code = s_bl[b0 + j], s0 = code & 0xFFFF, t0 = code >> 16;
+                const int t = fl ? s0 : t0;
+                s_Cb[(j * 2 + fl) * Nmax + f] = phi_orb<T>(phase, s_coef + fl * 2 * Ns, Nk, Ns, L, t, s_worb[fl * Nmax + f]);
+            }
+            __syncthreads();
+            // Z_o = sum_f R[f][o] C[f] of every bond of the batch in one pass over R
+            // (each sum in the order long_stage takes it)
+            for (int idx = tid; idx < 2 * Ns; idx += NT) {
+                const int fl = idx / Ns, o = idx % Ns;
+                const cx<T>* R = D[fl].R;
+                cx<T> z[kLongBonds];
+#pragma unroll
+                for (int j = 0; j < kLongBonds; ++j) z[j] = cx<T>{T(0), T(0)};
+                int f = 0;
+                for (; f + 4 <= N; f += 4) {
+                    cx<T> r[4];
+#pragma unroll
+                    for (int q = 0; q < 4; ++q) r[q] = R[size_t(f + q) * Ns + o];
+#pragma unroll
+                    for (int q = 0; q < 4; ++q)
+#pragma unroll
+                        for (int j = 0; j < kLongBonds; ++j)
+                            if (j < nb) cmac(z[j], r[q], s_Cb[(j * 2 + fl) * Nmax + f + q]);
+                }
+                for (; f < N; ++f) {
+                    const cx<T> r = R[size_t(f) * Ns + o];
+#pragma unroll
+                    for (int j = 0; j < kLongBonds; ++j)
+                        if (j < nb) cmac(z[j], r, s_Cb[(j * 2 + fl) * Nmax + f]);
+                }
+#pragma unroll
+                for (int j = 0; j < kLongBonds; ++j)
+                    if (j < nb) s_Zb[j * 2 * Ns + idx] = z[j];
+            }
+            __syncthreads();
+            for (int j = 0; j < nb; ++j) {
+                const int code = s_bl[b0 + j], s0 = code & 0xFFFF, t0 = code >> 16;
+                cx<T> m11[2];
+                long_stage<T, NT>(J, w, s0, t0, s_fock, s_worb, s_coef, s_rowc, s_del, s_C, nullptr, s_pt, s_dd, s_red,
+                                  m11);
+                D[0].M11 = m11[0];
+                D[1].M11 = m11[1];
+                D[0].Z = s_Zb + j * 2 * Ns;
+                D[1].Z = s_Zb + j * 2 * Ns + Ns;
+                for (int k = tid; k < Nexc; k += NT) {
+                    const cx<double> q = to_d(long_state_ratio<T>(D, cur, k, s_exu, s_exd, s_pre, Ns, nullptr));
+                    s_S[k].x += q.x;
+                    s_S[k].y += q.y;
+                }
+                __syncthreads();   // the next bond restages
+            }
         }
         const double npar = double(2 * Ns - nanti), na = double(nanti);
         for (int k = tid; k < Nexc; k += NT) {
