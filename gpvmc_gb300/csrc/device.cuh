@@ -132,6 +132,10 @@ __host__ __device__ __forceinline__ double uniform_at(uint64_t seed, uint32_t wa
     return (k & 1) ? u01(x[2], x[3]) : u01(x[0], x[1]);
 }
 
+// Exciton ProjHeis measurements of a mixed job summed in FP32 before one FP64
+// add per H / O entry (a block of this many measurements per walker).
+constexpr int kHoSlots = 32;
+
 // Everything a kernel needs about a job (device pointers, sizes).
 struct DevJob {
     int L, Ns, Nk, Nexc, W;
@@ -188,7 +192,12 @@ struct DevJob {
     void* gup;                 // W*N0*Nexc, GupT[f][k] = sum_p phi_{exc_up[k]}(x_p) (A0^-1)(p, f)
     void* gdn;                 // W*Nmax,    g[f] = sum_p phi_{exc_dn[cur]}(x_p) (A1^-1)(p, f)
     cx<double>* pjx;           // W*2*Nexc*Nexc ProjHeis H and O sums
-    cx<float>* zbuf;           // W*N1*Nexc tensor-core Z[d][k] = sum_f GupT[f][k] phi_f(d) (mixed, or null)
+    // Mixed exciton jobs: each measurement's FP32 factors (conj(a)/w, h, a; 3*Nexc
+    // each) wait in one of kHoSlots slots per walker and are folded into pjx as a
+    // block every kHoSlots measurements (null for FP64 jobs, which add at once).
+    cx<float>* pxs;            // W*kHoSlots*3*Nexc
+    int32_t* pxs_n;            // W: measurements waiting in pxs
+    cx<float>* zbuf;          // W*N1*Nexc tensor-core Z[d][k] = sum_f GupT[f][k] phi_f(d) (mixed, or null)
     int wait_limit;            // polls before a bounded mbarrier wait of the tensor-core kernels gives up
     // Single-walker stepping (gv_job_trystep / gv_job_step, LatticeStepper::trystep / step):
     // when forced_walker >= 0 the streaming walk kernels run that walker only, take the

@@ -946,6 +946,10 @@ std::vector<CkptSection> ckpt_sections(gv_job* j, bool inverses)
         s.push_back({d.wsign, W * sizeof(int32_t)});
         s.push_back({d.sigma, W * sizeof(double)});
         s.push_back({d.pjx, W * 2 * Nexc * Nexc * sizeof(cx<double>)});
+        if (d.pxs) {
+            s.push_back({d.pxs, W * kHoSlots * 3 * Nexc * sizeof(cx<float>)});
+            s.push_back({d.pxs_n, W * sizeof(int32_t)});
+        }
     }
     if (inverses) {
         const size_t es = j->cfg.precision == GV_PREC_FP64 ? sizeof(cx<double>) : sizeof(cx<float>);
@@ -1149,6 +1153,11 @@ gv_status gv_job_footprint(const gv_job_config* c, uint64_t* bytes)
         b += W * 2 * Nexc * Nexc * 16;       // ProjHeis H and O sums
         if (c->precision == GV_PREC_MIXED) b += W * N1 * Nexc * 8;   // tensor-core overlap rows
     }
+    if ((tr || lg) && c->precision != GV_PREC_FP64) {
+        b += W * (uint64_t(kHoSlots) * 3 * Nexc * 8 + 4);   // FP32 factors of measurements waiting for their block
+        const uint64_t per = 2 * Nexc * Nexc * 16;
+        b += std::max<uint64_t>(1, std::min<uint64_t>(W, (uint64_t(32) << 20) / per)) * per;   // read-out scratch
+    }
     if (lg) {
         b += W * 2 * Nmax * Ns * es;         // overlap table R of both flavours
         b += W * (2 * Ns + 2 * Nmax) * 2;    // wavefunction Fock state
@@ -1312,6 +1321,7 @@ gv_status gv_job_create(const gv_job_config* cfg, gv_job** out)
     d.Ai[0] = a0; d.Ai[1] = a1;
     d.worb = nullptr; d.wslot = nullptr; d.exc_up = nullptr; d.exc_dn = nullptr; d.cur = nullptr; d.wsign = nullptr;
     d.sigma = nullptr; d.gup = nullptr; d.gdn = nullptr; d.pjx = nullptr; d.zbuf = nullptr;
+    d.pxs = nullptr; d.pxs_n = nullptr;
     d.track_sm = nullptr; d.track_lw = nullptr; d.track_n = nullptr; d.track_cap = 0;
     if (exc(j)) {
         const int Nexc = j->ch.Nexc;
@@ -1330,6 +1340,10 @@ gv_status gv_job_create(const gv_job_config* cfg, gv_job** out)
             (st = dalloc(j, &d.pjx, size_t(j->W) * 2 * Nexc * Nexc * sizeof(cx<double>))))
             return fail(st);
         if (trans_z_tc_ok(j) && (st = dalloc(j, &d.zbuf, size_t(j->W) * j->N[1] * Nexc * sizeof(cx<float>))))
+            return fail(st);
+        if (j->cfg.precision != GV_PREC_FP64 &&
+            ((st = dalloc(j, &d.pxs, size_t(j->W) * kHoSlots * 3 * Nexc * sizeof(cx<float>))) ||
+             (st = dalloc(j, &d.pxs_n, size_t(j->W) * sizeof(int32_t)))))
             return fail(st);
         d.exc_up = eu; d.exc_dn = ed;
         if (copy_async(eu, j->exu.data(), Nexc * sizeof(int16_t), cudaMemcpyHostToDevice, j->stream) ||
@@ -1396,6 +1410,7 @@ static gv_status reset_quantities(gv_job* j)
     GV_CK(cudaMemsetAsync(j->d.ss32, 0, sizeof(float2) * j->Ns * j->Ns, j->stream));
     if (exc(j))
         GV_CK(cudaMemsetAsync(j->d.pjx, 0, sizeof(cx<double>) * 2 * size_t(j->W) * j->ch.Nexc * j->ch.Nexc, j->stream));
+    if (j->d.pxs_n) GV_CK(cudaMemsetAsync(j->d.pxs_n, 0, sizeof(int32_t) * j->W, j->stream));
     if (j->d.track_n) GV_CK(cudaMemsetAsync(j->d.track_n, 0, sizeof(int32_t) * j->W, j->stream));
     return GV_OK;
 }
@@ -2022,7 +2037,24 @@ gv_status gv_job_read_projheis(gv_job* j, double* vals, int32_t* nmeas)
 {
     if (!j || !vals) return GV_ERR_INVALID;
     GV_CK(cudaStreamSynchronize(j->stream));
-    if (exc(j))
+    if (exc(j) && j->d.pxs) {
+        // the sums with every walker's waiting measurements folded in, through a
+        // scratch of at most 32 MB (whole walkers)
+        const size_t per = size_t(2) * j->ch.Nexc * j->ch.Nexc;
+        const int chunk = int(std::max<size_t>(1, std::min<size_t>(j->W, (size_t(32) << 20) / (per * sizeof(cx<double>)))));
+        void* p = nullptr;
+        gv_status st = diag_scratch(j, size_t(chunk) * per * sizeof(cx<double>), &p);
+        if (st != GV_OK) return st;
+        for (int w0 = 0; w0 < j->W; w0 += chunk) {
+            const int nw = std::min(chunk, j->W - w0);
+            k_ho_read<256><<<nw, 256, 0, j->stream>>>(j->d, w0, static_cast<cx<double>*>(p));
+            GV_CK(cudaGetLastError());
+            ++j->total_launches;
+            GV_CK(cudaStreamSynchronize(j->stream));
+            GV_CK(copy_sync(vals + 2 * per * size_t(w0), p, size_t(nw) * per * sizeof(cx<double>),
+                            cudaMemcpyDeviceToHost));
+        }
+    } else if (exc(j))
         GV_CK(copy_sync(vals, j->d.pjx, sizeof(cx<double>) * 2 * size_t(j->W) * j->ch.Nexc * j->ch.Nexc,
                          cudaMemcpyDeviceToHost));
     else

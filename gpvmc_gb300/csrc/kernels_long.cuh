@@ -867,9 +867,10 @@ __global__ void __launch_bounds__(NT) k_measure_long(DevJob J, int mask)
         const double iw = 1.0 / wsum;
         cx<double>* H = J.pjx + size_t(w) * 2 * Nexc * Nexc;
         cx<double>* O = H + size_t(Nexc) * Nexc;
-        // Mixed form: the outer products in FP32, widened exactly and summed in
-        // FP64 (as the transverse channel's measurement; FP64 products for a
-        // walker whose factors exceed 1e15)
+        // Mixed form: the outer products in FP32, summed over a block of
+        // measurements and widened into the FP64 sums (ho_push, as the
+        // transverse channel's measurement; FP64 products at once for a walker
+        // whose factors exceed 1e15)
         bool narrow = false;
         if constexpr (sizeof(T) == 4) {
             cx<float>* s_caf = reinterpret_cast<cx<float>*>(smem + lay.f32);
@@ -886,16 +887,7 @@ __global__ void __launch_bounds__(NT) k_measure_long(DevJob J, int mask)
             narrow = !__syncthreads_or(big);
         }
         if (narrow) {
-            const cx<float>* s_caf = reinterpret_cast<const cx<float>*>(smem + lay.f32);
-            const cx<float>* s_hf = s_caf + Nexc;
-            const cx<float>* s_af = s_hf + Nexc;
-            for (int idx = tid; idx < Nexc * Nexc; idx += NT) {
-                const int k1 = idx / Nexc, k2 = idx % Nexc;
-                const cx<float> ca = s_caf[k1];
-                const cx<float> hv = cmul_rn(ca, s_hf[k2]), ov = cmul_rn(ca, s_af[k2]);
-                H[idx].x += f32_to_f64(hv.x); H[idx].y += f32_to_f64(hv.y);
-                O[idx].x += f32_to_f64(ov.x); O[idx].y += f32_to_f64(ov.y);
-            }
+            ho_push<NT>(J, w, reinterpret_cast<const cx<float>*>(smem + lay.f32));
         } else {
             for (int idx = tid; idx < Nexc * Nexc; idx += NT) {
                 const int k1 = idx / Nexc, k2 = idx % Nexc;

@@ -629,6 +629,81 @@ __host__ __device__ inline MeasLayout meas_layout(int Ns, int Nmax, int Nexc)
     return l;
 }
 
+// H / O of a mixed job in blocks of measurements.  A measurement leaves its
+// FP32 factors caf = conj(a) / w, hf = h, af = a (each Nexc long) in the
+// walker's next slot; n waiting slots fold as
+//     dst[k1 k2] = src[k1 k2] + fp64( sum_{m < n} caf_m[k1] hf_m[k2] )
+// (and O with af): the block sum in FP32 (FMA, m ascending), then one exact
+// widening and one FP64 add per entry.  Per entry, component and block the
+// FP32 sum is off by at most 2n 2^-24 sum_m |caf_m[k1]| |hf_m[k2]| (two FMA
+// roundings per term, each at most 2^-24 of a partial sum): 4e-6 of the
+// block's absolute sum for n = 32.  Each thread owns 4 rows k1 of one column
+// k2: the column's factors are coalesced loads, the rows' are broadcasts.
+template <int NT>
+__device__ void ho_fold(const cx<float>* slots, int n, int Nexc, const cx<double>* src, cx<double>* dst)
+{
+    constexpr int KB = 4;
+    const size_t NN = size_t(Nexc) * Nexc;
+    const int nkb = (Nexc + KB - 1) / KB;
+    for (int t = threadIdx.x; t < nkb * Nexc; t += NT) {
+        const int k2 = t % Nexc, k1b = (t / Nexc) * KB;
+        cx<float> h[KB], o[KB];
+#pragma unroll
+        for (int i = 0; i < KB; ++i) h[i] = o[i] = cx<float>{0.f, 0.f};
+        for (int m = 0; m < n; ++m) {
+            const cx<float>* s = slots + size_t(m) * 3 * Nexc;
+            const cx<float> hv = s[Nexc + k2], av = s[2 * Nexc + k2];
+#pragma unroll
+            for (int i = 0; i < KB; ++i)
+                if (k1b + i < Nexc) {
+                    const cx<float> ca = s[k1b + i];
+                    cmac(h[i], ca, hv);
+                    cmac(o[i], ca, av);
+                }
+        }
+#pragma unroll
+        for (int i = 0; i < KB; ++i)
+            if (k1b + i < Nexc) {
+                const size_t idx = size_t(k1b + i) * Nexc + k2;
+                const cx<double> a = src[idx], b = src[NN + idx];
+                dst[idx] = cx<double>{a.x + f32_to_f64(h[i].x), a.y + f32_to_f64(h[i].y)};
+                dst[NN + idx] = cx<double>{b.x + f32_to_f64(o[i].x), b.y + f32_to_f64(o[i].y)};
+            }
+    }
+}
+
+// One measurement's factors (f: 3*Nexc in shared memory) into walker w's next
+// slot; the kHoSlots-th folds the block into the walker's FP64 sums.
+template <int NT>
+__device__ void ho_push(const DevJob& J, int w, const cx<float>* f)
+{
+    const int Nexc = J.Nexc;
+    const int n = J.pxs_n[w];
+    cx<float>* slots = J.pxs + size_t(w) * kHoSlots * 3 * Nexc;
+    for (int i = threadIdx.x; i < 3 * Nexc; i += NT) slots[size_t(n) * 3 * Nexc + i] = f[i];
+    __syncthreads();   // the slot's stores are visible to the whole block
+    if (n + 1 == kHoSlots) {
+        cx<double>* H = J.pjx + size_t(w) * 2 * Nexc * Nexc;
+        ho_fold<NT>(slots, kHoSlots, Nexc, H, H);
+    }
+    if (threadIdx.x == 0) J.pxs_n[w] = (n + 1) % kHoSlots;
+}
+
+// Read-out of the H / O sums of walkers w0 .. w0 + gridDim.x - 1 with their
+// waiting slots folded in (into out, one 2*Nexc*Nexc block per walker); the
+// job's own sums and slots stay as they are, so what a walk accumulates does
+// not depend on when it is read.
+template <int NT>
+__global__ void __launch_bounds__(NT) k_ho_read(DevJob J, int w0, cx<double>* out)
+{
+    const int w = w0 + blockIdx.x;
+    if (w >= J.W) return;
+    const int Nexc = J.Nexc;
+    const size_t per = size_t(2) * Nexc * Nexc;
+    ho_fold<NT>(J.pxs + size_t(w) * kHoSlots * 3 * Nexc, J.pxs_n[w], Nexc, J.pjx + size_t(w) * per,
+                out + size_t(blockIdx.x) * per);
+}
+
 template <typename T, int NT>
 __global__ void __launch_bounds__(NT) k_measure_trans(DevJob J, int mask, const cx<float>* zpre)
 {
@@ -863,10 +938,11 @@ __global__ void __launch_bounds__(NT) k_measure_trans(DevJob J, int mask, const 
         if constexpr (sizeof(T) == 4) {
             // Mixed form: the Nexc^2 outer products in FP32 (their factors come
             // from FP32 ratios; conj(a_k1) / sum|a|^2 rounded once per state),
-            // widened exactly and summed into the FP64 sums: four FP64 adds per
-            // entry instead of sixteen FP64 operations on GB300's narrow FP64
-            // pipe.  A walker whose factors could take a product near the FP32
-            // range (any |factor| > 1e15) keeps the FP64 products.
+            // summed over a block of kHoSlots measurements and then widened
+            // into the FP64 sums (ho_push): per measurement 3 Nexc FP32 factors
+            // are written instead of the 2 Nexc^2 FP64 sums read and written.
+            // A walker whose factors could take a product near the FP32 range
+            // (any |factor| > 1e15) adds FP64 products at once.
             cx<float>* s_caf = reinterpret_cast<cx<float>*>(smem + lay.f32);
             cx<float>* s_hf = s_caf + Nexc;
             cx<float>* s_af = s_hf + Nexc;
@@ -881,16 +957,7 @@ __global__ void __launch_bounds__(NT) k_measure_trans(DevJob J, int mask, const 
             narrow = !__syncthreads_or(big);
         }
         if (narrow) {
-            const cx<float>* s_caf = reinterpret_cast<const cx<float>*>(smem + lay.f32);
-            const cx<float>* s_hf = s_caf + Nexc;
-            const cx<float>* s_af = s_hf + Nexc;
-            for (int idx = tid; idx < Nexc * Nexc; idx += NT) {
-                const int k1 = idx / Nexc, k2 = idx % Nexc;
-                const cx<float> ca = s_caf[k1];
-                const cx<float> hv = cmul_rn(ca, s_hf[k2]), ov = cmul_rn(ca, s_af[k2]);
-                H[idx].x += f32_to_f64(hv.x); H[idx].y += f32_to_f64(hv.y);
-                O[idx].x += f32_to_f64(ov.x); O[idx].y += f32_to_f64(ov.y);
-            }
+            ho_push<NT>(J, w, reinterpret_cast<const cx<float>*>(smem + lay.f32));
         } else {
             for (int idx = tid; idx < Nexc * Nexc; idx += NT) {
                 const int k1 = idx / Nexc, k2 = idx % Nexc;

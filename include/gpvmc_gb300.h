@@ -288,7 +288,10 @@ gv_status gv_job_read_weight(gv_job* job, double* sigma /* n_walkers */);
  * ProjHeis m_vals (2*Nexc*Nexc complex per walker; for the ground state
  * [E*L^2-normalised sum, count]), StagMagnZ (1 complex per walker), and the
  * job-wide StatSpinStruct sums (5*Ns*Ns complex: szz, s+-, s-+, s++, s--),
- * with the number of measurements each walker made. */
+ * with the number of measurements each walker made.  A mixed exciton job sums
+ * its H / O outer products in FP32 over blocks of 32 measurements before one
+ * FP64 add per entry; the read folds a block still open into what it returns
+ * and leaves the job's sums as they are. */
 gv_status gv_job_read_projheis(gv_job* job, double* vals, int32_t* nmeas);
 gv_status gv_job_read_stagmagn(gv_job* job, double* vals, int32_t* nmeas);
 gv_status gv_job_read_statspin(gv_job* job, double* vals, int32_t* nmeas);
