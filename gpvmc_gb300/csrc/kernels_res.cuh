@@ -652,22 +652,37 @@ __global__ void __launch_bounds__(kResThreads, 1) k_walk_gs_res(DevJob J, uint64
                     tab[e] = pi >= 0 ? (pi | (kk << 8) | (i << 10)) : -1;
                 }
                 wg_sync(g);
-                // phase rows of the eight sites of a group of 32 bonds, fetched one group ahead
-                auto fetch_rows = [&](int e0, cx<T> (&ph)[8]) {
+                // phase rows of the eight sites of a group of 32 bonds and the
+                // sites' coefficients, fetched one group ahead (u_f = phase * coef)
+                // (branch-free: clamped indices, zeros selected afterwards)
+                auto fetch_rows = [&](int e0, cx<T> (&ph)[8], cx<T> (&co)[8]) {
+                    const int fi = min(f, N - 1);
+                    int js[8];
+#pragma unroll
+                    for (int k = 0; k < 8; ++k) js[k] = s_part[(1 - g) * N + min((e0 >> 2) + k, N - 1)];
 #pragma unroll
                     for (int k = 0; k < 8; ++k) {
-                        const int q = (e0 >> 2) + k;
-                        ph[k] = (q < N && f < N) ? phase[size_t(s_part[(1 - g) * N + q]) * Nk + f] : cx<T>{0.f, 0.f};
+                        ph[k] = phase[size_t(js[k]) * Nk + fi];
+                        co[k] = cf[s_sub[js[k]] * N + fi];
                     }
+#pragma unroll
+                    for (int k = 0; k < 8; ++k)
+                        if (!((e0 >> 2) + k < N && f < N)) co[k] = cx<T>{0.f, 0.f};
                 };
-                cx<T> phn[8];
-                fetch_rows(0, phn);
+                cx<T> phn[8], con[8];
+                fetch_rows(0, phn, con);
                 for (int e0 = 0; e0 < NE; e0 += 32) {
-                    uint32_t rr[64];
+                    // the group's 32 entries first (NE is a multiple of 4: whole int4s),
+                    // then the 32 TMEM loads back to back
                     int ent[32];
 #pragma unroll
+                    for (int q = 0; q < 8; ++q) {
+                        const int4 x = e0 + 4 * q < NE ? reinterpret_cast<const int4*>(tab + e0)[q] : make_int4(-1, -1, -1, -1);
+                        ent[4 * q] = x.x; ent[4 * q + 1] = x.y; ent[4 * q + 2] = x.z; ent[4 * q + 3] = x.w;
+                    }
+                    uint32_t rr[64];
+#pragma unroll
                     for (int t = 0; t < 32; ++t) {   // branch-free: a bond without a ratio loads particle 0
-                        ent[t] = e0 + t < NE ? tab[e0 + t] : -1;
                         uint32_t r2[2];
                         tmem_ld2(trow + 2 * (ent[t] >= 0 ? (ent[t] & 0xFF) : 0), r2);
                         rr[2 * t] = r2[0];
@@ -675,13 +690,8 @@ __global__ void __launch_bounds__(kResThreads, 1) k_walk_gs_res(DevJob J, uint64
                     }
                     cx<T> phk[8];
 #pragma unroll
-                    for (int k = 0; k < 8; ++k) phk[k] = phn[k];
-                    if (e0 + 32 < NE) fetch_rows(e0 + 32, phn);
-#pragma unroll
-                    for (int k = 0; k < 8; ++k) {   // the eight sites of this group of 32 bonds
-                        const int q = (e0 >> 2) + k;
-                        if (q < N && f < N) phk[k] = cmul_rn(phk[k], cf[s_sub[s_part[(1 - g) * N + q]] * N + f]);
-                    }
+                    for (int k = 0; k < 8; ++k) phk[k] = cmul_rn(phn[k], con[k]);   // the eight sites of this group
+                    if (e0 + 32 < NE) fetch_rows(e0 + 32, phn, con);
                     tmem_wait_ld(rr);
                     cx<T> v[32];
 #pragma unroll

@@ -7,9 +7,11 @@
 //   BigDouble / BigComplex (BigDouble.h:11,       gv::BigDouble / gv::BigComplex
 //     BigComplex.h:10)
 //   hop_t / hop_path_t (defs.h:5-7)               gv::hop_t / gv::hop_path_t
-//   StagFluxGroundState, StagFluxTransExciton     gv::StagFluxGroundState, gv::StagFluxTransExciton
+//   StagFluxGroundState, StagFluxTransExciton,    gv::StagFluxGroundState, gv::StagFluxTransExciton,
+//     StagFluxLongExciton                         gv::StagFluxLongExciton
 //     (StagFluxGroundState.cpp:3-15,              GetHops / GetHop from the walker's current state
-//      StagFluxTransExciton.cpp:7-44;
+//      StagFluxTransExciton.cpp:7-44,
+//      StagFluxLongExciton.cpp:6-66;
 //      WaveFunction.cpp:69-83)
 //   SlaterDeterminant (SlaterDeterminant.h:44)    gv::SlaterDeterminant  Init, Amp, VirtUpdate(rhop, khop, qs),
 //                                                                        Update(rhop, khop)
@@ -27,6 +29,7 @@
 // std::logic_error under -DEXCEPT and aborts otherwise).
 #pragma once
 
+#include <algorithm>
 #include <cmath>
 #include <complex>
 #include <cstdint>
@@ -145,6 +148,14 @@ struct StagFluxTransExciton : WaveFunctionParams {
         : WaveFunctionParams{L_, GV_CH_TRANS, {qx, qy}, phi_, neel_, neel_exp_, {bcx, bcy}} {}
 };
 
+// StagFluxLongExciton (StagFluxLongExciton.cpp:6-66): momentum q = (qx, qy);
+// L^2 particle-hole states within one flavour plus the unexcited state.
+struct StagFluxLongExciton : WaveFunctionParams {
+    StagFluxLongExciton(int L_, double phi_, double neel_, int qx, int qy, double neel_exp_ = 0.0, double bcx = 1.0,
+                        double bcy = 1.0)
+        : WaveFunctionParams{L_, GV_CH_LONG, {qx, qy}, phi_, neel_, neel_exp_, {bcx, bcy}} {}
+};
+
 class Job {
   public:
     Job(const WaveFunctionParams& wav, int n_walkers, uint64_t seed, int precision = GV_PREC_FP64,
@@ -170,7 +181,7 @@ class Job {
         check(gv_job_create(&c, &job_), "gv_job_create");
         check(gv_job_dims(job_, &Ns_, &N_[0], &N_[1], &Nexc_), "gv_job_dims");
         walkers_ = n_walkers;
-        if (wav.channel == GV_CH_TRANS) {
+        if (wav.channel != GV_CH_GROUNDSTATE) {
             exc_up_.resize(Nexc_);
             exc_dn_.resize(Nexc_);
             check(gv_channel_states(wav.L, wav.phase_shift, wav.channel, wav.q, exc_up_.data(), exc_dn_.data()),
@@ -242,26 +253,52 @@ class Job {
 };
 
 // The wavefunction of one walker: its channel states and the hops between
-// them (WaveFunction::GetHops / GetHop, WaveFunction.cpp:69-83).  From the
-// current state c, state k differs by flavour 0: exc_up[c] -> exc_up[k] and
-// flavour 1: exc_dn[k] -> exc_dn[c] (none for k = c); the ground state has
-// one state and no hops.
+// them (WaveFunction::GetHops / GetHop, WaveFunction.cpp:69-83); the ground
+// state has one state and no hops.  Transverse exciton: from the current
+// state c, state k differs by flavour 0: exc_up[c] -> exc_up[k] and flavour 1:
+// exc_dn[k] -> exc_dn[c] (none for k = c).  Longitudinal exciton: state
+// k < Ns lifts one particle of flavour k % 2 from orbital exc_dn[k] to
+// exc_up[k], state Ns lifts none; from c to k a flavour carrying both
+// excitations takes the two hops {exc_up[c], exc_dn[k]} -> {exc_up[k],
+// exc_dn[c]} (each side in increasing order, paired in that order), one
+// carrying only c's undoes it (exc_up[c] -> exc_dn[c]), one carrying only k's
+// makes it (exc_dn[k] -> exc_up[k]).
 class WaveFunction {
   public:
     WaveFunction(Job& job, int walker = 0) : job_(job), walker_(walker) {}
     int GetNExc() const { return job_.Nexc(); }
-    int GetCurrentState() const { return job_.wav().channel == GV_CH_TRANS ? job_.CurrentState(walker_) : 0; }
+    int GetCurrentState() const { return job_.wav().channel != GV_CH_GROUNDSTATE ? job_.CurrentState(walker_) : 0; }
     std::vector<std::vector<hop_path_t>> GetHops() const
     {
         const int Nexc = job_.Nexc();
         std::vector<std::vector<hop_path_t>> h(Nexc, std::vector<hop_path_t>(2));
-        if (job_.wav().channel != GV_CH_TRANS) return h;
+        if (job_.wav().channel == GV_CH_GROUNDSTATE) return h;
         const int c = GetCurrentState();
-        for (int k = 0; k < Nexc; ++k) {
-            if (k == c) continue;
-            h[k][0].push_back(hop_t(job_.exc_up()[c], job_.exc_up()[k]));
-            h[k][1].push_back(hop_t(job_.exc_dn()[k], job_.exc_dn()[c]));
+        const std::vector<int32_t>& up = job_.exc_up();
+        const std::vector<int32_t>& dn = job_.exc_dn();
+        if (job_.wav().channel == GV_CH_TRANS) {
+            for (int k = 0; k < Nexc; ++k) {
+                if (k == c) continue;
+                h[k][0].push_back(hop_t(up[c], up[k]));
+                h[k][1].push_back(hop_t(dn[k], dn[c]));
+            }
+            return h;
         }
+        const int Ns = job_.Ns();
+        auto kind = [Ns](int k) { return k < Ns ? (k & 1) : 2; };
+        for (int k = 0; k < Nexc; ++k)
+            for (int fl = 0; fl < 2; ++fl) {
+                const bool ec = kind(c) == fl, ek = kind(k) == fl;
+                if (ec && ek && k != c) {
+                    const std::pair<int, int> v = std::minmax(up[c], dn[k]), f = std::minmax(up[k], dn[c]);
+                    h[k][fl].push_back(hop_t(v.first, f.first));
+                    h[k][fl].push_back(hop_t(v.second, f.second));
+                } else if (ec && !ek) {
+                    h[k][fl].push_back(hop_t(up[c], dn[c]));
+                } else if (ek && !ec) {
+                    h[k][fl].push_back(hop_t(dn[k], up[k]));
+                }
+            }
         return h;
     }
     std::vector<hop_path_t> GetHop(int k) const { return GetHops()[k]; }

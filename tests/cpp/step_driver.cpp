@@ -3,7 +3,7 @@
 // LatticeStepper::trystep, MetroMC::YesNo on new_weight / state_weight,
 // LatticeStepper::step on acceptance -- with every step printed, then the
 // second half of the steps through MetroMC::Step itself.
-//   step_driver gs|trans L phi_over_pi neel seed steps qx qy fp64|mixed
+//   step_driver gs|trans|long L phi_over_pi neel seed steps qx qy fp64|mixed
 // Output lines:
 //   S v1 v2 khop accepted ratio        one per step of the first half
 //   V K Nr state <re im exp10 of VirtUpdate(rhop, khop, qs) for every state, no hop
@@ -19,10 +19,10 @@
 int main(int argc, char** argv)
 {
     if (argc < 10) {
-        std::fprintf(stderr, "usage: %s gs|trans L phi_over_pi neel seed steps qx qy fp64|mixed\n", argv[0]);
+        std::fprintf(stderr, "usage: %s gs|trans|long L phi_over_pi neel seed steps qx qy fp64|mixed\n", argv[0]);
         return 2;
     }
-    const bool trans = std::string(argv[1]) == "trans";
+    const std::string channel = argv[1];
     const int L = std::atoi(argv[2]);
     const double phi = std::atof(argv[3]) * M_PI;   // vmc.cpp:120
     const double neel = std::atof(argv[4]);
@@ -33,7 +33,11 @@ int main(int argc, char** argv)
     try {
         gv::StagFluxGroundState gs(L, phi, neel);
         gv::StagFluxTransExciton tx(L, phi, neel, qx, qy);
-        gv::Job job(trans ? static_cast<const gv::WaveFunctionParams&>(tx) : gs, 1, seed, prec);
+        gv::StagFluxLongExciton lx(L, phi, neel, qx, qy);
+        const gv::WaveFunctionParams& wav = channel == "trans"  ? static_cast<const gv::WaveFunctionParams&>(tx)
+                                            : channel == "long" ? static_cast<const gv::WaveFunctionParams&>(lx)
+                                                                : gs;
+        gv::Job job(wav, 1, seed, prec);
         job.InitWalkers();
         gv::LatticeStepper stepper(job);
         gv::MetroMC varmc(stepper);

@@ -53,7 +53,8 @@ def test_driver_matches_python_api(tmp_path, engine):
 
 @pytest.mark.gpu
 @pytest.mark.parametrize("channel,L,q,steps", [("gs", 8, (0, 0), 1000), ("gs", 16, (0, 0), 400),
-                                               ("trans", 8, (4, 4), 400), ("trans", 4, (2, 2), 600)])
+                                               ("trans", 8, (4, 4), 400), ("trans", 4, (2, 2), 600),
+                                               ("long", 4, (2, 2), 600), ("long", 8, (0, 0), 400)])
 def test_step_driver_matches_oracle(tmp_path, engine, oracle, channel, L, q, steps):
     """The step-level adapter (LatticeStepper::trystep / step, MetroMC::YesNo,
     MetroMC::Step, SlaterDeterminant::VirtUpdate(rhop, khop, qs)) driven by C++
@@ -72,7 +73,7 @@ def test_step_driver_matches_oracle(tmp_path, engine, oracle, channel, L, q, ste
     t = np.zeros(len(S), dtype=[("v1", "<i4"), ("v2", "<i4"), ("kind", "<i4"), ("accepted", "<i4"), ("ratio", "<f8")])
     for i, x in enumerate(S):
         t[i] = (int(x[0]), int(x[1]), int(int(x[2]) >= 0), int(x[3]), float(x[4]))
-    ch = oracle.TRANS if channel == "trans" else oracle.GROUNDSTATE
+    ch = {"gs": oracle.GROUNDSTATE, "trans": oracle.TRANS, "long": oracle.LONG}[channel]
 
     def fresh():
         o = oracle.OracleChain(L, 0.25 * math.pi, 0.1, channel=ch, q=q, seed=seed, walker=0)

@@ -22,11 +22,13 @@ PHI = 0.25 * math.pi
 def _wav(engine, channel, L, q):
     if channel == "trans":
         return engine.StagFluxTransExciton(L, PHI, 0.1, q=q)
+    if channel == "long":
+        return engine.StagFluxLongExciton(L, PHI, 0.1, q=q)
     return engine.StagFluxGroundState(L, PHI, 0.1)
 
 
 def _oracle(oracle, channel, L, q, seed, walker):
-    ch = oracle.TRANS if channel == "trans" else oracle.GROUNDSTATE
+    ch = {"gs": oracle.GROUNDSTATE, "trans": oracle.TRANS, "long": oracle.LONG}[channel]
     o = oracle.OracleChain(L, PHI, 0.1, channel=ch, q=q, seed=seed, walker=walker)
     assert o.random_start() == 0
     return o
@@ -53,7 +55,8 @@ def _step_trace(mc, stepper, n):
 
 
 @pytest.mark.parametrize("channel,L,q,seed,steps", [("gs", 8, (0, 0), 77, 1200), ("gs", 16, (0, 0), 5, 600),
-                                                    ("trans", 8, (4, 4), 7, 500), ("trans", 4, (2, 2), 7, 500)])
+                                                    ("trans", 8, (4, 4), 7, 500), ("trans", 4, (2, 2), 7, 500),
+                                                    ("long", 4, (2, 2), 7, 500), ("long", 8, (0, 0), 7, 400)])
 def test_metromc_step_matches_oracle(engine, oracle, channel, L, q, seed, steps):
     job = engine.Job(_wav(engine, channel, L, q), walkers=1, seed=seed, precision="fp64")
     job.init_walkers()
@@ -83,7 +86,8 @@ def test_metromc_step_matches_oracle(engine, oracle, channel, L, q, seed, steps)
         assert (job.config()[0] == orc.config()).all()
 
 
-@pytest.mark.parametrize("channel,L,q", [("gs", 8, (0, 0)), ("gs", 12, (0, 0)), ("trans", 8, (4, 4))])
+@pytest.mark.parametrize("channel,L,q", [("gs", 8, (0, 0)), ("gs", 12, (0, 0)), ("trans", 8, (4, 4)),
+                                         ("long", 8, (2, 2))])
 def test_update_replays_a_walk_bit_for_bit(engine, channel, L, q):
     """SlaterDeterminant::Update with the exchanges and channel states a walk
     accepted gives that walk's configuration, amplitude and inverses exactly."""
@@ -97,14 +101,14 @@ def test_update_replays_a_walk_bit_for_bit(engine, channel, L, q):
         v1, v2 = int(r["v1"]), int(r["v2"])
         up = b.config()[1].astype(bool)
         u, d = (v1, v2) if up[v1] else (v2, v1)
-        b.update(1, (u, d, d, u), int(r["khop"]) if channel == "trans" else -1)
+        b.update(1, (u, d, d, u), int(r["khop"]) if channel != "gs" else -1)
     assert (a.config()[1] == b.config()[1]).all()
     ma, ea = a.amplitude()
     mb, eb = b.amplitude()
     assert ea[1] == eb[1] and ma[1] == mb[1]
     for fl in (0, 1):
         assert np.array_equal(a.inverse(1, fl), b.inverse(1, fl))
-    if channel == "trans":
+    if channel != "gs":
         assert a.state_index()[1] == b.state_index()[1]
     # walker 0 untouched by the updates on walker 1
     c = engine.Job(wav, walkers=2, seed=11, precision="fp64")
