@@ -472,7 +472,7 @@ bool trans_z_tc_ok(const gv_job* j)
 bool statspin_tc_ok(const gv_job* j)
 {
     return !exc(j) && j->cfg.precision == GV_PREC_MIXED && j->N[0] == j->N[1] && j->N[0] <= kTcM &&
-           !(j->cfg.flags & GV_FLAG_SCALAR_PAIRS);
+           j->Ns <= kTcThreads && !(j->cfg.flags & GV_FLAG_SCALAR_PAIRS);
 }
 
 // mode bit 0: StatSpinStruct; bit 1: ProjHeis from the tensor-core pair products
@@ -491,7 +491,7 @@ gv_status statspin_dispatch(gv_job* j, int mode = 1)
             j->last_launches += 2;
             j->total_launches += 2;
         }
-        k_statspin_tc<<<std::min(j->W, j->n_sm), kTcThreads, lay.total, j->stream>>>(j->d, mode);
+        k_statspin_tc<<<std::min(j->W, j->n_sm), kTcBlock, lay.total, j->stream>>>(j->d, mode);
         GV_CK(cudaGetLastError());
         if (mode & 1) {
             k_fold_ss<<<j->n_sm, 256, 0, j->stream>>>(j->d);
@@ -603,7 +603,7 @@ gv_status launch_measure_trans(gv_job* j, int mask)
         GV_CK(raise_smem_limit(k_trans_z_tc, zl.total));
         int zs;
         GV_CK(mark_begin(j, 2, &zs));
-        k_trans_z_tc<<<std::min(j->W, j->n_sm), kTcThreads, zl.total, j->stream>>>(j->d, j->d.zbuf);
+        k_trans_z_tc<<<std::min(j->W, j->n_sm), kTcBlock, zl.total, j->stream>>>(j->d, j->d.zbuf);
         GV_CK(cudaGetLastError());
         GV_CK(mark_end(j, zs));
         ++j->last_launches;

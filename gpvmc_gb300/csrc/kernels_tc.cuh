@@ -18,19 +18,22 @@
 // each real product is x_hi y_hi + x_hi y_lo + x_lo y_hi, accumulated in
 // FP32, which recovers FP32 accuracy (relative error ~1e-6 per element).  A
 // complex product is four real ones: Re = Ar Br + Ai (-Bi), Im = Ar Bi + Ai Br,
-// with -Bi stored as its own operand, so every walker and K chunk issues
-// 4 x 3 x 4 = 48 MMAs per matrix.
+// the -Bi terms through the MMA's negate-B bit, so every walker and K chunk
+// issues 4 x 3 x 4 = 48 MMAs per matrix.
 //
 // Operands are K-major in shared memory with the 128-byte swizzle: one row
 // (a particle) holds 32 TF32 values of K (the Slater rows f of one chunk) in
 // 128 bytes, 8-row groups 1024 bytes apart, 16-byte unit u of row r stored at
 // unit u ^ (r mod 8).  The CTA's threads build the operands directly from the
 // FP32 inverses (HBM) and the phase / coefficient tables (L2), so that the
-// split happens on the way in; one elected thread issues the MMAs and commits
-// them to an mbarrier that the CTA waits on (bounded).  The epilogue reads
-// the accumulators with tcgen05.ld and adds the pair ratios into the
-// job-wide sums.  One CTA per SM (its shared memory takes more than half of
-// the SM's), persistent over the walkers.
+// split happens on the way in; a ninth warp, which builds nothing, issues the
+// MMAs from one thread and commits them to an mbarrier that the CTA waits on
+// (bounded), so that the building warps fetch the next chunk meanwhile.  The
+// epilogue reads the accumulators with tcgen05.ld, stages the pair ratios in
+// the (then idle) tile region and adds them into the job-wide sums in
+// increasing site order, so that a warp's atomics fall on a few cache lines.
+// One CTA per SM (its shared memory takes more than half of the SM's),
+// persistent over the walkers.
 #pragma once
 
 #include "kernels_res.cuh"
@@ -38,25 +41,30 @@
 namespace gv {
 namespace {
 
-constexpr int kTcThreads = 256;
+constexpr int kTcThreads = 256;          // operand-building threads (warps 0..7)
+constexpr int kTcBlock = kTcThreads + 32; // + one warp that only issues the MMAs
+constexpr int kTcIssuer = kTcThreads;     // its elected thread
 constexpr int kTcM = 128;                 // MMA rows (up particles, zero padded)
 
 __host__ __device__ inline int tc_ncols(int N) { return (N + 15) & ~15; }
 
 struct TcLayout {
-    size_t a[4], b[6], site, coef, bar, tbase, red, total;
+    size_t a[4], b[4], site, coef, bar, tbase, red, srt, total;
 };
 
 // Operand tiles at 1024-byte multiples from a 1024-aligned base:
-// A: Re hi, Re lo, Im hi, Im lo (128 rows); B: the same and -Im hi, -Im lo
-// (tc_ncols(N) rows); each row 128 bytes.
+// A: Re hi, Re lo, Im hi, Im lo (128 rows); B: the same (tc_ncols(N) rows);
+// each row 128 bytes.  The -Im terms of the complex products read the Im
+// tiles through the MMA's negate-B bit.  After a walker's last MMAs the tile
+// region holds its pair ratios (N x tc_ncols(N) complex FP32, at most the
+// 128 KB of the tiles) for the sorted scatter into the pair sums.
 __host__ __device__ inline TcLayout tc_layout(int N)
 {
     TcLayout l;
     size_t o = 0;
     const size_t at = size_t(kTcM) * 128, bt = size_t(tc_ncols(N)) * 128;
     for (int i = 0; i < 4; ++i) { l.a[i] = o; o += at; }
-    for (int i = 0; i < 6; ++i) { l.b[i] = o; o += bt; }
+    for (int i = 0; i < 4; ++i) { l.b[i] = o; o += bt; }
     l.site = o;
     o += sizeof(int16_t) * 2 * 2 * kTcM;     // two walkers' buffers
     l.coef = o;
@@ -67,6 +75,8 @@ __host__ __device__ inline TcLayout tc_layout(int N)
     o += 8;
     l.red = o;                                 // per-warp ProjHeis partial sums
     o += sizeof(double) * 4 * (kTcThreads / 32);
+    l.srt = o;                                 // occupied sites in increasing order: [fl][site, particle][128], counts
+    o += sizeof(int16_t) * 2 * 2 * kTcM + sizeof(int) * 2 * (kTcThreads / 32);
     l.total = o + 1024;   // room to align the base
     return l;
 }
@@ -82,17 +92,20 @@ __device__ __forceinline__ uint32_t sw128(int r, int u)
     return uint32_t((r >> 3) * 1024 + (r & 7) * 128 + (((u ^ r) & 7) << 4));
 }
 
+// Round to the nearest TF32 value, ties away from zero, on the integer pipe:
+// half a TF32 unit (bit 12) is added to the magnitude bits and the 13 bits
+// below the TF32 mantissa are cleared (a carry moves into the exponent as the
+// rounding requires).  For finite inputs this is the rounding of
+// cvt.rna.tf32.f32, without the conversion pipe.
 __device__ __forceinline__ float tf32_rna(float x)
 {
-    uint32_t r;
-    asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(r) : "f"(x));
-    return __uint_as_float(r);
+    return __uint_as_float((__float_as_uint(x) + 0x1000u) & 0xFFFFE000u);
 }
 
 // Four consecutive K values of one row (real and imaginary parts) -> the
-// hi / lo tiles (and the negated imaginary tiles when nt == 6).
-__device__ __forceinline__ void tc_store_split(char* base, const size_t* tiles, int nt, uint32_t off,
-                                               const float (&re)[4], const float (&im)[4])
+// hi / lo tiles.
+__device__ __forceinline__ void tc_store_split(char* base, const size_t* tiles, uint32_t off, const float (&re)[4],
+                                               const float (&im)[4])
 {
     float4 rh, rl, ih, il;
     float* prh = &rh.x; float* prl = &rl.x; float* pih = &ih.x; float* pil = &il.x;
@@ -107,17 +120,16 @@ __device__ __forceinline__ void tc_store_split(char* base, const size_t* tiles, 
     *reinterpret_cast<float4*>(base + tiles[1] + off) = rl;
     *reinterpret_cast<float4*>(base + tiles[2] + off) = ih;
     *reinterpret_cast<float4*>(base + tiles[3] + off) = il;
-    if (nt == 6) {
-        *reinterpret_cast<float4*>(base + tiles[4] + off) = make_float4(-ih.x, -ih.y, -ih.z, -ih.w);
-        *reinterpret_cast<float4*>(base + tiles[5] + off) = make_float4(-il.x, -il.y, -il.z, -il.w);
-    }
 }
 
 // Operand rows of one K chunk (f = 32 kc .. 32 kc + 31), fetched a chunk
 // ahead into registers so that the global loads fly while the previous
-// chunk's MMAs run.  Item i of a thread covers row r = it % rows and 16-byte
-// unit u = it / rows (K values 4u .. 4u + 3), it = threadIdx.x + 256 i; lanes
-// run over rows, so a warp reads whole runs of an AiT row.
+// chunk's MMAs run.  it = threadIdx.x + 256 i numbers the (row, 16-byte unit)
+// items of a tile (unit u = K values 4u .. 4u + 3).  Inverse operands (K-major
+// in memory, AiT[f][r]) take row r = it % rows, unit u = it / rows: lanes run
+// over rows, so a warp reads whole runs of an AiT row.  Orbital operands
+// (row-major in memory, phase[site][f]) take row r = it / 8, unit u = it % 8:
+// a warp reads 32 contiguous bytes of each of four phase rows.
 constexpr int kTcItems = 4;   // rows * 8 / kTcThreads for rows <= 128
 
 struct TcRegs {
@@ -151,8 +163,8 @@ __device__ __forceinline__ void tc_load_phase_cols(TcRegs& R, const cx<float>* p
 {
 #pragma unroll
     for (int i = 0; i < kTcItems; ++i) {
-        const int it = threadIdx.x + kTcThreads * i, r = it % rows, u = it / rows;
-        const int s = (it < rows * 8 && r < nr) ? site[r] : -1;
+        const int it = threadIdx.x + kTcThreads * i, r = it >> 3, u = it & 7;
+        const int s = (r < rows && r < nr) ? site[r] : -1;
 #pragma unroll
         for (int t = 0; t < 4; ++t) {
             const int f = 32 * kc + 4 * u + t;
@@ -161,23 +173,35 @@ __device__ __forceinline__ void tc_load_phase_cols(TcRegs& R, const cx<float>* p
     }
 }
 
+// Phase values phase[site r][f] of rows r < N, K values f < N; four
+// consecutive values as two 16-byte loads where the row stride allows.
 __device__ __forceinline__ void tc_load_phase(TcRegs& R, const cx<float>* phase, int Nk, const int16_t* site, int N,
                                               int rows, int kc)
 {
+    const bool vec = (Nk & 1) == 0;   // 16-byte aligned pairs of complex values
 #pragma unroll
     for (int i = 0; i < kTcItems; ++i) {
-        const int it = threadIdx.x + kTcThreads * i, r = it % rows, u = it / rows;
-        const int s = (it < rows * 8 && r < N) ? site[r] : -1;
+        const int it = threadIdx.x + kTcThreads * i, r = it >> 3, u = it & 7;
+        const int s = (r < rows && r < N) ? site[r] : -1;
+        const int f0 = 32 * kc + 4 * u;
+        const cx<float>* p = phase + size_t(s < 0 ? 0 : s) * Nk + f0;
+        if (s >= 0 && vec && f0 + 3 < N) {
+            const float4 a = *reinterpret_cast<const float4*>(p);
+            const float4 b = *reinterpret_cast<const float4*>(p + 2);
+            R.ph[i][0] = {a.x, a.y};
+            R.ph[i][1] = {a.z, a.w};
+            R.ph[i][2] = {b.x, b.y};
+            R.ph[i][3] = {b.z, b.w};
+        } else {
 #pragma unroll
-        for (int t = 0; t < 4; ++t) {
-            const int f = 32 * kc + 4 * u + t;
-            R.ph[i][t] = (s >= 0 && f < N) ? phase[size_t(s) * Nk + f] : cx<float>{0.f, 0.f};
+            for (int t = 0; t < 4; ++t)
+                R.ph[i][t] = (s >= 0 && f0 + t < N) ? p[t] : cx<float>{0.f, 0.f};
         }
     }
 }
 
 // Inverse operand rows -> split tiles.
-__device__ __forceinline__ void tc_store_inverse(char* base, const size_t* tiles, int nt, const TcRegs& R, int rows)
+__device__ __forceinline__ void tc_store_inverse(char* base, const size_t* tiles, const TcRegs& R, int rows)
 {
 #pragma unroll
     for (int i = 0; i < kTcItems; ++i) {
@@ -187,20 +211,19 @@ __device__ __forceinline__ void tc_store_inverse(char* base, const size_t* tiles
         float re[4], im[4];
 #pragma unroll
         for (int t = 0; t < 4; ++t) { re[t] = R.inv[i][t].x; im[t] = R.inv[i][t].y; }
-        tc_store_split(base, tiles, nt, sw128(r, u), re, im);
+        tc_store_split(base, tiles, sw128(r, u), re, im);
     }
 }
 
 // Orbital operand rows phi_{2f}(site r) = phase[site][f] coef[sub(site)][f]
 // (the walk's own FP32 product) -> split tiles.
-__device__ __forceinline__ void tc_store_phi(char* base, const size_t* tiles, int nt, const TcRegs& R,
+__device__ __forceinline__ void tc_store_phi(char* base, const size_t* tiles, const TcRegs& R,
                                              const cx<float>* coef, const int16_t* site, int N, int L, int rows, int kc)
 {
 #pragma unroll
     for (int i = 0; i < kTcItems; ++i) {
-        const int it = threadIdx.x + kTcThreads * i;
-        if (it >= rows * 8) break;
-        const int r = it % rows, u = it / rows;
+        const int it = threadIdx.x + kTcThreads * i, r = it >> 3, u = it & 7;
+        if (r >= rows) break;
         const int sub = r < N ? sublattice(site[r], L) : 0;
         float re[4], im[4];
 #pragma unroll
@@ -210,21 +233,20 @@ __device__ __forceinline__ void tc_store_phi(char* base, const size_t* tiles, in
             re[t] = v.x;
             im[t] = v.y;
         }
-        tc_store_split(base, tiles, nt, sw128(r, u), re, im);
+        tc_store_split(base, tiles, sw128(r, u), re, im);
     }
 }
 
 // Orbital operand with an explicit row -> coefficient table: row r, K value f
 // holds phase[site r][pcol f] coef[sub(site r) * cld + f] (rows r < nr, f < nk).
-__device__ __forceinline__ void tc_store_phi_cols(char* base, const size_t* tiles, int nt, const TcRegs& R,
+__device__ __forceinline__ void tc_store_phi_cols(char* base, const size_t* tiles, const TcRegs& R,
                                                   const cx<float>* coef, int cld, const int16_t* site, int nr, int nk,
                                                   int L, int rows, int kc)
 {
 #pragma unroll
     for (int i = 0; i < kTcItems; ++i) {
-        const int it = threadIdx.x + kTcThreads * i;
-        if (it >= rows * 8) break;
-        const int r = it % rows, u = it / rows;
+        const int it = threadIdx.x + kTcThreads * i, r = it >> 3, u = it & 7;
+        if (r >= rows) break;
         const int sub = r < nr ? sublattice(site[r], L) : 0;
         float re[4], im[4];
 #pragma unroll
@@ -234,7 +256,7 @@ __device__ __forceinline__ void tc_store_phi_cols(char* base, const size_t* tile
             re[t] = v.x;
             im[t] = v.y;
         }
-        tc_store_split(base, tiles, nt, sw128(r, u), re, im);
+        tc_store_split(base, tiles, sw128(r, u), re, im);
     }
 }
 
@@ -288,15 +310,14 @@ __device__ __forceinline__ void tmem_ld16(uint32_t taddr, uint32_t* r)
 // The 48 MMAs of one K chunk into the accumulator pair at column dcol:
 // Re += Ar Br + Ai (-Bi), Im += Ar Bi + Ai Br, each real product as three
 // split-precision terms, K = 8 per instruction (32 bytes along the row).
-// With neg_bit the -Bi terms read the Bi tiles through the instruction
-// descriptor's negate-B bit (bit 14), so the negated tiles need not be built.
+// The -Bi terms read the Bi tiles through the instruction descriptor's
+// negate-B bit (bit 14).
 __device__ __forceinline__ void tc_issue_chunk(uint32_t tbase, uint32_t dcol, uint32_t sbase, const TcLayout& lay,
-                                               uint32_t idesc, bool first, bool neg_bit = false)
+                                               uint32_t idesc, bool first)
 {
-    enum { RH = 0, RL = 1, IH = 2, IL = 3, NH = 4, NL = 5 };
-    const int re_terms[6][2] = {{RH, RH}, {RH, RL}, {RL, RH}, {IH, neg_bit ? IH : NH}, {IH, neg_bit ? IL : NL},
-                                {IL, neg_bit ? IH : NH}};
-    const uint32_t idesc_neg = idesc | (neg_bit ? (1u << 14) : 0u);
+    enum { RH = 0, RL = 1, IH = 2, IL = 3 };
+    const int re_terms[6][2] = {{RH, RH}, {RH, RL}, {RL, RH}, {IH, IH}, {IH, IL}, {IL, IH}};
+    const uint32_t idesc_neg = idesc | (1u << 14);
     const int im_terms[6][2] = {{RH, IH}, {RH, IL}, {RL, IH}, {IH, RH}, {IH, RL}, {IL, RH}};
 #pragma unroll
     for (int kk = 0; kk < 4; ++kk) {
@@ -351,7 +372,7 @@ __global__ void k_fold_ss(DevJob J)
 // and down sites are nearest neighbours are the antiparallel bonds, and with
 // n_anti of them E/site = (Ns / 2 - n_anti / 2 - sum_bonds r / 2) / Ns per
 // walker (parallel bonds +1/4, antiparallel -1/4 - r/2).
-__global__ void __launch_bounds__(kTcThreads, 1) k_statspin_tc(DevJob J, int mode)
+__global__ void __launch_bounds__(kTcBlock, 1) k_statspin_tc(DevJob J, int mode)
 {
     extern __shared__ __align__(16) char smem_raw[];
     const uint32_t raw = smem_addr(smem_raw);
@@ -381,8 +402,11 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_statspin_tc(DevJob J, int mod
     uint32_t parity = 0;
     bool failed = false;
 
+    const bool worker = tid < kTcThreads;   // the issuing warp builds no operands
+
     // per-walker tables into buffer b
     auto tables = [&](int w, int b) {
+        if (!worker) return;
         int16_t* st = s_site + b * 2 * kTcM;
         cx<float>* sc = s_coef + b * 4 * kTcM;
         for (int i = tid; i < 2 * N; i += kTcThreads) {
@@ -398,6 +422,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_statspin_tc(DevJob J, int mod
     // chunk (gm, kc) of walker w: the inverse operand is A for G_up and B for
     // G_dn^T; the orbital operand the other one
     auto fetch = [&](TcRegs& R, int w, int b, int gm, int kc) {
+        if (!worker) return;
         const int16_t* st = s_site + b * 2 * kTcM;
         tc_load_inverse(R, ai_ptr<float>(J, gm, w), N, gm == 0 ? kTcM : Nt, kc);
         tc_load_phase(R, J.phase32, Nk, gm == 0 ? st + kTcM : st, N, gm == 0 ? Nt : kTcM, kc);
@@ -425,19 +450,20 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_statspin_tc(DevJob J, int mod
                 parity ^= 1u;
             }
             first = false;
-            if (gm == 0) {   // G_up: A = AiT_up^T (rows c), B = Phi_up at the down sites (rows q)
-                tc_store_inverse(base, lay.a, 4, R, kTcM);
-                tc_store_phi(base, lay.b, 4, R, sc, st + kTcM, N, L, Nt, kc);
-            } else {         // G_dn^T: A = Phi_dn at the up sites (rows c), B = AiT_dn^T (rows q)
-                tc_store_phi(base, lay.a, 4, R, sc + 2 * N, st, N, L, kTcM, kc);
-                tc_store_inverse(base, lay.b, 4, R, Nt);
+            if (!worker) {
+            } else if (gm == 0) {   // G_up: A = AiT_up^T (rows c), B = Phi_up at the down sites (rows q)
+                tc_store_inverse(base, lay.a, R, kTcM);
+                tc_store_phi(base, lay.b, R, sc, st + kTcM, N, L, Nt, kc);
+            } else {                // G_dn^T: A = Phi_dn at the up sites (rows c), B = AiT_dn^T (rows q)
+                tc_store_phi(base, lay.a, R, sc + 2 * N, st, N, L, kTcM, kc);
+                tc_store_inverse(base, lay.b, R, Nt);
             }
             asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
             tmem_fence_before();
             __syncthreads();
-            if (tid == 0) {
+            if (tid == kTcIssuer) {   // the building warps go on to fetch the next chunk meanwhile
                 tmem_fence_after();
-                tc_issue_chunk(tbase, uint32_t(256 * gm), sbase, lay, idesc, kc == 0, true);
+                tc_issue_chunk(tbase, uint32_t(256 * gm), sbase, lay, idesc, kc == 0);
                 tc_commit(bar);
             }
             if (step + 1 < 2 * KC) {
@@ -462,45 +488,111 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_statspin_tc(DevJob J, int mod
             parity ^= 1u;
         }
         tmem_fence_after();
-        // epilogue: warp -> TMEM lanes 32 (warp % 4) .. +31 (rows c), 16-column
-        // chunks of q split between the two warps of a lane group
-        const int lg = warp & 3, c = 32 * lg + lane;
-        const bool crow = c < N;
-        const int si = crow ? st[c] : 0;
-        int nb[4];
+        // epilogue.  (1) which sites each flavour occupies (a ballot over the
+        // sites, counted per warp), for the lists of occupied sites in
+        // increasing order built in (3)
+        int16_t* srt = reinterpret_cast<int16_t*>(base + lay.srt);   // [fl][site | particle][kTcM]
+        int* s_cnt = reinterpret_cast<int*>(srt + 4 * kTcM);          // [warp][fl]
+        int fk[2] = {-1, -1};
+        unsigned occ[2] = {0u, 0u};
+        if (worker) {
+            if (tid < Ns) {
+                fk[0] = J.fock[size_t(w) * 2 * Ns + tid];
+                fk[1] = J.fock[(size_t(w) * 2 + 1) * Ns + tid];
+            }
+            // only particle indices that address V are listed
+            occ[0] = __ballot_sync(0xffffffffu, fk[0] >= 0 && fk[0] < N);
+            occ[1] = __ballot_sync(0xffffffffu, fk[1] >= 0 && fk[1] < N);
+            if (lane == 0) { s_cnt[warp * 2] = __popc(occ[0]); s_cnt[warp * 2 + 1] = __popc(occ[1]); }
+        }
+        // (2) warp -> TMEM lanes 32 (warp % 4) .. +31 (rows c), 16-column chunks
+        // of q split between the two warps of a lane group; the pair ratios
+        // r(c, q) go to V[c][q ^ (c % 16)] in the tile region (the XOR spreads
+        // a column's rows over the banks)
+        cx<float>* V = reinterpret_cast<cx<float>*>(base);
+        {
+            const int lg = warp & 3, c = 32 * lg + lane;
+            for (int cc = warp >> 2; worker && cc < Nt / 16; cc += 2) {
+                uint32_t r[64];
+                const uint32_t ta = tbase + (uint32_t(32 * lg) << 16) + uint32_t(16 * cc);
+                tmem_ld16(ta, r);
+                tmem_ld16(ta + 128, r + 16);
+                tmem_ld16(ta + 256, r + 32);
+                tmem_ld16(ta + 384, r + 48);
+                tmem_wait_ld(r);
+                if (c < N) {
 #pragma unroll
-        for (int k = 0; k < 4; ++k) nb[k] = J.nbr[si * 4 + k];
-        cx<double> eb = {0.0, 0.0};   // sum of the bond ratios of this thread's pairs
-        int nanti = 0;
-        for (int cc = warp >> 2; cc < Nt / 16; cc += 2) {
-            uint32_t r[64];
-            const uint32_t ta = tbase + (uint32_t(32 * lg) << 16) + uint32_t(16 * cc);
-            tmem_ld16(ta, r);
-            tmem_ld16(ta + 128, r + 16);
-            tmem_ld16(ta + 256, r + 32);
-            tmem_ld16(ta + 384, r + 48);
-            tmem_wait_ld(r);
-            if (crow) {
-#pragma unroll
-                for (int t = 0; t < 16; ++t) {
-                    const int q = 16 * cc + t;
-                    if (q < N) {
+                    for (int t = 0; t < 16; ++t) {
                         const cx<float> gu = {__uint_as_float(r[t]), __uint_as_float(r[16 + t])};
                         const cx<float> gd = {__uint_as_float(r[32 + t]), __uint_as_float(r[48 + t])};
-                        const cx<float> v = cmul_rn(gu, gd);
-                        const int sj = st[kTcM + q];
-                        if (mode & 1)   // FP32 staging sums, folded into the FP64 sums after the launch
-                            atomicAdd(J.ss32 + size_t(si) * Ns + sj, make_float2(v.x, v.y));
-                        if ((mode & 2) && (sj == nb[0] || sj == nb[1] || sj == nb[2] || sj == nb[3])) {
-                            eb.x += f32_to_f64(v.x);
-                            eb.y += f32_to_f64(v.y);
-                            ++nanti;
-                        }
+                        V[c * Nt + ((16 * cc + t) ^ (c & 15))] = cmul_rn(gu, gd);
                     }
                 }
             }
         }
         tmem_fence_before();
+        __syncthreads();
+        // (3) the sorted lists: site and particle of the k-th occupied site
+        if (worker) {
+            const unsigned below = (1u << lane) - 1u;
+#pragma unroll
+            for (int fl = 0; fl < 2; ++fl) {
+                if ((occ[fl] >> lane) & 1u) {
+                    int off = __popc(occ[fl] & below);
+                    for (int q = 0; q < warp; ++q) off += s_cnt[q * 2 + fl];
+                    if (off < kTcM) {
+                        srt[fl * 2 * kTcM + off] = int16_t(tid);
+                        srt[fl * 2 * kTcM + kTcM + off] = int16_t(fk[fl]);
+                    }
+                }
+            }
+        }
+        __syncthreads();
+        // (4) pair sums in site order: warp -> up sites a = warp, warp + 8, ...;
+        // lane -> down sites b = lane + 32 k, so that one atomic instruction
+        // covers 32 increasing sites of one row of the table
+        cx<double> eb = {0.0, 0.0};   // sum of the bond ratios of this thread's pairs
+        int nanti = 0;
+        if (worker) {
+            const int16_t* ups = srt;
+            const int16_t* upp = srt + kTcM;
+            const int16_t* dns = srt + 2 * kTcM;
+            const int16_t* dnp = srt + 3 * kTcM;
+            int n_up = 0, n_dn = 0;   // entries written for this walker (N each for a consistent state)
+            for (int q = 0; q < kTcThreads / 32; ++q) { n_up += s_cnt[q * 2]; n_dn += s_cnt[q * 2 + 1]; }
+            n_up = min(n_up, kTcM);
+            n_dn = min(n_dn, kTcM);
+            int jj[kTcM / 32], qq[kTcM / 32];
+#pragma unroll
+            for (int k = 0; k < kTcM / 32; ++k) {
+                const int bq = lane + 32 * k;
+                jj[k] = bq < n_dn ? dns[bq] : -1;
+                qq[k] = bq < n_dn ? dnp[bq] : 0;
+            }
+            for (int a = warp; a < n_up; a += kTcThreads / 32) {
+                const int i = ups[a], c = upp[a];
+                const cx<float>* Vc = V + c * Nt;
+                const int sw = c & 15;
+                float2* Ti = J.ss32 + size_t(i) * Ns;
+                int nb[4] = {-1, -1, -1, -1};
+                if (mode & 2) {
+#pragma unroll
+                    for (int k = 0; k < 4; ++k) nb[k] = J.nbr[i * 4 + k];
+                }
+#pragma unroll
+                for (int k = 0; k < kTcM / 32; ++k) {
+                    if (jj[k] < 0) continue;
+                    const cx<float> v = Vc[qq[k] ^ sw];
+                    if (mode & 1)   // FP32 staging sums, folded into the FP64 sums after the launch
+                        atomicAdd(Ti + jj[k], make_float2(v.x, v.y));
+                    if ((mode & 2) && (jj[k] == nb[0] || jj[k] == nb[1] || jj[k] == nb[2] || jj[k] == nb[3])) {
+                        eb.x += f32_to_f64(v.x);
+                        eb.y += f32_to_f64(v.y);
+                        ++nanti;
+                    }
+                }
+            }
+        }
         if (mode & 2) {   // the walker's ProjHeis sample
 #pragma unroll
             for (int o = 16; o; o >>= 1) {
@@ -508,7 +600,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_statspin_tc(DevJob J, int mod
                 eb.y += __shfl_xor_sync(0xffffffffu, eb.y, o);
                 nanti += __shfl_xor_sync(0xffffffffu, nanti, o);
             }
-            if (lane == 0) { s_red[warp * 4] = eb.x; s_red[warp * 4 + 1] = eb.y; s_red[warp * 4 + 2] = double(nanti); }
+            if (lane == 0 && worker) { s_red[warp * 4] = eb.x; s_red[warp * 4 + 1] = eb.y; s_red[warp * 4 + 2] = double(nanti); }
             __syncthreads();
             if (tid == 0) {
                 double ex = 0.0, ey = 0.0, na = 0.0;
@@ -521,6 +613,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_statspin_tc(DevJob J, int mod
             }
         }
         if (tid == 0 && (mode & 1)) atomicAdd(J.ss_n, w == 0 ? 1 : 0);
+        __syncthreads();   // V is read: the next walker's operands may overwrite the tiles
         first = true;   // the next walker's first MMAs follow the __syncthreads of its first chunk
         w = wn;
         b ^= 1;
@@ -548,7 +641,7 @@ __host__ __device__ inline TcLayout tc_layout_z(int N1)
     size_t o = 0;
     const size_t at = size_t(kTcM) * 128, bt = size_t(tc_ncols(N1)) * 128;
     for (int i = 0; i < 4; ++i) { l.a[i] = o; o += at; }
-    for (int i = 0; i < 6; ++i) { l.b[i] = o; o += bt; }
+    for (int i = 0; i < 4; ++i) { l.b[i] = o; o += bt; }
     l.site = o;   // [buf][ flavour-1 sites (128) | phase column of row f (kTcMaxK) ]
     o += sizeof(int16_t) * 2 * (kTcM + kTcMaxK);
     l.coef = o;   // [buf][sub][f]
@@ -561,7 +654,7 @@ __host__ __device__ inline TcLayout tc_layout_z(int N1)
     return l;
 }
 
-__global__ void __launch_bounds__(kTcThreads, 1) k_trans_z_tc(DevJob J, cx<float>* Z)
+__global__ void __launch_bounds__(kTcBlock, 1) k_trans_z_tc(DevJob J, cx<float>* Z)
 {
     extern __shared__ __align__(16) char smem_raw[];
     const uint32_t raw = smem_addr(smem_raw);
@@ -590,7 +683,9 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_trans_z_tc(DevJob J, cx<float
     uint32_t parity = 0;
     bool failed = false;
 
+    const bool worker = tid < kTcThreads;   // the issuing warp builds no operands
     auto tables = [&](int w, int b) {
+        if (!worker) return;
         int16_t* site = s_tab + b * (kTcM + kTcMaxK);
         int16_t* pcol = site + kTcM;
         cx<float>* cf = s_cf + b * 2 * kTcMaxK;
@@ -604,6 +699,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_trans_z_tc(DevJob J, cx<float
         }
     };
     auto fetch = [&](TcRegs& R, int w, int b, int kc) {
+        if (!worker) return;
         const int16_t* site = s_tab + b * (kTcM + kTcMaxK);
         const cx<float>* G = static_cast<const cx<float>*>(J.gup) + size_t(w) * N0 * Nexc;
         tc_load_rows(R, G, Nexc, Nexc, N0, kTcM, kc);
@@ -631,12 +727,14 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_trans_z_tc(DevJob J, cx<float
                 parity ^= 1u;
             }
             first = false;
-            tc_store_inverse(base, lay.a, 4, R, kTcM);
-            tc_store_phi_cols(base, lay.b, 6, R, cf, kTcMaxK, site, N1, N0, L, Nt, kc);
+            if (worker) {
+                tc_store_inverse(base, lay.a, R, kTcM);
+                tc_store_phi_cols(base, lay.b, R, cf, kTcMaxK, site, N1, N0, L, Nt, kc);
+            }
             asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
             tmem_fence_before();
             __syncthreads();
-            if (tid == 0) {
+            if (tid == kTcIssuer) {
                 tmem_fence_after();
                 tc_issue_chunk(tbase, 0u, sbase, lay, idesc, kc == 0);
                 tc_commit(bar);
@@ -665,7 +763,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_trans_z_tc(DevJob J, cx<float
         tmem_fence_after();
         // epilogue: lane k of TMEM -> Z[w][d][k], 16 columns d at a time
         const int lg = warp & 3, k = 32 * lg + lane;
-        for (int cc = warp >> 2; cc < Nt / 16; cc += 2) {
+        for (int cc = warp >> 2; worker && cc < Nt / 16; cc += 2) {
             uint32_t r[32];
             const uint32_t ta = tbase + (uint32_t(32 * lg) << 16) + uint32_t(16 * cc);
             tmem_ld16(ta, r);
