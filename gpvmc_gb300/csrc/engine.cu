@@ -472,7 +472,7 @@ bool trans_z_tc_ok(const gv_job* j)
 bool statspin_tc_ok(const gv_job* j)
 {
     return !exc(j) && j->cfg.precision == GV_PREC_MIXED && j->N[0] == j->N[1] && j->N[0] <= kTcM &&
-           j->Ns <= kTcThreads && !(j->cfg.flags & GV_FLAG_SCALAR_PAIRS);
+           j->Ns <= kTcThreads && j->Ns <= kOccMaxNs && !(j->cfg.flags & GV_FLAG_SCALAR_PAIRS);
 }
 
 // mode bit 0: StatSpinStruct; bit 1: ProjHeis from the tensor-core pair products
@@ -485,8 +485,7 @@ gv_status statspin_dispatch(gv_job* j, int mode = 1)
         int slot;
         GV_CK(mark_begin(j, 2, &slot));
         if (mode & 1) {   // antiparallel counts from occupation bitsets
-            const int cells = j->Ns * ((j->W + 31) / 32);
-            k_occ_bits<<<(cells + 255) / 256, 256, 0, j->stream>>>(j->d, j->d.occ);
+            k_occ_bits<<<(j->W + 31) / 32, 256, 0, j->stream>>>(j->d, j->d.occ);
             k_occ_pairs<<<j->Ns, 256, 0, j->stream>>>(j->d, j->d.occ);
             j->last_launches += 2;
             j->total_launches += 2;

@@ -49,7 +49,7 @@ constexpr int kTcM = 128;                 // MMA rows (up particles, zero padded
 __host__ __device__ inline int tc_ncols(int N) { return (N + 15) & ~15; }
 
 struct TcLayout {
-    size_t a[4], b[4], site, coef, bar, tbase, red, srt, total;
+    size_t a[4], b[4], site, coef, bar, tbase, red, srt, nbr, total;
 };
 
 // Operand tiles at 1024-byte multiples from a 1024-aligned base:
@@ -77,6 +77,8 @@ __host__ __device__ inline TcLayout tc_layout(int N)
     o += sizeof(double) * 4 * (kTcThreads / 32);
     l.srt = o;                                 // occupied sites in increasing order: [fl][site, particle][128], counts
     o += sizeof(int16_t) * 2 * 2 * kTcM + sizeof(int) * 2 * (kTcThreads / 32);
+    l.nbr = o;                                 // neighbour table (ProjHeis mode): 4 sites per site
+    o += sizeof(int16_t) * 4 * 2 * kTcM;
     l.total = o + 1024;   // room to align the base
     return l;
 }
@@ -130,7 +132,7 @@ __device__ __forceinline__ void tc_store_split(char* base, const size_t* tiles, 
 // over rows, so a warp reads whole runs of an AiT row.  Orbital operands
 // (row-major in memory, phase[site][f]) take row r = it / 8, unit u = it % 8:
 // a warp reads 32 contiguous bytes of each of four phase rows.
-constexpr int kTcItems = 4;   // rows * 8 / kTcThreads for rows <= 128
+constexpr int kTcItems = kTcM * 8 / kTcThreads;   // (row, unit) items per thread for rows <= 128
 
 struct TcRegs {
     cx<float> inv[kTcItems][4];   // inverse operand: AiT[f][r] = (A^-1)(r, f)
@@ -403,6 +405,9 @@ __global__ void __launch_bounds__(kTcBlock, 1) k_statspin_tc(DevJob J, int mode)
     bool failed = false;
 
     const bool worker = tid < kTcThreads;   // the issuing warp builds no operands
+    int16_t* s_nbr = reinterpret_cast<int16_t*>(base + lay.nbr);      // [site][4]
+    if (mode & 2)
+        for (int i = tid; i < 4 * Ns; i += kTcBlock) s_nbr[i] = int16_t(J.nbr[i]);   // read after the barriers below
 
     // per-walker tables into buffer b
     auto tables = [&](int w, int b) {
@@ -442,6 +447,13 @@ __global__ void __launch_bounds__(kTcBlock, 1) k_statspin_tc(DevJob J, int mode)
         const int wn = tc_next_walker(J, w);
         const int16_t* st = s_site + b * 2 * kTcM;
         const cx<float>* sc = s_coef + b * 4 * kTcM;
+        // site lists of the walker for the epilogue: fk = particle at site tid
+        // of each flavour (or -1), loaded at step 0; occ = the warp's ballot
+        // of the sites that list a particle, counted per warp at step 1
+        int16_t* srt = reinterpret_cast<int16_t*>(base + lay.srt);   // [fl][site | particle][kTcM]
+        int* s_cnt = reinterpret_cast<int*>(srt + 4 * kTcM);          // [warp][fl]
+        int fk[2] = {-1, -1};
+        unsigned occ[2] = {0u, 0u};
         for (int step = 0; step < 2 * KC; ++step) {
             const int gm = step / KC, kc = step % KC;
             if (!first) {   // the previous chunk's MMAs are done with the tiles
@@ -473,6 +485,15 @@ __global__ void __launch_bounds__(kTcBlock, 1) k_statspin_tc(DevJob J, int mode)
                 __syncthreads();
                 fetch(R, wn, b ^ 1, 0, 0);
             }
+            if (step == 0 && worker && tid < Ns) {   // loads that land while the MMAs run
+                fk[0] = J.fock[size_t(w) * 2 * Ns + tid];
+                fk[1] = J.fock[(size_t(w) * 2 + 1) * Ns + tid];
+            }
+            if (step == 1 && worker) {   // only particle indices that address V are listed
+                occ[0] = __ballot_sync(0xffffffffu, fk[0] >= 0 && fk[0] < N);
+                occ[1] = __ballot_sync(0xffffffffu, fk[1] >= 0 && fk[1] < N);
+                if (lane == 0) { s_cnt[warp * 2] = __popc(occ[0]); s_cnt[warp * 2 + 1] = __popc(occ[1]); }
+            }
         }
         if (failed) {
             if (tid == 0) J.status[w] = GV_ERR_TIMEOUT;
@@ -488,51 +509,9 @@ __global__ void __launch_bounds__(kTcBlock, 1) k_statspin_tc(DevJob J, int mode)
             parity ^= 1u;
         }
         tmem_fence_after();
-        // epilogue.  (1) which sites each flavour occupies (a ballot over the
-        // sites, counted per warp), for the lists of occupied sites in
-        // increasing order built in (3)
-        int16_t* srt = reinterpret_cast<int16_t*>(base + lay.srt);   // [fl][site | particle][kTcM]
-        int* s_cnt = reinterpret_cast<int*>(srt + 4 * kTcM);          // [warp][fl]
-        int fk[2] = {-1, -1};
-        unsigned occ[2] = {0u, 0u};
-        if (worker) {
-            if (tid < Ns) {
-                fk[0] = J.fock[size_t(w) * 2 * Ns + tid];
-                fk[1] = J.fock[(size_t(w) * 2 + 1) * Ns + tid];
-            }
-            // only particle indices that address V are listed
-            occ[0] = __ballot_sync(0xffffffffu, fk[0] >= 0 && fk[0] < N);
-            occ[1] = __ballot_sync(0xffffffffu, fk[1] >= 0 && fk[1] < N);
-            if (lane == 0) { s_cnt[warp * 2] = __popc(occ[0]); s_cnt[warp * 2 + 1] = __popc(occ[1]); }
-        }
-        // (2) warp -> TMEM lanes 32 (warp % 4) .. +31 (rows c), 16-column chunks
-        // of q split between the two warps of a lane group; the pair ratios
-        // r(c, q) go to V[c][q ^ (c % 16)] in the tile region (the XOR spreads
-        // a column's rows over the banks)
-        cx<float>* V = reinterpret_cast<cx<float>*>(base);
-        {
-            const int lg = warp & 3, c = 32 * lg + lane;
-            for (int cc = warp >> 2; worker && cc < Nt / 16; cc += 2) {
-                uint32_t r[64];
-                const uint32_t ta = tbase + (uint32_t(32 * lg) << 16) + uint32_t(16 * cc);
-                tmem_ld16(ta, r);
-                tmem_ld16(ta + 128, r + 16);
-                tmem_ld16(ta + 256, r + 32);
-                tmem_ld16(ta + 384, r + 48);
-                tmem_wait_ld(r);
-                if (c < N) {
-#pragma unroll
-                    for (int t = 0; t < 16; ++t) {
-                        const cx<float> gu = {__uint_as_float(r[t]), __uint_as_float(r[16 + t])};
-                        const cx<float> gd = {__uint_as_float(r[32 + t]), __uint_as_float(r[48 + t])};
-                        V[c * Nt + ((16 * cc + t) ^ (c & 15))] = cmul_rn(gu, gd);
-                    }
-                }
-            }
-        }
-        tmem_fence_before();
-        __syncthreads();
-        // (3) the sorted lists: site and particle of the k-th occupied site
+        // epilogue.  (1) the sorted site lists: site and particle of the k-th
+        // occupied site of each flavour (the per-warp counts were written at
+        // step 1, before the barriers since)
         if (worker) {
             const unsigned below = (1u << lane) - 1u;
 #pragma unroll
@@ -547,6 +526,37 @@ __global__ void __launch_bounds__(kTcBlock, 1) k_statspin_tc(DevJob J, int mode)
                 }
             }
         }
+        // (2) warp -> TMEM lanes 32 (warp % 4) .. +31 (rows c), 16-column chunks
+        // of q split between the two warps of a lane group; the pair ratios
+        // r(c, q) go to V in the tile region, row c, the pairs (q, q + 1) of
+        // even q at pair slot (q / 2) ^ (c % 8) (the XOR spreads a column's
+        // rows over the banks; a pair is one 16-byte store)
+        cx<float>* V = reinterpret_cast<cx<float>*>(base);
+        {
+            const int lg = warp & 3, c = 32 * lg + lane;
+            for (int cc = warp >> 2; worker && cc < Nt / 16; cc += 2) {
+                uint32_t r[64];
+                const uint32_t ta = tbase + (uint32_t(32 * lg) << 16) + uint32_t(16 * cc);
+                tmem_ld16(ta, r);
+                tmem_ld16(ta + 128, r + 16);
+                tmem_ld16(ta + 256, r + 32);
+                tmem_ld16(ta + 384, r + 48);
+                tmem_wait_ld(r);
+                if (c < N) {
+#pragma unroll
+                    for (int t = 0; t < 16; t += 2) {
+                        const cx<float> v0 = cmul_rn(cx<float>{__uint_as_float(r[t]), __uint_as_float(r[16 + t])},
+                                                     cx<float>{__uint_as_float(r[32 + t]), __uint_as_float(r[48 + t])});
+                        const cx<float> v1 =
+                            cmul_rn(cx<float>{__uint_as_float(r[t + 1]), __uint_as_float(r[17 + t])},
+                                    cx<float>{__uint_as_float(r[33 + t]), __uint_as_float(r[49 + t])});
+                        const int slot = ((16 * cc + t) >> 1) ^ (c & 7);
+                        *reinterpret_cast<float4*>(V + c * Nt + 2 * slot) = make_float4(v0.x, v0.y, v1.x, v1.y);
+                    }
+                }
+            }
+        }
+        tmem_fence_before();
         __syncthreads();
         // (4) pair sums in site order: warp -> up sites a = warp, warp + 8, ...;
         // lane -> down sites b = lane + 32 k, so that one atomic instruction
@@ -572,17 +582,17 @@ __global__ void __launch_bounds__(kTcBlock, 1) k_statspin_tc(DevJob J, int mode)
             for (int a = warp; a < n_up; a += kTcThreads / 32) {
                 const int i = ups[a], c = upp[a];
                 const cx<float>* Vc = V + c * Nt;
-                const int sw = c & 15;
+                const int sw = c & 7;
                 float2* Ti = J.ss32 + size_t(i) * Ns;
                 int nb[4] = {-1, -1, -1, -1};
                 if (mode & 2) {
 #pragma unroll
-                    for (int k = 0; k < 4; ++k) nb[k] = J.nbr[i * 4 + k];
+                    for (int k = 0; k < 4; ++k) nb[k] = s_nbr[i * 4 + k];
                 }
 #pragma unroll
                 for (int k = 0; k < kTcM / 32; ++k) {
                     if (jj[k] < 0) continue;
-                    const cx<float> v = Vc[qq[k] ^ sw];
+                    const cx<float> v = Vc[2 * ((qq[k] >> 1) ^ sw) + (qq[k] & 1)];
                     if (mode & 1)   // FP32 staging sums, folded into the FP64 sums after the launch
                         atomicAdd(Ti + jj[k], make_float2(v.x, v.y));
                     if ((mode & 2) && (jj[k] == nb[0] || jj[k] == nb[1] || jj[k] == nb[2] || jj[k] == nb[3])) {
@@ -790,37 +800,52 @@ __global__ void __launch_bounds__(kTcBlock, 1) k_trans_z_tc(DevJob J, cx<float>*
     if (warp == 0) tmem_dealloc(tbase, 256);
 }
 
-// Occupation bitsets of the walkers still running: bit w % 32 of word
-// [fl][site][w / 32] is set when walker w holds flavour fl at the site.
+// Occupation bitsets of the walkers still running, word-major: bit b of word
+// [fl][k][site] is set when walker 32 k + b holds flavour fl at the site.  One
+// block per word k: the 32 walkers' flavour-0 occupancies are staged in
+// shared memory by coalesced row loads, then thread i packs site i's bits.
+// (Every site of a running walker holds one flavour, so flavour 1's bits are
+// the running walkers without flavour 0.)
+constexpr int kOccMaxNs = 512;
+
 __global__ void k_occ_bits(DevJob J, uint32_t* bits)
 {
-    const int nw = (J.W + 31) / 32;
-    const int idx = blockIdx.x * blockDim.x + threadIdx.x;
-    if (idx >= J.Ns * nw) return;
-    const int i = idx / nw, k = idx % nw;
-    uint32_t u = 0, d = 0;
+    __shared__ int16_t s_f0[32][kOccMaxNs];
+    __shared__ int s_run[32];
+    const int nw = (J.W + 31) / 32, Ns = J.Ns, k = blockIdx.x;
+    if (threadIdx.x < 32) {
+        const int w = 32 * k + threadIdx.x;
+        s_run[threadIdx.x] = w < J.W && J.status[w] == GV_OK;
+    }
     for (int b = 0; b < 32; ++b) {
         const int w = 32 * k + b;
-        if (w >= J.W || J.status[w] != GV_OK) continue;
-        if (J.fock[size_t(w) * 2 * J.Ns + i] >= 0) u |= 1u << b;
-        else d |= 1u << b;
+        if (w >= J.W) break;
+        for (int i = threadIdx.x; i < Ns; i += blockDim.x) s_f0[b][i] = J.fock[size_t(w) * 2 * Ns + i];
     }
-    bits[size_t(i) * nw + k] = u;
-    bits[size_t(J.Ns + i) * nw + k] = d;
+    __syncthreads();
+    for (int i = threadIdx.x; i < Ns; i += blockDim.x) {
+        uint32_t u = 0, d = 0;
+        for (int b = 0; b < 32; ++b) {
+            if (!s_run[b]) continue;
+            if (s_f0[b][i] >= 0) u |= 1u << b;
+            else d |= 1u << b;
+        }
+        bits[size_t(k) * Ns + i] = u;
+        bits[size_t(nw + k) * Ns + i] = d;
+    }
 }
 
 // Aud[i][j] += number of running walkers with flavour 0 at site i and
 // flavour 1 at site j (one thread per entry, so no atomics): the
-// antiparallel counts of StatSpinStruct without one atomic per pair.
+// antiparallel counts of StatSpinStruct without one atomic per pair.  Block
+// i; the flavour-1 words of consecutive sites j are contiguous.
 __global__ void k_occ_pairs(DevJob J, const uint32_t* bits)
 {
     const int nw = (J.W + 31) / 32, Ns = J.Ns, i = blockIdx.x;
     double* Aud = J.ss + 2 * size_t(Ns) * Ns;
-    const uint32_t* U = bits + size_t(i) * nw;
     for (int j = threadIdx.x; j < Ns; j += blockDim.x) {
-        const uint32_t* D = bits + size_t(Ns + j) * nw;
         int c = 0;
-        for (int k = 0; k < nw; ++k) c += __popc(U[k] & D[k]);
+        for (int k = 0; k < nw; ++k) c += __popc(bits[size_t(k) * Ns + i] & bits[size_t(nw + k) * Ns + j]);
         if (c) Aud[size_t(i) * Ns + j] += double(c);
     }
 }
