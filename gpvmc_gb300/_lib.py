@@ -59,7 +59,8 @@ class Result(ctypes.Structure):
     _fields_ = [("state", ctypes.c_int32), ("status", ctypes.c_int32), ("steps", ctypes.c_uint64),
                 ("accepted", ctypes.c_uint64), ("footprint", ctypes.c_uint64), ("e_site", ctypes.c_double),
                 ("stagmagn", ctypes.c_double), ("validation_error", ctypes.c_double), ("t_submit", ctypes.c_double),
-                ("t_admit", ctypes.c_double), ("t_done", ctypes.c_double)]
+                ("t_admit", ctypes.c_double), ("t_done", ctypes.c_double), ("t_started", ctypes.c_double),
+                ("t_walked", ctypes.c_double)]
 
 
 

@@ -274,6 +274,10 @@ void gv_server::run()
             Req* q = starting[i];
             if (q->start_f.wait_for(std::chrono::seconds(0)) != std::future_status::ready) { ++i; continue; }
             const gv_status st = q->start_f.get();
+            {
+                std::lock_guard<std::mutex> lk(m);   // poll() reads the result under the lock
+                q->res.t_started = now();
+            }
             starting.erase(starting.begin() + i);
             if (st) {
                 q->finish_f = std::async(std::launch::async, [this, q, st] { finish(q, st); });
@@ -287,6 +291,10 @@ void gv_server::run()
             Req* q = running[i];
             moved |= advance(q);
             if (q->issued == q->total && q->inflight == 0) {
+                {
+                    std::lock_guard<std::mutex> lk(m);
+                    q->res.t_walked = now();
+                }
                 running.erase(running.begin() + i);
                 const gv_status st = q->res.status;
                 q->finish_f = std::async(std::launch::async, [this, q, st] { finish(q, st); });

@@ -9,7 +9,7 @@ percentiles come from the results themselves.
 
     srv = Server(max_jobs=16, chunk_sweeps=4)
     t = srv.submit(StagFluxGroundState(16, 0.25 * pi, 0.1), walkers=256, sweeps=100, meas=256)
-    r = srv.wait(t)          # dict: e_site, stagmagn, steps, accepted, t_submit, t_admit, t_done, ...
+    r = srv.wait(t)          # dict: e_site, stagmagn, steps, accepted, t_submit, t_admit, t_started, t_walked, t_done, ...
     srv.close()
 """
 import ctypes

@@ -469,6 +469,8 @@ typedef struct {
     double validation_error;  /* validate = 1: ground state max |dE/site| over walkers; exciton
                                  max |H,O - H,O(FP64)| / max |H,O(FP64)|; -1 otherwise */
     double t_submit, t_admit, t_done;   /* seconds since the server started */
+    double t_started;         /* job created and walkers started (FP64 start inversions done) */
+    double t_walked;          /* last walk call of the job complete on the device (0: never walked) */
 } gv_result;
 
 gv_status gv_server_create(const gv_server_config* cfg, gv_server** out);

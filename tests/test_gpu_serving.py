@@ -41,6 +41,7 @@ def test_results_same_alone_and_in_the_mix(engine):
     for r in mixed:
         assert r["state"] == 2 and r["status"] == 0
         assert r["t_submit"] <= r["t_admit"] <= r["t_done"]
+        assert r["t_admit"] <= r["t_started"] <= r["t_walked"] <= r["t_done"]
         assert np.isfinite(r["e_site"]) and r["steps"] > 0
     # jobs overlapped on the device: some job was admitted before another finished
     admits = sorted(r["t_admit"] for r in mixed)
