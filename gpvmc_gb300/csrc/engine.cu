@@ -468,6 +468,15 @@ bool trans_z_tc_ok(const gv_job* j)
            j->N[0] <= kTcMaxK && !(j->cfg.flags & GV_FLAG_SCALAR_PAIRS);
 }
 
+// Tensor-core overlap sums of the longitudinal measurement: mixed, N <= 128,
+// the Z buffer (W x 2 x 2 Ns x Ns complex FP32) at most 8 GB.
+bool long_z_tc_ok(const gv_job* j)
+{
+    return j->lng && j->cfg.precision == GV_PREC_MIXED && j->N[0] == j->N[1] && j->N[0] <= kTcM &&
+           j->Ns <= kOccMaxNs && size_t(j->W) * 4 * j->Ns * j->Ns * sizeof(cx<float>) <= (size_t(8) << 30) &&
+           !(j->cfg.flags & GV_FLAG_SCALAR_PAIRS);
+}
+
 // Tensor-core StatSpinStruct: mixed ground state with N_0 = N_1 <= 128.
 bool statspin_tc_ok(const gv_job* j)
 {
@@ -655,10 +664,23 @@ gv_status launch_measure_long(gv_job* j, int mask)
 {
     constexpr int NT = 256;
     const LongMeasLayout lay = long_meas_layout<T, NT>(j->Ns, j->Nmax, j->ch.Nexc);
+    const cx<float>* zpre = nullptr;
+    if (sizeof(T) == 4 && j->d.zbuf && (mask & GV_MEAS_PROJHEIS)) {   // the bonds' Z on the tensor cores first
+        const TcLayout zl = tc_layout_lz(j->N[0]);
+        GV_CK(raise_smem_limit(k_long_z_tc, zl.total));
+        int zs;
+        GV_CK(mark_begin(j, 2, &zs));
+        k_long_z_tc<<<std::min(j->W, j->n_sm), kTcBlock, zl.total, j->stream>>>(j->d, j->d.zbuf);
+        GV_CK(cudaGetLastError());
+        GV_CK(mark_end(j, zs));
+        ++j->last_launches;
+        ++j->total_launches;
+        zpre = j->d.zbuf;
+    }
     GV_CK(raise_smem_limit(k_measure_long<T, NT>, lay.total));
     int slot;
     GV_CK(mark_begin(j, 2, &slot));
-    k_measure_long<T, NT><<<j->W, NT, lay.total, j->stream>>>(j->d, mask);
+    k_measure_long<T, NT><<<j->W, NT, lay.total, j->stream>>>(j->d, mask, zpre);
     GV_CK(cudaGetLastError());
     GV_CK(mark_end(j, slot));
     ++j->last_launches;
@@ -1161,6 +1183,8 @@ gv_status gv_job_footprint(const gv_job_config* c, uint64_t* bytes)
         b += W * 2 * Nmax * Ns * es;         // overlap table R of both flavours
         b += W * (2 * Ns + 2 * Nmax) * 2;    // wavefunction Fock state
         b += W * 2 * Nexc * Nexc * 16;       // ProjHeis H and O sums
+        if (c->precision == GV_PREC_MIXED && Ns / 2 <= uint64_t(kTcM) && W * 4 * Ns * Ns * 8 <= (uint64_t(8) << 30))
+            b += W * 4 * Ns * Ns * 8;        // tensor-core overlap sums of the bonds
     }
     *bytes = b;
     return GV_OK;
@@ -1339,6 +1363,8 @@ gv_status gv_job_create(const gv_job_config* cfg, gv_job** out)
             (st = dalloc(j, &d.pjx, size_t(j->W) * 2 * Nexc * Nexc * sizeof(cx<double>))))
             return fail(st);
         if (trans_z_tc_ok(j) && (st = dalloc(j, &d.zbuf, size_t(j->W) * j->N[1] * Nexc * sizeof(cx<float>))))
+            return fail(st);
+        if (long_z_tc_ok(j) && (st = dalloc(j, &d.zbuf, size_t(j->W) * 4 * j->Ns * j->Ns * sizeof(cx<float>))))
             return fail(st);
         if (j->cfg.precision != GV_PREC_FP64 &&
             ((st = dalloc(j, &d.pxs, size_t(j->W) * kHoSlots * 3 * Nexc * sizeof(cx<float>))) ||

@@ -711,8 +711,11 @@ __device__ __forceinline__ void long_load(const DevJob& J, int w, const LongMeas
 //     h_k = a_k (npar - nanti) / 4 - S_k / 2,
 //     H[k1][k2] += conj(a_k1) h_k2 / w,  O[k1][k2] += conj(a_k1) a_k2 / w,
 // w = sum_k |a_k|^2, as the transverse channel's measurement.
+//
+// zpre (mixed form, or null): the bonds' overlap sums Z[w][fl][b][o] from the
+// tensor cores (k_long_z_tc), in place of the sums formed here from R.
 template <typename T, int NT>
-__global__ void __launch_bounds__(NT) k_measure_long(DevJob J, int mask)
+__global__ void __launch_bounds__(NT) k_measure_long(DevJob J, int mask, const cx<float>* zpre)
 {
     extern __shared__ __align__(16) char smem[];
     constexpr int NW = NT / 32;
@@ -794,19 +797,27 @@ __global__ void __launch_bounds__(NT) k_measure_long(DevJob J, int mask)
         cx<T>* s_Zb = reinterpret_cast<cx<T>*>(smem + lay.Zb);
         const int N = J.N[0], Nk = J.Nk;
         const cx<T>* phase = Tab<T>::phase(J);
+        bool zt = false;   // Z of every bond precomputed
+        if constexpr (sizeof(T) == 4) zt = zpre != nullptr;
         for (int b0 = 0; b0 < nanti; b0 += kLongBonds) {
             const int nb = nanti - b0 < kLongBonds ? nanti - b0 : kLongBonds;
             // the new columns C of the batch's bonds (as long_stage forms them)
-            for (int idx = tid; idx < nb * 2 * N; idx += NT) {
+            for (int idx = tid; !zt && idx < nb * 2 * N; idx += NT) {
                 const int j = idx / (2 * N), fl = (idx / N) & 1, f = idx % N;
                 const int code = s_bl[b0 + j], s0 = code & 0xFFFF, t0 = code >> 16;
                 const int t = fl ? s0 : t0;
                 s_Cb[(j * 2 + fl) * Nmax + f] = phi_orb<T>(phase, s_coef + fl * 2 * Ns, Nk, Ns, L, t, s_worb[fl * Nmax + f]);
             }
             __syncthreads();
+            if constexpr (sizeof(T) == 4) {   // the batch's precomputed sums into shared memory (coalesced)
+                for (int idx = tid; zt && idx < nb * 2 * Ns; idx += NT) {
+                    const int j = idx / (2 * Ns), fl = (idx / Ns) & 1, o = idx % Ns;
+                    s_Zb[idx] = zpre[((size_t(w) * 2 + fl) * 2 * Ns + (b0 + j)) * Ns + o];
+                }
+            }
             // Z_o = sum_f R[f][o] C[f] of every bond of the batch in one pass over R
             // (each sum in the order long_stage takes it)
-            for (int idx = tid; idx < 2 * Ns; idx += NT) {
+            for (int idx = tid; !zt && idx < 2 * Ns; idx += NT) {
                 const int fl = idx / Ns, o = idx % Ns;
                 const cx<T>* R = D[fl].R;
                 cx<T> z[kLongBonds];

@@ -45,6 +45,7 @@ constexpr int kTcThreads = 256;          // operand-building threads (warps 0..7
 constexpr int kTcBlock = kTcThreads + 32; // + one warp that only issues the MMAs
 constexpr int kTcIssuer = kTcThreads;     // its elected thread
 constexpr int kTcM = 128;                 // MMA rows (up particles, zero padded)
+constexpr int kOccMaxNs = 512;            // sites of the occupancy kernels and the bond lists
 
 __host__ __device__ inline int tc_ncols(int N) { return (N + 15) & ~15; }
 
@@ -800,13 +801,212 @@ __global__ void __launch_bounds__(kTcBlock, 1) k_trans_z_tc(DevJob J, cx<float>*
     if (warp == 0) tmem_dealloc(tbase, 256);
 }
 
+// ---- Longitudinal-exciton overlap sums on the tensor cores (mixed) ----
+// The longitudinal ProjHeis needs, for every antiparallel bond b (flavour 0
+// moving s0 -> t0, flavour 1 t0 -> s0) and every orbital o of each flavour,
+//     Z_b[fl][o] = sum_f R_fl[f][o] C_b,fl[f],   C_b,fl[f] = phi_{worb_fl[f]}(t_b,fl)
+// (t_b,0 = t0, t_b,1 = s0): the Z_o of linalg::DetUpdate's capacitance
+// matrices (linalg.cpp:107-400) for all bonds at once, per walker and flavour
+// an (Ns x N) x (N x nanti) complex product.  Same split-TF32 scheme and
+// pipeline as k_trans_z_tc: A = R_fl^T (rows o, 128 per tile, K = f), B = the
+// bonds' new columns (rows b, 128 per chunk), one accumulator pair in TMEM
+// (256 columns, lane = o).  The bonds are listed in creation order
+// (SquareLattice.cpp:9-28), as k_measure_long lists them.  Output
+// Z[w][fl][b][o] (FP32, o fastest, b < 2 Ns) for k_measure_long.
+__host__ __device__ inline TcLayout tc_layout_lz(int N)
+{
+    TcLayout l;
+    size_t o = 0;
+    const size_t t = size_t(kTcM) * 128;
+    for (int i = 0; i < 4; ++i) { l.a[i] = o; o += t; }
+    for (int i = 0; i < 4; ++i) { l.b[i] = o; o += t; }
+    l.site = o;   // [fl][bond] new site of the flavour's moving particle, then [fl][f] phase column of row f
+    o += sizeof(int16_t) * 2 * (2 * kOccMaxNs + kTcM);
+    l.coef = o;   // [fl][sub][f] coefficient of row f's orbital
+    o += sizeof(cx<float>) * 2 * 2 * kTcM;
+    l.bar = o;
+    o += 8;
+    l.tbase = o;
+    o += 8;
+    l.red = o;    // per-warp bond counts
+    o += sizeof(int) * (kTcBlock / 32 + 1);
+    l.srt = l.nbr = 0;
+    l.total = o + 1024;
+    (void)N;
+    return l;
+}
+
+__global__ void __launch_bounds__(kTcBlock, 1) k_long_z_tc(DevJob J, cx<float>* Z)
+{
+    extern __shared__ __align__(16) char smem_raw[];
+    const uint32_t raw = smem_addr(smem_raw);
+    char* base = smem_raw + ((1024u - (raw & 1023u)) & 1023u);
+    const uint32_t sbase = smem_addr(base);
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int N = J.N[0], Ns = J.Ns, L = J.L, Nk = J.Nk, Nmax = J.Nmax, Bmax = 2 * Ns;
+    const TcLayout lay = tc_layout_lz(N);
+    int16_t* s_bs = reinterpret_cast<int16_t*>(base + lay.site);   // [fl][b]
+    int16_t* s_pcol = s_bs + 2 * 2 * kOccMaxNs;                     // [fl][f]
+    cx<float>* s_cf = reinterpret_cast<cx<float>*>(base + lay.coef);   // [fl][sub][f]
+    uint64_t* s_bar = reinterpret_cast<uint64_t*>(base + lay.bar);
+    uint32_t* s_tbase = reinterpret_cast<uint32_t*>(base + lay.tbase);
+    int* s_cnt = reinterpret_cast<int*>(base + lay.red);
+    const uint32_t bar = smem_addr(s_bar);
+
+    if (warp == 0) tmem_alloc(s_tbase, 256);
+    if (tid == 0) {
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(bar) : "memory");
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    tmem_fence_before();
+    __syncthreads();
+    tmem_fence_after();
+    const uint32_t tbase = *s_tbase;
+    const uint32_t idesc = tc_idesc(kTcM);
+    const int KC = (N + 31) / 32;
+    const int MT = (Ns + kTcM - 1) / kTcM;   // orbital tiles
+    uint32_t parity = 0;
+    bool failed = false;
+    const bool worker = tid < kTcThreads;   // the issuing warp builds no operands
+    int nanti = 0;
+
+    // the walker's bond list (all threads; ends synchronised) and row tables
+    auto tables = [&](int w) {
+        nanti = 0;
+        for (int e0 = 0; e0 < Bmax; e0 += kTcBlock) {
+            const int e = e0 + tid;
+            bool anti = false;
+            int s0 = 0, t0 = 0;
+            if (e < Bmax) {
+                const int4 E = J.edges[e];
+                const bool ua = J.fock[size_t(w) * 2 * Ns + E.x] >= 0, ub = J.fock[size_t(w) * 2 * Ns + E.y] >= 0;
+                anti = ua != ub;
+                s0 = ua ? E.x : E.y;
+                t0 = ua ? E.y : E.x;
+            }
+            const unsigned bal = __ballot_sync(0xffffffffu, anti);
+            if (lane == 0) s_cnt[warp] = __popc(bal);
+            __syncthreads();
+            int off = nanti, tot = 0;
+            for (int q = 0; q < kTcBlock / 32; ++q) {
+                if (q < warp) off += s_cnt[q];
+                tot += s_cnt[q];
+            }
+            if (anti) {
+                const int b = off + __popc(bal & ((1u << lane) - 1u));
+                s_bs[b] = int16_t(t0);                  // flavour 0 moves s0 -> t0
+                s_bs[2 * kOccMaxNs + b] = int16_t(s0);  // flavour 1 moves t0 -> s0
+            }
+            nanti += tot;
+            __syncthreads();
+        }
+        const cx<float>* cg = J.coef32 + size_t(w) * 4 * Ns;   // [fl][sub][orbital]
+        for (int i = tid; i < 2 * N; i += kTcBlock) {
+            const int fl = i / N, f = i % N;
+            const int o = J.worb[(size_t(w) * 2 + fl) * Nmax + f];
+            s_pcol[fl * kTcM + f] = int16_t(o >> 1);
+            s_cf[(fl * 2 + 0) * kTcM + f] = cg[(size_t(fl) * 2 + 0) * Ns + o];
+            s_cf[(fl * 2 + 1) * kTcM + f] = cg[(size_t(fl) * 2 + 1) * Ns + o];
+        }
+        __syncthreads();
+    };
+    // pass p = (fl, bond chunk bc, orbital tile mt), mt fastest
+    auto pass_of = [&](int p, int& fl, int& bc, int& mt) {
+        const int nbc = (nanti + kTcM - 1) / kTcM;
+        mt = p % MT;
+        bc = (p / MT) % nbc;
+        fl = p / (MT * nbc);
+    };
+    auto fetch = [&](TcRegs& R, int w, int p, int kc) {
+        if (!worker) return;
+        int fl, bc, mt;
+        pass_of(p, fl, bc, mt);
+        const cx<float>* Rf = static_cast<const cx<float>*>(J.gup) + (size_t(w) * 2 + fl) * size_t(Nmax) * Ns;
+        tc_load_rows(R, Rf + mt * kTcM, Ns, min(kTcM, Ns - mt * kTcM), N, kTcM, kc);
+        tc_load_phase_cols(R, J.phase32, Nk, s_bs + fl * 2 * kOccMaxNs + bc * kTcM, s_pcol + fl * kTcM,
+                           min(kTcM, nanti - bc * kTcM), N, kTcM, kc);
+    };
+
+    TcRegs R;
+    for (int w = blockIdx.x; w < J.W && !failed; w += gridDim.x) {
+        if (J.status[w] != GV_OK) continue;
+        tables(w);
+        const int P = 2 * ((nanti + kTcM - 1) / kTcM) * MT;   // passes of this walker
+        if (P == 0) continue;
+        fetch(R, w, 0, 0);
+        bool first = true;
+        for (int p = 0; p < P && !failed; ++p) {
+            int fl, bc, mt;
+            pass_of(p, fl, bc, mt);
+            const int nr = min(kTcM, nanti - bc * kTcM);
+            for (int kc = 0; kc < KC; ++kc) {
+                if (!first) {   // the previous chunk's MMAs are done with the tiles
+                    const bool ok = mbar_wait(bar, parity, J.wait_limit);
+                    if (__syncthreads_or(!ok)) { failed = true; break; }
+                    parity ^= 1u;
+                }
+                first = false;
+                if (worker) {
+                    tc_store_inverse(base, lay.a, R, kTcM);
+                    tc_store_phi_cols(base, lay.b, R, s_cf + fl * 2 * kTcM, kTcM, s_bs + fl * 2 * kOccMaxNs + bc * kTcM,
+                                      nr, N, L, kTcM, kc);
+                }
+                asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+                tmem_fence_before();
+                __syncthreads();
+                if (tid == kTcIssuer) {
+                    tmem_fence_after();
+                    tc_issue_chunk(tbase, 0u, sbase, lay, idesc, kc == 0);
+                    tc_commit(bar);
+                }
+                if (kc + 1 < KC) fetch(R, w, p, kc + 1);
+                else if (p + 1 < P) fetch(R, w, p + 1, 0);
+            }
+            if (failed) break;
+            {
+                const bool ok = mbar_wait(bar, parity, J.wait_limit);
+                if (__syncthreads_or(!ok)) { failed = true; break; }
+                parity ^= 1u;
+            }
+            tmem_fence_after();
+            // epilogue: lane o of TMEM -> Z[w][fl][b][o], 16 bonds at a time
+            const int lg = warp & 3, o = mt * kTcM + 32 * lg + lane;
+            cx<float>* Zw = Z + (size_t(w) * 2 + fl) * size_t(Bmax) * Ns;
+            for (int cc = warp >> 2; worker && cc < kTcM / 16; cc += 2) {
+                if (16 * cc >= nr) break;
+                uint32_t r[32];
+                const uint32_t ta = tbase + (uint32_t(32 * lg) << 16) + uint32_t(16 * cc);
+                tmem_ld16(ta, r);
+                tmem_ld16(ta + 128, r + 16);
+                tmem_wait_ld(r);
+                if (o < Ns) {
+#pragma unroll
+                    for (int t = 0; t < 16; ++t) {
+                        const int bl = 16 * cc + t;
+                        if (bl < nr)
+                            Zw[size_t(bc * kTcM + bl) * Ns + o] = cx<float>{__uint_as_float(r[t]), __uint_as_float(r[16 + t])};
+                    }
+                }
+            }
+            tmem_fence_before();
+            first = true;   // the next pass's first MMAs follow the __syncthreads of its first chunk
+        }
+        if (failed && tid == 0) J.status[w] = GV_ERR_TIMEOUT;
+        __syncthreads();   // the tables of the next walker
+    }
+    if (failed) mbar_wait(bar, parity);   // the phase that timed out: MMAs in flight finish before TMEM is freed
+    tmem_fence_before();
+    __syncthreads();
+    tmem_fence_after();
+    if (warp == 0) tmem_dealloc(tbase, 256);
+}
+
 // Occupation bitsets of the walkers still running, word-major: bit b of word
 // [fl][k][site] is set when walker 32 k + b holds flavour fl at the site.  One
 // block per word k: the 32 walkers' flavour-0 occupancies are staged in
 // shared memory by coalesced row loads, then thread i packs site i's bits.
 // (Every site of a running walker holds one flavour, so flavour 1's bits are
 // the running walkers without flavour 0.)
-constexpr int kOccMaxNs = 512;
 
 __global__ void k_occ_bits(DevJob J, uint32_t* bits)
 {

@@ -82,11 +82,13 @@ typedef int32_t gv_status;
                                      pair (the nearest-neighbour pairs are the bonds) instead
                                      of the per-particle FP32 dot products in the walk kernel;
                                      GV_ERR_INVALID at creation where it does not apply */
-#define GV_FLAG_SCALAR_PAIRS 16   /* mixed precision: StatSpinStruct pair ratios (ground state)
-                                     and the exciton ProjHeis overlap rows Z = GupT^T Phi from
-                                     FP32 dot products on the CUDA cores instead of split-TF32
-                                     tensor-core products (the tensor-core forms run by default
-                                     when N_0 = N_1 <= 128, resp. Nexc, N_1 <= 128, N_0 <= 160) */
+#define GV_FLAG_SCALAR_PAIRS 16   /* mixed precision: StatSpinStruct pair ratios (ground state),
+                                     the transverse exciton's ProjHeis overlap rows
+                                     Z = GupT^T Phi and the longitudinal exciton's bond overlap
+                                     sums Z_b = R^T C_b from FP32 dot products on the CUDA cores
+                                     instead of split-TF32 tensor-core products (the tensor-core
+                                     forms run by default when N_0 = N_1 <= 128, resp.
+                                     Nexc, N_1 <= 128, N_0 <= 160, resp. N_0 = N_1 <= 128) */
 
 #define GV_MEAS_PROJHEIS 1    /* ProjHeis (ProjHeis.cpp:40-158), Bx = 0 */
 #define GV_MEAS_STAGMAGN 2    /* StagMagnZ (StagMagnZ.cpp:12-43) */

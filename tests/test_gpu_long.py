@@ -236,3 +236,41 @@ def test_long_mixed_vs_fp64(engine, L, q):
     print("long exciton H/O error vs FP64: median %.2e max %.2e" % (np.median(err), err.max()))
     assert np.median(err) < 1e-4 and err.max() < 1e-2
     assert mixed.drift().max() < 1e-3
+
+
+@pytest.mark.parametrize("L,q", [(8, (4, 4)), (16, (8, 8)), (16, (0, 0))])
+def test_long_overlap_sums_on_tensor_cores(engine, L, q):
+    """Longitudinal ProjHeis with the bonds' overlap sums Z_b = R^T C_b from
+    split-TF32 tensor-core products (k_long_z_tc) against the FP32 CUDA-core
+    sums (scalar_pairs) on the same FP32 state, and against the FP64 engine on
+    the same configurations (H and O depend on the configuration only)."""
+    W = 12
+    wav = engine.StagFluxLongExciton(L, PHI, 0.1, q=q)
+    mk = lambda prec, **kw: engine.Job(wav, walkers=W, seed=23, precision=prec, reinv_every=L * L,
+                                       deferred_reinversion=True, **kw)
+    j0 = mk("mixed")
+    j0.set_measurements(1)
+    j0.init_walkers()
+    j0.walk(L * L * 3, 0)
+    assert (j0.status() == 0).all()
+    cfg = j0.config()
+    j0.close()
+    out = []
+    for j in (mk("mixed"), mk("mixed", scalar_pairs=True), mk("fp64")):
+        j.set_measurements(1)
+        j.init_walkers(cfg)
+        j.reset_quantities()
+        j.measure()
+        pj, n = j.projheis()
+        assert (n == 1).all() and (j.status() == 0).all()
+        out.append(pj)
+        j.close()
+    pt, ps, p64 = out
+    scale = np.abs(p64).max(axis=(1, 2))
+    e_ts = np.abs(pt - ps).max(axis=(1, 2)) / scale
+    e_t64 = np.abs(pt - p64).max(axis=(1, 2)) / scale
+    e_s64 = np.abs(ps - p64).max(axis=(1, 2)) / scale
+    print("long H/O: tensor vs CUDA cores median %.2e max %.2e; vs FP64 median %.2e max %.2e (CUDA cores %.2e)"
+          % (np.median(e_ts), e_ts.max(), np.median(e_t64), e_t64.max(), np.median(e_s64)))
+    assert np.median(e_ts) < 2e-5 and e_ts.max() < 1e-3
+    assert np.median(e_t64) < 1e-4 and e_t64.max() < 1e-2
