@@ -640,6 +640,7 @@ __global__ void __launch_bounds__(NT) k_walk_long(DevJob J, uint64_t nsteps, int
 
 // Shared-memory pieces of the measurement and VirtUpdate kernels.
 constexpr int kLongBonds = 8;   // bonds whose overlap sums Z share one pass over R in a measurement
+constexpr int kLongZBonds = 4;  // bonds staged together when the sums come from the tensor cores
 
 struct LongMeasLayout {
     size_t fock, part, wslot, worb, exu, exd, pre, coef, rowc, del, C, Z, pt, dd, S, a, hh, f32, bl, Cb, Zb, red, total;
@@ -798,26 +799,94 @@ __global__ void __launch_bounds__(NT) k_measure_long(DevJob J, int mask, const c
         const int N = J.N[0], Nk = J.Nk;
         const cx<T>* phase = Tab<T>::phase(J);
         bool zt = false;   // Z of every bond precomputed
-        if constexpr (sizeof(T) == 4) zt = zpre != nullptr;
-        for (int b0 = 0; b0 < nanti; b0 += kLongBonds) {
+        if constexpr (sizeof(T) == 4) {
+            zt = zpre != nullptr;
+            if (zt) {
+                // Bonds in batches of kLongZBonds: per batch one staging pass
+                // (Z rows copied in, phi_o(t) and phi_o(t) - phi_o(s) of every
+                // orbital, the moving particles' inverse rows and M11 with a
+                // warp per bond and flavour), one barrier, then every state's
+                // ratio for every bond of the batch.  The batch arrays reuse the
+                // buffers of the per-bond form: Z and phi(t) rows over Zb,
+                // phi(t) - phi(s) over Cb, inverse rows and deltas over
+                // rowc .. dd (contiguous), M11 over the reduction scratch.
+                constexpr int NBZ = kLongZBonds;
+                cx<float>* ZB = s_Zb;
+                cx<float>* ptB = s_Zb + NBZ * 2 * Ns;
+                cx<float>* ddB = s_Cb;
+                cx<float>* rowcB = s_rowc;
+                cx<float>* delB = s_rowc + NBZ * 2 * Nmax;
+                cx<float>* m11B = reinterpret_cast<cx<float>*>(s_red);
+                for (int b0 = 0; b0 < nanti; b0 += NBZ) {
+                    const int nb = nanti - b0 < NBZ ? nanti - b0 : NBZ;
+                    for (int idx = tid; idx < nb * 2 * Ns; idx += NT) {
+                        const int j = idx / (2 * Ns), fl = (idx / Ns) & 1, o = idx % Ns;
+                        const int code = s_bl[b0 + j], s0 = code & 0xFFFF, t0 = code >> 16;
+                        const int sf = fl ? t0 : s0, tf = fl ? s0 : t0;
+                        const cx<float>* cf = s_coef + fl * 2 * Ns;
+                        ZB[idx] = zpre[((size_t(w) * 2 + fl) * 2 * Ns + (b0 + j)) * Ns + o];
+                        const cx<float> pt = phi_orb<float>(phase, cf, Nk, Ns, L, tf, o);
+                        ptB[idx] = pt;
+                        ddB[idx] = pt - phi_orb<float>(phase, cf, Nk, Ns, L, sf, o);
+                    }
+                    for (int seg = warp; seg < nb * 2; seg += NW) {
+                        const int j = seg >> 1, fl = seg & 1;
+                        const int code = s_bl[b0 + j], s0 = code & 0xFFFF, t0 = code >> 16;
+                        const int sf = fl ? t0 : s0, tf = fl ? s0 : t0;
+                        const int c = max(int(s_fock[fl * Ns + sf]), 0);   // the exchange moves a particle of each flavour
+                        const cx<float>* cf = s_coef + fl * 2 * Ns;
+                        const cx<float>* ai = ai_ptr<float>(J, fl, w);
+                        cx<float> acc = {0.f, 0.f};
+                        for (int f = lane; f < N; f += 32) {
+                            const int o = s_worb[fl * Nmax + f];
+                            const cx<float> a = ai[size_t(f) * N + c];
+                            const cx<float> C = phi_orb<float>(phase, cf, Nk, Ns, L, tf, o);
+                            rowcB[seg * Nmax + f] = a;
+                            delB[seg * Nmax + f] = C - phi_orb<float>(phase, cf, Nk, Ns, L, sf, o);
+                            cmac(acc, a, C);
+                        }
+                        acc = warp_sum(acc);
+                        if (lane == 0) m11B[seg] = acc;
+                    }
+                    __syncthreads();
+                    for (int k = tid; k < Nexc; k += NT) {
+                        cx<double> sk = {0.0, 0.0};
+                        for (int j = 0; j < nb; ++j) {
+                            LongFl<float> Dj[2] = {D[0], D[1]};
+                            for (int fl = 0; fl < 2; ++fl) {
+                                const int seg = j * 2 + fl;
+                                Dj[fl].rowc = rowcB + seg * Nmax;
+                                Dj[fl].del = delB + seg * Nmax;
+                                Dj[fl].Z = ZB + seg * Ns;
+                                Dj[fl].pt = ptB + seg * Ns;
+                                Dj[fl].dd = ddB + seg * Ns;
+                                Dj[fl].M11 = m11B[seg];
+                                Dj[fl].moved = true;
+                            }
+                            const cx<double> q = to_d(long_state_ratio<float>(Dj, cur, k, s_exu, s_exd, s_pre, Ns, nullptr));
+                            sk.x += q.x;
+                            sk.y += q.y;
+                        }
+                        s_S[k].x += sk.x;
+                        s_S[k].y += sk.y;
+                    }
+                    __syncthreads();   // the next batch restages
+                }
+            }
+        }
+        for (int b0 = 0; !zt && b0 < nanti; b0 += kLongBonds) {
             const int nb = nanti - b0 < kLongBonds ? nanti - b0 : kLongBonds;
             // the new columns C of the batch's bonds (as long_stage forms them)
-            for (int idx = tid; !zt && idx < nb * 2 * N; idx += NT) {
+            for (int idx = tid; idx < nb * 2 * N; idx += NT) {
                 const int j = idx / (2 * N), fl = (idx / N) & 1, f = idx % N;
                 const int code = s_bl[b0 + j], s0 = code & 0xFFFF, t0 = code >> 16;
                 const int t = fl ? s0 : t0;
                 s_Cb[(j * 2 + fl) * Nmax + f] = phi_orb<T>(phase, s_coef + fl * 2 * Ns, Nk, Ns, L, t, s_worb[fl * Nmax + f]);
             }
             __syncthreads();
-            if constexpr (sizeof(T) == 4) {   // the batch's precomputed sums into shared memory (coalesced)
-                for (int idx = tid; zt && idx < nb * 2 * Ns; idx += NT) {
-                    const int j = idx / (2 * Ns), fl = (idx / Ns) & 1, o = idx % Ns;
-                    s_Zb[idx] = zpre[((size_t(w) * 2 + fl) * 2 * Ns + (b0 + j)) * Ns + o];
-                }
-            }
             // Z_o = sum_f R[f][o] C[f] of every bond of the batch in one pass over R
             // (each sum in the order long_stage takes it)
-            for (int idx = tid; !zt && idx < 2 * Ns; idx += NT) {
+            for (int idx = tid; idx < 2 * Ns; idx += NT) {
                 const int fl = idx / Ns, o = idx % Ns;
                 const cx<T>* R = D[fl].R;
                 cx<T> z[kLongBonds];
