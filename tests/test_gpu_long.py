@@ -274,3 +274,43 @@ def test_long_overlap_sums_on_tensor_cores(engine, L, q):
           % (np.median(e_ts), e_ts.max(), np.median(e_t64), e_t64.max(), np.median(e_s64)))
     assert np.median(e_ts) < 2e-5 and e_ts.max() < 1e-3
     assert np.median(e_t64) < 1e-4 and e_t64.max() < 1e-2
+
+
+def test_long_overlap_sums_bounded_wait(engine):
+    """The tensor-core bond sums' mbarrier waits are bounded: with a poll
+    budget of zero every wait gives up at once, the walkers reached report
+    GV_ERR_TIMEOUT (a host-visible status; the MMAs issued finish before the
+    kernel frees its tensor memory) and are skipped by the measurement; the
+    same job measures normally again with the default budget, as a fresh job
+    on the same configurations does."""
+    L, W = 8, 12
+    wav = engine.StagFluxLongExciton(L, PHI, 0.1, q=(4, 4))
+    mk = lambda: engine.Job(wav, walkers=W, seed=29, precision="mixed", reinv_every=L * L,
+                            deferred_reinversion=True)
+    job = mk()
+    job.set_measurements(1)
+    job.init_walkers()
+    job.walk(L * L * 2, 0)
+    cfg = job.config()
+    job.reset_quantities()
+    job.set_wait_limit(0)
+    with pytest.raises(engine.GvError) as err:
+        job.measure()
+    assert err.value.status == 6
+    st = job.status()
+    assert (st == 6).any() and set(st.tolist()) <= {0, 6}
+    job.set_wait_limit(-1)
+    job.init_walkers(cfg)                 # clears the statuses, fresh FP64 inverses
+    job.reset_quantities()
+    job.measure()
+    got, n = job.projheis()
+    assert (n == 1).all() and (job.status() == 0).all()
+    ref = mk()
+    ref.set_measurements(1)
+    ref.init_walkers(cfg)
+    ref.reset_quantities()
+    ref.measure()
+    want, _ = ref.projheis()
+    assert np.array_equal(got, want)
+    job.close()
+    ref.close()
