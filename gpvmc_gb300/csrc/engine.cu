@@ -46,6 +46,10 @@ struct gv_job {
     int N[2] = {0, 0};
     cudaStream_t stream = nullptr;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    // tensor-core StatSpinStruct: the antiparallel counts run on a second
+    // stream beside the pair kernel (forked from and joined back into stream)
+    cudaStream_t side = nullptr;
+    cudaEvent_t fork_ev = nullptr, join_ev = nullptr;
     DevJob d{};
     std::vector<void*> allocs;
     bool ready = false;
@@ -493,14 +497,24 @@ gv_status statspin_dispatch(gv_job* j, int mode = 1)
         GV_CK(raise_smem_limit(k_statspin_tc, lay.total));
         int slot;
         GV_CK(mark_begin(j, 2, &slot));
-        if (mode & 1) {   // antiparallel counts from occupation bitsets
-            k_occ_bits<<<(j->W + 31) / 32, 256, 0, j->stream>>>(j->d, j->d.occ);
-            k_occ_pairs<<<j->Ns, 256, 0, j->stream>>>(j->d, j->d.occ);
+        const bool side = (mode & 1) && j->side;
+        if (mode & 1) {   // antiparallel counts from occupation bitsets (Aud: no overlap with the pair sums)
+            cudaStream_t s = j->stream;
+            if (side) {   // beside the pair kernel, which holds one CTA per SM
+                GV_CK(cudaEventRecord(j->fork_ev, j->stream));
+                GV_CK(cudaStreamWaitEvent(j->side, j->fork_ev, 0));
+                s = j->side;
+            }
+            k_occ_bits<<<(j->W + 31) / 32, 256, 0, s>>>(j->d, j->d.occ);
+            k_occ_pairs<<<j->Ns, 256, 0, s>>>(j->d, j->d.occ);
+            GV_CK(cudaGetLastError());
+            if (side) GV_CK(cudaEventRecord(j->join_ev, j->side));
             j->last_launches += 2;
             j->total_launches += 2;
         }
         k_statspin_tc<<<std::min(j->W, j->n_sm), kTcBlock, lay.total, j->stream>>>(j->d, mode);
         GV_CK(cudaGetLastError());
+        if (side) GV_CK(cudaStreamWaitEvent(j->stream, j->join_ev, 0));   // joined before anything reads the sums
         if (mode & 1) {
             k_fold_ss<<<j->n_sm, 256, 0, j->stream>>>(j->d);
             GV_CK(cudaGetLastError());
@@ -1297,6 +1311,16 @@ gv_status gv_job_create(const gv_job_config* cfg, gv_job** out)
         }
     }
     if (cudaStreamCreateWithFlags(&j->stream, cudaStreamNonBlocking) != cudaSuccess) { delete j; return GV_ERR_CUDA; }
+    if (statspin_tc_ok(j) &&   // created here: a measurement may run under stream capture
+        (cudaStreamCreateWithFlags(&j->side, cudaStreamNonBlocking) != cudaSuccess ||
+         cudaEventCreateWithFlags(&j->fork_ev, cudaEventDisableTiming) != cudaSuccess ||
+         cudaEventCreateWithFlags(&j->join_ev, cudaEventDisableTiming) != cudaSuccess)) {
+        if (j->side) cudaStreamDestroy(j->side);
+        if (j->fork_ev) cudaEventDestroy(j->fork_ev);
+        cudaStreamDestroy(j->stream);
+        delete j;
+        return GV_ERR_CUDA;
+    }
     if (cudaEventCreate(&j->ev0) != cudaSuccess || cudaEventCreate(&j->ev1) != cudaSuccess) return fail(GV_ERR_CUDA);
 
     DevJob& d = j->d;
@@ -1403,6 +1427,9 @@ gv_status gv_job_destroy(gv_job* j)
     if (j->tev1) cudaEventDestroy(j->tev1);
     if (j->ev1) cudaEventDestroy(j->ev1);
     if (j->stream) cudaStreamDestroy(j->stream);
+    if (j->side) cudaStreamDestroy(j->side);
+    if (j->fork_ev) cudaEventDestroy(j->fork_ev);
+    if (j->join_ev) cudaEventDestroy(j->join_ev);
     delete j;
     return GV_OK;
 }
