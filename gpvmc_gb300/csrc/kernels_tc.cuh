@@ -455,6 +455,7 @@ __global__ void __launch_bounds__(kTcBlock, 1) k_statspin_tc(DevJob J, int mode)
         int* s_cnt = reinterpret_cast<int*>(srt + 4 * kTcM);          // [warp][fl]
         int fk[2] = {-1, -1};
         unsigned occ[2] = {0u, 0u};
+        int qn[4] = {-1, -1, -1, -1};   // ProjHeis only: down particle at each neighbour of row c's site, or -1
         for (int step = 0; step < 2 * KC; ++step) {
             const int gm = step / KC, kc = step % KC;
             if (!first) {   // the previous chunk's MMAs are done with the tiles
@@ -490,6 +491,18 @@ __global__ void __launch_bounds__(kTcBlock, 1) k_statspin_tc(DevJob J, int mode)
                 fk[0] = J.fock[size_t(w) * 2 * Ns + tid];
                 fk[1] = J.fock[(size_t(w) * 2 + 1) * Ns + tid];
             }
+            if (step == 0 && worker && mode == 2) {   // ProjHeis only: the down particles next to row c's site
+                const int c = 32 * (warp & 3) + lane;
+                const int si = c < N ? st[c] : -1;
+#pragma unroll
+                for (int k = 0; k < 4; ++k) {
+                    const int v = si >= 0 ? s_nbr[si * 4 + k] : -1;
+                    bool dup = false;
+#pragma unroll
+                    for (int k2 = 0; k2 < k; ++k2) dup = dup || (si >= 0 && s_nbr[si * 4 + k2] == v);
+                    qn[k] = (v >= 0 && !dup) ? J.fock[(size_t(w) * 2 + 1) * Ns + v] : -1;
+                }
+            }
             if (step == 1 && worker) {   // only particle indices that address V are listed
                 occ[0] = __ballot_sync(0xffffffffu, fk[0] >= 0 && fk[0] < N);
                 occ[1] = __ballot_sync(0xffffffffu, fk[1] >= 0 && fk[1] < N);
@@ -510,30 +523,104 @@ __global__ void __launch_bounds__(kTcBlock, 1) k_statspin_tc(DevJob J, int mode)
             parity ^= 1u;
         }
         tmem_fence_after();
-        // epilogue.  (1) the sorted site lists: site and particle of the k-th
-        // occupied site of each flavour (the per-warp counts were written at
-        // step 1, before the barriers since)
-        if (worker) {
-            const unsigned below = (1u << lane) - 1u;
-#pragma unroll
-            for (int fl = 0; fl < 2; ++fl) {
-                if ((occ[fl] >> lane) & 1u) {
-                    int off = __popc(occ[fl] & below);
-                    for (int q = 0; q < warp; ++q) off += s_cnt[q * 2 + fl];
-                    if (off < kTcM) {
-                        srt[fl * 2 * kTcM + off] = int16_t(tid);
-                        srt[fl * 2 * kTcM + kTcM + off] = int16_t(fk[fl]);
+        cx<double> eb = {0.0, 0.0};   // sum of the bond ratios of this thread's pairs
+        int nanti = 0;
+        if (mode != 2) {   // StatSpinStruct (and ProjHeis from the same pairs)
+            // epilogue.  (1) the sorted site lists: site and particle of the k-th
+            // occupied site of each flavour (the per-warp counts were written at
+            // step 1, before the barriers since)
+            if (worker) {
+                const unsigned below = (1u << lane) - 1u;
+    #pragma unroll
+                for (int fl = 0; fl < 2; ++fl) {
+                    if ((occ[fl] >> lane) & 1u) {
+                        int off = __popc(occ[fl] & below);
+                        for (int q = 0; q < warp; ++q) off += s_cnt[q * 2 + fl];
+                        if (off < kTcM) {
+                            srt[fl * 2 * kTcM + off] = int16_t(tid);
+                            srt[fl * 2 * kTcM + kTcM + off] = int16_t(fk[fl]);
+                        }
                     }
                 }
             }
-        }
-        // (2) warp -> TMEM lanes 32 (warp % 4) .. +31 (rows c), 16-column chunks
-        // of q split between the two warps of a lane group; the pair ratios
-        // r(c, q) go to V in the tile region, row c, the pairs (q, q + 1) of
-        // even q at pair slot (q / 2) ^ (c % 8) (the XOR spreads a column's
-        // rows over the banks; a pair is one 16-byte store)
-        cx<float>* V = reinterpret_cast<cx<float>*>(base);
-        {
+            // (2) warp -> TMEM lanes 32 (warp % 4) .. +31 (rows c), 16-column chunks
+            // of q split between the two warps of a lane group; the pair ratios
+            // r(c, q) go to V in the tile region, row c, the pairs (q, q + 1) of
+            // even q at pair slot (q / 2) ^ (c % 8) (the XOR spreads a column's
+            // rows over the banks; a pair is one 16-byte store)
+            cx<float>* V = reinterpret_cast<cx<float>*>(base);
+            {
+                const int lg = warp & 3, c = 32 * lg + lane;
+                for (int cc = warp >> 2; worker && cc < Nt / 16; cc += 2) {
+                    uint32_t r[64];
+                    const uint32_t ta = tbase + (uint32_t(32 * lg) << 16) + uint32_t(16 * cc);
+                    tmem_ld16(ta, r);
+                    tmem_ld16(ta + 128, r + 16);
+                    tmem_ld16(ta + 256, r + 32);
+                    tmem_ld16(ta + 384, r + 48);
+                    tmem_wait_ld(r);
+                    if (c < N) {
+    #pragma unroll
+                        for (int t = 0; t < 16; t += 2) {
+                            const cx<float> v0 = cmul_rn(cx<float>{__uint_as_float(r[t]), __uint_as_float(r[16 + t])},
+                                                         cx<float>{__uint_as_float(r[32 + t]), __uint_as_float(r[48 + t])});
+                            const cx<float> v1 =
+                                cmul_rn(cx<float>{__uint_as_float(r[t + 1]), __uint_as_float(r[17 + t])},
+                                        cx<float>{__uint_as_float(r[33 + t]), __uint_as_float(r[49 + t])});
+                            const int slot = ((16 * cc + t) >> 1) ^ (c & 7);
+                            *reinterpret_cast<float4*>(V + c * Nt + 2 * slot) = make_float4(v0.x, v0.y, v1.x, v1.y);
+                        }
+                    }
+                }
+            }
+            tmem_fence_before();
+            __syncthreads();
+            // (4) pair sums in site order: warp -> up sites a = warp, warp + 8, ...;
+            // lane -> down sites b = lane + 32 k, so that one atomic instruction
+            // covers 32 increasing sites of one row of the table
+            if (worker) {
+                const int16_t* ups = srt;
+                const int16_t* upp = srt + kTcM;
+                const int16_t* dns = srt + 2 * kTcM;
+                const int16_t* dnp = srt + 3 * kTcM;
+                int n_up = 0, n_dn = 0;   // entries written for this walker (N each for a consistent state)
+                for (int q = 0; q < kTcThreads / 32; ++q) { n_up += s_cnt[q * 2]; n_dn += s_cnt[q * 2 + 1]; }
+                n_up = min(n_up, kTcM);
+                n_dn = min(n_dn, kTcM);
+                int jj[kTcM / 32], qq[kTcM / 32];
+    #pragma unroll
+                for (int k = 0; k < kTcM / 32; ++k) {
+                    const int bq = lane + 32 * k;
+                    jj[k] = bq < n_dn ? dns[bq] : -1;
+                    qq[k] = bq < n_dn ? dnp[bq] : 0;
+                }
+                for (int a = warp; a < n_up; a += kTcThreads / 32) {
+                    const int i = ups[a], c = upp[a];
+                    const cx<float>* Vc = V + c * Nt;
+                    const int sw = c & 7;
+                    float2* Ti = J.ss32 + size_t(i) * Ns;
+                    int nb[4] = {-1, -1, -1, -1};
+                    if (mode & 2) {
+    #pragma unroll
+                        for (int k = 0; k < 4; ++k) nb[k] = s_nbr[i * 4 + k];
+                    }
+    #pragma unroll
+                    for (int k = 0; k < kTcM / 32; ++k) {
+                        if (jj[k] < 0) continue;
+                        const cx<float> v = Vc[2 * ((qq[k] >> 1) ^ sw) + (qq[k] & 1)];
+                        if (mode & 1)   // FP32 staging sums, folded into the FP64 sums after the launch
+                            atomicAdd(Ti + jj[k], make_float2(v.x, v.y));
+                        if ((mode & 2) && (jj[k] == nb[0] || jj[k] == nb[1] || jj[k] == nb[2] || jj[k] == nb[3])) {
+                            eb.x += f32_to_f64(v.x);
+                            eb.y += f32_to_f64(v.y);
+                            ++nanti;
+                        }
+                    }
+                }
+            }
+        } else {
+            // ProjHeis only: the thread of row c takes its up particle's
+            // antiparallel bonds (columns qn) straight out of the TMEM loads
             const int lg = warp & 3, c = 32 * lg + lane;
             for (int cc = warp >> 2; worker && cc < Nt / 16; cc += 2) {
                 uint32_t r[64];
@@ -545,64 +632,20 @@ __global__ void __launch_bounds__(kTcBlock, 1) k_statspin_tc(DevJob J, int mode)
                 tmem_wait_ld(r);
                 if (c < N) {
 #pragma unroll
-                    for (int t = 0; t < 16; t += 2) {
-                        const cx<float> v0 = cmul_rn(cx<float>{__uint_as_float(r[t]), __uint_as_float(r[16 + t])},
-                                                     cx<float>{__uint_as_float(r[32 + t]), __uint_as_float(r[48 + t])});
-                        const cx<float> v1 =
-                            cmul_rn(cx<float>{__uint_as_float(r[t + 1]), __uint_as_float(r[17 + t])},
-                                    cx<float>{__uint_as_float(r[33 + t]), __uint_as_float(r[49 + t])});
-                        const int slot = ((16 * cc + t) >> 1) ^ (c & 7);
-                        *reinterpret_cast<float4*>(V + c * Nt + 2 * slot) = make_float4(v0.x, v0.y, v1.x, v1.y);
+                    for (int t = 0; t < 16; ++t) {
+                        const int q = 16 * cc + t;
+                        if (q == qn[0] || q == qn[1] || q == qn[2] || q == qn[3]) {
+                            const cx<float> v =
+                                cmul_rn(cx<float>{__uint_as_float(r[t]), __uint_as_float(r[16 + t])},
+                                        cx<float>{__uint_as_float(r[32 + t]), __uint_as_float(r[48 + t])});
+                            eb.x += f32_to_f64(v.x);
+                            eb.y += f32_to_f64(v.y);
+                            ++nanti;
+                        }
                     }
                 }
             }
-        }
-        tmem_fence_before();
-        __syncthreads();
-        // (4) pair sums in site order: warp -> up sites a = warp, warp + 8, ...;
-        // lane -> down sites b = lane + 32 k, so that one atomic instruction
-        // covers 32 increasing sites of one row of the table
-        cx<double> eb = {0.0, 0.0};   // sum of the bond ratios of this thread's pairs
-        int nanti = 0;
-        if (worker) {
-            const int16_t* ups = srt;
-            const int16_t* upp = srt + kTcM;
-            const int16_t* dns = srt + 2 * kTcM;
-            const int16_t* dnp = srt + 3 * kTcM;
-            int n_up = 0, n_dn = 0;   // entries written for this walker (N each for a consistent state)
-            for (int q = 0; q < kTcThreads / 32; ++q) { n_up += s_cnt[q * 2]; n_dn += s_cnt[q * 2 + 1]; }
-            n_up = min(n_up, kTcM);
-            n_dn = min(n_dn, kTcM);
-            int jj[kTcM / 32], qq[kTcM / 32];
-#pragma unroll
-            for (int k = 0; k < kTcM / 32; ++k) {
-                const int bq = lane + 32 * k;
-                jj[k] = bq < n_dn ? dns[bq] : -1;
-                qq[k] = bq < n_dn ? dnp[bq] : 0;
-            }
-            for (int a = warp; a < n_up; a += kTcThreads / 32) {
-                const int i = ups[a], c = upp[a];
-                const cx<float>* Vc = V + c * Nt;
-                const int sw = c & 7;
-                float2* Ti = J.ss32 + size_t(i) * Ns;
-                int nb[4] = {-1, -1, -1, -1};
-                if (mode & 2) {
-#pragma unroll
-                    for (int k = 0; k < 4; ++k) nb[k] = s_nbr[i * 4 + k];
-                }
-#pragma unroll
-                for (int k = 0; k < kTcM / 32; ++k) {
-                    if (jj[k] < 0) continue;
-                    const cx<float> v = Vc[2 * ((qq[k] >> 1) ^ sw) + (qq[k] & 1)];
-                    if (mode & 1)   // FP32 staging sums, folded into the FP64 sums after the launch
-                        atomicAdd(Ti + jj[k], make_float2(v.x, v.y));
-                    if ((mode & 2) && (jj[k] == nb[0] || jj[k] == nb[1] || jj[k] == nb[2] || jj[k] == nb[3])) {
-                        eb.x += f32_to_f64(v.x);
-                        eb.y += f32_to_f64(v.y);
-                        ++nanti;
-                    }
-                }
-            }
+            tmem_fence_before();
         }
         if (mode & 2) {   // the walker's ProjHeis sample
 #pragma unroll
