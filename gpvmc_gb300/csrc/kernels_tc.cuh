@@ -348,6 +348,15 @@ __device__ __forceinline__ void tc_issue_chunk(uint32_t tbase, uint32_t dcol, ui
 // one) while the MMAs run.  The epilogue of a walker follows its last chunk;
 // the per-walker tables (sites, coefficients) are double-buffered so that the
 // next walker's first rows can be fetched before it.
+// The walkers after w that a CTA gives up before reaching (a bounded wait ran
+// out on walker w): marked GV_ERR_TIMEOUT as well, so that no later kernel of
+// the measurement reads results that were never written.  Called by one thread.
+__device__ __forceinline__ void tc_mark_rest(const DevJob& J, int w)
+{
+    for (int r = w + int(gridDim.x); r < J.W; r += gridDim.x)
+        if (J.status[r] == GV_OK) J.status[r] = GV_ERR_TIMEOUT;
+}
+
 __device__ __forceinline__ int tc_next_walker(const DevJob& J, int w)
 {
     for (w += gridDim.x; w < J.W; w += gridDim.x)
@@ -672,6 +681,7 @@ __global__ void __launch_bounds__(kTcBlock, 1) k_statspin_tc(DevJob J, int mode)
         w = wn;
         b ^= 1;
     }
+    if (failed && tid == 0) tc_mark_rest(J, w);
     if (failed) mbar_wait(bar, parity);   // the phase that timed out: MMAs in flight finish before TMEM is freed
     tmem_fence_before();
     __syncthreads();
@@ -837,6 +847,7 @@ __global__ void __launch_bounds__(kTcBlock, 1) k_trans_z_tc(DevJob J, cx<float>*
         w = wn;
         b ^= 1;
     }
+    if (failed && tid == 0) tc_mark_rest(J, w);
     if (failed) mbar_wait(bar, parity);
     tmem_fence_before();
     __syncthreads();
@@ -971,6 +982,7 @@ __global__ void __launch_bounds__(kTcBlock, 1) k_long_z_tc(DevJob J, cx<float>* 
     };
 
     TcRegs R;
+    int wf = -1;   // the walker whose wait ran out
     for (int w = blockIdx.x; w < J.W && !failed; w += gridDim.x) {
         if (J.status[w] != GV_OK) continue;
         tables(w);
@@ -1034,9 +1046,13 @@ __global__ void __launch_bounds__(kTcBlock, 1) k_long_z_tc(DevJob J, cx<float>* 
             tmem_fence_before();
             first = true;   // the next pass's first MMAs follow the __syncthreads of its first chunk
         }
-        if (failed && tid == 0) J.status[w] = GV_ERR_TIMEOUT;
+        if (failed) {
+            wf = w;
+            if (tid == 0) J.status[w] = GV_ERR_TIMEOUT;
+        }
         __syncthreads();   // the tables of the next walker
     }
+    if (failed && tid == 0) tc_mark_rest(J, wf);
     if (failed) mbar_wait(bar, parity);   // the phase that timed out: MMAs in flight finish before TMEM is freed
     tmem_fence_before();
     __syncthreads();

@@ -278,11 +278,12 @@ def test_long_overlap_sums_on_tensor_cores(engine, L, q):
 
 def test_long_overlap_sums_bounded_wait(engine):
     """The tensor-core bond sums' mbarrier waits are bounded: with a poll
-    budget of zero every wait gives up at once, the walkers reached report
-    GV_ERR_TIMEOUT (a host-visible status; the MMAs issued finish before the
-    kernel frees its tensor memory) and are skipped by the measurement; the
-    same job measures normally again with the default budget, as a fresh job
-    on the same configurations does."""
+    budget of zero every wait gives up at once; the walker each CTA was on,
+    and those it did not reach, report GV_ERR_TIMEOUT (a host-visible status;
+    the MMAs issued finish before the kernel frees its tensor memory) and are
+    skipped by the measurement, so no unwritten sums are read; the same job
+    measures normally again with the default budget, as a fresh job on the
+    same configurations does."""
     L, W = 8, 12
     wav = engine.StagFluxLongExciton(L, PHI, 0.1, q=(4, 4))
     mk = lambda: engine.Job(wav, walkers=W, seed=29, precision="mixed", reinv_every=L * L,

@@ -113,10 +113,11 @@ def test_exciton_overlap_rows_on_tensor_cores(engine, oracle, L, q):
 
 def test_bounded_wait_gives_up_with_a_status(engine, oracle):
     """The tensor-core kernel's mbarrier waits are bounded: with a poll budget
-    of zero every wait gives up at once, the walkers it reached report
-    GV_ERR_TIMEOUT (host-visible status, no hang, no fault: the MMAs issued
-    still finish before the kernel frees its tensor memory), and the same job
-    then measures normally again with the default budget."""
+    of zero every wait gives up at once, the walker each CTA was on and those
+    it did not reach report GV_ERR_TIMEOUT (host-visible status, no hang, no
+    fault: the MMAs issued still finish before the kernel frees its tensor
+    memory), and the same job then measures normally again with the default
+    budget."""
     L, W = 8, 24
     job = _mixed(engine, L, W, 3)
     job.init_walkers()
@@ -181,3 +182,40 @@ def test_tensor_core_projheis_rejected_where_it_does_not_apply(engine):
         engine.Job(engine.StagFluxGroundState(8, PHI, 0.1), walkers=2, seed=1, precision="fp64", tc_projheis=True)
     with pytest.raises(engine.GvError):
         engine.Job(engine.StagFluxGroundState(20, PHI, 0.1), walkers=2, seed=1, precision="mixed", tc_projheis=True)
+
+
+def test_exciton_overlap_rows_bounded_wait(engine, oracle):
+    """The transverse exciton's tensor-core overlap rows (k_trans_z_tc) give up
+    at a zero poll budget with GV_ERR_TIMEOUT on the walker each CTA was on and
+    on those it did not reach, so the measurement reads no unwritten rows; the
+    job measures as a fresh one afterwards."""
+    L, W = 8, 12
+    wav = engine.StagFluxTransExciton(L, PHI, 0.1, q=(4, 4))
+    mk = lambda: engine.Job(wav, walkers=W, seed=31, precision="mixed", reinv_every=64, deferred_reinversion=True)
+    job = mk()
+    job.init_walkers()
+    job.walk(L * L * 2, 0)
+    cfg = job.config()
+    job.set_measurements(oracle.MEAS_PROJHEIS)
+    job.reset_quantities()
+    job.set_wait_limit(0)
+    with pytest.raises(engine.GvError) as err:
+        job.measure()
+    assert err.value.status == 6
+    st = job.status()
+    assert (st == 6).all()   # one walker per CTA here (W < SMs): every walker's wait ran out
+    job.set_wait_limit(-1)
+    job.init_walkers(cfg)
+    job.reset_quantities()
+    job.measure()
+    got, n = job.projheis()
+    assert (n == 1).all() and (job.status() == 0).all()
+    ref = mk()
+    ref.init_walkers(cfg)
+    ref.set_measurements(oracle.MEAS_PROJHEIS)
+    ref.reset_quantities()
+    ref.measure()
+    want, _ = ref.projheis()
+    assert np.array_equal(got, want)
+    job.close()
+    ref.close()
