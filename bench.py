@@ -826,6 +826,38 @@ def serving_requests(g, n=SERVE_JOBS, scale=SERVE_SWEEP_SCALE):
     return reqs
 
 
+def serving_phases(reqs, res):
+    """Where each request's time went (host clock): queue (submitted ->
+    admitted), start (job creation, walker start, FP64 start inversions),
+    walk (the walk calls, sharing the device with the other admitted jobs),
+    retire (final reads, summary, FP64 validation, teardown); means by L and
+    channel over the requests that finished without error, and the share of
+    the admitted time (start + walk + retire) each phase took overall."""
+    phases = {}
+    for (t, q), r in zip(reqs, res):
+        if r["status"] != 0:
+            continue
+        key = "L%d_%s" % (q["wav"].L, "gs" if q["wav"].channel == "groundstate" else "trans")
+        d = phases.setdefault(key, {"jobs": 0, "queue_s": 0.0, "start_s": 0.0, "walk_s": 0.0, "retire_s": 0.0,
+                                    "steps": 0})
+        d["jobs"] += 1
+        d["queue_s"] += r["t_admit"] - r["t_submit"]
+        d["start_s"] += r["t_started"] - r["t_admit"]
+        d["walk_s"] += r["t_walked"] - r["t_started"]
+        d["retire_s"] += r["t_done"] - r["t_walked"]
+        d["steps"] += r["steps"]
+    tot = {k: sum(d[k] for d in phases.values()) for k in ("queue_s", "start_s", "walk_s", "retire_s")}
+    for d in phases.values():
+        n = d["jobs"]
+        d["walk_steps_per_s"] = d["steps"] / d["walk_s"] if d["walk_s"] > 0 else None
+        for k in ("queue_s", "start_s", "walk_s", "retire_s"):
+            d[k] /= n
+        d["steps_per_job"] = d.pop("steps") / n
+    busy = tot["start_s"] + tot["walk_s"] + tot["retire_s"]
+    share = {k: tot[k] / busy for k in ("start_s", "walk_s", "retire_s")} if busy > 0 else None
+    return phases, share
+
+
 def run_serving(g):
     import numpy as np
     reqs = serving_requests(g)
@@ -853,31 +885,7 @@ def run_serving(g):
     # sweeps): the stream kept the device saturated (queue p99 above), so its
     # steps/s is the mix's service capacity, and a queue stays bounded while
     # rate x mean steps per request < capacity.
-    # where a request's time goes (host clock): queue (submitted -> admitted),
-    # start (job creation, walker start, FP64 start inversions), walk (the
-    # walk calls, sharing the device with the other admitted jobs), retire
-    # (final reads, summary, FP64 validation, job teardown); by L and channel
-    phases = {}
-    for (t, q), r in zip(reqs, res):
-        if r["status"] != 0:
-            continue
-        key = "L%d_%s" % (q["wav"].L, "gs" if q["wav"].channel == "groundstate" else "trans")
-        d = phases.setdefault(key, {"jobs": 0, "queue_s": 0.0, "start_s": 0.0, "walk_s": 0.0, "retire_s": 0.0,
-                                    "steps": 0})
-        d["jobs"] += 1
-        d["queue_s"] += r["t_admit"] - r["t_submit"]
-        d["start_s"] += r["t_started"] - r["t_admit"]
-        d["walk_s"] += r["t_walked"] - r["t_started"]
-        d["retire_s"] += r["t_done"] - r["t_walked"]
-        d["steps"] += r["steps"]
-    for d in phases.values():
-        n = d["jobs"]
-        d["walk_steps_per_s"] = d["steps"] / d["walk_s"] if d["walk_s"] > 0 else None
-        for k in ("queue_s", "start_s", "walk_s", "retire_s"):
-            d[k] /= n
-        d["steps_per_job"] = d.pop("steps") / n
-    tot = {k: sum(d[k] * d["jobs"] for d in phases.values()) for k in ("queue_s", "start_s", "walk_s", "retire_s")}
-    busy = sum(tot[k] for k in ("start_s", "walk_s", "retire_s"))
+    phases, share = serving_phases(reqs, res)
     unscaled = serving_requests(g, n=4000, scale=1)
     mean_steps = float(np.mean([q["walkers"] * (q["sweeps"] + q["therm_sweeps"]) * q["wav"].L ** 2
                                 for _, q in unscaled]))
@@ -895,7 +903,7 @@ def run_serving(g):
             "exciton_ho_error_vs_fp64_max": max(tr_err) if tr_err else None,
             "validated_jobs": len(gs_err) + len(tr_err),
             "phases_by_L": phases,
-            "admitted_time_share": {k: tot[k] / busy for k in ("start_s", "walk_s", "retire_s")} if busy > 0 else None,
+            "admitted_time_share": share,
             "unscaled": {"mean_steps_per_request": mean_steps,
                          "sustained_rate_jobs_per_s": cap / mean_steps,
                          "rate_at_80pct_load_jobs_per_s": 0.8 * cap / mean_steps,

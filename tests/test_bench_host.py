@@ -56,3 +56,32 @@ def test_no_sampler(bench):
 def test_measured_peaks(bench):
     peak, kind = bench.measured_peaks()
     assert peak > 0 and kind in ("measured", "fallback")
+
+
+def test_serving_phases(bench):
+    """The serving stream's per-request phase split: means by lattice size and
+    channel, failed requests left out, shares of the admitted time."""
+    class Wav:
+        def __init__(self, L, channel):
+            self.L, self.channel = L, channel
+
+    def req(L, ch):
+        return (0.0, {"wav": Wav(L, ch)})
+
+    def res(sub, adm, sta, wal, don, steps, status=0):
+        return {"status": status, "t_submit": sub, "t_admit": adm, "t_started": sta, "t_walked": wal,
+                "t_done": don, "steps": steps}
+
+    reqs = [req(8, "groundstate"), req(8, "groundstate"), req(16, "trans"), req(16, "trans")]
+    out = [res(0.0, 1.0, 2.0, 5.0, 6.0, 300), res(1.0, 1.0, 3.0, 4.0, 6.0, 100),
+           res(0.0, 0.5, 1.0, 3.0, 4.0, 400), res(0.0, 0.0, 0.0, 0.0, 0.0, 0, status=6)]
+    phases, share = bench.serving_phases(reqs, out)
+    assert set(phases) == {"L8_gs", "L16_trans"}
+    gs = phases["L8_gs"]
+    assert gs["jobs"] == 2 and gs["queue_s"] == 0.5 and gs["start_s"] == 1.5 and gs["walk_s"] == 2.0
+    assert gs["retire_s"] == 1.5 and gs["steps_per_job"] == 200 and gs["walk_steps_per_s"] == 100.0
+    tr = phases["L16_trans"]
+    assert tr["jobs"] == 1 and tr["walk_s"] == 2.0 and tr["walk_steps_per_s"] == 200.0
+    # admitted time: start 3 + 0.5, walk 4 + 2, retire 3 + 1
+    assert abs(share["start_s"] - 3.5 / 13.5) < 1e-12 and abs(share["walk_s"] - 6.0 / 13.5) < 1e-12
+    assert abs(sum(share.values()) - 1.0) < 1e-12
