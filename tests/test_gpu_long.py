@@ -238,7 +238,7 @@ def test_long_mixed_vs_fp64(engine, L, q):
     assert mixed.drift().max() < 1e-3
 
 
-@pytest.mark.parametrize("L,q", [(8, (4, 4)), (16, (8, 8)), (16, (0, 0))])
+@pytest.mark.parametrize("L,q", [(4, (2, 2)), (8, (4, 4)), (12, (6, 6)), (12, (0, 0)), (16, (8, 8)), (16, (0, 0))])
 def test_long_overlap_sums_on_tensor_cores(engine, L, q):
     """Longitudinal ProjHeis with the bonds' overlap sums Z_b = R^T C_b from
     split-TF32 tensor-core products (k_long_z_tc) against the FP32 CUDA-core
