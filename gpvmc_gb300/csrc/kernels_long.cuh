@@ -278,13 +278,16 @@ __device__ __forceinline__ void long_stage_phi(const DevJob& J, int s0, int t0, 
 
 // Stage one exchange for both flavours: flavour 0 moves from s0 to t0 and
 // flavour 1 from t0 to s0 (rowc, the new column C, delta, phi(t), d, M11,
-// and Z over all orbitals; s_Z == nullptr: Z already staged by the caller).
-// Ends with the CTA synchronised and M11 of both flavours in m11[].
+// and Z; s_Z == nullptr: Z already staged by the caller).  Ends with the CTA
+// synchronised and M11 of both flavours in m11[].  zhole < -1: Z over every
+// orbital; otherwise only where a state's capacitance matrix reads it: the
+// upper-band orbitals (odd, the states' entering orbitals exc_up) of both
+// flavours and, when zhole >= 0, the current state's hole zo in flavour zhole.
 template <typename T, int NT>
 __device__ __forceinline__ void long_stage(const DevJob& J, int w, int s0, int t0, const int16_t* s_fock,
                                            const int16_t* s_worb, const cx<T>* s_coef, cx<T>* s_rowc, cx<T>* s_del,
                                            cx<T>* s_C, cx<T>* s_Z, cx<T>* s_pt, cx<T>* s_dd, double* s_red,
-                                           cx<T> m11[2])
+                                           cx<T> m11[2], int zhole = -2, int zo = -1)
 {
     constexpr int NW = NT / 32;
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
@@ -319,9 +322,11 @@ __device__ __forceinline__ void long_stage(const DevJob& J, int w, int s0, int t
         long_stage_phi<T, NT>(J, s0, t0, s_coef, s_pt, s_dd);
         return;
     }
-    // Z_o = sum_f R[f][o] C[f] for every orbital of both flavours
-    for (int idx = tid; idx < 2 * Ns; idx += NT) {
-        const int fl = idx / Ns, o = idx % Ns;
+    // Z_o = sum_f R[f][o] C[f] for every orbital of both flavours (or the odd ones)
+    const bool sel = zhole >= -1;
+    const int nz = sel ? Ns : 2 * Ns, per = nz / 2;
+    for (int idx = tid; idx < nz; idx += NT) {
+        const int fl = idx / per, o = sel ? 2 * (idx % per) + 1 : idx % Ns;
         const cx<T>* R = static_cast<const cx<T>*>(J.gup) + (size_t(w) * 2 + fl) * size_t(Nmax) * Ns;
         const cx<T>* C = s_C + fl * Nmax;
         cx<T> z = {T(0), T(0)};
@@ -334,7 +339,15 @@ __device__ __forceinline__ void long_stage(const DevJob& J, int w, int s0, int t
             for (int q = 0; q < 4; ++q) cmac(z, r[q], C[f + q]);
         }
         for (; f < N; ++f) cmac(z, R[size_t(f) * Ns + o], C[f]);
-        s_Z[idx] = z;
+        s_Z[fl * Ns + o] = z;
+    }
+    if (zhole >= 0 && warp == NW - 1) {   // the current hole's sum, split over a warp's lanes
+        const cx<T>* R = static_cast<const cx<T>*>(J.gup) + (size_t(w) * 2 + zhole) * size_t(Nmax) * Ns;
+        const cx<T>* C = s_C + zhole * Nmax;
+        cx<T> z = {T(0), T(0)};
+        for (int f = lane; f < N; f += 32) cmac(z, R[size_t(f) * Ns + zo], C[f]);
+        z = warp_sum(z);
+        if (lane == 0) s_Z[zhole * Ns + zo] = z;
     }
     __syncthreads();
     long_stage_phi<T, NT>(J, s0, t0, s_coef, s_pt, s_dd);
@@ -438,7 +451,12 @@ __global__ void __launch_bounds__(NT) k_walk_long(DevJob J, uint64_t nsteps, int
             kind = 1;
             const int s0 = (f1 == 0) ? v1 : v2, t0 = (f1 == 0) ? v2 : v1;
             cx<T> m11[2];
-            long_stage<T, NT>(J, w, s0, t0, s_fock, s_worb, s_coef, s_rowc, s_del, s_C, s_Z, s_pt, s_dd, s_red, m11);
+            // Z where the states read it: the odd orbitals, and the current hole in
+            // the flavour holding the current pair (the update below forms the rest)
+            const int hk = long_kind(cur, Ns);
+            const int zhole = hk < 2 ? hk : -1, zo = hk < 2 ? int(s_exd[cur]) : -1;
+            long_stage<T, NT>(J, w, s0, t0, s_fock, s_worb, s_coef, s_rowc, s_del, s_C, s_Z, s_pt, s_dd, s_red, m11,
+                              zhole, zo);
             D[0].M11 = m11[0];
             D[1].M11 = m11[1];
             // every state's amplitude after the exchange, their weight sum and first arg-max
@@ -541,8 +559,22 @@ __global__ void __launch_bounds__(NT) k_walk_long(DevJob J, uint64_t nsteps, int
                     const int m = h[5];
                     cx<T>* R = static_cast<cx<T>*>(J.gup) + (size_t(w) * 2 + fl) * size_t(Nmax) * Ns;
                     const cx<T> d = s_dd[fl * Ns + o];
+                    cx<T> zv = s_Z[fl * Ns + o];
+                    if (!(o & 1) && !(fl == zhole && o == zo)) {   // an orbital the staging left out
+                        const cx<T>* C = s_C + fl * Nmax;
+                        zv = cx<T>{T(0), T(0)};
+                        int f = 0;
+                        for (; f + 4 <= N; f += 4) {
+                            cx<T> r[4];
+#pragma unroll
+                            for (int q = 0; q < 4; ++q) r[q] = R[size_t(f + q) * Ns + o];
+#pragma unroll
+                            for (int q = 0; q < 4; ++q) cmac(zv, r[q], C[f + q]);
+                        }
+                        for (; f < N; ++f) cmac(zv, R[size_t(f) * Ns + o], C[f]);
+                    }
                     cx<T> X[3];
-                    X[0] = s_Z[fl * Ns + o] + d * D[fl].M11 - s_pt[fl * Ns + o];
+                    X[0] = zv + d * D[fl].M11 - s_pt[fl * Ns + o];
                     for (int j = 0; j < h[0]; ++j) X[1 + j] = R[size_t(h[1 + j]) * Ns + o] + d * s_rowc[fl * Nmax + h[1 + j]];
                     const cx<T>* Bi = s_Bi + 9 * fl;
                     cx<T> be[3];
