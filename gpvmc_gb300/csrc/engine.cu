@@ -473,11 +473,12 @@ bool trans_z_tc_ok(const gv_job* j)
 }
 
 // Tensor-core overlap sums of the longitudinal measurement: mixed, N <= 128,
-// the Z buffer (W x 2 x 2 Ns x Ns complex FP32) at most 8 GB.
+// the Z buffer (W x 2 flavours x 2 Ns bonds x Ns/2 upper-band orbitals,
+// complex FP32) at most 8 GB.
 bool long_z_tc_ok(const gv_job* j)
 {
     return j->lng && j->cfg.precision == GV_PREC_MIXED && j->N[0] == j->N[1] && j->N[0] <= kTcM &&
-           j->Ns <= kOccMaxNs && size_t(j->W) * 4 * j->Ns * j->Ns * sizeof(cx<float>) <= (size_t(8) << 30) &&
+           j->Ns <= kOccMaxNs && size_t(j->W) * 2 * j->Ns * j->Ns * sizeof(cx<float>) <= (size_t(8) << 30) &&
            !(j->cfg.flags & GV_FLAG_SCALAR_PAIRS);
 }
 
@@ -1197,8 +1198,8 @@ gv_status gv_job_footprint(const gv_job_config* c, uint64_t* bytes)
         b += W * 2 * Nmax * Ns * es;         // overlap table R of both flavours
         b += W * (2 * Ns + 2 * Nmax) * 2;    // wavefunction Fock state
         b += W * 2 * Nexc * Nexc * 16;       // ProjHeis H and O sums
-        if (c->precision == GV_PREC_MIXED && Ns / 2 <= uint64_t(kTcM) && W * 4 * Ns * Ns * 8 <= (uint64_t(8) << 30))
-            b += W * 4 * Ns * Ns * 8;        // tensor-core overlap sums of the bonds
+        if (c->precision == GV_PREC_MIXED && Ns / 2 <= uint64_t(kTcM) && W * 2 * Ns * Ns * 8 <= (uint64_t(8) << 30))
+            b += W * 2 * Ns * Ns * 8;        // tensor-core overlap sums of the bonds (upper-band orbitals)
     }
     *bytes = b;
     return GV_OK;
@@ -1388,7 +1389,7 @@ gv_status gv_job_create(const gv_job_config* cfg, gv_job** out)
             return fail(st);
         if (trans_z_tc_ok(j) && (st = dalloc(j, &d.zbuf, size_t(j->W) * j->N[1] * Nexc * sizeof(cx<float>))))
             return fail(st);
-        if (long_z_tc_ok(j) && (st = dalloc(j, &d.zbuf, size_t(j->W) * 4 * j->Ns * j->Ns * sizeof(cx<float>))))
+        if (long_z_tc_ok(j) && (st = dalloc(j, &d.zbuf, size_t(j->W) * 2 * j->Ns * j->Ns * sizeof(cx<float>))))
             return fail(st);
         if (j->cfg.precision != GV_PREC_FP64 &&
             ((st = dalloc(j, &d.pxs, size_t(j->W) * kHoSlots * 3 * Nexc * sizeof(cx<float>))) ||

@@ -843,6 +843,11 @@ __global__ void __launch_bounds__(NT) k_measure_long(DevJob J, int mask, const c
                 // phi(t) - phi(s) over Cb, inverse rows and deltas over
                 // rowc .. dd (contiguous), M11 over the reduction scratch.
                 constexpr int NBZ = kLongZBonds;
+                // the states read Z, phi(t) and phi(t) - phi(s) only at the orbitals
+                // they enter: the upper-band orbitals (odd) and the current hole
+                const int Nh = Ns / 2;
+                const int hk = long_kind(cur, Ns);
+                const int zhole = hk < 2 ? hk : -1, zo = hk < 2 ? int(s_exd[cur]) : -1;
                 cx<float>* ZB = s_Zb;
                 cx<float>* ptB = s_Zb + NBZ * 2 * Ns;
                 cx<float>* ddB = s_Cb;
@@ -851,15 +856,18 @@ __global__ void __launch_bounds__(NT) k_measure_long(DevJob J, int mask, const c
                 cx<float>* m11B = reinterpret_cast<cx<float>*>(s_red);
                 for (int b0 = 0; b0 < nanti; b0 += NBZ) {
                     const int nb = nanti - b0 < NBZ ? nanti - b0 : NBZ;
-                    for (int idx = tid; idx < nb * 2 * Ns; idx += NT) {
-                        const int j = idx / (2 * Ns), fl = (idx / Ns) & 1, o = idx % Ns;
+                    for (int idx = tid; idx < nb * 2 * (Nh + 1); idx += NT) {
+                        const int j = idx / (2 * (Nh + 1)), fl = (idx / (Nh + 1)) & 1, r = idx % (Nh + 1);
+                        if (r == Nh && fl != zhole) continue;   // no hole in this flavour
+                        const int o = r < Nh ? 2 * r + 1 : zo;
                         const int code = s_bl[b0 + j], s0 = code & 0xFFFF, t0 = code >> 16;
                         const int sf = fl ? t0 : s0, tf = fl ? s0 : t0;
                         const cx<float>* cf = s_coef + fl * 2 * Ns;
-                        ZB[idx] = zpre[((size_t(w) * 2 + fl) * 2 * Ns + (b0 + j)) * Ns + o];
+                        const int e = (j * 2 + fl) * Ns + o;
+                        if (r < Nh) ZB[e] = zpre[((size_t(w) * 2 + fl) * 2 * Ns + (b0 + j)) * Nh + r];
                         const cx<float> pt = phi_orb<float>(phase, cf, Nk, Ns, L, tf, o);
-                        ptB[idx] = pt;
-                        ddB[idx] = pt - phi_orb<float>(phase, cf, Nk, Ns, L, sf, o);
+                        ptB[e] = pt;
+                        ddB[e] = pt - phi_orb<float>(phase, cf, Nk, Ns, L, sf, o);
                     }
                     for (int seg = warp; seg < nb * 2; seg += NW) {
                         const int j = seg >> 1, fl = seg & 1;
@@ -868,7 +876,8 @@ __global__ void __launch_bounds__(NT) k_measure_long(DevJob J, int mask, const c
                         const int c = max(int(s_fock[fl * Ns + sf]), 0);   // the exchange moves a particle of each flavour
                         const cx<float>* cf = s_coef + fl * 2 * Ns;
                         const cx<float>* ai = ai_ptr<float>(J, fl, w);
-                        cx<float> acc = {0.f, 0.f};
+                        const cx<float>* Rh = fl == zhole ? D[fl].R + zo : nullptr;   // the hole's column of R
+                        cx<float> acc = {0.f, 0.f}, zh = {0.f, 0.f};
                         for (int f = lane; f < N; f += 32) {
                             const int o = s_worb[fl * Nmax + f];
                             const cx<float> a = ai[size_t(f) * N + c];
@@ -876,9 +885,14 @@ __global__ void __launch_bounds__(NT) k_measure_long(DevJob J, int mask, const c
                             rowcB[seg * Nmax + f] = a;
                             delB[seg * Nmax + f] = C - phi_orb<float>(phase, cf, Nk, Ns, L, sf, o);
                             cmac(acc, a, C);
+                            if (Rh) cmac(zh, Rh[size_t(f) * Ns], C);
                         }
                         acc = warp_sum(acc);
                         if (lane == 0) m11B[seg] = acc;
+                        if (Rh) {   // Z at the hole, which the tensor-core sums leave out
+                            zh = warp_sum(zh);
+                            if (lane == 0) ZB[seg * Ns + zo] = zh;
+                        }
                     }
                     __syncthreads();
                     for (int k = tid; k < Nexc; k += NT) {

@@ -140,9 +140,10 @@ struct TcRegs {
     cx<float> ph[kTcItems][4];    // orbital operand: phase[site r][f]
 };
 
-// Rows r < nr of a matrix stored K-major in memory, M[f][r] at M + f ld + r,
+// Rows r < nr of a matrix stored K-major in memory, M[f][r] at M + f ld + r rs,
 // K values f < nk (zero elsewhere).
-__device__ __forceinline__ void tc_load_rows(TcRegs& R, const cx<float>* M, int ld, int nr, int nk, int rows, int kc)
+__device__ __forceinline__ void tc_load_rows(TcRegs& R, const cx<float>* M, int ld, int nr, int nk, int rows, int kc,
+                                             int rs = 1)
 {
 #pragma unroll
     for (int i = 0; i < kTcItems; ++i) {
@@ -150,7 +151,7 @@ __device__ __forceinline__ void tc_load_rows(TcRegs& R, const cx<float>* M, int 
 #pragma unroll
         for (int t = 0; t < 4; ++t) {
             const int f = 32 * kc + 4 * u + t;
-            R.inv[i][t] = (it < rows * 8 && r < nr && f < nk) ? M[size_t(f) * ld + r] : cx<float>{0.f, 0.f};
+            R.inv[i][t] = (it < rows * 8 && r < nr && f < nk) ? M[size_t(f) * ld + size_t(r) * rs] : cx<float>{0.f, 0.f};
         }
     }
 }
@@ -861,12 +862,15 @@ __global__ void __launch_bounds__(kTcBlock, 1) k_trans_z_tc(DevJob J, cx<float>*
 //     Z_b[fl][o] = sum_f R_fl[f][o] C_b,fl[f],   C_b,fl[f] = phi_{worb_fl[f]}(t_b,fl)
 // (t_b,0 = t0, t_b,1 = s0): the Z_o of linalg::DetUpdate's capacitance
 // matrices (linalg.cpp:107-400) for all bonds at once, per walker and flavour
-// an (Ns x N) x (N x nanti) complex product.  Same split-TF32 scheme and
-// pipeline as k_trans_z_tc: A = R_fl^T (rows o, 128 per tile, K = f), B = the
-// bonds' new columns (rows b, 128 per chunk), one accumulator pair in TMEM
-// (256 columns, lane = o).  The bonds are listed in creation order
-// (SquareLattice.cpp:9-28), as k_measure_long lists them.  Output
-// Z[w][fl][b][o] (FP32, o fastest, b < 2 Ns) for k_measure_long.
+// an (Ns/2 x N) x (N x nanti) complex product over the upper-band orbitals
+// o = 2 r + 1, the orbitals the channel states enter (their Z is all the
+// measurement reads, apart from the current hole's, which it forms itself).
+// Same split-TF32 scheme and pipeline as k_trans_z_tc: A = R_fl^T (rows o,
+// 128 per tile, K = f), B = the bonds' new columns (rows b, 128 per chunk),
+// one accumulator pair in TMEM (256 columns, lane = o).  The bonds are listed
+// in creation order (SquareLattice.cpp:9-28), as k_measure_long lists them.
+// Output Z[w][fl][b][r] (FP32, the odd orbitals o = 2 r + 1 fastest, b < 2 Ns)
+// for k_measure_long.
 __host__ __device__ inline TcLayout tc_layout_lz(int N)
 {
     TcLayout l;
@@ -918,7 +922,8 @@ __global__ void __launch_bounds__(kTcBlock, 1) k_long_z_tc(DevJob J, cx<float>* 
     const uint32_t tbase = *s_tbase;
     const uint32_t idesc = tc_idesc(kTcM);
     const int KC = (N + 31) / 32;
-    const int MT = (Ns + kTcM - 1) / kTcM;   // orbital tiles
+    const int No = Ns / 2;                   // upper-band (odd) orbitals
+    const int MT = (No + kTcM - 1) / kTcM;   // orbital tiles
     uint32_t parity = 0;
     bool failed = false;
     const bool worker = tid < kTcThreads;   // the issuing warp builds no operands
@@ -976,7 +981,7 @@ __global__ void __launch_bounds__(kTcBlock, 1) k_long_z_tc(DevJob J, cx<float>* 
         int fl, bc, mt;
         pass_of(p, fl, bc, mt);
         const cx<float>* Rf = static_cast<const cx<float>*>(J.gup) + (size_t(w) * 2 + fl) * size_t(Nmax) * Ns;
-        tc_load_rows(R, Rf + mt * kTcM, Ns, min(kTcM, Ns - mt * kTcM), N, kTcM, kc);
+        tc_load_rows(R, Rf + 2 * mt * kTcM + 1, Ns, min(kTcM, No - mt * kTcM), N, kTcM, kc, 2);
         tc_load_phase_cols(R, J.phase32, Nk, s_bs + fl * 2 * kOccMaxNs + bc * kTcM, s_pcol + fl * kTcM,
                            min(kTcM, nanti - bc * kTcM), N, kTcM, kc);
     };
@@ -1025,8 +1030,8 @@ __global__ void __launch_bounds__(kTcBlock, 1) k_long_z_tc(DevJob J, cx<float>* 
             }
             tmem_fence_after();
             // epilogue: lane o of TMEM -> Z[w][fl][b][o], 16 bonds at a time
-            const int lg = warp & 3, o = mt * kTcM + 32 * lg + lane;
-            cx<float>* Zw = Z + (size_t(w) * 2 + fl) * size_t(Bmax) * Ns;
+            const int lg = warp & 3, oi = mt * kTcM + 32 * lg + lane;
+            cx<float>* Zw = Z + (size_t(w) * 2 + fl) * size_t(Bmax) * No;
             for (int cc = warp >> 2; worker && cc < kTcM / 16; cc += 2) {
                 if (16 * cc >= nr) break;
                 uint32_t r[32];
@@ -1034,12 +1039,12 @@ __global__ void __launch_bounds__(kTcBlock, 1) k_long_z_tc(DevJob J, cx<float>* 
                 tmem_ld16(ta, r);
                 tmem_ld16(ta + 128, r + 16);
                 tmem_wait_ld(r);
-                if (o < Ns) {
+                if (oi < No) {
 #pragma unroll
                     for (int t = 0; t < 16; ++t) {
                         const int bl = 16 * cc + t;
                         if (bl < nr)
-                            Zw[size_t(bc * kTcM + bl) * Ns + o] = cx<float>{__uint_as_float(r[t]), __uint_as_float(r[16 + t])};
+                            Zw[size_t(bc * kTcM + bl) * No + oi] = cx<float>{__uint_as_float(r[t]), __uint_as_float(r[16 + t])};
                     }
                 }
             }
