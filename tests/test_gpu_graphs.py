@@ -36,6 +36,9 @@ CASES = {
                                 reinv_every=64, cuda_graphs=g), 3),
     "exciton": (lambda e, g: e.Job(e.StagFluxTransExciton(8, PHI, 0.1, q=(4, 4)), walkers=8, seed=5,
                                    precision="mixed", reinv_every=32, drift_threshold=1e-5, cuda_graphs=g), 3),
+    # longitudinal exciton: the measuring calls capture the tensor-core bond sums too
+    "long": (lambda e, g: e.Job(e.StagFluxLongExciton(8, PHI, 0.1, q=(4, 4)), walkers=8, seed=6,
+                                precision="mixed", reinv_every=32, drift_threshold=1e-5, cuda_graphs=g), 3),
 }
 
 
