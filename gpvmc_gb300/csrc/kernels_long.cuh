@@ -853,7 +853,10 @@ __global__ void __launch_bounds__(NT) k_measure_long(DevJob J, int mask, const c
                 cx<float>* ddB = s_Cb;
                 cx<float>* rowcB = s_rowc;
                 cx<float>* delB = s_rowc + NBZ * 2 * Nmax;
-                cx<float>* m11B = reinterpret_cast<cx<float>*>(s_red);
+                cx<float>* m11B = reinterpret_cast<cx<float>*>(s_red);   // 2 NBZ values (64 B)
+                // the ratios of the states past the block's threads (Nexc <= Ns + 1 <= NT + 1
+                // here, so at most NBZ values) before they are added in bond order
+                cx<double>* xq = reinterpret_cast<cx<double>*>(s_red + 16);
                 for (int b0 = 0; b0 < nanti; b0 += NBZ) {
                     const int nb = nanti - b0 < NBZ ? nanti - b0 : NBZ;
                     for (int idx = tid; idx < nb * 2 * (Nh + 1); idx += NT) {
@@ -895,20 +898,30 @@ __global__ void __launch_bounds__(NT) k_measure_long(DevJob J, int mask, const c
                         }
                     }
                     __syncthreads();
-                    for (int k = tid; k < Nexc; k += NT) {
+                    // the bond's view of both flavours for state evaluations
+                    auto bond_view = [&](int jb, LongFl<float> (&Dj)[2]) {
+                        Dj[0] = D[0];
+                        Dj[1] = D[1];
+                        for (int fl = 0; fl < 2; ++fl) {
+                            const int seg = jb * 2 + fl;
+                            Dj[fl].rowc = rowcB + seg * Nmax;
+                            Dj[fl].del = delB + seg * Nmax;
+                            Dj[fl].Z = ZB + seg * Ns;
+                            Dj[fl].pt = ptB + seg * Ns;
+                            Dj[fl].dd = ddB + seg * Ns;
+                            Dj[fl].M11 = m11B[seg];
+                            Dj[fl].moved = true;
+                        }
+                    };
+                    // one state per thread for every bond of the batch; the states past
+                    // the block's threads (the ground state, Nexc = Ns + 1) one
+                    // (state, bond) pair per thread, so that no thread takes two states
+                    const int k1 = Nexc < NT ? Nexc : NT;
+                    for (int k = tid; k < k1; k += NT) {
                         cx<double> sk = {0.0, 0.0};
-                        for (int j = 0; j < nb; ++j) {
-                            LongFl<float> Dj[2] = {D[0], D[1]};
-                            for (int fl = 0; fl < 2; ++fl) {
-                                const int seg = j * 2 + fl;
-                                Dj[fl].rowc = rowcB + seg * Nmax;
-                                Dj[fl].del = delB + seg * Nmax;
-                                Dj[fl].Z = ZB + seg * Ns;
-                                Dj[fl].pt = ptB + seg * Ns;
-                                Dj[fl].dd = ddB + seg * Ns;
-                                Dj[fl].M11 = m11B[seg];
-                                Dj[fl].moved = true;
-                            }
+                        for (int jb = 0; jb < nb; ++jb) {
+                            LongFl<float> Dj[2];
+                            bond_view(jb, Dj);
                             const cx<double> q = to_d(long_state_ratio<float>(Dj, cur, k, s_exu, s_exd, s_pre, Ns, nullptr));
                             sk.x += q.x;
                             sk.y += q.y;
@@ -916,8 +929,21 @@ __global__ void __launch_bounds__(NT) k_measure_long(DevJob J, int mask, const c
                         s_S[k].x += sk.x;
                         s_S[k].y += sk.y;
                     }
+                    for (int pq = tid; pq < (Nexc - k1) * nb; pq += NT) {   // into xq, added in bond order below
+                        const int k = k1 + pq / nb, jb = pq % nb;
+                        LongFl<float> Dj[2];
+                        bond_view(jb, Dj);
+                        xq[pq] = to_d(long_state_ratio<float>(Dj, cur, k, s_exu, s_exd, s_pre, Ns, nullptr));
+                    }
                     __syncthreads();   // the next batch restages
+                    if (tid == 0)
+                        for (int k = k1; k < Nexc; ++k)
+                            for (int jb = 0; jb < nb; ++jb) {
+                                s_S[k].x += xq[(k - k1) * nb + jb].x;
+                                s_S[k].y += xq[(k - k1) * nb + jb].y;
+                            }
                 }
+                __syncthreads();   // every state's bond sums are in s_S
             }
         }
         for (int b0 = 0; !zt && b0 < nanti; b0 += kLongBonds) {
