@@ -260,18 +260,19 @@ __host__ __device__ inline LongLayout long_layout(int Ns, int Nmax, int Nexc, bo
 // exchange moving flavour 0 from s0 to t0 and flavour 1 from t0 to s0
 template <typename T, int NT>
 __device__ __forceinline__ void long_stage_phi(const DevJob& J, int s0, int t0, const cx<T>* s_coef, cx<T>* s_pt,
-                                               cx<T>* s_dd)
+                                               cx<T>* s_dd, bool odd_only = false)
 {
     const int tid = threadIdx.x;
     const int Ns = J.Ns, Nk = J.Nk, L = J.L;
     const cx<T>* phase = Tab<T>::phase(J);
-    for (int idx = tid; idx < 2 * Ns; idx += NT) {
-        const int fl = idx / Ns, o = idx % Ns;
+    const int nz = odd_only ? Ns : 2 * Ns, per = nz / 2;   // odd_only: the upper-band (odd) orbitals
+    for (int idx = tid; idx < nz; idx += NT) {
+        const int fl = idx / per, o = odd_only ? 2 * (idx % per) + 1 : idx % Ns;
         const int s = fl ? t0 : s0, t = fl ? s0 : t0;
         const cx<T>* cf = s_coef + fl * 2 * Ns;
         const cx<T> pt = phi_orb<T>(phase, cf, Nk, Ns, L, t, o);
-        s_pt[idx] = pt;
-        s_dd[idx] = pt - phi_orb<T>(phase, cf, Nk, Ns, L, s, o);
+        s_pt[fl * Ns + o] = pt;
+        s_dd[fl * Ns + o] = pt - phi_orb<T>(phase, cf, Nk, Ns, L, s, o);
     }
     __syncthreads();
 }
@@ -347,10 +348,18 @@ __device__ __forceinline__ void long_stage(const DevJob& J, int w, int s0, int t
         cx<T> z = {T(0), T(0)};
         for (int f = lane; f < N; f += 32) cmac(z, R[size_t(f) * Ns + zo], C[f]);
         z = warp_sum(z);
-        if (lane == 0) s_Z[zhole * Ns + zo] = z;
+        if (lane == 0) {
+            s_Z[zhole * Ns + zo] = z;
+            // and the hole's orbital rows (the odd ones come from long_stage_phi)
+            const int s = zhole ? t0 : s0, t = zhole ? s0 : t0;
+            const cx<T>* cf = s_coef + zhole * 2 * Ns;
+            const cx<T> pt = phi_orb<T>(phase, cf, Nk, Ns, L, t, zo);
+            s_pt[zhole * Ns + zo] = pt;
+            s_dd[zhole * Ns + zo] = pt - phi_orb<T>(phase, cf, Nk, Ns, L, s, zo);
+        }
     }
     __syncthreads();
-    long_stage_phi<T, NT>(J, s0, t0, s_coef, s_pt, s_dd);
+    long_stage_phi<T, NT>(J, s0, t0, s_coef, s_pt, s_dd, sel);
 }
 
 // ------------------------------------------------------------------------
@@ -558,9 +567,13 @@ __global__ void __launch_bounds__(NT) k_walk_long(DevJob J, uint64_t nsteps, int
                     const int* h = s_hop + 6 * fl;
                     const int m = h[5];
                     cx<T>* R = static_cast<cx<T>*>(J.gup) + (size_t(w) * 2 + fl) * size_t(Nmax) * Ns;
-                    const cx<T> d = s_dd[fl * Ns + o];
+                    cx<T> d = s_dd[fl * Ns + o], ptv = s_pt[fl * Ns + o];
                     cx<T> zv = s_Z[fl * Ns + o];
                     if (!(o & 1) && !(fl == zhole && o == zo)) {   // an orbital the staging left out
+                        const int sf = fl ? t0 : s0, tf = fl ? s0 : t0;
+                        const cx<T>* cfo = s_coef + fl * 2 * Ns;
+                        ptv = phi_orb<T>(Tab<T>::phase(J), cfo, J.Nk, Ns, J.L, tf, o);
+                        d = ptv - phi_orb<T>(Tab<T>::phase(J), cfo, J.Nk, Ns, J.L, sf, o);
                         const cx<T>* C = s_C + fl * Nmax;
                         zv = cx<T>{T(0), T(0)};
                         int f = 0;
@@ -574,7 +587,7 @@ __global__ void __launch_bounds__(NT) k_walk_long(DevJob J, uint64_t nsteps, int
                         for (; f < N; ++f) cmac(zv, R[size_t(f) * Ns + o], C[f]);
                     }
                     cx<T> X[3];
-                    X[0] = zv + d * D[fl].M11 - s_pt[fl * Ns + o];
+                    X[0] = zv + d * D[fl].M11 - ptv;
                     for (int j = 0; j < h[0]; ++j) X[1 + j] = R[size_t(h[1 + j]) * Ns + o] + d * s_rowc[fl * Nmax + h[1 + j]];
                     const cx<T>* Bi = s_Bi + 9 * fl;
                     cx<T> be[3];
